@@ -1,0 +1,491 @@
+"""Python binding of libb2g.so (the GB300 world step) shaped like box2d-rs's `B2world`.
+
+The reference's public API is Rust (`B2world::new`, `create_body`, `create_fixture`,
+`step`, `set_contact_listener`, `get_profile`; src/b2_world.rs:22-284). This module
+exposes the same calls over the C ABI declared in include/b2g.h. Bodies and
+fixtures can be created one at a time (like the reference) or in bulk from numpy
+arrays of the C structs (how large scenes are uploaded).
+
+There is no CPU fallback: if libb2g.so is missing or fails to load, importing
+`load_library` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libb2g.so")
+
+STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
+CIRCLE, EDGE, POLYGON = 0, 1, 2
+POLYGON_HULL, POLYGON_BOX, POLYGON_BOX_ORIENTED = 0, 1, 2
+POLYGON_RADIUS = np.float32(0.01)  # B2_POLYGON_RADIUS = 2 * linear slop
+
+OK = 0
+ERRORS = {
+    -1: "invalid argument",
+    -2: "out of memory",
+    -3: "capacity overflow",
+    -4: "device wait timed out",
+    -5: "CUDA error",
+    -6: "unsupported",
+    -7: "world locked",
+}
+
+
+class B2GError(RuntimeError):
+    def __init__(self, code, msg=""):
+        super().__init__(f"b2g error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+# ---- struct layouts (must match include/b2g.h) ----
+class Vec2(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_float), ("y", ctypes.c_float)]
+
+
+class WorldDef(ctypes.Structure):
+    _fields_ = [
+        ("gravity", Vec2),
+        ("num_worlds", ctypes.c_int32),
+        ("device", ctypes.c_int32),
+        ("body_capacity", ctypes.c_int32),
+        ("fixture_capacity", ctypes.c_int32),
+        ("contact_capacity", ctypes.c_int32),
+        ("pair_capacity", ctypes.c_int32),
+    ]
+
+
+BODY_DEF = np.dtype(
+    [
+        ("type", "<i4"),
+        ("position", "<f4", (2,)),
+        ("angle", "<f4"),
+        ("linear_velocity", "<f4", (2,)),
+        ("angular_velocity", "<f4"),
+        ("linear_damping", "<f4"),
+        ("angular_damping", "<f4"),
+        ("gravity_scale", "<f4"),
+        ("allow_sleep", "u1"),
+        ("awake", "u1"),
+        ("fixed_rotation", "u1"),
+        ("bullet", "u1"),
+        ("enabled", "u1"),
+        ("pad_", "u1", (3,)),
+        ("world_index", "<u4"),
+        ("user_data", "<u8"),
+    ],
+    align=True,
+)
+
+FIXTURE_DEF = np.dtype(
+    [
+        ("body", "<u4"),
+        ("shape_type", "<i4"),
+        ("polygon_mode", "<i4"),
+        ("vertex_count", "<i4"),
+        ("vertices", "<f4", (8, 2)),
+        ("radius", "<f4"),
+        ("box_half_extents", "<f4", (2,)),
+        ("box_center", "<f4", (2,)),
+        ("box_angle", "<f4"),
+        ("one_sided", "<i4"),
+        ("friction", "<f4"),
+        ("restitution", "<f4"),
+        ("restitution_threshold", "<f4"),
+        ("density", "<f4"),
+        ("is_sensor", "<i4"),
+        ("category_bits", "<u2"),
+        ("mask_bits", "<u2"),
+        ("group_index", "<i2"),
+        ("pad_", "<i2"),
+        ("user_data", "<u8"),
+    ],
+    align=True,
+)
+
+BODY_STATE = np.dtype(
+    [
+        ("position", "<f4", (2,)),
+        ("angle", "<f4"),
+        ("linear_velocity", "<f4", (2,)),
+        ("angular_velocity", "<f4"),
+        ("world_center", "<f4", (2,)),
+    ]
+)
+
+CONTACT_INFO = np.dtype(
+    [
+        ("fixture_a", "<u4"),
+        ("fixture_b", "<u4"),
+        ("touching", "<i4"),
+        ("manifold_type", "<i4"),
+        ("point_count", "<i4"),
+        ("local_normal", "<f4", (2,)),
+        ("local_point", "<f4", (2,)),
+        ("point_local", "<f4", (2, 2)),
+        ("normal_impulse", "<f4", (2,)),
+        ("tangent_impulse", "<f4", (2,)),
+        ("point_id", "<u4", (2,)),
+        ("friction", "<f4"),
+        ("restitution", "<f4"),
+        ("restitution_threshold", "<f4"),
+    ]
+)
+
+EVENT = np.dtype([("kind", "<i4"), ("fixture_a", "<u4"), ("fixture_b", "<u4")])
+
+
+class Profile(ctypes.Structure):
+    _fields_ = [
+        (n, ctypes.c_float)
+        for n in ("step", "collide", "solve", "solve_init", "solve_velocity", "solve_position", "broadphase", "solve_toi")
+    ]
+
+    def as_dict(self):
+        return {n: float(getattr(self, n)) for n, _ in self._fields_}
+
+
+class Counts(ctypes.Structure):
+    _fields_ = [
+        (n, ctypes.c_int32)
+        for n in ("bodies", "fixtures", "proxies", "contacts", "touching_contacts", "islands_solved", "colours", "pairs")
+    ]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+assert BODY_DEF.itemsize == 64, BODY_DEF.itemsize
+assert FIXTURE_DEF.itemsize == 144, FIXTURE_DEF.itemsize
+assert BODY_STATE.itemsize == 32
+assert CONTACT_INFO.itemsize == 88
+assert ctypes.sizeof(WorldDef) == 32
+
+
+# ---- defs (defaults of B2bodyDef, src/b2_body.rs:39-59, and B2fixtureDef, src/b2_fixture.rs:44-56) ----
+def body_defs(n):
+    d = np.zeros(n, BODY_DEF)
+    d["type"] = STATIC
+    d["gravity_scale"] = 1.0
+    d["allow_sleep"] = 1
+    d["awake"] = 1
+    d["enabled"] = 1
+    return d
+
+
+def fixture_defs(n):
+    d = np.zeros(n, FIXTURE_DEF)
+    d["friction"] = 0.2
+    d["restitution_threshold"] = 1.0
+    d["category_bits"] = 0x0001
+    d["mask_bits"] = 0xFFFF
+    d["radius"] = POLYGON_RADIUS
+    return d
+
+
+def body_def(type=STATIC, position=(0.0, 0.0), angle=0.0, linear_velocity=(0.0, 0.0), angular_velocity=0.0,
+             linear_damping=0.0, angular_damping=0.0, gravity_scale=1.0, allow_sleep=True, awake=True,
+             fixed_rotation=False, bullet=False, enabled=True, world_index=0):
+    d = body_defs(1)
+    d["type"] = type
+    d["position"] = position
+    d["angle"] = angle
+    d["linear_velocity"] = linear_velocity
+    d["angular_velocity"] = angular_velocity
+    d["linear_damping"] = linear_damping
+    d["angular_damping"] = angular_damping
+    d["gravity_scale"] = gravity_scale
+    d["allow_sleep"] = allow_sleep
+    d["awake"] = awake
+    d["fixed_rotation"] = fixed_rotation
+    d["bullet"] = bullet
+    d["enabled"] = enabled
+    d["world_index"] = world_index
+    return d
+
+
+def _material(d, density, friction, restitution, restitution_threshold, is_sensor):
+    d["density"] = density
+    d["friction"] = friction
+    d["restitution"] = restitution
+    d["restitution_threshold"] = restitution_threshold
+    d["is_sensor"] = is_sensor
+
+
+def circle_fixture(body, radius, center=(0.0, 0.0), density=0.0, friction=0.2, restitution=0.0,
+                   restitution_threshold=1.0, is_sensor=False):
+    d = fixture_defs(1)
+    d["body"] = body
+    d["shape_type"] = CIRCLE
+    d["radius"] = radius
+    d["vertices"][0, 0] = center
+    _material(d, density, friction, restitution, restitution_threshold, is_sensor)
+    return d
+
+
+def box_fixture(body, hx, hy, center=None, angle=0.0, density=0.0, friction=0.2, restitution=0.0,
+                restitution_threshold=1.0, is_sensor=False):
+    d = fixture_defs(1)
+    d["body"] = body
+    d["shape_type"] = POLYGON
+    if center is None:
+        d["polygon_mode"] = POLYGON_BOX
+    else:
+        d["polygon_mode"] = POLYGON_BOX_ORIENTED
+        d["box_center"] = center
+        d["box_angle"] = angle
+    d["box_half_extents"] = (hx, hy)
+    _material(d, density, friction, restitution, restitution_threshold, is_sensor)
+    return d
+
+
+def polygon_fixture(body, vertices, density=0.0, friction=0.2, restitution=0.0, restitution_threshold=1.0,
+                    is_sensor=False):
+    v = np.asarray(vertices, np.float32).reshape(-1, 2)
+    d = fixture_defs(1)
+    d["body"] = body
+    d["shape_type"] = POLYGON
+    d["polygon_mode"] = POLYGON_HULL
+    d["vertex_count"] = len(v)
+    d["vertices"][0, : len(v)] = v
+    _material(d, density, friction, restitution, restitution_threshold, is_sensor)
+    return d
+
+
+def edge_fixture(body, v1, v2, v0=None, v3=None, density=0.0, friction=0.2, restitution=0.0,
+                 restitution_threshold=1.0, is_sensor=False):
+    d = fixture_defs(1)
+    d["body"] = body
+    d["shape_type"] = EDGE
+    one_sided = v0 is not None and v3 is not None
+    d["vertices"][0, 0] = v0 if one_sided else (0.0, 0.0)
+    d["vertices"][0, 1] = v1
+    d["vertices"][0, 2] = v2
+    d["vertices"][0, 3] = v3 if one_sided else (0.0, 0.0)
+    d["one_sided"] = one_sided
+    _material(d, density, friction, restitution, restitution_threshold, is_sensor)
+    return d
+
+
+# ---- library ----
+_lib = None
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def load_library(path=LIB_PATH):
+    """Load libb2g.so; raises OSError if it is missing (there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError(f"{path} is missing: build it with __graft_entry__.build()")
+    lib = ctypes.CDLL(path)
+    vp, i32, u32, f32 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_float
+    sig = {
+        "b2g_world_create": [ctypes.POINTER(WorldDef), ctypes.POINTER(vp)],
+        "b2g_world_destroy": [vp],
+        "b2g_create_bodies": [vp, vp, i32, vp],
+        "b2g_create_fixtures": [vp, vp, i32, vp],
+        "b2g_step": [vp, f32, i32, i32],
+        "b2g_synchronize": [vp],
+        "b2g_get_body_states": [vp, u32, u32, vp],
+        "b2g_set_transform": [vp, u32, Vec2, f32],
+        "b2g_set_linear_velocity": [vp, u32, Vec2],
+        "b2g_set_angular_velocity": [vp, u32, f32],
+        "b2g_apply_force": [vp, u32, Vec2, Vec2, i32],
+        "b2g_apply_linear_impulse": [vp, u32, Vec2, Vec2, i32],
+        "b2g_set_gravity": [vp, Vec2],
+        "b2g_set_allow_sleeping": [vp, i32],
+        "b2g_set_warm_starting": [vp, i32],
+        "b2g_set_continuous_physics": [vp, i32],
+        "b2g_set_auto_clear_forces": [vp, i32],
+        "b2g_clear_forces": [vp],
+        "b2g_get_profile": [vp, ctypes.POINTER(Profile)],
+        "b2g_get_counts": [vp, ctypes.POINTER(Counts)],
+        "b2g_get_contacts": [vp, vp, i32, ctypes.POINTER(i32)],
+        "b2g_get_events": [vp, vp, i32, ctypes.POINTER(i32)],
+        "b2g_get_pairs": [vp, vp, i32, ctypes.POINTER(i32)],
+        "b2g_get_proxies": [vp, vp, vp, i32],
+        "b2g_get_solver_order": [vp, vp, i32, ctypes.POINTER(i32)],
+        "b2g_version": [],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    lib.b2g_last_error.argtypes = [vp]
+    lib.b2g_last_error.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+class B2world:
+    """A world (or a batch of independent worlds) stepped on the GPU.
+
+    Mirrors `B2world` of box2d-rs (src/b2_world.rs:22-284). With `num_worlds > 1`
+    every body carries `world_index`; worlds share launches but never interact.
+    """
+
+    def __init__(self, gravity=(0.0, -10.0), num_worlds=1, device=0, body_capacity=0, fixture_capacity=0,
+                 contact_capacity=0, pair_capacity=0):
+        self._lib = load_library()
+        d = WorldDef(Vec2(*gravity), num_worlds, device, body_capacity, fixture_capacity, contact_capacity,
+                     pair_capacity)
+        h = ctypes.c_void_p()
+        self._check(self._lib.b2g_world_create(ctypes.byref(d), ctypes.byref(h)), None)
+        self._h = h
+        self._listener = None
+        self.body_count = 0
+        self.fixture_count = 0
+
+    def _check(self, rc, h="self"):
+        if rc != OK:
+            msg = ""
+            hh = self._h if h == "self" else h
+            if hh is not None:
+                m = self._lib.b2g_last_error(hh)
+                msg = m.decode() if m else ""
+            raise B2GError(rc, msg)
+        return rc
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.b2g_world_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- creation --
+    def create_bodies(self, defs):
+        defs = np.ascontiguousarray(defs, BODY_DEF)
+        ids = np.zeros(len(defs), np.uint32)
+        self._check(self._lib.b2g_create_bodies(self._h, _ptr(defs), len(defs), _ptr(ids)))
+        self.body_count += len(defs)
+        return ids
+
+    def create_body(self, **kw):
+        return int(self.create_bodies(body_def(**kw))[0])
+
+    def create_fixtures(self, defs):
+        defs = np.ascontiguousarray(defs, FIXTURE_DEF)
+        ids = np.zeros(len(defs), np.uint32)
+        self._check(self._lib.b2g_create_fixtures(self._h, _ptr(defs), len(defs), _ptr(ids)))
+        self.fixture_count += len(defs)
+        return ids
+
+    def create_fixture(self, d):
+        return int(self.create_fixtures(d)[0])
+
+    # -- step --
+    def step(self, dt, velocity_iterations, position_iterations):
+        self._check(self._lib.b2g_step(self._h, dt, velocity_iterations, position_iterations))
+        if self._listener is not None:
+            for ev in self.get_events():
+                if ev["kind"] == 0:
+                    self._listener.begin_contact(int(ev["fixture_a"]), int(ev["fixture_b"]))
+                else:
+                    self._listener.end_contact(int(ev["fixture_a"]), int(ev["fixture_b"]))
+
+    def synchronize(self):
+        self._check(self._lib.b2g_synchronize(self._h))
+
+    # -- state --
+    def get_body_states(self, first=0, count=None, out=None):
+        if count is None:
+            count = self.body_count - first
+        if out is None:
+            out = np.zeros(count, BODY_STATE)
+        self._check(self._lib.b2g_get_body_states(self._h, first, count, _ptr(out)))
+        return out
+
+    def set_transform(self, body, position, angle):
+        self._check(self._lib.b2g_set_transform(self._h, body, Vec2(*position), angle))
+
+    def set_linear_velocity(self, body, v):
+        self._check(self._lib.b2g_set_linear_velocity(self._h, body, Vec2(*v)))
+
+    def set_angular_velocity(self, body, w):
+        self._check(self._lib.b2g_set_angular_velocity(self._h, body, w))
+
+    def apply_force(self, body, force, point, wake=True):
+        self._check(self._lib.b2g_apply_force(self._h, body, Vec2(*force), Vec2(*point), int(wake)))
+
+    def apply_linear_impulse(self, body, impulse, point, wake=True):
+        self._check(self._lib.b2g_apply_linear_impulse(self._h, body, Vec2(*impulse), Vec2(*point), int(wake)))
+
+    # -- flags --
+    def set_gravity(self, g):
+        self._check(self._lib.b2g_set_gravity(self._h, Vec2(*g)))
+
+    def set_allow_sleeping(self, flag):
+        self._check(self._lib.b2g_set_allow_sleeping(self._h, int(flag)))
+
+    def set_warm_starting(self, flag):
+        self._check(self._lib.b2g_set_warm_starting(self._h, int(flag)))
+
+    def set_continuous_physics(self, flag):
+        self._check(self._lib.b2g_set_continuous_physics(self._h, int(flag)))
+
+    def set_auto_clear_forces(self, flag):
+        self._check(self._lib.b2g_set_auto_clear_forces(self._h, int(flag)))
+
+    def clear_forces(self):
+        self._check(self._lib.b2g_clear_forces(self._h))
+
+    def set_contact_listener(self, listener):
+        """`listener` has begin_contact(fa, fb) and end_contact(fa, fb); events are replayed after each step."""
+        self._listener = listener
+
+    # -- introspection --
+    def get_profile(self):
+        p = Profile()
+        self._check(self._lib.b2g_get_profile(self._h, ctypes.byref(p)))
+        return p.as_dict()
+
+    def get_counts(self):
+        c = Counts()
+        self._check(self._lib.b2g_get_counts(self._h, ctypes.byref(c)))
+        return c.as_dict()
+
+    def _get_list(self, fn, dtype, cap_hint, width=1):
+        n = ctypes.c_int32(0)
+        cap = max(cap_hint, 1)
+        while True:
+            out = np.zeros(cap * width, dtype)
+            self._check(fn(self._h, _ptr(out), cap, ctypes.byref(n)))
+            if n.value <= cap:
+                return out[: n.value * width]
+            cap = n.value
+
+    def get_contacts(self):
+        return self._get_list(self._lib.b2g_get_contacts, CONTACT_INFO, 4096)
+
+    def get_events(self):
+        return self._get_list(self._lib.b2g_get_events, EVENT, 1024)
+
+    def get_pairs(self):
+        return self._get_list(self._lib.b2g_get_pairs, np.uint32, 65536, 2).reshape(-1, 2)
+
+    def get_solver_order(self):
+        return self._get_list(self._lib.b2g_get_solver_order, np.uint32, 65536, 2).reshape(-1, 2)
+
+    def get_proxies(self):
+        n = self.fixture_count
+        aabbs = np.zeros((n, 4), np.float32)
+        moved = np.zeros(n, np.uint8)
+        self._check(self._lib.b2g_get_proxies(self._h, _ptr(aabbs), _ptr(moved), n))
+        return aabbs, moved

@@ -1,0 +1,209 @@
+/*
+ * b2g.h — C ABI of the GB300-native Box2D world step (libb2g.so).
+ *
+ * This header is the drop-in boundary for box2d-rs 0.0.4's `B2world` step path.
+ * The reference has no FFI of its own; its seam is the public Rust `B2world`
+ * API, and each entry point below names the reference function it replaces
+ * (paths are inside the box2d-rs source tree).
+ *
+ * Conventions
+ *   - Every function returns an int status: B2G_OK (0) or a negative B2G_ERR_*.
+ *     The reference panics on misuse (src/private/dynamics/b2_world.rs:84-87);
+ *     here misuse returns B2G_ERR_INVALID_ARG / B2G_ERR_LOCKED and
+ *     b2g_last_error() holds a one-line reason.
+ *   - The library owns all device memory. The caller owns every host buffer
+ *     passed in or out. Ids are dense uint32 in creation order.
+ *   - One world (or batch of worlds) per host thread; the library starts no
+ *     threads. Each world has its own CUDA stream; b2g_step is asynchronous
+ *     and b2g_synchronize / any b2g_get_* call waits for it.
+ *   - Listener callbacks are never called from device code: begin/end contact
+ *     events are buffered on the device and read with b2g_get_events after a
+ *     step (the reference fires them inside `step`,
+ *     src/private/dynamics/b2_contact.rs:201-217).
+ *   - Arithmetic is IEEE f32 with no fused multiply-add, like the reference.
+ */
+#ifndef B2G_H
+#define B2G_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define B2G_OK 0
+#define B2G_ERR_INVALID_ARG (-1)
+#define B2G_ERR_OUT_OF_MEMORY (-2)
+#define B2G_ERR_CAPACITY (-3)     /* a device buffer overflowed; results of that step are void */
+#define B2G_ERR_TIMEOUT (-4)      /* a bounded device wait gave up (grid barrier)               */
+#define B2G_ERR_CUDA (-5)         /* a CUDA runtime call failed                                  */
+#define B2G_ERR_UNSUPPORTED (-6)  /* feature outside the GPU path (see b2g_last_error)           */
+#define B2G_ERR_LOCKED (-7)       /* world is inside a step                                      */
+
+#define B2G_MAX_POLYGON_VERTICES 8
+
+/* B2bodyType, src/b2_body.rs:20-30 */
+enum { B2G_STATIC_BODY = 0, B2G_KINEMATIC_BODY = 1, B2G_DYNAMIC_BODY = 2 };
+/* B2ShapeType order, src/b2_shape.rs:25-31 (chain shapes are not supported) */
+enum { B2G_SHAPE_CIRCLE = 0, B2G_SHAPE_EDGE = 1, B2G_SHAPE_POLYGON = 2 };
+/* How a polygon is built: B2polygonShape::set (hull, private/collision/b2_polygon_shape.rs:96-211),
+ * set_as_box (:12-23) or set_as_box_angle (:25-50). */
+enum { B2G_POLYGON_HULL = 0, B2G_POLYGON_BOX = 1, B2G_POLYGON_BOX_ORIENTED = 2 };
+
+typedef struct b2g_vec2 { float x, y; } b2g_vec2;
+
+typedef struct b2g_world_def {
+    b2g_vec2 gravity;          /* B2world::new(gravity), src/b2_world.rs:25-27 */
+    int32_t num_worlds;        /* >= 1. Bodies carry world_index; worlds never interact. */
+    int32_t device;            /* CUDA device ordinal */
+    int32_t body_capacity;     /* 0 = grow on demand at creation time */
+    int32_t fixture_capacity;
+    int32_t contact_capacity;  /* 0 = 8 x fixtures */
+    int32_t pair_capacity;     /* 0 = 16 x fixtures */
+} b2g_world_def;
+
+/* B2bodyDef, src/b2_body.rs:91-147 (defaults :39-59) */
+typedef struct b2g_body_def {
+    int32_t type;
+    b2g_vec2 position;
+    float angle;
+    b2g_vec2 linear_velocity;
+    float angular_velocity;
+    float linear_damping;
+    float angular_damping;
+    float gravity_scale;
+    uint8_t allow_sleep;
+    uint8_t awake;
+    uint8_t fixed_rotation;
+    uint8_t bullet;
+    uint8_t enabled;
+    uint8_t pad_[3];
+    uint32_t world_index;      /* which world of a batch (0 for a single world) */
+    uint64_t user_data;
+} b2g_body_def;
+
+/* B2fixtureDef (src/b2_fixture.rs:44-56) with its shape inlined.
+ *   circle : vertices[0] = centre (m_p), radius
+ *   edge   : vertices[0..3] = vertex0..vertex3, one_sided selects set_one_sided/set_two_sided
+ *   polygon: polygon_mode HULL uses vertices[0..vertex_count); BOX/BOX_ORIENTED use box_* fields
+ *   radius for polygons and edges is the skin radius (B2_POLYGON_RADIUS = 0.01 by default) */
+typedef struct b2g_fixture_def {
+    uint32_t body;
+    int32_t shape_type;
+    int32_t polygon_mode;
+    int32_t vertex_count;
+    b2g_vec2 vertices[B2G_MAX_POLYGON_VERTICES];
+    float radius;
+    b2g_vec2 box_half_extents;
+    b2g_vec2 box_center;
+    float box_angle;
+    int32_t one_sided;
+    float friction;
+    float restitution;
+    float restitution_threshold;
+    float density;
+    int32_t is_sensor;
+    uint16_t category_bits;
+    uint16_t mask_bits;
+    int16_t group_index;
+    int16_t pad_;
+    uint64_t user_data;
+} b2g_fixture_def;
+
+/* Body state read back after a step (B2body getters, src/b2_body.rs:650-680). */
+typedef struct b2g_body_state {
+    b2g_vec2 position;         /* m_xf.p  (get_position)        */
+    float angle;               /* m_sweep.a (get_angle)         */
+    b2g_vec2 linear_velocity;
+    float angular_velocity;
+    b2g_vec2 world_center;     /* m_sweep.c (get_world_center)  */
+} b2g_body_state;
+
+/* B2Profile, src/b2_time_step.rs:5-14; milliseconds measured with CUDA events. */
+typedef struct b2g_profile {
+    float step, collide, solve, solve_init, solve_velocity, solve_position, broadphase, solve_toi;
+} b2g_profile;
+
+typedef struct b2g_counts {
+    int32_t bodies, fixtures, proxies, contacts, touching_contacts, islands_solved, colours, pairs;
+} b2g_counts;
+
+/* One contact with its manifold (B2manifold, src/b2_collision.rs:104-114). */
+typedef struct b2g_contact_info {
+    uint32_t fixture_a, fixture_b;  /* after the primary-type ordering of b2_contact_registers.rs */
+    int32_t touching;
+    int32_t manifold_type;          /* 0 circles, 1 faceA, 2 faceB */
+    int32_t point_count;
+    b2g_vec2 local_normal;
+    b2g_vec2 local_point;
+    b2g_vec2 point_local[2];
+    float normal_impulse[2];
+    float tangent_impulse[2];
+    uint32_t point_id[2];           /* B2contactFeature packed: index_a | index_b<<8 | type_a<<16 | type_b<<24 */
+    float friction, restitution, restitution_threshold;
+} b2g_contact_info;
+
+enum { B2G_EVENT_BEGIN = 0, B2G_EVENT_END = 1 };
+typedef struct b2g_contact_event {
+    int32_t kind;
+    uint32_t fixture_a, fixture_b;
+} b2g_contact_event;
+
+/* ---- lifecycle (B2world::new / drop) ---- */
+int b2g_world_create(const b2g_world_def* def, void** out_world);
+int b2g_world_destroy(void* world);
+const char* b2g_last_error(const void* world);
+int b2g_version(void);
+
+/* ---- creation: B2world::create_body (src/b2_world.rs:60-62),
+ *                B2body::create_fixture (src/b2_body.rs:233) ---- */
+int b2g_create_bodies(void* world, const b2g_body_def* defs, int32_t n, uint32_t* out_ids);
+int b2g_create_fixtures(void* world, const b2g_fixture_def* defs, int32_t n, uint32_t* out_ids);
+
+/* ---- the step: B2world::step(dt, velocity_iterations, position_iterations),
+ *      src/b2_world.rs:98-100 -> src/private/dynamics/b2_world.rs:903-959 ---- */
+int b2g_step(void* world, float dt, int32_t velocity_iterations, int32_t position_iterations);
+int b2g_synchronize(void* world);
+
+/* ---- state I/O (src/b2_body.rs getters/setters) ---- */
+int b2g_get_body_states(void* world, uint32_t first, uint32_t count, b2g_body_state* out);
+/* B2body::set_transform, private/dynamics/b2_body.rs:418-447 */
+int b2g_set_transform(void* world, uint32_t body, b2g_vec2 position, float angle);
+int b2g_set_linear_velocity(void* world, uint32_t body, b2g_vec2 v);
+int b2g_set_angular_velocity(void* world, uint32_t body, float w);
+/* B2body::apply_force / apply_linear_impulse (src/b2_body.rs:870-940) */
+int b2g_apply_force(void* world, uint32_t body, b2g_vec2 force, b2g_vec2 point, int32_t wake);
+int b2g_apply_linear_impulse(void* world, uint32_t body, b2g_vec2 impulse, b2g_vec2 point, int32_t wake);
+
+/* ---- world flags, src/b2_world.rs:163-193, :232-253 ---- */
+int b2g_set_gravity(void* world, b2g_vec2 gravity);
+int b2g_set_allow_sleeping(void* world, int32_t flag);
+int b2g_set_warm_starting(void* world, int32_t flag);
+int b2g_set_continuous_physics(void* world, int32_t flag);
+int b2g_set_auto_clear_forces(void* world, int32_t flag);
+int b2g_clear_forces(void* world);
+
+/* ---- introspection ---- */
+int b2g_get_profile(void* world, b2g_profile* out);       /* B2world::get_profile, src/b2_world.rs:268-270 */
+int b2g_get_counts(void* world, b2g_counts* out);         /* get_body_count / get_contact_count / get_proxy_count */
+int b2g_get_contacts(void* world, b2g_contact_info* out, int32_t capacity, int32_t* out_count);
+/* begin/end events produced since the previous call (B2contactListener, src/b2_world_callbacks.rs:68-104) */
+int b2g_get_events(void* world, b2g_contact_event* out, int32_t capacity, int32_t* out_count);
+
+/* ---- parity hooks ---- */
+/* Pairs emitted by the last broadphase pass (update_pairs, src/b2_broad_phase.rs:200-249),
+ * as fixture-id pairs (a < b), sorted. 2 uint32 per pair. */
+int b2g_get_pairs(void* world, uint32_t* out_pairs, int32_t capacity, int32_t* out_count);
+/* Fat AABBs (lower.x, lower.y, upper.x, upper.y per fixture) and moved flags
+ * (B2dynamicTree::move_proxy, private/collision/b2_dynamic_tree.rs:109-168). */
+int b2g_get_proxies(void* world, float* out_aabbs, uint8_t* out_moved, int32_t capacity);
+/* The constraint order the GPU solved in during the last step: one (fixture_a, fixture_b)
+ * pair per island contact, grouped by colour. Feeding it to the host reference solver as its
+ * island contact order reproduces the GPU's Gauss-Seidel sweep
+ * (B2island::solve, private/dynamics/b2_island_private.rs:129-328). */
+int b2g_get_solver_order(void* world, uint32_t* out_pairs, int32_t capacity, int32_t* out_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* B2G_H */

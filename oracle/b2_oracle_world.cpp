@@ -1,0 +1,1317 @@
+/*
+ * Oracle world step — TEST INFRASTRUCTURE ONLY.
+ *
+ * This is the CPU restatement of box2d-rs 0.0.4's `B2world::step` path that the
+ * tests (and bench.py's cpu_baseline leg) use as the checker for the GPU path.
+ * It is never linked into, loaded by or called from the product library.
+ *
+ * Restated reference code (paths inside the box2d-rs tree):
+ *   B2world::step / solve / clear_forces     src/private/dynamics/b2_world.rs:356-531, 903-967
+ *   B2world::create_body                     src/private/dynamics/b2_world.rs:83-98
+ *   B2body (new, create_fixture, reset_mass_data, should_collide, synchronize_fixtures,
+ *           set_transform, set_awake)        src/private/dynamics/b2_body.rs:15-78, 155-200,
+ *                                            292-350, 391-475; src/b2_body.rs:783-801, 974-977
+ *   B2fixture create_proxies / synchronize   src/private/dynamics/b2_fixture.rs:114-173
+ *   B2contactManager collide / add_pair / destroy
+ *                                            src/private/dynamics/b2_contact_manager.rs:24-302
+ *   B2contact create / update / mixing       src/private/dynamics/b2_contact.rs:11-218,
+ *                                            src/b2_contact.rs:29-46, b2_contact_registers.rs:67-103
+ *   default contact filter                   src/private/dynamics/b2_world_callbacks.rs:6-18
+ *   B2island::solve                          src/private/dynamics/b2_island_private.rs:129-328
+ *   B2contactSolver (new, initialize_velocity_constraints, warm_start,
+ *     solve_velocity_constraints, store_impulses, solve_position_constraints)
+ *                                            src/private/dynamics/b2_contact_solver_private.rs:20-730
+ * Linked lists keep the reference's newest-first order (src/b2rs_double_linked_list.rs:200-222).
+ *
+ * Added for parity (not in the reference): an ordering hook that replaces each
+ * island's contact order with a caller-given order (the GPU's colour order), a
+ * switch between libm and the project's sin/cos, and state export functions.
+ * Not restated: continuous collision (solve_toi), joints, sensors' shape
+ * overlap test, chain shapes, re-filtering. ora_set_flags rejects continuous=1.
+ */
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <unordered_map>
+#include <vector>
+
+#include "../include/b2g.h"
+#include "b2_oracle_collide.h"
+#include "b2_oracle_tree.h"
+
+namespace ora {
+
+enum { STATIC = 0, KINEMATIC = 1, DYNAMIC = 2 };
+
+struct Body {
+    int type = STATIC;
+    Xf xf{};
+    Sweep sweep{};
+    Vec2 v{0, 0};
+    float w = 0.0f;
+    Vec2 force{0, 0};
+    float torque = 0.0f;
+    float mass = 0, inv_mass = 0, I = 0, inv_I = 0;
+    float lin_damp = 0, ang_damp = 0, grav_scale = 1;
+    float sleep_time = 0;
+    bool awake = false, enabled = true, auto_sleep = true, fixed_rotation = false, bullet = false;
+    bool island_flag = false;
+    int island_index = -1;
+    int prev = -1, next = -1;
+    int fixture_head = -1;
+    int edge_head = -1;
+};
+
+struct Fixture {
+    int body = -1;
+    Shape shape;
+    float density = 0, friction = 0.2f, restitution = 0, threshold = 1.0f;
+    bool sensor = false;
+    uint16_t category = 1, mask = 0xffff;
+    int16_t group = 0;
+    int proxy = -1;
+    int next = -1;
+};
+
+struct Edge {
+    int contact = -1;
+    int other = -1;
+    int prev = -1, next = -1;
+};
+
+struct Contact {
+    int fa = -1, fb = -1;
+    Manifold m;
+    bool touching = false, enabled = true, island_flag = false;
+    float friction = 0, restitution = 0, threshold = 0, tangent_speed = 0;
+    int prev = -1, next = -1;
+    bool alive = false;
+};
+
+struct Position {
+    Vec2 c;
+    float a;
+};
+struct Velocity {
+    Vec2 v;
+    float w;
+};
+struct VCPoint {
+    Vec2 rA, rB;
+    float ni, ti, nm, tm, bias;
+};
+struct VelocityConstraint {
+    VCPoint p[2];
+    Vec2 normal;
+    Mat22 normal_mass, K;
+    int ia, ib;
+    float ma, mb, Ia, Ib;
+    float friction, restitution, threshold, tangent_speed;
+    int count;
+    int contact;
+};
+struct PositionConstraint {
+    Vec2 lp[2];
+    Vec2 ln, lpt, lcA, lcB;
+    int ia, ib;
+    float ma, mb, IA, IB, rA, rB;
+    int type, count;
+};
+
+struct Step {
+    float dt, inv_dt, dt_ratio;
+    int vi, pi;
+    bool warm;
+};
+
+struct World {
+    Vec2 gravity{0, -10};
+    std::vector<Body> bodies;
+    std::vector<Fixture> fixtures;
+    std::vector<Contact> contacts;
+    std::vector<int> free_contacts;
+    std::vector<Edge> edges;  /* 2 per contact slot: [2c] = node A, [2c+1] = node B */
+    int body_head = -1;
+    int contact_head = -1;
+    int contact_count = 0;
+    BroadPhase bp;
+    bool warm_starting = true, continuous = false, allow_sleep = true, auto_clear = true;
+    bool new_contacts = false, locked = false;
+    float inv_dt0 = 0.0f;
+    b2g_profile profile{};
+    /* parity / export */
+    bool record_events = false;
+    std::vector<b2g_contact_event> events;
+    std::vector<Pair> last_pairs;   /* proxy-id pairs of the last update_pairs */
+    std::vector<uint8_t> last_moved; /* per fixture: was in the move buffer at the last update_pairs */
+    std::vector<int> proxy_to_fixture;
+    bool hook = false;
+    std::unordered_map<uint64_t, int> hook_rank;
+    int hook_misses = 0;
+    std::vector<uint64_t> last_order;  /* island contact order solved last step */
+    int islands_solved = 0;
+    /* island scratch */
+    std::vector<int> isl_bodies, isl_contacts, stack;
+    std::vector<Position> pos;
+    std::vector<Velocity> vel;
+    std::vector<VelocityConstraint> vcs;
+    std::vector<PositionConstraint> pcs;
+    std::vector<Pair> pairs;
+};
+
+static inline uint64_t pair_key(int fa, int fb) { return ((uint64_t)(uint32_t)fa << 32) | (uint32_t)fb; }
+
+/* ---- bodies ---- */
+
+/* b2_body, private/dynamics/b2_body.rs:15-78 */
+static int create_body(World& w, const b2g_body_def& d) {
+    Body b;
+    b.type = d.type;
+    b.auto_sleep = d.allow_sleep != 0;
+    b.fixed_rotation = d.fixed_rotation != 0;
+    b.bullet = d.bullet != 0;
+    b.awake = d.awake != 0 && d.type != STATIC;
+    b.enabled = d.enabled != 0;
+    b.xf.p = v2(d.position.x, d.position.y);
+    b.xf.q = rot(d.angle);
+    b.sweep.local_center = v2(0, 0);
+    b.sweep.c0 = b.xf.p;
+    b.sweep.c = b.xf.p;
+    b.sweep.a0 = d.angle;
+    b.sweep.a = d.angle;
+    b.sweep.alpha0 = 0.0f;
+    b.v = v2(d.linear_velocity.x, d.linear_velocity.y);
+    b.w = d.angular_velocity;
+    b.lin_damp = d.linear_damping;
+    b.ang_damp = d.angular_damping;
+    b.grav_scale = d.gravity_scale;
+    int id = (int)w.bodies.size();
+    /* push_front onto the world body list (private/dynamics/b2_world.rs:83-98) */
+    b.next = w.body_head;
+    if (w.body_head >= 0) w.bodies[w.body_head].prev = id;
+    w.body_head = id;
+    w.bodies.push_back(b);
+    return id;
+}
+
+static void set_awake(Body& b, bool flag) {
+    if (b.type == STATIC) return;
+    b.awake = flag;
+    b.sleep_time = 0.0f;
+    if (!flag) {
+        b.v = v2(0, 0);
+        b.w = 0.0f;
+        b.force = v2(0, 0);
+        b.torque = 0.0f;
+    }
+}
+
+/* reset_mass_data, private/dynamics/b2_body.rs:292-350 */
+static void reset_mass_data(World& w, Body& b) {
+    b.mass = 0.0f;
+    b.inv_mass = 0.0f;
+    b.I = 0.0f;
+    b.inv_I = 0.0f;
+    b.sweep.local_center = v2(0, 0);
+    if (b.type == STATIC || b.type == KINEMATIC) {
+        b.sweep.c0 = b.xf.p;
+        b.sweep.c = b.xf.p;
+        b.sweep.a0 = b.sweep.a;
+        return;
+    }
+    Vec2 lc{0, 0};
+    for (int f = b.fixture_head; f >= 0; f = w.fixtures[f].next) {
+        const Fixture& fx = w.fixtures[f];
+        if (fx.density == 0.0f) continue;
+        MassData md;
+        compute_mass(fx.shape, fx.density, md);
+        b.mass += md.mass;
+        lc += md.mass * md.center;
+        b.I += md.I;
+    }
+    if (b.mass > 0.0f) {
+        b.inv_mass = 1.0f / b.mass;
+        lc *= b.inv_mass;
+    }
+    if (b.I > 0.0f && !b.fixed_rotation) {
+        b.I -= b.mass * dot(lc, lc);
+        b.inv_I = 1.0f / b.I;
+    } else {
+        b.I = 0.0f;
+        b.inv_I = 0.0f;
+    }
+    Vec2 oldCenter = b.sweep.c;
+    b.sweep.local_center = lc;
+    b.sweep.c0 = mul(b.xf, b.sweep.local_center);
+    b.sweep.c = b.sweep.c0;
+    b.v += cross_sv(b.w, b.sweep.c - oldCenter);
+}
+
+static void build_shape(const b2g_fixture_def& d, Shape& s) {
+    s.type = d.shape_type;
+    s.radius = d.radius;
+    if (d.shape_type == SHAPE_CIRCLE) {
+        s.p = v2(d.vertices[0].x, d.vertices[0].y);
+    } else if (d.shape_type == SHAPE_EDGE) {
+        s.v0 = v2(d.vertices[0].x, d.vertices[0].y);
+        s.v1 = v2(d.vertices[1].x, d.vertices[1].y);
+        s.v2 = v2(d.vertices[2].x, d.vertices[2].y);
+        s.v3 = v2(d.vertices[3].x, d.vertices[3].y);
+        s.one_sided = d.one_sided != 0;
+    } else {
+        if (d.polygon_mode == B2G_POLYGON_BOX) {
+            polygon_set_as_box(s, d.box_half_extents.x, d.box_half_extents.y);
+        } else if (d.polygon_mode == B2G_POLYGON_BOX_ORIENTED) {
+            polygon_set_as_box_oriented(s, d.box_half_extents.x, d.box_half_extents.y,
+                                        v2(d.box_center.x, d.box_center.y), d.box_angle);
+        } else {
+            Vec2 pts[kMaxPolygonVertices];
+            int n = d.vertex_count < kMaxPolygonVertices ? d.vertex_count : kMaxPolygonVertices;
+            for (int i = 0; i < n; ++i) pts[i] = v2(d.vertices[i].x, d.vertices[i].y);
+            polygon_set_hull(s, pts, n);
+        }
+        s.radius = d.radius;
+    }
+}
+
+/* create_fixture, private/dynamics/b2_body.rs:155-200; create_proxies, private/dynamics/b2_fixture.rs:114-133 */
+static int create_fixture(World& w, const b2g_fixture_def& d) {
+    Fixture f;
+    f.body = (int)d.body;
+    build_shape(d, f.shape);
+    f.density = d.density;
+    f.friction = d.friction;
+    f.restitution = d.restitution;
+    f.threshold = d.restitution_threshold;
+    f.sensor = d.is_sensor != 0;
+    f.category = d.category_bits;
+    f.mask = d.mask_bits;
+    f.group = d.group_index;
+    int id = (int)w.fixtures.size();
+    Body& b = w.bodies[f.body];
+    if (b.enabled) {
+        AABB aabb;
+        compute_aabb(f.shape, b.xf, aabb);
+        f.proxy = w.bp.create_proxy(aabb, id);
+        if ((int)w.proxy_to_fixture.size() <= f.proxy) w.proxy_to_fixture.resize((size_t)f.proxy + 1, -1);
+        w.proxy_to_fixture[f.proxy] = id;
+    }
+    f.next = b.fixture_head;
+    b.fixture_head = id;
+    w.fixtures.push_back(f);
+    w.last_moved.push_back(0);
+    if (f.density > 0.0f) reset_mass_data(w, w.bodies[f.body]);
+    w.new_contacts = true;
+    return id;
+}
+
+/* b2_fixture_synchronize, private/dynamics/b2_fixture.rs:147-173 */
+static void synchronize_fixture(World& w, Fixture& f, const Xf& xf1, const Xf& xf2) {
+    if (f.proxy < 0) return;
+    AABB a1, a2;
+    compute_aabb(f.shape, xf1, a1);
+    compute_aabb(f.shape, xf2, a2);
+    AABB swept = combine(a1, a2);
+    Vec2 disp = center(a2) - center(a1);
+    w.bp.move_proxy(f.proxy, swept, disp);
+}
+
+/* synchronize_fixtures_internal, private/dynamics/b2_body.rs:455-475 */
+static void synchronize_fixtures(World& w, Body& b) {
+    if (b.awake) {
+        Xf xf1;
+        xf1.q = rot(b.sweep.a0);
+        xf1.p = b.sweep.c0 - mul(xf1.q, b.sweep.local_center);
+        for (int f = b.fixture_head; f >= 0; f = w.fixtures[f].next) synchronize_fixture(w, w.fixtures[f], xf1, b.xf);
+    } else {
+        for (int f = b.fixture_head; f >= 0; f = w.fixtures[f].next) synchronize_fixture(w, w.fixtures[f], b.xf, b.xf);
+    }
+}
+
+static void synchronize_transform(Body& b) {
+    b.xf.q = rot(b.sweep.a);
+    b.xf.p = b.sweep.c - mul(b.xf.q, b.sweep.local_center);
+}
+
+/* ---- contacts ---- */
+
+static void list_unlink_edge(World& w, int bodyId, int e) {
+    Edge& E = w.edges[e];
+    if (E.prev >= 0) w.edges[E.prev].next = E.next;
+    else w.bodies[bodyId].edge_head = E.next;
+    if (E.next >= 0) w.edges[E.next].prev = E.prev;
+    E.prev = E.next = -1;
+}
+
+static void list_push_edge(World& w, int bodyId, int e) {
+    Edge& E = w.edges[e];
+    E.prev = -1;
+    E.next = w.bodies[bodyId].edge_head;
+    if (E.next >= 0) w.edges[E.next].prev = e;
+    w.bodies[bodyId].edge_head = e;
+}
+
+/* default filter, private/dynamics/b2_world_callbacks.rs:6-18 */
+static bool filter_should_collide(const Fixture& a, const Fixture& b) {
+    if (a.group == b.group && a.group != 0) return a.group > 0;
+    return (a.mask & b.category) != 0 && (a.category & b.mask) != 0;
+}
+
+/* b2_contact_registers.rs:67-103: which (typeA, typeB) has a manifold routine with A first */
+static int register_kind(int t1, int t2) {
+    /* +1 primary, -1 swap, 0 none */
+    static const int table[3][3] = {
+        /* circle  edge  polygon */
+        {+1, -1, -1}, /* circle */
+        {+1, 0, +1},  /* edge   */
+        {+1, -1, +1}, /* polygon*/
+    };
+    return table[t1][t2];
+}
+
+/* b2_contact_manager_add_pair, private/dynamics/b2_contact_manager.rs:178-302 */
+static void add_pair(World& w, int fixA, int fixB) {
+    int bodyA = w.fixtures[fixA].body;
+    int bodyB = w.fixtures[fixB].body;
+    if (bodyA == bodyB) return;
+    for (int e = w.bodies[bodyB].edge_head; e >= 0; e = w.edges[e].next) {
+        if (w.edges[e].other == bodyA) {
+            const Contact& c = w.contacts[w.edges[e].contact];
+            if (c.fa == fixA && c.fb == fixB) return;
+            if (c.fa == fixB && c.fb == fixA) return;
+        }
+    }
+    /* should_collide: at least one dynamic body (joints are not restated) */
+    if (w.bodies[bodyB].type != DYNAMIC && w.bodies[bodyA].type != DYNAMIC) return;
+    if (!filter_should_collide(w.fixtures[fixA], w.fixtures[fixB])) return;
+    int kind = register_kind(w.fixtures[fixA].shape.type, w.fixtures[fixB].shape.type);
+    if (kind == 0) return;
+    if (kind < 0) std::swap(fixA, fixB);
+    int id;
+    if (!w.free_contacts.empty()) {
+        id = w.free_contacts.back();
+        w.free_contacts.pop_back();
+    } else {
+        id = (int)w.contacts.size();
+        w.contacts.emplace_back();
+        w.edges.emplace_back();
+        w.edges.emplace_back();
+    }
+    Contact& c = w.contacts[id];
+    c = Contact{};
+    c.alive = true;
+    c.fa = fixA;
+    c.fb = fixB;
+    const Fixture& FA = w.fixtures[fixA];
+    const Fixture& FB = w.fixtures[fixB];
+    c.friction = std::sqrt(FA.friction * FB.friction);
+    c.restitution = FA.restitution > FB.restitution ? FA.restitution : FB.restitution;
+    c.threshold = FA.threshold < FB.threshold ? FA.threshold : FB.threshold;
+    c.tangent_speed = 0.0f;
+    c.enabled = true;
+    c.m.point_count = 0;
+    /* push_front onto the world contact list */
+    c.prev = -1;
+    c.next = w.contact_head;
+    if (w.contact_head >= 0) w.contacts[w.contact_head].prev = id;
+    w.contact_head = id;
+    int bA = FA.body, bB = FB.body;
+    w.edges[2 * id].contact = id;
+    w.edges[2 * id].other = bB;
+    list_push_edge(w, bA, 2 * id);
+    w.edges[2 * id + 1].contact = id;
+    w.edges[2 * id + 1].other = bA;
+    list_push_edge(w, bB, 2 * id + 1);
+    ++w.contact_count;
+}
+
+/* b2_contact_manager_destroy, private/dynamics/b2_contact_manager.rs:24-78 */
+static void destroy_contact(World& w, int id) {
+    Contact& c = w.contacts[id];
+    if (w.record_events && c.touching)
+        w.events.push_back(b2g_contact_event{B2G_EVENT_END, (uint32_t)c.fa, (uint32_t)c.fb});
+    if (c.prev >= 0) w.contacts[c.prev].next = c.next;
+    else w.contact_head = c.next;
+    if (c.next >= 0) w.contacts[c.next].prev = c.prev;
+    int bA = w.fixtures[c.fa].body, bB = w.fixtures[c.fb].body;
+    list_unlink_edge(w, bA, 2 * id);
+    list_unlink_edge(w, bB, 2 * id + 1);
+    /* B2contact::destroy wakes both bodies of a touching, non-sensor contact */
+    if (c.m.point_count > 0 && !w.fixtures[c.fa].sensor && !w.fixtures[c.fb].sensor) {
+        set_awake(w.bodies[bA], true);
+        set_awake(w.bodies[bB], true);
+    }
+    c.alive = false;
+    w.free_contacts.push_back(id);
+    --w.contact_count;
+}
+
+static void evaluate(const Contact& c, const World& w, Manifold& m, const Xf& xfA, const Xf& xfB) {
+    const Shape& sa = w.fixtures[c.fa].shape;
+    const Shape& sb = w.fixtures[c.fb].shape;
+    if (sa.type == SHAPE_CIRCLE) collide_circles(m, sa, xfA, sb, xfB);
+    else if (sa.type == SHAPE_POLYGON && sb.type == SHAPE_CIRCLE) collide_polygon_circle(m, sa, xfA, sb, xfB);
+    else if (sa.type == SHAPE_POLYGON) collide_polygons(m, sa, xfA, sb, xfB);
+    else if (sb.type == SHAPE_CIRCLE) collide_edge_circle(m, sa, xfA, sb, xfB);
+    else collide_edge_polygon(m, sa, xfA, sb, xfB);
+}
+
+/* b2_contact_update, private/dynamics/b2_contact.rs:103-218 */
+static void update_contact(World& w, int id) {
+    Contact& c = w.contacts[id];
+    c.enabled = true;
+    Manifold old = c.m;
+    bool wasTouching = c.touching;
+    bool sensor = w.fixtures[c.fa].sensor || w.fixtures[c.fb].sensor;
+    Body& bA = w.bodies[w.fixtures[c.fa].body];
+    Body& bB = w.bodies[w.fixtures[c.fb].body];
+    bool touching;
+    if (sensor) {
+        /* shape overlap for sensors is not restated (GJK is outside this path) */
+        touching = false;
+        c.m.point_count = 0;
+    } else {
+        Manifold nm;
+        evaluate(c, w, nm, bA.xf, bB.xf);
+        c.m = nm;
+        touching = c.m.point_count > 0;
+        for (int i = 0; i < c.m.point_count; ++i) {
+            ManifoldPoint& mp2 = c.m.points[i];
+            mp2.normal_impulse = 0.0f;
+            mp2.tangent_impulse = 0.0f;
+            for (int j = 0; j < old.point_count; ++j) {
+                if (old.points[j].id == mp2.id) {
+                    mp2.normal_impulse = old.points[j].normal_impulse;
+                    mp2.tangent_impulse = old.points[j].tangent_impulse;
+                    break;
+                }
+            }
+        }
+        if (touching != wasTouching) {
+            set_awake(bA, true);
+            set_awake(bB, true);
+        }
+    }
+    c.touching = touching;
+    if (w.record_events) {
+        if (!wasTouching && touching) w.events.push_back(b2g_contact_event{B2G_EVENT_BEGIN, (uint32_t)c.fa, (uint32_t)c.fb});
+        if (wasTouching && !touching) w.events.push_back(b2g_contact_event{B2G_EVENT_END, (uint32_t)c.fa, (uint32_t)c.fb});
+    }
+}
+
+/* b2_contact_manager_collide, private/dynamics/b2_contact_manager.rs:83-171 */
+static void collide(World& w) {
+    std::vector<int> to_destroy;
+    for (int id = w.contact_head; id >= 0; id = w.contacts[id].next) {
+        Contact& c = w.contacts[id];
+        const Fixture& FA = w.fixtures[c.fa];
+        const Fixture& FB = w.fixtures[c.fb];
+        const Body& bA = w.bodies[FA.body];
+        const Body& bB = w.bodies[FB.body];
+        bool activeA = bA.awake && bA.type != STATIC;
+        bool activeB = bB.awake && bB.type != STATIC;
+        if (!activeA && !activeB) continue;
+        if (!w.bp.test_overlap(FA.proxy, FB.proxy)) {
+            to_destroy.push_back(id);
+            continue;
+        }
+        update_contact(w, id);
+    }
+    for (int id : to_destroy) destroy_contact(w, id);
+}
+
+/* find_new_contacts -> update_pairs -> add_pair */
+static void find_new_contacts(World& w) {
+    std::fill(w.last_moved.begin(), w.last_moved.end(), 0);
+    for (int q : w.bp.move_buffer())
+        if (q != kNullNode) w.last_moved[w.bp.tree.user(q)] = 1;
+    w.bp.update_pairs(w.pairs);
+    w.last_pairs = w.pairs;
+    for (const Pair& p : w.pairs) add_pair(w, w.bp.tree.user(p.a), w.bp.tree.user(p.b));
+}
+
+/* ---- island solver ---- */
+
+/* B2contactSolver::new + initialize_velocity_constraints, b2_contact_solver_private.rs:20-226 */
+static void init_constraints(World& w, const Step& step) {
+    int n = (int)w.isl_contacts.size();
+    w.vcs.resize(n);
+    w.pcs.resize(n);
+    for (int i = 0; i < n; ++i) {
+        const Contact& c = w.contacts[w.isl_contacts[i]];
+        const Fixture& FA = w.fixtures[c.fa];
+        const Fixture& FB = w.fixtures[c.fb];
+        const Body& bA = w.bodies[FA.body];
+        const Body& bB = w.bodies[FB.body];
+        const Manifold& m = c.m;
+        VelocityConstraint& vc = w.vcs[i];
+        vc.friction = c.friction;
+        vc.restitution = c.restitution;
+        vc.threshold = c.threshold;
+        vc.tangent_speed = c.tangent_speed;
+        vc.ia = bA.island_index;
+        vc.ib = bB.island_index;
+        vc.ma = bA.inv_mass;
+        vc.mb = bB.inv_mass;
+        vc.Ia = bA.inv_I;
+        vc.Ib = bB.inv_I;
+        vc.contact = i;
+        vc.count = m.point_count;
+        vc.K = Mat22{v2(0, 0), v2(0, 0)};
+        vc.normal_mass = Mat22{v2(0, 0), v2(0, 0)};
+        PositionConstraint& pc = w.pcs[i];
+        pc.ia = bA.island_index;
+        pc.ib = bB.island_index;
+        pc.ma = bA.inv_mass;
+        pc.mb = bB.inv_mass;
+        pc.lcA = bA.sweep.local_center;
+        pc.lcB = bB.sweep.local_center;
+        pc.IA = bA.inv_I;
+        pc.IB = bB.inv_I;
+        pc.ln = m.local_normal;
+        pc.lpt = m.local_point;
+        pc.count = m.point_count;
+        pc.rA = FA.shape.radius;
+        pc.rB = FB.shape.radius;
+        pc.type = m.type;
+        for (int j = 0; j < m.point_count; ++j) {
+            VCPoint& p = vc.p[j];
+            if (step.warm) {
+                p.ni = step.dt_ratio * m.points[j].normal_impulse;
+                p.ti = step.dt_ratio * m.points[j].tangent_impulse;
+            } else {
+                p.ni = 0.0f;
+                p.ti = 0.0f;
+            }
+            p.rA = v2(0, 0);
+            p.rB = v2(0, 0);
+            p.nm = 0.0f;
+            p.tm = 0.0f;
+            p.bias = 0.0f;
+            pc.lp[j] = m.points[j].local_point;
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        VelocityConstraint& vc = w.vcs[i];
+        PositionConstraint& pc = w.pcs[i];
+        const Manifold& m = w.contacts[w.isl_contacts[vc.contact]].m;
+        float mA = vc.ma, mB = vc.mb, iA = vc.Ia, iB = vc.Ib;
+        Vec2 cA = w.pos[vc.ia].c;
+        float aA = w.pos[vc.ia].a;
+        Vec2 vA = w.vel[vc.ia].v;
+        float wA = w.vel[vc.ia].w;
+        Vec2 cB = w.pos[vc.ib].c;
+        float aB = w.pos[vc.ib].a;
+        Vec2 vB = w.vel[vc.ib].v;
+        float wB = w.vel[vc.ib].w;
+        Xf xfA, xfB;
+        xfA.q = rot(aA);
+        xfB.q = rot(aB);
+        xfA.p = cA - mul(xfA.q, pc.lcA);
+        xfB.p = cB - mul(xfB.q, pc.lcB);
+        WorldManifold wm;
+        world_manifold(wm, m, xfA, pc.rA, xfB, pc.rB);
+        vc.normal = wm.normal;
+        for (int j = 0; j < vc.count; ++j) {
+            VCPoint& p = vc.p[j];
+            p.rA = wm.points[j] - cA;
+            p.rB = wm.points[j] - cB;
+            float rnA = cross(p.rA, vc.normal);
+            float rnB = cross(p.rB, vc.normal);
+            float kNormal = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+            p.nm = kNormal > 0.0f ? 1.0f / kNormal : 0.0f;
+            Vec2 tangent = cross_vs(vc.normal, 1.0f);
+            float rtA = cross(p.rA, tangent);
+            float rtB = cross(p.rB, tangent);
+            float kTangent = mA + mB + iA * rtA * rtA + iB * rtB * rtB;
+            p.tm = kTangent > 0.0f ? 1.0f / kTangent : 0.0f;
+            p.bias = 0.0f;
+            float vRel = dot(vc.normal, vB + cross_sv(wB, p.rB) - vA - cross_sv(wA, p.rA));
+            if (vRel < -vc.threshold) p.bias = -vc.restitution * vRel;
+        }
+        if (vc.count == 2) {
+            const VCPoint& p1 = vc.p[0];
+            const VCPoint& p2 = vc.p[1];
+            float rn1A = cross(p1.rA, vc.normal);
+            float rn1B = cross(p1.rB, vc.normal);
+            float rn2A = cross(p2.rA, vc.normal);
+            float rn2B = cross(p2.rB, vc.normal);
+            float k11 = mA + mB + iA * rn1A * rn1A + iB * rn1B * rn1B;
+            float k22 = mA + mB + iA * rn2A * rn2A + iB * rn2B * rn2B;
+            float k12 = mA + mB + iA * rn1A * rn2A + iB * rn1B * rn2B;
+            const float kMaxConditionNumber = 1000.0f;
+            if (k11 * k11 < kMaxConditionNumber * (k11 * k22 - k12 * k12)) {
+                vc.K.ex = v2(k11, k12);
+                vc.K.ey = v2(k12, k22);
+                vc.normal_mass = inverse(vc.K);
+            } else {
+                vc.count = 1;
+            }
+        }
+    }
+}
+
+/* warm_start, :228-266 */
+static void warm_start(World& w) {
+    for (VelocityConstraint& vc : w.vcs) {
+        float mA = vc.ma, iA = vc.Ia, mB = vc.mb, iB = vc.Ib;
+        Vec2 vA = w.vel[vc.ia].v;
+        float wA = w.vel[vc.ia].w;
+        Vec2 vB = w.vel[vc.ib].v;
+        float wB = w.vel[vc.ib].w;
+        Vec2 normal = vc.normal;
+        Vec2 tangent = cross_vs(normal, 1.0f);
+        for (int j = 0; j < vc.count; ++j) {
+            const VCPoint& p = vc.p[j];
+            Vec2 P = p.ni * normal + p.ti * tangent;
+            wA -= iA * cross(p.rA, P);
+            vA -= mA * P;
+            wB += iB * cross(p.rB, P);
+            vB += mB * P;
+        }
+        w.vel[vc.ia].v = vA;
+        w.vel[vc.ia].w = wA;
+        w.vel[vc.ib].v = vB;
+        w.vel[vc.ib].w = wB;
+    }
+}
+
+/* solve_velocity_constraints, :268-583 (friction, then normal: 1-point or 2-point block LCP) */
+static void solve_velocity(World& w) {
+    for (VelocityConstraint& vc : w.vcs) {
+        float mA = vc.ma, iA = vc.Ia, mB = vc.mb, iB = vc.Ib;
+        Vec2 vA = w.vel[vc.ia].v;
+        float wA = w.vel[vc.ia].w;
+        Vec2 vB = w.vel[vc.ib].v;
+        float wB = w.vel[vc.ib].w;
+        Vec2 normal = vc.normal;
+        Vec2 tangent = cross_vs(normal, 1.0f);
+        float friction = vc.friction;
+        for (int j = 0; j < vc.count; ++j) {
+            VCPoint& p = vc.p[j];
+            Vec2 dv = vB + cross_sv(wB, p.rB) - vA - cross_sv(wA, p.rA);
+            float vt = dot(dv, tangent) - vc.tangent_speed;
+            float lambda = p.tm * (-vt);
+            float maxFriction = friction * p.ni;
+            float newImpulse = bclamp(p.ti + lambda, -maxFriction, maxFriction);
+            lambda = newImpulse - p.ti;
+            p.ti = newImpulse;
+            Vec2 P = lambda * tangent;
+            vA -= mA * P;
+            wA -= iA * cross(p.rA, P);
+            vB += mB * P;
+            wB += iB * cross(p.rB, P);
+        }
+        if (vc.count == 1) {
+            VCPoint& p = vc.p[0];
+            Vec2 dv = vB + cross_sv(wB, p.rB) - vA - cross_sv(wA, p.rA);
+            float vn = dot(dv, normal);
+            float lambda = -p.nm * (vn - p.bias);
+            float newImpulse = bmax(p.ni + lambda, 0.0f);
+            lambda = newImpulse - p.ni;
+            p.ni = newImpulse;
+            Vec2 P = lambda * normal;
+            vA -= mA * P;
+            wA -= iA * cross(p.rA, P);
+            vB += mB * P;
+            wB += iB * cross(p.rB, P);
+        } else {
+            VCPoint& cp1 = vc.p[0];
+            VCPoint& cp2 = vc.p[1];
+            Vec2 a{cp1.ni, cp2.ni};
+            Vec2 dv1 = vB + cross_sv(wB, cp1.rB) - vA - cross_sv(wA, cp1.rA);
+            Vec2 dv2 = vB + cross_sv(wB, cp2.rB) - vA - cross_sv(wA, cp2.rA);
+            float vn1 = dot(dv1, normal);
+            float vn2 = dot(dv2, normal);
+            Vec2 b{vn1 - cp1.bias, vn2 - cp2.bias};
+            b -= mul(vc.K, a);
+            for (;;) {
+                Vec2 x = -mul(vc.normal_mass, b);
+                if (x.x >= 0.0f && x.y >= 0.0f) goto apply;
+                x.x = -cp1.nm * b.x;
+                x.y = 0.0f;
+                vn2 = vc.K.ex.y * x.x + b.y;
+                if (x.x >= 0.0f && vn2 >= 0.0f) goto apply;
+                x.x = 0.0f;
+                x.y = -cp2.nm * b.y;
+                vn1 = vc.K.ey.x * x.y + b.x;
+                if (x.y >= 0.0f && vn1 >= 0.0f) goto apply;
+                x.x = 0.0f;
+                x.y = 0.0f;
+                vn1 = b.x;
+                vn2 = b.y;
+                if (vn1 >= 0.0f && vn2 >= 0.0f) goto apply;
+                break;
+            apply : {
+                Vec2 d = x - a;
+                Vec2 P1 = d.x * normal;
+                Vec2 P2 = d.y * normal;
+                vA -= mA * (P1 + P2);
+                wA -= iA * (cross(cp1.rA, P1) + cross(cp2.rA, P2));
+                vB += mB * (P1 + P2);
+                wB += iB * (cross(cp1.rB, P1) + cross(cp2.rB, P2));
+                cp1.ni = x.x;
+                cp2.ni = x.y;
+                break;
+            }
+            }
+        }
+        w.vel[vc.ia].v = vA;
+        w.vel[vc.ia].w = wA;
+        w.vel[vc.ib].v = vB;
+        w.vel[vc.ib].w = wB;
+    }
+}
+
+/* store_impulses, :585-598 */
+static void store_impulses(World& w) {
+    for (const VelocityConstraint& vc : w.vcs) {
+        Manifold& m = w.contacts[w.isl_contacts[vc.contact]].m;
+        for (int j = 0; j < vc.count; ++j) {
+            m.points[j].normal_impulse = vc.p[j].ni;
+            m.points[j].tangent_impulse = vc.p[j].ti;
+        }
+    }
+}
+
+/* B2positionSolverManifold::initialize, :600-642 */
+static void position_manifold(const PositionConstraint& pc, const Xf& xfA, const Xf& xfB, int index, Vec2& normal,
+                              Vec2& point, float& separation) {
+    if (pc.type == MANIFOLD_CIRCLES) {
+        Vec2 pA = mul(xfA, pc.lpt);
+        Vec2 pB = mul(xfB, pc.lp[0]);
+        normal = pB - pA;
+        normalize(normal);
+        point = 0.5f * (pA + pB);
+        separation = dot(pB - pA, normal) - pc.rA - pc.rB;
+    } else if (pc.type == MANIFOLD_FACE_A) {
+        normal = mul(xfA.q, pc.ln);
+        Vec2 plane = mul(xfA, pc.lpt);
+        Vec2 clip = mul(xfB, pc.lp[index]);
+        separation = dot(clip - plane, normal) - pc.rA - pc.rB;
+        point = clip;
+    } else {
+        normal = mul(xfB.q, pc.ln);
+        Vec2 plane = mul(xfB, pc.lpt);
+        Vec2 clip = mul(xfA, pc.lp[index]);
+        separation = dot(clip - plane, normal) - pc.rA - pc.rB;
+        point = clip;
+        normal = -normal;
+    }
+}
+
+/* solve_position_constraints, :653-730 */
+static bool solve_position(World& w) {
+    float minSeparation = 0.0f;
+    for (const PositionConstraint& pc : w.pcs) {
+        Vec2 lcA = pc.lcA, lcB = pc.lcB;
+        float mA = pc.ma, iA = pc.IA, mB = pc.mb, iB = pc.IB;
+        Vec2 cA = w.pos[pc.ia].c;
+        float aA = w.pos[pc.ia].a;
+        Vec2 cB = w.pos[pc.ib].c;
+        float aB = w.pos[pc.ib].a;
+        for (int j = 0; j < pc.count; ++j) {
+            Xf xfA, xfB;
+            xfA.q = rot(aA);
+            xfB.q = rot(aB);
+            xfA.p = cA - mul(xfA.q, lcA);
+            xfB.p = cB - mul(xfB.q, lcB);
+            Vec2 normal, point;
+            float separation;
+            position_manifold(pc, xfA, xfB, j, normal, point, separation);
+            Vec2 rA = point - cA;
+            Vec2 rB = point - cB;
+            minSeparation = bmin(minSeparation, separation);
+            float C = bclamp(kBaumgarte * (separation + kLinearSlop), -kMaxLinearCorrection, 0.0f);
+            float rnA = cross(rA, normal);
+            float rnB = cross(rB, normal);
+            float K = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+            float impulse = K > 0.0f ? -C / K : 0.0f;
+            Vec2 P = impulse * normal;
+            cA -= mA * P;
+            aA -= iA * cross(rA, P);
+            cB += mB * P;
+            aB += iB * cross(rB, P);
+        }
+        w.pos[pc.ia].c = cA;
+        w.pos[pc.ia].a = aA;
+        w.pos[pc.ib].c = cB;
+        w.pos[pc.ib].a = aB;
+    }
+    return minSeparation >= -3.0f * kLinearSlop;
+}
+
+/* B2island::solve, b2_island_private.rs:129-328 */
+static void solve_island(World& w, const Step& step) {
+    float h = step.dt;
+    int nb = (int)w.isl_bodies.size();
+    w.pos.resize(nb);
+    w.vel.resize(nb);
+    for (int i = 0; i < nb; ++i) {
+        Body& b = w.bodies[w.isl_bodies[i]];
+        Vec2 c = b.sweep.c;
+        float a = b.sweep.a;
+        Vec2 v = b.v;
+        float wv = b.w;
+        b.sweep.c0 = b.sweep.c;
+        b.sweep.a0 = b.sweep.a;
+        if (b.type == DYNAMIC) {
+            v += (h * b.inv_mass) * ((b.grav_scale * b.mass) * w.gravity + b.force);
+            wv += h * b.inv_I * b.torque;
+            v *= 1.0f / (1.0f + h * b.lin_damp);
+            wv *= 1.0f / (1.0f + h * b.ang_damp);
+        }
+        w.pos[i].c = c;
+        w.pos[i].a = a;
+        w.vel[i].v = v;
+        w.vel[i].w = wv;
+    }
+    init_constraints(w, step);
+    if (step.warm) warm_start(w);
+    for (int it = 0; it < step.vi; ++it) solve_velocity(w);
+    store_impulses(w);
+    for (int i = 0; i < nb; ++i) {
+        Vec2 c = w.pos[i].c;
+        float a = w.pos[i].a;
+        Vec2 v = w.vel[i].v;
+        float wv = w.vel[i].w;
+        Vec2 translation = h * v;
+        if (dot(translation, translation) > kMaxTranslationSquared) {
+            float ratio = kMaxTranslation / length(translation);
+            v *= ratio;
+        }
+        float rotation = h * wv;
+        if (rotation * rotation > kMaxRotationSquared) {
+            float ratio = kMaxRotation / std::fabs(rotation);
+            wv *= ratio;
+        }
+        c += h * v;
+        a += h * wv;
+        w.pos[i].c = c;
+        w.pos[i].a = a;
+        w.vel[i].v = v;
+        w.vel[i].w = wv;
+    }
+    bool positionSolved = false;
+    for (int it = 0; it < step.pi; ++it) {
+        if (solve_position(w)) {
+            positionSolved = true;
+            break;
+        }
+    }
+    for (int i = 0; i < nb; ++i) {
+        Body& b = w.bodies[w.isl_bodies[i]];
+        b.sweep.c = w.pos[i].c;
+        b.sweep.a = w.pos[i].a;
+        b.v = w.vel[i].v;
+        b.w = w.vel[i].w;
+        synchronize_transform(b);
+    }
+    if (w.allow_sleep) {
+        float minSleepTime = kMaxFloat;
+        const float linTolSqr = kLinearSleepTolerance * kLinearSleepTolerance;
+        const float angTolSqr = kAngularSleepTolerance * kAngularSleepTolerance;
+        for (int i = 0; i < nb; ++i) {
+            Body& b = w.bodies[w.isl_bodies[i]];
+            if (b.type == STATIC) continue;
+            if (!b.auto_sleep || b.w * b.w > angTolSqr || dot(b.v, b.v) > linTolSqr) {
+                b.sleep_time = 0.0f;
+                minSleepTime = 0.0f;
+            } else {
+                b.sleep_time += h;
+                minSleepTime = bmin(minSleepTime, b.sleep_time);
+            }
+        }
+        if (minSleepTime >= kTimeToSleep && positionSolved) {
+            for (int i = 0; i < nb; ++i) set_awake(w.bodies[w.isl_bodies[i]], false);
+        }
+    }
+}
+
+/* B2world::solve, private/dynamics/b2_world.rs:356-531 */
+static void solve(World& w, const Step& step) {
+    for (int b = w.body_head; b >= 0; b = w.bodies[b].next) w.bodies[b].island_flag = false;
+    for (int c = w.contact_head; c >= 0; c = w.contacts[c].next) w.contacts[c].island_flag = false;
+    w.last_order.clear();
+    w.islands_solved = 0;
+    for (int seed = w.body_head; seed >= 0; seed = w.bodies[seed].next) {
+        Body& S = w.bodies[seed];
+        if (S.island_flag) continue;
+        if (!S.awake || !S.enabled) continue;
+        if (S.type == STATIC) continue;
+        w.isl_bodies.clear();
+        w.isl_contacts.clear();
+        w.stack.clear();
+        w.stack.push_back(seed);
+        S.island_flag = true;
+        while (!w.stack.empty()) {
+            int bi = w.stack.back();
+            w.stack.pop_back();
+            Body& b = w.bodies[bi];
+            b.island_index = (int)w.isl_bodies.size();
+            w.isl_bodies.push_back(bi);
+            if (b.type == STATIC) continue;
+            b.awake = true;
+            for (int e = b.edge_head; e >= 0; e = w.edges[e].next) {
+                int ci = w.edges[e].contact;
+                Contact& c = w.contacts[ci];
+                if (c.island_flag) continue;
+                if (!c.enabled || !c.touching) continue;
+                if (w.fixtures[c.fa].sensor || w.fixtures[c.fb].sensor) continue;
+                w.isl_contacts.push_back(ci);
+                c.island_flag = true;
+                int other = w.edges[e].other;
+                if (w.bodies[other].island_flag) continue;
+                w.stack.push_back(other);
+                w.bodies[other].island_flag = true;
+            }
+        }
+        if (w.hook) {
+            /* ordering hook: solve this island's contacts in the caller's order */
+            std::stable_sort(w.isl_contacts.begin(), w.isl_contacts.end(), [&](int x, int y) {
+                auto ix = w.hook_rank.find(pair_key(w.contacts[x].fa, w.contacts[x].fb));
+                auto iy = w.hook_rank.find(pair_key(w.contacts[y].fa, w.contacts[y].fb));
+                int rx = ix == w.hook_rank.end() ? 0x7fffffff : ix->second;
+                int ry = iy == w.hook_rank.end() ? 0x7fffffff : iy->second;
+                return rx < ry;
+            });
+            for (int ci : w.isl_contacts)
+                if (w.hook_rank.find(pair_key(w.contacts[ci].fa, w.contacts[ci].fb)) == w.hook_rank.end()) ++w.hook_misses;
+        }
+        for (int ci : w.isl_contacts) w.last_order.push_back(pair_key(w.contacts[ci].fa, w.contacts[ci].fb));
+        solve_island(w, step);
+        ++w.islands_solved;
+        for (int bi : w.isl_bodies)
+            if (w.bodies[bi].type == STATIC) w.bodies[bi].island_flag = false;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    for (int b = w.body_head; b >= 0; b = w.bodies[b].next) {
+        Body& B = w.bodies[b];
+        if (!B.island_flag) continue;
+        if (B.type == STATIC) continue;
+        synchronize_fixtures(w, B);
+    }
+    find_new_contacts(w);
+    w.profile.broadphase = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+/* B2world::step, private/dynamics/b2_world.rs:903-959 */
+static void step(World& w, float dt, int vi, int pi) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (w.new_contacts) {
+        find_new_contacts(w);
+        w.new_contacts = false;
+    }
+    w.locked = true;
+    Step s;
+    s.dt = dt;
+    s.vi = vi;
+    s.pi = pi;
+    s.inv_dt = dt > 0.0f ? 1.0f / dt : 0.0f;
+    s.dt_ratio = w.inv_dt0 * dt;
+    s.warm = w.warm_starting;
+    auto t1 = std::chrono::steady_clock::now();
+    collide(w);
+    auto t2 = std::chrono::steady_clock::now();
+    w.profile.collide = std::chrono::duration<float, std::milli>(t2 - t1).count();
+    if (dt > 0.0f) {
+        solve(w, s);
+        w.profile.solve = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t2).count();
+    }
+    if (dt > 0.0f) w.inv_dt0 = s.inv_dt;
+    if (w.auto_clear) {
+        for (int b = w.body_head; b >= 0; b = w.bodies[b].next) {
+            w.bodies[b].force = v2(0, 0);
+            w.bodies[b].torque = 0.0f;
+        }
+    }
+    w.locked = false;
+    w.profile.step = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace ora
+
+using namespace ora;
+
+extern "C" {
+
+int ora_set_trig_libm(int flag) {
+    g_trig_libm = flag != 0;
+    return 0;
+}
+
+int ora_world_create(float gx, float gy, void** out) {
+    World* w = new World();
+    w->gravity = v2(gx, gy);
+    *out = w;
+    return 0;
+}
+
+int ora_world_destroy(void* p) {
+    delete (World*)p;
+    return 0;
+}
+
+int ora_set_flags(void* p, int allow_sleep, int warm_starting, int continuous, int auto_clear) {
+    World& w = *(World*)p;
+    if (continuous) return B2G_ERR_UNSUPPORTED;
+    w.allow_sleep = allow_sleep != 0;
+    w.warm_starting = warm_starting != 0;
+    w.continuous = false;
+    w.auto_clear = auto_clear != 0;
+    return 0;
+}
+
+int ora_set_record_events(void* p, int flag) {
+    ((World*)p)->record_events = flag != 0;
+    return 0;
+}
+
+int ora_create_bodies(void* p, const b2g_body_def* defs, int n, uint32_t* ids) {
+    World& w = *(World*)p;
+    for (int i = 0; i < n; ++i) {
+        int id = create_body(w, defs[i]);
+        if (ids) ids[i] = (uint32_t)id;
+    }
+    return 0;
+}
+
+int ora_create_fixtures(void* p, const b2g_fixture_def* defs, int n, uint32_t* ids) {
+    World& w = *(World*)p;
+    for (int i = 0; i < n; ++i) {
+        if (defs[i].body >= w.bodies.size()) return B2G_ERR_INVALID_ARG;
+        int id = create_fixture(w, defs[i]);
+        if (ids) ids[i] = (uint32_t)id;
+    }
+    return 0;
+}
+
+int ora_step(void* p, float dt, int vi, int pi) {
+    step(*(World*)p, dt, vi, pi);
+    return 0;
+}
+
+int ora_steps(void* p, float dt, int vi, int pi, int n) {
+    for (int i = 0; i < n; ++i) step(*(World*)p, dt, vi, pi);
+    return 0;
+}
+
+int ora_get_body_states(void* p, uint32_t first, uint32_t count, b2g_body_state* out) {
+    World& w = *(World*)p;
+    if ((size_t)first + count > w.bodies.size()) return B2G_ERR_INVALID_ARG;
+    for (uint32_t i = 0; i < count; ++i) {
+        const Body& b = w.bodies[first + i];
+        b2g_body_state& s = out[i];
+        s.position = b2g_vec2{b.xf.p.x, b.xf.p.y};
+        s.angle = b.sweep.a;
+        s.linear_velocity = b2g_vec2{b.v.x, b.v.y};
+        s.angular_velocity = b.w;
+        s.world_center = b2g_vec2{b.sweep.c.x, b.sweep.c.y};
+    }
+    return 0;
+}
+
+/* B2body::set_transform, private/dynamics/b2_body.rs:418-447 */
+int ora_set_transform(void* p, uint32_t id, b2g_vec2 pos, float angle) {
+    World& w = *(World*)p;
+    if (id >= w.bodies.size()) return B2G_ERR_INVALID_ARG;
+    Body& b = w.bodies[id];
+    b.xf.q = rot(angle);
+    b.xf.p = v2(pos.x, pos.y);
+    b.sweep.c = mul(b.xf, b.sweep.local_center);
+    b.sweep.a = angle;
+    b.sweep.c0 = b.sweep.c;
+    b.sweep.a0 = angle;
+    for (int f = b.fixture_head; f >= 0; f = w.fixtures[f].next) synchronize_fixture(w, w.fixtures[f], b.xf, b.xf);
+    w.new_contacts = true;
+    return 0;
+}
+
+/* B2body::set_linear_velocity / set_angular_velocity (src/b2_body.rs:684-705) */
+int ora_set_velocity(void* p, uint32_t id, b2g_vec2 v, float av) {
+    World& w = *(World*)p;
+    if (id >= w.bodies.size()) return B2G_ERR_INVALID_ARG;
+    Body& b = w.bodies[id];
+    if (b.type == STATIC) return 0;
+    Vec2 vv = v2(v.x, v.y);
+    if (dot(vv, vv) > 0.0f) set_awake(b, true);
+    b.v = vv;
+    if (av * av > 0.0f) set_awake(b, true);
+    b.w = av;
+    return 0;
+}
+
+int ora_get_counts(void* p, b2g_counts* out) {
+    World& w = *(World*)p;
+    memset(out, 0, sizeof(*out));
+    out->bodies = (int)w.bodies.size();
+    out->fixtures = (int)w.fixtures.size();
+    out->proxies = w.bp.proxy_count;
+    out->contacts = w.contact_count;
+    int touching = 0;
+    for (int c = w.contact_head; c >= 0; c = w.contacts[c].next) touching += w.contacts[c].touching ? 1 : 0;
+    out->touching_contacts = touching;
+    out->islands_solved = w.islands_solved;
+    out->pairs = (int)w.last_pairs.size();
+    return 0;
+}
+
+int ora_get_profile(void* p, b2g_profile* out) {
+    *out = ((World*)p)->profile;
+    return 0;
+}
+
+/* Contacts in world-list order (newest first). */
+int ora_get_contacts(void* p, b2g_contact_info* out, int cap, int* n) {
+    World& w = *(World*)p;
+    int k = 0;
+    for (int c = w.contact_head; c >= 0; c = w.contacts[c].next) {
+        if (k < cap && out) {
+            const Contact& C = w.contacts[c];
+            b2g_contact_info& o = out[k];
+            memset(&o, 0, sizeof(o));
+            o.fixture_a = (uint32_t)C.fa;
+            o.fixture_b = (uint32_t)C.fb;
+            o.touching = C.touching ? 1 : 0;
+            o.manifold_type = C.m.type;
+            o.point_count = C.m.point_count;
+            o.local_normal = b2g_vec2{C.m.local_normal.x, C.m.local_normal.y};
+            o.local_point = b2g_vec2{C.m.local_point.x, C.m.local_point.y};
+            for (int j = 0; j < 2; ++j) {
+                o.point_local[j] = b2g_vec2{C.m.points[j].local_point.x, C.m.points[j].local_point.y};
+                o.normal_impulse[j] = C.m.points[j].normal_impulse;
+                o.tangent_impulse[j] = C.m.points[j].tangent_impulse;
+                o.point_id[j] = C.m.points[j].id;
+            }
+            o.friction = C.friction;
+            o.restitution = C.restitution;
+            o.restitution_threshold = C.threshold;
+        }
+        ++k;
+    }
+    *n = k;
+    return 0;
+}
+
+/* Pairs of the last update_pairs as fixture ids (min, max), in emission order (may repeat). */
+int ora_get_pairs(void* p, uint32_t* out, int cap, int* n) {
+    World& w = *(World*)p;
+    int k = 0;
+    for (const Pair& pr : w.last_pairs) {
+        if (k < cap && out) {
+            int fa = w.bp.tree.user(pr.a), fb = w.bp.tree.user(pr.b);
+            out[2 * k] = (uint32_t)(fa < fb ? fa : fb);
+            out[2 * k + 1] = (uint32_t)(fa < fb ? fb : fa);
+        }
+        ++k;
+    }
+    *n = k;
+    return 0;
+}
+
+/* Fat AABB per fixture, whether it was in the move buffer at the last update_pairs, and its proxy id. */
+int ora_get_proxies(void* p, float* aabbs, uint8_t* moved, int* proxy_ids, int cap) {
+    World& w = *(World*)p;
+    int n = (int)w.fixtures.size();
+    for (int i = 0; i < n && i < cap; ++i) {
+        const Fixture& f = w.fixtures[i];
+        if (f.proxy < 0) continue;
+        const AABB& a = w.bp.tree.fat_aabb(f.proxy);
+        aabbs[4 * i + 0] = a.lo.x;
+        aabbs[4 * i + 1] = a.lo.y;
+        aabbs[4 * i + 2] = a.hi.x;
+        aabbs[4 * i + 3] = a.hi.y;
+        if (moved) moved[i] = w.last_moved[i];
+        if (proxy_ids) proxy_ids[i] = f.proxy;
+    }
+    return 0;
+}
+
+/* Ordering hook: pairs (fixture_a, fixture_b) in the order islands must solve them; n = 0 clears. */
+int ora_set_solver_order(void* p, const uint32_t* pairs, int n) {
+    World& w = *(World*)p;
+    w.hook_rank.clear();
+    w.hook_misses = 0;
+    w.hook = n > 0;
+    w.hook_rank.reserve((size_t)n * 2);
+    for (int i = 0; i < n; ++i) w.hook_rank[pair_key((int)pairs[2 * i], (int)pairs[2 * i + 1])] = i;
+    return 0;
+}
+
+int ora_get_hook_misses(void* p) { return ((World*)p)->hook_misses; }
+
+int ora_get_solver_order(void* p, uint32_t* out, int cap, int* n) {
+    World& w = *(World*)p;
+    int k = 0;
+    for (uint64_t key : w.last_order) {
+        if (k < cap && out) {
+            out[2 * k] = (uint32_t)(key >> 32);
+            out[2 * k + 1] = (uint32_t)(key & 0xffffffffu);
+        }
+        ++k;
+    }
+    *n = k;
+    return 0;
+}
+
+int ora_get_events(void* p, b2g_contact_event* out, int cap, int* n) {
+    World& w = *(World*)p;
+    int k = (int)w.events.size();
+    for (int i = 0; i < k && i < cap; ++i) out[i] = w.events[i];
+    *n = k;
+    w.events.clear();
+    return 0;
+}
+
+/* Shape helpers exposed for known-answer tests (collision_test.rs / math_test.rs). */
+int ora_polygon_mass(const b2g_fixture_def* d, float* out_centroid_mass_center_I) {
+    Shape s;
+    build_shape(*d, s);
+    MassData md;
+    compute_mass(s, d->density, md);
+    out_centroid_mass_center_I[0] = s.centroid.x;
+    out_centroid_mass_center_I[1] = s.centroid.y;
+    out_centroid_mass_center_I[2] = md.mass;
+    out_centroid_mass_center_I[3] = md.center.x;
+    out_centroid_mass_center_I[4] = md.center.y;
+    out_centroid_mass_center_I[5] = md.I;
+    return s.count;
+}
+
+int ora_sincos(const float* x, float* s, float* c, int n) {
+    for (int i = 0; i < n; ++i) {
+        Rot q = rot(x[i]);
+        s[i] = q.s;
+        c[i] = q.c;
+    }
+    return 0;
+}
+
+/* Manifold of two standalone shapes at given transforms (narrowphase known-answer tests). */
+int ora_collide(const b2g_fixture_def* da, const float* xfa, const b2g_fixture_def* db, const float* xfb,
+                b2g_contact_info* out) {
+    Shape sa, sb;
+    build_shape(*da, sa);
+    build_shape(*db, sb);
+    Xf A{v2(xfa[0], xfa[1]), rot(xfa[2])}, B{v2(xfb[0], xfb[1]), rot(xfb[2])};
+    Manifold m;
+    int ta = sa.type, tb = sb.type;
+    if (ta == SHAPE_CIRCLE && tb == SHAPE_CIRCLE) collide_circles(m, sa, A, sb, B);
+    else if (ta == SHAPE_POLYGON && tb == SHAPE_CIRCLE) collide_polygon_circle(m, sa, A, sb, B);
+    else if (ta == SHAPE_POLYGON && tb == SHAPE_POLYGON) collide_polygons(m, sa, A, sb, B);
+    else if (ta == SHAPE_EDGE && tb == SHAPE_CIRCLE) collide_edge_circle(m, sa, A, sb, B);
+    else if (ta == SHAPE_EDGE && tb == SHAPE_POLYGON) collide_edge_polygon(m, sa, A, sb, B);
+    else return B2G_ERR_INVALID_ARG;
+    memset(out, 0, sizeof(*out));
+    out->manifold_type = m.type;
+    out->point_count = m.point_count;
+    out->local_normal = b2g_vec2{m.local_normal.x, m.local_normal.y};
+    out->local_point = b2g_vec2{m.local_point.x, m.local_point.y};
+    for (int j = 0; j < 2; ++j) {
+        out->point_local[j] = b2g_vec2{m.points[j].local_point.x, m.points[j].local_point.y};
+        out->point_id[j] = m.points[j].id;
+    }
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,236 @@
+"""ctypes binding of the oracle (liboracle.so) — TEST INFRASTRUCTURE ONLY.
+
+The oracle is a CPU restatement of box2d-rs 0.0.4's `B2world::step` path (see the
+header of b2_oracle_world.cpp for the reference lines it follows). Only tests,
+`__graft_entry__.smoke()` and bench.py's CPU-baseline / reference legs use it, as
+the checker; the product never imports it.
+
+`OracleWorld` has the same method names as `b2g.B2world`, so a parity test can
+build one scene into both and step them side by side.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liboracle.so")
+sys.path.insert(0, os.path.join(os.path.dirname(_HERE), "box2d-rs_gb300"))
+import b2g  # noqa: E402  (struct layouts of include/b2g.h)
+
+_lib = None
+
+
+def build(force=False):
+    """Compile liboracle.so with the Makefile beside this file (-ffp-contract=off)."""
+    if force and os.path.exists(LIB_PATH):
+        os.remove(LIB_PATH)
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return LIB_PATH
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        build()
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, i32, u32, f32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_float
+    pi32 = ctypes.POINTER(ctypes.c_int)
+    sig = {
+        "ora_set_trig_libm": [i32],
+        "ora_world_create": [f32, f32, ctypes.POINTER(vp)],
+        "ora_world_destroy": [vp],
+        "ora_set_flags": [vp, i32, i32, i32, i32],
+        "ora_set_record_events": [vp, i32],
+        "ora_create_bodies": [vp, vp, i32, vp],
+        "ora_create_fixtures": [vp, vp, i32, vp],
+        "ora_step": [vp, f32, i32, i32],
+        "ora_steps": [vp, f32, i32, i32, i32],
+        "ora_get_body_states": [vp, u32, u32, vp],
+        "ora_set_transform": [vp, u32, b2g.Vec2, f32],
+        "ora_set_velocity": [vp, u32, b2g.Vec2, f32],
+        "ora_get_counts": [vp, ctypes.POINTER(b2g.Counts)],
+        "ora_get_profile": [vp, ctypes.POINTER(b2g.Profile)],
+        "ora_get_contacts": [vp, vp, i32, pi32],
+        "ora_get_pairs": [vp, vp, i32, pi32],
+        "ora_get_proxies": [vp, vp, vp, vp, i32],
+        "ora_set_solver_order": [vp, vp, i32],
+        "ora_get_hook_misses": [vp],
+        "ora_get_solver_order": [vp, vp, i32, pi32],
+        "ora_get_events": [vp, vp, i32, pi32],
+        "ora_polygon_mass": [vp, vp],
+        "ora_sincos": [vp, vp, vp, i32],
+        "ora_collide": [vp, vp, vp, vp, vp],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def set_trig(libm: bool):
+    """libm=True: sin/cos from the platform libm (what the Rust reference calls).
+    libm=False: the project's correctly rounded sin/cos, identical to the GPU's."""
+    load().ora_set_trig_libm(int(libm))
+
+
+def sincos(x):
+    x = np.ascontiguousarray(x, np.float32)
+    s = np.zeros_like(x)
+    c = np.zeros_like(x)
+    load().ora_sincos(_ptr(x), _ptr(s), _ptr(c), len(x))
+    return s, c
+
+
+def polygon_mass(fixture_def):
+    out = np.zeros(6, np.float32)
+    d = np.ascontiguousarray(fixture_def, b2g.FIXTURE_DEF)
+    count = load().ora_polygon_mass(_ptr(d), _ptr(out))
+    return {"centroid": out[0:2].copy(), "mass": out[2], "center": out[3:5].copy(), "I": out[5], "count": count}
+
+
+def collide(def_a, xf_a, def_b, xf_b):
+    """Manifold of two standalone shapes; xf = (x, y, angle)."""
+    da = np.ascontiguousarray(def_a, b2g.FIXTURE_DEF)
+    db = np.ascontiguousarray(def_b, b2g.FIXTURE_DEF)
+    xa = np.asarray(xf_a, np.float32)
+    xb = np.asarray(xf_b, np.float32)
+    out = np.zeros(1, b2g.CONTACT_INFO)
+    rc = load().ora_collide(_ptr(da), _ptr(xa), _ptr(db), _ptr(xb), _ptr(out))
+    if rc != 0:
+        raise ValueError("unsupported shape pair")
+    return out[0]
+
+
+class OracleWorld:
+    """The CPU restatement of B2world; same method names as b2g.B2world."""
+
+    def __init__(self, gravity=(0.0, -10.0), allow_sleep=False, warm_starting=True, record_events=False):
+        self._lib = load()
+        h = ctypes.c_void_p()
+        self._lib.ora_world_create(gravity[0], gravity[1], ctypes.byref(h))
+        self._h = h
+        self.body_count = 0
+        self.fixture_count = 0
+        self._allow_sleep = allow_sleep
+        self._warm = warm_starting
+        self._apply_flags()
+        self._lib.ora_set_record_events(self._h, int(record_events))
+
+    def _apply_flags(self):
+        rc = self._lib.ora_set_flags(self._h, int(self._allow_sleep), int(self._warm), 0, 1)
+        assert rc == 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ora_world_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_allow_sleeping(self, flag):
+        self._allow_sleep = bool(flag)
+        self._apply_flags()
+
+    def set_warm_starting(self, flag):
+        self._warm = bool(flag)
+        self._apply_flags()
+
+    def create_bodies(self, defs):
+        defs = np.ascontiguousarray(defs, b2g.BODY_DEF)
+        ids = np.zeros(len(defs), np.uint32)
+        self._lib.ora_create_bodies(self._h, _ptr(defs), len(defs), _ptr(ids))
+        self.body_count += len(defs)
+        return ids
+
+    def create_fixtures(self, defs):
+        defs = np.ascontiguousarray(defs, b2g.FIXTURE_DEF)
+        ids = np.zeros(len(defs), np.uint32)
+        rc = self._lib.ora_create_fixtures(self._h, _ptr(defs), len(defs), _ptr(ids))
+        assert rc == 0, rc
+        self.fixture_count += len(defs)
+        return ids
+
+    def step(self, dt, vi, pi):
+        self._lib.ora_step(self._h, dt, vi, pi)
+
+    def steps(self, dt, vi, pi, n):
+        self._lib.ora_steps(self._h, dt, vi, pi, n)
+
+    def get_body_states(self, first=0, count=None):
+        if count is None:
+            count = self.body_count - first
+        out = np.zeros(count, b2g.BODY_STATE)
+        self._lib.ora_get_body_states(self._h, first, count, _ptr(out))
+        return out
+
+    def set_transform(self, body, position, angle):
+        self._lib.ora_set_transform(self._h, body, b2g.Vec2(*position), angle)
+
+    def set_velocity(self, body, v, w):
+        self._lib.ora_set_velocity(self._h, body, b2g.Vec2(*v), w)
+
+    def get_counts(self):
+        c = b2g.Counts()
+        self._lib.ora_get_counts(self._h, ctypes.byref(c))
+        return c.as_dict()
+
+    def get_profile(self):
+        p = b2g.Profile()
+        self._lib.ora_get_profile(self._h, ctypes.byref(p))
+        return p.as_dict()
+
+    def _get_list(self, fn, dtype, width=1):
+        n = ctypes.c_int(0)
+        fn(self._h, None, 0, ctypes.byref(n))
+        out = np.zeros(max(n.value, 1) * width, dtype)
+        fn(self._h, _ptr(out), n.value, ctypes.byref(n))
+        return out[: n.value * width]
+
+    def get_contacts(self):
+        return self._get_list(self._lib.ora_get_contacts, b2g.CONTACT_INFO)
+
+    def get_pairs(self):
+        """Emitted pairs of the last update_pairs as (min fixture, max fixture), in emission order."""
+        return self._get_list(self._lib.ora_get_pairs, np.uint32, 2).reshape(-1, 2)
+
+    def get_solver_order(self):
+        return self._get_list(self._lib.ora_get_solver_order, np.uint32, 2).reshape(-1, 2)
+
+    def get_events(self):
+        return self._get_list(self._lib.ora_get_events, b2g.EVENT)
+
+    def get_proxies(self):
+        n = self.fixture_count
+        aabbs = np.zeros((n, 4), np.float32)
+        moved = np.zeros(n, np.uint8)
+        ids = np.full(n, -1, np.int32)
+        self._lib.ora_get_proxies(self._h, _ptr(aabbs), _ptr(moved), _ptr(ids), n)
+        return aabbs, moved, ids
+
+    def set_solver_order(self, pairs):
+        """Ordering hook: each island solves its contacts in this (fixture_a, fixture_b) order."""
+        if pairs is None or len(pairs) == 0:
+            self._lib.ora_set_solver_order(self._h, None, 0)
+            return
+        p = np.ascontiguousarray(pairs, np.uint32).reshape(-1, 2)
+        self._lib.ora_set_solver_order(self._h, _ptr(p), len(p))
+
+    def hook_misses(self):
+        return self._lib.ora_get_hook_misses(self._h)
