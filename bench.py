@@ -1,0 +1,276 @@
+"""Benchmark: body-steps/s of the GPU world step on the 100k-body mixed scene.
+
+Workload (one "step" = one B2world::step(1/60, 8, 3) of the whole scene):
+  100k-body mixed scene: 50k circles (r 0.1-0.5 m) + 50k convex 3-8-gons (extent 0.1-0.6 m)
+  seeded uniformly in a 1000 x 1000 m box of static edge walls, density 1, friction 0.4,
+  v ~ N(0,1), gravity -10, dt = 1/60, 8 velocity / 3 position iterations, sleeping off,
+  continuous physics off. Synthetic data from a seeded splitmix64 stream.
+
+Legs
+  value       device-resident throughput: N_dynamic * K / (sum of per-step device times),
+              each step bracketed by CUDA events on the world's stream; an L2 flush
+              (a 256 MiB write) runs between steps outside the timed events.
+  e2e         the same steps through the public API with host buffers: b2g_step plus a
+              read of every body's state (position, angle, velocities) into host memory,
+              timed on the host clock around the whole loop.
+  cpu_baseline the oracle (a faithful single-threaded CPU restatement of box2d-rs's step,
+              libm sin/cos) timed on this host on a bounded sample of the same workload.
+  --impl reference  times that CPU restatement alone (the real Rust crate cannot be built
+              without cargo) and prints the reference line.
+Multi-GPU (torchrun): the single world does not shard, so each rank steps its own replica
+("replicas only"); value is all ranks' body-steps over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "box2d-rs_gb300"))
+
+import b2g  # noqa: E402
+import scenes  # noqa: E402
+
+WORKLOAD = "mixed-100k: 50k circles + 50k 3-8-gons, 1000x1000 m walled box, 8/3 iterations, dt=1/60"
+METRIC = "body-steps/s @100k bodies (mixed scene)"
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def bytes_model(counts, scene_stats, vi, pi):
+    """Algorithmic HBM bytes of one step by phase (SoA layout of csrc/b2g_internal.h).
+
+    per dynamic body   integrate velocities 72 B, integrate positions 48 B, write-back 40 B,
+                       fixture sync 76 B + 16 B/vertex
+    per contact        collide: 116 B state + shape bytes (polygon 16 B/vertex + 12, circle 12, edge 36)
+    per constraint     init + warm start 320 B, velocity iteration 208 B, position iteration 128 B,
+                       store 16 B
+    per proxy          broadphase keys/sort/build/refit 16 B + 8 B per new pair
+    """
+    nb, nc, ncons = scene_stats["n_dynamic"], counts["contacts"], counts["islands_solved"]
+    shape = scene_stats["shape_bytes_mean"]
+    collide = nc * (116 + 2 * shape)
+    solver = nb * (72 + 48 + 40) + ncons * (320 + 208 * vi + 128 * pi + 16) + scene_stats["n_fixtures"] * (76 + shape)
+    broad = scene_stats["n_fixtures"] * 16 * 6 + counts["pairs"] * 8
+    return {"collide": collide, "solver": solver, "broadphase": broad}
+
+
+def scene_stats(scene):
+    f = scene["fixtures"]
+    st = f["shape_type"]
+    shape = np.where(st == b2g.CIRCLE, 12, np.where(st == b2g.EDGE, 36, 16 * np.maximum(f["vertex_count"], 4) + 12))
+    return {"n_dynamic": scene["n_dynamic"], "n_fixtures": len(f), "shape_bytes_mean": float(shape.mean())}
+
+
+def run_cpu_baseline(scene, budget_s=15.0, max_steps=60):
+    """Time the oracle (libm trig, single thread) on the first steps of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.set_trig(True)
+    w = oracle.OracleWorld(gravity=scene["gravity"], allow_sleep=False)
+    scenes.build_world(w, scene)
+    steps = 0
+    t0 = time.perf_counter()
+    while steps < max_steps and time.perf_counter() - t0 < budget_s:
+        w.step(scene["dt"], scene["vi"], scene["pi"])
+        steps += 1
+    dt = time.perf_counter() - t0
+    return {"value": scene["n_dynamic"] * steps / dt, "unit": "body-steps/s", "cores": 1, "kind": "port",
+            "sample": f"first {steps} steps of the mixed-100k scene (oracle, libm sin/cos, 1 thread, {dt:.1f} s)"}
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=600)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--scale", type=float, default=1.0, help="fraction of the 100k bodies (testing only)")
+    args = ap.parse_args()
+    rank, world_size, local_rank = dist_info()
+    n_half = int(50_000 * args.scale)
+    scene = scenes.mixed(n_circles=n_half, n_polygons=n_half)
+    stats = scene_stats(scene)
+    config = {"workload": WORKLOAD, "bodies": stats["n_dynamic"], "fixtures": stats["n_fixtures"],
+              "velocity_iterations": 8, "position_iterations": 3, "dt": 1 / 60, "sleep": False,
+              "continuous": False, "l2": "256 MiB flush between timed steps", "parallelism": "replicas"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = run_cpu_baseline(scene, budget_s=20.0, max_steps=max(args.steps, 1))
+        line = {"metric": METRIC, "value": cb["value"], "unit": "body-steps/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
+                "dtype": "f32", "data": "synthetic (seeded splitmix64)", "config": config, "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "vs_baseline": None,
+                "note": "box2d-rs cannot be compiled here (no Rust toolchain); timed its faithful C++ restatement"}
+        print(json.dumps(line))
+        return
+
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    if world_size > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    w = b2g.B2world(gravity=scene["gravity"], device=local_rank)
+    w.set_allow_sleeping(False)
+    w.set_continuous_physics(False)
+    scenes.build_world(w, scene)
+    dt, vi, pi = scene["dt"], scene["vi"], scene["pi"]
+    for _ in range(args.warmup):
+        w.step(dt, vi, pi)
+    w.synchronize()
+
+    sampler = ClockSampler(local_rank)
+    if world_size > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    launches0 = w._lib.b2g_get_launch_count()
+    total_ms = 0.0
+    phase_ms = {"collide": 0.0, "solve_init": 0.0, "solve_velocity": 0.0, "broadphase": 0.0}
+    per_step = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        w.step(dt, vi, pi)
+        p = w.get_profile()  # synchronizes the world's stream; event times of this step
+        total_ms += p["step"]
+        per_step.append(p["step"])
+        for k in phase_ms:
+            phase_ms[k] += p[k]
+    launches = w._lib.b2g_get_launch_count() - launches0
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    counts = w.get_counts()
+
+    # e2e: steps through the API with every body's state read back to host memory
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 200))
+    states = np.zeros(w.body_count, b2g.BODY_STATE)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        w.step(dt, vi, pi)
+        w.get_body_states(out=states)
+    e2e_s = time.perf_counter() - t0
+    d2h = w.body_count * 48  # three float4 arrays per body
+
+    if world_size > 1:
+        t = torch.tensor([total_ms, e2e_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms, e2e_s = float(t[0]), float(t[1])
+    units = stats["n_dynamic"] * args.steps * world_size
+    value = units / (total_ms / 1e3)
+    e2e_value = stats["n_dynamic"] * e2e_steps * world_size / e2e_s
+
+    peak, peak_kind = load_peaks()
+    bm = bytes_model(counts, stats, vi, pi)
+    ms_phase = {"collide": phase_ms["collide"], "solver": phase_ms["solve_velocity"] + phase_ms["solve_init"],
+                "broadphase": phase_ms["broadphase"]}
+    dominant = max(ms_phase, key=ms_phase.get)
+    achieved = bm[dominant] / (ms_phase[dominant] / args.steps / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded splitmix64)",
+        "config": config,
+        "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,
+                "steps": e2e_steps},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel_phase": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None},
+        "phase_ms_per_step": {k: v / args.steps for k, v in ms_phase.items()},
+        "counts_last_step": counts,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = run_cpu_baseline(scene)
+    if rank == 0:
+        print(json.dumps(line))
+    if world_size > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

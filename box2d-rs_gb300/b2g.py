@@ -313,6 +313,8 @@ def load_library(path=LIB_PATH):
         "b2g_get_pairs": [vp, vp, i32, ctypes.POINTER(i32)],
         "b2g_get_proxies": [vp, vp, vp, i32],
         "b2g_get_solver_order": [vp, vp, i32, ctypes.POINTER(i32)],
+        "b2g_set_contact_events": [vp, i32],
+        "b2g_set_record_pairs": [vp, i32],
         "b2g_version": [],
     }
     for name, args in sig.items():
@@ -321,8 +323,26 @@ def load_library(path=LIB_PATH):
         fn.restype = ctypes.c_int
     lib.b2g_last_error.argtypes = [vp]
     lib.b2g_last_error.restype = ctypes.c_char_p
+    lib.b2g_collide_pairs.argtypes = [vp, vp, vp, vp, i32, vp]
+    lib.b2g_collide_pairs.restype = ctypes.c_int
+    lib.b2g_get_launch_count.argtypes = []
+    lib.b2g_get_launch_count.restype = ctypes.c_int64
     _lib = lib
     return lib
+
+
+def collide_pairs(defs_a, xf_a, defs_b, xf_b):
+    """GPU manifolds of independent shape pairs (b2_collide_*); xf rows are (x, y, angle)."""
+    lib = load_library()
+    da = np.ascontiguousarray(defs_a, FIXTURE_DEF)
+    db = np.ascontiguousarray(defs_b, FIXTURE_DEF)
+    xa = np.ascontiguousarray(xf_a, np.float32)
+    xb = np.ascontiguousarray(xf_b, np.float32)
+    out = np.zeros(len(da), CONTACT_INFO)
+    rc = lib.b2g_collide_pairs(_ptr(da), _ptr(xa), _ptr(db), _ptr(xb), len(da), _ptr(out))
+    if rc != OK:
+        raise B2GError(rc, "b2g_collide_pairs")
+    return out
 
 
 class B2world:
@@ -449,6 +469,13 @@ class B2world:
     def set_contact_listener(self, listener):
         """`listener` has begin_contact(fa, fb) and end_contact(fa, fb); events are replayed after each step."""
         self._listener = listener
+        self.set_contact_events(listener is not None)
+
+    def set_contact_events(self, flag):
+        self._check(self._lib.b2g_set_contact_events(self._h, int(flag)))
+
+    def set_record_pairs(self, flag):
+        self._check(self._lib.b2g_set_record_pairs(self._h, int(flag)))
 
     # -- introspection --
     def get_profile(self):

@@ -1,0 +1,1239 @@
+/*
+ * api.cu — the C ABI of include/b2g.h and the host-side world that drives the kernels.
+ *
+ * Creation (B2world::create_body, B2body::create_fixture) runs on the host, because it
+ * is rare and sequential: polygon hulls (B2polygonShape::set), mass data
+ * (compute_mass + reset_mass_data) and the first fat AABB of each proxy are computed
+ * here with the same f32 operation order as the reference, then uploaded. After the
+ * first step the device copy is authoritative; setters launch small kernels.
+ *
+ * A step (B2world::step, src/private/dynamics/b2_world.rs:903-959) is a fixed sequence
+ * of launches on the world's stream with no host synchronisation:
+ *   [broadphase if fixtures were added] -> collide -> islands + constraints ->
+ *   colouring (cooperative) -> solver (cooperative) -> broadphase + contact merge.
+ * Counts that vary per step live in device memory and every kernel reads them there.
+ *
+ * Proxy ids: the reference's proxy id is the node-pool index of the proxy's leaf in its
+ * dynamic tree. Without destruction that index depends only on creation order (the k-th
+ * proxy gets 0 for k = 0 and 2k - 1 afterwards, since every later insertion also takes
+ * one internal node and moves return what they take), so it is reproduced exactly and
+ * used for the same purposes: which fixture of a same-type pair is A, and the moved rule.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/b2g.h"
+#include "b2g_internal.h"
+
+using namespace b2g;
+
+namespace {
+
+constexpr int kVersion = 1;
+
+struct Timer {
+    cudaEvent_t e[8] = {};
+    bool valid = false;
+};
+
+struct World {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 152;
+    b2g_vec2 gravity{0.0f, -10.0f};
+    int num_worlds = 1;
+    bool warm = true, continuous = false, allow_sleep = true, auto_clear = true;
+    bool record_events = false, record_pairs = false;
+    bool new_contacts = false;
+    float inv_dt0 = 0.0f;
+    std::string err;
+    int steps = 0;
+    /* host mirrors (authoritative until the first upload) */
+    std::vector<float4> h_xf, h_pos, h_pos0, h_vel, h_force, h_mass, h_damp;
+    std::vector<float2> h_lc;
+    std::vector<uint32_t> h_flags, h_world;
+    std::vector<std::vector<int>> body_fixtures;  /* newest first, like the reference's fixture list */
+    std::vector<ShapeRec> h_shape;
+    std::vector<int> h_fbody;
+    std::vector<float4> h_fmat, h_fat;
+    std::vector<uint32_t> h_filter, h_group, h_refid;
+    std::vector<uint8_t> h_moved;
+    int proxies_created = 0;
+    /* device */
+    DevWorld d{};
+    bool allocated = false;
+    int uploaded_bodies = 0, uploaded_fixtures = 0;
+    bool device_authoritative = false;
+    std::vector<void*> allocations;
+    int user_contact_cap = 0, user_pair_cap = 0;
+    Timer timer;
+    b2g_profile profile{};
+    int last_colours = 0;
+};
+
+int fail(World* w, int code, const char* msg) {
+    if (w) w->err = msg;
+    return code;
+}
+
+#define CUDA_OK(w, call)                                                       \
+    do {                                                                       \
+        cudaError_t e_ = (call);                                               \
+        if (e_ != cudaSuccess) {                                               \
+            (w)->err = std::string(#call) + ": " + cudaGetErrorString(e_);     \
+            return B2G_ERR_CUDA;                                               \
+        }                                                                      \
+    } while (0)
+
+template <class T>
+int dalloc(World* w, T** p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        w->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        return B2G_ERR_OUT_OF_MEMORY;
+    }
+    w->allocations.push_back((void*)*p);
+    cudaMemsetAsync(*p, 0, n * sizeof(T), w->stream);
+    return B2G_OK;
+}
+
+void free_all(World* w) {
+    for (void* p : w->allocations) cudaFree(p);
+    w->allocations.clear();
+    w->allocated = false;
+}
+
+int bits_for(uint64_t v) {
+    int b = 1;
+    while ((1ull << b) <= v) ++b;
+    return b;
+}
+
+/* ---- creation-time geometry (host) ---- */
+
+/* B2polygonShape::set_as_box, private/collision/b2_polygon_shape.rs:12-23 */
+void polygon_box(ShapeRec& s, float hx, float hy) {
+    s.v[0] = mk(-hx, -hy);
+    s.v[1] = mk(hx, -hy);
+    s.v[2] = mk(hx, hy);
+    s.v[3] = mk(-hx, hy);
+    s.n[0] = mk(0.0f, -1.0f);
+    s.n[1] = mk(1.0f, 0.0f);
+    s.n[2] = mk(0.0f, 1.0f);
+    s.n[3] = mk(-1.0f, 0.0f);
+    s.centroid = mk(0.0f, 0.0f);
+    s.meta = SHAPE_POLYGON | (4 << 8);
+}
+
+/* polygon centroid, b2_polygon_shape.rs:53-77 */
+V2 polygon_centroid(const V2* vs, int count) {
+    V2 c = mk(0.0f, 0.0f);
+    float area = 0.0f;
+    const V2 s = vs[0];
+    const float inv3 = 1.0f / 3.0f;
+    for (int i = 0; i < count; ++i) {
+        V2 p1 = sub(vs[0], s);
+        V2 p2 = sub(vs[i], s);
+        V2 p3 = (i + 1 < count) ? sub(vs[i + 1], s) : sub(vs[0], s);
+        V2 e1 = sub(p2, p1);
+        V2 e2 = sub(p3, p1);
+        float d = cross(e1, e2);
+        float tri = 0.5f * d;
+        area += tri;
+        c = add(c, scale(tri * inv3, add(add(p1, p2), p3)));
+    }
+    return add(scale(1.0f / area, c), s);
+}
+
+/* B2polygonShape::set (gift wrapping), b2_polygon_shape.rs:96-211; false -> unit box fallback */
+bool polygon_hull(ShapeRec& s, const b2g_vec2* in, int count) {
+    if (count < 3) {
+        polygon_box(s, 1.0f, 1.0f);
+        return false;
+    }
+    int n = count < kMaxPolygonVertices ? count : kMaxPolygonVertices;
+    V2 ps[kMaxPolygonVertices];
+    int temp = 0;
+    for (int i = 0; i < n; ++i) {
+        V2 v = mk(in[i].x, in[i].y);
+        bool unique = true;
+        for (int j = 0; j < temp; ++j) {
+            if (dist_sq(v, ps[j]) < ((0.5f * kLinearSlop) * (0.5f * kLinearSlop))) {
+                unique = false;
+                break;
+            }
+        }
+        if (unique) ps[temp++] = v;
+    }
+    n = temp;
+    if (n < 3) {
+        polygon_box(s, 1.0f, 1.0f);
+        return false;
+    }
+    int i0 = 0;
+    float x0 = ps[0].x;
+    for (int i = 1; i < n; ++i) {
+        float x = ps[i].x;
+        if (x > x0 || (x == x0 && ps[i].y < ps[i0].y)) {
+            i0 = i;
+            x0 = x;
+        }
+    }
+    int hull[kMaxPolygonVertices];
+    int m = 0, ih = i0;
+    for (;;) {
+        if (m >= kMaxPolygonVertices) {
+            polygon_box(s, 1.0f, 1.0f);
+            return false;
+        }
+        hull[m] = ih;
+        int ie = 0;
+        for (int j = 1; j < n; ++j) {
+            if (ie == ih) {
+                ie = j;
+                continue;
+            }
+            V2 r = sub(ps[ie], ps[hull[m]]);
+            V2 v = sub(ps[j], ps[hull[m]]);
+            float c = cross(r, v);
+            if (c < 0.0f) ie = j;
+            if (c == 0.0f && length_sq(v) > length_sq(r)) ie = j;
+        }
+        ++m;
+        ih = ie;
+        if (ie == i0) break;
+    }
+    if (m < 3) {
+        polygon_box(s, 1.0f, 1.0f);
+        return false;
+    }
+    for (int i = 0; i < m; ++i) s.v[i] = ps[hull[i]];
+    for (int i = 0; i < m; ++i) {
+        int i2 = (i + 1 < m) ? i + 1 : 0;
+        s.n[i] = cross_vs(sub(s.v[i2], s.v[i]), 1.0f);
+        normalize(s.n[i]);
+    }
+    s.centroid = polygon_centroid(s.v, m);
+    s.meta = SHAPE_POLYGON | (m << 8);
+    return true;
+}
+
+void build_shape(const b2g_fixture_def& d, ShapeRec& s) {
+    memset(&s, 0, sizeof(s));
+    s.radius = d.radius;
+    if (d.shape_type == B2G_SHAPE_CIRCLE) {
+        s.v[0] = mk(d.vertices[0].x, d.vertices[0].y);
+        s.meta = SHAPE_CIRCLE | (1 << 8);
+    } else if (d.shape_type == B2G_SHAPE_EDGE) {
+        for (int i = 0; i < 4; ++i) s.v[i] = mk(d.vertices[i].x, d.vertices[i].y);
+        s.meta = SHAPE_EDGE | (2 << 8) | ((d.one_sided ? 1 : 0) << 16);
+    } else {
+        if (d.polygon_mode == B2G_POLYGON_BOX) {
+            polygon_box(s, d.box_half_extents.x, d.box_half_extents.y);
+        } else if (d.polygon_mode == B2G_POLYGON_BOX_ORIENTED) {
+            /* set_as_box_angle, b2_polygon_shape.rs:25-50 */
+            polygon_box(s, d.box_half_extents.x, d.box_half_extents.y);
+            Xf xf;
+            xf.p = mk(d.box_center.x, d.box_center.y);
+            xf.q = rot(d.box_angle);
+            s.centroid = xf.p;
+            for (int i = 0; i < 4; ++i) {
+                s.v[i] = mul(xf, s.v[i]);
+                s.n[i] = mul(xf.q, s.n[i]);
+            }
+        } else {
+            polygon_hull(s, d.vertices, d.vertex_count);
+        }
+        s.radius = d.radius;
+    }
+}
+
+/* compute_mass of each shape: b2_polygon_shape.rs:314-390, b2_circle_shape.rs:79-86, b2_edge_shape.rs:126-132 */
+void shape_mass(const ShapeRec& s, float density, float& mass, V2& center, float& I) {
+    const int t = shape_type(s);
+    if (t == SHAPE_CIRCLE) {
+        mass = density * kPi * s.radius * s.radius;
+        center = s.v[0];
+        I = mass * (0.5f * s.radius * s.radius + dot(s.v[0], s.v[0]));
+    } else if (t == SHAPE_EDGE) {
+        mass = 0.0f;
+        center = scale(0.5f, add(s.v[1], s.v[2]));
+        I = 0.0f;
+    } else {
+        const int n = shape_count(s);
+        V2 c = mk(0.0f, 0.0f);
+        float area = 0.0f, inert = 0.0f;
+        const V2 o = s.v[0];
+        const float inv3 = 1.0f / 3.0f;
+        for (int i = 0; i < n; ++i) {
+            V2 e1 = sub(s.v[i], o);
+            V2 e2 = (i + 1 < n) ? sub(s.v[i + 1], o) : sub(s.v[0], o);
+            float d = cross(e1, e2);
+            float tri = 0.5f * d;
+            area += tri;
+            c = add(c, scale(tri * inv3, add(e1, e2)));
+            float intx2 = e1.x * e1.x + e2.x * e1.x + e2.x * e2.x;
+            float inty2 = e1.y * e1.y + e2.y * e1.y + e2.y * e2.y;
+            inert += ((0.25f * inv3) * d) * (intx2 + inty2);
+        }
+        mass = density * area;
+        c = scale(1.0f / area, c);
+        center = add(c, o);
+        I = density * inert;
+        I += mass * (dot(center, center) - dot(c, c));
+    }
+}
+
+Xf host_xf(const World* w, int b) {
+    Xf x;
+    x.p = mk(w->h_xf[b].x, w->h_xf[b].y);
+    x.q.s = w->h_xf[b].z;
+    x.q.c = w->h_xf[b].w;
+    return x;
+}
+
+/* reset_mass_data, private/dynamics/b2_body.rs:292-350 */
+void reset_mass_data(World* w, int b) {
+    float4& pos = w->h_pos[b];
+    float4& pos0 = w->h_pos0[b];
+    float4& m = w->h_mass[b];
+    float4& v = w->h_vel[b];
+    const uint32_t fl = w->h_flags[b];
+    const Xf xf = host_xf(w, b);
+    m = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    w->h_lc[b] = make_float2(0.0f, 0.0f);
+    const int type = (int)(fl & BF_TYPE_MASK);
+    if (type != BODY_DYNAMIC) {
+        pos = make_float4(xf.p.x, xf.p.y, pos.z, 0.0f);
+        pos0 = make_float4(xf.p.x, xf.p.y, pos.z, 0.0f);
+        return;
+    }
+    V2 lc = mk(0.0f, 0.0f);
+    float mass = 0.0f, I = 0.0f, inv_mass = 0.0f, inv_I = 0.0f;
+    for (int f : w->body_fixtures[b]) {
+        const float density = w->h_fmat[f].w;
+        if (density == 0.0f) continue;
+        float fm, fi;
+        V2 fc;
+        shape_mass(w->h_shape[f], density, fm, fc, fi);
+        mass += fm;
+        lc = add(lc, scale(fm, fc));
+        I += fi;
+    }
+    if (mass > 0.0f) {
+        inv_mass = 1.0f / mass;
+        lc.x *= inv_mass;
+        lc.y *= inv_mass;
+    }
+    if (I > 0.0f && !(fl & BF_FIXED_ROTATION)) {
+        I -= mass * dot(lc, lc);
+        inv_I = 1.0f / I;
+    } else {
+        I = 0.0f;
+        inv_I = 0.0f;
+    }
+    m = make_float4(mass, inv_mass, I, inv_I);
+    const V2 old_center = mk(pos.x, pos.y);
+    w->h_lc[b] = make_float2(lc.x, lc.y);
+    const V2 c0 = mul(xf, lc);
+    pos = make_float4(c0.x, c0.y, pos.z, 0.0f);
+    pos0 = make_float4(c0.x, c0.y, pos0.z, 0.0f);
+    const V2 dv = cross_sv(v.z, sub(c0, old_center));
+    v.x += dv.x;
+    v.y += dv.y;
+}
+
+/* host copy of the fat-AABB rule of B2dynamicTree::move_proxy (private/collision/b2_dynamic_tree.rs:109-168) */
+void host_move_proxy(World* w, int f, const AABB& aabb, V2 disp) {
+    const V2 r = mk(kAabbExtension, kAabbExtension);
+    AABB fat;
+    fat.lo = sub(aabb.lo, r);
+    fat.hi = add(aabb.hi, r);
+    const V2 d = scale(kAabbMultiplier, disp);
+    if (d.x < 0.0f) fat.lo.x += d.x; else fat.hi.x += d.x;
+    if (d.y < 0.0f) fat.lo.y += d.y; else fat.hi.y += d.y;
+    const float4 t = w->h_fat[f];
+    AABB tree;
+    tree.lo = mk(t.x, t.y);
+    tree.hi = mk(t.z, t.w);
+    if (contains(tree, aabb)) {
+        AABB huge;
+        huge.lo = sub(fat.lo, scale(4.0f, r));
+        huge.hi = add(fat.hi, scale(4.0f, r));
+        if (contains(huge, tree)) return;
+    }
+    w->h_fat[f] = make_float4(fat.lo.x, fat.lo.y, fat.hi.x, fat.hi.y);
+    w->h_moved[f] = 1;
+}
+
+/* ---- device allocation, upload and download ---- */
+
+int allocate(World* w, int nb, int nf) {
+    DevWorld& d = w->d;
+    const int body_cap = nb + nb / 4 + 1024;
+    const int fix_cap = nf + nf / 4 + 1024;
+    /* a capacity given in b2g_world_def is used as is; 0 picks one proportional to the fixtures */
+    const int contact_cap = w->user_contact_cap > 0 ? w->user_contact_cap : 6 * fix_cap + 4096;
+    const int pair_cap = w->user_pair_cap > 0 ? w->user_pair_cap : 4 * fix_cap + 4096;
+    d.body_cap = body_cap;
+    d.fix_cap = fix_cap;
+    d.contact_cap = contact_cap;
+    d.pair_cap = pair_cap;
+    d.event_cap = contact_cap;
+    d.cons_cap = contact_cap;
+    d.num_worlds = w->num_worlds;
+    int rc = B2G_OK;
+#define A(ptr, n)                                      \
+    do {                                               \
+        if ((rc = dalloc(w, &(ptr), (size_t)(n))) != B2G_OK) return rc; \
+    } while (0)
+    A(d.b_xf, body_cap); A(d.b_pos, body_cap); A(d.b_pos0, body_cap); A(d.b_vel, body_cap);
+    A(d.b_force, body_cap); A(d.b_mass, body_cap); A(d.b_damp, body_cap); A(d.b_lc, body_cap);
+    A(d.b_flags, body_cap); A(d.b_world, body_cap); A(d.b_island, body_cap);
+    A(d.b_cmin, body_cap); A(d.b_cmask, body_cap);
+    A(d.isl_minsep, 2 * (size_t)body_cap); A(d.isl_done, body_cap); A(d.isl_sleep, body_cap);
+    A(d.f_shape, fix_cap); A(d.f_body, fix_cap); A(d.f_mat, fix_cap); A(d.f_filter, fix_cap);
+    A(d.f_group, fix_cap); A(d.f_refid, fix_cap); A(d.f_fat, fix_cap); A(d.f_moved, fix_cap);
+    Contacts* cs[2] = {&d.c, &d.c_alt};
+    for (Contacts* c : cs) {
+        A(c->key, contact_cap); A(c->fix, contact_cap); A(c->body, contact_cap); A(c->flags, contact_cap);
+        A(c->mat, contact_cap); A(c->mgeo, contact_cap); A(c->mpts, contact_cap); A(c->mimp, contact_cap);
+        A(c->mids, contact_cap);
+    }
+    A(d.c_rank, contact_cap);
+    A(d.n_key, pair_cap); A(d.n_fix, pair_cap); A(d.n_idx, pair_cap); A(d.n_key_alt, pair_cap); A(d.n_idx_alt, pair_cap);
+    A(d.cons_contact, contact_cap); A(d.cons_colour, contact_cap); A(d.cons_island, contact_cap);
+    A(d.s_contact, contact_cap); A(d.s_cons, contact_cap); A(d.s_fix, contact_cap);
+    A(d.col_off, kMaxColours + 1); A(d.col_hist, kMaxColours);
+    A(d.vc_idx, contact_cap); A(d.vc_inv, contact_cap); A(d.vc_nf, contact_cap); A(d.vc_r0, contact_cap);
+    A(d.vc_r1, contact_cap); A(d.vc_m0, contact_cap); A(d.vc_m1, contact_cap); A(d.vc_imp, contact_cap);
+    A(d.vc_k, contact_cap); A(d.vc_island, contact_cap);
+    A(d.pc_lp, contact_cap); A(d.pc_geo, contact_cap); A(d.pc_lc, contact_cap); A(d.pc_inv, contact_cap);
+    A(d.pc_meta, contact_cap);
+    A(d.bp_key, fix_cap); A(d.bp_val, fix_cap); A(d.bp_key_alt, fix_cap); A(d.bp_val_alt, fix_cap);
+    A(d.bp_leaf, fix_cap); A(d.bp_node_b0, fix_cap); A(d.bp_node_b1, fix_cap); A(d.bp_node_child, fix_cap);
+    A(d.bp_parent, 2 * (size_t)fix_cap); A(d.bp_flag, fix_cap);
+    A(d.bp_world_root, w->num_worlds); A(d.bp_world_first, w->num_worlds);
+    A(d.events, d.event_cap);
+    A(d.pairs, pair_cap);
+    A(d.scan_tmp, 2 * (size_t)contact_cap + scan_tmp_size(contact_cap) + 64);
+    const size_t hist = radix_sort_hist_size(std::max(fix_cap, pair_cap));
+    A(d.sort_hist, hist);
+    A(d.cnt, CNT_SIZE);
+#undef A
+    w->allocated = true;
+    return B2G_OK;
+}
+
+int upload(World* w) {
+    DevWorld& d = w->d;
+    const int nb = (int)w->h_flags.size();
+    const int nf = (int)w->h_fbody.size();
+    cudaStream_t s = w->stream;
+#define U(dst, src) CUDA_OK(w, cudaMemcpyAsync((dst), (src).data(), (src).size() * sizeof((src)[0]), cudaMemcpyHostToDevice, s))
+    if (nb > 0) {
+        U(d.b_xf, w->h_xf); U(d.b_pos, w->h_pos); U(d.b_pos0, w->h_pos0); U(d.b_vel, w->h_vel);
+        U(d.b_force, w->h_force); U(d.b_mass, w->h_mass); U(d.b_damp, w->h_damp); U(d.b_lc, w->h_lc);
+        U(d.b_flags, w->h_flags); U(d.b_world, w->h_world);
+    }
+    if (nf > 0) {
+        U(d.f_shape, w->h_shape); U(d.f_body, w->h_fbody); U(d.f_mat, w->h_fmat); U(d.f_filter, w->h_filter);
+        U(d.f_group, w->h_group); U(d.f_refid, w->h_refid); U(d.f_fat, w->h_fat); U(d.f_moved, w->h_moved);
+    }
+#undef U
+    CUDA_OK(w, cudaStreamSynchronize(s));
+    w->uploaded_bodies = nb;
+    w->uploaded_fixtures = nf;
+    d.n_bodies = nb;
+    d.n_fixtures = nf;
+    return B2G_OK;
+}
+
+/* device -> host mirrors for bodies and fixtures (before host-side edits after stepping) */
+int download_state(World* w) {
+    DevWorld& d = w->d;
+    const int nb = w->uploaded_bodies;
+    const int nf = w->uploaded_fixtures;
+    cudaStream_t s = w->stream;
+#define D(src, dst, n) CUDA_OK(w, cudaMemcpyAsync((dst).data(), (src), (size_t)(n) * sizeof((dst)[0]), cudaMemcpyDeviceToHost, s))
+    if (nb > 0) {
+        D(d.b_xf, w->h_xf, nb); D(d.b_pos, w->h_pos, nb); D(d.b_pos0, w->h_pos0, nb); D(d.b_vel, w->h_vel, nb);
+        D(d.b_force, w->h_force, nb); D(d.b_flags, w->h_flags, nb);
+    }
+    if (nf > 0) {
+        D(d.f_fat, w->h_fat, nf); D(d.f_moved, w->h_moved, nf);
+    }
+#undef D
+    CUDA_OK(w, cudaStreamSynchronize(s));
+    return B2G_OK;
+}
+
+/* Makes the device hold every created body and fixture; grows capacities by rebuilding. */
+int prepare(World* w) {
+    const int nb = (int)w->h_flags.size();
+    const int nf = (int)w->h_fbody.size();
+    if (w->allocated && nb == w->uploaded_bodies && nf == w->uploaded_fixtures) return B2G_OK;
+    if (w->allocated && (nb > w->d.body_cap || nf > w->d.fix_cap)) {
+        /* rebuild: keep the current contact table (its keys and impulses) across the reallocation */
+        CUDA_OK(w, cudaStreamSynchronize(w->stream));
+        int n_contacts = 0;
+        CUDA_OK(w, cudaMemcpy(&n_contacts, w->d.cnt + CNT_CONTACTS, sizeof(int), cudaMemcpyDeviceToHost));
+        Contacts old = w->d.c;
+        const int old_cap = w->d.contact_cap;
+        std::vector<unsigned long long> key(n_contacts);
+        std::vector<int2> fix(n_contacts), body(n_contacts);
+        std::vector<uint32_t> flags(n_contacts);
+        std::vector<float4> mat(n_contacts), mgeo(n_contacts), mpts(n_contacts), mimp(n_contacts);
+        std::vector<uint4> mids(n_contacts);
+        if (n_contacts > 0) {
+            cudaMemcpy(key.data(), old.key, n_contacts * sizeof(uint64_t), cudaMemcpyDeviceToHost);
+            cudaMemcpy(fix.data(), old.fix, n_contacts * sizeof(int2), cudaMemcpyDeviceToHost);
+            cudaMemcpy(body.data(), old.body, n_contacts * sizeof(int2), cudaMemcpyDeviceToHost);
+            cudaMemcpy(flags.data(), old.flags, n_contacts * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+            cudaMemcpy(mat.data(), old.mat, n_contacts * sizeof(float4), cudaMemcpyDeviceToHost);
+            cudaMemcpy(mgeo.data(), old.mgeo, n_contacts * sizeof(float4), cudaMemcpyDeviceToHost);
+            cudaMemcpy(mpts.data(), old.mpts, n_contacts * sizeof(float4), cudaMemcpyDeviceToHost);
+            cudaMemcpy(mimp.data(), old.mimp, n_contacts * sizeof(float4), cudaMemcpyDeviceToHost);
+            CUDA_OK(w, cudaMemcpy(mids.data(), old.mids, n_contacts * sizeof(uint4), cudaMemcpyDeviceToHost));
+        }
+        (void)old_cap;
+        const int old_key_bits = w->d.key_bits;
+        free_all(w);
+        int rc = allocate(w, nb, nf);
+        if (rc != B2G_OK) return rc;
+        if (n_contacts > 0) {
+            Contacts& c = w->d.c;
+            cudaMemcpy(c.key, key.data(), n_contacts * sizeof(uint64_t), cudaMemcpyHostToDevice);
+            cudaMemcpy(c.fix, fix.data(), n_contacts * sizeof(int2), cudaMemcpyHostToDevice);
+            cudaMemcpy(c.body, body.data(), n_contacts * sizeof(int2), cudaMemcpyHostToDevice);
+            cudaMemcpy(c.flags, flags.data(), n_contacts * sizeof(uint32_t), cudaMemcpyHostToDevice);
+            cudaMemcpy(c.mat, mat.data(), n_contacts * sizeof(float4), cudaMemcpyHostToDevice);
+            cudaMemcpy(c.mgeo, mgeo.data(), n_contacts * sizeof(float4), cudaMemcpyHostToDevice);
+            cudaMemcpy(c.mpts, mpts.data(), n_contacts * sizeof(float4), cudaMemcpyHostToDevice);
+            cudaMemcpy(c.mimp, mimp.data(), n_contacts * sizeof(float4), cudaMemcpyHostToDevice);
+            CUDA_OK(w, cudaMemcpy(c.mids, mids.data(), n_contacts * sizeof(uint4), cudaMemcpyHostToDevice));
+            CUDA_OK(w, cudaMemcpy(w->d.cnt + CNT_CONTACTS, &n_contacts, sizeof(int), cudaMemcpyHostToDevice));
+        }
+        w->d.key_bits = old_key_bits;
+    } else if (!w->allocated) {
+        int rc = allocate(w, nb, nf);
+        if (rc != B2G_OK) return rc;
+    }
+    /* contact keys are refid_min << key_bits | refid_max; widening key_bits keeps their order */
+    const int kb = bits_for((uint64_t)std::max(1, 2 * w->proxies_created));
+    if (kb != w->d.key_bits) {
+        if (w->d.key_bits != 0) {
+            /* re-key the current table: decode with the old width, encode with the new one */
+            int n_contacts = 0;
+            CUDA_OK(w, cudaMemcpy(&n_contacts, w->d.cnt + CNT_CONTACTS, sizeof(int), cudaMemcpyDeviceToHost));
+            if (n_contacts > 0) {
+                std::vector<unsigned long long> key(n_contacts);
+                CUDA_OK(w, cudaMemcpy(key.data(), w->d.c.key, n_contacts * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+                const uint64_t mask = (1ull << w->d.key_bits) - 1;
+                for (unsigned long long& k : key) k = ((k >> w->d.key_bits) << kb) | (k & mask);
+                CUDA_OK(w, cudaMemcpy(w->d.c.key, key.data(), n_contacts * sizeof(uint64_t), cudaMemcpyHostToDevice));
+            }
+        }
+        w->d.key_bits = kb;
+    }
+    w->d.morton_world_bits = w->num_worlds > 1 ? bits_for((uint64_t)(w->num_worlds - 1)) : 0;
+    return upload(w);
+}
+
+int check_status(World* w) {
+    if (!w->allocated) return B2G_OK;
+    int status = 0;
+    CUDA_OK(w, cudaStreamSynchronize(w->stream));
+    CUDA_OK(w, cudaMemcpy(&status, w->d.cnt + CNT_STATUS, sizeof(int), cudaMemcpyDeviceToHost));
+    if (status == 0) return B2G_OK;
+    const int zero = 0;
+    cudaMemcpy(w->d.cnt + CNT_STATUS, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    if (status & ST_BARRIER_TIMEOUT) {
+        /* the barrier counters may be left mid-count: reset them */
+        const int z2[2] = {0, 0};
+        cudaMemcpy(w->d.cnt + CNT_BARRIER, z2, sizeof(z2), cudaMemcpyHostToDevice);
+        return fail(w, B2G_ERR_TIMEOUT, "a grid barrier wait timed out; the step's results are void");
+    }
+    if (status & (ST_CONTACT_OVERFLOW | ST_PAIR_OVERFLOW | ST_STACK_OVERFLOW | ST_COLOUR_OVERFLOW))
+        return fail(w, B2G_ERR_CAPACITY,
+                    "a device capacity overflowed (contacts, pairs, traversal stack or colours); raise "
+                    "contact_capacity / pair_capacity in b2g_world_def");
+    if (status & ST_EVENT_OVERFLOW) return fail(w, B2G_ERR_CAPACITY, "contact event buffer overflowed");
+    if (status & ST_RECORD_OVERFLOW) return fail(w, B2G_ERR_CAPACITY, "recorded pair buffer overflowed");
+    return B2G_OK;
+}
+
+void swap_contacts(World* w) { std::swap(w->d.c, w->d.c_alt); }
+
+StepParams make_params(World* w, float dt, int vi, int pi) {
+    StepParams sp{};
+    sp.dt = dt;
+    sp.inv_dt = dt > 0.0f ? 1.0f / dt : 0.0f;
+    sp.dt_ratio = w->inv_dt0 * dt;
+    sp.gx = w->gravity.x;
+    sp.gy = w->gravity.y;
+    sp.vi = vi;
+    sp.pi = pi;
+    sp.warm = w->warm ? 1 : 0;
+    sp.allow_sleep = w->allow_sleep ? 1 : 0;
+    sp.auto_clear = w->auto_clear ? 1 : 0;
+    sp.record_events = w->record_events ? 1 : 0;
+    sp.record_pairs = w->record_pairs ? 1 : 0;
+    return sp;
+}
+
+/* B2world::step, src/private/dynamics/b2_world.rs:903-959 */
+int step(World* w, float dt, int vi, int pi) {
+    if (w->h_flags.empty()) return B2G_OK;
+    if (vi < 0 || pi < 0 || !(dt >= 0.0f)) return fail(w, B2G_ERR_INVALID_ARG, "dt must be >= 0 and iterations >= 0");
+    int rc = prepare(w);
+    if (rc != B2G_OK) return rc;
+    w->device_authoritative = true;
+    StepParams sp = make_params(w, dt, vi, pi);
+    cudaStream_t s = w->stream;
+    Timer& t = w->timer;
+    if (!t.valid) {
+        for (auto& e : t.e) cudaEventCreate(&e);
+        t.valid = true;
+    }
+    cudaMemsetAsync(w->d.cnt + CNT_EVENTS, 0, sizeof(int), s);
+    cudaEventRecord(t.e[0], s);
+    if (w->new_contacts) {
+        launch_broadphase(w->d, sp, s, w->num_sms);
+        swap_contacts(w);
+        w->new_contacts = false;
+    }
+    cudaEventRecord(t.e[1], s);
+    launch_collide(w->d, sp, s);
+    cudaEventRecord(t.e[2], s);
+    if (dt > 0.0f) {
+        launch_islands_and_constraints(w->d, sp, s);
+        launch_colouring(w->d, s, w->num_sms);
+        cudaEventRecord(t.e[3], s);
+        CUDA_OK(w, (cudaError_t)launch_solver(w->d, sp, s, w->num_sms));
+        cudaEventRecord(t.e[4], s);
+        launch_broadphase(w->d, sp, s, w->num_sms);
+        swap_contacts(w);
+        cudaEventRecord(t.e[5], s);
+        w->inv_dt0 = sp.inv_dt;
+    } else {
+        cudaEventRecord(t.e[3], s);
+        cudaEventRecord(t.e[4], s);
+        if (w->auto_clear) launch_clear_forces(w->d, s);
+        cudaEventRecord(t.e[5], s);
+    }
+    CUDA_OK(w, cudaGetLastError());
+    ++w->steps;
+    return B2G_OK;
+}
+
+World* W(void* p) { return (World*)p; }
+
+/* small body edits after the device became authoritative */
+__global__ void k_body_op(DevWorld d, int op, int b, float x, float y, float z, float px, float py, int wake) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    uint32_t fl = d.b_flags[b];
+    const int type = (int)(fl & BF_TYPE_MASK);
+    float4 v = d.b_vel[b];
+    if (op == 0) { /* set_linear_velocity, src/b2_body.rs:684-694 */
+        if (type == BODY_STATIC) return;
+        if (x * x + y * y > 0.0f && !(fl & BF_AWAKE)) { fl |= BF_AWAKE; v.w = 0.0f; }
+        v.x = x;
+        v.y = y;
+    } else if (op == 1) { /* set_angular_velocity, :696-705 */
+        if (type == BODY_STATIC) return;
+        if (z * z > 0.0f && !(fl & BF_AWAKE)) { fl |= BF_AWAKE; v.w = 0.0f; }
+        v.z = z;
+    } else if (op == 2 || op == 3) { /* apply_force / apply_linear_impulse, src/b2_body.rs:870-940 */
+        if (type != BODY_DYNAMIC) return;
+        if (wake && !(fl & BF_AWAKE)) { fl |= BF_AWAKE; v.w = 0.0f; }
+        if (!(fl & BF_AWAKE)) { d.b_flags[b] = fl; d.b_vel[b] = v; return; }
+        const float4 p = d.b_pos[b];
+        const float cr = (px - p.x) * y - (py - p.y) * x;
+        if (op == 2) {
+            float4 f = d.b_force[b];
+            f.x += x;
+            f.y += y;
+            f.z += cr;
+            d.b_force[b] = f;
+        } else {
+            const float4 m = d.b_mass[b];
+            v.x += m.y * x;
+            v.y += m.y * y;
+            v.z += m.w * cr;
+        }
+    }
+    d.b_flags[b] = fl;
+    d.b_vel[b] = v;
+}
+
+int body_op(World* w, int op, uint32_t b, float x, float y, float z, float px, float py, int wake) {
+    if (b >= w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body id out of range");
+    if (w->device_authoritative) {
+        int rc = prepare(w);
+        if (rc != B2G_OK) return rc;
+        k_body_op<<<1, 32, 0, w->stream>>>(w->d, op, (int)b, x, y, z, px, py, wake); B2G_LAUNCHED(1);
+        CUDA_OK(w, cudaGetLastError());
+        return B2G_OK;
+    }
+    uint32_t& fl = w->h_flags[b];
+    const int type = (int)(fl & BF_TYPE_MASK);
+    float4& v = w->h_vel[b];
+    if (op == 0) {
+        if (type == BODY_STATIC) return B2G_OK;
+        if (x * x + y * y > 0.0f && !(fl & BF_AWAKE)) { fl |= BF_AWAKE; v.w = 0.0f; }
+        v.x = x;
+        v.y = y;
+    } else if (op == 1) {
+        if (type == BODY_STATIC) return B2G_OK;
+        if (z * z > 0.0f && !(fl & BF_AWAKE)) { fl |= BF_AWAKE; v.w = 0.0f; }
+        v.z = z;
+    } else {
+        if (type != BODY_DYNAMIC) return B2G_OK;
+        if (wake && !(fl & BF_AWAKE)) { fl |= BF_AWAKE; v.w = 0.0f; }
+        if (!(fl & BF_AWAKE)) return B2G_OK;
+        const float4 p = w->h_pos[b];
+        const float cr = (px - p.x) * y - (py - p.y) * x;
+        if (op == 2) {
+            w->h_force[b].x += x;
+            w->h_force[b].y += y;
+            w->h_force[b].z += cr;
+        } else {
+            v.x += w->h_mass[b].y * x;
+            v.y += w->h_mass[b].y * y;
+            v.z += w->h_mass[b].w * cr;
+        }
+    }
+    return B2G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int b2g_version(void) { return kVersion; }
+
+int64_t b2g_get_launch_count(void) { return (int64_t)g_kernel_launches; }
+
+int b2g_world_create(const b2g_world_def* def, void** out) {
+    if (!def || !out) return B2G_ERR_INVALID_ARG;
+    if (def->num_worlds < 1) return B2G_ERR_INVALID_ARG;
+    World* w = new World();
+    w->device = def->device;
+    w->gravity = def->gravity;
+    w->num_worlds = def->num_worlds;
+    w->user_contact_cap = def->contact_capacity;
+    w->user_pair_cap = def->pair_capacity;
+    if (cudaSetDevice(w->device) != cudaSuccess) {
+        delete w;
+        return B2G_ERR_CUDA;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, w->device) != cudaSuccess || cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete w;
+        return B2G_ERR_CUDA;
+    }
+    w->num_sms = prop.multiProcessorCount;
+    if (!prop.cooperativeLaunch) {
+        cudaStreamDestroy(w->stream);
+        delete w;
+        return B2G_ERR_UNSUPPORTED;
+    }
+    *out = w;
+    return B2G_OK;
+}
+
+int b2g_world_destroy(void* p) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    cudaStreamSynchronize(w->stream);
+    free_all(w);
+    if (w->timer.valid)
+        for (auto& e : w->timer.e) cudaEventDestroy(e);
+    cudaStreamDestroy(w->stream);
+    delete w;
+    return B2G_OK;
+}
+
+const char* b2g_last_error(const void* p) { return p ? W((void*)p)->err.c_str() : "null world"; }
+
+/* B2world::create_body -> b2_body (private/dynamics/b2_body.rs:15-78) */
+int b2g_create_bodies(void* p, const b2g_body_def* defs, int32_t n, uint32_t* ids) {
+    World* w = W(p);
+    if (!w || (!defs && n > 0) || n < 0) return B2G_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i) {
+        const b2g_body_def& d = defs[i];
+        if (d.type < 0 || d.type > 2) return fail(w, B2G_ERR_INVALID_ARG, "body type must be 0, 1 or 2");
+        if ((int)d.world_index >= w->num_worlds) return fail(w, B2G_ERR_INVALID_ARG, "world_index >= num_worlds");
+        if (!(d.linear_damping >= 0.0f) || !(d.angular_damping >= 0.0f))
+            return fail(w, B2G_ERR_INVALID_ARG, "damping must be >= 0");
+    }
+    if (w->device_authoritative) {
+        int rc = download_state(w);
+        if (rc != B2G_OK) return rc;
+    }
+    for (int i = 0; i < n; ++i) {
+        const b2g_body_def& d = defs[i];
+        uint32_t fl = (uint32_t)d.type;
+        if (d.awake && d.type != B2G_STATIC_BODY) fl |= BF_AWAKE;
+        if (d.enabled) fl |= BF_ENABLED;
+        if (d.allow_sleep) fl |= BF_AUTO_SLEEP;
+        if (d.fixed_rotation) fl |= BF_FIXED_ROTATION;
+        if (d.bullet) fl |= BF_BULLET;
+        const Rot q = rot(d.angle);
+        const int id = (int)w->h_flags.size();
+        w->h_flags.push_back(fl);
+        w->h_world.push_back(d.world_index);
+        w->h_xf.push_back(make_float4(d.position.x, d.position.y, q.s, q.c));
+        w->h_pos.push_back(make_float4(d.position.x, d.position.y, d.angle, 0.0f));
+        w->h_pos0.push_back(make_float4(d.position.x, d.position.y, d.angle, 0.0f));
+        w->h_vel.push_back(make_float4(d.linear_velocity.x, d.linear_velocity.y, d.angular_velocity, 0.0f));
+        w->h_force.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        w->h_mass.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        w->h_damp.push_back(make_float4(d.linear_damping, d.angular_damping, d.gravity_scale, 0.0f));
+        w->h_lc.push_back(make_float2(0.0f, 0.0f));
+        w->body_fixtures.emplace_back();
+        if (ids) ids[i] = (uint32_t)id;
+    }
+    return B2G_OK;
+}
+
+/* B2body::create_fixture (private/dynamics/b2_body.rs:155-200) + create_proxies (b2_fixture.rs:114-133) */
+int b2g_create_fixtures(void* p, const b2g_fixture_def* defs, int32_t n, uint32_t* ids) {
+    World* w = W(p);
+    if (!w || (!defs && n > 0) || n < 0) return B2G_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i) {
+        const b2g_fixture_def& d = defs[i];
+        if (d.body >= w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "fixture body id out of range");
+        if (d.shape_type < 0 || d.shape_type > 2)
+            return fail(w, B2G_ERR_UNSUPPORTED, "shape type must be circle, edge or polygon (chain shapes are not supported)");
+        if (!(d.density >= 0.0f) || !(d.friction >= 0.0f) || !(d.restitution >= 0.0f))
+            return fail(w, B2G_ERR_INVALID_ARG, "density, friction and restitution must be >= 0");
+    }
+    if (w->device_authoritative) {
+        int rc = download_state(w);
+        if (rc != B2G_OK) return rc;
+    }
+    for (int i = 0; i < n; ++i) {
+        const b2g_fixture_def& d = defs[i];
+        const int b = (int)d.body;
+        const int f = (int)w->h_fbody.size();
+        ShapeRec s;
+        build_shape(d, s);
+        w->h_shape.push_back(s);
+        w->h_fbody.push_back(b);
+        w->h_fmat.push_back(make_float4(d.friction, d.restitution, d.restitution_threshold, d.density));
+        w->h_filter.push_back((uint32_t)d.category_bits | ((uint32_t)d.mask_bits << 16));
+        w->h_group.push_back((uint32_t)(uint16_t)d.group_index | (d.is_sensor ? 0x10000u : 0u));
+        if (w->h_flags[b] & BF_ENABLED) {
+            AABB a;
+            shape_aabb(s, host_xf(w, b), a);
+            const V2 r = mk(kAabbExtension, kAabbExtension);
+            const V2 lo = sub(a.lo, r), hi = add(a.hi, r);
+            w->h_fat.push_back(make_float4(lo.x, lo.y, hi.x, hi.y));
+            w->h_moved.push_back(1);
+            w->h_refid.push_back(w->proxies_created == 0 ? 0u : (uint32_t)(2 * w->proxies_created - 1));
+            ++w->proxies_created;
+        } else {
+            const float inf = INFINITY;
+            w->h_fat.push_back(make_float4(inf, inf, -inf, -inf));
+            w->h_moved.push_back(0);
+            w->h_refid.push_back(0xffffffffu);
+        }
+        w->body_fixtures[b].insert(w->body_fixtures[b].begin(), f);
+        if (d.density > 0.0f) reset_mass_data(w, b);
+        w->new_contacts = true;
+        if (ids) ids[i] = (uint32_t)f;
+    }
+    return B2G_OK;
+}
+
+int b2g_step(void* p, float dt, int32_t vi, int32_t pi) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    if (w->continuous)
+        return fail(w, B2G_ERR_UNSUPPORTED, "continuous physics (time of impact) is not on the GPU path; call b2g_set_continuous_physics(world, 0)");
+    return step(w, dt, vi, pi);
+}
+
+int b2g_synchronize(void* p) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    return check_status(w);
+}
+
+int b2g_get_body_states(void* p, uint32_t first, uint32_t count, b2g_body_state* out) {
+    World* w = W(p);
+    if (!w || (!out && count > 0)) return B2G_ERR_INVALID_ARG;
+    if ((size_t)first + count > w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body range out of bounds");
+    std::vector<float4> xf(count), pos(count), vel(count);
+    if (w->device_authoritative && (int)(first + count) <= w->uploaded_bodies) {
+        int rc = check_status(w);
+        if (rc != B2G_OK) return rc;
+        CUDA_OK(w, cudaMemcpy(xf.data(), w->d.b_xf + first, count * sizeof(float4), cudaMemcpyDeviceToHost));
+        CUDA_OK(w, cudaMemcpy(pos.data(), w->d.b_pos + first, count * sizeof(float4), cudaMemcpyDeviceToHost));
+        CUDA_OK(w, cudaMemcpy(vel.data(), w->d.b_vel + first, count * sizeof(float4), cudaMemcpyDeviceToHost));
+    } else {
+        if (w->device_authoritative) {
+            int rc = download_state(w);
+            if (rc != B2G_OK) return rc;
+        }
+        for (uint32_t i = 0; i < count; ++i) {
+            xf[i] = w->h_xf[first + i];
+            pos[i] = w->h_pos[first + i];
+            vel[i] = w->h_vel[first + i];
+        }
+    }
+    for (uint32_t i = 0; i < count; ++i) {
+        b2g_body_state& s = out[i];
+        s.position = b2g_vec2{xf[i].x, xf[i].y};
+        s.angle = pos[i].z;
+        s.linear_velocity = b2g_vec2{vel[i].x, vel[i].y};
+        s.angular_velocity = vel[i].z;
+        s.world_center = b2g_vec2{pos[i].x, pos[i].y};
+    }
+    return B2G_OK;
+}
+
+/* B2body::set_transform, private/dynamics/b2_body.rs:418-447 */
+int b2g_set_transform(void* p, uint32_t b, b2g_vec2 position, float angle) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    if (b >= w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body id out of range");
+    if (w->device_authoritative) {
+        int rc = prepare(w);
+        if (rc != B2G_OK) return rc;
+        launch_set_transform(w->d, (int)b, position.x, position.y, angle, w->stream);
+        CUDA_OK(w, cudaGetLastError());
+    } else {
+        const Rot q = rot(angle);
+        w->h_xf[b] = make_float4(position.x, position.y, q.s, q.c);
+        const Xf xf = host_xf(w, (int)b);
+        const V2 c = mul(xf, mk(w->h_lc[b].x, w->h_lc[b].y));
+        w->h_pos[b] = make_float4(c.x, c.y, angle, 0.0f);
+        w->h_pos0[b] = make_float4(c.x, c.y, angle, 0.0f);
+        for (int f : w->body_fixtures[b]) {
+            if (w->h_refid[f] == 0xffffffffu) continue;
+            AABB a1, a2;
+            shape_aabb(w->h_shape[f], xf, a1);
+            shape_aabb(w->h_shape[f], xf, a2);
+            const AABB swept = combine(a1, a2);
+            host_move_proxy(w, f, swept, sub(center(a2), center(a1)));
+        }
+    }
+    w->new_contacts = true;
+    return B2G_OK;
+}
+
+int b2g_set_linear_velocity(void* p, uint32_t b, b2g_vec2 v) {
+    return p ? body_op(W(p), 0, b, v.x, v.y, 0.0f, 0.0f, 0.0f, 0) : B2G_ERR_INVALID_ARG;
+}
+int b2g_set_angular_velocity(void* p, uint32_t b, float av) {
+    return p ? body_op(W(p), 1, b, 0.0f, 0.0f, av, 0.0f, 0.0f, 0) : B2G_ERR_INVALID_ARG;
+}
+int b2g_apply_force(void* p, uint32_t b, b2g_vec2 force, b2g_vec2 point, int32_t wake) {
+    return p ? body_op(W(p), 2, b, force.x, force.y, 0.0f, point.x, point.y, wake) : B2G_ERR_INVALID_ARG;
+}
+int b2g_apply_linear_impulse(void* p, uint32_t b, b2g_vec2 impulse, b2g_vec2 point, int32_t wake) {
+    return p ? body_op(W(p), 3, b, impulse.x, impulse.y, 0.0f, point.x, point.y, wake) : B2G_ERR_INVALID_ARG;
+}
+
+int b2g_set_gravity(void* p, b2g_vec2 g) {
+    if (!p) return B2G_ERR_INVALID_ARG;
+    W(p)->gravity = g;
+    return B2G_OK;
+}
+int b2g_set_allow_sleeping(void* p, int32_t flag) {
+    if (!p) return B2G_ERR_INVALID_ARG;
+    W(p)->allow_sleep = flag != 0;
+    return B2G_OK;
+}
+int b2g_set_warm_starting(void* p, int32_t flag) {
+    if (!p) return B2G_ERR_INVALID_ARG;
+    W(p)->warm = flag != 0;
+    return B2G_OK;
+}
+int b2g_set_continuous_physics(void* p, int32_t flag) {
+    if (!p) return B2G_ERR_INVALID_ARG;
+    W(p)->continuous = flag != 0;
+    return B2G_OK;
+}
+int b2g_set_auto_clear_forces(void* p, int32_t flag) {
+    if (!p) return B2G_ERR_INVALID_ARG;
+    W(p)->auto_clear = flag != 0;
+    return B2G_OK;
+}
+int b2g_clear_forces(void* p) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    if (w->device_authoritative) {
+        launch_clear_forces(w->d, w->stream);
+    } else {
+        for (auto& f : w->h_force) f = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    return B2G_OK;
+}
+
+int b2g_set_contact_events(void* p, int32_t flag) {
+    if (!p) return B2G_ERR_INVALID_ARG;
+    W(p)->record_events = flag != 0;
+    return B2G_OK;
+}
+int b2g_set_record_pairs(void* p, int32_t flag) {
+    if (!p) return B2G_ERR_INVALID_ARG;
+    W(p)->record_pairs = flag != 0;
+    return B2G_OK;
+}
+
+int b2g_get_profile(void* p, b2g_profile* out) {
+    World* w = W(p);
+    if (!w || !out) return B2G_ERR_INVALID_ARG;
+    int rc = check_status(w);
+    if (rc != B2G_OK) return rc;
+    memset(out, 0, sizeof(*out));
+    if (!w->timer.valid || w->steps == 0) return B2G_OK;
+    float ms[6] = {0};
+    for (int i = 1; i < 6; ++i) cudaEventElapsedTime(&ms[i], w->timer.e[0], w->timer.e[i]);
+    out->collide = ms[2] - ms[1];
+    out->solve_init = ms[3] - ms[2];
+    out->solve_velocity = ms[4] - ms[3];  /* the persistent solver kernel: velocity and position iterations */
+    out->solve_position = 0.0f;
+    out->broadphase = (ms[5] - ms[4]) + ms[1];
+    out->solve = ms[5] - ms[2];
+    out->step = ms[5];
+    out->solve_toi = 0.0f;
+    return B2G_OK;
+}
+
+int b2g_get_counts(void* p, b2g_counts* out) {
+    World* w = W(p);
+    if (!w || !out) return B2G_ERR_INVALID_ARG;
+    memset(out, 0, sizeof(*out));
+    out->bodies = (int)w->h_flags.size();
+    out->fixtures = (int)w->h_fbody.size();
+    out->proxies = w->proxies_created;
+    if (!w->allocated) return B2G_OK;
+    int rc = check_status(w);
+    if (rc != B2G_OK) return rc;
+    int cnt[CNT_SIZE];
+    CUDA_OK(w, cudaMemcpy(cnt, w->d.cnt, sizeof(cnt), cudaMemcpyDeviceToHost));
+    out->contacts = cnt[CNT_CONTACTS];
+    out->islands_solved = 0;
+    out->colours = cnt[CNT_COLOURS];
+    out->pairs = cnt[CNT_PAIRS];
+    if (cnt[CNT_CONTACTS] > 0) {
+        std::vector<uint32_t> fl(cnt[CNT_CONTACTS]);
+        CUDA_OK(w, cudaMemcpy(fl.data(), w->d.c.flags, fl.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        int t = 0;
+        for (uint32_t f : fl) t += (f & CF_TOUCHING) && !(f & CF_DEAD) ? 1 : 0;
+        out->touching_contacts = t;
+    }
+    out->islands_solved = cnt[CNT_CONS];
+    return B2G_OK;
+}
+
+int b2g_get_contacts(void* p, b2g_contact_info* out, int32_t cap, int32_t* n) {
+    World* w = W(p);
+    if (!w || !n) return B2G_ERR_INVALID_ARG;
+    *n = 0;
+    if (!w->allocated) return B2G_OK;
+    int rc = check_status(w);
+    if (rc != B2G_OK) return rc;
+    int nc = 0;
+    CUDA_OK(w, cudaMemcpy(&nc, w->d.cnt + CNT_CONTACTS, sizeof(int), cudaMemcpyDeviceToHost));
+    *n = nc;
+    if (!out || cap < nc || nc == 0) return B2G_OK;
+    const Contacts& c = w->d.c;
+    std::vector<int2> fix(nc);
+    std::vector<uint32_t> flags(nc);
+    std::vector<float4> mat(nc), mgeo(nc), mpts(nc), mimp(nc);
+    std::vector<uint4> mids(nc);
+    cudaMemcpy(fix.data(), c.fix, nc * sizeof(int2), cudaMemcpyDeviceToHost);
+    cudaMemcpy(flags.data(), c.flags, nc * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaMemcpy(mat.data(), c.mat, nc * sizeof(float4), cudaMemcpyDeviceToHost);
+    cudaMemcpy(mgeo.data(), c.mgeo, nc * sizeof(float4), cudaMemcpyDeviceToHost);
+    cudaMemcpy(mpts.data(), c.mpts, nc * sizeof(float4), cudaMemcpyDeviceToHost);
+    cudaMemcpy(mimp.data(), c.mimp, nc * sizeof(float4), cudaMemcpyDeviceToHost);
+    CUDA_OK(w, cudaMemcpy(mids.data(), c.mids, nc * sizeof(uint4), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < nc; ++i) {
+        b2g_contact_info& o = out[i];
+        memset(&o, 0, sizeof(o));
+        o.fixture_a = (uint32_t)fix[i].x;
+        o.fixture_b = (uint32_t)fix[i].y;
+        o.touching = (flags[i] & CF_TOUCHING) ? 1 : 0;
+        o.manifold_type = (int)(mids[i].z & 0xffu);
+        o.point_count = (int)((mids[i].z >> 8) & 0xffu);
+        o.local_normal = b2g_vec2{mgeo[i].x, mgeo[i].y};
+        o.local_point = b2g_vec2{mgeo[i].z, mgeo[i].w};
+        o.point_local[0] = b2g_vec2{mpts[i].x, mpts[i].y};
+        o.point_local[1] = b2g_vec2{mpts[i].z, mpts[i].w};
+        o.normal_impulse[0] = mimp[i].x;
+        o.tangent_impulse[0] = mimp[i].y;
+        o.normal_impulse[1] = mimp[i].z;
+        o.tangent_impulse[1] = mimp[i].w;
+        o.point_id[0] = mids[i].x;
+        o.point_id[1] = mids[i].y;
+        o.friction = mat[i].x;
+        o.restitution = mat[i].y;
+        o.restitution_threshold = mat[i].z;
+    }
+    return B2G_OK;
+}
+
+int b2g_get_events(void* p, b2g_contact_event* out, int32_t cap, int32_t* n) {
+    World* w = W(p);
+    if (!w || !n) return B2G_ERR_INVALID_ARG;
+    *n = 0;
+    if (!w->allocated) return B2G_OK;
+    int rc = check_status(w);
+    if (rc != B2G_OK) return rc;
+    int ne = 0;
+    CUDA_OK(w, cudaMemcpy(&ne, w->d.cnt + CNT_EVENTS, sizeof(int), cudaMemcpyDeviceToHost));
+    ne = std::min(ne, w->d.event_cap);
+    *n = ne;
+    if (!out || cap < ne || ne == 0) return B2G_OK;
+    std::vector<int4> ev(ne);
+    CUDA_OK(w, cudaMemcpy(ev.data(), w->d.events, ne * sizeof(int4), cudaMemcpyDeviceToHost));
+    std::sort(ev.begin(), ev.end(), [](const int4& a, const int4& b) {
+        if (a.x != b.x) return a.x < b.x;
+        if (a.y != b.y) return a.y < b.y;
+        return a.z < b.z;
+    });
+    for (int i = 0; i < ne; ++i) out[i] = b2g_contact_event{ev[i].x, (uint32_t)ev[i].y, (uint32_t)ev[i].z};
+    return B2G_OK;
+}
+
+int b2g_get_pairs(void* p, uint32_t* out, int32_t cap, int32_t* n) {
+    World* w = W(p);
+    if (!w || !n) return B2G_ERR_INVALID_ARG;
+    *n = 0;
+    if (!w->allocated) return B2G_OK;
+    int rc = check_status(w);
+    if (rc != B2G_OK) return rc;
+    int np = 0;
+    CUDA_OK(w, cudaMemcpy(&np, w->d.cnt + CNT_PAIRS, sizeof(int), cudaMemcpyDeviceToHost));
+    np = std::min(np, w->d.pair_cap);
+    *n = np;
+    if (!out || cap < np || np == 0) return B2G_OK;
+    std::vector<uint2> pr(np);
+    CUDA_OK(w, cudaMemcpy(pr.data(), w->d.pairs, np * sizeof(uint2), cudaMemcpyDeviceToHost));
+    std::sort(pr.begin(), pr.end(), [](const uint2& a, const uint2& b) { return a.x != b.x ? a.x < b.x : a.y < b.y; });
+    for (int i = 0; i < np; ++i) {
+        out[2 * i] = pr[i].x;
+        out[2 * i + 1] = pr[i].y;
+    }
+    return B2G_OK;
+}
+
+int b2g_get_proxies(void* p, float* aabbs, uint8_t* moved, int32_t cap) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    const int nf = std::min((int)w->h_fbody.size(), (int)cap);
+    if (w->device_authoritative) {
+        int rc = check_status(w);
+        if (rc != B2G_OK) return rc;
+        if (aabbs) CUDA_OK(w, cudaMemcpy(aabbs, w->d.f_fat, nf * sizeof(float4), cudaMemcpyDeviceToHost));
+        if (moved) CUDA_OK(w, cudaMemcpy(moved, w->d.f_moved, nf, cudaMemcpyDeviceToHost));
+    } else {
+        if (aabbs) memcpy(aabbs, w->h_fat.data(), nf * sizeof(float4));
+        if (moved) memcpy(moved, w->h_moved.data(), nf);
+    }
+    return B2G_OK;
+}
+
+int b2g_collide_pairs(const b2g_fixture_def* da, const float* xfa, const b2g_fixture_def* db, const float* xfb,
+                      int32_t n, b2g_contact_info* out) {
+    if (n < 0 || (n > 0 && (!da || !db || !xfa || !xfb || !out))) return B2G_ERR_INVALID_ARG;
+    if (n == 0) return B2G_OK;
+    std::vector<ShapeRec> sa(n), sb(n);
+    std::vector<float4> xa(n), xb(n);
+    std::vector<int> kind(n);
+    for (int i = 0; i < n; ++i) {
+        build_shape(da[i], sa[i]);
+        build_shape(db[i], sb[i]);
+        const int ta = da[i].shape_type, tb = db[i].shape_type;
+        if (ta == B2G_SHAPE_CIRCLE && tb == B2G_SHAPE_CIRCLE) kind[i] = KIND_CIRCLES;
+        else if (ta == B2G_SHAPE_POLYGON && tb == B2G_SHAPE_CIRCLE) kind[i] = KIND_POLYGON_CIRCLE;
+        else if (ta == B2G_SHAPE_POLYGON && tb == B2G_SHAPE_POLYGON) kind[i] = KIND_POLYGONS;
+        else if (ta == B2G_SHAPE_EDGE && tb == B2G_SHAPE_CIRCLE) kind[i] = KIND_EDGE_CIRCLE;
+        else if (ta == B2G_SHAPE_EDGE && tb == B2G_SHAPE_POLYGON) kind[i] = KIND_EDGE_POLYGON;
+        else return B2G_ERR_INVALID_ARG;
+        const Rot qa = rot(xfa[3 * i + 2]), qb = rot(xfb[3 * i + 2]);
+        xa[i] = make_float4(xfa[3 * i], xfa[3 * i + 1], qa.s, qa.c);
+        xb[i] = make_float4(xfb[3 * i], xfb[3 * i + 1], qb.s, qb.c);
+    }
+    ShapeRec *d_sa = nullptr, *d_sb = nullptr;
+    float4 *d_xa = nullptr, *d_xb = nullptr, *d_geo = nullptr, *d_pts = nullptr;
+    uint4* d_ids = nullptr;
+    int* d_kind = nullptr;
+    int rc = B2G_OK;
+    if (cudaMalloc(&d_sa, n * sizeof(ShapeRec)) != cudaSuccess || cudaMalloc(&d_sb, n * sizeof(ShapeRec)) != cudaSuccess ||
+        cudaMalloc(&d_xa, n * sizeof(float4)) != cudaSuccess || cudaMalloc(&d_xb, n * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&d_geo, n * sizeof(float4)) != cudaSuccess || cudaMalloc(&d_pts, n * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&d_ids, n * sizeof(uint4)) != cudaSuccess || cudaMalloc(&d_kind, n * sizeof(int)) != cudaSuccess) {
+        rc = B2G_ERR_OUT_OF_MEMORY;
+    }
+    std::vector<float4> geo(n), pts(n);
+    std::vector<uint4> ids(n);
+    if (rc == B2G_OK) {
+        cudaMemcpy(d_sa, sa.data(), n * sizeof(ShapeRec), cudaMemcpyHostToDevice);
+        cudaMemcpy(d_sb, sb.data(), n * sizeof(ShapeRec), cudaMemcpyHostToDevice);
+        cudaMemcpy(d_xa, xa.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
+        cudaMemcpy(d_xb, xb.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
+        cudaMemcpy(d_kind, kind.data(), n * sizeof(int), cudaMemcpyHostToDevice);
+        launch_collide_pairs(d_sa, d_xa, d_sb, d_xb, d_kind, n, d_geo, d_pts, d_ids, 0);
+        if (cudaMemcpy(geo.data(), d_geo, n * sizeof(float4), cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(pts.data(), d_pts, n * sizeof(float4), cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(ids.data(), d_ids, n * sizeof(uint4), cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = B2G_ERR_CUDA;
+    }
+    cudaFree(d_sa);
+    cudaFree(d_sb);
+    cudaFree(d_xa);
+    cudaFree(d_xb);
+    cudaFree(d_geo);
+    cudaFree(d_pts);
+    cudaFree(d_ids);
+    cudaFree(d_kind);
+    if (rc != B2G_OK) return rc;
+    for (int i = 0; i < n; ++i) {
+        b2g_contact_info& o = out[i];
+        memset(&o, 0, sizeof(o));
+        o.fixture_a = o.fixture_b = (uint32_t)i;
+        o.manifold_type = (int)(ids[i].z & 0xffu);
+        o.point_count = (int)((ids[i].z >> 8) & 0xffu);
+        o.touching = o.point_count > 0;
+        o.local_normal = b2g_vec2{geo[i].x, geo[i].y};
+        o.local_point = b2g_vec2{geo[i].z, geo[i].w};
+        o.point_local[0] = b2g_vec2{pts[i].x, pts[i].y};
+        o.point_local[1] = b2g_vec2{pts[i].z, pts[i].w};
+        o.point_id[0] = ids[i].x;
+        o.point_id[1] = ids[i].y;
+    }
+    return B2G_OK;
+}
+
+int b2g_get_solver_order(void* p, uint32_t* out, int32_t cap, int32_t* n) {
+    World* w = W(p);
+    if (!w || !n) return B2G_ERR_INVALID_ARG;
+    *n = 0;
+    if (!w->allocated) return B2G_OK;
+    int rc = check_status(w);
+    if (rc != B2G_OK) return rc;
+    int nc = 0;
+    CUDA_OK(w, cudaMemcpy(&nc, w->d.cnt + CNT_CONS, sizeof(int), cudaMemcpyDeviceToHost));
+    *n = nc;
+    if (!out || cap < nc || nc == 0) return B2G_OK;
+    CUDA_OK(w, cudaMemcpy(out, w->d.s_fix, nc * sizeof(int2), cudaMemcpyDeviceToHost));
+    return B2G_OK;
+}
+
+}  // extern "C"
+

@@ -1,0 +1,206 @@
+/*
+ * b2g_internal.h — device data layout of a GPU world (or batch of worlds) and the
+ * launchers each kernel file exports to the host-side world (api.cu).
+ *
+ * Layout (all arrays in HBM, structure-of-arrays, 16-byte vectors where a kernel
+ * reads several fields of one object together):
+ *   bodies    b_xf(p.x,p.y,sin,cos) b_pos(c.x,c.y,a,-) b_pos0(c0.x,c0.y,a0,-)
+ *             b_vel(v.x,v.y,w,sleep_time) b_force(f.x,f.y,torque,-) b_mass(m,1/m,I,1/I)
+ *             b_damp(lin,ang,gravity_scale,-) b_lc(local centre) b_flags b_world b_island
+ *   fixtures  f_shape (144-byte ShapeRec) f_body f_mat(friction,restitution,threshold,density)
+ *             f_filter(category|mask<<16, group|sensor<<16) f_refid (the reference's proxy id)
+ *             f_fat (fat AABB lo.x,lo.y,hi.x,hi.y) f_moved
+ *   contacts  sorted by key = refid_min << 32 | refid_max (double-buffered, merged each step)
+ *   solver    per constraint slot, slots grouped by colour: vc_* (velocity), pc_* (position)
+ *   LBVH      sorted leaf keys/ids, internal nodes holding both child boxes
+ */
+#ifndef B2G_INTERNAL_H
+#define B2G_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "b2g_collide.cuh"
+
+namespace b2g {
+
+/* body flag bits (BodyFlags, src/b2_body.rs:212-229, plus the body type) */
+enum : uint32_t {
+    BF_TYPE_MASK = 3u,
+    BF_AWAKE = 1u << 2,
+    BF_ENABLED = 1u << 3,
+    BF_AUTO_SLEEP = 1u << 4,
+    BF_FIXED_ROTATION = 1u << 5,
+    BF_BULLET = 1u << 6,
+    BF_ISLAND = 1u << 7,   /* member of an island solved this step */
+};
+enum { BODY_STATIC = 0, BODY_KINEMATIC = 1, BODY_DYNAMIC = 2 };
+
+/* contact flag bits (ContactFlags, src/b2_contact.rs:283-305) */
+enum : uint32_t {
+    CF_TOUCHING = 1u << 0,
+    CF_ENABLED = 1u << 1,
+    CF_DEAD = 1u << 2,
+    CF_SENSOR = 1u << 3,
+    CF_KIND_SHIFT = 8,
+};
+
+/* device status bits (sticky until read by the host) */
+enum : uint32_t {
+    ST_CONTACT_OVERFLOW = 1u << 0,
+    ST_PAIR_OVERFLOW = 1u << 1,
+    ST_EVENT_OVERFLOW = 1u << 2,
+    ST_COLOUR_OVERFLOW = 1u << 3,
+    ST_BARRIER_TIMEOUT = 1u << 4,
+    ST_STACK_OVERFLOW = 1u << 5,
+    ST_RECORD_OVERFLOW = 1u << 6,
+};
+
+/* device counters (d_cnt[]) */
+enum {
+    CNT_CONTACTS = 0,     /* contacts in the current table */
+    CNT_CONS = 1,         /* island constraints this step */
+    CNT_COLOURS = 2,      /* non-empty colours */
+    CNT_NEW = 3,          /* new contacts found by the broadphase */
+    CNT_EVENTS = 4,
+    CNT_PAIRS = 5,        /* recorded emitted pairs (parity hook) */
+    CNT_STATUS = 6,
+    CNT_ALIVE = 7,        /* surviving old contacts during a merge */
+    CNT_UNCOLOURED = 8,   /* 2 ints, alternating by colouring round */
+    CNT_ROUNDS = 10,
+    CNT_TOUCHING = 11,
+    CNT_BOUNDS = 12,      /* 4 ints: ordered-int min.x, min.y, max.x, max.y of proxy centres */
+    CNT_BARRIER = 16,     /* 2 uints: grid barrier count / generation */
+    CNT_ISLANDS = 18,
+    CNT_SIZE = 32
+};
+
+constexpr int kMaxColours = 256;   /* first-fit colours 0..63, then one per colouring round */
+constexpr int kFirstFitColours = 64;
+constexpr int kMaxPosIters = 64;
+
+struct Contacts {
+    unsigned long long* key;
+    int2* fix;        /* fixture A, fixture B (A = primary shape type) */
+    int2* body;
+    uint32_t* flags;
+    float4* mat;      /* friction, restitution, restitution threshold, tangent speed */
+    float4* mgeo;     /* local normal, local point */
+    float4* mpts;     /* point 0 local, point 1 local */
+    float4* mimp;     /* normal 0, tangent 0, normal 1, tangent 1 impulses */
+    uint4* mids;      /* id 0, id 1, type | count << 8, - */
+};
+
+struct StepParams {
+    float dt, inv_dt, dt_ratio;
+    float gx, gy;
+    int vi, pi;
+    int warm;
+    int allow_sleep;
+    int auto_clear;
+    int record_events;
+    int record_pairs;
+};
+
+struct DevWorld {
+    int body_cap, fix_cap, contact_cap, pair_cap, event_cap, cons_cap;
+    int n_bodies, n_fixtures, num_worlds;
+    int key_bits;      /* bits of the contact key (2 x refid bits) */
+    int morton_world_bits;
+    /* bodies */
+    float4 *b_xf, *b_pos, *b_pos0, *b_vel, *b_force, *b_mass, *b_damp;
+    float2* b_lc;
+    uint32_t* b_flags;
+    uint32_t* b_world;
+    int* b_island;
+    unsigned long long* b_cmin;  /* colouring: minimum priority of uncoloured constraints */
+    unsigned long long* b_cmask; /* colouring: colours used at this body */
+    uint32_t* isl_minsep;        /* 2 x body_cap: per-island max(-separation) bits, double-buffered */
+    uint8_t* isl_done;
+    float* isl_sleep;            /* per island root: min sleep time (as ordered uint bits) */
+    /* fixtures */
+    ShapeRec* f_shape;
+    int* f_body;
+    float4* f_mat;
+    uint32_t* f_filter;          /* category | mask << 16 */
+    uint32_t* f_group;           /* (uint16) group | sensor << 16 */
+    uint32_t* f_refid;
+    float4* f_fat;
+    uint8_t* f_moved;
+    /* contacts: current table and the merge target */
+    Contacts c, c_alt;
+    int* c_rank;                 /* exclusive scan of alive flags during a merge */
+    /* new contacts from the broadphase */
+    unsigned long long* n_key;   /* keys; sorted in place */
+    int2* n_fix;                 /* fixture pair per new key (before sorting) */
+    uint32_t* n_idx;             /* sort payload */
+    unsigned long long* n_key_alt;
+    uint32_t* n_idx_alt;
+    /* constraints */
+    int* cons_contact;           /* unsorted: contact index per constraint */
+    int* cons_colour;
+    int* cons_island;
+    int* s_contact;              /* slot -> contact (sorted by colour) */
+    int* s_cons;                 /* slot -> constraint */
+    int2* s_fix;                 /* slot -> (fixture A, fixture B): the solve order exported to the host */
+    int* col_off;                /* kMaxColours + 1 offsets of non-empty colours */
+    int* col_hist;               /* kMaxColours counts */
+    int4* vc_idx;                /* ia, ib, point count, flags (bit0 A dynamic, bit1 B dynamic) */
+    float4 *vc_inv, *vc_nf, *vc_r0, *vc_r1, *vc_m0, *vc_m1, *vc_imp, *vc_k;
+    float4 *pc_lp, *pc_geo, *pc_lc, *pc_inv, *pc_meta;
+    int* vc_island;
+    /* broadphase */
+    unsigned long long* bp_key;
+    uint32_t* bp_val;
+    unsigned long long* bp_key_alt;
+    uint32_t* bp_val_alt;
+    float4* bp_leaf;             /* leaf fat AABB in sorted order */
+    float4* bp_node_b0;          /* internal node: child 0 box */
+    float4* bp_node_b1;          /* internal node: child 1 box */
+    int2* bp_node_child;         /* child indices; leaves encoded as ~leaf */
+    int* bp_parent;              /* parent of internal nodes [0,n-1) and leaves [n-1, 2n-1) */
+    uint32_t* bp_flag;           /* refit arrival counters */
+    int* bp_world_root;          /* per world: root node (encoded like children), or INT_MIN if empty */
+    int* bp_world_first;         /* per world: first sorted leaf */
+    /* outputs for the host */
+    int4* events;                /* kind, fixture a, fixture b, - */
+    uint2* pairs;                /* recorded emitted pairs (fixture ids) */
+    /* scratch for the primitives */
+    uint32_t* scan_tmp;
+    uint32_t* sort_hist;
+    int sort_hist_cap;
+    int* cnt;
+};
+
+/* kernel-file launchers */
+void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s);
+void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cudaStream_t s);
+void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms);
+int launch_solver(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms);
+void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms);
+void launch_set_transform(const DevWorld& w, int body, float px, float py, float angle, cudaStream_t s);
+void launch_clear_forces(const DevWorld& w, cudaStream_t s);
+void launch_collide_pairs(const ShapeRec* a, const float4* xa, const ShapeRec* b, const float4* xb, const int* kind,
+                          int n, float4* geo, float4* pts, uint4* ids, cudaStream_t s);
+
+/* primitives (k_prims.cu) */
+void scan_exclusive_u32(const uint32_t* in, uint32_t* out, const int* d_n, int max_n, uint32_t* tmp, int* d_total,
+                        cudaStream_t s);
+/* stable LSD radix sort of (key, value) pairs by key bits [0, bits); n from device; result in *_a. */
+void radix_sort_pairs(unsigned long long* key_a, uint32_t* val_a, unsigned long long* key_b, uint32_t* val_b,
+                      const int* d_n, int max_n, int bits, uint32_t* hist, cudaStream_t s);
+size_t radix_sort_hist_size(int max_n);
+size_t scan_tmp_size(int max_n);
+
+/* Host-side count of the kernels this library has launched (bench.py reports it per step). */
+extern unsigned long long g_kernel_launches;
+#define B2G_LAUNCHED(n) (::b2g::g_kernel_launches += (unsigned long long)(n))
+
+inline int grid_for(int n, int block, int max_blocks) {
+    int g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    return g < max_blocks ? g : max_blocks;
+}
+
+}  // namespace b2g
+#endif

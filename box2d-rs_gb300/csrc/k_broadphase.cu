@@ -1,0 +1,426 @@
+/*
+ * k_broadphase.cu — pair finding and contact creation (find_new_contacts).
+ *
+ * Reference: B2broadPhase::update_pairs (src/b2_broad_phase.rs:200-249) with its query
+ * callback (src/private/collision/b2_broad_phase.rs:86-111) over B2dynamicTree, then
+ * b2_contact_manager_add_pair (src/private/dynamics/b2_contact_manager.rs:178-302).
+ *
+ * The reference inserts moved proxies into an incremental AVL-balanced tree and queries
+ * it once per moved proxy. Here the tree is rebuilt every pass as a linear BVH:
+ *   1. centre bounds of all fat AABBs (atomic min/max on order-preserving ints),
+ *   2. 64-bit keys world << 32 | Morton(16-bit x, 16-bit y), radix-sorted with the
+ *      fixture index as payload (worlds occupy disjoint key ranges),
+ *   3. Karras (2012) hierarchy over the sorted keys (ties broken by position) — every
+ *      internal node stores both children's boxes, so a traversal step is one 48-byte
+ *      fetch and two overlap tests,
+ *   4. bottom-up refit with per-node arrival counters,
+ *   5. one thread per moved proxy walks its world's subtree with a short stack and
+ *      applies the reference's rule: skip itself; skip a moved partner whose proxy id is
+ *      larger (that partner reports the pair); emit (min id, max id).
+ * The emitted set equals the reference's: every pair of overlapping fat AABBs with at
+ * least one moved proxy, each once (b2_test_overlap is closed, so touching boxes pair).
+ * add_pair's rejections run inline (same body, no dynamic body, default filter, edge-edge),
+ * and a binary search in the key-sorted contact table drops pairs that already have a
+ * live contact. New keys are radix-sorted and merged with the surviving contacts into the
+ * second contact buffer, which keeps the table sorted by key = refid_min << kb | refid_max.
+ */
+#include <climits>
+
+#include "b2g_internal.h"
+
+namespace b2g {
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kStack = 64;
+
+__device__ __forceinline__ int f2ord(float f) {
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+__device__ __forceinline__ uint32_t spread16(uint32_t x) {
+    x &= 0xffffu;
+    x = (x | (x << 8)) & 0x00ff00ffu;
+    x = (x | (x << 4)) & 0x0f0f0f0fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    x = (x | (x << 1)) & 0x55555555u;
+    return x;
+}
+
+__global__ void k_bp_init(DevWorld w) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) {
+        w.cnt[CNT_BOUNDS + 0] = INT_MAX;
+        w.cnt[CNT_BOUNDS + 1] = INT_MAX;
+        w.cnt[CNT_BOUNDS + 2] = INT_MIN;
+        w.cnt[CNT_BOUNDS + 3] = INT_MIN;
+        w.cnt[CNT_NEW] = 0;
+        w.cnt[CNT_PAIRS] = 0;
+    }
+    for (int i = t; i < w.num_worlds; i += gridDim.x * blockDim.x) {
+        w.bp_world_first[i] = -1;
+        w.bp_world_root[i] = INT_MIN;
+    }
+}
+
+__global__ void k_bp_bounds(DevWorld w) {
+    int mnx = INT_MAX, mny = INT_MAX, mxx = INT_MIN, mxy = INT_MIN;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < w.n_fixtures; f += gridDim.x * blockDim.x) {
+        const float4 a = w.f_fat[f];
+        const float cx = 0.5f * (a.x + a.z), cy = 0.5f * (a.y + a.w);
+        if (!(cx - cx == 0.0f) || !(cy - cy == 0.0f)) continue;  /* disabled proxies hold infinite boxes */
+        const int ix = f2ord(cx), iy = f2ord(cy);
+        mnx = min(mnx, ix);
+        mny = min(mny, iy);
+        mxx = max(mxx, ix);
+        mxy = max(mxy, iy);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mnx = min(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mny = min(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mxx = max(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&w.cnt[CNT_BOUNDS + 0], mnx);
+        atomicMin(&w.cnt[CNT_BOUNDS + 1], mny);
+        atomicMax(&w.cnt[CNT_BOUNDS + 2], mxx);
+        atomicMax(&w.cnt[CNT_BOUNDS + 3], mxy);
+    }
+}
+
+__global__ void k_bp_keys(DevWorld w) {
+    float lx = 0.0f, ly = 0.0f, sx = 0.0f, sy = 0.0f;
+    if (w.cnt[CNT_BOUNDS + 0] != INT_MAX) {
+        lx = ord2f(w.cnt[CNT_BOUNDS + 0]);
+        ly = ord2f(w.cnt[CNT_BOUNDS + 1]);
+        const float ex = ord2f(w.cnt[CNT_BOUNDS + 2]) - lx;
+        const float ey = ord2f(w.cnt[CNT_BOUNDS + 3]) - ly;
+        sx = ex > 0.0f ? 65535.0f / ex : 0.0f;
+        sy = ey > 0.0f ? 65535.0f / ey : 0.0f;
+    }
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < w.n_fixtures; f += gridDim.x * blockDim.x) {
+        const float4 a = w.f_fat[f];
+        const float cx = 0.5f * (a.x + a.z), cy = 0.5f * (a.y + a.w);
+        float qx = (cx - lx) * sx, qy = (cy - ly) * sy;
+        qx = (qx - qx == 0.0f) ? fminf(fmaxf(qx, 0.0f), 65535.0f) : 65535.0f;
+        qy = (qy - qy == 0.0f) ? fminf(fmaxf(qy, 0.0f), 65535.0f) : 65535.0f;
+        const uint32_t m = spread16((uint32_t)qx) | (spread16((uint32_t)qy) << 1);
+        const uint32_t world = w.b_world[w.f_body[f]];
+        w.bp_key[f] = ((unsigned long long)world << 32) | m;
+        w.bp_val[f] = (uint32_t)f;
+    }
+}
+
+__device__ __forceinline__ int delta(const unsigned long long* k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    const unsigned long long a = k[i], b = k[j];
+    if (a == b) return 64 + __clz((unsigned)(i ^ j));
+    return __clzll((long long)(a ^ b));
+}
+
+/* Karras, "Maximizing parallelism in the construction of BVHs, octrees, and k-d trees" (HPG 2012) */
+__global__ void k_bp_build(DevWorld w) {
+    const int n = w.n_fixtures;
+    const unsigned long long* k = w.bp_key;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
+        const int d = (delta(k, n, i, i + 1) - delta(k, n, i, i - 1)) >= 0 ? 1 : -1;
+        const int dmin = delta(k, n, i, i - d);
+        int lmax = 2;
+        while (delta(k, n, i, i + lmax * d) > dmin) lmax <<= 1;
+        int l = 0;
+        for (int t = lmax >> 1; t >= 1; t >>= 1)
+            if (delta(k, n, i, i + (l + t) * d) > dmin) l += t;
+        const int j = i + l * d;
+        const int dnode = delta(k, n, i, j);
+        int s = 0;
+        int t = l;
+        do {
+            t = (t + 1) >> 1;
+            if (delta(k, n, i, i + (s + t) * d) > dnode) s += t;
+        } while (t > 1);
+        const int gamma = i + s * d + (d < 0 ? -1 : 0);
+        const int lo = i < j ? i : j, hi = i < j ? j : i;
+        const int left = (lo == gamma) ? ~gamma : gamma;
+        const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+        w.bp_node_child[i] = make_int2(left, right);
+        if (left < 0) w.bp_parent[n - 1 + gamma] = i; else w.bp_parent[gamma] = i;
+        if (right < 0) w.bp_parent[n - 1 + gamma + 1] = i; else w.bp_parent[gamma + 1] = i;
+        w.bp_flag[i] = 0u;
+        /* world root: the node whose leaf range is exactly one world's range */
+        const uint32_t wl = (uint32_t)(k[lo] >> 32), wh = (uint32_t)(k[hi] >> 32);
+        if (wl == wh) {
+            const bool first = lo == 0 || (uint32_t)(k[lo - 1] >> 32) != wl;
+            const bool last = hi == n - 1 || (uint32_t)(k[hi + 1] >> 32) != wl;
+            if (first && last) w.bp_world_root[wl] = i;
+        }
+    }
+}
+
+__global__ void k_bp_leaves(DevWorld w) {
+    const int n = w.n_fixtures;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        w.bp_leaf[p] = w.f_fat[w.bp_val[p]];
+        const uint32_t wd = (uint32_t)(w.bp_key[p] >> 32);
+        const bool first = p == 0 || (uint32_t)(w.bp_key[p - 1] >> 32) != wd;
+        const bool last = p == n - 1 || (uint32_t)(w.bp_key[p + 1] >> 32) != wd;
+        if (first) w.bp_world_first[wd] = p;
+        if (first && last) w.bp_world_root[wd] = ~p;  /* a world with a single proxy */
+    }
+}
+
+__device__ __forceinline__ float4 box_union(float4 a, float4 b) {
+    return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fmaxf(a.z, b.z), fmaxf(a.w, b.w));
+}
+
+__global__ void k_bp_refit(DevWorld w) {
+    const int n = w.n_fixtures;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        if (n < 2) break;
+        int child = ~p;
+        float4 box = w.bp_leaf[p];
+        int node = w.bp_parent[n - 1 + p];
+        for (int guard = 0; guard < 128; ++guard) {
+            const int2 ch = w.bp_node_child[node];
+            if (ch.x == child) w.bp_node_b0[node] = box; else w.bp_node_b1[node] = box;
+            __threadfence();
+            if (atomicAdd(&w.bp_flag[node], 1u) == 0u) break;  /* the sibling finishes this node */
+            __threadfence();
+            const float4 b0 = __ldcg(&w.bp_node_b0[node]);
+            const float4 b1 = __ldcg(&w.bp_node_b1[node]);
+            box = box_union(b0, b1);
+            if (node == 0) break;
+            child = node;
+            node = w.bp_parent[node];
+        }
+    }
+}
+
+__device__ __forceinline__ bool box_overlap(float4 a, float4 b) { return overlap4(a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w); }
+
+/* register table of b2_contact_registers.rs:67-103: +1 keep order, -1 swap, 0 no contact */
+__device__ __forceinline__ int register_kind(int ta, int tb) {
+    const int table[9] = {+1, -1, -1, +1, 0, +1, +1, -1, +1};
+    return table[ta * 3 + tb];
+}
+__device__ __forceinline__ int contact_kind(int ta, int tb) {
+    if (ta == SHAPE_CIRCLE) return KIND_CIRCLES;
+    if (ta == SHAPE_POLYGON) return tb == SHAPE_CIRCLE ? KIND_POLYGON_CIRCLE : KIND_POLYGONS;
+    return tb == SHAPE_CIRCLE ? KIND_EDGE_CIRCLE : KIND_EDGE_POLYGON;
+}
+
+__device__ __forceinline__ int lower_bound_u64(const unsigned long long* a, int n, unsigned long long key) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ void handle_pair(const DevWorld& w, const StepParams& sp, int f, int g, int n_contacts) {
+    const uint32_t rf = w.f_refid[f], rg = w.f_refid[g];
+    if (sp.record_pairs) {
+        const int slot = atomicAdd(&w.cnt[CNT_PAIRS], 1);
+        if (slot < w.pair_cap) w.pairs[slot] = make_uint2((uint32_t)min(f, g), (uint32_t)max(f, g));
+        else atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_RECORD_OVERFLOW);
+    }
+    /* add_pair: fixture A is the one with the smaller proxy id */
+    int fa = rf < rg ? f : g, fb = rf < rg ? g : f;
+    const int ba = w.f_body[fa], bb = w.f_body[fb];
+    if (ba == bb) return;
+    const uint32_t fla = w.b_flags[ba], flb = w.b_flags[bb];
+    if ((fla & BF_TYPE_MASK) != BODY_DYNAMIC && (flb & BF_TYPE_MASK) != BODY_DYNAMIC) return;
+    /* default contact filter, private/dynamics/b2_world_callbacks.rs:6-18
+     * f_filter = category | mask << 16, f_group = group (int16) | sensor << 16 */
+    const uint32_t xa = w.f_filter[fa], xb = w.f_filter[fb];
+    const int grp_a = (int)(int16_t)(w.f_group[fa] & 0xffffu);
+    const int grp_b = (int)(int16_t)(w.f_group[fb] & 0xffffu);
+    if (grp_a == grp_b && grp_a != 0) {
+        if (grp_a <= 0) return;
+    } else if (((xa >> 16) & (xb & 0xffffu)) == 0u || ((xa & 0xffffu) & (xb >> 16)) == 0u) {
+        return;
+    }
+    const int ta = shape_type(w.f_shape[fa]), tb = shape_type(w.f_shape[fb]);
+    const int reg = register_kind(ta, tb);
+    if (reg == 0) return;
+    if (reg < 0) {
+        const int t = fa;
+        fa = fb;
+        fb = t;
+    }
+    const uint32_t lo = rf < rg ? rf : rg, hi = rf < rg ? rg : rf;
+    const unsigned long long key = ((unsigned long long)lo << w.key_bits) | hi;
+    const int pos = lower_bound_u64(w.c.key, n_contacts, key);
+    if (pos < n_contacts && w.c.key[pos] == key && !(w.c.flags[pos] & CF_DEAD)) return;
+    const int slot = atomicAdd(&w.cnt[CNT_NEW], 1);
+    if (slot < w.pair_cap) {
+        w.n_key[slot] = key;
+        w.n_fix[slot] = make_int2(fa, fb);
+        w.n_idx[slot] = (uint32_t)slot;
+    } else {
+        atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_PAIR_OVERFLOW);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams sp) {
+    const int n = w.n_fixtures;
+    const int n_contacts = w.cnt[CNT_CONTACTS];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const int f = (int)w.bp_val[p];
+        if (!w.f_moved[f]) continue;
+        const float4 q = w.bp_leaf[p];
+        const uint32_t wd = (uint32_t)(w.bp_key[p] >> 32);
+        const int root = w.bp_world_root[wd];
+        if (root < 0) continue;  /* single-proxy world (or empty) */
+        const uint32_t rq = w.f_refid[f];
+        int stack[kStack];
+        int sp_top = 0;
+        stack[sp_top++] = root;
+        while (sp_top > 0) {
+            const int node = stack[--sp_top];
+            const int2 ch = w.bp_node_child[node];
+            const float4 b0 = w.bp_node_b0[node];
+            const float4 b1 = w.bp_node_b1[node];
+            const int kids[2] = {ch.x, ch.y};
+            const bool hit[2] = {box_overlap(b0, q), box_overlap(b1, q)};
+            for (int c = 0; c < 2; ++c) {
+                if (!hit[c]) continue;
+                const int id = kids[c];
+                if (id < 0) {
+                    const int g = (int)w.bp_val[~id];
+                    if (g == f) continue;
+                    if (w.f_moved[g] && w.f_refid[g] > rq) continue;
+                    handle_pair(w, sp, f, g, n_contacts);
+                } else if (sp_top < kStack) {
+                    stack[sp_top++] = id;
+                } else {
+                    atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_STACK_OVERFLOW);
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_bp_clear_moved(DevWorld w) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < w.n_fixtures; f += gridDim.x * blockDim.x) w.f_moved[f] = 0;
+}
+
+__global__ void k_bp_clamp_new(DevWorld w) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && w.cnt[CNT_NEW] > w.pair_cap) w.cnt[CNT_NEW] = w.pair_cap;
+}
+
+/* ---- merge of surviving contacts and new contacts (both key-sorted) ---- */
+__global__ void k_merge_flags(DevWorld w, uint32_t* flag) {
+    const int n = w.cnt[CNT_CONTACTS];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        flag[i] = (w.c.flags[i] & CF_DEAD) ? 0u : 1u;
+}
+
+__device__ __forceinline__ void copy_contact(const Contacts& s, int i, const Contacts& d, int o) {
+    d.key[o] = s.key[i];
+    d.fix[o] = s.fix[i];
+    d.body[o] = s.body[i];
+    d.flags[o] = s.flags[i];
+    d.mat[o] = s.mat[i];
+    d.mgeo[o] = s.mgeo[i];
+    d.mpts[o] = s.mpts[i];
+    d.mimp[o] = s.mimp[i];
+    d.mids[o] = s.mids[i];
+}
+
+__global__ void k_merge_old(DevWorld w, const uint32_t* flag, const uint32_t* rank) {
+    const int n = w.cnt[CNT_CONTACTS];
+    const int nn = w.cnt[CNT_NEW];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!flag[i]) continue;
+        const int pos = (int)rank[i] + lower_bound_u64(w.n_key, nn, w.c.key[i]);
+        if (pos < w.contact_cap) copy_contact(w.c, i, w.c_alt, pos);
+        else atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_CONTACT_OVERFLOW);
+    }
+}
+
+/* b2_contact_create + B2contact::new (private/dynamics/b2_contact.rs:11-60): mixing laws of src/b2_contact.rs:29-46 */
+__global__ void k_merge_new(DevWorld w, const uint32_t* rank) {
+    const int n = w.cnt[CNT_CONTACTS];
+    const int nn = w.cnt[CNT_NEW];
+    const int alive = w.cnt[CNT_ALIVE];
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nn; j += gridDim.x * blockDim.x) {
+        const unsigned long long key = w.n_key[j];
+        const int2 fx = w.n_fix[w.n_idx[j]];
+        const int at = lower_bound_u64(w.c.key, n, key);
+        const int before = at < n ? (int)rank[at] : alive;
+        const int pos = j + before;
+        if (pos >= w.contact_cap) {
+            atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_CONTACT_OVERFLOW);
+            continue;
+        }
+        const float4 ma = w.f_mat[fx.x], mb = w.f_mat[fx.y];
+        const ShapeRec& sa = w.f_shape[fx.x];
+        const ShapeRec& sb = w.f_shape[fx.y];
+        const int kind = contact_kind(shape_type(sa), shape_type(sb));
+        const bool sensor = ((w.f_group[fx.x] | w.f_group[fx.y]) & 0x10000u) != 0u;
+        const Contacts& d = w.c_alt;
+        d.key[pos] = key;
+        d.fix[pos] = fx;
+        d.body[pos] = make_int2(w.f_body[fx.x], w.f_body[fx.y]);
+        d.flags[pos] = CF_ENABLED | (sensor ? CF_SENSOR : 0u) | ((uint32_t)kind << CF_KIND_SHIFT);
+        const float friction = fsqrt(ma.x * mb.x);
+        const float restitution = ma.y > mb.y ? ma.y : mb.y;
+        const float threshold = ma.z < mb.z ? ma.z : mb.z;
+        d.mat[pos] = make_float4(friction, restitution, threshold, 0.0f);
+        d.mgeo[pos] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        d.mpts[pos] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        d.mimp[pos] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        d.mids[pos] = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+__global__ void k_merge_finish(DevWorld w) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        int total = w.cnt[CNT_ALIVE] + w.cnt[CNT_NEW];
+        if (total > w.contact_cap) {
+            total = w.contact_cap;
+            atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_CONTACT_OVERFLOW);
+        }
+        w.cnt[CNT_CONTACTS] = total;
+    }
+}
+
+}  // namespace
+
+/* Runs update_pairs + add_pair and merges: the caller swaps w.c and w.c_alt afterwards. */
+void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms) {
+    const int n = w.n_fixtures;
+    const int gf = grid_for(n, kBlock, num_sms * 8);
+    k_bp_init<<<grid_for(w.num_worlds, kBlock, 64), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+    if (n > 0) {
+        k_bp_bounds<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        k_bp_keys<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        radix_sort_pairs(w.bp_key, w.bp_val, w.bp_key_alt, w.bp_val_alt, nullptr, n, 32 + w.morton_world_bits,
+                         w.sort_hist, s);
+        if (n > 1) k_bp_build<<<grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        k_bp_leaves<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        k_bp_refit<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        k_bp_traverse<<<gf, kBlock, 0, s>>>(w, sp); B2G_LAUNCHED(1);
+        k_bp_clear_moved<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+    }
+    k_bp_clamp_new<<<1, 32, 0, s>>>(w); B2G_LAUNCHED(1);
+    /* sort new keys; payload = emission slot */
+    radix_sort_pairs(w.n_key, w.n_idx, w.n_key_alt, w.n_idx_alt, &w.cnt[CNT_NEW], w.pair_cap, 2 * w.key_bits,
+                     w.sort_hist, s);
+    uint32_t* flag = w.scan_tmp;
+    uint32_t* rank = w.scan_tmp + w.contact_cap;
+    uint32_t* tmp = w.scan_tmp + 2 * (size_t)w.contact_cap;
+    const int gc = grid_for(w.contact_cap, kBlock, num_sms * 8);
+    k_merge_flags<<<gc, kBlock, 0, s>>>(w, flag); B2G_LAUNCHED(1);
+    scan_exclusive_u32(flag, rank, &w.cnt[CNT_CONTACTS], w.contact_cap, tmp, &w.cnt[CNT_ALIVE], s);
+    k_merge_old<<<gc, kBlock, 0, s>>>(w, flag, rank); B2G_LAUNCHED(1);
+    k_merge_new<<<grid_for(w.pair_cap, kBlock, num_sms * 8), kBlock, 0, s>>>(w, rank); B2G_LAUNCHED(1);
+    k_merge_finish<<<1, 32, 0, s>>>(w); B2G_LAUNCHED(1);
+}
+
+}  // namespace b2g

@@ -1,0 +1,157 @@
+/*
+ * k_collide.cu — the narrowphase pass of a step (B2contactManager::collide).
+ *
+ * Reference: b2_contact_manager_collide, src/private/dynamics/b2_contact_manager.rs:83-171,
+ * and b2_contact_update, src/private/dynamics/b2_contact.rs:103-218.
+ *
+ * One thread per contact of the (key-sorted) contact table:
+ *   - skip when neither body is awake and non-static;
+ *   - if the two fat AABBs stopped overlapping, flag the contact dead (the next merge
+ *     drops it), emit an end event if it was touching, and wake both bodies if its
+ *     manifold had points (B2contact::destroy);
+ *   - otherwise evaluate the manifold with the routine of the contact's kind, carry
+ *     normal/tangent impulses from old points with the same feature id, update the
+ *     touching flag, wake both bodies when it changes, and emit begin/end events.
+ * Algorithmic bytes per evaluated contact: ~116 B of contact/manifold state + two
+ * 144-byte shape records + two body transforms.
+ */
+#include "b2g_internal.h"
+
+namespace b2g {
+
+__device__ __forceinline__ void wake_body(const DevWorld& w, int b) {
+    uint32_t f = w.b_flags[b];
+    if ((f & BF_TYPE_MASK) == BODY_STATIC) return;
+    if (!(f & BF_AWAKE)) {
+        atomicOr(&w.b_flags[b], BF_AWAKE);
+        w.b_vel[b].w = 0.0f;  /* sleep_time = 0 */
+    }
+}
+
+__device__ __forceinline__ void push_event(const DevWorld& w, int kind, int fa, int fb) {
+    int slot = atomicAdd(&w.cnt[CNT_EVENTS], 1);
+    if (slot < w.event_cap) w.events[slot] = make_int4(kind, fa, fb, 0);
+    else atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_EVENT_OVERFLOW);
+}
+
+__device__ __forceinline__ Xf load_xf(const DevWorld& w, int b) {
+    float4 x = w.b_xf[b];
+    Xf r;
+    r.p = mk(x.x, x.y);
+    r.q.s = x.z;
+    r.q.c = x.w;
+    return r;
+}
+
+__global__ void __launch_bounds__(128) k_collide(DevWorld w, StepParams sp) {
+    const int n = w.cnt[CNT_CONTACTS];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t flags = w.c.flags[i];
+        if (flags & CF_DEAD) continue;
+        const int2 fx = w.c.fix[i];
+        const int2 bd = w.c.body[i];
+        const uint32_t fa_flags = w.b_flags[bd.x];
+        const uint32_t fb_flags = w.b_flags[bd.y];
+        const bool activeA = (fa_flags & BF_AWAKE) && (fa_flags & BF_TYPE_MASK) != BODY_STATIC;
+        const bool activeB = (fb_flags & BF_AWAKE) && (fb_flags & BF_TYPE_MASK) != BODY_STATIC;
+        if (!activeA && !activeB) continue;
+        const float4 A = w.f_fat[fx.x];
+        const float4 B = w.f_fat[fx.y];
+        const bool was_touching = (flags & CF_TOUCHING) != 0;
+        const uint4 ids = w.c.mids[i];
+        const int old_count = (int)((ids.z >> 8) & 0xffu);
+        if (!overlap4(A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w)) {
+            if (sp.record_events && was_touching) push_event(w, 1, fx.x, fx.y);
+            if (old_count > 0 && !(flags & CF_SENSOR)) {
+                wake_body(w, bd.x);
+                wake_body(w, bd.y);
+            }
+            w.c.flags[i] = (flags | CF_DEAD) & ~CF_TOUCHING;
+            continue;
+        }
+        flags |= CF_ENABLED;
+        bool touching = false;
+        if (flags & CF_SENSOR) {
+            /* sensor overlap tests (GJK) are outside the GPU path: sensors never touch */
+            w.c.mids[i] = make_uint4(ids.x, ids.y, ids.z & 0xffu, 0u);
+        } else {
+            const int kind = (int)((flags >> CF_KIND_SHIFT) & 7u);
+            const Xf xfA = load_xf(w, bd.x);
+            const Xf xfB = load_xf(w, bd.y);
+            const ShapeRec sa = w.f_shape[fx.x];
+            const ShapeRec sb = w.f_shape[fx.y];
+            Manifold m;
+            m.type = MANIFOLD_CIRCLES;
+            m.count = 0;
+            m.ln = mk(0.0f, 0.0f);
+            m.lp = mk(0.0f, 0.0f);
+            m.p[0] = m.p[1] = mk(0.0f, 0.0f);
+            m.id[0] = m.id[1] = 0u;
+            evaluate(kind, m, sa, xfA, sb, xfB);
+            const float4 oldimp = w.c.mimp[i];
+            float ni[2] = {0.0f, 0.0f}, ti[2] = {0.0f, 0.0f};
+            for (int p = 0; p < m.count; ++p) {
+                if (old_count > 0 && ids.x == m.id[p]) {
+                    ni[p] = oldimp.x;
+                    ti[p] = oldimp.y;
+                } else if (old_count > 1 && ids.y == m.id[p]) {
+                    ni[p] = oldimp.z;
+                    ti[p] = oldimp.w;
+                }
+            }
+            touching = m.count > 0;
+            w.c.mgeo[i] = make_float4(m.ln.x, m.ln.y, m.lp.x, m.lp.y);
+            w.c.mpts[i] = make_float4(m.p[0].x, m.p[0].y, m.p[1].x, m.p[1].y);
+            w.c.mimp[i] = make_float4(ni[0], ti[0], ni[1], ti[1]);
+            w.c.mids[i] = make_uint4(m.id[0], m.id[1], (uint32_t)m.type | ((uint32_t)m.count << 8), 0u);
+            if (touching != was_touching) {
+                wake_body(w, bd.x);
+                wake_body(w, bd.y);
+            }
+        }
+        w.c.flags[i] = touching ? (flags | CF_TOUCHING) : (flags & ~CF_TOUCHING);
+        if (sp.record_events) {
+            if (!was_touching && touching) push_event(w, 0, fx.x, fx.y);
+            if (was_touching && !touching) push_event(w, 1, fx.x, fx.y);
+        }
+    }
+}
+
+void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s) {
+    k_collide<<<grid_for(w.contact_cap, 128, 152 * 16), 128, 0, s>>>(w, sp); B2G_LAUNCHED(1);
+}
+
+/* Stand-alone manifolds of independent shape pairs (the public b2_collide_* functions,
+ * src/b2_collision.rs:259-315). xf = (x, y, sin, cos) per shape. */
+__global__ void k_collide_pairs(const ShapeRec* a, const float4* xa, const ShapeRec* b, const float4* xb,
+                                const int* kind, int n, float4* geo, float4* pts, uint4* ids) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        Xf A, B;
+        const float4 x0 = xa[i], x1 = xb[i];
+        A.p = mk(x0.x, x0.y);
+        A.q.s = x0.z;
+        A.q.c = x0.w;
+        B.p = mk(x1.x, x1.y);
+        B.q.s = x1.z;
+        B.q.c = x1.w;
+        Manifold m;
+        m.type = MANIFOLD_CIRCLES;
+        m.count = 0;
+        m.ln = m.lp = mk(0.0f, 0.0f);
+        m.p[0] = m.p[1] = mk(0.0f, 0.0f);
+        m.id[0] = m.id[1] = 0u;
+        const ShapeRec sa = a[i];
+        const ShapeRec sb = b[i];
+        evaluate(kind[i], m, sa, A, sb, B);
+        geo[i] = make_float4(m.ln.x, m.ln.y, m.lp.x, m.lp.y);
+        pts[i] = make_float4(m.p[0].x, m.p[0].y, m.p[1].x, m.p[1].y);
+        ids[i] = make_uint4(m.id[0], m.id[1], (uint32_t)m.type | ((uint32_t)m.count << 8), 0u);
+    }
+}
+
+void launch_collide_pairs(const ShapeRec* a, const float4* xa, const ShapeRec* b, const float4* xb, const int* kind,
+                          int n, float4* geo, float4* pts, uint4* ids, cudaStream_t s) {
+    k_collide_pairs<<<grid_for(n, 128, 152 * 16), 128, 0, s>>>(a, xa, b, xb, kind, n, geo, pts, ids); B2G_LAUNCHED(1);
+}
+
+}  // namespace b2g

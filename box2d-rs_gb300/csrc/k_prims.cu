@@ -1,0 +1,242 @@
+/*
+ * k_prims.cu — device-wide exclusive scan and stable LSD radix sort.
+ *
+ * Both take the element count from device memory (d_n), so a step can chain them
+ * after kernels that produce a variable number of items without a host round trip;
+ * grids are sized for the capacity and tiles past n do no work.
+ *
+ * Radix sort: 8-bit digits, tiles of 2048 items per 256-thread block. A pass is
+ *   1. per-tile digit histograms, stored digit-major (hist[d * tiles + t]),
+ *   2. an exclusive scan of that array, which yields each (digit, tile) output base,
+ *   3. a stable scatter: the tile is walked in 8 rounds of 256 items; inside a warp
+ *      __match_any_sync groups equal digits, and per-warp counts are prefixed across
+ *      the 8 warps in shared memory, so every item's rank preserves input order.
+ */
+#include "b2g_internal.h"
+
+namespace b2g {
+
+unsigned long long g_kernel_launches = 0;
+
+namespace {
+constexpr int kScanBlock = 256;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanBlock * kScanItems;
+constexpr int kSortBlock = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortBlock * kSortItems;
+
+__device__ __forceinline__ int load_n(const int* d_n, int max_n) {
+    if (!d_n) return max_n;
+    int n = *d_n;
+    return n < max_n ? n : max_n;
+}
+
+/* block-wide exclusive scan of one value per thread; returns the block total in *total */
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t warp_sums[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t s = lane < nwarps ? warp_sums[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        warp_sums[lane] = s;  /* inclusive */
+    }
+    __syncthreads();
+    uint32_t warp_prefix = warp > 0 ? warp_sums[warp - 1] : 0u;
+    *total = warp_sums[nwarps - 1];
+    __syncthreads();
+    return warp_prefix + x - v;
+}
+
+__global__ void k_scan_tiles(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, const int* d_n, int max_n,
+                             uint32_t* __restrict__ tile_sums) {
+    const int n = load_n(d_n, max_n);
+    const int base = blockIdx.x * kScanTile;
+    if (base >= n) {
+        if (threadIdx.x == 0) tile_sums[blockIdx.x] = 0;
+        return;
+    }
+    uint32_t v[kScanItems];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        int idx = base + threadIdx.x * kScanItems + i;
+        v[i] = idx < n ? in[idx] : 0u;
+        sum += v[i];
+    }
+    uint32_t total;
+    uint32_t off = block_exclusive_scan(sum, &total);
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        int idx = base + threadIdx.x * kScanItems + i;
+        if (idx < n) out[idx] = off;
+        off += v[i];
+    }
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+/* one block scans all tile sums (looping over chunks), writes the grand total */
+__global__ void k_scan_sums(uint32_t* tile_sums, int tiles, int* d_total) {
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < tiles; base += blockDim.x) {
+        int i = base + threadIdx.x;
+        uint32_t v = i < tiles ? tile_sums[i] : 0u;
+        uint32_t total;
+        uint32_t ex = block_exclusive_scan(v, &total);
+        if (i < tiles) tile_sums[i] = carry + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && d_total) *d_total = (int)carry;
+}
+
+__global__ void k_scan_add(uint32_t* __restrict__ out, const int* d_n, int max_n, const uint32_t* __restrict__ tile_sums) {
+    const int n = load_n(d_n, max_n);
+    const int base = blockIdx.x * kScanTile;
+    if (base >= n) return;
+    const uint32_t add = tile_sums[blockIdx.x];
+    for (int i = threadIdx.x; i < kScanTile; i += blockDim.x) {
+        int idx = base + i;
+        if (idx < n) out[idx] += add;
+    }
+}
+
+__global__ void k_sort_hist(const unsigned long long* __restrict__ keys, const int* d_n, int max_n, int shift,
+                            uint32_t* __restrict__ hist, int tiles) {
+    __shared__ uint32_t h[256];
+    const int n = load_n(d_n, max_n);
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile;
+    for (int i = threadIdx.x; i < kSortTile; i += kSortBlock) {
+        int idx = base + i;
+        if (idx < n) atomicAdd(&h[(unsigned)(keys[idx] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void k_sort_scatter(const unsigned long long* __restrict__ kin, const uint32_t* __restrict__ vin,
+                               unsigned long long* __restrict__ kout, uint32_t* __restrict__ vout, const int* d_n,
+                               int max_n, int shift, const uint32_t* __restrict__ offsets, int tiles) {
+    __shared__ uint32_t s_base[256];
+    __shared__ uint32_t s_run[256];
+    __shared__ uint32_t s_warp[8][256];
+    const int n = load_n(d_n, max_n);
+    const int tile_base = blockIdx.x * kSortTile;
+    if (tile_base >= n) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    s_base[threadIdx.x] = offsets[threadIdx.x * tiles + blockIdx.x];
+    s_run[threadIdx.x] = 0;
+    for (int w = 0; w < 8; ++w) s_warp[w][threadIdx.x] = 0;
+    __syncthreads();
+    const unsigned lt_mask = (1u << lane) - 1u;
+    for (int r = 0; r < kSortItems; ++r) {
+        const int idx = tile_base + r * kSortBlock + threadIdx.x;
+        const bool valid = idx < n;
+        unsigned long long k = 0;
+        uint32_t v = 0;
+        uint32_t d = 256u + (uint32_t)lane;  /* distinct dummy digits for invalid lanes */
+        if (valid) {
+            k = kin[idx];
+            v = vin[idx];
+            d = (uint32_t)(k >> shift) & 255u;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t rank = (uint32_t)__popc(peers & lt_mask);
+        const bool leader = (peers & lt_mask) == 0u;
+        if (valid && leader) s_warp[warp][d] = (uint32_t)__popc(peers);
+        __syncthreads();
+        {
+            /* thread t owns digit t: prefix its count across the 8 warps */
+            const int dd = threadIdx.x;
+            uint32_t run = s_run[dd];
+#pragma unroll
+            for (int w = 0; w < 8; ++w) {
+                uint32_t c = s_warp[w][dd];
+                s_warp[w][dd] = run;
+                run += c;
+            }
+            s_run[dd] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t dst = s_base[d] + s_warp[warp][d] + rank;
+            if (dst < (uint32_t)n) {  /* always true for a correct scan; keeps writes in bounds */
+                kout[dst] = k;
+                vout[dst] = v;
+            }
+        }
+        __syncthreads();
+        for (int w = 0; w < 8; ++w) s_warp[w][threadIdx.x] = 0;
+        __syncthreads();
+    }
+}
+
+__global__ void k_copy_pairs(const unsigned long long* __restrict__ kin, const uint32_t* __restrict__ vin,
+                             unsigned long long* __restrict__ kout, uint32_t* __restrict__ vout, const int* d_n, int max_n) {
+    const int n = load_n(d_n, max_n);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        kout[i] = kin[i];
+        vout[i] = vin[i];
+    }
+}
+}  // namespace
+
+size_t scan_tmp_size(int max_n) { return (size_t)((max_n + kScanTile - 1) / kScanTile + 1); }
+
+void scan_exclusive_u32(const uint32_t* in, uint32_t* out, const int* d_n, int max_n, uint32_t* tmp, int* d_total,
+                        cudaStream_t s) {
+    const int tiles = (max_n + kScanTile - 1) / kScanTile;
+    if (tiles == 0) return;
+    k_scan_tiles<<<tiles, kScanBlock, 0, s>>>(in, out, d_n, max_n, tmp); B2G_LAUNCHED(1);
+    k_scan_sums<<<1, 1024, 0, s>>>(tmp, tiles, d_total); B2G_LAUNCHED(1);
+    k_scan_add<<<tiles, kScanBlock, 0, s>>>(out, d_n, max_n, tmp); B2G_LAUNCHED(1);
+}
+
+size_t radix_sort_hist_size(int max_n) {
+    const int tiles = (max_n + kSortTile - 1) / kSortTile;
+    return (size_t)tiles * 256 * 2 + scan_tmp_size(tiles * 256) + 16;
+}
+
+void radix_sort_pairs(unsigned long long* key_a, uint32_t* val_a, unsigned long long* key_b, uint32_t* val_b,
+                      const int* d_n, int max_n, int bits, uint32_t* hist, cudaStream_t s) {
+    const int tiles = (max_n + kSortTile - 1) / kSortTile;
+    if (tiles == 0 || bits <= 0) return;
+    uint32_t* h = hist;
+    uint32_t* off = hist + (size_t)tiles * 256;
+    uint32_t* tmp = off + (size_t)tiles * 256;
+    int passes = (bits + 7) / 8;
+    unsigned long long* kin = key_a;
+    uint32_t* vin = val_a;
+    unsigned long long* kout = key_b;
+    uint32_t* vout = val_b;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = 8 * p;
+        k_sort_hist<<<tiles, kSortBlock, 0, s>>>(kin, d_n, max_n, shift, h, tiles); B2G_LAUNCHED(1);
+        scan_exclusive_u32(h, off, nullptr, tiles * 256, tmp, nullptr, s);
+        k_sort_scatter<<<tiles, kSortBlock, 0, s>>>(kin, vin, kout, vout, d_n, max_n, shift, off, tiles); B2G_LAUNCHED(1);
+        unsigned long long* tk = kin; kin = kout; kout = tk;
+        uint32_t* tv = vin; vin = vout; vout = tv;
+    }
+    if (kin != key_a) {
+        k_copy_pairs<<<grid_for(max_n, 256, 4096), 256, 0, s>>>(kin, vin, key_a, val_a, d_n, max_n); B2G_LAUNCHED(1);
+    }
+}
+
+}  // namespace b2g

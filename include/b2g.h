@@ -154,6 +154,8 @@ int b2g_world_create(const b2g_world_def* def, void** out_world);
 int b2g_world_destroy(void* world);
 const char* b2g_last_error(const void* world);
 int b2g_version(void);
+/* Number of CUDA kernels this library has launched so far (all worlds of the process). */
+int64_t b2g_get_launch_count(void);
 
 /* ---- creation: B2world::create_body (src/b2_world.rs:60-62),
  *                B2body::create_fixture (src/b2_body.rs:233) ---- */
@@ -190,7 +192,21 @@ int b2g_get_contacts(void* world, b2g_contact_info* out, int32_t capacity, int32
 /* begin/end events produced since the previous call (B2contactListener, src/b2_world_callbacks.rs:68-104) */
 int b2g_get_events(void* world, b2g_contact_event* out, int32_t capacity, int32_t* out_count);
 
+/* Buffer begin/end contact events during steps (off by default: the reference only
+ * calls a listener once one is installed, src/b2_world.rs:44-46). */
+int b2g_set_contact_events(void* world, int32_t flag);
+
+/* Manifolds of n independent shape pairs evaluated on the GPU, like the reference's public
+ * b2_collide_circles / polygon_and_circle / polygons / edge_and_circle / edge_and_polygon
+ * (src/b2_collision.rs:259-315). Shape A must be the routine's first type (circle-circle,
+ * polygon-circle, polygon-polygon, edge-circle, edge-polygon); xf_a/xf_b hold (x, y, angle)
+ * per pair. Fills fixture_a = fixture_b = pair index and the manifold fields of out[i]. */
+int b2g_collide_pairs(const b2g_fixture_def* shape_a, const float* xf_a, const b2g_fixture_def* shape_b,
+                      const float* xf_b, int32_t n, b2g_contact_info* out);
+
 /* ---- parity hooks ---- */
+/* Record every pair the broadphase emits (off by default; needed by b2g_get_pairs). */
+int b2g_set_record_pairs(void* world, int32_t flag);
 /* Pairs emitted by the last broadphase pass (update_pairs, src/b2_broad_phase.rs:200-249),
  * as fixture-id pairs (a < b), sorted. 2 uint32 per pair. */
 int b2g_get_pairs(void* world, uint32_t* out_pairs, int32_t capacity, int32_t* out_count);

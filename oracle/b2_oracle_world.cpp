@@ -1257,8 +1257,9 @@ int ora_get_solver_order(void* p, uint32_t* out, int cap, int* n) {
 int ora_get_events(void* p, b2g_contact_event* out, int cap, int* n) {
     World& w = *(World*)p;
     int k = (int)w.events.size();
-    for (int i = 0; i < k && i < cap; ++i) out[i] = w.events[i];
     *n = k;
+    if (!out) return 0; /* size query: keep the events for the copying call */
+    for (int i = 0; i < k && i < cap; ++i) out[i] = w.events[i];
     w.events.clear();
     return 0;
 }

@@ -1,0 +1,121 @@
+"""Reference behaviours through the GPU path's B2world-shaped API (the reference's own KATs
+re-expressed on the GPU, listener events, flags and error handling)."""
+import numpy as np
+import pytest
+
+import b2g
+import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def test_hello_world_gpu(built):
+    """box2d-rs tests/test.rs:26-102 on the GPU: y = 1.01 +- 0.01 after 60 steps of 6/2."""
+    s = scenes.hello_world()
+    w = b2g.B2world(gravity=s["gravity"])
+    scenes.build_world(w, s)
+    for _ in range(60):
+        w.step(np.float32(1.0 / 60.0), 6, 2)
+    st = w.get_body_states()[1]
+    assert abs(st["position"][0]) < 0.01
+    assert abs(st["position"][1] - 1.01) < 0.01
+    assert abs(st["angle"]) < 0.01
+
+
+class Listener:
+    def __init__(self):
+        self.begin = []
+        self.end = []
+
+    def begin_contact(self, fa, fb):
+        self.begin.append((fa, fb))
+
+    def end_contact(self, fa, fb):
+        self.end.append((fa, fb))
+
+
+def test_begin_contact_gpu(built):
+    """box2d-rs tests/world_test.rs:51-87 on the GPU, with events replayed to a listener."""
+    w = b2g.B2world(gravity=(0.0, -10.0))
+    lst = Listener()
+    w.set_contact_listener(lst)
+    bd = b2g.body_defs(2)
+    bd["type"] = b2g.DYNAMIC
+    w.create_bodies(bd)
+    w.create_fixtures(np.concatenate([b2g.circle_fixture(0, 5.0), b2g.circle_fixture(1, 5.0)]))
+    w.set_transform(0, (0.0, 0.0), 0.0)
+    w.set_transform(1, (100.0, 0.0), 0.0)
+    w.step(np.float32(1.0 / 60.0), 6, 2)
+    assert w.get_counts()["contacts"] == 0
+    assert lst.begin == []
+    w.set_transform(1, (1.0, 0.0), 0.0)
+    w.step(np.float32(1.0 / 60.0), 6, 2)
+    assert w.get_counts()["contacts"] > 0
+    assert lst.begin == [(0, 1)]
+    w.set_transform(1, (100.0, 0.0), 0.0)
+    w.step(np.float32(1.0 / 60.0), 6, 2)
+    assert lst.end == [(0, 1)]
+
+
+def test_empty_and_zero_dt(built):
+    w = b2g.B2world()
+    w.step(np.float32(1 / 60), 8, 3)  # no bodies: a no-op
+    s = scenes.pyramid(rows=3)
+    scenes.build_world(w, s)
+    before = w.get_body_states()
+    w.step(np.float32(0.0), 8, 3)  # dt = 0: collide only, bodies do not move
+    after = w.get_body_states()
+    assert np.array_equal(before["position"], after["position"])
+
+
+def test_continuous_physics_is_refused(built):
+    w = b2g.B2world()
+    scenes.build_world(w, scenes.pyramid(rows=2))
+    w.set_continuous_physics(True)
+    with pytest.raises(b2g.B2GError) as e:
+        w.step(np.float32(1 / 60), 8, 3)
+    assert e.value.code == -6
+    w.set_continuous_physics(False)
+    w.step(np.float32(1 / 60), 8, 3)
+
+
+def test_contact_capacity_overflow_reports(built):
+    """A too-small contact table reports B2G_ERR_CAPACITY instead of writing out of bounds."""
+    s = scenes.pile(n_boxes=600, width=6.0, height=30.0, seed=1, spacing=0.45)
+    w = b2g.B2world(gravity=s["gravity"], contact_capacity=64, pair_capacity=64)
+    w.set_allow_sleeping(False)
+    scenes.build_world(w, s)
+    with pytest.raises(b2g.B2GError) as e:
+        for _ in range(200):
+            w.step(s["dt"], 8, 3)
+        w.synchronize()
+    assert e.value.code == -3
+
+
+def test_forces_and_impulses(built):
+    w = b2g.B2world(gravity=(0.0, 0.0))
+    bd = b2g.body_defs(1)
+    bd["type"] = b2g.DYNAMIC
+    w.create_bodies(bd)
+    w.create_fixture(b2g.circle_fixture(0, 0.5, density=1.0))
+    w.step(np.float32(1 / 60), 8, 3)
+    w.apply_linear_impulse(0, (1.0, 0.0), (0.0, 0.0))
+    st = w.get_body_states()[0]
+    mass = np.float32(np.pi) * 0.25
+    assert abs(st["linear_velocity"][0] - 1.0 / mass) < 1e-5
+    w.set_linear_velocity(0, (0.0, 2.0))
+    w.step(np.float32(0.5), 8, 3)
+    assert abs(w.get_body_states()[0]["position"][1] - 1.0) < 1e-5
+
+
+def test_sleeping_bodies_stop(built):
+    """With sleep allowed, a resting pyramid falls asleep (velocities zeroed) like the reference."""
+    s = scenes.pyramid(rows=4)
+    s["bodies"]["allow_sleep"] = 1
+    w = b2g.B2world(gravity=s["gravity"])
+    w.set_allow_sleeping(True)
+    scenes.build_world(w, s)
+    for _ in range(400):
+        w.step(s["dt"], 8, 3)
+    st = w.get_body_states()
+    assert np.abs(st["linear_velocity"][1:]).max() == 0.0

@@ -1,0 +1,169 @@
+"""GPU path vs the oracle (CPU restatement of box2d-rs) through the C ABI.
+
+Bar: broadphase pair sets equal (bit-exact fat AABBs), manifold feature ids exact and
+points/normals/impulses within 1e-5, bodies within 1e-5 per step with the oracle solved
+in the GPU's constraint-colour order. With identical IEEE f32 operations the GPU is
+expected to be bit-exact, and most checks assert exactly that.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import b2g
+import oracle
+import parity
+import scenes
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _assert_step(r, bitexact=True):
+    assert r["hook_misses"] == 0, r
+    assert r["pairs_equal"], r
+    assert r["fat_aabb_equal"], r
+    assert r["contact_key_mismatch"] == 0, r
+    assert r["contact_id_mismatch"] == 0, r
+    assert r["manifold_max_diff"] <= TOL, r
+    assert r["body_rel"] <= TOL, r
+    if bitexact:
+        assert r["bitexact_bodies"], r
+
+
+def test_narrowphase_golden(built):
+    """All five manifold routines on 3000 posed shape pairs: ids exact, geometry bit-exact."""
+    g = np.load(os.path.join(GOLDEN, "golden_oracle.npz"))
+    da = g["narrow_def_a"].view(b2g.FIXTURE_DEF)
+    db = g["narrow_def_b"].view(b2g.FIXTURE_DEF)
+    ref = g["narrow_out"].view(b2g.CONTACT_INFO)
+    out = b2g.collide_pairs(da, g["narrow_xf_a"], db, g["narrow_xf_b"])
+    assert np.array_equal(out["point_count"], ref["point_count"])
+    t = ref["point_count"] > 0
+    assert np.array_equal(out["manifold_type"][t], ref["manifold_type"][t])
+    for i in np.nonzero(t)[0]:
+        n = ref["point_count"][i]
+        assert list(out["point_id"][i][:n]) == list(ref["point_id"][i][:n]), i
+        for f in ("local_normal", "local_point"):
+            assert np.array_equal(out[f][i], ref[f][i]), (i, f)
+        assert np.array_equal(out["point_local"][i][:n], ref["point_local"][i][:n]), i
+
+
+def test_narrowphase_vs_live_oracle(built):
+    """Same check against the oracle evaluated in this process (random poses, new seed)."""
+    import sys
+
+    sys.path.insert(0, GOLDEN)
+    import make_golden
+
+    oracle.set_trig(False)
+    try:
+        da, xa, db, xb = make_golden.random_shape_pairs(n=2000, seed=77)
+        ref = make_golden.run_narrow(da, xa, db, xb)
+    finally:
+        oracle.set_trig(True)
+    out = b2g.collide_pairs(da, xa, db, xb)
+    assert np.array_equal(out["point_count"], ref["point_count"])
+    t = ref["point_count"] > 0
+    assert np.array_equal(out["point_id"][t], ref["point_id"][t]) or all(
+        list(out["point_id"][i][: ref["point_count"][i]]) == list(ref["point_id"][i][: ref["point_count"][i]])
+        for i in np.nonzero(t)[0])
+    assert np.array_equal(out["local_normal"][t], ref["local_normal"][t])
+
+
+def test_pyramid_lockstep(built):
+    """20-row pyramid, 120 steps of 8/3: bit-exact bodies, equal pair sets, every step."""
+    s = scenes.pyramid()
+    recs, gpu, _ = parity.lockstep(s, 120)
+    for r in recs:
+        _assert_step(r)
+    assert recs[-1]["constraints"] > 200
+
+
+def test_pyramid_golden(built):
+    """8-row pyramid against the committed oracle trajectory (30/60/120 steps), bit for bit."""
+    g = np.load(os.path.join(GOLDEN, "golden_oracle.npz"))
+    s = scenes.pyramid(rows=8, steps=120)
+    w = b2g.B2world(gravity=s["gravity"])
+    w.set_allow_sleeping(False)
+    scenes.build_world(w, s)
+    for k in range(1, 121):
+        w.step(s["dt"], s["vi"], s["pi"])
+        if k in (30, 60, 120):
+            ref = g[f"pyr_{k}"].view(b2g.BODY_STATE)
+            got = w.get_body_states()
+            for f in parity.BODY_FIELDS:
+                assert np.array_equal(got[f], ref[f]), (k, f)
+
+
+def test_mixed_small_lockstep(built):
+    """400 circles and polygons (3-8 vertices) in a 20 m walled box under gravity: 60 steps."""
+    s = scenes.mixed(n_circles=200, n_polygons=200, size=20.0, seed=9)
+    recs, gpu, ora = parity.lockstep(s, 60)
+    for r in recs:
+        _assert_step(r)
+    g = np.load(os.path.join(GOLDEN, "golden_oracle.npz"))
+    ref = g["mix_60"].view(b2g.BODY_STATE)
+    got = gpu.get_body_states()
+    for f in parity.BODY_FIELDS:
+        assert np.array_equal(got[f], ref[f]), f
+    assert parity.pair_set(g["mix_pairs"]) == parity.pair_set(gpu.get_pairs())
+
+
+def test_mixed_dense_lockstep(built):
+    """A denser pile of 3000 mixed bodies in a 40 m box (hundreds of multi-body islands)."""
+    s = scenes.mixed(n_circles=1500, n_polygons=1500, size=40.0, seed=13)
+    recs, _, _ = parity.lockstep(s, 40)
+    for r in recs:
+        _assert_step(r)
+    assert max(r["constraints"] for r in recs) > 500
+
+
+def test_batched_worlds_lockstep(built):
+    """Several independent worlds in one batch: never any cross-world pair."""
+    s = scenes.batched(num_worlds=6, lo=16, hi=200, seed=5)
+    recs, gpu, _ = parity.lockstep(s, 30)
+    for r in recs:
+        _assert_step(r)
+    world = s["bodies"]["world_index"]
+    fb = s["fixtures"]["body"]
+    for a, b in gpu.get_pairs():
+        assert world[fb[a]] == world[fb[b]]
+
+
+def test_pile_boxes_lockstep(built):
+    """Small boxes dropped into a walled container settle into a pile (2-point manifolds,
+    block solver, warm starting through many steps)."""
+    s = scenes.pile(n_boxes=2000, width=12.0, height=40.0, seed=3, spacing=0.6)
+    recs, _, _ = parity.lockstep(s, 150, check_pairs=True)
+    for r in recs:
+        _assert_step(r)
+
+
+def test_one_sided_edges_and_kinematic(built):
+    """One-sided edge chain, a kinematic paddle and circles/polygons dropped on them."""
+    bodies = b2g.body_defs(40)
+    bodies["allow_sleep"] = 0
+    bodies[1]["type"] = b2g.KINEMATIC
+    bodies[1]["position"] = (0.0, 3.0)
+    bodies[1]["angular_velocity"] = 1.0
+    bodies[2:]["type"] = b2g.DYNAMIC
+    rng = np.random.default_rng(3)
+    bodies[2:]["position"][:, 0] = rng.uniform(-4, 4, 38)
+    bodies[2:]["position"][:, 1] = rng.uniform(5, 15, 38)
+    fx = [b2g.edge_fixture(0, (-5.0, 0.0), (0.0, -1.0), v0=(-6.0, 1.0), v3=(5.0, 0.0)),
+          b2g.edge_fixture(0, (0.0, -1.0), (5.0, 0.0), v0=(-5.0, 0.0), v3=(6.0, 1.0)),
+          b2g.box_fixture(1, 2.0, 0.1, density=1.0)]
+    for i in range(2, 40):
+        if i % 2:
+            fx.append(b2g.circle_fixture(i, 0.3, density=1.0, friction=0.5))
+        else:
+            fx.append(b2g.polygon_fixture(i, [(-0.3, -0.2), (0.3, -0.25), (0.35, 0.2), (0.0, 0.4), (-0.3, 0.2)],
+                                          density=1.0, friction=0.5))
+    s = {"bodies": bodies, "fixtures": np.concatenate(fx), "gravity": (0.0, -10.0), "dt": np.float32(1 / 60),
+         "vi": 8, "pi": 3, "num_worlds": 1, "allow_sleep": False}
+    recs, _, _ = parity.lockstep(s, 200)
+    for r in recs:
+        _assert_step(r)
