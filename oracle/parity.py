@@ -24,6 +24,83 @@ import scenes  # noqa: E402
 BODY_FIELDS = ("position", "angle", "linear_velocity", "angular_velocity", "world_center")
 
 
+class MultiOracle:
+    """One oracle world per world of a batched scene, addressed with the batch's global ids.
+
+    The reference has one world per B2world; a batch of independent worlds is checked by
+    running each in its own oracle and mapping body/fixture ids. Creation order inside each
+    world follows the batch's order, so proxy ids keep the same relative order."""
+
+    def __init__(self, scene, **kw):
+        bodies, fixtures = scene["bodies"], scene["fixtures"]
+        wi = bodies["world_index"]
+        self.n_bodies, self.n_fixtures = len(bodies), len(fixtures)
+        self.worlds = []
+        self.fix_world = np.zeros(len(fixtures), np.int64)
+        self.fix_local = np.zeros(len(fixtures), np.int64)
+        for w in range(scene["num_worlds"]):
+            bidx = np.nonzero(wi == w)[0]
+            remap = np.full(len(bodies), -1, np.int64)
+            remap[bidx] = np.arange(len(bidx))
+            fidx = np.nonzero(remap[fixtures["body"]] >= 0)[0]
+            bd = bodies[bidx].copy()
+            bd["world_index"] = 0
+            fx = fixtures[fidx].copy()
+            fx["body"] = remap[fx["body"]]
+            o = oracle.OracleWorld(gravity=scene["gravity"], **kw)
+            o.create_bodies(bd)
+            o.create_fixtures(fx)
+            self.fix_world[fidx] = w
+            self.fix_local[fidx] = np.arange(len(fidx))
+            self.worlds.append((o, bidx, fidx))
+
+    def step(self, dt, vi, pi):
+        for o, _, _ in self.worlds:
+            o.step(dt, vi, pi)
+
+    def set_solver_order(self, pairs):
+        p = np.asarray(pairs, np.int64).reshape(-1, 2)
+        w = self.fix_world[p[:, 0]] if len(p) else np.zeros(0, np.int64)
+        for k, (o, _, _) in enumerate(self.worlds):
+            sel = p[w == k]
+            o.set_solver_order(np.stack([self.fix_local[sel[:, 0]], self.fix_local[sel[:, 1]]], 1) if len(sel) else None)
+
+    def hook_misses(self):
+        return sum(o.hook_misses() for o, _, _ in self.worlds)
+
+    def get_body_states(self):
+        out = np.zeros(self.n_bodies, b2g.BODY_STATE)
+        for o, bidx, _ in self.worlds:
+            out[bidx] = o.get_body_states()
+        return out
+
+    def get_pairs(self):
+        res = [fidx[o.get_pairs()] for o, _, fidx in self.worlds]
+        res = [r.reshape(-1, 2) for r in res if len(r)]
+        if not res:
+            return np.zeros((0, 2), np.uint32)
+        p = np.concatenate(res)
+        return np.stack([p.min(1), p.max(1)], 1).astype(np.uint32)
+
+    def get_contacts(self):
+        res = []
+        for o, _, fidx in self.worlds:
+            c = o.get_contacts().copy()
+            c["fixture_a"] = fidx[c["fixture_a"]]
+            c["fixture_b"] = fidx[c["fixture_b"]]
+            res.append(c)
+        return np.concatenate(res) if res else np.zeros(0, b2g.CONTACT_INFO)
+
+    def get_proxies(self):
+        aabbs = np.zeros((self.n_fixtures, 4), np.float32)
+        moved = np.zeros(self.n_fixtures, np.uint8)
+        ids = np.zeros(self.n_fixtures, np.int32)
+        for o, _, fidx in self.worlds:
+            a, m, i = o.get_proxies()
+            aabbs[fidx], moved[fidx], ids[fidx] = a, m, i
+        return aabbs, moved, ids
+
+
 def make_pair(scene, record_pairs=True, record_events=False, warm_starting=True):
     oracle.set_trig(False)  # the project's correctly rounded sin/cos, which the GPU uses
     gpu = b2g.B2world(gravity=scene["gravity"], num_worlds=scene.get("num_worlds", 1))
@@ -32,10 +109,13 @@ def make_pair(scene, record_pairs=True, record_events=False, warm_starting=True)
     gpu.set_continuous_physics(False)
     gpu.set_record_pairs(record_pairs)
     gpu.set_contact_events(record_events)
-    ora = oracle.OracleWorld(gravity=scene["gravity"], allow_sleep=scene.get("allow_sleep", False),
-                             warm_starting=warm_starting, record_events=record_events)
+    kw = dict(allow_sleep=scene.get("allow_sleep", False), warm_starting=warm_starting, record_events=record_events)
     scenes.build_world(gpu, scene)
-    scenes.build_world(ora, scene)
+    if scene.get("num_worlds", 1) > 1:
+        ora = MultiOracle(scene, **kw)
+    else:
+        ora = oracle.OracleWorld(gravity=scene["gravity"], **kw)
+        scenes.build_world(ora, scene)
     return gpu, ora
 
 
