@@ -147,6 +147,40 @@ def run_cpu_baseline(scene, budget_s=15.0, max_steps=60):
             "sample": f"first {steps} steps of the mixed-100k scene (oracle, libm sin/cos, 1 thread, {dt:.1f} s)"}
 
 
+def snapshot(world):
+    """Post-step state of a GPU world, enough for the oracle to continue from it."""
+    aabbs, _ = world.get_proxies()
+    return {"bodies": world.get_body_states(), "aabbs": aabbs, "contacts": world.get_contacts()}
+
+
+def run_cpu_on_snapshots(scene, snaps, budget_s=24.0):
+    """Time the oracle (libm sin/cos, 1 thread) for a few steps from each GPU snapshot, so the
+    CPU sample covers the same part of the trajectory as the timed GPU steps."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.set_trig(True)
+    dt = scene["dt"]
+    total_steps, total_s, where = 0, 0.0, []
+    per_snap = budget_s / max(1, len(snaps))
+    for step_index, snap in snaps:
+        w = oracle.OracleWorld(gravity=scene["gravity"], allow_sleep=False)
+        scenes.build_world(w, scene)
+        w.import_state(snap["bodies"], snap["aabbs"], snap["contacts"], np.float32(1.0) / dt)
+        n = 0
+        t0 = time.perf_counter()
+        while n < 20 and (n < 2 or time.perf_counter() - t0 < per_snap):
+            w.step(dt, scene["vi"], scene["pi"])
+            n += 1
+        total_s += time.perf_counter() - t0
+        total_steps += n
+        where.append(f"{n}@{step_index}")
+        w.close()
+    return {"value": scene["n_dynamic"] * total_steps / total_s, "unit": "body-steps/s", "cores": 1, "kind": "port",
+            "sample": f"oracle (libm sin/cos, 1 thread) stepped from GPU snapshots of the timed window: "
+                      f"steps@step-index {', '.join(where)}; {total_s:.1f} s"}
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -163,6 +197,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the 100k bodies (testing only)")
+    ap.add_argument("--no-graphs", action="store_true", help="launch kernels directly instead of CUDA graphs")
     args = ap.parse_args()
     rank, world_size, local_rank = dist_info()
     n_half = int(50_000 * args.scale)
@@ -170,7 +205,8 @@ def main():
     stats = scene_stats(scene)
     config = {"workload": WORKLOAD, "bodies": stats["n_dynamic"], "fixtures": stats["n_fixtures"],
               "velocity_iterations": 8, "position_iterations": 3, "dt": 1 / 60, "sleep": False,
-              "continuous": False, "l2": "256 MiB flush between timed steps", "parallelism": "replicas"}
+              "continuous": False, "l2": "256 MiB flush between timed steps", "parallelism": "replicas",
+              "cuda_graphs": not args.no_graphs}
 
     if args.impl == "reference":
         if rank != 0:
@@ -197,6 +233,7 @@ def main():
     w = b2g.B2world(gravity=scene["gravity"], device=local_rank)
     w.set_allow_sleeping(False)
     w.set_continuous_physics(False)
+    w.set_graph_capture(not args.no_graphs)
     scenes.build_world(w, scene)
     dt, vi, pi = scene["dt"], scene["vi"], scene["pi"]
     for _ in range(args.warmup):
@@ -211,23 +248,35 @@ def main():
     launches0 = w._lib.b2g_get_launch_count()
     total_ms = 0.0
     phase_ms = {"collide": 0.0, "solve_init": 0.0, "solve_velocity": 0.0, "broadphase": 0.0}
-    per_step = []
-    for _ in range(args.steps):
+    snap_at = set(int(x) for x in np.linspace(0, args.steps - 1, 4)) if rank == 0 and not args.no_cpu_baseline else set()
+    snaps = []
+    for k in range(args.steps):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         w.step(dt, vi, pi)
         p = w.get_profile()  # synchronizes the world's stream; event times of this step
         total_ms += p["step"]
-        per_step.append(p["step"])
-        for k in phase_ms:
-            phase_ms[k] += p[k]
+        for ph in phase_ms:
+            phase_ms[ph] += p[ph]
+        if k in snap_at:  # outside the timed events: the state after this step
+            snaps.append((args.warmup + k + 1, snapshot(w)))
     launches = w._lib.b2g_get_launch_count() - launches0
     torch.cuda.synchronize()
     clocks = sampler.stop()
     counts = w.get_counts()
+    w.close()
 
-    # e2e: steps through the API with every body's state read back to host memory
-    e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(1, min(args.steps, 200))
+    # e2e: a fresh world over the same step window, stepped through the API with every body's
+    # state read back into host memory each step
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else args.steps
+    w = b2g.B2world(gravity=scene["gravity"], device=local_rank)
+    w.set_allow_sleeping(False)
+    w.set_continuous_physics(False)
+    w.set_graph_capture(not args.no_graphs)
+    scenes.build_world(w, scene)
+    for _ in range(args.warmup):
+        w.step(dt, vi, pi)
+    w.synchronize()
     states = np.zeros(w.body_count, b2g.BODY_STATE)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -235,6 +284,7 @@ def main():
         w.get_body_states(out=states)
     e2e_s = time.perf_counter() - t0
     d2h = w.body_count * 48  # three float4 arrays per body
+    w.close()
 
     if world_size > 1:
         t = torch.tensor([total_ms, e2e_s], device="cuda", dtype=torch.float64)
@@ -265,7 +315,7 @@ def main():
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = run_cpu_baseline(scene)
+        line["cpu_baseline"] = run_cpu_on_snapshots(scene, snaps)
     if rank == 0:
         print(json.dumps(line))
     if world_size > 1:

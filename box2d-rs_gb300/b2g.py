@@ -315,6 +315,7 @@ def load_library(path=LIB_PATH):
         "b2g_get_solver_order": [vp, vp, i32, ctypes.POINTER(i32)],
         "b2g_set_contact_events": [vp, i32],
         "b2g_set_record_pairs": [vp, i32],
+        "b2g_set_graph_capture": [vp, i32],
         "b2g_version": [],
     }
     for name, args in sig.items():
@@ -476,6 +477,9 @@ class B2world:
 
     def set_record_pairs(self, flag):
         self._check(self._lib.b2g_set_record_pairs(self._h, int(flag)))
+
+    def set_graph_capture(self, flag):
+        self._check(self._lib.b2g_set_graph_capture(self._h, int(flag)))
 
     # -- introspection --
     def get_profile(self):

@@ -42,6 +42,19 @@ struct Timer {
     bool valid = false;
 };
 
+/* What a captured step graph depends on besides device memory contents. */
+struct GraphKey {
+    float dt, dt_ratio, gx, gy;
+    int vi, pi, flags;
+    int generation, n_bodies, n_fixtures;
+};
+
+struct GraphSlot {
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long kernels = 0;  /* kernel nodes in the graph */
+    GraphKey key{};
+};
+
 struct World {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -75,7 +88,20 @@ struct World {
     Timer timer;
     b2g_profile profile{};
     int last_colours = 0;
+    /* CUDA graphs of the steady-state step, one per contact-buffer parity */
+    bool use_graphs = true;
+    GraphSlot graphs[2];
+    int swaps = 0;
+    int alloc_generation = 0;
+    int minsep_buffers = 2;  /* position-iteration separation buffers held in d.isl_minsep */
 };
+
+void drop_graphs(World* w) {
+    for (GraphSlot& g : w->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+    }
+}
 
 int fail(World* w, int code, const char* msg) {
     if (w) w->err = msg;
@@ -104,10 +130,14 @@ int dalloc(World* w, T** p, size_t n) {
     return B2G_OK;
 }
 
+void drop_graphs(World* w);
+
 void free_all(World* w) {
+    drop_graphs(w);
     for (void* p : w->allocations) cudaFree(p);
     w->allocations.clear();
     w->allocated = false;
+    ++w->alloc_generation;
 }
 
 int bits_for(uint64_t v) {
@@ -397,8 +427,11 @@ int allocate(World* w, int nb, int nf) {
     A(d.b_xf, body_cap); A(d.b_pos, body_cap); A(d.b_pos0, body_cap); A(d.b_vel, body_cap);
     A(d.b_force, body_cap); A(d.b_mass, body_cap); A(d.b_damp, body_cap); A(d.b_lc, body_cap);
     A(d.b_flags, body_cap); A(d.b_world, body_cap); A(d.b_island, body_cap);
-    A(d.b_cmin, body_cap); A(d.b_cmask, body_cap);
-    A(d.isl_minsep, 2 * (size_t)body_cap); A(d.isl_done, body_cap); A(d.isl_sleep, body_cap);
+    A(d.b_cmin, 2 * (size_t)body_cap); A(d.b_cmask, body_cap);
+    /* one per-island separation buffer per position iteration (at least 2: the island pass
+     * uses the second as its "has an awake member" flag) */
+    w->minsep_buffers = std::max(2, w->minsep_buffers);
+    A(d.isl_minsep, (size_t)w->minsep_buffers * body_cap); A(d.isl_done, body_cap); A(d.isl_sleep, body_cap);
     A(d.f_shape, fix_cap); A(d.f_body, fix_cap); A(d.f_mat, fix_cap); A(d.f_filter, fix_cap);
     A(d.f_group, fix_cap); A(d.f_refid, fix_cap); A(d.f_fat, fix_cap); A(d.f_moved, fix_cap);
     Contacts* cs[2] = {&d.c, &d.c_alt};
@@ -570,7 +603,10 @@ int check_status(World* w) {
     return B2G_OK;
 }
 
-void swap_contacts(World* w) { std::swap(w->d.c, w->d.c_alt); }
+void swap_contacts(World* w) {
+    std::swap(w->d.c, w->d.c_alt);
+    ++w->swaps;
+}
 
 StepParams make_params(World* w, float dt, int vi, int pi) {
     StepParams sp{};
@@ -589,11 +625,66 @@ StepParams make_params(World* w, float dt, int vi, int pi) {
     return sp;
 }
 
+/* The launch sequence of one step on the world's stream (captured into a graph or run directly).
+ * Under capture the profile events become external event-record nodes, so the host can still
+ * time the graph's phases with cudaEventElapsedTime. */
+void issue_step(World* w, const StepParams& sp, float dt, bool capturing = false) {
+    cudaStream_t s = w->stream;
+    Timer& t = w->timer;
+    auto mark = [&](cudaEvent_t e) {
+        if (capturing) cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+        else cudaEventRecord(e, s);
+    };
+    cudaMemsetAsync(w->d.cnt + CNT_EVENTS, 0, sizeof(int), s);
+    mark(t.e[0]);
+    if (w->new_contacts) {
+        launch_broadphase(w->d, sp, s, w->num_sms);
+        swap_contacts(w);
+        w->new_contacts = false;
+    }
+    mark(t.e[1]);
+    launch_collide(w->d, sp, s);
+    mark(t.e[2]);
+    if (dt > 0.0f) {
+        launch_islands_and_constraints(w->d, sp, s);
+        launch_colouring(w->d, s, w->num_sms);
+        mark(t.e[3]);
+        launch_solver(w->d, sp, s, w->num_sms);
+        mark(t.e[4]);
+        launch_broadphase(w->d, sp, s, w->num_sms);
+        swap_contacts(w);
+        mark(t.e[5]);
+        w->inv_dt0 = sp.inv_dt;
+    } else {
+        mark(t.e[3]);
+        mark(t.e[4]);
+        if (w->auto_clear) launch_clear_forces(w->d, s);
+        mark(t.e[5]);
+    }
+}
+
+/* More position iterations than separation buffers: replace that one allocation. */
+int ensure_minsep_buffers(World* w, int pi) {
+    if (pi <= w->minsep_buffers) return B2G_OK;
+    CUDA_OK(w, cudaStreamSynchronize(w->stream));
+    auto it = std::find(w->allocations.begin(), w->allocations.end(), (void*)w->d.isl_minsep);
+    if (it != w->allocations.end()) w->allocations.erase(it);
+    cudaFree(w->d.isl_minsep);
+    w->minsep_buffers = pi;
+    int rc = dalloc(w, &w->d.isl_minsep, (size_t)pi * w->d.body_cap);
+    if (rc != B2G_OK) return rc;
+    drop_graphs(w);
+    ++w->alloc_generation;
+    return B2G_OK;
+}
+
 /* B2world::step, src/private/dynamics/b2_world.rs:903-959 */
 int step(World* w, float dt, int vi, int pi) {
     if (w->h_flags.empty()) return B2G_OK;
     if (vi < 0 || pi < 0 || !(dt >= 0.0f)) return fail(w, B2G_ERR_INVALID_ARG, "dt must be >= 0 and iterations >= 0");
     int rc = prepare(w);
+    if (rc != B2G_OK) return rc;
+    rc = ensure_minsep_buffers(w, pi);
     if (rc != B2G_OK) return rc;
     w->device_authoritative = true;
     StepParams sp = make_params(w, dt, vi, pi);
@@ -603,31 +694,63 @@ int step(World* w, float dt, int vi, int pi) {
         for (auto& e : t.e) cudaEventCreate(&e);
         t.valid = true;
     }
-    cudaMemsetAsync(w->d.cnt + CNT_EVENTS, 0, sizeof(int), s);
-    cudaEventRecord(t.e[0], s);
-    if (w->new_contacts) {
-        launch_broadphase(w->d, sp, s, w->num_sms);
+    /* Steady state (no fixtures added since the last step, dt > 0, warm-start ratio already
+     * set): the step's launch sequence depends only on the parameters, the allocation and the
+     * contact-buffer parity, so it runs as one of two captured CUDA graphs. */
+    const bool graphable = w->use_graphs && !w->new_contacts && dt > 0.0f && w->steps > 0;
+    if (graphable) {
+        GraphKey key{};
+        key.dt = dt;
+        key.dt_ratio = sp.dt_ratio;
+        key.gx = sp.gx;
+        key.gy = sp.gy;
+        key.vi = vi;
+        key.pi = pi;
+        key.flags = sp.warm | (sp.allow_sleep << 1) | (sp.auto_clear << 2) | (sp.record_events << 3) |
+                    (sp.record_pairs << 4);
+        key.generation = w->alloc_generation;
+        key.n_bodies = w->d.n_bodies;
+        key.n_fixtures = w->d.n_fixtures;
+        const int parity = w->swaps & 1;
+        GraphSlot& g = w->graphs[parity];
+        if (!g.exec || memcmp(&g.key, &key, sizeof(key)) != 0) {
+            if (g.exec) {
+                cudaGraphExecDestroy(g.exec);
+                g.exec = nullptr;
+            }
+            DevWorld saved = w->d;
+            const int saved_swaps = w->swaps;
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                const unsigned long long before = g_kernel_launches;
+                issue_step(w, sp, dt, true);
+                g.kernels = g_kernel_launches - before;  /* counted per replay instead */
+                g_kernel_launches = before;
+                e = cudaStreamEndCapture(s, &graph);
+            }
+            w->d = saved;  /* the capture recorded the launches; the real swap happens below */
+            w->swaps = saved_swaps;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&g.exec, graph, 0);
+            if (graph) cudaGraphDestroy(graph);
+            if (e != cudaSuccess) {
+                /* capture unsupported here: fall back to direct launches for this world */
+                cudaGetLastError();
+                g.exec = nullptr;
+                w->use_graphs = false;
+                issue_step(w, sp, dt);
+                CUDA_OK(w, cudaGetLastError());
+                ++w->steps;
+                return B2G_OK;
+            }
+            g.key = key;
+        }
+        CUDA_OK(w, cudaGraphLaunch(g.exec, s));
+        B2G_LAUNCHED(g.kernels);
         swap_contacts(w);
-        w->new_contacts = false;
-    }
-    cudaEventRecord(t.e[1], s);
-    launch_collide(w->d, sp, s);
-    cudaEventRecord(t.e[2], s);
-    if (dt > 0.0f) {
-        launch_islands_and_constraints(w->d, sp, s);
-        launch_colouring(w->d, s, w->num_sms);
-        cudaEventRecord(t.e[3], s);
-        CUDA_OK(w, (cudaError_t)launch_solver(w->d, sp, s, w->num_sms));
-        cudaEventRecord(t.e[4], s);
-        launch_broadphase(w->d, sp, s, w->num_sms);
-        swap_contacts(w);
-        cudaEventRecord(t.e[5], s);
         w->inv_dt0 = sp.inv_dt;
     } else {
-        cudaEventRecord(t.e[3], s);
-        cudaEventRecord(t.e[4], s);
-        if (w->auto_clear) launch_clear_forces(w->d, s);
-        cudaEventRecord(t.e[5], s);
+        issue_step(w, sp, dt);
     }
     CUDA_OK(w, cudaGetLastError());
     ++w->steps;
@@ -992,6 +1115,14 @@ int b2g_set_record_pairs(void* p, int32_t flag) {
     return B2G_OK;
 }
 
+int b2g_set_graph_capture(void* p, int32_t flag) {
+    if (!p) return B2G_ERR_INVALID_ARG;
+    World* w = W(p);
+    w->use_graphs = flag != 0;
+    if (!w->use_graphs) drop_graphs(w);
+    return B2G_OK;
+}
+
 int b2g_get_profile(void* p, b2g_profile* out) {
     World* w = W(p);
     if (!w || !out) return B2G_ERR_INVALID_ARG;
@@ -1000,7 +1131,12 @@ int b2g_get_profile(void* p, b2g_profile* out) {
     memset(out, 0, sizeof(*out));
     if (!w->timer.valid || w->steps == 0) return B2G_OK;
     float ms[6] = {0};
-    for (int i = 1; i < 6; ++i) cudaEventElapsedTime(&ms[i], w->timer.e[0], w->timer.e[i]);
+    for (int i = 1; i < 6; ++i) {
+        if (cudaEventElapsedTime(&ms[i], w->timer.e[0], w->timer.e[i]) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(w, B2G_ERR_CUDA, "profile events could not be timed");
+        }
+    }
     out->collide = ms[2] - ms[1];
     out->solve_init = ms[3] - ms[2];
     out->solve_velocity = ms[4] - ms[3];  /* the persistent solver kernel: velocity and position iterations */

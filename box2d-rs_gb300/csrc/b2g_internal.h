@@ -189,6 +189,10 @@ void scan_exclusive_u32(const uint32_t* in, uint32_t* out, const int* d_n, int m
 /* stable LSD radix sort of (key, value) pairs by key bits [0, bits); n from device; result in *_a. */
 void radix_sort_pairs(unsigned long long* key_a, uint32_t* val_a, unsigned long long* key_b, uint32_t* val_b,
                       const int* d_n, int max_n, int bits, uint32_t* hist, cudaStream_t s);
+/* the same sort as one cooperative launch (3 grid barriers per 8-bit pass; inputs of at most
+ * 2048 items are sorted by a single block); uses cnt's barrier words */
+void radix_sort_pairs_coop(unsigned long long* key_a, uint32_t* val_a, unsigned long long* key_b, uint32_t* val_b,
+                           const int* d_n, int max_n, int bits, uint32_t* hist, int* cnt, cudaStream_t s, int num_sms);
 size_t radix_sort_hist_size(int max_n);
 size_t scan_tmp_size(int max_n);
 

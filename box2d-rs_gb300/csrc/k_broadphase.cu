@@ -400,9 +400,11 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
     if (n > 0) {
         k_bp_bounds<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_keys<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
-        radix_sort_pairs(w.bp_key, w.bp_val, w.bp_key_alt, w.bp_val_alt, nullptr, n, 32 + w.morton_world_bits,
-                         w.sort_hist, s);
-        if (n > 1) k_bp_build<<<grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        radix_sort_pairs_coop(w.bp_key, w.bp_val, w.bp_key_alt, w.bp_val_alt, nullptr, n, 32 + w.morton_world_bits,
+                              w.sort_hist, w.cnt, s, num_sms);
+        if (n > 1) {
+            k_bp_build<<<grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        }
         k_bp_leaves<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_refit<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_traverse<<<gf, kBlock, 0, s>>>(w, sp); B2G_LAUNCHED(1);
@@ -410,8 +412,8 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
     }
     k_bp_clamp_new<<<1, 32, 0, s>>>(w); B2G_LAUNCHED(1);
     /* sort new keys; payload = emission slot */
-    radix_sort_pairs(w.n_key, w.n_idx, w.n_key_alt, w.n_idx_alt, &w.cnt[CNT_NEW], w.pair_cap, 2 * w.key_bits,
-                     w.sort_hist, s);
+    radix_sort_pairs_coop(w.n_key, w.n_idx, w.n_key_alt, w.n_idx_alt, &w.cnt[CNT_NEW], w.pair_cap, 2 * w.key_bits,
+                          w.sort_hist, w.cnt, s, num_sms);
     uint32_t* flag = w.scan_tmp;
     uint32_t* rank = w.scan_tmp + w.contact_cap;
     uint32_t* tmp = w.scan_tmp + 2 * (size_t)w.contact_cap;

@@ -13,6 +13,7 @@
  *      the 8 warps in shared memory, so every item's rank preserves input order.
  */
 #include "b2g_internal.h"
+#include "b2g_sync.cuh"
 
 namespace b2g {
 
@@ -188,6 +189,158 @@ __global__ void k_sort_scatter(const unsigned long long* __restrict__ kin, const
     }
 }
 
+/* ---- single-launch cooperative radix sort ---- */
+
+/* Stable scatter of one 2048-item tile given its per-digit output bases in s_base. */
+__device__ void scatter_tile(const unsigned long long* __restrict__ kin, const uint32_t* __restrict__ vin,
+                             unsigned long long* __restrict__ kout, uint32_t* __restrict__ vout, int n, int shift,
+                             int tile_base, const uint32_t* s_base, uint32_t* s_run, uint32_t (*s_warp)[256]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    s_run[threadIdx.x] = 0;
+    for (int w = 0; w < 8; ++w) s_warp[w][threadIdx.x] = 0;
+    __syncthreads();
+    const unsigned lt_mask = (1u << lane) - 1u;
+    for (int r = 0; r < kSortItems; ++r) {
+        const int idx = tile_base + r * kSortBlock + threadIdx.x;
+        const bool valid = idx < n;
+        unsigned long long k = 0;
+        uint32_t v = 0;
+        uint32_t d = 256u + (uint32_t)lane;
+        if (valid) {
+            k = kin[idx];
+            v = vin[idx];
+            d = (uint32_t)(k >> shift) & 255u;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t rank = (uint32_t)__popc(peers & lt_mask);
+        if (valid && (peers & lt_mask) == 0u) s_warp[warp][d] = (uint32_t)__popc(peers);
+        __syncthreads();
+        {
+            const int dd = threadIdx.x;
+            uint32_t run = s_run[dd];
+#pragma unroll
+            for (int w = 0; w < 8; ++w) {
+                uint32_t c = s_warp[w][dd];
+                s_warp[w][dd] = run;
+                run += c;
+            }
+            s_run[dd] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t dst = s_base[d] + s_warp[warp][d] + rank;
+            if (dst < (uint32_t)n) {
+                kout[dst] = k;
+                vout[dst] = v;
+            }
+        }
+        __syncthreads();
+        for (int w = 0; w < 8; ++w) s_warp[w][threadIdx.x] = 0;
+        __syncthreads();
+    }
+}
+
+/* 256-bin histogram of one tile into s_cnt (block-wide) */
+__device__ void tile_histogram(const unsigned long long* __restrict__ keys, int n, int shift, int tile_base, uint32_t* s_cnt) {
+    s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < kSortTile; i += kSortBlock) {
+        const int idx = tile_base + i;
+        if (idx < n) atomicAdd(&s_cnt[(unsigned)(keys[idx] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kSortBlock) k_radix_coop(unsigned long long* ka, uint32_t* va, unsigned long long* kb,
+                                                           uint32_t* vb, const int* d_n, int max_n, int bits,
+                                                           uint32_t* hist, int* cnt) {
+    __shared__ uint32_t s_base[256];
+    __shared__ uint32_t s_run[256];
+    __shared__ uint32_t s_warp[8][256];
+    __shared__ uint32_t s_cnt[256];
+    const int n = load_n(d_n, max_n);
+    const int passes = (bits + 7) / 8;
+    if (n <= 0 || passes <= 0) return;
+    if (n <= kSortTile) {
+        /* one tile: block 0 sorts alone, synchronising with __syncthreads only */
+        if (blockIdx.x != 0) return;
+        unsigned long long *kin = ka, *kout = kb;
+        uint32_t *vin = va, *vout = vb;
+        for (int p = 0; p < passes; ++p) {
+            tile_histogram(kin, n, 8 * p, 0, s_cnt);
+            uint32_t total;
+            const uint32_t ex = block_exclusive_scan(s_cnt[threadIdx.x], &total);
+            s_base[threadIdx.x] = ex;
+            __syncthreads();
+            scatter_tile(kin, vin, kout, vout, n, 8 * p, 0, s_base, s_run, s_warp);
+            __syncthreads();
+            unsigned long long* tk = kin; kin = kout; kout = tk;
+            uint32_t* tv = vin; vin = vout; vout = tv;
+        }
+        if (kin != ka)
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                ka[i] = kin[i];
+                va[i] = vin[i];
+            }
+        return;
+    }
+    const int tiles = (n + kSortTile - 1) / kSortTile;
+    uint32_t* dtot = hist + (size_t)256 * tiles;
+    unsigned long long *kin = ka, *kout = kb;
+    uint32_t *vin = va, *vout = vb;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = 8 * p;
+        /* H: per-tile digit counts, digit-major */
+        for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+            tile_histogram(kin, n, shift, t * kSortTile, s_cnt);
+            hist[threadIdx.x * tiles + t] = s_cnt[threadIdx.x];
+            __syncthreads();
+        }
+        if (!grid_barrier(cnt)) return;
+        /* S: exclusive scan of each digit's column over the tiles; column totals to dtot */
+        for (int d = blockIdx.x; d < 256; d += gridDim.x) {
+            uint32_t* col = hist + (size_t)d * tiles;
+            __shared__ uint32_t carry;
+            if (threadIdx.x == 0) carry = 0;
+            __syncthreads();
+            for (int base = 0; base < tiles; base += blockDim.x) {
+                const int i = base + threadIdx.x;
+                const uint32_t v = i < tiles ? col[i] : 0u;
+                uint32_t total;
+                const uint32_t ex = block_exclusive_scan(v, &total);
+                if (i < tiles) col[i] = carry + ex;
+                __syncthreads();
+                if (threadIdx.x == 0) carry += total;
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) dtot[d] = carry;
+            __syncthreads();
+        }
+        if (!grid_barrier(cnt)) return;
+        /* X: digit bases (each block scans the 256 totals), then stable scatter of its tiles */
+        {
+            uint32_t total;
+            const uint32_t ex = block_exclusive_scan(dtot[threadIdx.x], &total);
+            s_cnt[threadIdx.x] = ex;
+            __syncthreads();
+        }
+        for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+            s_base[threadIdx.x] = s_cnt[threadIdx.x] + hist[threadIdx.x * tiles + t];
+            __syncthreads();
+            scatter_tile(kin, vin, kout, vout, n, shift, t * kSortTile, s_base, s_run, s_warp);
+        }
+        if (!grid_barrier(cnt)) return;
+        unsigned long long* tk = kin; kin = kout; kout = tk;
+        uint32_t* tv = vin; vin = vout; vout = tv;
+    }
+    if (kin != ka) {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+            ka[i] = kin[i];
+            va[i] = vin[i];
+        }
+    }
+}
+
 __global__ void k_copy_pairs(const unsigned long long* __restrict__ kin, const uint32_t* __restrict__ vin,
                              unsigned long long* __restrict__ kout, uint32_t* __restrict__ vout, const int* d_n, int max_n) {
     const int n = load_n(d_n, max_n);
@@ -207,6 +360,21 @@ void scan_exclusive_u32(const uint32_t* in, uint32_t* out, const int* d_n, int m
     k_scan_tiles<<<tiles, kScanBlock, 0, s>>>(in, out, d_n, max_n, tmp); B2G_LAUNCHED(1);
     k_scan_sums<<<1, 1024, 0, s>>>(tmp, tiles, d_total); B2G_LAUNCHED(1);
     k_scan_add<<<tiles, kScanBlock, 0, s>>>(out, d_n, max_n, tmp); B2G_LAUNCHED(1);
+}
+
+void radix_sort_pairs_coop(unsigned long long* key_a, uint32_t* val_a, unsigned long long* key_b, uint32_t* val_b,
+                           const int* d_n, int max_n, int bits, uint32_t* hist, int* cnt, cudaStream_t s, int num_sms) {
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_radix_coop, kSortBlock, 0);
+        if (per_sm < 1) per_sm = 1;
+        if (per_sm > 2) per_sm = 2;
+    }
+    /* one block per SM keeps the grid barrier short; per_sm only guards co-residency */
+    const int blocks = num_sms;
+    void* args[] = {&key_a, &val_a, &key_b, &val_b, (void*)&d_n, &max_n, &bits, &hist, &cnt};
+    cudaLaunchCooperativeKernel((const void*)k_radix_coop, dim3(blocks), dim3(kSortBlock), args, 0, s);
+    B2G_LAUNCHED(1);
 }
 
 size_t radix_sort_hist_size(int max_n) {

@@ -26,9 +26,8 @@
  * The host reference solved in the GPU's colour order (the oracle's ordering hook)
  * gives bit-identical bodies, because each operation is the same IEEE f32 operation.
  */
-#include <cooperative_groups.h>
-
 #include "b2g_internal.h"
+#include "b2g_sync.cuh"
 
 namespace b2g {
 
@@ -39,44 +38,6 @@ constexpr int kBlock = 256;
 __device__ __forceinline__ bool is_dynamic(uint32_t flags) { return (flags & BF_TYPE_MASK) == BODY_DYNAMIC; }
 __device__ __forceinline__ bool is_static(uint32_t flags) { return (flags & BF_TYPE_MASK) == BODY_STATIC; }
 
-/* ---------------- grid barrier with a bounded wait ---------------- */
-__device__ __forceinline__ bool grid_barrier(const DevWorld& w) {
-    /* thread 0 decides for its block and the decision is broadcast through shared memory,
-     * so every thread of a block returns the same value. Once any block has timed out,
-     * later barriers return at once without waiting. */
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        s_ok = (((volatile int*)w.cnt)[CNT_STATUS] & ST_BARRIER_TIMEOUT) == 0;
-    }
-    __syncthreads();
-    if (!s_ok) return false;
-    if (threadIdx.x == 0) {
-        volatile unsigned* vgen = (volatile unsigned*)&w.cnt[CNT_BARRIER + 1];
-        unsigned* count = (unsigned*)&w.cnt[CNT_BARRIER];
-        const unsigned gen = *vgen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(count, 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(count, 0u);
-            __threadfence();
-            atomicAdd((unsigned*)&w.cnt[CNT_BARRIER + 1], 1u);
-        } else {
-            const long long t0 = clock64();
-            while (*vgen == gen) {
-                __nanosleep(64);
-                if (clock64() - t0 > 2000000000LL) { /* ~1 s at 2 GHz; a sweep takes microseconds */
-                    atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_BARRIER_TIMEOUT);
-                    break;
-                }
-            }
-        }
-        __threadfence();
-        s_ok = (((volatile int*)w.cnt)[CNT_STATUS] & ST_BARRIER_TIMEOUT) == 0;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
 
 /* ---------------- islands ---------------- */
 __device__ __forceinline__ int uf_find(int* parent, int x) {
@@ -190,8 +151,11 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w) {
     const int gsize = gridDim.x * blockDim.x;
     const int n = w.cnt[CNT_CONS];
     const unsigned long long kNone = ~0ull;
+    /* offers are double-buffered by round parity: round r offers into buffer r & 1, and the
+     * entries of buffer (r - 1) & 1 are reset during round r, so a round needs two barriers */
     for (int b = gtid; b < w.n_bodies; b += gsize) {
         w.b_cmin[b] = kNone;
+        w.b_cmin[w.body_cap + b] = kNone;
         w.b_cmask[b] = 0ull;
     }
     for (int k = gtid; k < n; k += gsize) w.cons_colour[k] = -1;
@@ -208,13 +172,26 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w) {
     for (;;) {
         const int remaining = ((volatile int*)w.cnt)[CNT_UNCOLOURED + ((round + 1) & 1)];
         if (remaining <= 0) break;
+        if (round >= kMaxColours - kFirstFitColours) {
+            /* cannot happen for rounds bounded by the maximum body degree; keep the kernel finite */
+            for (int k = gtid; k < n; k += gsize)
+                if (w.cons_colour[k] < 0) w.cons_colour[k] = kMaxColours - 1;
+            if (gtid == 0) atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_COLOUR_OVERFLOW);
+            break;
+        }
+        unsigned long long* offer = w.b_cmin + (size_t)(round & 1) * w.body_cap;
+        unsigned long long* stale = w.b_cmin + (size_t)((round + 1) & 1) * w.body_cap;
         /* A: each uncoloured constraint offers its priority to its dynamic bodies */
         for (int k = gtid; k < n; k += gsize) {
-            if (w.cons_colour[k] >= 0) continue;
             const int2 bd = w.c.body[w.cons_contact[k]];
+            if (round > 0) {
+                stale[bd.x] = kNone;
+                stale[bd.y] = kNone;
+            }
+            if (w.cons_colour[k] >= 0) continue;
             const unsigned long long key = ((unsigned long long)hash32((uint32_t)k) << 32) | (uint32_t)k;
-            if (is_dynamic(w.b_flags[bd.x])) atomicMin(&w.b_cmin[bd.x], key);
-            if (is_dynamic(w.b_flags[bd.y])) atomicMin(&w.b_cmin[bd.y], key);
+            if (is_dynamic(w.b_flags[bd.x])) atomicMin(&offer[bd.x], key);
+            if (is_dynamic(w.b_flags[bd.y])) atomicMin(&offer[bd.y], key);
         }
         if (gtid == 0) w.cnt[CNT_UNCOLOURED + (round & 1)] = 0;
         if (!grid_barrier(w)) return;
@@ -224,8 +201,8 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w) {
             const int2 bd = w.c.body[w.cons_contact[k]];
             const unsigned long long key = ((unsigned long long)hash32((uint32_t)k) << 32) | (uint32_t)k;
             const bool da = is_dynamic(w.b_flags[bd.x]), db = is_dynamic(w.b_flags[bd.y]);
-            const bool winA = !da || w.b_cmin[bd.x] == key;
-            const bool winB = !db || w.b_cmin[bd.y] == key;
+            const bool winA = !da || offer[bd.x] == key;
+            const bool winB = !db || offer[bd.y] == key;
             if (winA && winB) {
                 const unsigned long long used = (da ? w.b_cmask[bd.x] : 0ull) | (db ? w.b_cmask[bd.y] : 0ull);
                 int colour;
@@ -246,22 +223,8 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w) {
                 atomicAdd(&w.cnt[CNT_UNCOLOURED + (round & 1)], 1);
             }
         }
-        if (!grid_barrier(w)) return;
-        /* C: reset the offers of every body touched this round */
-        for (int k = gtid; k < n; k += gsize) {
-            const int2 bd = w.c.body[w.cons_contact[k]];
-            w.b_cmin[bd.x] = kNone;
-            w.b_cmin[bd.y] = kNone;
-        }
         ++round;
         if (!grid_barrier(w)) return;
-        if (round >= kMaxColours - kFirstFitColours && ((volatile int*)w.cnt)[CNT_UNCOLOURED + ((round + 1) & 1)] > 0) {
-            /* cannot happen for rounds bounded by the maximum body degree; keep the kernel finite */
-            for (int k = gtid; k < n; k += gsize)
-                if (w.cons_colour[k] < 0) w.cons_colour[k] = kMaxColours - 1;
-            if (gtid == 0) atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_COLOUR_OVERFLOW);
-            break;
-        }
     }
     if (gtid == 0) w.cnt[CNT_ROUNDS] = round;
     /* histogram, dense colour offsets, scatter into slots */
@@ -396,7 +359,7 @@ __device__ void init_slot(const DevWorld& w, const StepParams& sp, int k) {
         if (vRel < -mat.z) bias[j] = -mat.y * vRel;
     }
     int vcount = count;
-    float k11 = 0.0f, k12 = 0.0f, k22 = 0.0f, na = 0.0f, nb = 0.0f, nc = 0.0f, nd = 0.0f;
+    float k11 = 0.0f, k12 = 0.0f, k22 = 0.0f, na = 0.0f, nb = 0.0f, nd = 0.0f;
     if (count == 2) {
         float rn1A = cross(ra[0], normal);
         float rn1B = cross(rb[0], normal);
@@ -411,7 +374,7 @@ __device__ void init_slot(const DevWorld& w, const StepParams& sp, int k) {
             float det = k11 * k22 - k12 * k12;
             if (det != 0.0f) det = fdiv(1.0f, det);
             na = det * k22;      /* ex.x */
-            nc = -det * k12;     /* ex.y */
+            /* ex.y = -det * k12 equals ey.x (K is symmetric) */
             nb = -det * k12;     /* ey.x */
             nd = det * k11;      /* ey.y */
         } else {
@@ -438,7 +401,6 @@ __device__ void init_slot(const DevWorld& w, const StepParams& sp, int k) {
     w.pc_meta[k] = make_float4(rA, rB, __int_as_float(mtype), __int_as_float(count));
     w.vc_island[k] = w.cons_island[w.s_cons[k]];
     w.s_fix[k] = fx;
-    (void)nc;
 }
 
 __device__ __forceinline__ void warm_slot(const DevWorld& w, int k) {
@@ -761,31 +723,30 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
         p.z += h * wv;
         w.b_pos[b] = p;
         w.b_vel[b] = make_float4(vv.x, vv.y, wv, v.w);
-        w.isl_minsep[b] = 0u;
-        w.isl_done[b] = 0;
+        for (int j = 0; j < sp.pi; ++j) w.isl_minsep[(size_t)j * w.body_cap + b] = 0u;
     }
     if (!grid_barrier(w)) return;
-    /* phase 5: position iterations with the per-island early exit (:257-274) */
+    /* phase 5: position iterations with the per-island early exit (:257-274).
+     * Iteration j accumulates max(-separation) of each island into its own buffer j (all
+     * zeroed in phase 4); an island has stopped before iteration `it` if some earlier buffer
+     * shows min separation >= -3 slop. Buffers of finished iterations are complete after the
+     * colour barriers, so no extra barrier per iteration is needed. */
     const float tol = 3.0f * kLinearSlop;
     for (int it = 0; it < sp.pi; ++it) {
-        uint32_t* cur = w.isl_minsep + (size_t)(it & 1) * w.body_cap;
-        uint32_t* nxt = w.isl_minsep + (size_t)((it + 1) & 1) * w.body_cap;
+        uint32_t* cur = w.isl_minsep + (size_t)it * w.body_cap;
         for (int c = 0; c < ncol; ++c) {
             const int beg = w.col_off[c], end = w.col_off[c + 1];
             for (int k = beg + gtid; k < end; k += gsize) {
                 const int isl = w.vc_island[k];
-                if (w.isl_done[isl]) continue;
+                bool done = false;
+                for (int j = 0; j < it && !done; ++j)
+                    done = __uint_as_float(w.isl_minsep[(size_t)j * w.body_cap + isl]) <= tol;
+                if (done) continue;
                 const float ms = solve_position_slot(w, k);
                 if (ms < 0.0f) atomicMax(&cur[isl], __float_as_uint(-ms));
             }
             if (!grid_barrier(w)) return;
         }
-        for (int b = gtid; b < nb; b += gsize) {
-            if (!(w.b_flags[b] & BF_ISLAND) || w.b_island[b] != b) continue;
-            if (!w.isl_done[b] && __uint_as_float(cur[b]) <= tol) w.isl_done[b] = 1;
-            nxt[b] = 0u;
-        }
-        if (!grid_barrier(w)) return;
     }
     /* phase 6a: copy back (synchronize_transform), sleep bookkeeping, clear forces */
     const float linTolSqr = kLinearSleepTolerance * kLinearSleepTolerance;
@@ -820,7 +781,9 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
             const uint32_t f = w.b_flags[b];
             if (!(f & BF_ISLAND)) continue;
             const int r = w.b_island[b];
-            const bool solved = sp.pi > 0 && w.isl_done[r];
+            bool solved = false;  /* position_solved: some iteration ended with min separation >= -3 slop */
+            for (int j = 0; j < sp.pi && !solved; ++j)
+                solved = __uint_as_float(w.isl_minsep[(size_t)j * w.body_cap + r]) <= tol;
             if (solved && w.isl_sleep[r] >= kTimeToSleep) {
                 w.b_flags[b] = f & ~BF_AWAKE;
                 w.b_vel[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);

@@ -87,17 +87,26 @@ def _walls(body, corners, friction):
     return f
 
 
+_ANGLE_COS = np.zeros((9, 8))
+_ANGLE_SIN = np.zeros((9, 8))
+for _n in range(3, 9):
+    for _k in range(_n):
+        _ANGLE_COS[_n, _k] = math.cos(2.0 * math.pi * _k / _n)
+        _ANGLE_SIN[_n, _k] = math.sin(2.0 * math.pi * _k / _n)
+
+
 def _polygon_vertices(rng: SplitMix64, count: int, extents: np.ndarray, nverts: np.ndarray) -> np.ndarray:
-    """Convex n-gons with vertices at angles 2*pi*k/n and radii extent*(0.8..1.0)."""
-    out = np.zeros((count, 8, 2), np.float32)
+    """Convex n-gons with vertices at angles 2*pi*k/n and radii extent*(0.8..1.0).
+
+    The angles come from a table of libm cos/sin values, so the vertices are identical on
+    every machine; unused vertex slots stay zero."""
     jitter = rng.uniform(count * 8, 0.8, 1.0).reshape(count, 8)
-    for i in range(count):
-        n = int(nverts[i])
-        for k in range(n):
-            a = 2.0 * math.pi * k / n
-            r = float(extents[i]) * float(jitter[i, k])
-            out[i, k, 0] = r * math.cos(a)
-            out[i, k, 1] = r * math.sin(a)
+    n = np.asarray(nverts, np.int64).reshape(-1)
+    r = np.asarray(extents, np.float64).reshape(-1, 1) * jitter
+    used = np.arange(8)[None, :] < n[:, None]
+    out = np.zeros((count, 8, 2), np.float32)
+    out[:, :, 0] = np.where(used, r * _ANGLE_COS[n], 0.0)
+    out[:, :, 1] = np.where(used, r * _ANGLE_SIN[n], 0.0)
     return out
 
 

@@ -204,6 +204,11 @@ int b2g_set_contact_events(void* world, int32_t flag);
 int b2g_collide_pairs(const b2g_fixture_def* shape_a, const float* xf_a, const b2g_fixture_def* shape_b,
                       const float* xf_b, int32_t n, b2g_contact_info* out);
 
+/* Run steady-state steps as captured CUDA graphs (on by default). A step is captured once
+ * per contact-buffer parity and replayed while dt, iterations, flags, gravity and the body
+ * and fixture counts stay the same; any change re-captures. */
+int b2g_set_graph_capture(void* world, int32_t flag);
+
 /* ---- parity hooks ---- */
 /* Record every pair the broadphase emits (off by default; needed by b2g_get_pairs). */
 int b2g_set_record_pairs(void* world, int32_t flag);

@@ -66,6 +66,16 @@ int DynamicTree::create_proxy(const AABB& aabb, int user) {
     return id;
 }
 
+int DynamicTree::create_proxy_fat(const AABB& fat, int user) {
+    int id = allocate_node();
+    nodes_[id].aabb = fat;
+    nodes_[id].user = user;
+    nodes_[id].height = 0;
+    nodes_[id].moved = false;
+    insert_leaf(id);
+    return id;
+}
+
 void DynamicTree::destroy_proxy(int id) {
     remove_leaf(id);
     free_node(id);

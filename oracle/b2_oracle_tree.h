@@ -34,6 +34,8 @@ class DynamicTree {
    public:
     DynamicTree();
     int create_proxy(const AABB& aabb, int user);
+    /* state import: insert a leaf whose fat AABB is given as is, not marked moved */
+    int create_proxy_fat(const AABB& fat, int user);
     void destroy_proxy(int id);
     bool move_proxy(int id, const AABB& aabb, Vec2 displacement);
     const AABB& fat_aabb(int id) const { return nodes_[id].aabb; }
@@ -82,6 +84,10 @@ struct Pair {
 class BroadPhase {
    public:
     int create_proxy(const AABB& aabb, int user);
+    int create_proxy_fat(const AABB& fat, int user) {
+        ++proxy_count;
+        return tree.create_proxy_fat(fat, user);
+    }
     void destroy_proxy(int id);
     void move_proxy(int id, const AABB& aabb, Vec2 displacement);
     void touch_proxy(int id) { buffer_move(id); }

@@ -1264,6 +1264,76 @@ int ora_get_events(void* p, b2g_contact_event* out, int cap, int* n) {
     return 0;
 }
 
+/* Replace the world's dynamic state with a snapshot taken after a step of another engine
+ * (the GPU): body poses and velocities, every proxy's fat AABB (empty move buffer), the
+ * contact list with manifolds, impulses and touching flags, and 1/dt of the last step.
+ * Bodies and fixtures must have been created identically beforehand. Contacts are pushed
+ * so that the world list ends up in the given order. */
+int ora_import_state(void* p, const b2g_body_state* bodies, int nb, const float* fat, int nf,
+                     const b2g_contact_info* contacts, int nc, float inv_dt0) {
+    World& w = *(World*)p;
+    if (nb != (int)w.bodies.size() || nf != (int)w.fixtures.size()) return B2G_ERR_INVALID_ARG;
+    for (int i = 0; i < nb; ++i) {
+        Body& b = w.bodies[i];
+        if (b.type == STATIC) continue;
+        const b2g_body_state& s = bodies[i];
+        b.sweep.c = v2(s.world_center.x, s.world_center.y);
+        b.sweep.a = s.angle;
+        b.sweep.c0 = b.sweep.c;
+        b.sweep.a0 = b.sweep.a;
+        b.xf.p = v2(s.position.x, s.position.y);
+        b.xf.q = rot(s.angle);
+        b.v = v2(s.linear_velocity.x, s.linear_velocity.y);
+        b.w = s.angular_velocity;
+        b.force = v2(0, 0);
+        b.torque = 0.0f;
+        b.awake = true;
+        b.sleep_time = 0.0f;
+    }
+    /* broadphase: rebuild the tree with the given fat AABBs in fixture order */
+    w.bp = BroadPhase();
+    w.proxy_to_fixture.clear();
+    for (int f = 0; f < nf; ++f) {
+        Fixture& F = w.fixtures[f];
+        if (F.proxy < 0) continue;
+        AABB a{v2(fat[4 * f], fat[4 * f + 1]), v2(fat[4 * f + 2], fat[4 * f + 3])};
+        F.proxy = w.bp.create_proxy_fat(a, f);
+        if ((int)w.proxy_to_fixture.size() <= F.proxy) w.proxy_to_fixture.resize((size_t)F.proxy + 1, -1);
+        w.proxy_to_fixture[F.proxy] = f;
+    }
+    /* contacts: drop all, then recreate from the snapshot */
+    w.contacts.clear();
+    w.edges.clear();
+    w.free_contacts.clear();
+    w.contact_head = -1;
+    w.contact_count = 0;
+    for (Body& b : w.bodies) b.edge_head = -1;
+    for (int i = nc - 1; i >= 0; --i) {
+        const b2g_contact_info& c = contacts[i];
+        const int fa = (int)c.fixture_a, fb = (int)c.fixture_b;
+        if (fa < 0 || fa >= nf || fb < 0 || fb >= nf) return B2G_ERR_INVALID_ARG;
+        const int before = w.contact_count;
+        add_pair(w, fa, fb);
+        if (w.contact_count == before) return B2G_ERR_INVALID_ARG;  /* rejected by add_pair */
+        Contact& C = w.contacts[w.contact_head];
+        if (C.fa != fa || C.fb != fb) return B2G_ERR_INVALID_ARG;  /* not in primary order */
+        C.touching = c.touching != 0;
+        C.m.type = c.manifold_type;
+        C.m.point_count = c.point_count;
+        C.m.local_normal = v2(c.local_normal.x, c.local_normal.y);
+        C.m.local_point = v2(c.local_point.x, c.local_point.y);
+        for (int j = 0; j < 2; ++j) {
+            C.m.points[j].local_point = v2(c.point_local[j].x, c.point_local[j].y);
+            C.m.points[j].normal_impulse = c.normal_impulse[j];
+            C.m.points[j].tangent_impulse = c.tangent_impulse[j];
+            C.m.points[j].id = c.point_id[j];
+        }
+    }
+    w.inv_dt0 = inv_dt0;
+    w.new_contacts = false;
+    return 0;
+}
+
 /* Shape helpers exposed for known-answer tests (collision_test.rs / math_test.rs). */
 int ora_polygon_mass(const b2g_fixture_def* d, float* out_centroid_mass_center_I) {
     Shape s;

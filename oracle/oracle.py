@@ -67,6 +67,7 @@ def load():
         "ora_polygon_mass": [vp, vp],
         "ora_sincos": [vp, vp, vp, i32],
         "ora_collide": [vp, vp, vp, vp, vp],
+        "ora_import_state": [vp, vp, i32, vp, i32, vp, i32, f32],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -234,3 +235,13 @@ class OracleWorld:
 
     def hook_misses(self):
         return self._lib.ora_get_hook_misses(self._h)
+
+    def import_state(self, bodies, fat_aabbs, contacts, inv_dt0):
+        """Continue from another engine's post-step state (see ora_import_state)."""
+        b = np.ascontiguousarray(bodies, b2g.BODY_STATE)
+        a = np.ascontiguousarray(fat_aabbs, np.float32)
+        c = np.ascontiguousarray(contacts, b2g.CONTACT_INFO)
+        rc = self._lib.ora_import_state(self._h, _ptr(b), len(b), _ptr(a), len(a), _ptr(c), len(c),
+                                        np.float32(inv_dt0))
+        if rc != 0:
+            raise ValueError(f"ora_import_state failed ({rc})")
