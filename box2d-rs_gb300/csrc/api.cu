@@ -25,6 +25,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1339,6 +1340,113 @@ int b2g_collide_pairs(const b2g_fixture_def* da, const float* xfa, const b2g_fix
     cudaFree(d_ids);
     cudaFree(d_kind);
     if (rc != B2G_OK) return rc;
+    for (int i = 0; i < n; ++i) {
+        b2g_contact_info& o = out[i];
+        memset(&o, 0, sizeof(o));
+        o.fixture_a = o.fixture_b = (uint32_t)i;
+        o.manifold_type = (int)(ids[i].z & 0xffu);
+        o.point_count = (int)((ids[i].z >> 8) & 0xffu);
+        o.touching = o.point_count > 0;
+        o.local_normal = b2g_vec2{geo[i].x, geo[i].y};
+        o.local_point = b2g_vec2{geo[i].z, geo[i].w};
+        o.point_local[0] = b2g_vec2{pts[i].x, pts[i].y};
+        o.point_local[1] = b2g_vec2{pts[i].z, pts[i].w};
+        o.point_id[0] = ids[i].x;
+        o.point_id[1] = ids[i].y;
+    }
+    return B2G_OK;
+}
+
+}  // extern "C"
+
+/* ---- allocation-free variant of b2g_collide_pairs ----
+ * For callers that must not allocate (a frame loop with a fixed time budget, where freeing
+ * device memory can wait for the whole device, or a program whose device memory belongs to
+ * its own pool allocator). The kernel is k_collide_pairs; its staging buffers are one fixed
+ * device array below instead of cudaMalloc'd memory, and host-side staging is a fixed array
+ * too, so a call allocates nothing. */
+namespace {
+constexpr int kNoAllocMax = B2G_NOALLOC_MAX_PAIRS;
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+/* byte offsets of the sections inside the scratch array, each 256-byte aligned */
+constexpr size_t kOffShapeA = 0;
+constexpr size_t kOffShapeB = align256(kOffShapeA + sizeof(ShapeRec) * kNoAllocMax);
+constexpr size_t kOffXfA = align256(kOffShapeB + sizeof(ShapeRec) * kNoAllocMax);
+constexpr size_t kOffXfB = align256(kOffXfA + sizeof(float4) * kNoAllocMax);
+constexpr size_t kOffKind = align256(kOffXfB + sizeof(float4) * kNoAllocMax);
+constexpr size_t kOffGeo = align256(kOffKind + sizeof(int) * kNoAllocMax);
+constexpr size_t kOffPts = align256(kOffGeo + sizeof(float4) * kNoAllocMax);
+constexpr size_t kOffIds = align256(kOffPts + sizeof(float4) * kNoAllocMax);
+constexpr size_t kNoAllocBytes = align256(kOffIds + sizeof(uint4) * kNoAllocMax);
+}  // namespace
+
+/* Device scratch of b2g_collide_pairs_noalloc (about 6 MB). Every GPU that loads this library
+ * holds it until the process exits. Host code must not use the symbol as a pointer: its
+ * device address is looked up per device with cudaGetSymbolAddress. */
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+alignas(256) unsigned char g_noalloc_host[kNoAllocBytes]; /* host staging, same layout */
+std::mutex g_noalloc_lock;
+constexpr int kNoAllocDevices = 64;
+void* g_noalloc_dev[kNoAllocDevices] = {}; /* device address of the scratch, per device ordinal */
+}  // namespace
+
+extern "C" {
+
+int b2g_collide_pairs_noalloc(const b2g_fixture_def* da, const float* xfa, const b2g_fixture_def* db,
+                              const float* xfb, int32_t n, b2g_contact_info* out) {
+    if (n < 0 || (n > 0 && (!da || !db || !xfa || !xfb || !out))) return B2G_ERR_INVALID_ARG;
+    if (n > kNoAllocMax) return B2G_ERR_CAPACITY; /* more pairs than the fixed scratch holds */
+    if (n == 0) return B2G_OK;
+    std::lock_guard<std::mutex> guard(g_noalloc_lock);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocDevices) return B2G_ERR_CUDA;
+    if (!g_noalloc_dev[dev]) {
+        /* set-up on the first call on this device (the device is current here) */
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return B2G_ERR_CUDA;
+        g_noalloc_dev[dev] = p;
+    }
+    unsigned char* d = (unsigned char*)g_noalloc_dev[dev];
+    ShapeRec* ha = (ShapeRec*)(g_noalloc_host + kOffShapeA);
+    ShapeRec* hb = (ShapeRec*)(g_noalloc_host + kOffShapeB);
+    float4* hxa = (float4*)(g_noalloc_host + kOffXfA);
+    float4* hxb = (float4*)(g_noalloc_host + kOffXfB);
+    int* hkind = (int*)(g_noalloc_host + kOffKind);
+    for (int i = 0; i < n; ++i) {
+        build_shape(da[i], ha[i]);
+        build_shape(db[i], hb[i]);
+        const int ta = da[i].shape_type, tb = db[i].shape_type;
+        if (ta == B2G_SHAPE_CIRCLE && tb == B2G_SHAPE_CIRCLE) hkind[i] = KIND_CIRCLES;
+        else if (ta == B2G_SHAPE_POLYGON && tb == B2G_SHAPE_CIRCLE) hkind[i] = KIND_POLYGON_CIRCLE;
+        else if (ta == B2G_SHAPE_POLYGON && tb == B2G_SHAPE_POLYGON) hkind[i] = KIND_POLYGONS;
+        else if (ta == B2G_SHAPE_EDGE && tb == B2G_SHAPE_CIRCLE) hkind[i] = KIND_EDGE_CIRCLE;
+        else if (ta == B2G_SHAPE_EDGE && tb == B2G_SHAPE_POLYGON) hkind[i] = KIND_EDGE_POLYGON;
+        else return B2G_ERR_INVALID_ARG;
+        const Rot qa = rot(xfa[3 * i + 2]), qb = rot(xfb[3 * i + 2]);
+        hxa[i] = make_float4(xfa[3 * i], xfa[3 * i + 1], qa.s, qa.c);
+        hxb[i] = make_float4(xfb[3 * i], xfb[3 * i + 1], qb.s, qb.c);
+    }
+    /* every element the kernel reads is written by these copies, and it writes every output
+     * element it is asked for, so nothing left over from an earlier call is ever read */
+    const size_t sizes[5] = {sizeof(ShapeRec), sizeof(ShapeRec), sizeof(float4), sizeof(float4), sizeof(int)};
+    const size_t offs[5] = {kOffShapeA, kOffShapeB, kOffXfA, kOffXfB, kOffKind};
+    for (int k = 0; k < 5; ++k)
+        if (cudaMemcpy(d + offs[k], g_noalloc_host + offs[k], sizes[k] * n, cudaMemcpyHostToDevice) != cudaSuccess)
+            return B2G_ERR_CUDA;
+    launch_collide_pairs((const ShapeRec*)(d + kOffShapeA), (const float4*)(d + kOffXfA),
+                         (const ShapeRec*)(d + kOffShapeB), (const float4*)(d + kOffXfB), (const int*)(d + kOffKind),
+                         n, (float4*)(d + kOffGeo), (float4*)(d + kOffPts), (uint4*)(d + kOffIds), 0);
+    if (cudaGetLastError() != cudaSuccess) return B2G_ERR_CUDA;
+    const size_t osz[3] = {sizeof(float4), sizeof(float4), sizeof(uint4)};
+    const size_t ooff[3] = {kOffGeo, kOffPts, kOffIds};
+    for (int k = 0; k < 3; ++k)
+        if (cudaMemcpy(g_noalloc_host + ooff[k], d + ooff[k], osz[k] * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return B2G_ERR_CUDA;
+    const float4* geo = (const float4*)(g_noalloc_host + kOffGeo);
+    const float4* pts = (const float4*)(g_noalloc_host + kOffPts);
+    const uint4* ids = (const uint4*)(g_noalloc_host + kOffIds);
     for (int i = 0; i < n; ++i) {
         b2g_contact_info& o = out[i];
         memset(&o, 0, sizeof(o));

@@ -209,6 +209,23 @@ int b2g_collide_pairs(const b2g_fixture_def* shape_a, const float* xf_a, const b
  * and fixture counts stay the same; any change re-captures. */
 int b2g_set_graph_capture(void* world, int32_t flag);
 
+/* The same stand-alone manifolds as b2g_collide_pairs, for callers that must not allocate
+ * memory: a frame loop with a fixed time budget (freeing device memory can wait for the whole
+ * device) or a host program whose device memory is owned by its own pool allocator. It calls
+ * no cudaMalloc/cudaFree and no host heap allocation; its staging buffers are fixed arrays
+ * inside the library, sized for at most B2G_NOALLOC_MAX_PAIRS pairs (about 6 MB of device
+ * memory that every GPU using the library keeps until the process exits).
+ *   - n > B2G_NOALLOC_MAX_PAIRS returns B2G_ERR_CAPACITY and does nothing.
+ *   - The first call on a device looks up the device address of the scratch array; make
+ *     that first call before any stream capture.
+ *   - All calls share the one scratch array. The function holds a process-wide lock and
+ *     returns only after its results are copied back, because two calls running on the GPU
+ *     at the same time would overwrite each other's data.
+ * It has no counterpart in the reference. */
+#define B2G_NOALLOC_MAX_PAIRS 16384
+int b2g_collide_pairs_noalloc(const b2g_fixture_def* shape_a, const float* xf_a, const b2g_fixture_def* shape_b,
+                              const float* xf_b, int32_t n, b2g_contact_info* out);
+
 /* ---- parity hooks ---- */
 /* Record every pair the broadphase emits (off by default; needed by b2g_get_pairs). */
 int b2g_set_record_pairs(void* world, int32_t flag);
