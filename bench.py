@@ -181,6 +181,75 @@ def run_cpu_on_snapshots(scene, snaps, budget_s=24.0):
                       f"steps@step-index {', '.join(where)}; {total_s:.1f} s"}
 
 
+def timed_steps(world, scene, steps, flush, torch):
+    """Sum of per-step device times (CUDA events on the world's stream), L2 flushed between steps."""
+    total = 0.0
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        world.step(scene["dt"], scene["vi"], scene["pi"])
+        total += world.get_profile()["step"]
+    return total
+
+
+def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_bucket=6):
+    """Batched uneven worlds: one world batch stepped together vs. the same worlds stepped one
+    at a time. The sequential time is the sum over all worlds of each world's mean step time,
+    estimated from `per_bucket` worlds of every log2 size bucket, each timed over the same
+    steps as the batch."""
+    scene = scenes.batched(num_worlds=num_worlds, steps=steps)
+    w = b2g.B2world(gravity=scene["gravity"], num_worlds=num_worlds, device=device)
+    w.set_allow_sleeping(False)
+    scenes.build_world(w, scene)
+    for _ in range(warmup):
+        w.step(scene["dt"], scene["vi"], scene["pi"])
+    w.synchronize()
+    batch_ms = timed_steps(w, scene, steps, flush, torch)
+    counts = w.get_counts()
+    w.close()
+    sizes = scene["world_body_counts"]
+    bucket = np.floor(np.log2(sizes)).astype(int)
+    bodies, fixtures = scene["bodies"], scene["fixtures"]
+    world_of_body = bodies["world_index"]
+    est_ms, sampled = 0.0, []
+    for b in np.unique(bucket):
+        members = np.nonzero(bucket == b)[0]
+        pick = members[np.linspace(0, len(members) - 1, min(per_bucket, len(members))).astype(int)]
+        ms = []
+        for wi in pick:
+            bidx = np.nonzero(world_of_body == wi)[0]
+            remap = np.full(len(bodies), -1, np.int64)
+            remap[bidx] = np.arange(len(bidx))
+            fidx = np.nonzero(remap[fixtures["body"]] >= 0)[0]
+            bd = bodies[bidx].copy()
+            bd["world_index"] = 0
+            fx = fixtures[fidx].copy()
+            fx["body"] = remap[fx["body"]]
+            single = b2g.B2world(gravity=scene["gravity"], device=device)
+            single.set_allow_sleeping(False)
+            single.create_bodies(bd)
+            single.create_fixtures(fx)
+            sub = dict(scene, bodies=bd, fixtures=fx)
+            for _ in range(warmup):
+                single.step(scene["dt"], scene["vi"], scene["pi"])
+            single.synchronize()
+            ms.append(timed_steps(single, sub, steps, flush, torch) / steps)
+            single.close()
+        est_ms += len(members) * float(np.mean(ms)) * steps
+        sampled.append({"bodies": f"{2 ** b}-{2 ** (b + 1) - 1}", "worlds": int(len(members)),
+                        "sampled": int(len(pick)), "ms_per_step": float(np.mean(ms))})
+    batched = num_worlds * steps / (batch_ms / 1e3)
+    sequential = num_worlds * steps / (est_ms / 1e3)
+    return {"metric": "world-steps/s, 4096 uneven worlds (16-2048 bodies)", "value": batched,
+            "unit": "world-steps/s", "body_steps_per_s": scene["n_dynamic"] * steps / (batch_ms / 1e3),
+            "bodies": scene["n_dynamic"], "steps": steps, "ms_per_step": batch_ms / steps,
+            "sequential_single_world_gpu": {"value": sequential, "unit": "world-steps/s",
+                                            "estimate": "sum over worlds of the mean per-step time of sampled worlds "
+                                                        "in the same log2 size bucket", "buckets": sampled},
+            "speedup_vs_sequential": batched / sequential, "contacts_last_step": counts["contacts"],
+            "l2": "256 MiB flush between timed steps"}
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -198,6 +267,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the 100k bodies (testing only)")
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels directly instead of CUDA graphs")
+    ap.add_argument("--batched-steps", type=int, default=300, help="steps of the 4096-world leg (0 skips it)")
     args = ap.parse_args()
     rank, world_size, local_rank = dist_info()
     n_half = int(50_000 * args.scale)
@@ -248,6 +318,7 @@ def main():
     launches0 = w._lib.b2g_get_launch_count()
     total_ms = 0.0
     phase_ms = {"collide": 0.0, "solve_init": 0.0, "solve_velocity": 0.0, "broadphase": 0.0}
+    fine_ms = dict.fromkeys(b2g.B2world.PHASES, 0.0)
     snap_at = set(int(x) for x in np.linspace(0, args.steps - 1, 4)) if rank == 0 and not args.no_cpu_baseline else set()
     snaps = []
     for k in range(args.steps):
@@ -258,6 +329,8 @@ def main():
         total_ms += p["step"]
         for ph in phase_ms:
             phase_ms[ph] += p[ph]
+        for ph, v in w.get_phase_times().items():
+            fine_ms[ph] += v
         if k in snap_at:  # outside the timed events: the state after this step
             snaps.append((args.warmup + k + 1, snapshot(w)))
     launches = w._lib.b2g_get_launch_count() - launches0
@@ -310,10 +383,12 @@ def main():
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel_phase": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None},
-        "phase_ms_per_step": {k: v / args.steps for k, v in ms_phase.items()},
+        "phase_ms_per_step": {k: v / args.steps for k, v in fine_ms.items()},
         "counts_last_step": counts,
         "clocks": clocks,
     }
+    if args.batched_steps > 0:
+        line["batched"] = run_batched(torch, flush, local_rank, steps=args.batched_steps, warmup=args.warmup)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = run_cpu_on_snapshots(scene, snaps)
     if rank == 0:

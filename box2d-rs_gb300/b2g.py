@@ -316,6 +316,7 @@ def load_library(path=LIB_PATH):
         "b2g_set_contact_events": [vp, i32],
         "b2g_set_record_pairs": [vp, i32],
         "b2g_set_graph_capture": [vp, i32],
+        "b2g_get_phase_times": [vp, vp, i32],
         "b2g_version": [],
     }
     for name, args in sig.items():
@@ -486,6 +487,14 @@ class B2world:
         p = Profile()
         self._check(self._lib.b2g_get_profile(self._h, ctypes.byref(p)))
         return p.as_dict()
+
+    PHASES = ("initial_broadphase", "collide", "islands", "colouring", "solver", "broadphase_tree", "contact_merge")
+
+    def get_phase_times(self):
+        """Device milliseconds of the last step's phases (see b2g_get_phase_times)."""
+        out = np.zeros(7, np.float32)
+        self._check(self._lib.b2g_get_phase_times(self._h, _ptr(out), 7))
+        return dict(zip(self.PHASES, map(float, out)))
 
     def get_counts(self):
         c = Counts()

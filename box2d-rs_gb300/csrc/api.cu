@@ -648,17 +648,20 @@ void issue_step(World* w, const StepParams& sp, float dt, bool capturing = false
     mark(t.e[2]);
     if (dt > 0.0f) {
         launch_islands_and_constraints(w->d, sp, s);
+        mark(t.e[6]);
         launch_colouring(w->d, s, w->num_sms);
         mark(t.e[3]);
         launch_solver(w->d, sp, s, w->num_sms);
         mark(t.e[4]);
-        launch_broadphase(w->d, sp, s, w->num_sms);
+        launch_broadphase(w->d, sp, s, w->num_sms, [&]() { mark(t.e[7]); });
         swap_contacts(w);
         mark(t.e[5]);
         w->inv_dt0 = sp.inv_dt;
     } else {
+        mark(t.e[6]);
         mark(t.e[3]);
         mark(t.e[4]);
+        mark(t.e[7]);
         if (w->auto_clear) launch_clear_forces(w->d, s);
         mark(t.e[5]);
     }
@@ -1146,6 +1149,27 @@ int b2g_get_profile(void* p, b2g_profile* out) {
     out->solve = ms[5] - ms[2];
     out->step = ms[5];
     out->solve_toi = 0.0f;
+    return B2G_OK;
+}
+
+int b2g_get_phase_times(void* p, float* out, int32_t n) {
+    World* w = W(p);
+    if (!w || !out || n < 7) return B2G_ERR_INVALID_ARG;
+    int rc = check_status(w);
+    if (rc != B2G_OK) return rc;
+    for (int i = 0; i < 7; ++i) out[i] = 0.0f;
+    if (!w->timer.valid || w->steps == 0) return B2G_OK;
+    /* event order within a step: 0 start, 1 after the initial broadphase, 2 after collide,
+     * 6 after islands, 3 after colouring, 4 after the solver, 7 after the tree pass, 5 end */
+    const int order[8] = {0, 1, 2, 6, 3, 4, 7, 5};
+    float t[8] = {0};
+    for (int i = 1; i < 8; ++i) {
+        if (cudaEventElapsedTime(&t[i], w->timer.e[order[0]], w->timer.e[order[i]]) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(w, B2G_ERR_CUDA, "profile events could not be timed");
+        }
+    }
+    for (int i = 0; i < 7; ++i) out[i] = t[i + 1] - t[i];
     return B2G_OK;
 }
 

@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
+
 #include "b2g_collide.cuh"
 
 namespace b2g {
@@ -177,7 +179,10 @@ void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s);
 void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cudaStream_t s);
 void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms);
 int launch_solver(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms);
-void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms);
+/* after_tree (optional) is called between the tree pass (keys, sort, build, refit, traverse)
+ * and the contact merge, so the caller can record a profiling event there */
+void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms,
+                       const std::function<void()>& after_tree = nullptr);
 void launch_set_transform(const DevWorld& w, int body, float px, float py, float angle, cudaStream_t s);
 void launch_clear_forces(const DevWorld& w, cudaStream_t s);
 void launch_collide_pairs(const ShapeRec* a, const float4* xa, const ShapeRec* b, const float4* xb, const int* kind,

@@ -393,7 +393,8 @@ __global__ void k_merge_finish(DevWorld w) {
 }  // namespace
 
 /* Runs update_pairs + add_pair and merges: the caller swaps w.c and w.c_alt afterwards. */
-void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms) {
+void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms,
+                       const std::function<void()>& after_tree) {
     const int n = w.n_fixtures;
     const int gf = grid_for(n, kBlock, num_sms * 8);
     k_bp_init<<<grid_for(w.num_worlds, kBlock, 64), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
@@ -411,6 +412,7 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
         k_bp_clear_moved<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
     }
     k_bp_clamp_new<<<1, 32, 0, s>>>(w); B2G_LAUNCHED(1);
+    if (after_tree) after_tree();
     /* sort new keys; payload = emission slot */
     radix_sort_pairs_coop(w.n_key, w.n_idx, w.n_key_alt, w.n_idx_alt, &w.cnt[CNT_NEW], w.pair_cap, 2 * w.key_bits,
                           w.sort_hist, w.cnt, s, num_sms);

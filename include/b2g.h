@@ -188,6 +188,10 @@ int b2g_clear_forces(void* world);
 /* ---- introspection ---- */
 int b2g_get_profile(void* world, b2g_profile* out);       /* B2world::get_profile, src/b2_world.rs:268-270 */
 int b2g_get_counts(void* world, b2g_counts* out);         /* get_body_count / get_contact_count / get_proxy_count */
+/* Device times (ms, CUDA events) of the last step's phases, n >= 7: initial broadphase (only
+ * after fixtures were added), collide, islands + constraint list, colouring, solver kernel,
+ * broadphase tree pass (keys, sort, hierarchy, traversal), contact merge. */
+int b2g_get_phase_times(void* world, float* out, int32_t n);
 int b2g_get_contacts(void* world, b2g_contact_info* out, int32_t capacity, int32_t* out_count);
 /* begin/end events produced since the previous call (B2contactListener, src/b2_world_callbacks.rs:68-104) */
 int b2g_get_events(void* world, b2g_contact_event* out, int32_t capacity, int32_t* out_count);
