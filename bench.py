@@ -250,6 +250,62 @@ def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_
             "l2": "256 MiB flush between timed steps"}
 
 
+def _stack_loss_grad(world, scene):
+    """dL/d(final state) of L = sum over worlds of |centre of mass of the stack - target|^2."""
+    st = world.get_body_states()
+    d = np.zeros(world.body_count, b2g.BODY_STATE)
+    stacks = scene.get("stacks", [scene.get("stack")])
+    targets = scene.get("targets", [scene.get("target")])
+    for stack, target in zip(stacks, targets):
+        com = st["world_center"][stack].astype(np.float64).mean(0)
+        d["world_center"][stack] = 2.0 * (com - target) / len(stack)
+    return d
+
+
+def run_adjoint(torch, flush, device, steps=240, seeds=512, repeats=3):
+    """Differentiable throw-and-stack (64 boxes + a circle projectile, loss = squared distance of the
+    stack's centre of mass from a target after `steps` steps): device time of the plain forward
+    steps, of the same steps while recording the tape, and wall time of the backward pass over
+    the tape (checkpoints every 16 steps, solver iterations recomputed); one world, and `seeds`
+    worlds stepped as one batch."""
+    out = {"workload": f"throw-and-stack: 8x8 boxes (half 0.25 m) + circle r 0.5 m, {steps} steps, dt 1/60, "
+                       "8/3 iterations, checkpoint every 16 steps"}
+    for name, scene in (("single_world", scenes.throw_stack(steps=steps)),
+                        (f"batched_{seeds}_worlds", scenes.throw_stack_batch(seeds=seeds, steps=steps))):
+        def fresh():
+            w = b2g.B2world(gravity=scene["gravity"], num_worlds=scene["num_worlds"], device=device)
+            w.set_allow_sleeping(False)
+            scenes.build_world(w, scene)
+            return w
+
+        w = fresh()
+        fwd_ms = timed_steps(w, scene, steps, flush, torch)
+        w.close()
+        w = fresh()
+        w.tape_begin(steps)
+        taped_ms = timed_steps(w, scene, steps, flush, torch)
+        w.tape_end()
+        d_final = _stack_loss_grad(w, scene)
+        times = []
+        for _ in range(repeats):  # the first call also allocates the work buffers
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            w.backward(d_final)
+            times.append(time.perf_counter() - t0)
+        info = w.tape_info()
+        w.close()
+        bwd_ms = 1e3 * min(times[1:] if len(times) > 1 else times)
+        out[name] = {"worlds": int(scene["num_worlds"]), "dynamic_bodies": int(scene["n_dynamic"]),
+                     "forward_ms_per_step": fwd_ms / steps, "taped_forward_ms_per_step": taped_ms / steps,
+                     "backward_ms_per_step": bwd_ms / steps,
+                     "backward_over_forward": bwd_ms / fwd_ms,
+                     "taped_forward_plus_backward_over_forward": (taped_ms + bwd_ms) / fwd_ms,
+                     "tape_slots": info["slots"], "device_bytes": info["device_bytes"],
+                     "replay_mismatches": info["replay_mismatches"]}
+    return out
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -268,6 +324,7 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the 100k bodies (testing only)")
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels directly instead of CUDA graphs")
     ap.add_argument("--batched-steps", type=int, default=300, help="steps of the 4096-world leg (0 skips it)")
+    ap.add_argument("--adjoint-steps", type=int, default=240, help="steps of the differentiable leg (0 skips it)")
     args = ap.parse_args()
     rank, world_size, local_rank = dist_info()
     n_half = int(50_000 * args.scale)
@@ -389,6 +446,8 @@ def main():
     }
     if args.batched_steps > 0:
         line["batched"] = run_batched(torch, flush, local_rank, steps=args.batched_steps, warmup=args.warmup)
+    if args.adjoint_steps > 0:
+        line["adjoint"] = run_adjoint(torch, flush, local_rank, steps=args.adjoint_steps)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = run_cpu_on_snapshots(scene, snaps)
     if rank == 0:

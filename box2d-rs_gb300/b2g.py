@@ -137,6 +137,64 @@ CONTACT_INFO = np.dtype(
 
 EVENT = np.dtype([("kind", "<i4"), ("fixture_a", "<u4"), ("fixture_b", "<u4")])
 
+# b2g_tape_slot / b2g_tape_step (include/b2g.h)
+TAPE_SLOT = np.dtype(
+    [
+        ("body_a", "<i4"),
+        ("body_b", "<i4"),
+        ("count_type_flags", "<i4"),
+        ("colour", "<i4"),
+        ("local_normal", "<f4", (2,)),
+        ("local_point", "<f4", (2,)),
+        ("points", "<f4", (4,)),
+        ("inv_mass", "<f4", (2,)),
+        ("inv_inertia", "<f4", (2,)),
+        ("local_center_a", "<f4", (2,)),
+        ("local_center_b", "<f4", (2,)),
+        ("friction", "<f4"),
+        ("restitution", "<f4"),
+        ("restitution_threshold", "<f4"),
+        ("tangent_speed", "<f4"),
+        ("radius", "<f4", (2,)),
+        ("island", "<i4"),
+        ("position_iterations", "<i4"),
+        ("impulses", "<f4", (4,)),
+        ("carry", "<i4", (2,)),
+        ("ids", "<u4", (2,)),
+    ]
+)
+TAPE_STEP = np.dtype(
+    [
+        ("dt", "<f4"),
+        ("dt_ratio", "<f4"),
+        ("gravity", "<f4", (2,)),
+        ("velocity_iterations", "<i4"),
+        ("position_iterations", "<i4"),
+        ("warm_starting", "<i4"),
+        ("num_slots", "<i4"),
+        ("slot_offset", "<i8"),
+        ("num_colours", "<i4"),
+        ("num_contacts", "<i4"),
+    ]
+)
+assert TAPE_SLOT.itemsize == 144 and TAPE_STEP.itemsize == 48
+
+
+class TapeInfo(ctypes.Structure):
+    _fields_ = [
+        ("recording", ctypes.c_int32),
+        ("steps", ctypes.c_int32),
+        ("slots", ctypes.c_int64),
+        ("checkpoint_interval", ctypes.c_int32),
+        ("valid", ctypes.c_int32),
+        ("device_bytes", ctypes.c_int64),
+        ("replay_mismatches", ctypes.c_uint32),
+        ("pad", ctypes.c_int32),
+    ]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_ if n != "pad"}
+
 
 class Profile(ctypes.Structure):
     _fields_ = [
@@ -295,6 +353,7 @@ def load_library(path=LIB_PATH):
         "b2g_step": [vp, f32, i32, i32],
         "b2g_synchronize": [vp],
         "b2g_get_body_states": [vp, u32, u32, vp],
+        "b2g_get_mass_data": [vp, u32, u32, vp],
         "b2g_set_transform": [vp, u32, Vec2, f32],
         "b2g_set_linear_velocity": [vp, u32, Vec2],
         "b2g_set_angular_velocity": [vp, u32, f32],
@@ -317,6 +376,12 @@ def load_library(path=LIB_PATH):
         "b2g_set_record_pairs": [vp, i32],
         "b2g_set_graph_capture": [vp, i32],
         "b2g_get_phase_times": [vp, vp, i32],
+        "b2g_tape_begin": [vp, i32, i32, ctypes.c_int64],
+        "b2g_tape_end": [vp],
+        "b2g_tape_info_get": [vp, ctypes.POINTER(TapeInfo)],
+        "b2g_backward": [vp, vp, vp],
+        "b2g_tape_get_step": [vp, i32, vp, vp, vp, i32],
+        "b2g_tape_get_checkpoint": [vp, i32, vp, u32],
         "b2g_version": [],
     }
     for name, args in sig.items():
@@ -434,6 +499,14 @@ class B2world:
         self._check(self._lib.b2g_get_body_states(self._h, first, count, _ptr(out)))
         return out
 
+    def get_mass_data(self, first=0, count=None):
+        """(n, 6) float32: mass, 1/mass, inertia about the centre, its inverse, local centre x, y."""
+        if count is None:
+            count = self.body_count - first
+        out = np.zeros((count, 6), np.float32)
+        self._check(self._lib.b2g_get_mass_data(self._h, first, count, _ptr(out)))
+        return out
+
     def set_transform(self, body, position, angle):
         self._check(self._lib.b2g_set_transform(self._h, body, Vec2(*position), angle))
 
@@ -522,6 +595,44 @@ class B2world:
 
     def get_solver_order(self):
         return self._get_list(self._lib.b2g_get_solver_order, np.uint32, 65536, 2).reshape(-1, 2)
+
+    # ---- differentiable step ----
+    def tape_begin(self, max_steps, checkpoint_interval=16, max_slots=0):
+        """Record the next steps for backward() (sleeping must be off)."""
+        self._check(self._lib.b2g_tape_begin(self._h, int(max_steps), int(checkpoint_interval), int(max_slots)))
+
+    def tape_end(self):
+        self._check(self._lib.b2g_tape_end(self._h))
+
+    def tape_info(self):
+        t = TapeInfo()
+        self._check(self._lib.b2g_tape_info_get(self._h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def backward(self, d_final):
+        """dL/d(initial state) from dL/d(final state), both BODY_STATE arrays over all bodies."""
+        d_final = np.ascontiguousarray(d_final, dtype=BODY_STATE)
+        if d_final.shape != (self.body_count,):
+            raise ValueError("d_final must hold one BODY_STATE per body")
+        out = np.zeros(self.body_count, BODY_STATE)
+        self._check(self._lib.b2g_backward(self._h, _ptr(d_final), _ptr(out)))
+        return out
+
+    def tape_step(self, step):
+        """(step parameters, colour offsets, slots) of one taped step."""
+        info = np.zeros(1, TAPE_STEP)
+        self._check(self._lib.b2g_tape_get_step(self._h, int(step), _ptr(info), None, None, 0))
+        ns, nc = int(info["num_slots"][0]), int(info["num_colours"][0])
+        col = np.zeros(nc + 1, np.int32)
+        slots = np.zeros(max(ns, 1), TAPE_SLOT)
+        self._check(self._lib.b2g_tape_get_step(self._h, int(step), _ptr(info), _ptr(col), _ptr(slots), ns))
+        return info[0], col, slots[:ns]
+
+    def tape_checkpoint(self, index):
+        """(n, 8) float32: centre x, y, angle, -, vx, vy, w, - per body; index -1 is the final state."""
+        out = np.zeros((self.body_count, 8), np.float32)
+        self._check(self._lib.b2g_tape_get_checkpoint(self._h, int(index), _ptr(out), self.body_count))
+        return out
 
     def get_proxies(self):
         n = self.fixture_count

@@ -31,6 +31,7 @@
 
 #include "../../include/b2g.h"
 #include "b2g_internal.h"
+#include "b2g_tape.h"
 
 using namespace b2g;
 
@@ -54,6 +55,26 @@ struct GraphSlot {
     cudaGraphExec_t exec = nullptr;
     unsigned long long kernels = 0;  /* kernel nodes in the graph */
     GraphKey key{};
+};
+
+/* The step tape of a world and the work buffers of its last backward pass. */
+struct TapeHost {
+    bool recording = false;
+    bool valid = true;
+    TapeDev d{};
+    std::vector<void*> mem;
+    int step_cap = 0;
+    long long slot_cap = 0;
+    int ckpt_every = 16;
+    int steps = 0;                 /* steps with dt > 0 issued while recording */
+    int n_bodies = 0;
+    size_t bytes = 0;
+    /* backward work buffers and the sizes they were made for */
+    AdjWork work{};
+    std::vector<void*> work_mem;
+    size_t work_bytes = 0;
+    int work_slots = 0, work_vi = 0, work_pi = 0;
+    unsigned mismatches = 0;
 };
 
 struct World {
@@ -95,7 +116,29 @@ struct World {
     int swaps = 0;
     int alloc_generation = 0;
     int minsep_buffers = 2;  /* position-iteration separation buffers held in d.isl_minsep */
+    TapeHost* tape = nullptr;
 };
+
+/* an edit between taped steps that the tape cannot represent */
+void tape_touch(World* w) {
+    if (w->tape && w->tape->recording) w->tape->valid = false;
+}
+
+void tape_free_work(TapeHost* t) {
+    for (void* p : t->work_mem) cudaFree(p);
+    t->work_mem.clear();
+    t->work_bytes = 0;
+    t->work_slots = t->work_vi = t->work_pi = 0;
+}
+
+void tape_free(World* w) {
+    if (!w->tape) return;
+    cudaStreamSynchronize(w->stream);
+    for (void* p : w->tape->mem) cudaFree(p);
+    tape_free_work(w->tape);
+    delete w->tape;
+    w->tape = nullptr;
+}
 
 void drop_graphs(World* w) {
     for (GraphSlot& g : w->graphs) {
@@ -650,8 +693,11 @@ void issue_step(World* w, const StepParams& sp, float dt, bool capturing = false
         launch_islands_and_constraints(w->d, sp, s);
         mark(t.e[6]);
         launch_colouring(w->d, s, w->num_sms);
+        const bool taping = w->tape && w->tape->recording;
+        if (taping) launch_tape_record(w->d, w->tape->d, sp, s, w->num_sms);
         mark(t.e[3]);
         launch_solver(w->d, sp, s, w->num_sms);
+        if (taping) launch_tape_post(w->d, w->tape->d, sp, s, w->num_sms);
         mark(t.e[4]);
         launch_broadphase(w->d, sp, s, w->num_sms, [&]() { mark(t.e[7]); });
         swap_contacts(w);
@@ -691,6 +737,10 @@ int step(World* w, float dt, int vi, int pi) {
     rc = ensure_minsep_buffers(w, pi);
     if (rc != B2G_OK) return rc;
     w->device_authoritative = true;
+    if (w->tape && w->tape->recording) {
+        if (dt > 0.0f) ++w->tape->steps;
+        else w->tape->valid = false;  /* a collide-only step re-matches impulses outside the tape */
+    }
     StepParams sp = make_params(w, dt, vi, pi);
     cudaStream_t s = w->stream;
     Timer& t = w->timer;
@@ -711,7 +761,7 @@ int step(World* w, float dt, int vi, int pi) {
         key.vi = vi;
         key.pi = pi;
         key.flags = sp.warm | (sp.allow_sleep << 1) | (sp.auto_clear << 2) | (sp.record_events << 3) |
-                    (sp.record_pairs << 4);
+                    (sp.record_pairs << 4) | ((w->tape && w->tape->recording) ? (1 << 5) : 0);
         key.generation = w->alloc_generation;
         key.n_bodies = w->d.n_bodies;
         key.n_fixtures = w->d.n_fixtures;
@@ -803,6 +853,7 @@ __global__ void k_body_op(DevWorld d, int op, int b, float x, float y, float z, 
 
 int body_op(World* w, int op, uint32_t b, float x, float y, float z, float px, float py, int wake) {
     if (b >= w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body id out of range");
+    tape_touch(w);
     if (w->device_authoritative) {
         int rc = prepare(w);
         if (rc != B2G_OK) return rc;
@@ -881,6 +932,7 @@ int b2g_world_destroy(void* p) {
     World* w = W(p);
     if (!w) return B2G_ERR_INVALID_ARG;
     cudaStreamSynchronize(w->stream);
+    tape_free(w);
     free_all(w);
     if (w->timer.valid)
         for (auto& e : w->timer.e) cudaEventDestroy(e);
@@ -902,6 +954,7 @@ int b2g_create_bodies(void* p, const b2g_body_def* defs, int32_t n, uint32_t* id
         if (!(d.linear_damping >= 0.0f) || !(d.angular_damping >= 0.0f))
             return fail(w, B2G_ERR_INVALID_ARG, "damping must be >= 0");
     }
+    if (n > 0) tape_touch(w);
     if (w->device_authoritative) {
         int rc = download_state(w);
         if (rc != B2G_OK) return rc;
@@ -944,6 +997,7 @@ int b2g_create_fixtures(void* p, const b2g_fixture_def* defs, int32_t n, uint32_
         if (!(d.density >= 0.0f) || !(d.friction >= 0.0f) || !(d.restitution >= 0.0f))
             return fail(w, B2G_ERR_INVALID_ARG, "density, friction and restitution must be >= 0");
     }
+    if (n > 0) tape_touch(w);
     if (w->device_authoritative) {
         int rc = download_state(w);
         if (rc != B2G_OK) return rc;
@@ -1029,11 +1083,43 @@ int b2g_get_body_states(void* p, uint32_t first, uint32_t count, b2g_body_state*
     return B2G_OK;
 }
 
+/* B2body::get_mass_data / get_local_center (src/b2_body.rs): per body mass, 1/mass, rotational
+ * inertia about the centre of mass (m_I; get_inertia adds mass * |local centre|^2), its inverse,
+ * local centre x, y. */
+int b2g_get_mass_data(void* p, uint32_t first, uint32_t count, float* out) {
+    World* w = W(p);
+    if (!w || (!out && count > 0)) return B2G_ERR_INVALID_ARG;
+    if ((size_t)first + count > w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body range out of bounds");
+    std::vector<float4> m(count);
+    std::vector<float2> lc(count);
+    if (w->device_authoritative && (int)(first + count) <= w->uploaded_bodies) {
+        CUDA_OK(w, cudaStreamSynchronize(w->stream));
+        CUDA_OK(w, cudaMemcpy(m.data(), w->d.b_mass + first, count * sizeof(float4), cudaMemcpyDeviceToHost));
+        CUDA_OK(w, cudaMemcpy(lc.data(), w->d.b_lc + first, count * sizeof(float2), cudaMemcpyDeviceToHost));
+    } else {
+        for (uint32_t i = 0; i < count; ++i) {
+            m[i] = w->h_mass[first + i];
+            lc[i] = w->h_lc[first + i];
+        }
+    }
+    for (uint32_t i = 0; i < count; ++i) {
+        float* o = out + 6 * (size_t)i;
+        o[0] = m[i].x;
+        o[1] = m[i].y;
+        o[2] = m[i].z;
+        o[3] = m[i].w;
+        o[4] = lc[i].x;
+        o[5] = lc[i].y;
+    }
+    return B2G_OK;
+}
+
 /* B2body::set_transform, private/dynamics/b2_body.rs:418-447 */
 int b2g_set_transform(void* p, uint32_t b, b2g_vec2 position, float angle) {
     World* w = W(p);
     if (!w) return B2G_ERR_INVALID_ARG;
     if (b >= w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body id out of range");
+    tape_touch(w);
     if (w->device_authoritative) {
         int rc = prepare(w);
         if (rc != B2G_OK) return rc;
@@ -1079,6 +1165,7 @@ int b2g_set_gravity(void* p, b2g_vec2 g) {
 }
 int b2g_set_allow_sleeping(void* p, int32_t flag) {
     if (!p) return B2G_ERR_INVALID_ARG;
+    if (flag) tape_touch(W(p));
     W(p)->allow_sleep = flag != 0;
     return B2G_OK;
 }
@@ -1505,3 +1592,309 @@ int b2g_get_solver_order(void* p, uint32_t* out, int32_t cap, int32_t* n) {
 
 }  // extern "C"
 
+/* ---- differentiable step: tape and backward ---- */
+
+namespace {
+
+template <class T>
+int talloc(World* w, std::vector<void*>& mem, size_t& bytes, T** p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        w->err = std::string("cudaMalloc (tape): ") + cudaGetErrorString(e);
+        return B2G_ERR_OUT_OF_MEMORY;
+    }
+    mem.push_back((void*)*p);
+    bytes += n * sizeof(T);
+    return B2G_OK;
+}
+
+int tape_final_index(const TapeHost* t) { return t->step_cap / t->ckpt_every + 1; }
+
+int tape_status(World* w, TapeHost* t, long long* steps, long long* slots) {
+    long long c[TAPE_CNT_SIZE] = {};
+    CUDA_OK(w, cudaMemcpyAsync(c, t->d.cnt, sizeof(c), cudaMemcpyDeviceToHost, w->stream));
+    CUDA_OK(w, cudaStreamSynchronize(w->stream));
+    if (steps) *steps = c[TAPE_CNT_STEPS];
+    if (slots) *slots = c[TAPE_CNT_SLOTS];
+    if (c[TAPE_CNT_STATUS] != 0) {
+        t->valid = false;
+        return fail(w, B2G_ERR_CAPACITY, "the tape overflowed: raise max_steps / max_slots in b2g_tape_begin");
+    }
+    return B2G_OK;
+}
+
+/* work buffers for segments of ckpt_every steps with up to `slots` constraints */
+int tape_work(World* w, TapeHost* t, int slots, int vi, int pi) {
+    if (slots < 1) slots = 1;
+    if (vi < 1) vi = 1;
+    if (pi < 1) pi = 1;
+    if (!t->work_mem.empty() && slots <= t->work_slots && vi <= t->work_vi && pi <= t->work_pi) return B2G_OK;
+    tape_free_work(t);
+    AdjWork& a = t->work;
+    a = AdjWork{};
+    const size_t nb = (size_t)t->n_bodies, seg = (size_t)t->ckpt_every, ns = (size_t)slots;
+    std::vector<void*>& m = t->work_mem;
+    size_t& by = t->work_bytes;
+    int rc = B2G_OK;
+    auto A = [&](auto** ptr, size_t n) {
+        if (rc == B2G_OK) rc = talloc(w, m, by, ptr, n);
+    };
+    A(&a.cur_pos, nb);
+    A(&a.cur_vel, nb);
+    A(&a.ws_pos, seg * nb);
+    A(&a.ws_vel1, seg * nb);
+    A(&a.ws_vel2, seg * nb);
+    A(&a.vc, ns);
+    A(&a.imp, ns);
+    A(&a.wv, seg * vi * ns * 3);
+    A(&a.ww, seg * ns * 2);
+    A(&a.wp, seg * pi * ns * 2);
+    A(&a.g_pos, nb);
+    A(&a.g_vel, nb);
+    A(&a.gvc, ns);
+    A(&a.g_imp, ns);
+    A(&a.g_end[0], ns);
+    A(&a.g_end[1], ns);
+    A(&a.cnt, (size_t)CNT_SIZE);
+    A(&a.mismatch, (size_t)1);
+    if (rc != B2G_OK) {
+        tape_free_work(t);
+        return rc;
+    }
+    t->work_slots = slots;
+    t->work_vi = vi;
+    t->work_pi = pi;
+    a.max_slots = slots;
+    a.max_vi = vi;
+    a.max_pi = pi;
+    return B2G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int b2g_tape_begin(void* p, int32_t max_steps, int32_t every, int64_t max_slots) {
+    World* w = W(p);
+    if (!w || max_steps <= 0) return B2G_ERR_INVALID_ARG;
+    if (w->h_flags.empty()) return fail(w, B2G_ERR_INVALID_ARG, "the world has no bodies");
+    if (w->allow_sleep)
+        return fail(w, B2G_ERR_UNSUPPORTED, "the tape needs sleeping off: call b2g_set_allow_sleeping(world, 0)");
+    int rc = prepare(w);
+    if (rc != B2G_OK) return rc;
+    tape_free(w);
+    TapeHost* t = new TapeHost;
+    t->ckpt_every = every > 0 ? every : 16;
+    t->step_cap = max_steps;
+    t->slot_cap = max_slots > 0 ? (long long)max_slots : (long long)max_steps * (4LL * w->d.n_fixtures + 1024);
+    t->n_bodies = w->d.n_bodies;
+    const size_t nck = (size_t)(max_steps / t->ckpt_every + 2) * t->n_bodies;
+    TapeDev& d = t->d;
+    auto A = [&](auto** ptr, size_t n) {
+        if (rc == B2G_OK) rc = talloc(w, t->mem, t->bytes, ptr, n);
+    };
+    A(&d.slots, (size_t)t->slot_cap);
+    A(&d.steps, (size_t)max_steps);
+    A(&d.col_off, (size_t)max_steps * (kMaxColours + 1));
+    A(&d.cmap[0], (size_t)w->d.contact_cap);
+    A(&d.cmap[1], (size_t)w->d.contact_cap);
+    A(&d.ckpt_pos, nck);
+    A(&d.ckpt_vel, nck);
+    A(&d.cnt, (size_t)TAPE_CNT_SIZE);
+    if (rc != B2G_OK) {
+        w->tape = t;
+        tape_free(w);
+        return rc;
+    }
+    d.slot_cap = t->slot_cap;
+    d.step_cap = max_steps;
+    d.ckpt_every = t->ckpt_every;
+    d.n_bodies = t->n_bodies;
+    cudaMemsetAsync(d.cnt, 0, TAPE_CNT_SIZE * sizeof(long long), w->stream);
+    cudaMemsetAsync(d.cmap[0], 0, (size_t)w->d.contact_cap * sizeof(unsigned long long), w->stream);
+    cudaMemsetAsync(d.cmap[1], 0, (size_t)w->d.contact_cap * sizeof(unsigned long long), w->stream);
+    CUDA_OK(w, cudaGetLastError());
+    t->recording = true;
+    w->tape = t;
+    drop_graphs(w);  /* the step graphs gain the recording kernels */
+    return B2G_OK;
+}
+
+int b2g_tape_end(void* p) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    TapeHost* t = w->tape;
+    if (!t || !t->recording) return fail(w, B2G_ERR_INVALID_ARG, "no tape is recording");
+    launch_tape_snapshot(w->d, t->d, tape_final_index(t), w->stream);
+    t->recording = false;
+    drop_graphs(w);
+    long long steps = 0;
+    int rc = tape_status(w, t, &steps, nullptr);
+    if (rc != B2G_OK) return rc;
+    if (steps != t->steps) {
+        t->valid = false;
+        return fail(w, B2G_ERR_CUDA, "taped step count differs from the steps issued");
+    }
+    return check_status(w);
+}
+
+int b2g_tape_info_get(void* p, b2g_tape_info* out) {
+    World* w = W(p);
+    if (!w || !out) return B2G_ERR_INVALID_ARG;
+    *out = b2g_tape_info{};
+    TapeHost* t = w->tape;
+    if (!t) return B2G_OK;
+    long long steps = 0, slots = 0;
+    int rc = tape_status(w, t, &steps, &slots);
+    out->recording = t->recording ? 1 : 0;
+    out->steps = (int32_t)steps;
+    out->slots = slots;
+    out->checkpoint_interval = t->ckpt_every;
+    out->valid = (t->valid && rc == B2G_OK) ? 1 : 0;
+    out->device_bytes = (int64_t)(t->bytes + t->work_bytes);
+    out->replay_mismatches = t->mismatches;
+    return B2G_OK;
+}
+
+int b2g_tape_get_step(void* p, int32_t step, b2g_tape_step* out_step, int32_t* out_col, b2g_tape_slot* out_slots,
+                      int32_t cap) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    TapeHost* t = w->tape;
+    if (!t) return fail(w, B2G_ERR_INVALID_ARG, "no tape");
+    long long steps = 0;
+    int rc = tape_status(w, t, &steps, nullptr);
+    if (rc != B2G_OK) return rc;
+    if (step < 0 || step >= steps) return fail(w, B2G_ERR_INVALID_ARG, "step out of range");
+    TapeStep st;
+    CUDA_OK(w, cudaMemcpy(&st, t->d.steps + step, sizeof(st), cudaMemcpyDeviceToHost));
+    if (out_step) memcpy(out_step, &st, sizeof(st));
+    if (out_col)
+        CUDA_OK(w, cudaMemcpy(out_col, t->d.col_off + (size_t)step * (kMaxColours + 1), (st.ncol + 1) * sizeof(int),
+                              cudaMemcpyDeviceToHost));
+    if (out_slots) {
+        if (cap < st.nslots) return fail(w, B2G_ERR_CAPACITY, "slot buffer too small");
+        if (st.nslots > 0)
+            CUDA_OK(w, cudaMemcpy(out_slots, t->d.slots + st.slot_off, (size_t)st.nslots * sizeof(TapeSlot),
+                                  cudaMemcpyDeviceToHost));
+    }
+    return B2G_OK;
+}
+
+int b2g_tape_get_checkpoint(void* p, int32_t index, float* out, uint32_t count) {
+    World* w = W(p);
+    if (!w || !out) return B2G_ERR_INVALID_ARG;
+    TapeHost* t = w->tape;
+    if (!t) return fail(w, B2G_ERR_INVALID_ARG, "no tape");
+    if (count > (uint32_t)t->n_bodies) return fail(w, B2G_ERR_INVALID_ARG, "more bodies than the tape holds");
+    if (index == -1) {
+        if (t->recording) return fail(w, B2G_ERR_INVALID_ARG, "the final state exists after b2g_tape_end");
+        index = tape_final_index(t);
+    } else if (index < 0 || index > (t->steps - 1) / t->ckpt_every) {
+        return fail(w, B2G_ERR_INVALID_ARG, "checkpoint index out of range");
+    }
+    std::vector<float4> pos(count), vel(count);
+    const size_t o = (size_t)index * t->n_bodies;
+    CUDA_OK(w, cudaStreamSynchronize(w->stream));
+    CUDA_OK(w, cudaMemcpy(pos.data(), t->d.ckpt_pos + o, count * sizeof(float4), cudaMemcpyDeviceToHost));
+    CUDA_OK(w, cudaMemcpy(vel.data(), t->d.ckpt_vel + o, count * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (uint32_t b = 0; b < count; ++b) {
+        memcpy(out + 8 * (size_t)b, &pos[b], sizeof(float4));
+        memcpy(out + 8 * (size_t)b + 4, &vel[b], sizeof(float4));
+    }
+    return B2G_OK;
+}
+
+/* Reverse pass: segments of ckpt_every steps from the last to the first; each replays its
+ * steps from the segment's checkpoint, then runs the adjoint backwards through them. */
+int b2g_backward(void* p, const b2g_body_state* d_final, b2g_body_state* d_initial) {
+    World* w = W(p);
+    if (!w || !d_final || !d_initial) return B2G_ERR_INVALID_ARG;
+    TapeHost* t = w->tape;
+    if (!t) return fail(w, B2G_ERR_INVALID_ARG, "no tape: call b2g_tape_begin, step, b2g_tape_end");
+    if (t->recording) return fail(w, B2G_ERR_INVALID_ARG, "call b2g_tape_end before b2g_backward");
+    if (!t->valid)
+        return fail(w, B2G_ERR_INVALID_ARG,
+                    "the tape is invalid: bodies were edited or created, or a dt = 0 step ran, while recording");
+    long long nsteps = 0;
+    int rc = tape_status(w, t, &nsteps, nullptr);
+    if (rc != B2G_OK) return rc;
+    const int T = (int)nsteps;
+    const int nb = t->n_bodies;
+    std::vector<TapeStep> st(std::max(T, 1));
+    if (T > 0) CUDA_OK(w, cudaMemcpy(st.data(), t->d.steps, T * sizeof(TapeStep), cudaMemcpyDeviceToHost));
+    int max_slots = 1, max_vi = 1, max_pi = 1;
+    for (int i = 0; i < T; ++i) {
+        max_slots = std::max(max_slots, st[i].nslots);
+        max_vi = std::max(max_vi, st[i].vi);
+        max_pi = std::max(max_pi, st[i].pi);
+    }
+    rc = tape_work(w, t, max_slots, max_vi, max_pi);
+    if (rc != B2G_OK) return rc;
+    AdjWork a = t->work;
+    a.t = t->d;
+    a.b_mass = w->d.b_mass;
+    a.b_damp = w->d.b_damp;
+    a.b_flags = w->d.b_flags;
+    a.b_lc = w->d.b_lc;
+    a.nb = nb;
+    /* dL/d(final solver state): the origin p = c - R(a) lc moves with c and a */
+    std::vector<float4> fpos(nb), gpos(nb), gvel(nb);
+    const size_t fo = (size_t)tape_final_index(t) * nb;
+    CUDA_OK(w, cudaMemcpy(fpos.data(), t->d.ckpt_pos + fo, nb * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (int b = 0; b < nb; ++b) {
+        const b2g_body_state& g = d_final[b];
+        const double an = fpos[b].z, sn = std::sin(an), cs = std::cos(an);
+        const double lx = w->h_lc[b].x, ly = w->h_lc[b].y;
+        const double drx = -sn * lx - cs * ly, dry = cs * lx - sn * ly;
+        const double gcx = (double)g.position.x + g.world_center.x, gcy = (double)g.position.y + g.world_center.y;
+        const double ga = (double)g.angle - ((double)g.position.x * drx + (double)g.position.y * dry);
+        gpos[b] = make_float4((float)gcx, (float)gcy, (float)ga, 0.0f);
+        gvel[b] = make_float4(g.linear_velocity.x, g.linear_velocity.y, g.angular_velocity, 0.0f);
+    }
+    cudaStream_t s = w->stream;
+    CUDA_OK(w, cudaMemcpyAsync(a.g_pos, gpos.data(), nb * sizeof(float4), cudaMemcpyHostToDevice, s));
+    CUDA_OK(w, cudaMemcpyAsync(a.g_vel, gvel.data(), nb * sizeof(float4), cudaMemcpyHostToDevice, s));
+    CUDA_OK(w, cudaMemsetAsync(a.g_end[0], 0, (size_t)a.max_slots * sizeof(float4), s));
+    CUDA_OK(w, cudaMemsetAsync(a.g_end[1], 0, (size_t)a.max_slots * sizeof(float4), s));
+    CUDA_OK(w, cudaMemsetAsync(a.cnt, 0, CNT_SIZE * sizeof(int), s));
+    CUDA_OK(w, cudaMemsetAsync(a.mismatch, 0, sizeof(unsigned), s));
+    const int every = t->ckpt_every;
+    const int nseg = (T + every - 1) / every;
+    for (int g = nseg - 1; g >= 0; --g) {
+        a.t0 = g * every;
+        a.t1 = std::min(T, a.t0 + every);
+        const size_t eo = (size_t)(a.t1 == T ? tape_final_index(t) : a.t1 / every) * nb;
+        a.end_pos = t->d.ckpt_pos + eo;
+        a.end_vel = t->d.ckpt_vel + eo;
+        const int e = launch_adjoint_segment(a, s, w->num_sms);
+        if (e != 0) return fail(w, B2G_ERR_CUDA, cudaGetErrorString((cudaError_t)e));
+    }
+    int dcnt[CNT_SIZE] = {};
+    unsigned mism = 0;
+    CUDA_OK(w, cudaMemcpyAsync(gpos.data(), a.g_pos, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
+    CUDA_OK(w, cudaMemcpyAsync(gvel.data(), a.g_vel, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
+    CUDA_OK(w, cudaMemcpyAsync(fpos.data(), t->d.ckpt_pos, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
+    CUDA_OK(w, cudaMemcpyAsync(dcnt, a.cnt, sizeof(dcnt), cudaMemcpyDeviceToHost, s));
+    CUDA_OK(w, cudaMemcpyAsync(&mism, a.mismatch, sizeof(mism), cudaMemcpyDeviceToHost, s));
+    CUDA_OK(w, cudaStreamSynchronize(s));
+    if (dcnt[CNT_STATUS] & ST_BARRIER_TIMEOUT)
+        return fail(w, B2G_ERR_TIMEOUT, "a grid barrier of the backward pass timed out");
+    t->mismatches = mism;
+    /* dL/d(initial origin, angle): c0 = p0 + R(a0) lc */
+    for (int b = 0; b < nb; ++b) {
+        const double an = fpos[b].z, sn = std::sin(an), cs = std::cos(an);
+        const double lx = w->h_lc[b].x, ly = w->h_lc[b].y;
+        const double drx = -sn * lx - cs * ly, dry = cs * lx - sn * ly;
+        b2g_body_state& o = d_initial[b];
+        o.position = b2g_vec2{gpos[b].x, gpos[b].y};
+        o.angle = (float)((double)gpos[b].z + (double)gpos[b].x * drx + (double)gpos[b].y * dry);
+        o.linear_velocity = b2g_vec2{gvel[b].x, gvel[b].y};
+        o.angular_velocity = gvel[b].z;
+        o.world_center = b2g_vec2{gpos[b].x, gpos[b].y};
+    }
+    return B2G_OK;
+}
+
+}  // extern "C"

@@ -305,6 +305,29 @@ def throw_stack(seed=5, steps=240, rows=8, cols=8, half=0.25, projectile_velocit
                   projectile=p)
 
 
+def throw_stack_batch(seeds=512, steps=240):
+    """`seeds` throw-and-stack worlds in one batch: world s is throw_stack(seed=s) with its
+    projectile velocity drawn per seed (vx in [10, 14], vy in [2, 4]) and its own target."""
+    bodies, fixtures, targets, stacks, projectiles = [], [], [], [], []
+    nb = 0
+    for s in range(seeds):
+        rng = SplitMix64(1000003 * (s + 1))
+        v = (float(10.0 + 4.0 * rng.uniform(1)[0]), float(2.0 + 2.0 * rng.uniform(1)[0]))
+        sc = throw_stack(seed=s + 1, steps=steps, projectile_velocity=v)
+        b = sc["bodies"].copy()
+        b["world_index"] = s
+        f = sc["fixtures"].copy()
+        f["body"] += nb
+        bodies.append(b)
+        fixtures.append(f)
+        targets.append(sc["target"])
+        stacks.append(sc["stack"] + nb)
+        projectiles.append(sc["projectile"] + nb)
+        nb += len(b)
+    return _scene("throw_stack_batch", np.concatenate(bodies), np.concatenate(fixtures), steps, num_worlds=seeds,
+                  targets=np.array(targets, F32), stacks=np.array(stacks), projectiles=np.array(projectiles))
+
+
 def hello_world():
     """box2d-rs tests/test.rs:26-102: a 1x1 box (density 1, friction 0.3) dropped on a 50x10 box ground."""
     bodies = b2g.body_defs(2)

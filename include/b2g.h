@@ -169,6 +169,9 @@ int b2g_synchronize(void* world);
 
 /* ---- state I/O (src/b2_body.rs getters/setters) ---- */
 int b2g_get_body_states(void* world, uint32_t first, uint32_t count, b2g_body_state* out);
+/* B2body::get_mass_data / get_local_center: 6 floats per body: mass, 1/mass, rotational inertia
+ * about the centre of mass (get_inertia adds mass * |local centre|^2), its inverse, local centre. */
+int b2g_get_mass_data(void* world, uint32_t first, uint32_t count, float* out);
 /* B2body::set_transform, private/dynamics/b2_body.rs:418-447 */
 int b2g_set_transform(void* world, uint32_t body, b2g_vec2 position, float angle);
 int b2g_set_linear_velocity(void* world, uint32_t body, b2g_vec2 v);
@@ -229,6 +232,76 @@ int b2g_set_graph_capture(void* world, int32_t flag);
 #define B2G_NOALLOC_MAX_PAIRS 16384
 int b2g_collide_pairs_noalloc(const b2g_fixture_def* shape_a, const float* xf_a, const b2g_fixture_def* shape_b,
                               const float* xf_b, int32_t n, b2g_contact_info* out);
+
+/* ---- differentiable step: a recorded tape and its hand-written adjoint ----
+ * The model differentiated is the solver of every taped step (B2island::solve,
+ * private/dynamics/b2_island_private.rs:129-328, with B2contactSolver,
+ * private/dynamics/b2_contact_solver_private.rs) with its discrete decisions frozen from the
+ * forward pass: the contact set and each manifold in local coordinates, the colour order,
+ * restitution triggers, friction-cone and normal clamp states, the 2-point block-solver case,
+ * translation/rotation clamps, position-correction clamps and each island's position-iteration
+ * count. Velocity integration, constraint initialisation (world manifold from the poses),
+ * warm starting with impulses carried between steps, velocity iterations, position
+ * integration and position iterations are differentiated exactly. It has no counterpart in
+ * the reference. */
+typedef struct b2g_tape_slot {           /* one solver constraint of one taped step (144 bytes) */
+    int32_t body_a, body_b;
+    int32_t count_type_flags;            /* point count | manifold type << 8 | dynamic A/B << 16 */
+    int32_t colour;
+    float local_normal[2], local_point[2];
+    float points[4];                     /* manifold points (local) */
+    float inv_mass_a, inv_mass_b, inv_inertia_a, inv_inertia_b;
+    float local_center_a[2], local_center_b[2];
+    float friction, restitution, restitution_threshold, tangent_speed;
+    float radius_a, radius_b;
+    int32_t island;                      /* island root body */
+    int32_t position_iterations;         /* position iterations this slot's island ran */
+    float impulses[4];                   /* normal 0, tangent 0, normal 1, tangent 1 as carried in */
+    int32_t carry[2];                    /* previous step's slot * 2 + point each impulse came from, or -1 */
+    uint32_t ids[2];                     /* contact feature ids */
+} b2g_tape_slot;
+
+typedef struct b2g_tape_step {           /* 48 bytes */
+    float dt, dt_ratio, gravity_x, gravity_y;
+    int32_t velocity_iterations, position_iterations, warm_starting, num_slots;
+    int64_t slot_offset;
+    int32_t num_colours, num_contacts;
+} b2g_tape_step;
+
+typedef struct b2g_tape_info {
+    int32_t recording;                   /* 1 between b2g_tape_begin and b2g_tape_end */
+    int32_t steps;                       /* taped steps (steps with dt > 0) */
+    int64_t slots;                       /* constraint slots over all taped steps */
+    int32_t checkpoint_interval;
+    int32_t valid;                       /* 0 once an edit between steps or an overflow broke it */
+    int64_t device_bytes;                /* tape plus backward work buffers */
+    uint32_t replay_mismatches;          /* bodies whose replayed state differed from the recorded one
+                                            in the last b2g_backward (0 expected) */
+    int32_t pad;
+} b2g_tape_info;
+
+/* Start recording the next steps (up to max_steps; max_slots constraint slots in total, <= 0
+ * picks max_steps x (4 x fixtures + 1024)); body state is checkpointed every
+ * checkpoint_interval steps (<= 0: 16). Needs sleeping off. Editing bodies between taped steps
+ * (transforms, velocities, forces, impulses, new bodies or fixtures) invalidates the tape and
+ * b2g_backward then fails; gravity, iterations, dt and warm starting may change per step. */
+int b2g_tape_begin(void* world, int32_t max_steps, int32_t checkpoint_interval, int64_t max_slots);
+/* Stop recording and checkpoint the final state. */
+int b2g_tape_end(void* world);
+int b2g_tape_info_get(void* world, b2g_tape_info* out);
+/* Reverse pass over the whole tape. d_final: dL/d(state after the last taped step) per body,
+ * in b2g_body_state layout (position, angle, linear and angular velocity, world centre; the
+ * position and world-centre terms add up). d_initial receives dL/d(state before the first
+ * taped step) in the same layout: position = dL/d(body origin) with the angle held,
+ * angle = dL/d(angle) with the origin held, world_center = dL/d(centre of mass) with the angle
+ * held. Either pointer covers all bodies. */
+int b2g_backward(void* world, const b2g_body_state* d_final, b2g_body_state* d_initial);
+/* Copy one taped step out: its parameters, colour offsets (num_colours + 1 ints) and slots. */
+int b2g_tape_get_step(void* world, int32_t step, b2g_tape_step* out_step, int32_t* out_colour_offsets,
+                      b2g_tape_slot* out_slots, int32_t slot_capacity);
+/* Body solver state (centre x, y, angle, -, vx, vy, w, - per body) of checkpoint `index`
+ * (state before step index x interval), or after the last taped step for index = -1. */
+int b2g_tape_get_checkpoint(void* world, int32_t index, float* out, uint32_t count);
 
 /* ---- parity hooks ---- */
 /* Record every pair the broadphase emits (off by default; needed by b2g_get_pairs). */

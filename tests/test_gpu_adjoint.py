@@ -1,0 +1,161 @@
+"""Differentiable step on the GPU: tape, bit-exact replay, gradient against the host f64 reference
+and central finite differences of the frozen-decision model.
+
+Scene: the throw-and-stack workload (8 x 8 boxes of half-extent 0.25 m and a circle of radius
+0.5 m thrown at them, dt = 1/60, 8 velocity / 3 position iterations). Loss: squared distance of
+the stack's centre of mass from a seeded target after the taped steps. Tolerances: the GPU's f32
+gradient within 1e-3 relative (vector 2-norm) of the host f64 reverse pass, which itself matches
+central differences of the f64 frozen forward to 1e-5 relative (plus 1e-7 of the largest
+gradient entry for the differencing noise).
+"""
+import numpy as np
+import pytest
+
+import adjoint_ref
+import b2g
+import scenes
+
+DT = 1.0 / 60.0
+
+
+def _world(sc, num_worlds=1):
+    w = b2g.B2world(gravity=(0.0, -10.0), num_worlds=num_worlds)
+    w.set_allow_sleeping(False)
+    w.create_bodies(sc["bodies"])
+    w.create_fixtures(sc["fixtures"])
+    return w
+
+
+def _loss_grad_c(centres, stack, target):
+    com = centres[stack].mean(0)
+    g = np.zeros((len(centres), 2))
+    g[stack] = 2.0 * (com - target) / len(stack)
+    return float(((com - target) ** 2).sum()), g
+
+
+def _run_taped(sc, steps, every=16):
+    w = _world(sc)
+    w.tape_begin(steps, every)
+    for _ in range(steps):
+        w.step(DT, 8, 3)
+    w.tape_end()
+    return w
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("steps", [48, 120])
+def test_gradient_matches_host_reference_and_finite_differences(built, oracle_lib, steps):
+    sc = scenes.throw_stack(steps=steps)
+    stack, target = sc["stack"], sc["target"].astype(np.float64)
+    w = _run_taped(sc, steps)
+    info = w.tape_info()
+    assert info["steps"] == steps and info["valid"] == 1 and not info["recording"]
+    assert info["slots"] > 0
+
+    final = w.get_body_states()
+    _, gc = _loss_grad_c(final["world_center"].astype(np.float64), stack, target)
+    d_final = np.zeros(w.body_count, b2g.BODY_STATE)
+    d_final["world_center"] = gc
+    g_gpu = w.backward(d_final)
+    assert w.tape_info()["replay_mismatches"] == 0, "GPU replay left the recorded trajectory"
+
+    ref = adjoint_ref.AdjointRef.from_world(w, sc["bodies"])
+    init = adjoint_ref.state_from_checkpoint(w.tape_checkpoint(0))
+    fin = adjoint_ref.state_from_checkpoint(w.tape_checkpoint(-1))
+    rep, carry_mismatches = ref.replay_f32(init)
+    assert np.array_equal(rep.view(np.uint32), fin.view(np.uint32)), "host f32 replay differs from the GPU"
+    assert carry_mismatches == 0
+
+    init64 = init.astype(np.float64)
+    f64 = ref.forward_f64(init64)
+    assert np.abs(f64[:, :3] - fin[:, :3]).max() < 1e-3
+
+    def loss(s0):
+        return _loss_grad_c(ref.forward_f64(s0)[:, :2], stack, target)[0]
+
+    _, gc64 = _loss_grad_c(f64[:, :2], stack, target)
+    gd = np.zeros((w.body_count, 6))
+    gd[:, 0:2] = gc64
+    g_ref = ref.backward_f64(init64, gd)
+
+    # f64 reverse pass vs central differences of the frozen f64 forward
+    proj = sc["projectile"]
+    probes = [(proj, 3), (proj, 4), (proj, 0), (proj, 1)]
+    probes += [(int(b), k) for b in stack[[0, 7, 27, 56, 63]] for k in (0, 1, 2)]
+    gmax = np.abs(g_ref).max()
+    for b, k in probes:
+        h = 1e-5 * max(1.0, abs(init64[b, k]))
+        xp, xm = init64.copy(), init64.copy()
+        xp[b, k] += h
+        xm[b, k] -= h
+        fd = (loss(xp) - loss(xm)) / (2 * h)
+        assert abs(fd - g_ref[b, k]) <= 1e-5 * abs(fd) + 1e-7 * gmax, (b, k, fd, g_ref[b, k])
+
+    # GPU f32 reverse pass vs the f64 one (centre-of-mass coordinates; boxes and circles have lc = 0)
+    g_gpu6 = np.stack([g_gpu["world_center"][:, 0], g_gpu["world_center"][:, 1], g_gpu["angle"],
+                       g_gpu["linear_velocity"][:, 0], g_gpu["linear_velocity"][:, 1], g_gpu["angular_velocity"]],
+                      axis=1).astype(np.float64)
+    rel = np.linalg.norm(g_gpu6 - g_ref) / np.linalg.norm(g_ref)
+    assert rel <= 1e-3, rel
+    # and per probe against finite differences, 1e-3 relative
+    for b, k in probes:
+        scale = max(abs(g_ref[b, k]), 1e-3 * np.abs(g_ref).max())
+        assert abs(g_gpu6[b, k] - g_ref[b, k]) <= 1e-3 * scale, (b, k, g_gpu6[b, k], g_ref[b, k])
+    ref.close()
+    w.close()
+
+
+@pytest.mark.gpu
+def test_checkpoint_interval_does_not_change_the_gradient(built):
+    sc = scenes.throw_stack(steps=40)
+    grads = []
+    for every in (16, 5):
+        w = _run_taped(sc, 40, every)
+        d = np.zeros(w.body_count, b2g.BODY_STATE)
+        d["linear_velocity"][sc["projectile"]] = (1.0, 0.5)
+        d["world_center"][sc["stack"]] = (0.3, -0.2)
+        grads.append(w.backward(d))
+        assert w.tape_info()["replay_mismatches"] == 0
+        w.close()
+    for f in ("position", "angle", "linear_velocity", "angular_velocity"):
+        assert np.array_equal(grads[0][f], grads[1][f])
+
+
+@pytest.mark.gpu
+def test_edits_while_recording_invalidate_the_tape(built):
+    sc = scenes.throw_stack(steps=10)
+    w = _world(sc)
+    w.tape_begin(10)
+    w.step(DT, 8, 3)
+    w.set_linear_velocity(sc["projectile"], (1.0, 0.0))
+    w.step(DT, 8, 3)
+    w.tape_end()
+    assert w.tape_info()["valid"] == 0
+    with pytest.raises(b2g.B2GError):
+        w.backward(np.zeros(w.body_count, b2g.BODY_STATE))
+    w.close()
+
+
+@pytest.mark.gpu
+def test_tape_overflow_is_reported(built):
+    sc = scenes.throw_stack(steps=10)
+    w = _world(sc)
+    w.tape_begin(3)
+    for _ in range(5):
+        w.step(DT, 8, 3)
+    with pytest.raises(b2g.B2GError) as e:
+        w.tape_end()
+    assert e.value.code == -3
+    w.close()
+
+
+@pytest.mark.gpu
+def test_tape_refuses_sleeping_worlds(built):
+    sc = scenes.throw_stack(steps=10)
+    w = b2g.B2world(gravity=(0.0, -10.0))
+    w.create_bodies(sc["bodies"])
+    w.create_fixtures(sc["fixtures"])
+    with pytest.raises(b2g.B2GError) as e:
+        w.tape_begin(10)
+    assert e.value.code == -6
+    w.close()
