@@ -840,12 +840,13 @@ __global__ void k_clear_forces(DevWorld w) {
         w.b_force[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
+/* One block per SM: the persistent kernels are bound by grid-barrier latency, which grows with
+ * the number of arriving blocks (measured on the 100k-body scene: 152 blocks take 21% less solver
+ * time than 304); one block of 256 threads per SM still covers a colour of ~39k slots in a single
+ * pass. (If not even one block fit, the cooperative launch would fail and the step report it.) */
 int coop_blocks(const void* fn, int num_sms) {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBlock, 0);
-    if (per_sm < 1) per_sm = 1;
-    if (per_sm > 2) per_sm = 2;
-    return per_sm * num_sms;
+    (void)fn;
+    return num_sms;
 }
 
 }  // namespace
