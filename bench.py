@@ -38,6 +38,7 @@ sys.path.insert(0, os.path.join(ROOT, "box2d-rs_gb300"))
 
 import b2g  # noqa: E402
 import scenes  # noqa: E402
+import shard  # noqa: E402
 
 WORKLOAD = "mixed-100k: 50k circles + 50k 3-8-gons, 1000x1000 m walled box, 8/3 iterations, dt=1/60"
 METRIC = "body-steps/s @100k bodies (mixed scene)"
@@ -192,21 +193,32 @@ def timed_steps(world, scene, steps, flush, torch):
     return total
 
 
-def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_bucket=6):
+def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_bucket=6, rank=0, world_size=1):
     """Batched uneven worlds: one world batch stepped together vs. the same worlds stepped one
     at a time. The sequential time is the sum over all worlds of each world's mean step time,
     estimated from `per_bucket` worlds of every log2 size bucket, each timed over the same
-    steps as the batch."""
-    scene = scenes.batched(num_worlds=num_worlds, steps=steps)
-    w = b2g.B2world(gravity=scene["gravity"], num_worlds=num_worlds, device=device)
+    steps as the batch. With several ranks each steps its contiguous range of the worlds
+    (shard.py) and the batch time is the slowest rank's."""
+    full = scenes.batched(num_worlds=num_worlds, steps=steps)
+    part = shard.shard_scene(full, rank, world_size) if world_size > 1 else full
+    w = b2g.B2world(gravity=part["gravity"], num_worlds=part["num_worlds"], device=device)
     w.set_allow_sleeping(False)
-    scenes.build_world(w, scene)
+    scenes.build_world(w, part)
     for _ in range(warmup):
-        w.step(scene["dt"], scene["vi"], scene["pi"])
+        w.step(part["dt"], part["vi"], part["pi"])
     w.synchronize()
-    batch_ms = timed_steps(w, scene, steps, flush, torch)
+    if world_size > 1:
+        torch.distributed.barrier()
+    batch_ms = timed_steps(w, part, steps, flush, torch)
     counts = w.get_counts()
     w.close()
+    if world_size > 1:
+        t = torch.tensor([batch_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        batch_ms = float(t[0])
+    scene = full
+    if rank != 0:
+        return None
     sizes = scene["world_body_counts"]
     bucket = np.floor(np.log2(sizes)).astype(int)
     bodies, fixtures = scene["bodies"], scene["fixtures"]
@@ -241,6 +253,7 @@ def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_
     batched = num_worlds * steps / (batch_ms / 1e3)
     sequential = num_worlds * steps / (est_ms / 1e3)
     return {"metric": "world-steps/s, 4096 uneven worlds (16-2048 bodies)", "value": batched,
+            "ranks": world_size, "sharding": "contiguous world ranges, no collective" if world_size > 1 else None,
             "unit": "world-steps/s", "body_steps_per_s": scene["n_dynamic"] * steps / (batch_ms / 1e3),
             "bodies": scene["n_dynamic"], "steps": steps, "ms_per_step": batch_ms / steps,
             "sequential_single_world_gpu": {"value": sequential, "unit": "world-steps/s",
@@ -325,6 +338,10 @@ def main():
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels directly instead of CUDA graphs")
     ap.add_argument("--batched-steps", type=int, default=300, help="steps of the 4096-world leg (0 skips it)")
     ap.add_argument("--adjoint-steps", type=int, default=240, help="steps of the differentiable leg (0 skips it)")
+    ap.add_argument("--skip-steps", type=int, default=0,
+                    help="untimed steps before the warm-up (profiling a later window of the scene)")
+    ap.add_argument("--profile-window", action="store_true",
+                    help="bracket the timed steps with cudaProfilerStart/Stop (ncu --profile-from-start off)")
     args = ap.parse_args()
     rank, world_size, local_rank = dist_info()
     n_half = int(50_000 * args.scale)
@@ -363,7 +380,7 @@ def main():
     w.set_graph_capture(not args.no_graphs)
     scenes.build_world(w, scene)
     dt, vi, pi = scene["dt"], scene["vi"], scene["pi"]
-    for _ in range(args.warmup):
+    for _ in range(args.skip_steps + args.warmup):
         w.step(dt, vi, pi)
     w.synchronize()
 
@@ -372,6 +389,8 @@ def main():
         torch.distributed.barrier()
     torch.cuda.synchronize()
     sampler.start()
+    if args.profile_window:
+        torch.cuda.profiler.start()
     launches0 = w._lib.b2g_get_launch_count()
     total_ms = 0.0
     phase_ms = {"collide": 0.0, "solve_init": 0.0, "solve_velocity": 0.0, "broadphase": 0.0}
@@ -392,6 +411,8 @@ def main():
             snaps.append((args.warmup + k + 1, snapshot(w)))
     launches = w._lib.b2g_get_launch_count() - launches0
     torch.cuda.synchronize()
+    if args.profile_window:
+        torch.cuda.profiler.stop()
     clocks = sampler.stop()
     counts = w.get_counts()
     w.close()
@@ -445,8 +466,9 @@ def main():
         "clocks": clocks,
     }
     if args.batched_steps > 0:
-        line["batched"] = run_batched(torch, flush, local_rank, steps=args.batched_steps, warmup=args.warmup)
-    if args.adjoint_steps > 0:
+        line["batched"] = run_batched(torch, flush, local_rank, steps=args.batched_steps, warmup=args.warmup,
+                                      rank=rank, world_size=world_size)
+    if args.adjoint_steps > 0 and rank == 0:
         line["adjoint"] = run_adjoint(torch, flush, local_rank, steps=args.adjoint_steps)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = run_cpu_on_snapshots(scene, snaps)

@@ -484,7 +484,7 @@ int allocate(World* w, int nb, int nf) {
         A(c->mat, contact_cap); A(c->mgeo, contact_cap); A(c->mpts, contact_cap); A(c->mimp, contact_cap);
         A(c->mids, contact_cap);
     }
-    A(d.c_rank, contact_cap);
+    A(d.c_rank, contact_cap); A(d.c_row, 2 * (size_t)fix_cap + 2);
     A(d.n_key, pair_cap); A(d.n_fix, pair_cap); A(d.n_idx, pair_cap); A(d.n_key_alt, pair_cap); A(d.n_idx_alt, pair_cap);
     A(d.cons_contact, contact_cap); A(d.cons_colour, contact_cap); A(d.cons_island, contact_cap);
     A(d.s_contact, contact_cap); A(d.s_cons, contact_cap); A(d.s_fix, contact_cap);

@@ -74,6 +74,7 @@ enum {
     CNT_BOUNDS = 12,      /* 4 ints: ordered-int min.x, min.y, max.x, max.y of proxy centres */
     CNT_BARRIER = 16,     /* 2 uints: grid barrier count / generation */
     CNT_ISLANDS = 18,
+    CNT_COLOURINGS = 19,  /* colourings done so far: the stamp of colours kept in contacts (mids.w) */
     CNT_SIZE = 32
 };
 
@@ -90,7 +91,8 @@ struct Contacts {
     float4* mgeo;     /* local normal, local point */
     float4* mpts;     /* point 0 local, point 1 local */
     float4* mimp;     /* normal 0, tangent 0, normal 1, tangent 1 impulses */
-    uint4* mids;      /* id 0, id 1, type | count << 8, - */
+    uint4* mids;      /* id 0, id 1, type | count << 8, colour | stamp << 6 (the colour this contact
+                         had as a constraint of the colouring with that stamp; 0 = none) */
 };
 
 struct StepParams {
@@ -132,6 +134,8 @@ struct DevWorld {
     /* contacts: current table and the merge target */
     Contacts c, c_alt;
     int* c_rank;                 /* exclusive scan of alive flags during a merge */
+    int* c_row;                  /* per proxy id: first contact of the sorted table whose key starts with
+                                    it (valid only when that contact's key does: see k_bp_rows) */
     /* new contacts from the broadphase */
     unsigned long long* n_key;   /* keys; sorted in place */
     int2* n_fix;                 /* fixture pair per new key (before sorting) */

@@ -221,13 +221,44 @@ __device__ __forceinline__ int lower_bound_u64(const unsigned long long* a, int 
     return lo;
 }
 
-__device__ void handle_pair(const DevWorld& w, const StepParams& sp, int f, int g, int n_contacts) {
-    const uint32_t rf = w.f_refid[f], rg = w.f_refid[g];
+/* Row index of the key-sorted contact table: c_row[r] = first contact whose key's high part is
+ * proxy id r. Entries of ids with no contact keep stale values; a reader accepts c_row[r] only if
+ * that contact's key starts with r, which a stale entry cannot satisfy (ids with contacts are
+ * rewritten every pass and the table is sorted). */
+__global__ void k_bp_rows(DevWorld w) {
+    const int n = w.cnt[CNT_CONTACTS];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned long long r = w.c.key[i] >> w.key_bits;
+        if (i == 0 || (w.c.key[i - 1] >> w.key_bits) != r) w.c_row[r] = i;
+    }
+}
+
+/* A live contact with this key exists: a short scan of the key's row instead of a binary search
+ * over the whole table (the check the reference makes by walking body B's contact list,
+ * private/dynamics/b2_contact_manager.rs:199-224). */
+__device__ __forceinline__ bool contact_exists(const DevWorld& w, uint32_t lo, unsigned long long key, int n_contacts) {
+    const int start = w.c_row[lo];
+    if (start < 0 || start >= n_contacts || (w.c.key[start] >> w.key_bits) != lo) return false;
+    for (int i = start; i < n_contacts; ++i) {
+        const unsigned long long k = w.c.key[i];
+        if (k >= key) return k == key && !(w.c.flags[i] & CF_DEAD);
+        if ((k >> w.key_bits) != lo) return false;
+    }
+    return false;
+}
+
+__device__ void handle_pair(const DevWorld& w, const StepParams& sp, int f, int g, uint32_t rf, int n_contacts) {
+    const uint32_t rg = w.f_refid[g];
     if (sp.record_pairs) {
         const int slot = atomicAdd(&w.cnt[CNT_PAIRS], 1);
         if (slot < w.pair_cap) w.pairs[slot] = make_uint2((uint32_t)min(f, g), (uint32_t)max(f, g));
         else atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_RECORD_OVERFLOW);
     }
+    /* most overlapping pairs already have a contact: test that first (the order of the tests
+     * does not change which pairs are added) */
+    const uint32_t lo = rf < rg ? rf : rg, hi = rf < rg ? rg : rf;
+    const unsigned long long key = ((unsigned long long)lo << w.key_bits) | hi;
+    if (contact_exists(w, lo, key, n_contacts)) return;
     /* add_pair: fixture A is the one with the smaller proxy id */
     int fa = rf < rg ? f : g, fb = rf < rg ? g : f;
     const int ba = w.f_body[fa], bb = w.f_body[fb];
@@ -252,10 +283,6 @@ __device__ void handle_pair(const DevWorld& w, const StepParams& sp, int f, int 
         fa = fb;
         fb = t;
     }
-    const uint32_t lo = rf < rg ? rf : rg, hi = rf < rg ? rg : rf;
-    const unsigned long long key = ((unsigned long long)lo << w.key_bits) | hi;
-    const int pos = lower_bound_u64(w.c.key, n_contacts, key);
-    if (pos < n_contacts && w.c.key[pos] == key && !(w.c.flags[pos] & CF_DEAD)) return;
     const int slot = atomicAdd(&w.cnt[CNT_NEW], 1);
     if (slot < w.pair_cap) {
         w.n_key[slot] = key;
@@ -294,7 +321,7 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
                     const int g = (int)w.bp_val[~id];
                     if (g == f) continue;
                     if (w.f_moved[g] && w.f_refid[g] > rq) continue;
-                    handle_pair(w, sp, f, g, n_contacts);
+                    handle_pair(w, sp, f, g, rq, n_contacts);
                 } else if (sp_top < kStack) {
                     stack[sp_top++] = id;
                 } else {
@@ -408,6 +435,7 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
         }
         k_bp_leaves<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_refit<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        k_bp_rows<<<grid_for(w.contact_cap, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_traverse<<<gf, kBlock, 0, s>>>(w, sp); B2G_LAUNCHED(1);
         k_bp_clear_moved<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
     }

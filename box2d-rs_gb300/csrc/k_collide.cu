@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(128) k_collide(DevWorld w, StepParams sp) {
         bool touching = false;
         if (flags & CF_SENSOR) {
             /* sensor overlap tests (GJK) are outside the GPU path: sensors never touch */
-            w.c.mids[i] = make_uint4(ids.x, ids.y, ids.z & 0xffu, 0u);
+            w.c.mids[i] = make_uint4(ids.x, ids.y, ids.z & 0xffu, ids.w);
         } else {
             const int kind = (int)((flags >> CF_KIND_SHIFT) & 7u);
             const Xf xfA = load_xf(w, bd.x);
@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(128) k_collide(DevWorld w, StepParams sp) {
             w.c.mgeo[i] = make_float4(m.ln.x, m.ln.y, m.lp.x, m.lp.y);
             w.c.mpts[i] = make_float4(m.p[0].x, m.p[0].y, m.p[1].x, m.p[1].y);
             w.c.mimp[i] = make_float4(ni[0], ti[0], ni[1], ti[1]);
-            w.c.mids[i] = make_uint4(m.id[0], m.id[1], (uint32_t)m.type | ((uint32_t)m.count << 8), 0u);
+            w.c.mids[i] = make_uint4(m.id[0], m.id[1], (uint32_t)m.type | ((uint32_t)m.count << 8), ids.w);
             if (touching != was_touching) {
                 wake_body(w, bd.x);
                 wake_body(w, bd.y);

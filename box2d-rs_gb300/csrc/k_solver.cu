@@ -12,11 +12,13 @@
  *               island is solved if any member is awake; its members are woken.
  *   constraints the touching, enabled, non-sensor contacts of solved islands, compacted
  *               in contact-table order by a scan.
- *   colouring   rounds of: every uncoloured constraint whose hashed priority is the
- *               minimum at both of its dynamic bodies takes the lowest colour unused
- *               at either body (first fit over 64 colours; past that, one colour per
- *               round). Constraints of one colour share no dynamic body, so each colour
- *               is solved in parallel with results identical to any sequential order.
+ *   colouring   constraints that persist from the previous colouring keep their colour;
+ *               the new ones are coloured in rounds of: every uncoloured constraint whose
+ *               hashed priority is the minimum at both of its dynamic bodies takes the
+ *               lowest colour unused at either body (first fit over 64 colours; past that,
+ *               one colour per round). Constraints of one colour share no dynamic body, so
+ *               each colour is solved in parallel with results identical to any sequential
+ *               order.
  *   solver      one persistent cooperative kernel: integrate velocities, initialise
  *               constraints, warm start, velocity iterations, store impulses, integrate
  *               positions, position iterations with the per-island early exit, write
@@ -146,11 +148,18 @@ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
     return x;
 }
 
+/* Colouring. A constraint that was also a constraint of the previous colouring keeps its
+ * first-fit colour (stored in its contact with that colouring's stamp): the previous colours were
+ * a proper colouring of the previous constraints, so any subset of them still is. Only the new
+ * constraints are coloured, by Jones-Plassmann rounds (hash priorities; a local minimum at both
+ * of its dynamic bodies takes the lowest colour free at both), so a step whose contacts persist
+ * needs one or two rounds instead of one per colour. */
 __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w) {
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsize = gridDim.x * blockDim.x;
     const int n = w.cnt[CNT_CONS];
     const unsigned long long kNone = ~0ull;
+    const uint32_t stamp = (uint32_t)w.cnt[CNT_COLOURINGS] & 0x3ffffffu;  /* the previous colouring's */
     /* offers are double-buffered by round parity: round r offers into buffer r & 1, and the
      * entries of buffer (r - 1) & 1 are reset during round r, so a round needs two barriers */
     for (int b = gtid; b < w.n_bodies; b += gsize) {
@@ -158,8 +167,24 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w) {
         w.b_cmin[w.body_cap + b] = kNone;
         w.b_cmask[b] = 0ull;
     }
-    for (int k = gtid; k < n; k += gsize) w.cons_colour[k] = -1;
+    /* every 16th colouring starts afresh, so kept colours do not stay fragmented after the
+     * contact graph has changed (a fresh colouring of a settled stack needs fewer colours) */
+    const bool keep = stamp != 0u && (stamp & 15u) != 0u;
+    for (int k = gtid; k < n; k += gsize) {
+        const uint32_t kept = w.c.mids[w.cons_contact[k]].w;
+        w.cons_colour[k] = (keep && (kept >> 6) == stamp) ? (int)(kept & 63u) : -1;
+    }
     for (int c = gtid; c < kMaxColours; c += gsize) w.col_hist[c] = 0;
+    if (!grid_barrier(w)) return;
+    /* the kept colours are taken at their bodies */
+    for (int k = gtid; k < n; k += gsize) {
+        const int c = w.cons_colour[k];
+        if (c < 0) continue;
+        const int2 bd = w.c.body[w.cons_contact[k]];
+        const unsigned long long bit = 1ull << c;
+        if (is_dynamic(w.b_flags[bd.x])) atomicOr(&w.b_cmask[bd.x], bit);
+        if (is_dynamic(w.b_flags[bd.y])) atomicOr(&w.b_cmask[bd.y], bit);
+    }
     if (gtid == 0) {
         /* two "still uncoloured" counters alternate by round parity: round r counts into
          * [r & 1] and reads the previous round's result from [(r + 1) & 1] */
@@ -254,12 +279,19 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w) {
         for (int c = threadIdx.x; c < kMaxColours; c += blockDim.x) w.col_hist[c] = s_dense[c];  /* cursor */
     }
     if (!grid_barrier(w)) return;
+    const uint32_t next = (stamp + 1u) & 0x3ffffffu;
     for (int k = gtid; k < n; k += gsize) {
-        const int slot = atomicAdd(&w.col_hist[w.cons_colour[k]], 1);
+        const int c = w.cons_colour[k];
+        const int ci = w.cons_contact[k];
+        const int slot = atomicAdd(&w.col_hist[c], 1);
+        /* keep first-fit colours for the next colouring (the per-round overflow colours are not
+         * kept: a later round could hand the same one to a neighbour) */
+        w.c.mids[ci].w = (c < kFirstFitColours && next != 0u) ? ((next << 6) | (uint32_t)c) : 0u;
         if (slot < 0 || slot >= n) continue;  /* cannot happen with consistent offsets */
-        w.s_contact[slot] = w.cons_contact[k];
+        w.s_contact[slot] = ci;
         w.s_cons[slot] = k;
     }
+    if (gtid == 0) w.cnt[CNT_COLOURINGS] = (int)next;
 }
 
 /* ---------------- solver (cooperative) ---------------- */

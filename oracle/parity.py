@@ -203,3 +203,55 @@ def lockstep(scene, steps, check_pairs=True, check_contacts=True, resync=False, 
         if on_step is not None:
             on_step(rec)
     return out, gpu, ora
+
+
+def energy(states, mass, gravity):
+    """Kinetic energy (translation + rotation about the centre of mass) and potential energy
+    (-m g.c) summed over all bodies; mass is b2g.B2world.get_mass_data() (static bodies have 0)."""
+    m = mass[:, 0].astype(np.float64)
+    inertia = mass[:, 2].astype(np.float64)
+    v = states["linear_velocity"].astype(np.float64)
+    w = states["angular_velocity"].astype(np.float64)
+    c = states["world_center"].astype(np.float64)
+    ke = 0.5 * float((m * (v * v).sum(1) + inertia * w * w).sum())
+    pe = -float((m * (c @ np.asarray(gravity, np.float64))).sum())
+    return ke, pe
+
+
+def separations(contacts, states, radius, fixture_body):
+    """Separation of every touching manifold point, from each contact's local manifold and the
+    bodies' current transforms, as B2positionSolverManifold::initialize computes it
+    (b2_contact_solver_private.rs:600-642). radius: per fixture; fixture_body: body per fixture."""
+    out = []
+    p = states["position"].astype(np.float64)
+    a = states["angle"].astype(np.float64)
+    for ct in contacts:
+        n = int(ct["point_count"])
+        if not ct["touching"] or n == 0:
+            continue
+        fa, fb = int(ct["fixture_a"]), int(ct["fixture_b"])
+        ba, bb = int(fixture_body[fa]), int(fixture_body[fb])
+        ra, rb = float(radius[fa]), float(radius[fb])
+
+        def xf(b, v):
+            s, c = np.sin(a[b]), np.cos(a[b])
+            return np.array([c * v[0] - s * v[1] + p[b, 0], s * v[0] + c * v[1] + p[b, 1]])
+
+        def rot(b, v):
+            s, c = np.sin(a[b]), np.cos(a[b])
+            return np.array([c * v[0] - s * v[1], s * v[0] + c * v[1]])
+
+        ln, lp = ct["local_normal"].astype(np.float64), ct["local_point"].astype(np.float64)
+        pts = ct["point_local"].astype(np.float64)
+        mt = int(ct["manifold_type"])
+        for j in range(n):
+            if mt == 0:
+                pa, pb = xf(ba, lp), xf(bb, pts[0])
+                out.append(float(np.linalg.norm(pb - pa)) - ra - rb)
+            elif mt == 1:
+                nrm, plane, clip = rot(ba, ln), xf(ba, lp), xf(bb, pts[j])
+                out.append(float((clip - plane) @ nrm) - ra - rb)
+            else:
+                nrm, plane, clip = rot(bb, ln), xf(bb, lp), xf(ba, pts[j])
+                out.append(float((clip - plane) @ nrm) - ra - rb)
+    return np.array(out)
