@@ -193,7 +193,8 @@ def timed_steps(world, scene, steps, flush, torch):
     return total
 
 
-def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_bucket=6, rank=0, world_size=1):
+def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_bucket=6, rank=0, world_size=1,
+                autotune=True):
     """Batched uneven worlds: one world batch stepped together vs. the same worlds stepped one
     at a time. The sequential time is the sum over all worlds of each world's mean step time,
     estimated from `per_bucket` worlds of every log2 size bucket, each timed over the same
@@ -201,12 +202,19 @@ def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_
     (shard.py) and the batch time is the slowest rank's."""
     full = scenes.batched(num_worlds=num_worlds, steps=steps)
     part = shard.shard_scene(full, rank, world_size) if world_size > 1 else full
+    if autotune:
+        t = b2g.B2world(gravity=part["gravity"], num_worlds=part["num_worlds"], device=device)
+        t.set_allow_sleeping(False)
+        scenes.build_world(t, part)
+        t.autotune(part["dt"], part["vi"], part["pi"], 2)
+        t.close()
     w = b2g.B2world(gravity=part["gravity"], num_worlds=part["num_worlds"], device=device)
     w.set_allow_sleeping(False)
     scenes.build_world(w, part)
     for _ in range(warmup):
         w.step(part["dt"], part["vi"], part["pi"])
     w.synchronize()
+    launch_config = w.get_launch_config()
     if world_size > 1:
         torch.distributed.barrier()
     batch_ms = timed_steps(w, part, steps, flush, torch)
@@ -254,6 +262,7 @@ def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_
     sequential = num_worlds * steps / (est_ms / 1e3)
     return {"metric": "world-steps/s, 4096 uneven worlds (16-2048 bodies)", "value": batched,
             "ranks": world_size, "sharding": "contiguous world ranges, no collective" if world_size > 1 else None,
+            "launch_config": launch_config,
             "unit": "world-steps/s", "body_steps_per_s": scene["n_dynamic"] * steps / (batch_ms / 1e3),
             "bodies": scene["n_dynamic"], "steps": steps, "ms_per_step": batch_ms / steps,
             "sequential_single_world_gpu": {"value": sequential, "unit": "world-steps/s",
@@ -338,6 +347,7 @@ def main():
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels directly instead of CUDA graphs")
     ap.add_argument("--batched-steps", type=int, default=300, help="steps of the 4096-world leg (0 skips it)")
     ap.add_argument("--adjoint-steps", type=int, default=240, help="steps of the differentiable leg (0 skips it)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
     ap.add_argument("--skip-steps", type=int, default=0,
                     help="untimed steps before the warm-up (profiling a later window of the scene)")
     ap.add_argument("--profile-window", action="store_true",
@@ -374,15 +384,24 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
+    dt, vi, pi = scene["dt"], scene["vi"], scene["pi"]
+    if not args.no_autotune:
+        # tune on a scratch world of the same scene; the measured world inherits the choice
+        # through the size-bucket cache
+        t = b2g.B2world(gravity=scene["gravity"], device=local_rank)
+        t.set_allow_sleeping(False)
+        scenes.build_world(t, scene)
+        t.autotune(dt, vi, pi, 2)
+        t.close()
     w = b2g.B2world(gravity=scene["gravity"], device=local_rank)
     w.set_allow_sleeping(False)
     w.set_continuous_physics(False)
     w.set_graph_capture(not args.no_graphs)
     scenes.build_world(w, scene)
-    dt, vi, pi = scene["dt"], scene["vi"], scene["pi"]
     for _ in range(args.skip_steps + args.warmup):
         w.step(dt, vi, pi)
     w.synchronize()
+    config["launch_config"] = w.get_launch_config()
 
     sampler = ClockSampler(local_rank)
     if world_size > 1:
@@ -467,7 +486,7 @@ def main():
     }
     if args.batched_steps > 0:
         line["batched"] = run_batched(torch, flush, local_rank, steps=args.batched_steps, warmup=args.warmup,
-                                      rank=rank, world_size=world_size)
+                                      rank=rank, world_size=world_size, autotune=not args.no_autotune)
     if args.adjoint_steps > 0 and rank == 0:
         line["adjoint"] = run_adjoint(torch, flush, local_rank, steps=args.adjoint_steps)
     if rank == 0 and not args.no_cpu_baseline:

@@ -180,6 +180,14 @@ TAPE_STEP = np.dtype(
 assert TAPE_SLOT.itemsize == 144 and TAPE_STEP.itemsize == 48
 
 
+class LaunchConfig(ctypes.Structure):
+    _fields_ = [("coop_blocks_per_sm", ctypes.c_int32), ("collide_block", ctypes.c_int32),
+                ("traverse_block", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_ if n != "pad"}
+
+
 class TapeInfo(ctypes.Structure):
     _fields_ = [
         ("recording", ctypes.c_int32),
@@ -376,6 +384,9 @@ def load_library(path=LIB_PATH):
         "b2g_set_record_pairs": [vp, i32],
         "b2g_set_graph_capture": [vp, i32],
         "b2g_get_phase_times": [vp, vp, i32],
+        "b2g_get_launch_config": [vp, ctypes.POINTER(LaunchConfig)],
+        "b2g_set_launch_config": [vp, ctypes.POINTER(LaunchConfig)],
+        "b2g_autotune": [vp, f32, i32, i32, i32, ctypes.POINTER(LaunchConfig)],
         "b2g_tape_begin": [vp, i32, i32, ctypes.c_int64],
         "b2g_tape_end": [vp],
         "b2g_tape_info_get": [vp, ctypes.POINTER(TapeInfo)],
@@ -595,6 +606,25 @@ class B2world:
 
     def get_solver_order(self):
         return self._get_list(self._lib.b2g_get_solver_order, np.uint32, 65536, 2).reshape(-1, 2)
+
+    # ---- launch configuration ----
+    def get_launch_config(self):
+        c = LaunchConfig()
+        self._check(self._lib.b2g_get_launch_config(self._h, ctypes.byref(c)))
+        return c.as_dict()
+
+    def set_launch_config(self, coop_blocks_per_sm=1, collide_block=128, traverse_block=256):
+        c = LaunchConfig(coop_blocks_per_sm, collide_block, traverse_block, 0)
+        self._check(self._lib.b2g_set_launch_config(self._h, ctypes.byref(c)))
+
+    def autotune(self, dt, velocity_iterations, position_iterations, steps_per_candidate=4):
+        """Pick the fastest launch configuration on the world's next steps (they are real steps)."""
+        c = LaunchConfig()
+        self._check(self._lib.b2g_autotune(self._h, dt, velocity_iterations, position_iterations,
+                                           steps_per_candidate, ctypes.byref(c)))
+        return c.as_dict()
+
+    AUTOTUNE_CANDIDATES = 2 + 3 + 3  # one untimed + steps_per_candidate timed steps each
 
     # ---- differentiable step ----
     def tape_begin(self, max_steps, checkpoint_interval=16, max_slots=0):

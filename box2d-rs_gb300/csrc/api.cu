@@ -57,6 +57,15 @@ struct GraphSlot {
     GraphKey key{};
 };
 
+/* launch configuration: the user's (b2g_set_launch_config), else the autotuner's choice for the
+ * world's size bucket if one was made in this process, else the defaults */
+struct LaunchCfg {
+    int coop_per_sm = 1, collide_block = 128, traverse_block = 256;
+};
+
+std::mutex g_tune_mutex;
+std::vector<std::pair<int, LaunchCfg>> g_tuned;  /* (size bucket, configuration) */
+
 /* The step tape of a world and the work buffers of its last backward pass. */
 struct TapeHost {
     bool recording = false;
@@ -117,7 +126,32 @@ struct World {
     int alloc_generation = 0;
     int minsep_buffers = 2;  /* position-iteration separation buffers held in d.isl_minsep */
     TapeHost* tape = nullptr;
+    LaunchCfg cfg;
+    bool cfg_set = false;    /* chosen by the user or the autotuner: no bucket lookup */
 };
+
+/* bucket: log2 of the bodies per world (batched worlds of uneven size use the mean), and
+ * whether the world is a batch */
+int size_bucket(const World* w) {
+    const size_t nb = w->h_flags.size();
+    const size_t per = nb / (size_t)(w->num_worlds > 0 ? w->num_worlds : 1);
+    int b = 0;
+    while ((size_t(1) << (b + 1)) <= per) ++b;
+    return b * 2 + (w->num_worlds > 1 ? 1 : 0);
+}
+
+void apply_launch_config(World* w) {
+    if (!w->cfg_set) {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        const int b = size_bucket(w);
+        for (auto& e : g_tuned)
+            if (e.first == b) w->cfg = e.second;
+    }
+    w->d.cfg_coop_per_sm = w->cfg.coop_per_sm;
+    w->d.cfg_collide_block = w->cfg.collide_block;
+    w->d.cfg_traverse_block = w->cfg.traverse_block;
+}
+
 
 /* an edit between taped steps that the tape cannot represent */
 void tape_touch(World* w) {
@@ -463,6 +497,7 @@ int allocate(World* w, int nb, int nf) {
     d.event_cap = contact_cap;
     d.cons_cap = contact_cap;
     d.num_worlds = w->num_worlds;
+    apply_launch_config(w);
     int rc = B2G_OK;
 #define A(ptr, n)                                      \
     do {                                               \
@@ -1588,6 +1623,113 @@ int b2g_get_solver_order(void* p, uint32_t* out, int32_t cap, int32_t* n) {
     if (!out || cap < nc || nc == 0) return B2G_OK;
     CUDA_OK(w, cudaMemcpy(out, w->d.s_fix, nc * sizeof(int2), cudaMemcpyDeviceToHost));
     return B2G_OK;
+}
+
+}  // extern "C"
+
+/* ---- launch configuration and the autotuner ---- */
+
+extern "C" {
+
+int b2g_get_launch_config(void* p, b2g_launch_config* out) {
+    World* w = W(p);
+    if (!w || !out) return B2G_ERR_INVALID_ARG;
+    out->coop_blocks_per_sm = w->cfg.coop_per_sm;
+    out->collide_block = w->cfg.collide_block;
+    out->traverse_block = w->cfg.traverse_block;
+    out->pad = 0;
+    return B2G_OK;
+}
+
+int b2g_set_launch_config(void* p, const b2g_launch_config* c) {
+    World* w = W(p);
+    if (!w || !c) return B2G_ERR_INVALID_ARG;
+    auto pow2 = [](int v, int lo, int hi) { return v >= lo && v <= hi && (v & (v - 1)) == 0; };
+    if (c->coop_blocks_per_sm < 1 || c->coop_blocks_per_sm > 2 || !pow2(c->collide_block, 32, 256) ||
+        !pow2(c->traverse_block, 32, 256))
+        return fail(w, B2G_ERR_INVALID_ARG, "coop_blocks_per_sm in {1, 2}; block sizes powers of two in [32, 256]");
+    w->cfg.coop_per_sm = c->coop_blocks_per_sm;
+    w->cfg.collide_block = c->collide_block;
+    w->cfg.traverse_block = c->traverse_block;
+    w->cfg_set = true;
+    apply_launch_config(w);
+    drop_graphs(w);
+    return B2G_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+/* device milliseconds of `steps` steps (CUDA events around each step, summed) */
+int timed_steps(World* w, float dt, int vi, int pi, int steps, double* ms) {
+    *ms = 0.0;
+    for (int i = 0; i < steps; ++i) {
+        int rc = step(w, dt, vi, pi);
+        if (rc != B2G_OK) return rc;
+        rc = check_status(w);
+        if (rc != B2G_OK) return rc;
+        float t = 0.0f;
+        CUDA_OK(w, cudaEventElapsedTime(&t, w->timer.e[0], w->timer.e[5]));
+        *ms += t;
+    }
+    return B2G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+/* Coordinate search over the launch configuration on the world's own next steps: for each knob in
+ * turn (persistent-kernel blocks per SM, narrowphase block, traversal block) every candidate runs
+ * one untimed step (graph capture) and `steps_per_candidate` timed steps; the fastest is kept.
+ * The steps are real steps of the world (the configuration never changes results). The choice is
+ * applied to the world and remembered for later worlds of the same size bucket in this process. */
+int b2g_autotune(void* p, float dt, int32_t vi, int32_t pi, int32_t steps_per_candidate, b2g_launch_config* out) {
+    World* w = W(p);
+    if (!w || steps_per_candidate < 1 || !(dt > 0.0f)) return B2G_ERR_INVALID_ARG;
+    if (w->tape && w->tape->recording) return fail(w, B2G_ERR_INVALID_ARG, "not while a tape is recording");
+    if (w->h_flags.empty()) return fail(w, B2G_ERR_INVALID_ARG, "the world has no bodies");
+    LaunchCfg best = w->cfg;
+    w->cfg_set = true;
+    const int coop[] = {1, 2}, collide[] = {64, 128, 256}, traverse[] = {64, 128, 256};
+    for (int knob = 0; knob < 3; ++knob) {
+        const int* cand = knob == 0 ? coop : knob == 1 ? collide : traverse;
+        const int nc = knob == 0 ? 2 : 3;
+        double best_ms = 1e300;
+        int best_v = 0;
+        for (int i = 0; i < nc; ++i) {
+            LaunchCfg c = best;
+            (knob == 0 ? c.coop_per_sm : knob == 1 ? c.collide_block : c.traverse_block) = cand[i];
+            w->cfg = c;
+            apply_launch_config(w);
+            drop_graphs(w);
+            double ms = 0.0;
+            int rc = timed_steps(w, dt, vi, pi, 1, &ms);
+            if (rc == B2G_OK) rc = timed_steps(w, dt, vi, pi, steps_per_candidate, &ms);
+            if (rc != B2G_OK) return rc;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_v = cand[i];
+            }
+        }
+        (knob == 0 ? best.coop_per_sm : knob == 1 ? best.collide_block : best.traverse_block) = best_v;
+    }
+    w->cfg = best;
+    apply_launch_config(w);
+    drop_graphs(w);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        const int b = size_bucket(w);
+        bool found = false;
+        for (auto& e : g_tuned)
+            if (e.first == b) {
+                e.second = best;
+                found = true;
+            }
+        if (!found) g_tuned.emplace_back(b, best);
+    }
+    return b2g_get_launch_config(p, out);
 }
 
 }  // extern "C"

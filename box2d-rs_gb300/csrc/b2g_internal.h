@@ -108,6 +108,10 @@ struct StepParams {
 
 struct DevWorld {
     int body_cap, fix_cap, contact_cap, pair_cap, event_cap, cons_cap;
+    /* launch configuration (b2g_set_launch_config / b2g_autotune); results do not depend on it */
+    int cfg_coop_per_sm;      /* blocks per SM of the cooperative colouring and solver kernels */
+    int cfg_collide_block;    /* threads per block of the narrowphase */
+    int cfg_traverse_block;   /* threads per block of the broadphase traversal */
     int n_bodies, n_fixtures, num_worlds;
     int key_bits;      /* bits of the contact key (2 x refid bits) */
     int morton_world_bits;

@@ -436,7 +436,8 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
         k_bp_leaves<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_refit<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_rows<<<grid_for(w.contact_cap, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
-        k_bp_traverse<<<gf, kBlock, 0, s>>>(w, sp); B2G_LAUNCHED(1);
+        const int tb = w.cfg_traverse_block;
+        k_bp_traverse<<<grid_for(n, tb, num_sms * 2048 / tb), tb, 0, s>>>(w, sp); B2G_LAUNCHED(1);
         k_bp_clear_moved<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
     }
     k_bp_clamp_new<<<1, 32, 0, s>>>(w); B2G_LAUNCHED(1);

@@ -43,7 +43,7 @@ __device__ __forceinline__ Xf load_xf(const DevWorld& w, int b) {
     return r;
 }
 
-__global__ void __launch_bounds__(128) k_collide(DevWorld w, StepParams sp) {
+__global__ void __launch_bounds__(256) k_collide(DevWorld w, StepParams sp) {
     const int n = w.cnt[CNT_CONTACTS];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t flags = w.c.flags[i];
@@ -118,7 +118,8 @@ __global__ void __launch_bounds__(128) k_collide(DevWorld w, StepParams sp) {
 }
 
 void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s) {
-    k_collide<<<grid_for(w.contact_cap, 128, 152 * 16), 128, 0, s>>>(w, sp); B2G_LAUNCHED(1);
+    const int block = w.cfg_collide_block;
+    k_collide<<<grid_for(w.contact_cap, block, 152 * 2048 / block), block, 0, s>>>(w, sp); B2G_LAUNCHED(1);
 }
 
 /* Stand-alone manifolds of independent shape pairs (the public b2_collide_* functions,

@@ -872,10 +872,12 @@ __global__ void k_clear_forces(DevWorld w) {
         w.b_force[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
-/* One block per SM: the persistent kernels are bound by grid-barrier latency, which grows with
- * the number of arriving blocks (measured on the 100k-body scene: 152 blocks take 21% less solver
- * time than 304); one block of 256 threads per SM still covers a colour of ~39k slots in a single
- * pass. (If not even one block fit, the cooperative launch would fail and the step report it.) */
+/* Blocks of the persistent kernels: one per SM by default (cfg_coop_per_sm = 1). They are bound
+ * by grid-barrier latency, which grows with the number of arriving blocks (on the 100k-body scene
+ * 152 blocks take 21% less solver time than 304); one block of 256 threads per SM still covers a
+ * colour of ~39k slots in a single pass. The autotuner may pick two per SM (both fit at the
+ * kernels' register counts). If a block did not fit, the cooperative launch would fail and the
+ * step report it. */
 int coop_blocks(const void* fn, int num_sms) {
     (void)fn;
     return num_sms;
@@ -901,8 +903,7 @@ void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cud
 }
 
 void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms) {
-    static int blocks = 0;
-    if (!blocks) blocks = coop_blocks((const void*)k_colour, num_sms);
+    const int blocks = coop_blocks((const void*)k_colour, num_sms) * w.cfg_coop_per_sm;
     DevWorld wc = w;
     void* args[] = {&wc};
     cudaLaunchCooperativeKernel((const void*)k_colour, dim3(blocks), dim3(kBlock), args, 0, s);
@@ -910,8 +911,7 @@ void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms) {
 }
 
 int launch_solver(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms) {
-    static int blocks = 0;
-    if (!blocks) blocks = coop_blocks((const void*)k_solve, num_sms);
+    const int blocks = coop_blocks((const void*)k_solve, num_sms) * w.cfg_coop_per_sm;
     DevWorld wc = w;
     StepParams spc = sp;
     void* args[] = {&wc, &spc};

@@ -303,6 +303,24 @@ int b2g_tape_get_step(void* world, int32_t step, b2g_tape_step* out_step, int32_
  * (state before step index x interval), or after the last taped step for index = -1. */
 int b2g_tape_get_checkpoint(void* world, int32_t index, float* out, uint32_t count);
 
+/* ---- launch configuration and autotuner (no counterpart in the reference) ----
+ * How the step's kernels are launched; results are bit-identical for every configuration. */
+typedef struct b2g_launch_config {
+    int32_t coop_blocks_per_sm;   /* persistent colouring/solver kernels: 1 or 2 blocks per SM */
+    int32_t collide_block;        /* narrowphase threads per block: 32..256, power of two */
+    int32_t traverse_block;       /* broadphase traversal threads per block: 32..256, power of two */
+    int32_t pad;
+} b2g_launch_config;
+int b2g_get_launch_config(void* world, b2g_launch_config* out);
+int b2g_set_launch_config(void* world, const b2g_launch_config* config);
+/* Time the world's next steps under candidate configurations (one knob at a time: blocks per SM,
+ * narrowphase block, traversal block; each candidate 1 untimed + steps_per_candidate timed steps),
+ * keep the fastest for this world and for later worlds of the same size bucket (log2 bodies per
+ * world, single or batch) created in this process. The tuning steps are ordinary steps of the
+ * world with the given dt and iterations. */
+int b2g_autotune(void* world, float dt, int32_t velocity_iterations, int32_t position_iterations,
+                 int32_t steps_per_candidate, b2g_launch_config* out);
+
 /* ---- parity hooks ---- */
 /* Record every pair the broadphase emits (off by default; needed by b2g_get_pairs). */
 int b2g_set_record_pairs(void* world, int32_t flag);
