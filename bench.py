@@ -453,7 +453,7 @@ def main():
         w.step(dt, vi, pi)
         w.get_body_states(out=states)
     e2e_s = time.perf_counter() - t0
-    d2h = w.body_count * 48  # three float4 arrays per body
+    d2h = w.body_count * 32  # one b2g_body_state (32 bytes) per body
     w.close()
 
     if world_size > 1:

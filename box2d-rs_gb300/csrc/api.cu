@@ -128,6 +128,9 @@ struct World {
     TapeHost* tape = nullptr;
     LaunchCfg cfg;
     bool cfg_set = false;    /* chosen by the user or the autotuner: no bucket lookup */
+    bool pageable = false;   /* the device reads/writes pageable host memory coherently */
+    b2g_body_state* d_states = nullptr;  /* packing buffer for b2g_get_body_states otherwise */
+    int d_states_cap = 0;
 };
 
 /* bucket: log2 of the bodies per world (batched worlds of uneven size use the mean), and
@@ -848,6 +851,20 @@ int step(World* w, float dt, int vi, int pi) {
 
 World* W(void* p) { return (World*)p; }
 
+/* b2g_body_state of bodies [first, first + count) */
+__global__ void k_pack_states(DevWorld d, uint32_t first, uint32_t count, b2g_body_state* out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const float4 xf = d.b_xf[first + i], pos = d.b_pos[first + i], vel = d.b_vel[first + i];
+        b2g_body_state s;
+        s.position = b2g_vec2{xf.x, xf.y};
+        s.angle = pos.z;
+        s.linear_velocity = b2g_vec2{vel.x, vel.y};
+        s.angular_velocity = vel.z;
+        s.world_center = b2g_vec2{pos.x, pos.y};
+        out[i] = s;
+    }
+}
+
 /* small body edits after the device became authoritative */
 __global__ void k_body_op(DevWorld d, int op, int b, float x, float y, float z, float px, float py, int wake) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -954,6 +971,7 @@ int b2g_world_create(const b2g_world_def* def, void** out) {
         return B2G_ERR_CUDA;
     }
     w->num_sms = prop.multiProcessorCount;
+    w->pageable = prop.pageableMemoryAccess != 0;
     if (!prop.cooperativeLaunch) {
         cudaStreamDestroy(w->stream);
         delete w;
@@ -968,6 +986,7 @@ int b2g_world_destroy(void* p) {
     if (!w) return B2G_ERR_INVALID_ARG;
     cudaStreamSynchronize(w->stream);
     tape_free(w);
+    if (w->d_states) cudaFree(w->d_states);
     free_all(w);
     if (w->timer.valid)
         for (auto& e : w->timer.e) cudaEventDestroy(e);
@@ -1089,14 +1108,33 @@ int b2g_get_body_states(void* p, uint32_t first, uint32_t count, b2g_body_state*
     World* w = W(p);
     if (!w || (!out && count > 0)) return B2G_ERR_INVALID_ARG;
     if ((size_t)first + count > w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body range out of bounds");
-    std::vector<float4> xf(count), pos(count), vel(count);
+    if (count == 0) return B2G_OK;
     if (w->device_authoritative && (int)(first + count) <= w->uploaded_bodies) {
-        int rc = check_status(w);
-        if (rc != B2G_OK) return rc;
-        CUDA_OK(w, cudaMemcpy(xf.data(), w->d.b_xf + first, count * sizeof(float4), cudaMemcpyDeviceToHost));
-        CUDA_OK(w, cudaMemcpy(pos.data(), w->d.b_pos + first, count * sizeof(float4), cudaMemcpyDeviceToHost));
-        CUDA_OK(w, cudaMemcpy(vel.data(), w->d.b_vel + first, count * sizeof(float4), cudaMemcpyDeviceToHost));
-    } else {
+        /* one kernel packs the caller's layout; with coherent access to pageable host memory
+         * (Grace's C2C link) it writes straight into the caller's buffer, else into a device
+         * buffer that is copied out in one piece */
+        const int grid = grid_for((int)count, 256, w->num_sms * 8);
+        if (w->pageable) {
+            k_pack_states<<<grid, 256, 0, w->stream>>>(w->d, first, count, out);
+            B2G_LAUNCHED(1);
+            CUDA_OK(w, cudaGetLastError());
+        } else {
+            if (w->d_states_cap < (int)count) {
+                if (w->d_states) cudaFree(w->d_states);
+                w->d_states = nullptr;
+                w->d_states_cap = 0;
+                CUDA_OK(w, cudaMalloc((void**)&w->d_states, count * sizeof(b2g_body_state)));
+                w->d_states_cap = (int)count;
+            }
+            k_pack_states<<<grid, 256, 0, w->stream>>>(w->d, first, count, w->d_states);
+            B2G_LAUNCHED(1);
+            CUDA_OK(w, cudaMemcpyAsync(out, w->d_states, count * sizeof(b2g_body_state), cudaMemcpyDeviceToHost,
+                                       w->stream));
+        }
+        return check_status(w);  /* waits for the stream and reports device-side errors */
+    }
+    std::vector<float4> xf(count), pos(count), vel(count);
+    {
         if (w->device_authoritative) {
             int rc = download_state(w);
             if (rc != B2G_OK) return rc;
