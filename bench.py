@@ -206,7 +206,9 @@ def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_
         t = b2g.B2world(gravity=part["gravity"], num_worlds=part["num_worlds"], device=device)
         t.set_allow_sleeping(False)
         scenes.build_world(t, part)
-        t.autotune(part["dt"], part["vi"], part["pi"], 2)
+        for _ in range(warmup + steps // 2):
+            t.step(part["dt"], part["vi"], part["pi"])
+        t.autotune(part["dt"], part["vi"], part["pi"], 3)
         t.close()
     w = b2g.B2world(gravity=part["gravity"], num_worlds=part["num_worlds"], device=device)
     w.set_allow_sleeping(False)
@@ -386,12 +388,15 @@ def main():
 
     dt, vi, pi = scene["dt"], scene["vi"], scene["pi"]
     if not args.no_autotune:
-        # tune on a scratch world of the same scene; the measured world inherits the choice
+        # tune on a scratch world of the same scene, advanced to the middle of the timed window
+        # (the scene is sparse in its first steps); the measured world inherits the choice
         # through the size-bucket cache
         t = b2g.B2world(gravity=scene["gravity"], device=local_rank)
         t.set_allow_sleeping(False)
         scenes.build_world(t, scene)
-        t.autotune(dt, vi, pi, 2)
+        for _ in range(args.skip_steps + args.warmup + args.steps // 2):
+            t.step(dt, vi, pi)
+        t.autotune(dt, vi, pi, 3)
         t.close()
     w = b2g.B2world(gravity=scene["gravity"], device=local_rank)
     w.set_allow_sleeping(False)
