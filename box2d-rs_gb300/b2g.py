@@ -137,6 +137,9 @@ CONTACT_INFO = np.dtype(
 
 EVENT = np.dtype([("kind", "<i4"), ("fixture_a", "<u4"), ("fixture_b", "<u4")])
 
+RAY_HIT = np.dtype([("fixture", "<i4"), ("point", "<f4", (2,)), ("normal", "<f4", (2,)), ("fraction", "<f4")])
+assert RAY_HIT.itemsize == 24
+
 # b2g_tape_slot / b2g_tape_step (include/b2g.h)
 TAPE_SLOT = np.dtype(
     [
@@ -384,6 +387,8 @@ def load_library(path=LIB_PATH):
         "b2g_set_record_pairs": [vp, i32],
         "b2g_set_graph_capture": [vp, i32],
         "b2g_get_phase_times": [vp, vp, i32],
+        "b2g_ray_cast_closest": [vp, vp, vp, i32, vp],
+        "b2g_query_aabb": [vp, vp, vp, i32, vp, i32, ctypes.POINTER(i32)],
         "b2g_get_launch_config": [vp, ctypes.POINTER(LaunchConfig)],
         "b2g_set_launch_config": [vp, ctypes.POINTER(LaunchConfig)],
         "b2g_autotune": [vp, f32, i32, i32, i32, ctypes.POINTER(LaunchConfig)],
@@ -606,6 +611,32 @@ class B2world:
 
     def get_solver_order(self):
         return self._get_list(self._lib.b2g_get_solver_order, np.uint32, 65536, 2).reshape(-1, 2)
+
+    # ---- world queries (B2world::ray_cast / query_aabb) ----
+    def ray_cast_closest(self, rays, world_index=None):
+        """Closest hit per ray; rays (n, 4) = p1.x, p1.y, p2.x, p2.y. Returns a RAY_HIT array."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 4)
+        wi = None if world_index is None else np.ascontiguousarray(world_index, np.uint32)
+        out = np.zeros(len(rays), RAY_HIT)
+        self._check(self._lib.b2g_ray_cast_closest(self._h, _ptr(rays), None if wi is None else _ptr(wi), len(rays),
+                                                   _ptr(out)))
+        return out
+
+    def query_aabb(self, boxes, world_index=None):
+        """(m, 2) array of (box index, fixture) for every fat AABB overlapping each box."""
+        boxes = np.ascontiguousarray(boxes, np.float32).reshape(-1, 4)
+        wi = None if world_index is None else np.ascontiguousarray(world_index, np.uint32)
+        n = ctypes.c_int32(0)
+        cap = max(64, 16 * len(boxes))
+        while True:
+            out = np.zeros((cap, 2), np.uint32)
+            rc = self._lib.b2g_query_aabb(self._h, _ptr(boxes), None if wi is None else _ptr(wi), len(boxes),
+                                          _ptr(out), cap, ctypes.byref(n))
+            if rc == -3 and n.value > cap:
+                cap = n.value
+                continue
+            self._check(rc)
+            return out[: n.value]
 
     # ---- launch configuration ----
     def get_launch_config(self):

@@ -1665,6 +1665,103 @@ int b2g_get_solver_order(void* p, uint32_t* out, int32_t cap, int32_t* n) {
 
 }  // extern "C"
 
+/* ---- world queries ---- */
+
+extern "C" {
+
+int b2g_ray_cast_closest(void* p, const float* rays, const uint32_t* world_index, int32_t n, b2g_ray_hit* out) {
+    World* w = W(p);
+    if (!w || n < 0 || (n > 0 && (!rays || !out))) return B2G_ERR_INVALID_ARG;
+    if (n == 0) return B2G_OK;
+    if (!w->allocated || w->steps == 0) return fail(w, B2G_ERR_INVALID_ARG, "queries use the last step's hierarchy: step once first");
+    int rc = check_status(w);
+    if (rc != B2G_OK) return rc;
+    float4 *d_rays = nullptr, *d_a = nullptr, *d_b = nullptr;
+    uint32_t* d_world = nullptr;
+    cudaStream_t s = w->stream;
+    cudaError_t e = cudaMalloc((void**)&d_rays, n * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_a, n * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_b, n * sizeof(float4));
+    if (e == cudaSuccess && world_index) e = cudaMalloc((void**)&d_world, n * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_rays, rays, n * sizeof(float4), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && world_index)
+        e = cudaMemcpyAsync(d_world, world_index, n * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+    std::vector<float4> a(n), b(n);
+    if (e == cudaSuccess) {
+        launch_ray_cast(w->d, d_rays, d_world, n, d_a, d_b, s);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(a.data(), d_a, n * sizeof(float4), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b.data(), d_b, n * sizeof(float4), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d_rays);
+    cudaFree(d_a);
+    cudaFree(d_b);
+    if (d_world) cudaFree(d_world);
+    if (e != cudaSuccess) return fail(w, B2G_ERR_CUDA, cudaGetErrorString(e));
+    for (int i = 0; i < n; ++i) {
+        int f;
+        memcpy(&f, &a[i].x, 4);
+        out[i].fixture = f;
+        out[i].point = b2g_vec2{a[i].y, a[i].z};
+        out[i].normal = b2g_vec2{b[i].x, b[i].y};
+        out[i].fraction = b[i].z;
+    }
+    return check_status(w);
+}
+
+int b2g_query_aabb(void* p, const float* boxes, const uint32_t* world_index, int32_t n, uint32_t* out_pairs,
+                   int32_t capacity, int32_t* out_count) {
+    World* w = W(p);
+    if (!w || n < 0 || !out_count || (n > 0 && !boxes) || capacity < 0 || (capacity > 0 && !out_pairs))
+        return B2G_ERR_INVALID_ARG;
+    *out_count = 0;
+    if (n == 0) return B2G_OK;
+    if (!w->allocated || w->steps == 0) return fail(w, B2G_ERR_INVALID_ARG, "queries use the last step's hierarchy: step once first");
+    int rc = check_status(w);
+    if (rc != B2G_OK) return rc;
+    const int cap = capacity > 0 ? capacity : 1;
+    float4* d_boxes = nullptr;
+    uint32_t* d_world = nullptr;
+    uint2* d_out = nullptr;
+    int* d_count = nullptr;
+    cudaStream_t s = w->stream;
+    cudaError_t e = cudaMalloc((void**)&d_boxes, n * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_out, (size_t)cap * sizeof(uint2));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_count, sizeof(int));
+    if (e == cudaSuccess && world_index) e = cudaMalloc((void**)&d_world, n * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_boxes, boxes, n * sizeof(float4), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && world_index)
+        e = cudaMemcpyAsync(d_world, world_index, n * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_count, 0, sizeof(int), s);
+    if (e == cudaSuccess) {
+        launch_query_aabb(w->d, d_boxes, d_world, n, d_out, cap, d_count, s);
+        e = cudaGetLastError();
+    }
+    int total = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&total, d_count, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    std::vector<uint2> pairs(std::min(total, cap > 0 ? cap : 0));
+    if (e == cudaSuccess && !pairs.empty())
+        e = cudaMemcpy(pairs.data(), d_out, pairs.size() * sizeof(uint2), cudaMemcpyDeviceToHost);
+    cudaFree(d_boxes);
+    cudaFree(d_out);
+    cudaFree(d_count);
+    if (d_world) cudaFree(d_world);
+    if (e != cudaSuccess) return fail(w, B2G_ERR_CUDA, cudaGetErrorString(e));
+    *out_count = total;
+    if (total > capacity) return fail(w, B2G_ERR_CAPACITY, "more overlaps than capacity; *out_count holds the total");
+    std::sort(pairs.begin(), pairs.end(),
+              [](const uint2& x, const uint2& y) { return x.x != y.x ? x.x < y.x : x.y < y.y; });
+    for (size_t i = 0; i < pairs.size(); ++i) {
+        out_pairs[2 * i] = pairs[i].x;
+        out_pairs[2 * i + 1] = pairs[i].y;
+    }
+    return check_status(w);
+}
+
+}  // extern "C"
+
 /* ---- launch configuration and the autotuner ---- */
 
 extern "C" {

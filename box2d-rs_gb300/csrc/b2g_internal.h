@@ -196,6 +196,12 @@ void launch_clear_forces(const DevWorld& w, cudaStream_t s);
 void launch_collide_pairs(const ShapeRec* a, const float4* xa, const ShapeRec* b, const float4* xb, const int* kind,
                           int n, float4* geo, float4* pts, uint4* ids, cudaStream_t s);
 
+/* world queries on the last step's LBVH (k_query.cu) */
+void launch_ray_cast(const DevWorld& w, const float4* rays, const uint32_t* ray_world, int n, float4* out_a,
+                     float4* out_b, cudaStream_t s);
+void launch_query_aabb(const DevWorld& w, const float4* boxes, const uint32_t* box_world, int n, uint2* out, int cap,
+                       int* count, cudaStream_t s);
+
 /* primitives (k_prims.cu) */
 void scan_exclusive_u32(const uint32_t* in, uint32_t* out, const int* d_n, int max_n, uint32_t* tmp, int* d_total,
                         cudaStream_t s);

@@ -303,6 +303,27 @@ int b2g_tape_get_step(void* world, int32_t step, b2g_tape_step* out_step, int32_
  * (state before step index x interval), or after the last taped step for index = -1. */
 int b2g_tape_get_checkpoint(void* world, int32_t index, float* out, uint32_t count);
 
+/* ---- world queries: B2world::query_aabb / ray_cast (private/dynamics/b2_world.rs:969-1056),
+ *      many per call, on the hierarchy of the last step's broadphase (fat AABBs as of that step;
+ *      the world must have stepped once) ---- */
+typedef struct b2g_ray_hit {
+    int32_t fixture;            /* -1: no hit */
+    b2g_vec2 point;             /* (1 - fraction) * p1 + fraction * p2 */
+    b2g_vec2 normal;
+    float fraction;
+} b2g_ray_hit;
+/* Closest hit of each ray p1 -> p2 (rays: n x (p1.x, p1.y, p2.x, p2.y)), i.e. the result of the
+ * reference's ray cast with a callback that returns the reported fraction (clipping the ray).
+ * world_index: per ray, which world of a batch (NULL: world 0). Among hits at exactly the same
+ * fraction the GPU reports the first its hierarchy meets, which can differ from the reference. */
+int b2g_ray_cast_closest(void* world, const float* rays, const uint32_t* world_index, int32_t n, b2g_ray_hit* out);
+/* Fixtures whose fat AABB overlaps each box (boxes: n x (lower.x, lower.y, upper.x, upper.y)), as
+ * (box index, fixture) pairs sorted by box then fixture (the reference reports the same set per
+ * box through its query callback, in tree order). *out_count = total pairs; at most capacity are
+ * written (B2G_ERR_CAPACITY if more exist). */
+int b2g_query_aabb(void* world, const float* boxes, const uint32_t* world_index, int32_t n, uint32_t* out_pairs,
+                   int32_t capacity, int32_t* out_count);
+
 /* ---- launch configuration and autotuner (no counterpart in the reference) ----
  * How the step's kernels are launched; results are bit-identical for every configuration. */
 typedef struct b2g_launch_config {

@@ -13,6 +13,7 @@
 #ifndef B2_ORACLE_TREE_H
 #define B2_ORACLE_TREE_H
 
+#include <cmath>
 #include <vector>
 #include "b2_oracle_math.h"
 
@@ -59,6 +60,48 @@ class DynamicTree {
                     stack_.push_back(n.child1);
                     stack_.push_back(n.child2);
                 }
+            }
+        }
+    }
+
+    /* ray_cast, src/b2_dynamic_tree.rs:269-347: cb(max_fraction, proxy) returns the client's
+     * value: 0 stops the cast, a positive value clips the segment to that fraction */
+    template <class F>
+    void ray_cast(Vec2 p1, Vec2 p2, float max_fraction, F&& cb) const {
+        Vec2 r = p2 - p1;
+        normalize(r);
+        const Vec2 v = Vec2{-1.0f * r.y, 1.0f * r.x};  /* b2_cross_scalar_by_vec(1, r) */
+        const Vec2 abs_v = Vec2{std::fabs(v.x), std::fabs(v.y)};
+        AABB seg;
+        {
+            const Vec2 t = p1 + max_fraction * (p2 - p1);
+            seg.lo = vmin(p1, t);
+            seg.hi = vmax(p1, t);
+        }
+        stack_.clear();
+        stack_.push_back(root_);
+        while (!stack_.empty()) {
+            const int id = stack_.back();
+            stack_.pop_back();
+            if (id == kNullNode) continue;
+            const TreeNode& n = nodes_[id];
+            if (!overlap(n.aabb, seg)) continue;
+            const Vec2 c = 0.5f * (n.aabb.lo + n.aabb.hi);
+            const Vec2 h = 0.5f * (n.aabb.hi - n.aabb.lo);
+            const float separation = std::fabs(dot(v, p1 - c)) - dot(abs_v, h);
+            if (separation > 0.0f) continue;
+            if (n.is_leaf()) {
+                const float value = cb(max_fraction, id);
+                if (value == 0.0f) return;
+                if (value > 0.0f) {
+                    max_fraction = value;
+                    const Vec2 t = p1 + max_fraction * (p2 - p1);
+                    seg.lo = vmin(p1, t);
+                    seg.hi = vmax(p1, t);
+                }
+            } else {
+                stack_.push_back(n.child1);
+                stack_.push_back(n.child2);
             }
         }
     }

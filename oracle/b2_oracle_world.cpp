@@ -1386,3 +1386,132 @@ int ora_collide(const b2g_fixture_def* da, const float* xfa, const b2g_fixture_d
 }
 
 }  // extern "C"
+
+/* ---- world queries (B2world::query_aabb / ray_cast, private/dynamics/b2_world.rs:969-1056) ---- */
+
+namespace {
+
+/* fixture ray casts: B2circleShape (private/collision/b2_circle_shape.rs:26-59), B2polygonShape
+ * (private/collision/b2_polygon_shape.rs:226-287, whose lower bound starts at 0.032), B2edgeShape
+ * (private/collision/b2_edge_shape.rs:39-102) */
+bool shape_ray_cast(const Shape& sh, const Xf& xf, Vec2 ip1, Vec2 ip2, float max_fraction, float* fraction,
+                    Vec2* normal) {
+    if (sh.type == SHAPE_CIRCLE) {
+        const Vec2 position = xf.p + mul(xf.q, sh.p);
+        const Vec2 s = ip1 - position;
+        const float b = dot(s, s) - sh.radius * sh.radius;
+        const Vec2 r = ip2 - ip1;
+        const float c = dot(s, r);
+        const float rr = dot(r, r);
+        const float sigma = c * c - rr * b;
+        if (sigma < 0.0f || rr < kEpsilon) return false;
+        float a = -(c + std::sqrt(sigma));
+        if (0.0f <= a && a <= max_fraction * rr) {
+            a /= rr;
+            *fraction = a;
+            Vec2 n = s + a * r;
+            normalize(n);
+            *normal = n;
+            return true;
+        }
+        return false;
+    }
+    const Vec2 p1 = mul_t(xf.q, ip1 - xf.p);
+    const Vec2 p2 = mul_t(xf.q, ip2 - xf.p);
+    const Vec2 d = p2 - p1;
+    if (sh.type == SHAPE_POLYGON) {
+        float lower = 0.032f, upper = max_fraction;
+        int index = -1;
+        for (int i = 0; i < sh.count; ++i) {
+            const float numerator = dot(sh.normals[i], sh.verts[i] - p1);
+            const float denominator = dot(sh.normals[i], d);
+            if (denominator == 0.0f) {
+                if (numerator < 0.0f) return false;
+            } else {
+                if (denominator < 0.0f && numerator < lower * denominator) {
+                    lower = numerator / denominator;
+                    index = i;
+                } else if (denominator > 0.0f && numerator < upper * denominator) {
+                    upper = numerator / denominator;
+                }
+            }
+            if (upper < lower) return false;
+        }
+        if (index >= 0) {
+            *fraction = lower;
+            *normal = mul(xf.q, sh.normals[index]);
+            return true;
+        }
+        return false;
+    }
+    /* edge */
+    const Vec2 v1 = sh.v1, v2 = sh.v2;
+    const Vec2 e = v2 - v1;
+    Vec2 nrm{e.y, -e.x};
+    normalize(nrm);
+    const float numerator = dot(nrm, v1 - p1);
+    if (sh.one_sided && numerator > 0.0f) return false;
+    const float denominator = dot(nrm, d);
+    if (denominator == 0.0f) return false;
+    const float t = numerator / denominator;
+    if (t < 0.0f || max_fraction < t) return false;
+    const Vec2 q = p1 + t * d;
+    const Vec2 r = v2 - v1;
+    const float rr = dot(r, r);
+    if (rr == 0.0f) return false;
+    const float sf = dot(q - v1, r) / rr;
+    if (sf < 0.0f || 1.0f < sf) return false;
+    *fraction = t;
+    *normal = numerator > 0.0f ? -mul(xf.q, nrm) : mul(xf.q, nrm);
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+/* fixtures whose fat AABB overlaps the box, sorted; returns their number (writes at most cap) */
+int ora_query_aabb(void* p, float lx, float ly, float ux, float uy, int* out, int cap) {
+    World& w = *(World*)p;
+    std::vector<int> hits;
+    AABB box{Vec2{lx, ly}, Vec2{ux, uy}};
+    w.bp.tree.query(box, [&](int proxy) {
+        hits.push_back(w.bp.tree.user(proxy));
+        return true;
+    });
+    std::sort(hits.begin(), hits.end());
+    for (int i = 0; i < (int)hits.size() && i < cap; ++i) out[i] = hits[i];
+    return (int)hits.size();
+}
+
+/* the closest hit along p1 -> p2, with the callback that clips the ray to each reported fraction:
+ * out = fixture (as float bits; -1 if none), point x, y, normal x, y, fraction */
+int ora_ray_cast_closest(void* p, float p1x, float p1y, float p2x, float p2y, float* out) {
+    World& w = *(World*)p;
+    const Vec2 p1{p1x, p1y}, p2{p2x, p2y};
+    int hit_fixture = -1;
+    Vec2 hit_point{0, 0}, hit_normal{0, 0};
+    float hit_fraction = 1.0f;
+    w.bp.tree.ray_cast(p1, p2, 1.0f, [&](float max_fraction, int proxy) -> float {
+        const int fi = w.bp.tree.user(proxy);
+        const Fixture& f = w.fixtures[fi];
+        float fraction;
+        Vec2 normal;
+        if (!shape_ray_cast(f.shape, w.bodies[f.body].xf, p1, p2, max_fraction, &fraction, &normal))
+            return max_fraction;
+        hit_fixture = fi;
+        hit_point = (1.0f - fraction) * p1 + fraction * p2;
+        hit_normal = normal;
+        hit_fraction = fraction;
+        return fraction;
+    });
+    out[0] = (float)hit_fixture;
+    out[1] = hit_point.x;
+    out[2] = hit_point.y;
+    out[3] = hit_normal.x;
+    out[4] = hit_normal.y;
+    out[5] = hit_fraction;
+    return hit_fixture >= 0 ? 1 : 0;
+}
+
+}  // extern "C"

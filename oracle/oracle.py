@@ -58,6 +58,8 @@ def load():
         "ora_get_counts": [vp, ctypes.POINTER(b2g.Counts)],
         "ora_get_profile": [vp, ctypes.POINTER(b2g.Profile)],
         "ora_get_contacts": [vp, vp, i32, pi32],
+        "ora_query_aabb": [vp, f32, f32, f32, f32, vp, i32],
+        "ora_ray_cast_closest": [vp, f32, f32, f32, f32, vp],
         "ora_get_pairs": [vp, vp, i32, pi32],
         "ora_get_proxies": [vp, vp, vp, vp, i32],
         "ora_set_solver_order": [vp, vp, i32],
@@ -224,6 +226,30 @@ class OracleWorld:
         ids = np.full(n, -1, np.int32)
         self._lib.ora_get_proxies(self._h, _ptr(aabbs), _ptr(moved), _ptr(ids), n)
         return aabbs, moved, ids
+
+    def query_aabb(self, boxes):
+        """(m, 2) array of (box index, fixture): the reference's tree query per box (fat AABBs)."""
+        boxes = np.asarray(boxes, np.float32).reshape(-1, 4)
+        out = []
+        for i, b in enumerate(boxes):
+            buf = np.zeros(max(self.fixture_count, 1), np.int32)
+            n = self._lib.ora_query_aabb(self._h, float(b[0]), float(b[1]), float(b[2]), float(b[3]), _ptr(buf),
+                                         len(buf))
+            out.extend((i, int(f)) for f in buf[:n])
+        return np.array(out, np.uint32).reshape(-1, 2)
+
+    def ray_cast_closest(self, rays):
+        """The reference's world ray cast with a clipping (closest-hit) callback, per ray."""
+        rays = np.asarray(rays, np.float32).reshape(-1, 4)
+        out = np.zeros(len(rays), b2g.RAY_HIT)
+        buf = np.zeros(6, np.float32)
+        for i, r in enumerate(rays):
+            self._lib.ora_ray_cast_closest(self._h, float(r[0]), float(r[1]), float(r[2]), float(r[3]), _ptr(buf))
+            out[i]["fixture"] = int(buf[0])
+            out[i]["point"] = buf[1:3]
+            out[i]["normal"] = buf[3:5]
+            out[i]["fraction"] = buf[5]
+        return out
 
     def set_solver_order(self, pairs):
         """Ordering hook: each island solves its contacts in this (fixture_a, fixture_b) order."""
