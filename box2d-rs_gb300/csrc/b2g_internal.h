@@ -72,7 +72,7 @@ enum {
     CNT_ROUNDS = 10,
     CNT_TOUCHING = 11,
     CNT_BOUNDS = 12,      /* 4 ints: ordered-int min.x, min.y, max.x, max.y of proxy centres */
-    CNT_BARRIER = 16,     /* 2 uints: grid barrier count / generation */
+    CNT_BARRIER = 16,     /* grid barrier arrivals of the running cooperative launch (zeroed per launch) */
     CNT_ISLANDS = 18,
     CNT_COLOURINGS = 19,  /* colourings done so far: the stamp of colours kept in contacts (mids.w) */
     CNT_SIZE = 32

@@ -1,14 +1,16 @@
 /*
  * b2g_sync.cuh — grid-wide barrier for the cooperative (persistent) kernels.
  *
- * Sense-by-generation barrier over the co-resident blocks of a cooperative launch. Thread 0
- * of each block arrives with an acquire-release add on a counter; the last arrival resets the
- * counter and publishes the next generation with a release store; the others spin on an
- * acquire load and check a clock64 limit (~1 s at 2 GHz) every 256 polls. __syncthreads
- * around it orders the rest of the block. On timeout the block sets ST_BARRIER_TIMEOUT in the
- * status word; once set, every later barrier returns false at once, so all blocks leave the
- * kernel within one limit and the host reports B2G_ERR_TIMEOUT. Thread 0 decides for its block
- * and broadcasts through shared memory, so all threads of a block see the same result.
+ * Counting barrier over the co-resident blocks of a cooperative launch. The launcher zeroes the
+ * counter before every launch (a memset node in the step graph), so the k-th barrier of the
+ * launch completes when the counter reaches (k + 1) x gridDim.x. Thread 0 of each block keeps k in
+ * shared memory, arrives with one fire-and-forget release add and polls the counter with acquire
+ * loads; nobody resets anything, so the last block to arrive waits for no extra round trip. Each
+ * wait is bounded: a clock64 limit (~1 s at 2 GHz) checked every 256 polls. On timeout the block
+ * sets ST_BARRIER_TIMEOUT in the status word; once set, every later barrier returns false at once,
+ * so all blocks leave the kernel within one limit and the host reports B2G_ERR_TIMEOUT. Thread 0
+ * decides for its block and broadcasts through shared memory, so all threads of a block see the
+ * same result. Every cooperative kernel calls grid_barrier_start() first.
  */
 #ifndef B2G_SYNC_CUH
 #define B2G_SYNC_CUH
@@ -31,7 +33,18 @@ __device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-/* cnt: the world's counter block (uses CNT_BARRIER, CNT_BARRIER + 1 and CNT_STATUS) */
+__device__ __forceinline__ void red_release_add_gpu(unsigned* p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+/* barriers this block has passed in the current launch (used by thread 0) */
+static __shared__ unsigned b2g_barrier_epoch;
+
+__device__ __forceinline__ void grid_barrier_start() {
+    if (threadIdx.x == 0) b2g_barrier_epoch = 0u;  /* ordered by the barrier's first __syncthreads */
+}
+
+/* cnt: the counter block (uses CNT_BARRIER, zeroed by the launcher, and CNT_STATUS) */
 __device__ __forceinline__ bool grid_barrier(int* cnt) {
     __shared__ int s_ok;
     __syncthreads();
@@ -39,17 +52,15 @@ __device__ __forceinline__ bool grid_barrier(int* cnt) {
         int ok = (((volatile int*)cnt)[CNT_STATUS] & ST_BARRIER_TIMEOUT) == 0;
         if (ok) {
             unsigned* count = (unsigned*)&cnt[CNT_BARRIER];
-            unsigned* gen_ptr = (unsigned*)&cnt[CNT_BARRIER + 1];
-            const unsigned gen = ld_acquire_gpu(gen_ptr);
-            const unsigned arrived = atom_add_acq_rel_gpu(count, 1u);
-            if (arrived == gridDim.x - 1) {
-                atomicExch(count, 0u);
-                st_release_gpu(gen_ptr, gen + 1u);
-            } else {
-                const long long t0 = clock64();
-                unsigned polls = 0;
-                while (ld_acquire_gpu(gen_ptr) == gen) {
-                    if ((++polls & 255u) == 0u && clock64() - t0 > 2000000000LL) {
+            const unsigned target = (b2g_barrier_epoch + 1u) * gridDim.x;
+            ++b2g_barrier_epoch;
+            red_release_add_gpu(count, 1u);
+            const long long t0 = clock64();
+            unsigned polls = 0;
+            while ((int)(ld_acquire_gpu(count) - target) < 0) {
+                if ((++polls & 255u) == 0u) {
+                    if (((volatile int*)cnt)[CNT_STATUS] & ST_BARRIER_TIMEOUT) break;
+                    if (clock64() - t0 > 2000000000LL) {
                         atomicOr((unsigned*)&cnt[CNT_STATUS], ST_BARRIER_TIMEOUT);
                         break;
                     }

@@ -274,6 +274,7 @@ __device__ __forceinline__ float4* wp_rec(const AdjWork& a, int s, int it, int k
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_adj_replay(AdjWork a) {
+    grid_barrier_start();
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsize = gridDim.x * blockDim.x;
     const int nb = a.nb;
@@ -428,6 +429,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_replay(AdjWork a) {
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_adj_reverse(AdjWork a) {
+    grid_barrier_start();
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsize = gridDim.x * blockDim.x;
     const int nb = a.nb;
@@ -640,6 +642,7 @@ int launch_adjoint_segment(const AdjWork& a, cudaStream_t s, int num_sms) {
     void* args[] = {&ac};
     const bool single = a.max_slots <= 4096 && a.nb <= 16384;
     cudaError_t e;
+    int* bar = a.cnt + CNT_BARRIER;
     if (single) {
         e = cudaLaunchCooperativeKernel((const void*)k_adj_replay<512>, dim3(1), dim3(512), args, 0, s);
         if (e == cudaSuccess)
@@ -648,7 +651,10 @@ int launch_adjoint_segment(const AdjWork& a, cudaStream_t s, int num_sms) {
         static int br = 0, bv = 0;
         if (!br) br = coop_blocks_for((const void*)k_adj_replay<kBlock>, kBlock, num_sms);
         if (!bv) bv = coop_blocks_for((const void*)k_adj_reverse<kBlock>, kBlock, num_sms);
-        e = cudaLaunchCooperativeKernel((const void*)k_adj_replay<kBlock>, dim3(br), dim3(kBlock), args, 0, s);
+        e = cudaMemsetAsync(bar, 0, sizeof(int), s);
+        if (e == cudaSuccess)
+            e = cudaLaunchCooperativeKernel((const void*)k_adj_replay<kBlock>, dim3(br), dim3(kBlock), args, 0, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(bar, 0, sizeof(int), s);
         if (e == cudaSuccess)
             e = cudaLaunchCooperativeKernel((const void*)k_adj_reverse<kBlock>, dim3(bv), dim3(kBlock), args, 0, s);
     }

@@ -254,6 +254,7 @@ __device__ void tile_histogram(const unsigned long long* __restrict__ keys, int 
 __global__ void __launch_bounds__(kSortBlock) k_radix_coop(unsigned long long* ka, uint32_t* va, unsigned long long* kb,
                                                            uint32_t* vb, const int* d_n, int max_n, int bits,
                                                            uint32_t* hist, int* cnt) {
+    grid_barrier_start();
     __shared__ uint32_t s_base[256];
     __shared__ uint32_t s_run[256];
     __shared__ uint32_t s_warp[8][256];
@@ -373,6 +374,7 @@ void radix_sort_pairs_coop(unsigned long long* key_a, uint32_t* val_a, unsigned 
     /* one block per SM keeps the grid barrier short; per_sm only guards co-residency */
     const int blocks = num_sms;
     void* args[] = {&key_a, &val_a, &key_b, &val_b, (void*)&d_n, &max_n, &bits, &hist, &cnt};
+    cudaMemsetAsync(cnt + CNT_BARRIER, 0, sizeof(int), s);
     cudaLaunchCooperativeKernel((const void*)k_radix_coop, dim3(blocks), dim3(kSortBlock), args, 0, s);
     B2G_LAUNCHED(1);
 }

@@ -155,6 +155,7 @@ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
  * of its dynamic bodies takes the lowest colour free at both), so a step whose contacts persist
  * needs one or two rounds instead of one per colour. */
 __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w) {
+    grid_barrier_start();
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsize = gridDim.x * blockDim.x;
     const int n = w.cnt[CNT_CONS];
@@ -666,6 +667,7 @@ __device__ __forceinline__ void sync_fixture(const DevWorld& w, int f, const Xf&
 }
 
 __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
+    grid_barrier_start();
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsize = gridDim.x * blockDim.x;
     const int nb = w.n_bodies;
@@ -906,6 +908,7 @@ void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms) {
     const int blocks = coop_blocks((const void*)k_colour, num_sms) * w.cfg_coop_per_sm;
     DevWorld wc = w;
     void* args[] = {&wc};
+    cudaMemsetAsync(w.cnt + CNT_BARRIER, 0, sizeof(int), s);
     cudaLaunchCooperativeKernel((const void*)k_colour, dim3(blocks), dim3(kBlock), args, 0, s);
     B2G_LAUNCHED(1);
 }
@@ -916,6 +919,7 @@ int launch_solver(const DevWorld& w, const StepParams& sp, cudaStream_t s, int n
     StepParams spc = sp;
     void* args[] = {&wc, &spc};
     B2G_LAUNCHED(1);
+    cudaMemsetAsync(w.cnt + CNT_BARRIER, 0, sizeof(int), s);
     return (int)cudaLaunchCooperativeKernel((const void*)k_solve, dim3(blocks), dim3(kBlock), args, 0, s);
 }
 
