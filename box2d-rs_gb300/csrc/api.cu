@@ -662,11 +662,18 @@ int prepare(World* w) {
     return upload(w);
 }
 
+int status_error(World* w, int status);
+
 int check_status(World* w) {
     if (!w->allocated) return B2G_OK;
     int status = 0;
     CUDA_OK(w, cudaStreamSynchronize(w->stream));
     CUDA_OK(w, cudaMemcpy(&status, w->d.cnt + CNT_STATUS, sizeof(int), cudaMemcpyDeviceToHost));
+    return status_error(w, status);
+}
+
+/* the error for a device status word read after the stream drained (0: none); clears it */
+int status_error(World* w, int status) {
     if (status == 0) return B2G_OK;
     const int zero = 0;
     cudaMemcpy(w->d.cnt + CNT_STATUS, &zero, sizeof(int), cudaMemcpyHostToDevice);
@@ -851,8 +858,10 @@ int step(World* w, float dt, int vi, int pi) {
 
 World* W(void* p) { return (World*)p; }
 
-/* b2g_body_state of bodies [first, first + count) */
-__global__ void k_pack_states(DevWorld d, uint32_t first, uint32_t count, b2g_body_state* out) {
+/* b2g_body_state of bodies [first, first + count); thread 0 also copies the status word to
+ * *status (host memory the device writes coherently) so the caller needs no second copy */
+__global__ void k_pack_states(DevWorld d, uint32_t first, uint32_t count, b2g_body_state* out, int* status) {
+    if (status && blockIdx.x == 0 && threadIdx.x == 0) *status = ((volatile int*)d.cnt)[CNT_STATUS];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const float4 xf = d.b_xf[first + i], pos = d.b_pos[first + i], vel = d.b_vel[first + i];
         b2g_body_state s;
@@ -1115,9 +1124,12 @@ int b2g_get_body_states(void* p, uint32_t first, uint32_t count, b2g_body_state*
          * buffer that is copied out in one piece */
         const int grid = grid_for((int)count, 256, w->num_sms * 8);
         if (w->pageable) {
-            k_pack_states<<<grid, 256, 0, w->stream>>>(w->d, first, count, out);
+            int status = 0;
+            k_pack_states<<<grid, 256, 0, w->stream>>>(w->d, first, count, out, &status);
             B2G_LAUNCHED(1);
             CUDA_OK(w, cudaGetLastError());
+            CUDA_OK(w, cudaStreamSynchronize(w->stream));
+            return status_error(w, ((volatile int*)&status)[0]);
         } else {
             if (w->d_states_cap < (int)count) {
                 if (w->d_states) cudaFree(w->d_states);
@@ -1126,7 +1138,7 @@ int b2g_get_body_states(void* p, uint32_t first, uint32_t count, b2g_body_state*
                 CUDA_OK(w, cudaMalloc((void**)&w->d_states, count * sizeof(b2g_body_state)));
                 w->d_states_cap = (int)count;
             }
-            k_pack_states<<<grid, 256, 0, w->stream>>>(w->d, first, count, w->d_states);
+            k_pack_states<<<grid, 256, 0, w->stream>>>(w->d, first, count, w->d_states, nullptr);
             B2G_LAUNCHED(1);
             CUDA_OK(w, cudaMemcpyAsync(out, w->d_states, count * sizeof(b2g_body_state), cudaMemcpyDeviceToHost,
                                        w->stream));
