@@ -471,10 +471,19 @@ def main():
 
     peak, peak_kind = load_peaks()
     bm = bytes_model(counts, stats, vi, pi)
-    ms_phase = {"collide": phase_ms["collide"], "solver": phase_ms["solve_velocity"] + phase_ms["solve_init"],
-                "broadphase": phase_ms["broadphase"]}
+    # dominant kernel: the persistent solver k_solve (its own CUDA-event time, "solver" phase);
+    # achieved = its algorithmic bytes per launch / its mean launch time
+    ms_phase = {"collide": fine_ms["collide"], "solver": fine_ms["solver"],
+                "broadphase": fine_ms["broadphase_tree"] + fine_ms["contact_merge"]}
     dominant = max(ms_phase, key=ms_phase.get)
     achieved = bm[dominant] / (ms_phase[dominant] / args.steps / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    if dominant == "solver" and os.path.exists(tf):
+        with open(tf) as f:
+            rec = json.load(f)
+        if rec.get("kernel") == "k_solve" and rec.get("workload") == WORKLOAD:
+            traffic = rec["dram_bytes_per_launch"]
     line = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -483,8 +492,12 @@ def main():
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel_phase": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None},
+        "roofline": {"bound": "hbm", "kernel": "k_solve" if dominant == "solver" else dominant,
+                     "kernel_phase": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": bm[dominant],
+                     "traffic_note": "DRAM bytes per launch from one ncu capture at step 603 "
+                                     "(profiles/k_solve_mixed100k_step603.md)" if traffic else None},
         "phase_ms_per_step": {k: v / args.steps for k, v in fine_ms.items()},
         "counts_last_step": counts,
         "clocks": clocks,
