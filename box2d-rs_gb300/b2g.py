@@ -370,6 +370,11 @@ def load_library(path=LIB_PATH):
         "b2g_set_angular_velocity": [vp, u32, f32],
         "b2g_apply_force": [vp, u32, Vec2, Vec2, i32],
         "b2g_apply_linear_impulse": [vp, u32, Vec2, Vec2, i32],
+        "b2g_apply_force_to_center": [vp, u32, Vec2, i32],
+        "b2g_apply_torque": [vp, u32, f32, i32],
+        "b2g_apply_linear_impulse_to_center": [vp, u32, Vec2, i32],
+        "b2g_apply_angular_impulse": [vp, u32, f32, i32],
+        "b2g_set_awake": [vp, u32, i32],
         "b2g_set_gravity": [vp, Vec2],
         "b2g_set_allow_sleeping": [vp, i32],
         "b2g_set_warm_starting": [vp, i32],
@@ -537,6 +542,21 @@ class B2world:
 
     def apply_linear_impulse(self, body, impulse, point, wake=True):
         self._check(self._lib.b2g_apply_linear_impulse(self._h, body, Vec2(*impulse), Vec2(*point), int(wake)))
+
+    def apply_force_to_center(self, body, force, wake=True):
+        self._check(self._lib.b2g_apply_force_to_center(self._h, body, Vec2(*force), int(wake)))
+
+    def apply_torque(self, body, torque, wake=True):
+        self._check(self._lib.b2g_apply_torque(self._h, body, float(torque), int(wake)))
+
+    def apply_linear_impulse_to_center(self, body, impulse, wake=True):
+        self._check(self._lib.b2g_apply_linear_impulse_to_center(self._h, body, Vec2(*impulse), int(wake)))
+
+    def apply_angular_impulse(self, body, impulse, wake=True):
+        self._check(self._lib.b2g_apply_angular_impulse(self._h, body, float(impulse), int(wake)))
+
+    def set_awake(self, body, flag):
+        self._check(self._lib.b2g_set_awake(self._h, body, int(flag)))
 
     # -- flags --
     def set_gravity(self, g):

@@ -875,41 +875,66 @@ __global__ void k_pack_states(DevWorld d, uint32_t first, uint32_t count, b2g_bo
 }
 
 /* small body edits after the device became authoritative */
+/* One edit of one body (src/b2_body.rs): 0 set_linear_velocity (:684-694), 1 set_angular_velocity
+ * (:696-705), 2 apply_force, 3 apply_linear_impulse, 4 apply_force_to_center, 5 apply_torque,
+ * 6 apply_linear_impulse_to_center, 7 apply_angular_impulse (:870-980), 8 set_awake (:783-801).
+ * v.w holds the sleep time; f.z the torque. Shared by the device kernel and the host mirrors. */
+B2G_HD void edit_body(int op, uint32_t& fl, float4& v, float4& f, const float4& p, const float4& m, float x, float y,
+                      float z, float px, float py, int wake) {
+    const int type = (int)(fl & BF_TYPE_MASK);
+    if (op == 0 || op == 1) {
+        if (type == BODY_STATIC) return;
+        const bool nonzero = op == 0 ? x * x + y * y > 0.0f : z * z > 0.0f;
+        if (nonzero && !(fl & BF_AWAKE)) {
+            fl |= BF_AWAKE;
+            v.w = 0.0f;
+        }
+        if (op == 0) {
+            v.x = x;
+            v.y = y;
+        } else {
+            v.z = z;
+        }
+        return;
+    }
+    if (op == 8) {
+        if (type == BODY_STATIC) return;
+        if (wake) {
+            fl |= BF_AWAKE;
+            v.w = 0.0f;
+        } else {
+            fl &= ~BF_AWAKE;
+            v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            f = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        return;
+    }
+    if (type != BODY_DYNAMIC) return;
+    if (wake && !(fl & BF_AWAKE)) {
+        fl |= BF_AWAKE;
+        v.w = 0.0f;
+    }
+    if (!(fl & BF_AWAKE)) return;  /* a sleeping body accumulates nothing */
+    const float cr = (px - p.x) * y - (py - p.y) * x;  /* b2_cross(point - c, vector) */
+    switch (op) {
+        case 2: f.x += x; f.y += y; f.z += cr; break;
+        case 3: v.x += m.y * x; v.y += m.y * y; v.z += m.w * cr; break;
+        case 4: f.x += x; f.y += y; break;
+        case 5: f.z += z; break;
+        case 6: v.x += m.y * x; v.y += m.y * y; break;
+        case 7: v.z += m.w * z; break;
+        default: break;
+    }
+}
+
 __global__ void k_body_op(DevWorld d, int op, int b, float x, float y, float z, float px, float py, int wake) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     uint32_t fl = d.b_flags[b];
-    const int type = (int)(fl & BF_TYPE_MASK);
-    float4 v = d.b_vel[b];
-    if (op == 0) { /* set_linear_velocity, src/b2_body.rs:684-694 */
-        if (type == BODY_STATIC) return;
-        if (x * x + y * y > 0.0f && !(fl & BF_AWAKE)) { fl |= BF_AWAKE; v.w = 0.0f; }
-        v.x = x;
-        v.y = y;
-    } else if (op == 1) { /* set_angular_velocity, :696-705 */
-        if (type == BODY_STATIC) return;
-        if (z * z > 0.0f && !(fl & BF_AWAKE)) { fl |= BF_AWAKE; v.w = 0.0f; }
-        v.z = z;
-    } else if (op == 2 || op == 3) { /* apply_force / apply_linear_impulse, src/b2_body.rs:870-940 */
-        if (type != BODY_DYNAMIC) return;
-        if (wake && !(fl & BF_AWAKE)) { fl |= BF_AWAKE; v.w = 0.0f; }
-        if (!(fl & BF_AWAKE)) { d.b_flags[b] = fl; d.b_vel[b] = v; return; }
-        const float4 p = d.b_pos[b];
-        const float cr = (px - p.x) * y - (py - p.y) * x;
-        if (op == 2) {
-            float4 f = d.b_force[b];
-            f.x += x;
-            f.y += y;
-            f.z += cr;
-            d.b_force[b] = f;
-        } else {
-            const float4 m = d.b_mass[b];
-            v.x += m.y * x;
-            v.y += m.y * y;
-            v.z += m.w * cr;
-        }
-    }
+    float4 v = d.b_vel[b], f = d.b_force[b];
+    edit_body(op, fl, v, f, d.b_pos[b], d.b_mass[b], x, y, z, px, py, wake);
     d.b_flags[b] = fl;
     d.b_vel[b] = v;
+    d.b_force[b] = f;
 }
 
 int body_op(World* w, int op, uint32_t b, float x, float y, float z, float px, float py, int wake) {
@@ -922,34 +947,7 @@ int body_op(World* w, int op, uint32_t b, float x, float y, float z, float px, f
         CUDA_OK(w, cudaGetLastError());
         return B2G_OK;
     }
-    uint32_t& fl = w->h_flags[b];
-    const int type = (int)(fl & BF_TYPE_MASK);
-    float4& v = w->h_vel[b];
-    if (op == 0) {
-        if (type == BODY_STATIC) return B2G_OK;
-        if (x * x + y * y > 0.0f && !(fl & BF_AWAKE)) { fl |= BF_AWAKE; v.w = 0.0f; }
-        v.x = x;
-        v.y = y;
-    } else if (op == 1) {
-        if (type == BODY_STATIC) return B2G_OK;
-        if (z * z > 0.0f && !(fl & BF_AWAKE)) { fl |= BF_AWAKE; v.w = 0.0f; }
-        v.z = z;
-    } else {
-        if (type != BODY_DYNAMIC) return B2G_OK;
-        if (wake && !(fl & BF_AWAKE)) { fl |= BF_AWAKE; v.w = 0.0f; }
-        if (!(fl & BF_AWAKE)) return B2G_OK;
-        const float4 p = w->h_pos[b];
-        const float cr = (px - p.x) * y - (py - p.y) * x;
-        if (op == 2) {
-            w->h_force[b].x += x;
-            w->h_force[b].y += y;
-            w->h_force[b].z += cr;
-        } else {
-            v.x += w->h_mass[b].y * x;
-            v.y += w->h_mass[b].y * y;
-            v.z += w->h_mass[b].w * cr;
-        }
-    }
+    edit_body(op, w->h_flags[b], w->h_vel[b], w->h_force[b], w->h_pos[b], w->h_mass[b], x, y, z, px, py, wake);
     return B2G_OK;
 }
 
@@ -1241,6 +1239,21 @@ int b2g_apply_force(void* p, uint32_t b, b2g_vec2 force, b2g_vec2 point, int32_t
 }
 int b2g_apply_linear_impulse(void* p, uint32_t b, b2g_vec2 impulse, b2g_vec2 point, int32_t wake) {
     return p ? body_op(W(p), 3, b, impulse.x, impulse.y, 0.0f, point.x, point.y, wake) : B2G_ERR_INVALID_ARG;
+}
+int b2g_apply_force_to_center(void* p, uint32_t b, b2g_vec2 force, int32_t wake) {
+    return p ? body_op(W(p), 4, b, force.x, force.y, 0.0f, 0.0f, 0.0f, wake) : B2G_ERR_INVALID_ARG;
+}
+int b2g_apply_torque(void* p, uint32_t b, float torque, int32_t wake) {
+    return p ? body_op(W(p), 5, b, 0.0f, 0.0f, torque, 0.0f, 0.0f, wake) : B2G_ERR_INVALID_ARG;
+}
+int b2g_apply_linear_impulse_to_center(void* p, uint32_t b, b2g_vec2 impulse, int32_t wake) {
+    return p ? body_op(W(p), 6, b, impulse.x, impulse.y, 0.0f, 0.0f, 0.0f, wake) : B2G_ERR_INVALID_ARG;
+}
+int b2g_apply_angular_impulse(void* p, uint32_t b, float impulse, int32_t wake) {
+    return p ? body_op(W(p), 7, b, 0.0f, 0.0f, impulse, 0.0f, 0.0f, wake) : B2G_ERR_INVALID_ARG;
+}
+int b2g_set_awake(void* p, uint32_t b, int32_t flag) {
+    return p ? body_op(W(p), 8, b, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, flag) : B2G_ERR_INVALID_ARG;
 }
 
 int b2g_set_gravity(void* p, b2g_vec2 g) {

@@ -179,6 +179,13 @@ int b2g_set_angular_velocity(void* world, uint32_t body, float w);
 /* B2body::apply_force / apply_linear_impulse (src/b2_body.rs:870-940) */
 int b2g_apply_force(void* world, uint32_t body, b2g_vec2 force, b2g_vec2 point, int32_t wake);
 int b2g_apply_linear_impulse(void* world, uint32_t body, b2g_vec2 impulse, b2g_vec2 point, int32_t wake);
+/* B2body::apply_force_to_center, apply_torque, apply_linear_impulse_to_center, apply_angular_impulse
+ * (src/b2_body.rs:890-980) and set_awake (:783-801) */
+int b2g_apply_force_to_center(void* world, uint32_t body, b2g_vec2 force, int32_t wake);
+int b2g_apply_torque(void* world, uint32_t body, float torque, int32_t wake);
+int b2g_apply_linear_impulse_to_center(void* world, uint32_t body, b2g_vec2 impulse, int32_t wake);
+int b2g_apply_angular_impulse(void* world, uint32_t body, float impulse, int32_t wake);
+int b2g_set_awake(void* world, uint32_t body, int32_t flag);
 
 /* ---- world flags, src/b2_world.rs:163-193, :232-253 ---- */
 int b2g_set_gravity(void* world, b2g_vec2 gravity);

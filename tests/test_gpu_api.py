@@ -108,6 +108,40 @@ def test_forces_and_impulses(built):
     assert abs(w.get_body_states()[0]["position"][1] - 1.0) < 1e-5
 
 
+def test_center_force_torque_and_angular_impulse(built):
+    """apply_force_to_center / apply_torque act over one step (v += h/m F, w += h/I T);
+    the impulse forms change the velocity at once; set_awake(False) zeroes the motion."""
+    h = np.float32(1 / 60)
+    for device_first in (False, True):
+        w = b2g.B2world(gravity=(0.0, 0.0))
+        w.set_allow_sleeping(False)
+        bd = b2g.body_defs(1)
+        bd["type"] = b2g.DYNAMIC
+        w.create_bodies(bd)
+        w.create_fixture(b2g.box_fixture(0, 0.5, 0.5, density=2.0))
+        if device_first:
+            w.step(h, 8, 3)  # the device copy becomes authoritative
+            w.set_linear_velocity(0, (0.0, 0.0))
+        md = w.get_mass_data()[0]
+        inv_m, inv_i = np.float32(md[1]), np.float32(md[3])
+        w.apply_force_to_center(0, (3.0, 0.0))
+        w.apply_torque(0, 2.0)
+        w.step(h, 8, 3)
+        st = w.get_body_states()[0]
+        assert st["linear_velocity"][0] == np.float32(np.float32(h * inv_m) * np.float32(3.0))
+        assert st["angular_velocity"] == np.float32(np.float32(h * inv_i) * np.float32(2.0))
+        v0, w0 = st["linear_velocity"].copy(), np.float32(st["angular_velocity"])
+        w.apply_linear_impulse_to_center(0, (0.0, 1.0))
+        w.apply_angular_impulse(0, 0.5)
+        st = w.get_body_states()[0]
+        assert st["linear_velocity"][1] == np.float32(v0[1] + inv_m * np.float32(1.0))
+        assert st["angular_velocity"] == np.float32(w0 + inv_i * np.float32(0.5))
+        w.set_awake(0, False)
+        st = w.get_body_states()[0]
+        assert np.all(st["linear_velocity"] == 0.0) and st["angular_velocity"] == 0.0
+        w.close()
+
+
 def test_sleeping_bodies_stop(built):
     """With sleep allowed, a resting pyramid falls asleep (velocities zeroed) like the reference."""
     s = scenes.pyramid(rows=4)
