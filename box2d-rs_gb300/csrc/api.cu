@@ -535,7 +535,7 @@ int allocate(World* w, int nb, int nf) {
     A(d.bp_key, fix_cap); A(d.bp_val, fix_cap); A(d.bp_key_alt, fix_cap); A(d.bp_val_alt, fix_cap);
     A(d.bp_leaf, fix_cap); A(d.bp_node_b0, fix_cap); A(d.bp_node_b1, fix_cap); A(d.bp_node_child, fix_cap);
     A(d.bp_parent, 2 * (size_t)fix_cap); A(d.bp_flag, fix_cap);
-    A(d.bp_world_root, w->num_worlds); A(d.bp_world_first, w->num_worlds);
+    A(d.bp_world_root, 2 * (size_t)w->num_worlds); A(d.bp_world_first, 2 * (size_t)w->num_worlds);
     A(d.events, d.event_cap);
     A(d.pairs, pair_cap);
     A(d.scan_tmp, 2 * (size_t)contact_cap + scan_tmp_size(contact_cap) + 64);
@@ -658,7 +658,7 @@ int prepare(World* w) {
         }
         w->d.key_bits = kb;
     }
-    w->d.morton_world_bits = w->num_worlds > 1 ? bits_for((uint64_t)(w->num_worlds - 1)) : 0;
+    w->d.morton_world_bits = bits_for((uint64_t)(2 * w->num_worlds - 1));  /* key worlds: 2 per world */
     return upload(w);
 }
 

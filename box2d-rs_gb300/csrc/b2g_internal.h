@@ -75,6 +75,7 @@ enum {
     CNT_BARRIER = 16,     /* grid barrier arrivals of the running cooperative launch (zeroed per launch) */
     CNT_ISLANDS = 18,
     CNT_COLOURINGS = 19,  /* colourings done so far: the stamp of colours kept in contacts (mids.w) */
+    CNT_DYN_EXTENT = 20,  /* largest half-extent of a dynamic body's fat AABB (float bits), this pass */
     CNT_SIZE = 32
 };
 
@@ -170,8 +171,10 @@ struct DevWorld {
     int2* bp_node_child;         /* child indices; leaves encoded as ~leaf */
     int* bp_parent;              /* parent of internal nodes [0,n-1) and leaves [n-1, 2n-1) */
     uint32_t* bp_flag;           /* refit arrival counters */
-    int* bp_world_root;          /* per world: root node (encoded like children), or INT_MIN if empty */
-    int* bp_world_first;         /* per world: first sorted leaf */
+    int* bp_world_root;          /* per key world (2 x num_worlds): root node (encoded like children), or
+                                    INT_MIN if empty; key world w + num_worlds holds world w's large
+                                    static proxies (see k_bp_keys) */
+    int* bp_world_first;         /* per key world: first sorted leaf */
     /* outputs for the host */
     int4* events;                /* kind, fixture a, fixture b, - */
     uint2* pairs;                /* recorded emitted pairs (fixture ids) */

@@ -8,13 +8,16 @@
  * The reference inserts moved proxies into an incremental AVL-balanced tree and queries
  * it once per moved proxy. Here the tree is rebuilt every pass as a linear BVH:
  *   1. centre bounds of all fat AABBs (atomic min/max on order-preserving ints),
- *   2. 64-bit keys world << 32 | Morton(16-bit x, 16-bit y), radix-sorted with the
- *      fixture index as payload (worlds occupy disjoint key ranges),
+ *   2. 64-bit keys world << 30 | Morton(15-bit x, 15-bit y), radix-sorted with the
+ *      fixture index as payload (worlds occupy disjoint key ranges; a static proxy far
+ *      larger than every dynamic one takes key world  world + num_worlds, so grounds and
+ *      walls form a small hierarchy of their own instead of inflating every ancestor box;
+ *      a single world then sorts 31 key bits, four 8-bit passes),
  *   3. Karras (2012) hierarchy over the sorted keys (ties broken by position) — every
  *      internal node stores both children's boxes, so a traversal step is one 48-byte
  *      fetch and two overlap tests,
  *   4. bottom-up refit with per-node arrival counters,
- *   5. one thread per moved proxy walks its world's subtree with a short stack and
+ *   5. one thread per moved proxy walks its world's two subtrees with a short stack and
  *      applies the reference's rule: skip itself; skip a moved partner whose proxy id is
  *      larger (that partner reports the pair); emit (min id, max id).
  * The emitted set equals the reference's: every pair of overlapping fat AABBs with at
@@ -34,6 +37,8 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr int kStack = 64;
+constexpr int kMortonBits = 30;      /* 15 bits of cell per axis */
+constexpr float kCellMax = 32767.0f;
 
 __device__ __forceinline__ int f2ord(float f) {
     int i = __float_as_int(f);
@@ -59,19 +64,22 @@ __global__ void k_bp_init(DevWorld w) {
         w.cnt[CNT_BOUNDS + 3] = INT_MIN;
         w.cnt[CNT_NEW] = 0;
         w.cnt[CNT_PAIRS] = 0;
+        w.cnt[CNT_DYN_EXTENT] = 0;
     }
-    for (int i = t; i < w.num_worlds; i += gridDim.x * blockDim.x) {
+    for (int i = t; i < 2 * w.num_worlds; i += gridDim.x * blockDim.x) {
         w.bp_world_first[i] = -1;
         w.bp_world_root[i] = INT_MIN;
     }
 }
 
 __global__ void k_bp_bounds(DevWorld w) {
-    int mnx = INT_MAX, mny = INT_MAX, mxx = INT_MIN, mxy = INT_MIN;
+    int mnx = INT_MAX, mny = INT_MAX, mxx = INT_MIN, mxy = INT_MIN, dyn = 0;
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < w.n_fixtures; f += gridDim.x * blockDim.x) {
         const float4 a = w.f_fat[f];
         const float cx = 0.5f * (a.x + a.z), cy = 0.5f * (a.y + a.w);
         if (!(cx - cx == 0.0f) || !(cy - cy == 0.0f)) continue;  /* disabled proxies hold infinite boxes */
+        if ((w.b_flags[w.f_body[f]] & BF_TYPE_MASK) == BODY_DYNAMIC)
+            dyn = max(dyn, __float_as_int(0.5f * fmaxf(a.z - a.x, a.w - a.y)));  /* >= 0: ordered as int */
         const int ix = f2ord(cx), iy = f2ord(cy);
         mnx = min(mnx, ix);
         mny = min(mny, iy);
@@ -84,7 +92,9 @@ __global__ void k_bp_bounds(DevWorld w) {
         mxx = max(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
         mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
     }
+    for (int o = 16; o > 0; o >>= 1) dyn = max(dyn, __shfl_xor_sync(0xffffffffu, dyn, o));
     if ((threadIdx.x & 31) == 0) {
+        atomicMax(&w.cnt[CNT_DYN_EXTENT], dyn);
         atomicMin(&w.cnt[CNT_BOUNDS + 0], mnx);
         atomicMin(&w.cnt[CNT_BOUNDS + 1], mny);
         atomicMax(&w.cnt[CNT_BOUNDS + 2], mxx);
@@ -99,18 +109,26 @@ __global__ void k_bp_keys(DevWorld w) {
         ly = ord2f(w.cnt[CNT_BOUNDS + 1]);
         const float ex = ord2f(w.cnt[CNT_BOUNDS + 2]) - lx;
         const float ey = ord2f(w.cnt[CNT_BOUNDS + 3]) - ly;
-        sx = ex > 0.0f ? 65535.0f / ex : 0.0f;
-        sy = ey > 0.0f ? 65535.0f / ey : 0.0f;
+        sx = ex > 0.0f ? kCellMax / ex : 0.0f;
+        sy = ey > 0.0f ? kCellMax / ey : 0.0f;
     }
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < w.n_fixtures; f += gridDim.x * blockDim.x) {
         const float4 a = w.f_fat[f];
         const float cx = 0.5f * (a.x + a.z), cy = 0.5f * (a.y + a.w);
         float qx = (cx - lx) * sx, qy = (cy - ly) * sy;
-        qx = (qx - qx == 0.0f) ? fminf(fmaxf(qx, 0.0f), 65535.0f) : 65535.0f;
-        qy = (qy - qy == 0.0f) ? fminf(fmaxf(qy, 0.0f), 65535.0f) : 65535.0f;
+        qx = (qx - qx == 0.0f) ? fminf(fmaxf(qx, 0.0f), kCellMax) : kCellMax;
+        qy = (qy - qy == 0.0f) ? fminf(fmaxf(qy, 0.0f), kCellMax) : kCellMax;
         const uint32_t m = spread16((uint32_t)qx) | (spread16((uint32_t)qy) << 1);
-        const uint32_t world = w.b_world[w.f_body[f]];
-        w.bp_key[f] = ((unsigned long long)world << 32) | m;
+        /* A static proxy much larger than every dynamic one (a ground or a wall) would give all
+         * its ancestors a huge box that every query must descend; it goes to its world's second
+         * key range (world + num_worlds), a separate small hierarchy that queries also walk. */
+        const int b = w.f_body[f];
+        uint32_t world = w.b_world[b];
+        const float big = 4.0f * __int_as_float(w.cnt[CNT_DYN_EXTENT]);
+        if ((w.b_flags[b] & BF_TYPE_MASK) == BODY_STATIC && big > 0.0f &&
+            0.5f * fmaxf(a.z - a.x, a.w - a.y) > big)
+            world += (uint32_t)w.num_worlds;
+        w.bp_key[f] = ((unsigned long long)world << kMortonBits) | m;
         w.bp_val[f] = (uint32_t)f;
     }
 }
@@ -151,10 +169,10 @@ __global__ void k_bp_build(DevWorld w) {
         if (right < 0) w.bp_parent[n - 1 + gamma + 1] = i; else w.bp_parent[gamma + 1] = i;
         w.bp_flag[i] = 0u;
         /* world root: the node whose leaf range is exactly one world's range */
-        const uint32_t wl = (uint32_t)(k[lo] >> 32), wh = (uint32_t)(k[hi] >> 32);
+        const uint32_t wl = (uint32_t)(k[lo] >> kMortonBits), wh = (uint32_t)(k[hi] >> kMortonBits);
         if (wl == wh) {
-            const bool first = lo == 0 || (uint32_t)(k[lo - 1] >> 32) != wl;
-            const bool last = hi == n - 1 || (uint32_t)(k[hi + 1] >> 32) != wl;
+            const bool first = lo == 0 || (uint32_t)(k[lo - 1] >> kMortonBits) != wl;
+            const bool last = hi == n - 1 || (uint32_t)(k[hi + 1] >> kMortonBits) != wl;
             if (first && last) w.bp_world_root[wl] = i;
         }
     }
@@ -164,9 +182,9 @@ __global__ void k_bp_leaves(DevWorld w) {
     const int n = w.n_fixtures;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         w.bp_leaf[p] = w.f_fat[w.bp_val[p]];
-        const uint32_t wd = (uint32_t)(w.bp_key[p] >> 32);
-        const bool first = p == 0 || (uint32_t)(w.bp_key[p - 1] >> 32) != wd;
-        const bool last = p == n - 1 || (uint32_t)(w.bp_key[p + 1] >> 32) != wd;
+        const uint32_t wd = (uint32_t)(w.bp_key[p] >> kMortonBits);
+        const bool first = p == 0 || (uint32_t)(w.bp_key[p - 1] >> kMortonBits) != wd;
+        const bool last = p == n - 1 || (uint32_t)(w.bp_key[p + 1] >> kMortonBits) != wd;
         if (first) w.bp_world_first[wd] = p;
         if (first && last) w.bp_world_root[wd] = ~p;  /* a world with a single proxy */
     }
@@ -296,36 +314,48 @@ __device__ void handle_pair(const DevWorld& w, const StepParams& sp, int f, int 
 __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams sp) {
     const int n = w.n_fixtures;
     const int n_contacts = w.cnt[CNT_CONTACTS];
+    const uint32_t nw = (uint32_t)w.num_worlds;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const int f = (int)w.bp_val[p];
         if (!w.f_moved[f]) continue;
         const float4 q = w.bp_leaf[p];
-        const uint32_t wd = (uint32_t)(w.bp_key[p] >> 32);
-        const int root = w.bp_world_root[wd];
-        if (root < 0) continue;  /* single-proxy world (or empty) */
+        uint32_t wd = (uint32_t)(w.bp_key[p] >> kMortonBits);
+        if (wd >= nw) wd -= nw;
         const uint32_t rq = w.f_refid[f];
-        int stack[kStack];
-        int sp_top = 0;
-        stack[sp_top++] = root;
-        while (sp_top > 0) {
-            const int node = stack[--sp_top];
-            const int2 ch = w.bp_node_child[node];
-            const float4 b0 = w.bp_node_b0[node];
-            const float4 b1 = w.bp_node_b1[node];
-            const int kids[2] = {ch.x, ch.y};
-            const bool hit[2] = {box_overlap(b0, q), box_overlap(b1, q)};
-            for (int c = 0; c < 2; ++c) {
-                if (!hit[c]) continue;
-                const int id = kids[c];
-                if (id < 0) {
-                    const int g = (int)w.bp_val[~id];
-                    if (g == f) continue;
-                    if (w.f_moved[g] && w.f_refid[g] > rq) continue;
-                    handle_pair(w, sp, f, g, rq, n_contacts);
-                } else if (sp_top < kStack) {
-                    stack[sp_top++] = id;
-                } else {
-                    atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_STACK_OVERFLOW);
+        auto leaf = [&](int l) {
+            const int g = (int)w.bp_val[l];
+            if (g == f) return;
+            if (w.f_moved[g] && w.f_refid[g] > rq) return;
+            handle_pair(w, sp, f, g, rq, n_contacts);
+        };
+        /* the world's hierarchy, then the one of its large static proxies */
+        for (int h = 0; h < 2; ++h) {
+            const int root = w.bp_world_root[wd + (h ? nw : 0u)];
+            if (root == INT_MIN) continue;
+            if (root < 0) {  /* a single proxy */
+                if (box_overlap(w.bp_leaf[~root], q)) leaf(~root);
+                continue;
+            }
+            int stack[kStack];
+            int sp_top = 0;
+            stack[sp_top++] = root;
+            while (sp_top > 0) {
+                const int node = stack[--sp_top];
+                const int2 ch = w.bp_node_child[node];
+                const float4 b0 = w.bp_node_b0[node];
+                const float4 b1 = w.bp_node_b1[node];
+                const int kids[2] = {ch.x, ch.y};
+                const bool hit[2] = {box_overlap(b0, q), box_overlap(b1, q)};
+                for (int c = 0; c < 2; ++c) {
+                    if (!hit[c]) continue;
+                    const int id = kids[c];
+                    if (id < 0) {
+                        leaf(~id);
+                    } else if (sp_top < kStack) {
+                        stack[sp_top++] = id;
+                    } else {
+                        atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_STACK_OVERFLOW);
+                    }
                 }
             }
         }
@@ -424,11 +454,11 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
                        const std::function<void()>& after_tree) {
     const int n = w.n_fixtures;
     const int gf = grid_for(n, kBlock, num_sms * 8);
-    k_bp_init<<<grid_for(w.num_worlds, kBlock, 64), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+    k_bp_init<<<grid_for(2 * w.num_worlds, kBlock, 64), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
     if (n > 0) {
         k_bp_bounds<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_keys<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
-        radix_sort_pairs_coop(w.bp_key, w.bp_val, w.bp_key_alt, w.bp_val_alt, nullptr, n, 32 + w.morton_world_bits,
+        radix_sort_pairs_coop(w.bp_key, w.bp_val, w.bp_key_alt, w.bp_val_alt, nullptr, n, kMortonBits + w.morton_world_bits,
                               w.sort_hist, w.cnt, s, num_sms);
         if (n > 1) {
             k_bp_build<<<grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);

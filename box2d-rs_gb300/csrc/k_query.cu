@@ -131,8 +131,7 @@ __global__ void __launch_bounds__(kBlock) k_ray_cast(DevWorld w, const float4* r
         V2 hit_point = mk(0.0f, 0.0f), hit_normal = mk(0.0f, 0.0f);
         float hit_fraction = 1.0f;
         const uint32_t wd = ray_world ? ray_world[i] : 0u;
-        const int root = wd < (uint32_t)w.num_worlds ? w.bp_world_root[wd] : INT_MIN;
-        if (root != INT_MIN) {
+        if (wd < (uint32_t)w.num_worlds) {
             V2 r = sub(p2, p1);
             normalize(r);
             const V2 v = mk(-1.0f * r.y, 1.0f * r.x);
@@ -157,9 +156,14 @@ __global__ void __launch_bounds__(kBlock) k_ray_cast(DevWorld w, const float4* r
                     seg = seg_box();
                 }
             };
-            if (root < 0) {  /* a world with one proxy */
-                if (ray_box(w.bp_leaf[~root], seg, p1, v, abs_v)) leaf(~root);
-            } else {
+            /* the world's hierarchy, then the one of its large static proxies */
+            for (int h = 0; h < 2; ++h) {
+                const int root = w.bp_world_root[wd + (h ? (uint32_t)w.num_worlds : 0u)];
+                if (root == INT_MIN) continue;
+                if (root < 0) {  /* a hierarchy of one proxy */
+                    if (ray_box(w.bp_leaf[~root], seg, p1, v, abs_v)) leaf(~root);
+                    continue;
+                }
                 int stack[kStack];
                 int top = 0;
                 stack[top++] = root;
@@ -188,29 +192,32 @@ __global__ void __launch_bounds__(kBlock) k_query_aabb(DevWorld w, const float4*
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 q = boxes[i];
         const uint32_t wd = box_world ? box_world[i] : 0u;
-        const int root = wd < (uint32_t)w.num_worlds ? w.bp_world_root[wd] : INT_MIN;
-        if (root == INT_MIN) continue;
+        if (wd >= (uint32_t)w.num_worlds) continue;
         auto emit = [&](int p) {
             const int slot = atomicAdd(count, 1);
             if (slot < cap) out[slot] = make_uint2((uint32_t)i, w.bp_val[p]);
         };
-        if (root < 0) {
-            if (aabb_overlap(w.bp_leaf[~root], q)) emit(~root);
-            continue;
-        }
-        int stack[kStack];
-        int top = 0;
-        stack[top++] = root;
-        while (top > 0) {
-            const int node = stack[--top];
-            const int2 ch = w.bp_node_child[node];
-            const float4 bx[2] = {w.bp_node_b0[node], w.bp_node_b1[node]};
-            const int kids[2] = {ch.x, ch.y};
-            for (int c = 0; c < 2; ++c) {
-                if (!aabb_overlap(bx[c], q)) continue;
-                if (kids[c] < 0) emit(~kids[c]);
-                else if (top < kStack) stack[top++] = kids[c];
-                else atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_STACK_OVERFLOW);
+        for (int h = 0; h < 2; ++h) {
+            const int root = w.bp_world_root[wd + (h ? (uint32_t)w.num_worlds : 0u)];
+            if (root == INT_MIN) continue;
+            if (root < 0) {
+                if (aabb_overlap(w.bp_leaf[~root], q)) emit(~root);
+                continue;
+            }
+            int stack[kStack];
+            int top = 0;
+            stack[top++] = root;
+            while (top > 0) {
+                const int node = stack[--top];
+                const int2 ch = w.bp_node_child[node];
+                const float4 bx[2] = {w.bp_node_b0[node], w.bp_node_b1[node]};
+                const int kids[2] = {ch.x, ch.y};
+                for (int c = 0; c < 2; ++c) {
+                    if (!aabb_overlap(bx[c], q)) continue;
+                    if (kids[c] < 0) emit(~kids[c]);
+                    else if (top < kStack) stack[top++] = kids[c];
+                    else atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_STACK_OVERFLOW);
+                }
             }
         }
     }
