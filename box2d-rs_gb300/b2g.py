@@ -378,6 +378,7 @@ def load_library(path=LIB_PATH):
         "b2g_set_gravity": [vp, Vec2],
         "b2g_set_allow_sleeping": [vp, i32],
         "b2g_set_warm_starting": [vp, i32],
+        "b2g_set_part_solve": [vp, i32],
         "b2g_set_continuous_physics": [vp, i32],
         "b2g_set_auto_clear_forces": [vp, i32],
         "b2g_clear_forces": [vp],
@@ -567,6 +568,10 @@ class B2world:
 
     def set_warm_starting(self, flag):
         self._check(self._lib.b2g_set_warm_starting(self._h, int(flag)))
+
+    def set_part_solve(self, flag):
+        """Part-local solve on (default) or off (every constraint in grid-wide colours)."""
+        self._check(self._lib.b2g_set_part_solve(self._h, int(flag)))
 
     def set_continuous_physics(self, flag):
         self._check(self._lib.b2g_set_continuous_physics(self._h, int(flag)))

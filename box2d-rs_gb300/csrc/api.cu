@@ -121,6 +121,7 @@ struct World {
     int last_colours = 0;
     /* CUDA graphs of the steady-state step, one per contact-buffer parity */
     bool use_graphs = true;
+    bool part_solve = true;       /* b2g_set_part_solve */
     GraphSlot graphs[2];
     int swaps = 0;
     int alloc_generation = 0;
@@ -508,8 +509,9 @@ int allocate(World* w, int nb, int nf) {
     } while (0)
     A(d.b_xf, body_cap); A(d.b_pos, body_cap); A(d.b_pos0, body_cap); A(d.b_vel, body_cap);
     A(d.b_force, body_cap); A(d.b_mass, body_cap); A(d.b_damp, body_cap); A(d.b_lc, body_cap);
-    A(d.b_flags, body_cap); A(d.b_world, body_cap); A(d.b_island, body_cap);
-    A(d.b_cmin, 2 * (size_t)body_cap); A(d.b_cmask, body_cap);
+    A(d.b_flags, body_cap); A(d.b_world, body_cap); A(d.b_island, body_cap); A(d.b_rank, body_cap);
+    A(d.b_part, body_cap); A(d.b_cidx, body_cap);
+    A(d.b_cmin, 4 * (size_t)body_cap); A(d.b_cmask, 2 * (size_t)body_cap);
     /* one per-island separation buffer per position iteration (at least 2: the island pass
      * uses the second as its "has an awake member" flag) */
     w->minsep_buffers = std::max(2, w->minsep_buffers);
@@ -526,7 +528,11 @@ int allocate(World* w, int nb, int nf) {
     A(d.n_key, pair_cap); A(d.n_fix, pair_cap); A(d.n_idx, pair_cap); A(d.n_key_alt, pair_cap); A(d.n_idx_alt, pair_cap);
     A(d.cons_contact, contact_cap); A(d.cons_colour, contact_cap); A(d.cons_island, contact_cap);
     A(d.s_contact, contact_cap); A(d.s_cons, contact_cap); A(d.s_fix, contact_cap);
-    A(d.col_off, kMaxColours + 1); A(d.col_hist, kMaxColours);
+    A(d.cons_part, contact_cap);
+    A(d.col_off, kMaxColours + 1); A(d.col_hist, (size_t)(kMaxParts + 1) * kMaxColours);
+    A(d.part_off, (size_t)kMaxParts * (kMaxColours + 1)); A(d.part_ncol, kMaxParts); A(d.part_tot, kMaxParts + 1);
+    A(d.rank_x, fix_cap); A(d.blk_tot, kMaxParts); A(d.cache_body, fix_cap);
+    A(d.part_cbeg, kMaxParts); A(d.part_cend, kMaxParts);
     A(d.vc_idx, contact_cap); A(d.vc_inv, contact_cap); A(d.vc_nf, contact_cap); A(d.vc_r0, contact_cap);
     A(d.vc_r1, contact_cap); A(d.vc_m0, contact_cap); A(d.vc_m1, contact_cap); A(d.vc_imp, contact_cap);
     A(d.vc_k, contact_cap); A(d.vc_island, contact_cap);
@@ -689,6 +695,8 @@ int status_error(World* w, int status) {
                     "contact_capacity / pair_capacity in b2g_world_def");
     if (status & ST_EVENT_OVERFLOW) return fail(w, B2G_ERR_CAPACITY, "contact event buffer overflowed");
     if (status & ST_RECORD_OVERFLOW) return fail(w, B2G_ERR_CAPACITY, "recorded pair buffer overflowed");
+    if (status & ST_PART_MISMATCH)
+        return fail(w, B2G_ERR_CUDA, "the solver ran with a block count other than its colouring's");
     return B2G_OK;
 }
 
@@ -737,11 +745,11 @@ void issue_step(World* w, const StepParams& sp, float dt, bool capturing = false
     if (dt > 0.0f) {
         launch_islands_and_constraints(w->d, sp, s);
         mark(t.e[6]);
-        launch_colouring(w->d, s, w->num_sms);
         const bool taping = w->tape && w->tape->recording;
+        launch_colouring(w->d, s, w->num_sms, w->part_solve);
         if (taping) launch_tape_record(w->d, w->tape->d, sp, s, w->num_sms);
         mark(t.e[3]);
-        launch_solver(w->d, sp, s, w->num_sms);
+        launch_solver(w->d, sp, s, w->num_sms, w->part_solve);
         if (taping) launch_tape_post(w->d, w->tape->d, sp, s, w->num_sms);
         mark(t.e[4]);
         launch_broadphase(w->d, sp, s, w->num_sms, [&]() { mark(t.e[7]); });
@@ -1265,6 +1273,13 @@ int b2g_set_allow_sleeping(void* p, int32_t flag) {
     if (!p) return B2G_ERR_INVALID_ARG;
     if (flag) tape_touch(W(p));
     W(p)->allow_sleep = flag != 0;
+    return B2G_OK;
+}
+int b2g_set_part_solve(void* p, int32_t flag) {
+    if (!p) return B2G_ERR_INVALID_ARG;
+    World* w = W(p);
+    if (w->part_solve != (flag != 0)) drop_graphs(w);
+    w->part_solve = flag != 0;
     return B2G_OK;
 }
 int b2g_set_warm_starting(void* p, int32_t flag) {
@@ -1999,6 +2014,12 @@ int b2g_tape_begin(void* p, int32_t max_steps, int32_t every, int64_t max_slots)
     A(&d.slots, (size_t)t->slot_cap);
     A(&d.steps, (size_t)max_steps);
     A(&d.col_off, (size_t)max_steps * (kMaxColours + 1));
+    /* the part-local solve has at most one part per SM, each with a row of its colour offsets */
+    d.max_parts = std::max(1, std::min(w->num_sms, kMaxParts));
+    d.pool_cap = (long long)max_steps * d.max_parts * 20;
+    A(&d.part_np, (size_t)max_steps);
+    A(&d.part_row, (size_t)max_steps * d.max_parts);
+    A(&d.part_pool, (size_t)d.pool_cap);
     A(&d.cmap[0], (size_t)w->d.contact_cap);
     A(&d.cmap[1], (size_t)w->d.contact_cap);
     A(&d.ckpt_pos, nck);
@@ -2071,10 +2092,34 @@ int b2g_tape_get_step(void* p, int32_t step, b2g_tape_step* out_step, int32_t* o
     if (step < 0 || step >= steps) return fail(w, B2G_ERR_INVALID_ARG, "step out of range");
     TapeStep st;
     CUDA_OK(w, cudaMemcpy(&st, t->d.steps + step, sizeof(st), cudaMemcpyDeviceToHost));
-    if (out_step) memcpy(out_step, &st, sizeof(st));
-    if (out_col)
-        CUDA_OK(w, cudaMemcpy(out_col, t->d.col_off + (size_t)step * (kMaxColours + 1), (st.ncol + 1) * sizeof(int),
+    /* The solve order as one list of colour groups (slots of a group are independent): each
+     * part's interior colours, then the boundary colours. */
+    std::vector<int> groups;
+    int np = 0;
+    CUDA_OK(w, cudaMemcpy(&np, t->d.part_np + step, sizeof(int), cudaMemcpyDeviceToHost));
+    if (np > 0) {
+        std::vector<int> rows((size_t)np);
+        CUDA_OK(w, cudaMemcpy(rows.data(), t->d.part_row + (size_t)step * t->d.max_parts, np * sizeof(int),
                               cudaMemcpyDeviceToHost));
+        int last_n = 0;
+        CUDA_OK(w, cudaMemcpy(&last_n, t->d.part_pool + rows[np - 1], sizeof(int), cudaMemcpyDeviceToHost));
+        const int beg = rows[0], end = rows[np - 1] + last_n + 2;
+        std::vector<int> seg((size_t)(end - beg));
+        CUDA_OK(w, cudaMemcpy(seg.data(), t->d.part_pool + beg, seg.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        for (int q = 0; q < np; ++q) {
+            const int* row = seg.data() + (rows[q] - beg);
+            for (int c = 0; c < row[0]; ++c) groups.push_back(row[1 + c]);
+        }
+    }
+    std::vector<int> co((size_t)st.ncol + 1);
+    CUDA_OK(w, cudaMemcpy(co.data(), t->d.col_off + (size_t)step * (kMaxColours + 1), co.size() * sizeof(int),
+                          cudaMemcpyDeviceToHost));
+    for (int c = 0; c < st.ncol; ++c) groups.push_back(co[c]);
+    const int ngroups = (int)groups.size();
+    groups.push_back(st.nslots);
+    st.ncol = ngroups;
+    if (out_step) memcpy(out_step, &st, sizeof(st));
+    if (out_col) memcpy(out_col, groups.data(), groups.size() * sizeof(int));
     if (out_slots) {
         if (cap < st.nslots) return fail(w, B2G_ERR_CAPACITY, "slot buffer too small");
         if (st.nslots > 0)

@@ -56,6 +56,7 @@ enum : uint32_t {
     ST_BARRIER_TIMEOUT = 1u << 4,
     ST_STACK_OVERFLOW = 1u << 5,
     ST_RECORD_OVERFLOW = 1u << 6,
+    ST_PART_MISMATCH = 1u << 7,   /* the solver ran with other parts than its colouring */
 };
 
 /* device counters (d_cnt[]) */
@@ -76,11 +77,14 @@ enum {
     CNT_ISLANDS = 18,
     CNT_COLOURINGS = 19,  /* colourings done so far: the stamp of colours kept in contacts (mids.w) */
     CNT_DYN_EXTENT = 20,  /* largest half-extent of a dynamic body's fat AABB (float bits), this pass */
+    CNT_INTERIOR = 21,    /* constraint slots solved part-locally this step (slots [0, n)) */
+    CNT_PARTS = 22,       /* parts of this step's colouring (= blocks of the solver), 0 if off */
     CNT_SIZE = 32
 };
 
 constexpr int kMaxColours = 256;   /* first-fit colours 0..63, then one per colouring round */
 constexpr int kFirstFitColours = 64;
+constexpr int kMaxParts = 1024;    /* body parts of the part-local solve (at most one per solver block) */
 constexpr int kMaxPosIters = 64;
 
 struct Contacts {
@@ -105,6 +109,8 @@ struct StepParams {
     int auto_clear;
     int record_events;
     int record_pairs;
+    int part_bodies;      /* part-local solve: bodies cached in shared memory per block */
+    int part_slot_bytes;  /* part-local solve: shared memory per block for constraint slots */
 };
 
 struct DevWorld {
@@ -122,8 +128,14 @@ struct DevWorld {
     uint32_t* b_flags;
     uint32_t* b_world;
     int* b_island;
-    unsigned long long* b_cmin;  /* colouring: minimum priority of uncoloured constraints */
-    unsigned long long* b_cmask; /* colouring: colours used at this body */
+    int* b_rank;                 /* smallest sorted position of the body's proxies in the last
+                                    broadphase (Morton order), INT_MAX if none */
+    int* b_part;                 /* part-local solve: the body's part (valid for constraint bodies) */
+    int* b_cidx;                 /* part-local solve: the body's place among constraint bodies in
+                                    rank order (valid for constraint bodies) */
+    unsigned long long* b_cmin;  /* colouring: minimum priority of uncoloured constraints,
+                                    2 round parities x 2 classes x body_cap */
+    unsigned long long* b_cmask; /* colouring: colours used at this body, 2 classes x body_cap */
     uint32_t* isl_minsep;        /* 2 x body_cap: per-island max(-separation) bits, double-buffered */
     uint8_t* isl_done;
     float* isl_sleep;            /* per island root: min sleep time (as ordered uint bits) */
@@ -154,8 +166,20 @@ struct DevWorld {
     int* s_contact;              /* slot -> contact (sorted by colour) */
     int* s_cons;                 /* slot -> constraint */
     int2* s_fix;                 /* slot -> (fixture A, fixture B): the solve order exported to the host */
-    int* col_off;                /* kMaxColours + 1 offsets of non-empty colours */
-    int* col_hist;               /* kMaxColours counts */
+    int* cons_part;              /* part of an interior constraint, -1 for a boundary one */
+    int* col_off;                /* kMaxColours + 1 offsets of non-empty boundary colours */
+    int* col_hist;               /* (kMaxParts + 1) x kMaxColours counts, then slot cursors:
+                                    rows of the parts' interior colours, last row the boundary's */
+    int* part_off;               /* kMaxParts x (kMaxColours + 1): offsets of each part's
+                                    non-empty interior colours */
+    int* part_ncol;              /* kMaxParts: non-empty interior colours of each part */
+    int* part_tot;               /* kMaxParts + 1: slots of each histogram row */
+    unsigned long long* rank_x;  /* per Morton rank: constraint endpoints << 32 | has-any, then
+                                    its exclusive prefix within the scanning block's chunk */
+    unsigned long long* blk_tot; /* kMaxParts: chunk totals of that scan */
+    int* cache_body;             /* constraint bodies in rank order */
+    int* part_cbeg;              /* kMaxParts: each part's first entry of cache_body */
+    int* part_cend;              /* kMaxParts: one past its last */
     int4* vc_idx;                /* ia, ib, point count, flags (bit0 A dynamic, bit1 B dynamic) */
     float4 *vc_inv, *vc_nf, *vc_r0, *vc_r1, *vc_m0, *vc_m1, *vc_imp, *vc_k;
     float4 *pc_lp, *pc_geo, *pc_lc, *pc_inv, *pc_meta;
@@ -188,8 +212,9 @@ struct DevWorld {
 /* kernel-file launchers */
 void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s);
 void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cudaStream_t s);
-void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms);
-int launch_solver(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms);
+/* parts: allow the part-local solve (used where the world's size suits it) */
+void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms, bool parts);
+int launch_solver(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms, bool parts);
 /* after_tree (optional) is called between the tree pass (keys, sort, build, refit, traverse)
  * and the contact merge, so the caller can record a profiling event there */
 void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms,

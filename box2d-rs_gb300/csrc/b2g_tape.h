@@ -41,7 +41,7 @@ struct TapeStep {
 };
 static_assert(sizeof(TapeStep) == 48, "TapeStep layout");
 
-enum { TAPE_CNT_STEPS = 0, TAPE_CNT_SLOTS = 1, TAPE_CNT_STATUS = 2, TAPE_CNT_SIZE = 4 };
+enum { TAPE_CNT_STEPS = 0, TAPE_CNT_SLOTS = 1, TAPE_CNT_STATUS = 2, TAPE_CNT_POOL = 3, TAPE_CNT_SIZE = 4 };
 enum : unsigned long long { TAPE_ST_OVERFLOW = 1ull };
 
 struct TapeDev {
@@ -50,7 +50,14 @@ struct TapeDev {
     TapeStep* steps;
     int step_cap;
     int ckpt_every;
-    int* col_off;                    /* step_cap x (kMaxColours + 1) */
+    int* col_off;                    /* step_cap x (kMaxColours + 1): boundary colour offsets (all
+                                        colours of a step solved without parts) */
+    int* part_np;                    /* step_cap: parts of the step's part-local solve (0: none) */
+    int* part_row;                   /* step_cap x max_parts: each part's row in part_pool */
+    int* part_pool;                  /* rows [colours n, offset 0 .. offset n] of the parts' interior
+                                        colours */
+    long long pool_cap;
+    int max_parts;
     unsigned long long* cmap[2];     /* per step parity, per contact: (step + 1) << 32 | slot */
     float4* ckpt_pos;                /* (step_cap / ckpt_every + 2) x n_bodies: c.x, c.y, a, - */
     float4* ckpt_vel;                /* v.x, v.y, w, - */

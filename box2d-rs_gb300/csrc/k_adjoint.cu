@@ -76,6 +76,39 @@ __global__ void k_tape_record(DevWorld w, TapeDev t, StepParams sp) {
         t.steps[step] = s;
     }
     for (int c = gtid; c <= ncol; c += gsize) t.col_off[(size_t)step * (kMaxColours + 1) + c] = w.col_off[c];
+    if (blockIdx.x == 0) {
+        /* the part-local layout: one row [n, offsets 0..n] per part, packed into the pool */
+        __shared__ int s_row[kMaxParts + 2];
+        const int np = w.cnt[CNT_INTERIOR] > 0 ? min(w.cnt[CNT_PARTS], t.max_parts) : 0;
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int q = 0; q < np; ++q) {
+                s_row[q] = acc;
+                acc += w.part_ncol[q] + 2;
+            }
+            const long long at = t.cnt[TAPE_CNT_POOL];
+            if (w.cnt[CNT_INTERIOR] > 0 && w.cnt[CNT_PARTS] > t.max_parts) t.cnt[TAPE_CNT_STATUS] |= (long long)TAPE_ST_OVERFLOW;
+            if (at + acc > t.pool_cap) {
+                t.cnt[TAPE_CNT_STATUS] |= (long long)TAPE_ST_OVERFLOW;
+                s_row[kMaxParts + 1] = -1;
+            } else {
+                t.cnt[TAPE_CNT_POOL] = at + acc;
+                s_row[kMaxParts + 1] = (int)at;
+                t.part_np[step] = np;
+            }
+        }
+        __syncthreads();
+        const int at = s_row[kMaxParts + 1];
+        if (at >= 0) {
+            for (int q = threadIdx.x; q < np; q += blockDim.x) {
+                const int nc = w.part_ncol[q];
+                int* row = t.part_pool + at + s_row[q];
+                t.part_row[(size_t)step * t.max_parts + q] = at + s_row[q];
+                row[0] = nc;
+                for (int c = 0; c <= nc; ++c) row[1 + c] = w.part_off[(size_t)q * (kMaxColours + 1) + c];
+            }
+        }
+    }
     if (step % t.ckpt_every == 0) {
         const size_t o = (size_t)(step / t.ckpt_every) * t.n_bodies;
         for (int b = gtid; b < t.n_bodies; b += gsize) {
@@ -272,6 +305,69 @@ __device__ __forceinline__ float4* wp_rec(const AdjWork& a, int s, int it, int k
     return a.wp + (((size_t)s * a.max_pi + it) * a.max_slots + k) * 2;
 }
 
+/* A taped step's solve order: the interior colours of each part (the parts are independent, so a
+ * block sweeps whole parts, separated by __syncthreads), then the boundary colours grid-wide. */
+struct StepOrder {
+    const int* co;      /* boundary colour offsets */
+    int ncol;
+    int np;             /* parts (0: the step ran without) */
+    const int* rows;    /* per part: its row in the pool */
+    const int* pool;
+};
+
+__device__ __forceinline__ StepOrder step_order(const AdjWork& a, int t, const TapeStep& st) {
+    StepOrder o;
+    o.co = a.t.col_off + (size_t)t * (kMaxColours + 1);
+    o.ncol = st.ncol;
+    o.np = a.t.part_np[t];
+    o.rows = a.t.part_row + (size_t)t * a.t.max_parts;
+    o.pool = a.t.part_pool;
+    return o;
+}
+
+/* fn(k) for every slot in solve order, each colour complete before the next */
+template <class F>
+__device__ __forceinline__ bool sweep_forward(const StepOrder& o, int* cnt, F&& fn) {
+    if (o.np > 0) {
+        for (int p = blockIdx.x; p < o.np; p += gridDim.x) {
+            const int* row = o.pool + o.rows[p];
+            const int nc = row[0];
+            for (int c = 0; c < nc; ++c) {
+                for (int k = row[1 + c] + threadIdx.x; k < row[2 + c]; k += blockDim.x) fn(k);
+                __syncthreads();
+            }
+        }
+        if (!sync_all(cnt)) return false;
+    }
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gsize = gridDim.x * blockDim.x;
+    for (int c = 0; c < o.ncol; ++c) {
+        for (int k = o.co[c] + gtid; k < o.co[c + 1]; k += gsize) fn(k);
+        if (!sync_all(cnt)) return false;
+    }
+    return true;
+}
+
+/* the same colours in the reverse order */
+template <class F>
+__device__ __forceinline__ bool sweep_reverse(const StepOrder& o, int* cnt, F&& fn) {
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gsize = gridDim.x * blockDim.x;
+    for (int c = o.ncol - 1; c >= 0; --c) {
+        for (int k = o.co[c] + gtid; k < o.co[c + 1]; k += gsize) fn(k);
+        if (!sync_all(cnt)) return false;
+    }
+    if (o.np > 0) {
+        for (int p = blockIdx.x; p < o.np; p += gridDim.x) {
+            const int* row = o.pool + o.rows[p];
+            for (int c = row[0] - 1; c >= 0; --c) {
+                for (int k = row[1 + c] + threadIdx.x; k < row[2 + c]; k += blockDim.x) fn(k);
+                __syncthreads();
+            }
+        }
+        if (!sync_all(cnt)) return false;
+    }
+    return true;
+}
+
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_adj_replay(AdjWork a) {
     grid_barrier_start();
@@ -290,9 +386,9 @@ __global__ void __launch_bounds__(BLOCK) k_adj_replay(AdjWork a) {
         const int s = t - a.t0;
         const TapeStep st = a.t.steps[t];
         const TapeSlot* sl = a.t.slots + st.slot_off;
-        const int* co = a.t.col_off + (size_t)t * (kMaxColours + 1);
+        const StepOrder order = step_order(a, t, st);
         const float h = st.dt;
-        const int ns = st.nslots, ncol = st.ncol;
+        const int ns = st.nslots;
         float4* wsp = a.ws_pos + (size_t)s * nb;
         float4* wv1 = a.ws_vel1 + (size_t)s * nb;
         float4* wv2 = a.ws_vel2 + (size_t)s * nb;
@@ -335,8 +431,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_replay(AdjWork a) {
         }
         if (!sync_all(a.cnt)) return;
         if (st.warm) {
-            for (int c = 0; c < ncol; ++c) {
-                for (int k = co[c] + gtid; k < co[c + 1]; k += gsize) {
+            const bool ok = sweep_forward(order, a.cnt, [&](int k) {
                     const SlotStatic ss = slot_static(sl[k]);
                     const float4 vA = a.cur_vel[ss.a], vB = a.cur_vel[ss.b];
                     float4* rec = a.ww + ((size_t)s * a.max_slots + k) * 2;
@@ -350,14 +445,12 @@ __global__ void __launch_bounds__(BLOCK) k_adj_replay(AdjWork a) {
                     warm_slot(ss, vc, ni, ti, va, wa, vb, wb);
                     if (ss.flags & 1) a.cur_vel[ss.a] = make_float4(va.x, va.y, wa, vA.w);
                     if (ss.flags & 2) a.cur_vel[ss.b] = make_float4(vb.x, vb.y, wb, vB.w);
-                }
-                if (!sync_all(a.cnt)) return;
-            }
+            });
+            if (!ok) return;
         }
         /* velocity iterations */
         for (int it = 0; it < st.vi; ++it) {
-            for (int c = 0; c < ncol; ++c) {
-                for (int k = co[c] + gtid; k < co[c + 1]; k += gsize) {
+            const bool ok = sweep_forward(order, a.cnt, [&](int k) {
                     const SlotStatic ss = slot_static(sl[k]);
                     const float4 vA = a.cur_vel[ss.a], vB = a.cur_vel[ss.b];
                     const float4 im = a.imp[k];
@@ -376,9 +469,8 @@ __global__ void __launch_bounds__(BLOCK) k_adj_replay(AdjWork a) {
                     a.imp[k] = make_float4(ni[0], ti[0], ni[1], ti[1]);
                     if (ss.flags & 1) a.cur_vel[ss.a] = make_float4(va.x, va.y, wa, vA.w);
                     if (ss.flags & 2) a.cur_vel[ss.b] = make_float4(vb.x, vb.y, wb, vB.w);
-                }
-                if (!sync_all(a.cnt)) return;
-            }
+            });
+            if (!ok) return;
         }
         /* position integration with the translation / rotation clamps */
         for (int b = gtid; b < nb; b += gsize) {
@@ -396,10 +488,9 @@ __global__ void __launch_bounds__(BLOCK) k_adj_replay(AdjWork a) {
         if (!sync_all(a.cnt)) return;
         /* position iterations, each island for the number of iterations it ran */
         for (int it = 0; it < st.pi; ++it) {
-            for (int c = 0; c < ncol; ++c) {
-                for (int k = co[c] + gtid; k < co[c + 1]; k += gsize) {
+            const bool ok = sweep_forward(order, a.cnt, [&](int k) {
                     const TapeSlot ts = sl[k];
-                    if (it >= __float_as_int(ts.rad.w)) continue;
+                    if (it >= __float_as_int(ts.rad.w)) return;
                     const SlotStatic ss = slot_static(ts);
                     const float4 pA = a.cur_pos[ss.a], pB = a.cur_pos[ss.b];
                     P2<float> cA = p2(pA.x, pA.y), cB = p2(pB.x, pB.y);
@@ -411,9 +502,8 @@ __global__ void __launch_bounds__(BLOCK) k_adj_replay(AdjWork a) {
                     rec[1] = make_float4(pB.y, pB.z, __int_as_float(dec[0] | (dec[1] << 8)), 0.0f);
                     if (ss.flags & 1) a.cur_pos[ss.a] = make_float4(cA.x, cA.y, aA, pA.w);
                     if (ss.flags & 2) a.cur_pos[ss.b] = make_float4(cB.x, cB.y, aB, pB.w);
-                }
-                if (!sync_all(a.cnt)) return;
-            }
+            });
+            if (!ok) return;
         }
     }
     /* the replay must land on the recorded state bit for bit */
@@ -437,9 +527,9 @@ __global__ void __launch_bounds__(BLOCK) k_adj_reverse(AdjWork a) {
         const int s = t - a.t0;
         const TapeStep st = a.t.steps[t];
         const TapeSlot* sl = a.t.slots + st.slot_off;
-        const int* co = a.t.col_off + (size_t)t * (kMaxColours + 1);
+        const StepOrder order = step_order(a, t, st);
         const float h = st.dt;
-        const int ns = st.nslots, ncol = st.ncol;
+        const int ns = st.nslots;
         const int nprev = t > 0 ? a.t.steps[t - 1].nslots : 0;
         const float4* wsp = a.ws_pos + (size_t)s * nb;
         const float4* wv1 = a.ws_vel1 + (size_t)s * nb;
@@ -448,10 +538,9 @@ __global__ void __launch_bounds__(BLOCK) k_adj_reverse(AdjWork a) {
         float4* gend_prev = a.g_end[(t + 1) & 1];
         /* position iterations, last to first */
         for (int it = st.pi - 1; it >= 0; --it) {
-            for (int c = ncol - 1; c >= 0; --c) {
-                for (int k = co[c] + gtid; k < co[c + 1]; k += gsize) {
+            const bool ok = sweep_reverse(order, a.cnt, [&](int k) {
                     const TapeSlot ts = sl[k];
-                    if (it >= __float_as_int(ts.rad.w)) continue;
+                    if (it >= __float_as_int(ts.rad.w)) return;
                     const SlotStatic ss = slot_static(ts);
                     const float4* rec = wp_rec(a, s, it, k);
                     const float4 r0 = rec[0], r1 = rec[1];
@@ -466,9 +555,8 @@ __global__ void __launch_bounds__(BLOCK) k_adj_reverse(AdjWork a) {
                                        p2(r0.w, r1.x), r1.y, dec, gcA, gaA, gcB, gaB);
                     put_g(a.g_pos, ss.a, dA, gcA, gaA);
                     put_g(a.g_pos, ss.b, dB, gcB, gaB);
-                }
-                if (!sync_all(a.cnt)) return;
-            }
+            });
+            if (!ok) return;
         }
         /* position integration; constraint data of the step again; impulse adjoints */
         for (int b = gtid; b < nb; b += gsize) {
@@ -502,8 +590,7 @@ __global__ void __launch_bounds__(BLOCK) k_adj_reverse(AdjWork a) {
         if (!sync_all(a.cnt)) return;
         /* velocity iterations, last to first */
         for (int it = st.vi - 1; it >= 0; --it) {
-            for (int c = ncol - 1; c >= 0; --c) {
-                for (int k = co[c] + gtid; k < co[c + 1]; k += gsize) {
+            const bool ok = sweep_reverse(order, a.cnt, [&](int k) {
                     const SlotStatic ss = slot_static(sl[k]);
                     const float4* rec = wv_rec(a, s, it, k);
                     const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2];
@@ -528,9 +615,8 @@ __global__ void __launch_bounds__(BLOCK) k_adj_reverse(AdjWork a) {
                     a.g_imp[k] = make_float4(gni[0], gti[0], gni[1], gti[1]);
                     put_g(a.g_vel, ss.a, dA, gvA, gwA);
                     put_g(a.g_vel, ss.b, dB, gvB, gwB);
-                }
-                if (!sync_all(a.cnt)) return;
-            }
+            });
+            if (!ok) return;
         }
         /* warm start (reads the body adjoints only) and the impulse carry to the previous step */
         for (int k = gtid; k < ns; k += gsize) {
@@ -572,8 +658,8 @@ __global__ void __launch_bounds__(BLOCK) k_adj_reverse(AdjWork a) {
         }
         if (!sync_all(a.cnt)) return;
         /* constraint initialisation, colour by colour */
-        for (int c = ncol - 1; c >= 0; --c) {
-            for (int k = co[c] + gtid; k < co[c + 1]; k += gsize) {
+        {
+            const bool ok = sweep_reverse(order, a.cnt, [&](int k) {
                 const TapeSlot ts = sl[k];
                 const SlotStatic ss = slot_static(ts);
                 const float4 pA = wsp[ss.a], pB = wsp[ss.b];
@@ -592,8 +678,8 @@ __global__ void __launch_bounds__(BLOCK) k_adj_reverse(AdjWork a) {
                 put_g(a.g_pos, ss.b, dB, gcB, gaB);
                 put_g(a.g_vel, ss.a, dA, gvA, gwA);
                 put_g(a.g_vel, ss.b, dB, gvB, gwB);
-            }
-            if (!sync_all(a.cnt)) return;
+            });
+            if (!ok) return;
         }
         /* velocity integration */
         for (int b = gtid; b < nb; b += gsize) {

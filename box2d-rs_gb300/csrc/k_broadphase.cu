@@ -73,6 +73,8 @@ __global__ void k_bp_init(DevWorld w) {
 }
 
 __global__ void k_bp_bounds(DevWorld w) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x)
+        w.b_rank[b] = INT_MAX;
     int mnx = INT_MAX, mny = INT_MAX, mxx = INT_MIN, mxy = INT_MIN, dyn = 0;
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < w.n_fixtures; f += gridDim.x * blockDim.x) {
         const float4 a = w.f_fat[f];
@@ -181,7 +183,10 @@ __global__ void k_bp_build(DevWorld w) {
 __global__ void k_bp_leaves(DevWorld w) {
     const int n = w.n_fixtures;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        w.bp_leaf[p] = w.f_fat[w.bp_val[p]];
+        const uint32_t f = w.bp_val[p];
+        w.bp_leaf[p] = w.f_fat[f];
+        atomicMin(&w.b_rank[w.f_body[f]], p);  /* the body's Morton rank: its first proxy's position */
+        w.rank_x[p] = 0ull;                      /* the colouring weighs ranks by constraints */
         const uint32_t wd = (uint32_t)(w.bp_key[p] >> kMortonBits);
         const bool first = p == 0 || (uint32_t)(w.bp_key[p - 1] >> kMortonBits) != wd;
         const bool last = p == n - 1 || (uint32_t)(w.bp_key[p + 1] >> kMortonBits) != wd;

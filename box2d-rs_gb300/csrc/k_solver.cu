@@ -36,6 +36,7 @@ namespace b2g {
 namespace {
 
 constexpr int kBlock = 256;
+static_assert(kBlock == kMaxColours, "the colouring scans one histogram row of kMaxColours per block");
 
 __device__ __forceinline__ bool is_dynamic(uint32_t flags) { return (flags & BF_TYPE_MASK) == BODY_DYNAMIC; }
 __device__ __forceinline__ bool is_static(uint32_t flags) { return (flags & BF_TYPE_MASK) == BODY_STATIC; }
@@ -148,43 +149,176 @@ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
     return x;
 }
 
-/* Colouring. A constraint that was also a constraint of the previous colouring keeps its
- * first-fit colour (stored in its contact with that colouring's stamp): the previous colours were
- * a proper colouring of the previous constraints, so any subset of them still is. Only the new
- * constraints are coloured, by Jones-Plassmann rounds (hash priorities; a local minimum at both
- * of its dynamic bodies takes the lowest colour free at both), so a step whose contacts persist
- * needs one or two rounds instead of one per colour. */
-__global__ void __launch_bounds__(kBlock) k_colour(DevWorld w) {
+/* Block-wide exclusive scan of one int per thread (blockDim.x == kBlock); *total gets the sum. */
+__device__ __forceinline__ int block_scan_excl(int v, int* total) {
+    __shared__ int s_warp[kBlock / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[wid] = x;
+    __syncthreads();
+    int base = 0, tot = 0;
+    for (int i = 0; i < kBlock / 32; ++i) {
+        const int t = s_warp[i];
+        if (i < wid) base += t;
+        tot += t;
+    }
+    __syncthreads();
+    *total = tot;
+    return base + x - v;
+}
+
+/* Block-wide exclusive scan of one 64-bit value per thread; *total gets the sum. */
+__device__ __forceinline__ unsigned long long block_scan_excl64(unsigned long long v, unsigned long long* total) {
+    __shared__ unsigned long long s_warp64[kBlock / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned long long x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp64[wid] = x;
+    __syncthreads();
+    unsigned long long base = 0, tot = 0;
+    for (int i = 0; i < kBlock / 32; ++i) {
+        const unsigned long long t = s_warp64[i];
+        if (i < wid) base += t;
+        tot += t;
+    }
+    __syncthreads();
+    *total = tot;
+    return base + x - v;
+}
+
+constexpr uint32_t kStampMask = 0x1ffffffu;  /* colouring stamps kept in contacts: 25 bits */
+
+/* Colouring. Constraints are of two classes. With the part-local solve, the dynamic bodies are
+ * split into parts (one per solver block, by Morton rank); a constraint whose dynamic bodies all
+ * lie in one part is interior, the others are boundary. Interior constraints are solved by their
+ * part's block alone and boundary ones in grid-wide colour sweeps afterwards, so only constraints
+ * of the same class must differ in colour where they share a dynamic body: each class has its
+ * own colour masks and priority offers, and the sparse boundary class needs few colours. Without
+ * parts every constraint is boundary (one grid-wide colouring).
+ * A constraint of the previous colouring that keeps its class keeps its first-fit colour (stored
+ * in its contact with that colouring's stamp and class): the previous colours of a class were a
+ * proper colouring of its constraints, so any subset of them still is. Only the others are
+ * coloured, by Jones-Plassmann rounds (hash priorities; a local minimum at both of its dynamic
+ * bodies takes the lowest colour free at both), so a step whose contacts persist needs one or
+ * two rounds instead of one per colour.
+ * Slots are then ordered part by part, each part by colour, then the boundary colours: solving
+ * the parts concurrently is solving them one after the other, as no two parts share a dynamic
+ * body, so this slot order is the sequential solve order. */
+__global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
     grid_barrier_start();
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsize = gridDim.x * blockDim.x;
     const int n = w.cnt[CNT_CONS];
+    const int nf = w.n_fixtures;
+    const int P = (nf > 0 && nparts <= kMaxParts && nparts <= (int)gridDim.x) ? nparts : 0;
+    const size_t bc = (size_t)w.body_cap;
     const unsigned long long kNone = ~0ull;
-    const uint32_t stamp = (uint32_t)w.cnt[CNT_COLOURINGS] & 0x3ffffffu;  /* the previous colouring's */
+    const uint32_t stamp = (uint32_t)w.cnt[CNT_COLOURINGS] & kStampMask;  /* the previous colouring's */
     /* offers are double-buffered by round parity: round r offers into buffer r & 1, and the
      * entries of buffer (r - 1) & 1 are reset during round r, so a round needs two barriers */
     for (int b = gtid; b < w.n_bodies; b += gsize) {
-        w.b_cmin[b] = kNone;
-        w.b_cmin[w.body_cap + b] = kNone;
+        for (int j = 0; j < 4; ++j) w.b_cmin[j * bc + b] = kNone;
         w.b_cmask[b] = 0ull;
+        w.b_cmask[bc + b] = 0ull;
     }
     /* every 16th colouring starts afresh, so kept colours do not stay fragmented after the
      * contact graph has changed (a fresh colouring of a settled stack needs fewer colours) */
     const bool keep = stamp != 0u && (stamp & 15u) != 0u;
-    for (int k = gtid; k < n; k += gsize) {
-        const uint32_t kept = w.c.mids[w.cons_contact[k]].w;
-        w.cons_colour[k] = (keep && (kept >> 6) == stamp) ? (int)(kept & 63u) : -1;
+    if (P > 0) {
+        /* Parts of equal work: weigh each Morton rank by the constraint endpoints of its body and
+         * cut the weight prefix into P equal ranges. rank_x was zeroed by the broadphase. */
+        for (int k = gtid; k < n; k += gsize) {
+            const int2 bd = w.c.body[w.cons_contact[k]];
+            if (is_dynamic(w.b_flags[bd.x]) && w.b_rank[bd.x] < nf) atomicAdd(&w.rank_x[w.b_rank[bd.x]], 1ull << 32);
+            if (is_dynamic(w.b_flags[bd.y]) && w.b_rank[bd.y] < nf) atomicAdd(&w.rank_x[w.b_rank[bd.y]], 1ull << 32);
+        }
+        for (int q = gtid; q < P; q += gsize) {
+            w.part_cbeg[q] = 0;
+            w.part_cend[q] = 0;
+        }
+        if (!grid_barrier(w)) return;
+        /* each block scans its chunk of ranks: (weight << 32 | has weight), exclusive */
+        const int chunk = (nf + (int)gridDim.x - 1) / (int)gridDim.x;
+        const int r0 = min(nf, (int)blockIdx.x * chunk), r1 = min(nf, r0 + chunk);
+        unsigned long long carry = 0;
+        for (int base = r0; base < r1; base += blockDim.x) {
+            const int r = base + threadIdx.x;
+            unsigned long long v = r < r1 ? w.rank_x[r] : 0ull;
+            v += v ? 1ull : 0ull;
+            unsigned long long tot;
+            const unsigned long long ex = block_scan_excl64(v, &tot);
+            if (r < r1) w.rank_x[r] = carry + ex;
+            carry += tot;
+        }
+        if (threadIdx.x == 0) w.blk_tot[blockIdx.x] = carry;
+        if (!grid_barrier(w)) return;
+        unsigned long long before = 0, all = 0;
+        {
+            unsigned long long mine = 0, every = 0;
+            for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
+                const unsigned long long t = w.blk_tot[q];
+                if (q < (int)blockIdx.x) mine += t;
+                every += t;
+            }
+            block_scan_excl64(mine, &before);
+            block_scan_excl64(every, &all);
+        }
+        const unsigned long long wtot = all >> 32;
+        for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+            const unsigned long long x = before + w.rank_x[r];
+            const unsigned long long x1 = before + (r + 1 < r1 ? w.rank_x[r + 1] : carry);
+            if ((uint32_t)x1 == (uint32_t)x || wtot == 0ull) continue;  /* no constraint at this rank */
+            const int part = min(P - 1, (int)(((x >> 32) * (unsigned long long)P) / wtot));
+            const int c = (int)(uint32_t)x;
+            if (c >= nf) continue;  /* cannot happen: at most one constraint body per rank */
+            const int b = w.f_body[w.bp_val[r]];
+            w.b_part[b] = part;
+            w.b_cidx[b] = c;
+            w.cache_body[c] = b;
+        }
+        if (!grid_barrier(w)) return;
+        /* each part's range of constraint bodies */
+        const int ncache = min(nf, (int)(uint32_t)all);
+        for (int c = gtid; c < ncache; c += gsize) {
+            const int part = w.b_part[w.cache_body[c]];
+            if (c == 0 || w.b_part[w.cache_body[c - 1]] != part) w.part_cbeg[part] = c;
+            if (c == ncache - 1 || w.b_part[w.cache_body[c + 1]] != part) w.part_cend[part] = c + 1;
+        }
     }
-    for (int c = gtid; c < kMaxColours; c += gsize) w.col_hist[c] = 0;
+    for (int k = gtid; k < n; k += gsize) {
+        const int ci = w.cons_contact[k];
+        int part = -1;
+        if (P > 0) {
+            const int2 bd = w.c.body[ci];
+            const bool da = is_dynamic(w.b_flags[bd.x]), db = is_dynamic(w.b_flags[bd.y]);
+            const int pa = !da ? -1 : (w.b_rank[bd.x] < nf ? w.b_part[bd.x] : -2);
+            const int pb = !db ? -1 : (w.b_rank[bd.y] < nf ? w.b_part[bd.y] : -2);
+            part = !da ? pb : (!db ? pa : (pa == pb ? pa : -1));
+            if (part < 0) part = -1;
+        }
+        w.cons_part[k] = part;
+        const uint32_t cls = part < 0 ? 1u : 0u;
+        const uint32_t kept = w.c.mids[ci].w;
+        w.cons_colour[k] = (keep && (kept >> 7) == stamp && ((kept >> 6) & 1u) == cls) ? (int)(kept & 63u) : -1;
+    }
+    for (int c = gtid; c < (P + 1) * kMaxColours; c += gsize) w.col_hist[c] = 0;
     if (!grid_barrier(w)) return;
     /* the kept colours are taken at their bodies */
     for (int k = gtid; k < n; k += gsize) {
         const int c = w.cons_colour[k];
         if (c < 0) continue;
         const int2 bd = w.c.body[w.cons_contact[k]];
+        const size_t cm = w.cons_part[k] < 0 ? bc : 0;
         const unsigned long long bit = 1ull << c;
-        if (is_dynamic(w.b_flags[bd.x])) atomicOr(&w.b_cmask[bd.x], bit);
-        if (is_dynamic(w.b_flags[bd.y])) atomicOr(&w.b_cmask[bd.y], bit);
+        if (is_dynamic(w.b_flags[bd.x])) atomicOr(&w.b_cmask[cm + bd.x], bit);
+        if (is_dynamic(w.b_flags[bd.y])) atomicOr(&w.b_cmask[cm + bd.y], bit);
     }
     if (gtid == 0) {
         /* two "still uncoloured" counters alternate by round parity: round r counts into
@@ -205,19 +339,20 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w) {
             if (gtid == 0) atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_COLOUR_OVERFLOW);
             break;
         }
-        unsigned long long* offer = w.b_cmin + (size_t)(round & 1) * w.body_cap;
-        unsigned long long* stale = w.b_cmin + (size_t)((round + 1) & 1) * w.body_cap;
+        unsigned long long* offer = w.b_cmin + (size_t)(round & 1) * 2 * bc;
+        unsigned long long* stale = w.b_cmin + (size_t)((round + 1) & 1) * 2 * bc;
         /* A: each uncoloured constraint offers its priority to its dynamic bodies */
         for (int k = gtid; k < n; k += gsize) {
             const int2 bd = w.c.body[w.cons_contact[k]];
+            const size_t cm = w.cons_part[k] < 0 ? bc : 0;
             if (round > 0) {
-                stale[bd.x] = kNone;
-                stale[bd.y] = kNone;
+                stale[cm + bd.x] = kNone;
+                stale[cm + bd.y] = kNone;
             }
             if (w.cons_colour[k] >= 0) continue;
             const unsigned long long key = ((unsigned long long)hash32((uint32_t)k) << 32) | (uint32_t)k;
-            if (is_dynamic(w.b_flags[bd.x])) atomicMin(&offer[bd.x], key);
-            if (is_dynamic(w.b_flags[bd.y])) atomicMin(&offer[bd.y], key);
+            if (is_dynamic(w.b_flags[bd.x])) atomicMin(&offer[cm + bd.x], key);
+            if (is_dynamic(w.b_flags[bd.y])) atomicMin(&offer[cm + bd.y], key);
         }
         if (gtid == 0) w.cnt[CNT_UNCOLOURED + (round & 1)] = 0;
         if (!grid_barrier(w)) return;
@@ -225,18 +360,20 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w) {
         for (int k = gtid; k < n; k += gsize) {
             if (w.cons_colour[k] >= 0) continue;
             const int2 bd = w.c.body[w.cons_contact[k]];
+            const size_t cm = w.cons_part[k] < 0 ? bc : 0;
             const unsigned long long key = ((unsigned long long)hash32((uint32_t)k) << 32) | (uint32_t)k;
             const bool da = is_dynamic(w.b_flags[bd.x]), db = is_dynamic(w.b_flags[bd.y]);
-            const bool winA = !da || offer[bd.x] == key;
-            const bool winB = !db || offer[bd.y] == key;
+            const bool winA = !da || offer[cm + bd.x] == key;
+            const bool winB = !db || offer[cm + bd.y] == key;
             if (winA && winB) {
-                const unsigned long long used = (da ? w.b_cmask[bd.x] : 0ull) | (db ? w.b_cmask[bd.y] : 0ull);
+                const unsigned long long used =
+                    (da ? w.b_cmask[cm + bd.x] : 0ull) | (db ? w.b_cmask[cm + bd.y] : 0ull);
                 int colour;
                 if (~used != 0ull) {
                     colour = __ffsll((long long)~used) - 1;
                     const unsigned long long bit = 1ull << colour;
-                    if (da) w.b_cmask[bd.x] |= bit;
-                    if (db) w.b_cmask[bd.y] |= bit;
+                    if (da) w.b_cmask[cm + bd.x] |= bit;
+                    if (db) w.b_cmask[cm + bd.y] |= bit;
                 } else {
                     colour = kFirstFitColours + round;
                     if (colour >= kMaxColours) {
@@ -253,41 +390,53 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w) {
         if (!grid_barrier(w)) return;
     }
     if (gtid == 0) w.cnt[CNT_ROUNDS] = round;
-    /* histogram, dense colour offsets, scatter into slots */
-    for (int k = gtid; k < n; k += gsize) atomicAdd(&w.col_hist[w.cons_colour[k]], 1);
-    if (!grid_barrier(w)) return;
-    if (blockIdx.x == 0) {
-        __shared__ int s_cnt[kMaxColours];
-        __shared__ int s_dense[kMaxColours];
-        for (int c = threadIdx.x; c < kMaxColours; c += blockDim.x) s_cnt[c] = w.col_hist[c];
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int base = 0, dense = 0;
-            for (int c = 0; c < kMaxColours; ++c) {
-                if (s_cnt[c] == 0) {
-                    s_dense[c] = -1;
-                    continue;
-                }
-                w.col_off[dense] = base;
-                s_dense[c] = base;  /* running cursor start */
-                base += s_cnt[c];
-                ++dense;
-            }
-            w.col_off[dense] = base;
-            w.cnt[CNT_COLOURS] = dense;
-        }
-        __syncthreads();
-        for (int c = threadIdx.x; c < kMaxColours; c += blockDim.x) w.col_hist[c] = s_dense[c];  /* cursor */
+    /* histogram rows: part p's interior colours are row p, the boundary colours row P */
+    for (int k = gtid; k < n; k += gsize) {
+        const int part = w.cons_part[k];
+        atomicAdd(&w.col_hist[(part < 0 ? P : part) * kMaxColours + w.cons_colour[k]], 1);
     }
     if (!grid_barrier(w)) return;
-    const uint32_t next = (stamp + 1u) & 0x3ffffffu;
+    for (int r = blockIdx.x; r <= P; r += gridDim.x) {
+        int tot;
+        block_scan_excl(w.col_hist[r * kMaxColours + threadIdx.x], &tot);
+        if (threadIdx.x == 0) w.part_tot[r] = tot;
+    }
+    if (!grid_barrier(w)) return;
+    /* dense offsets of each row's non-empty colours; the histogram becomes the slot cursors */
+    for (int r = blockIdx.x; r <= P; r += gridDim.x) {
+        int part_sum = 0;
+        for (int q = threadIdx.x; q < r; q += blockDim.x) part_sum += w.part_tot[q];
+        int base;
+        block_scan_excl(part_sum, &base);
+        const int cnt = w.col_hist[r * kMaxColours + threadIdx.x];
+        int tot, ndense;
+        const int excl = block_scan_excl(cnt, &tot);
+        const int dense = block_scan_excl(cnt > 0 ? 1 : 0, &ndense);
+        int* out = r < P ? w.part_off + (size_t)r * (kMaxColours + 1) : w.col_off;
+        if (cnt > 0) out[dense] = base + excl;
+        w.col_hist[r * kMaxColours + threadIdx.x] = base + excl;
+        if (threadIdx.x == 0) {
+            out[ndense] = base + tot;
+            if (r < P) {
+                w.part_ncol[r] = ndense;
+            } else {
+                w.cnt[CNT_COLOURS] = ndense;
+                w.cnt[CNT_INTERIOR] = base;
+                w.cnt[CNT_PARTS] = P;
+            }
+        }
+    }
+    if (!grid_barrier(w)) return;
+    const uint32_t next = (stamp + 1u) & kStampMask;
     for (int k = gtid; k < n; k += gsize) {
         const int c = w.cons_colour[k];
         const int ci = w.cons_contact[k];
-        const int slot = atomicAdd(&w.col_hist[c], 1);
+        const int part = w.cons_part[k];
+        const int slot = atomicAdd(&w.col_hist[(part < 0 ? P : part) * kMaxColours + c], 1);
         /* keep first-fit colours for the next colouring (the per-round overflow colours are not
          * kept: a later round could hand the same one to a neighbour) */
-        w.c.mids[ci].w = (c < kFirstFitColours && next != 0u) ? ((next << 6) | (uint32_t)c) : 0u;
+        w.c.mids[ci].w = (c < kFirstFitColours && next != 0u)
+                             ? ((next << 7) | ((part < 0 ? 1u : 0u) << 6) | (uint32_t)c) : 0u;
         if (slot < 0 || slot >= n) continue;  /* cannot happen with consistent offsets */
         w.s_contact[slot] = ci;
         w.s_cons[slot] = k;
@@ -436,17 +585,60 @@ __device__ void init_slot(const DevWorld& w, const StepParams& sp, int k) {
     w.s_fix[k] = fx;
 }
 
-__device__ __forceinline__ void warm_slot(const DevWorld& w, int k) {
-    const int4 idx = w.vc_idx[k];
-    const float4 inv = w.vc_inv[k];
-    const float4 nf = w.vc_nf[k];
-    const float4 imp = w.vc_imp[k];
-    float4 va = w.b_vel[idx.x], vb = w.b_vel[idx.y];
+/* One constraint slot's velocity data (vc_* arrays); idx = (body code A, body code B, point count,
+ * flags). A body code is the body index in the global arrays, or in the part-local solve the
+ * body's place in the block's shared-memory cache (>= 0) or -(index + 1) for a body read from
+ * global memory. */
+struct VelSlot {
+    int4 idx;
+    float4 inv, nf, imp, r0, r1, m0, m1, k;
+};
+
+/* One constraint slot's position data (pc_* arrays), idx as in VelSlot */
+struct PosSlot {
+    int4 idx;
+    float4 lp, geo, lc, inv, meta;
+    int island;
+    int pad[3];
+};
+
+__device__ __forceinline__ VelSlot vel_slot(const DevWorld& w, int k) {
+    VelSlot s;
+    s.idx = w.vc_idx[k];
+    s.inv = w.vc_inv[k];
+    s.nf = w.vc_nf[k];
+    s.imp = w.vc_imp[k];
+    s.r0 = w.vc_r0[k];
+    s.r1 = w.vc_r1[k];
+    s.m0 = w.vc_m0[k];
+    s.m1 = w.vc_m1[k];
+    s.k = w.vc_k[k];
+    return s;
+}
+
+__device__ __forceinline__ PosSlot pos_slot(const DevWorld& w, int k) {
+    PosSlot s;
+    s.idx = w.vc_idx[k];
+    s.lp = w.pc_lp[k];
+    s.geo = w.pc_geo[k];
+    s.lc = w.pc_lc[k];
+    s.inv = w.pc_inv[k];
+    s.meta = w.pc_meta[k];
+    s.island = w.vc_island[k];
+    return s;
+}
+
+/* warm_start for one slot on the bodies' velocities (v, w, sleep time) va, vb */
+__device__ __forceinline__ void warm_math(const VelSlot& sl, float4& va, float4& vb) {
+    const int4 idx = sl.idx;
+    const float4 inv = sl.inv;
+    const float4 nf = sl.nf;
+    const float4 imp = sl.imp;
     V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
     float wA = va.z, wB = vb.z;
     const V2 normal = mk(nf.x, nf.y);
     const V2 tangent = cross_vs(normal, 1.0f);
-    const float4 r[2] = {w.vc_r0[k], w.vc_r1[k]};
+    const float4 r[2] = {sl.r0, sl.r1};
     const float ni[2] = {imp.x, imp.z}, ti[2] = {imp.y, imp.w};
     for (int j = 0; j < idx.z; ++j) {
         const V2 rA = mk(r[j].x, r[j].y), rB = mk(r[j].z, r[j].w);
@@ -456,19 +648,18 @@ __device__ __forceinline__ void warm_slot(const DevWorld& w, int k) {
         wB += inv.w * cross(rB, P);
         vB = add(vB, scale(inv.y, P));
     }
-    if (idx.w & 1) w.b_vel[idx.x] = make_float4(vA.x, vA.y, wA, va.w);
-    if (idx.w & 2) w.b_vel[idx.y] = make_float4(vB.x, vB.y, wB, vb.w);
+    va = make_float4(vA.x, vA.y, wA, va.w);
+    vb = make_float4(vB.x, vB.y, wB, vb.w);
 }
 
-__device__ __forceinline__ void solve_velocity_slot(const DevWorld& w, int k) {
-    const int4 idx = w.vc_idx[k];
-    const float4 inv = w.vc_inv[k];
-    const float4 nf = w.vc_nf[k];
-    float4 imp = w.vc_imp[k];
-    const float4 r0 = w.vc_r0[k], r1 = w.vc_r1[k];
-    const float4 m0 = w.vc_m0[k], m1 = w.vc_m1[k];
+/* solve_velocity_constraints for one slot: updates its impulses imp and the velocities va, vb */
+__device__ __forceinline__ void solve_velocity_math(const VelSlot& sl, float4& imp, float4& va, float4& vb) {
+    const int4 idx = sl.idx;
+    const float4 inv = sl.inv;
+    const float4 nf = sl.nf;
+    const float4 r0 = sl.r0, r1 = sl.r1;
+    const float4 m0 = sl.m0, m1 = sl.m1;
     const float mA = inv.x, mB = inv.y, iA = inv.z, iB = inv.w;
-    float4 va = w.b_vel[idx.x], vb = w.b_vel[idx.y];
     V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
     float wA = va.z, wB = vb.z;
     const V2 normal = mk(nf.x, nf.y);
@@ -518,7 +709,7 @@ __device__ __forceinline__ void solve_velocity_slot(const DevWorld& w, int k) {
         wB += iB * cross(rB0, P);
     } else {
         /* 2-point block LCP, b2_contact_solver_private.rs:380-575 */
-        const float4 K = w.vc_k[k];
+        const float4 K = sl.k;
         const float k11 = K.x, k12 = K.y, k22 = K.z;
         const float na = K.w, nbc = m0.w, nd = m1.w;
         const V2 a = mk(imp.x, imp.z);
@@ -565,15 +756,14 @@ __device__ __forceinline__ void solve_velocity_slot(const DevWorld& w, int k) {
             imp.z = x.y;
         }
     }
-    w.vc_imp[k] = imp;
-    if (idx.w & 1) w.b_vel[idx.x] = make_float4(vA.x, vA.y, wA, va.w);
-    if (idx.w & 2) w.b_vel[idx.y] = make_float4(vB.x, vB.y, wB, vb.w);
+    va = make_float4(vA.x, vA.y, wA, va.w);
+    vb = make_float4(vB.x, vB.y, wB, vb.w);
 }
 
-/* solve_position_constraints for one slot; returns this slot's min separation (<= 0) */
-__device__ __forceinline__ float solve_position_slot(const DevWorld& w, int k) {
-    const int4 idx = w.vc_idx[k];
-    const float4 lp = w.pc_lp[k], geo = w.pc_geo[k], lc = w.pc_lc[k], inv = w.pc_inv[k], meta = w.pc_meta[k];
+/* solve_position_constraints for one slot on the bodies' (c, a) pa, pb; returns this slot's min
+ * separation (<= 0) */
+__device__ __forceinline__ float solve_position_math(const PosSlot& sl, float4& pa, float4& pb) {
+    const float4 lp = sl.lp, geo = sl.geo, lc = sl.lc, inv = sl.inv, meta = sl.meta;
     const float mA = inv.x, mB = inv.y, iA = inv.z, iB = inv.w;
     const V2 lcA = mk(lc.x, lc.y), lcB = mk(lc.z, lc.w);
     const int mtype = __float_as_int(meta.z);
@@ -581,7 +771,6 @@ __device__ __forceinline__ float solve_position_slot(const DevWorld& w, int k) {
     const float rA = meta.x, rB = meta.y;
     const V2 ln = mk(geo.x, geo.y), lpt = mk(geo.z, geo.w);
     const V2 lps[2] = {mk(lp.x, lp.y), mk(lp.z, lp.w)};
-    float4 pa = w.b_pos[idx.x], pb = w.b_pos[idx.y];
     V2 cA = mk(pa.x, pa.y), cB = mk(pb.x, pb.y);
     float aA = pa.z, aB = pb.z;
     float minSep = 0.0f;
@@ -628,9 +817,150 @@ __device__ __forceinline__ float solve_position_slot(const DevWorld& w, int k) {
         cB = add(cB, scale(mB, P));
         aB += iB * cross(rb, P);
     }
-    if (idx.w & 1) w.b_pos[idx.x] = make_float4(cA.x, cA.y, aA, pa.w);
-    if (idx.w & 2) w.b_pos[idx.y] = make_float4(cB.x, cB.y, aB, pb.w);
+    pa = make_float4(cA.x, cA.y, aA, pa.w);
+    pb = make_float4(cB.x, cB.y, aB, pb.w);
     return minSep;
+}
+
+
+/* the slot routines on the global body arrays (slot order by colour) */
+__device__ __forceinline__ void warm_slot(const DevWorld& w, int k) {
+    const VelSlot sl = vel_slot(w, k);
+    float4 va = w.b_vel[sl.idx.x], vb = w.b_vel[sl.idx.y];
+    warm_math(sl, va, vb);
+    if (sl.idx.w & 1) w.b_vel[sl.idx.x] = va;
+    if (sl.idx.w & 2) w.b_vel[sl.idx.y] = vb;
+}
+
+__device__ __forceinline__ void solve_velocity_slot(const DevWorld& w, int k) {
+    const VelSlot sl = vel_slot(w, k);
+    float4 va = w.b_vel[sl.idx.x], vb = w.b_vel[sl.idx.y];
+    float4 imp = sl.imp;
+    solve_velocity_math(sl, imp, va, vb);
+    w.vc_imp[k] = imp;
+    if (sl.idx.w & 1) w.b_vel[sl.idx.x] = va;
+    if (sl.idx.w & 2) w.b_vel[sl.idx.y] = vb;
+}
+
+__device__ __forceinline__ float solve_position_slot(const DevWorld& w, int k) {
+    const PosSlot sl = pos_slot(w, k);
+    float4 pa = w.b_pos[sl.idx.x], pb = w.b_pos[sl.idx.y];
+    const float ms = solve_position_math(sl, pa, pb);
+    if (sl.idx.w & 1) w.b_pos[sl.idx.x] = pa;
+    if (sl.idx.w & 2) w.b_pos[sl.idx.y] = pb;
+    return ms;
+}
+
+/* ---------------- part-local solve ----------------
+ * Block p owns part p: a range of the constraint bodies in Morton-rank order (ranges of equal
+ * constraint work, set by the colouring). It caches their velocities (then positions) and its
+ * interior constraint slots in shared memory, sweeps its interior colours separated by
+ * __syncthreads, writes the bodies back, and the boundary colours follow grid-wide. A body or slot
+ * that does not fit the cache is read and written in global memory by the same block, which alone
+ * touches it in the interior phase. */
+struct PartCtx {
+    int cbeg;          /* the part's first entry of cache_body */
+    int nloc;          /* bodies cached (body[] entries) */
+    int ibeg;          /* first interior slot */
+    int ncol;          /* non-empty interior colours */
+    int cap_vel;       /* interior slots cached as VelSlot */
+    int cap_pos;       /* interior slots cached as PosSlot */
+    const int* off;    /* shared: offsets of the part's colours */
+    float4* state;     /* shared: cached velocities or positions */
+    int* body;         /* shared: the cached bodies */
+    void* slots;       /* shared: VelSlot[cap_vel] or PosSlot[cap_pos] */
+};
+
+__device__ __forceinline__ int body_code(const DevWorld& w, const PartCtx& pc, int b, bool dyn) {
+    if (dyn) {
+        const int l = w.b_cidx[b] - pc.cbeg;
+        if (l >= 0 && l < pc.nloc && pc.body[l] == b) return l;
+    }
+    return -(b + 1);
+}
+
+__device__ __forceinline__ float4 ld_body(const float4* st, const float4* glob, int code) {
+    return code >= 0 ? st[code] : glob[-code - 1];
+}
+
+__device__ __forceinline__ void st_body(float4* st, float4* glob, int code, float4 v) {
+    if (code >= 0) st[code] = v;
+    else glob[-code - 1] = v;
+}
+
+__device__ __forceinline__ VelSlot part_vel_slot(const DevWorld& w, const PartCtx& pc, int k) {
+    VelSlot sl = vel_slot(w, k);
+    sl.idx.x = body_code(w, pc, sl.idx.x, (sl.idx.w & 1) != 0);
+    sl.idx.y = body_code(w, pc, sl.idx.y, (sl.idx.w & 2) != 0);
+    return sl;
+}
+
+__device__ __forceinline__ PosSlot part_pos_slot(const DevWorld& w, const PartCtx& pc, int k) {
+    PosSlot sl = pos_slot(w, k);
+    sl.idx.x = body_code(w, pc, sl.idx.x, (sl.idx.w & 1) != 0);
+    sl.idx.y = body_code(w, pc, sl.idx.y, (sl.idx.w & 2) != 0);
+    return sl;
+}
+
+/* the part's interior colours (warm start or one velocity iteration) */
+__device__ void part_vel_sweeps(const DevWorld& w, const PartCtx& pc, bool warm) {
+    VelSlot* vs = (VelSlot*)pc.slots;
+    for (int c = 0; c < pc.ncol; ++c) {
+        const int beg = pc.off[c], end = pc.off[c + 1];
+        for (int k = beg + threadIdx.x; k < end; k += blockDim.x) {
+            const int j = k - pc.ibeg;
+            const bool cached = j < pc.cap_vel;
+            const VelSlot sl = cached ? vs[j] : part_vel_slot(w, pc, k);
+            float4 va = ld_body(pc.state, w.b_vel, sl.idx.x), vb = ld_body(pc.state, w.b_vel, sl.idx.y);
+            if (warm) {
+                warm_math(sl, va, vb);
+            } else {
+                float4 imp = sl.imp;
+                solve_velocity_math(sl, imp, va, vb);
+                if (cached) vs[j].imp = imp;
+                else w.vc_imp[k] = imp;
+            }
+            if (sl.idx.w & 1) st_body(pc.state, w.b_vel, sl.idx.x, va);
+            if (sl.idx.w & 2) st_body(pc.state, w.b_vel, sl.idx.y, vb);
+        }
+        __syncthreads();
+    }
+}
+
+/* the part's interior colours of position iteration `it` (per-island early exit as in k_solve) */
+__device__ void part_pos_sweeps(const DevWorld& w, const PartCtx& pc, int it, uint32_t* cur, float tol) {
+    const PosSlot* ps = (const PosSlot*)pc.slots;
+    for (int c = 0; c < pc.ncol; ++c) {
+        const int beg = pc.off[c], end = pc.off[c + 1];
+        for (int k = beg + threadIdx.x; k < end; k += blockDim.x) {
+            const int j = k - pc.ibeg;
+            const PosSlot sl = j < pc.cap_pos ? ps[j] : part_pos_slot(w, pc, k);
+            bool done = false;
+            for (int q = 0; q < it && !done; ++q)
+                done = __uint_as_float(w.isl_minsep[(size_t)q * w.body_cap + sl.island]) <= tol;
+            if (done) continue;
+            float4 pa = ld_body(pc.state, w.b_pos, sl.idx.x), pb = ld_body(pc.state, w.b_pos, sl.idx.y);
+            const float ms = solve_position_math(sl, pa, pb);
+            if (sl.idx.w & 1) st_body(pc.state, w.b_pos, sl.idx.x, pa);
+            if (sl.idx.w & 2) st_body(pc.state, w.b_pos, sl.idx.y, pb);
+            if (ms < 0.0f) atomicMax(&cur[sl.island], __float_as_uint(-ms));
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ void part_store(const PartCtx& pc, float4* glob) {
+    for (int l = threadIdx.x; l < pc.nloc; l += blockDim.x) {
+        const int b = pc.body[l];
+        if (b >= 0) glob[b] = pc.state[l];
+    }
+}
+
+__device__ __forceinline__ void part_load(const PartCtx& pc, const float4* glob) {
+    for (int l = threadIdx.x; l < pc.nloc; l += blockDim.x) {
+        const int b = pc.body[l];
+        if (b >= 0) pc.state[l] = glob[b];
+    }
 }
 
 /* B2dynamicTree::move_proxy, private/collision/b2_dynamic_tree.rs:109-168 (fat AABB rule only) */
@@ -704,20 +1034,88 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
     /* phase 1: constraint initialisation */
     for (int k = gtid; k < ncons; k += gsize) init_slot(w, sp, k);
     if (!grid_barrier(w)) return;
-    /* phase 2: warm start, colour by colour */
-    if (sp.warm) {
-        for (int c = 0; c < ncol; ++c) {
-            const int beg = w.col_off[c], end = w.col_off[c + 1];
-            for (int k = beg + gtid; k < end; k += gsize) warm_slot(w, k);
-            if (!grid_barrier(w)) return;
-        }
+    const int interior = w.cnt[CNT_INTERIOR];
+    const bool parts = interior > 0;
+    const int nparts = w.cnt[CNT_PARTS];
+    if (parts && (nparts <= 0 || nparts > (int)gridDim.x)) {  /* the same for every block: all return */
+        if (gtid == 0) atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_PART_MISMATCH);
+        return;
     }
-    /* phase 3: velocity iterations */
-    for (int it = 0; it < sp.vi; ++it) {
-        for (int c = 0; c < ncol; ++c) {
-            const int beg = w.col_off[c], end = w.col_off[c + 1];
-            for (int k = beg + gtid; k < end; k += gsize) solve_velocity_slot(w, k);
-            if (!grid_barrier(w)) return;
+    extern __shared__ float4 s_part[];
+    __shared__ int s_off[kMaxColours + 1];
+    PartCtx pc{};
+    if (parts) {
+        /* this block's part: its rank range, colour offsets and shared-memory caches (blocks
+         * past the part count own none and only join the boundary sweeps) */
+        const int p = blockIdx.x;
+        const bool owner = p < nparts;
+        pc.cbeg = owner ? w.part_cbeg[p] : 0;
+        pc.nloc = owner ? max(0, min(w.part_cend[p] - pc.cbeg, sp.part_bodies)) : 0;
+        pc.ncol = owner ? w.part_ncol[p] : 0;
+        for (int i = threadIdx.x; owner && i <= pc.ncol; i += blockDim.x)
+            s_off[i] = w.part_off[(size_t)p * (kMaxColours + 1) + i];
+        pc.off = s_off;
+        pc.state = s_part;
+        pc.body = (int*)(s_part + sp.part_bodies);
+        pc.slots = (void*)(s_part + sp.part_bodies + (sp.part_bodies + 3) / 4);
+        __syncthreads();
+        pc.ibeg = pc.ncol > 0 ? s_off[0] : 0;
+        const int nint = pc.ncol > 0 ? s_off[pc.ncol] - pc.ibeg : 0;
+        pc.cap_vel = min(nint, sp.part_slot_bytes / (int)sizeof(VelSlot));
+        pc.cap_pos = min(nint, sp.part_slot_bytes / (int)sizeof(PosSlot));
+        for (int l = threadIdx.x; l < pc.nloc; l += blockDim.x) {
+            const int b = w.cache_body[pc.cbeg + l];
+            pc.body[l] = b;
+            pc.state[l] = w.b_vel[b];
+        }
+        __syncthreads();
+        VelSlot* vs = (VelSlot*)pc.slots;
+        for (int j = threadIdx.x; j < pc.cap_vel; j += blockDim.x) vs[j] = part_vel_slot(w, pc, pc.ibeg + j);
+        __syncthreads();
+        /* phases 2 and 3: the warm start and each velocity iteration sweep the interior colours
+         * of every part, then the boundary colours grid-wide */
+        const int nsweeps = (sp.warm ? 1 : 0) + sp.vi;
+        for (int sw = 0; sw < nsweeps; ++sw) {
+            const bool warm = sp.warm && sw == 0;
+            const bool last = sw == nsweeps - 1;
+            part_vel_sweeps(w, pc, warm);
+            if (last)
+                for (int j = threadIdx.x; j < pc.cap_vel; j += blockDim.x) w.vc_imp[pc.ibeg + j] = vs[j].imp;
+            if (ncol > 0 || last) part_store(pc, w.b_vel);
+            if (ncol > 0) {
+                if (!grid_barrier(w)) return;
+                for (int c = 0; c < ncol; ++c) {
+                    const int beg = w.col_off[c], end = w.col_off[c + 1];
+                    for (int k = beg + gtid; k < end; k += gsize) {
+                        if (warm) warm_slot(w, k);
+                        else solve_velocity_slot(w, k);
+                    }
+                    if (!grid_barrier(w)) return;
+                }
+                if (!last) {
+                    part_load(pc, w.b_vel);
+                    __syncthreads();
+                }
+            } else if (last) {
+                if (!grid_barrier(w)) return;
+            }
+        }
+    } else {
+        /* phase 2: warm start, colour by colour */
+        if (sp.warm) {
+            for (int c = 0; c < ncol; ++c) {
+                const int beg = w.col_off[c], end = w.col_off[c + 1];
+                for (int k = beg + gtid; k < end; k += gsize) warm_slot(w, k);
+                if (!grid_barrier(w)) return;
+            }
+        }
+        /* phase 3: velocity iterations */
+        for (int it = 0; it < sp.vi; ++it) {
+            for (int c = 0; c < ncol; ++c) {
+                const int beg = w.col_off[c], end = w.col_off[c + 1];
+                for (int k = beg + gtid; k < end; k += gsize) solve_velocity_slot(w, k);
+                if (!grid_barrier(w)) return;
+            }
         }
     }
     /* phase 4: store impulses (:585-598) and integrate positions (:222-252) */
@@ -766,8 +1164,24 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
      * shows min separation >= -3 slop. Buffers of finished iterations are complete after the
      * colour barriers, so no extra barrier per iteration is needed. */
     const float tol = 3.0f * kLinearSlop;
+    if (parts && sp.pi > 0) {
+        for (int l = threadIdx.x; l < pc.nloc; l += blockDim.x) {
+            const int b = pc.body[l];
+            if (b >= 0) pc.state[l] = w.b_pos[b];
+        }
+        PosSlot* ps = (PosSlot*)pc.slots;
+        for (int j = threadIdx.x; j < pc.cap_pos; j += blockDim.x) ps[j] = part_pos_slot(w, pc, pc.ibeg + j);
+        __syncthreads();
+    }
     for (int it = 0; it < sp.pi; ++it) {
         uint32_t* cur = w.isl_minsep + (size_t)it * w.body_cap;
+        if (parts) {
+            /* the interior colours, then a barrier: islands span parts, and the next iteration's
+             * early exit reads this iteration's buffer */
+            part_pos_sweeps(w, pc, it, cur, tol);
+            part_store(pc, w.b_pos);
+            if (!grid_barrier(w)) return;
+        }
         for (int c = 0; c < ncol; ++c) {
             const int beg = w.col_off[c], end = w.col_off[c + 1];
             for (int k = beg + gtid; k < end; k += gsize) {
@@ -780,6 +1194,10 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
                 if (ms < 0.0f) atomicMax(&cur[isl], __float_as_uint(-ms));
             }
             if (!grid_barrier(w)) return;
+        }
+        if (parts && it < sp.pi - 1) {
+            part_load(pc, w.b_pos);
+            __syncthreads();
         }
     }
     /* phase 6a: copy back (synchronize_transform), sleep bookkeeping, clear forces */
@@ -904,23 +1322,63 @@ void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cud
     if (sp.allow_sleep) k_sleep_init<<<gb, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
 }
 
-void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms) {
+/* Parts of the part-local solve: about one per 256 proxies, at most one per SM, whatever the
+ * blocks per SM (so results do not depend on the launch configuration). A small world is one
+ * part, solved by one block without grid barriers between its colours. */
+int part_count(const DevWorld& w, int num_sms) {
+    return std::max(1, std::min(std::min(num_sms, kMaxParts), w.n_fixtures / 256));
+}
+
+/* The part-local solve pays off while a part's bodies and constraints fit its block's shared
+ * memory; a large batch of worlds (thousands of proxies per SM) keeps the grid-wide colour sweeps,
+ * which spread each colour over every thread of the GPU. */
+constexpr int kPartMaxProxiesPerSm = 2048;
+
+bool use_parts(const DevWorld& w, int num_sms, bool allowed) {
+    return allowed && w.n_fixtures > 0 && (long long)w.n_fixtures <= (long long)num_sms * kPartMaxProxiesPerSm;
+}
+
+void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms, bool parts) {
     const int blocks = coop_blocks((const void*)k_colour, num_sms) * w.cfg_coop_per_sm;
     DevWorld wc = w;
-    void* args[] = {&wc};
+    int nparts = use_parts(w, num_sms, parts) ? part_count(w, num_sms) : 0;
+    void* args[] = {&wc, &nparts};
     cudaMemsetAsync(w.cnt + CNT_BARRIER, 0, sizeof(int), s);
     cudaLaunchCooperativeKernel((const void*)k_colour, dim3(blocks), dim3(kBlock), args, 0, s);
     B2G_LAUNCHED(1);
 }
 
-int launch_solver(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms) {
+/* Shared memory of the part-local solve per block: most of an SM's with one block per SM, half
+ * of it with two; none with more (the part-local sweeps then work in global memory). There is
+ * one part per SM. */
+constexpr int kPartSmemOne = 200 * 1024;
+constexpr int kPartSmemTwo = 96 * 1024;
+
+int launch_solver(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms, bool parts) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute((const void*)k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, kPartSmemOne);
+        attr_set = true;
+    }
     const int blocks = coop_blocks((const void*)k_solve, num_sms) * w.cfg_coop_per_sm;
     DevWorld wc = w;
     StepParams spc = sp;
+    size_t smem = 0;
+    spc.part_bodies = 0;
+    spc.part_slot_bytes = 0;
+    if (use_parts(w, num_sms, parts)) {
+        const int budget = w.cfg_coop_per_sm == 1 ? kPartSmemOne : (w.cfg_coop_per_sm == 2 ? kPartSmemTwo : 0);
+        /* a part holds at most ceil(n_fixtures / blocks) ranks; bodies take at most half */
+        const int nb = (budget / 4 / 20) & ~3;  /* a quarter of it for bodies */
+        const int body_bytes = (nb + nb / 4) * 16;
+        spc.part_bodies = nb;
+        spc.part_slot_bytes = std::max(0, budget - body_bytes);
+        smem = (size_t)(budget > 0 ? body_bytes + spc.part_slot_bytes : 0);
+    }
     void* args[] = {&wc, &spc};
     B2G_LAUNCHED(1);
     cudaMemsetAsync(w.cnt + CNT_BARRIER, 0, sizeof(int), s);
-    return (int)cudaLaunchCooperativeKernel((const void*)k_solve, dim3(blocks), dim3(kBlock), args, 0, s);
+    return (int)cudaLaunchCooperativeKernel((const void*)k_solve, dim3(blocks), dim3(kBlock), args, smem, s);
 }
 
 void launch_set_transform(const DevWorld& w, int body, float px, float py, float angle, cudaStream_t s) {

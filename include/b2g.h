@@ -194,6 +194,13 @@ int b2g_set_warm_starting(void* world, int32_t flag);
 int b2g_set_continuous_physics(void* world, int32_t flag);
 int b2g_set_auto_clear_forces(void* world, int32_t flag);
 int b2g_clear_forces(void* world);
+/* Part-local solve (default on; not in the reference: a solver schedule). Each solver block owns a
+ * part of the constraint bodies (equal-work ranges in Morton order) and solves the constraints
+ * inside it from shared memory; the constraints between parts follow in grid-wide colours. It
+ * applies to worlds of up to 2048 proxies per SM. The solve order, and so the bits of the
+ * results, then depend on the GPU's SM count; with the flag off every constraint is solved in
+ * grid-wide colours, whose order does not. Both orders are exported by b2g_get_solver_order. */
+int b2g_set_part_solve(void* world, int32_t flag);
 
 /* ---- introspection ---- */
 int b2g_get_profile(void* world, b2g_profile* out);       /* B2world::get_profile, src/b2_world.rs:268-270 */
@@ -303,7 +310,10 @@ int b2g_tape_info_get(void* world, b2g_tape_info* out);
  * angle = dL/d(angle) with the origin held, world_center = dL/d(centre of mass) with the angle
  * held. Either pointer covers all bodies. */
 int b2g_backward(void* world, const b2g_body_state* d_final, b2g_body_state* d_initial);
-/* Copy one taped step out: its parameters, colour offsets (num_colours + 1 ints) and slots. */
+/* Copy one taped step out: its parameters, colour offsets (num_colours + 1 ints) and slots. The
+ * offsets list the step's solve order as groups of independent slots, in order: with the
+ * part-local solve, every part's interior colours, then the boundary colours. Call it first with
+ * out_colour_offsets = NULL to learn num_colours. */
 int b2g_tape_get_step(void* world, int32_t step, b2g_tape_step* out_step, int32_t* out_colour_offsets,
                       b2g_tape_slot* out_slots, int32_t slot_capacity);
 /* Body solver state (centre x, y, angle, -, vx, vy, w, - per body) of checkpoint `index`

@@ -49,7 +49,8 @@ def _p(a):
 def export_tape(world, body_defs):
     """The tape of `world` (a b2g.B2world after tape_end) as plain arrays: body_static (n, 10)
     float32 (mass, 1/mass, inertia, 1/inertia, linear and angular damping, gravity scale, local
-    centre x, y, type), steps (b2g.TAPE_STEP), cols (steps, 257) int32, slots (b2g.TAPE_SLOT).
+    centre x, y, type), steps (b2g.TAPE_STEP), cols int32 (each step's num_colours + 1 colour-group
+    offsets, concatenated), slots (b2g.TAPE_SLOT).
     body_defs: the b2g.BODY_DEF array the bodies were created from."""
     import b2g
 
@@ -63,21 +64,36 @@ def export_tape(world, body_defs):
     bs[:, 7:9] = mass[:, 4:6]
     bs[:, 9] = body_defs["type"]
     steps = np.zeros(T, b2g.TAPE_STEP)
-    cols = np.zeros((T, 257), np.int32)
+    cols = []
     slots = []
     for t in range(T):
         st, col, sl = world.tape_step(t)
         steps[t] = st
-        cols[t, : len(col)] = col
+        cols.append(np.asarray(col, np.int32))
         slots.append(sl)
     slots = np.concatenate(slots) if slots else np.zeros(0, b2g.TAPE_SLOT)
+    cols = np.concatenate(cols) if cols else np.zeros(0, np.int32)
     return {"body_static": bs, "steps": steps, "cols": cols, "slots": slots}
+
+
+def flat_cols(steps, cols):
+    """Colour-group offsets as one concatenated int32 array; a (steps, 257) array (one row per
+    step, num_colours + 1 used) is flattened."""
+    cols = np.asarray(cols, np.int32)
+    if cols.ndim == 1:
+        return cols
+    nc = np.asarray(steps["num_colours"], np.int64)
+    return np.concatenate([cols[t, : nc[t] + 1] for t in range(len(nc))]) if len(nc) else np.zeros(0, np.int32)
 
 
 class AdjointRef:
     def __init__(self, body_static, steps, cols, slots):
         """Build the reference from an exported tape (see export_tape)."""
         self._lib = load()
+        cols = flat_cols(steps, cols)
+        nc = np.asarray(steps["num_colours"], np.int64)
+        if len(cols) != int((nc + 1).sum()):
+            raise ValueError("cols must hold num_colours + 1 offsets per step")
         self._keep = tuple(np.ascontiguousarray(a) for a in (body_static, steps, cols, slots))
         bs, steps, cols, slots = self._keep
         self.n = len(bs)

@@ -267,6 +267,7 @@ void forward(Ref& R, bool frozen, std::vector<Body<T>>& st, Trace<T>* tr) {
 
 extern "C" {
 
+/* col: each step's colour-group offsets (its ncol + 1 ints), concatenated in step order */
 void* ora_adj_create(int32_t nb, const float* body_static, int32_t T, const void* steps, const int32_t* col,
                      const void* slots) {
     Ref* R = new Ref;
@@ -292,10 +293,11 @@ void* ora_adj_create(int32_t nb, const float* body_static, int32_t T, const void
     R->col.resize(T);
     R->slots.resize(T);
     const HSlot* sp = (const HSlot*)slots;
-    size_t off = 0;
+    size_t off = 0, coff = 0;
     for (int t = 0; t < T; ++t) {
         const int nc = R->steps[t].ncol;
-        R->col[t].assign(col + (size_t)t * 257, col + (size_t)t * 257 + nc + 1);
+        R->col[t].assign(col + coff, col + coff + nc + 1);
+        coff += (size_t)nc + 1;
         R->slots[t].assign(sp + off, sp + off + R->steps[t].nslots);
         off += R->steps[t].nslots;
     }

@@ -109,6 +109,7 @@ def make_pair(scene, record_pairs=True, record_events=False, warm_starting=True)
     gpu.set_continuous_physics(False)
     gpu.set_record_pairs(record_pairs)
     gpu.set_contact_events(record_events)
+    gpu.set_part_solve(scene.get("part_solve", True))
     kw = dict(allow_sleep=scene.get("allow_sleep", False), warm_starting=warm_starting, record_events=record_events)
     scenes.build_world(gpu, scene)
     if scene.get("num_worlds", 1) > 1:

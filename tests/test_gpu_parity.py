@@ -122,6 +122,27 @@ def test_mixed_dense_lockstep(built):
     assert max(r["constraints"] for r in recs) > 500
 
 
+def test_many_parts_lockstep(built):
+    """40 000 bodies: the part-local solve splits the constraint bodies into one part per SM, and
+    constraints between parts run in the grid-wide boundary colours; the oracle solved in the
+    exported order must agree bit for bit."""
+    s = scenes.mixed(n_circles=20000, n_polygons=20000, size=200.0, seed=21)
+    recs, _, _ = parity.lockstep(s, 12)
+    for r in recs:
+        _assert_step(r)
+    assert max(r["constraints"] for r in recs) > 5000
+
+
+def test_grid_colour_schedule_lockstep(built):
+    """With the part-local solve off every constraint is solved in grid-wide colours."""
+    s = scenes.mixed(n_circles=1500, n_polygons=1500, size=40.0, seed=13)
+    s["part_solve"] = False
+    recs, _, _ = parity.lockstep(s, 40)
+    for r in recs:
+        _assert_step(r)
+    assert max(r["constraints"] for r in recs) > 500
+
+
 def test_batched_worlds_lockstep(built):
     """Several independent worlds in one batch: never any cross-world pair."""
     s = scenes.batched(num_worlds=6, lo=16, hi=200, seed=5)
