@@ -185,10 +185,10 @@ assert TAPE_SLOT.itemsize == 144 and TAPE_STEP.itemsize == 48
 
 class LaunchConfig(ctypes.Structure):
     _fields_ = [("coop_blocks_per_sm", ctypes.c_int32), ("collide_block", ctypes.c_int32),
-                ("traverse_block", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("traverse_block", ctypes.c_int32), ("tuning_steps", ctypes.c_int32)]
 
     def as_dict(self):
-        return {n: int(getattr(self, n)) for n, _ in self._fields_ if n != "pad"}
+        return {n: int(getattr(self, n)) for n, _ in self._fields_ if n != "tuning_steps"}
 
 
 class TapeInfo(ctypes.Structure):
@@ -680,7 +680,11 @@ class B2world:
                                            steps_per_candidate, ctypes.byref(c)))
         return c.as_dict()
 
-    AUTOTUNE_CANDIDATES = 2 + 3 + 3  # one untimed + steps_per_candidate timed steps each
+    def tuning_steps(self):
+        """Steps the last autotune() ran on this world."""
+        c = LaunchConfig()
+        self._check(self._lib.b2g_get_launch_config(self._h, ctypes.byref(c)))
+        return int(c.tuning_steps)
 
     # ---- differentiable step ----
     def tape_begin(self, max_steps, checkpoint_interval=16, max_slots=0):

@@ -122,6 +122,7 @@ struct World {
     /* CUDA graphs of the steady-state step, one per contact-buffer parity */
     bool use_graphs = true;
     bool part_solve = true;       /* b2g_set_part_solve */
+    int tuning_steps = 0;         /* steps of the last b2g_autotune */
     GraphSlot graphs[2];
     int swaps = 0;
     int alloc_generation = 0;
@@ -532,7 +533,7 @@ int allocate(World* w, int nb, int nf) {
     A(d.col_off, kMaxColours + 1); A(d.col_hist, (size_t)(kMaxParts + 1) * kMaxColours);
     A(d.part_off, (size_t)kMaxParts * (kMaxColours + 1)); A(d.part_ncol, kMaxParts); A(d.part_tot, kMaxParts + 1);
     A(d.rank_x, fix_cap); A(d.blk_tot, kMaxParts); A(d.cache_body, fix_cap);
-    A(d.part_cbeg, kMaxParts); A(d.part_cend, kMaxParts);
+    A(d.part_cbeg, kMaxParts); A(d.part_cend, kMaxParts); A(d.part_rbeg, kMaxParts);
     A(d.vc_idx, contact_cap); A(d.vc_inv, contact_cap); A(d.vc_nf, contact_cap); A(d.vc_r0, contact_cap);
     A(d.vc_r1, contact_cap); A(d.vc_m0, contact_cap); A(d.vc_m1, contact_cap); A(d.vc_imp, contact_cap);
     A(d.vc_k, contact_cap); A(d.vc_island, contact_cap);
@@ -1812,7 +1813,7 @@ int b2g_get_launch_config(void* p, b2g_launch_config* out) {
     out->coop_blocks_per_sm = w->cfg.coop_per_sm;
     out->collide_block = w->cfg.collide_block;
     out->traverse_block = w->cfg.traverse_block;
-    out->pad = 0;
+    out->tuning_steps = w->tuning_steps;
     return B2G_OK;
 }
 
@@ -1856,8 +1857,10 @@ int timed_steps(World* w, float dt, int vi, int pi, int steps, double* ms) {
 extern "C" {
 
 /* Coordinate search over the launch configuration on the world's own next steps: for each knob in
- * turn (persistent-kernel blocks per SM, narrowphase block, traversal block) every candidate runs
- * one untimed step (graph capture) and `steps_per_candidate` timed steps; the fastest is kept.
+ * turn (persistent-kernel blocks per SM, narrowphase block, traversal block) the candidates take
+ * turns over up to four rounds, each turn one untimed step (graph capture) and its share of
+ * `steps_per_candidate` timed steps; the fastest in total is kept. With the part-local solve the
+ * persistent kernels keep one block per SM.
  * The steps are real steps of the world (the configuration never changes results). The choice is
  * applied to the world and remembered for later worlds of the same size bucket in this process. */
 int b2g_autotune(void* p, float dt, int32_t vi, int32_t pi, int32_t steps_per_candidate, b2g_launch_config* out) {
@@ -1868,29 +1871,43 @@ int b2g_autotune(void* p, float dt, int32_t vi, int32_t pi, int32_t steps_per_ca
     LaunchCfg best = w->cfg;
     w->cfg_set = true;
     const int coop[] = {1, 2}, collide[] = {64, 128, 256}, traverse[] = {64, 128, 256};
+    /* the part-local solve caches a part in its block's shared memory: one block per SM */
+    const int ncoop = use_parts(w->d, w->num_sms, w->part_solve) ? 1 : 2;
+    /* the world keeps evolving while candidates are timed, so the candidates take turns over
+     * several rounds (a step each) instead of running one after another */
+    const int rounds = std::max(1, std::min(steps_per_candidate, 4));
+    const int per_round = std::max(1, steps_per_candidate / rounds);
+    int tuned = 0;
     for (int knob = 0; knob < 3; ++knob) {
         const int* cand = knob == 0 ? coop : knob == 1 ? collide : traverse;
-        const int nc = knob == 0 ? 2 : 3;
-        double best_ms = 1e300;
-        int best_v = 0;
-        for (int i = 0; i < nc; ++i) {
-            LaunchCfg c = best;
-            (knob == 0 ? c.coop_per_sm : knob == 1 ? c.collide_block : c.traverse_block) = cand[i];
-            w->cfg = c;
-            apply_launch_config(w);
-            drop_graphs(w);
-            double ms = 0.0;
-            int rc = timed_steps(w, dt, vi, pi, 1, &ms);
-            if (rc == B2G_OK) rc = timed_steps(w, dt, vi, pi, steps_per_candidate, &ms);
-            if (rc != B2G_OK) return rc;
-            if (ms < best_ms) {
-                best_ms = ms;
-                best_v = cand[i];
+        const int nc = knob == 0 ? ncoop : 3;
+        if (nc == 1) {
+            (knob == 0 ? best.coop_per_sm : knob == 1 ? best.collide_block : best.traverse_block) = cand[0];
+            continue;
+        }
+        double total[3] = {0.0, 0.0, 0.0};
+        for (int r = 0; r < rounds; ++r) {
+            for (int i = 0; i < nc; ++i) {
+                LaunchCfg c = best;
+                (knob == 0 ? c.coop_per_sm : knob == 1 ? c.collide_block : c.traverse_block) = cand[i];
+                w->cfg = c;
+                apply_launch_config(w);
+                drop_graphs(w);
+                double ms = 0.0;
+                int rc = timed_steps(w, dt, vi, pi, 1, &ms);  /* graph capture, untimed */
+                if (rc == B2G_OK) rc = timed_steps(w, dt, vi, pi, per_round, &ms);
+                tuned += 1 + per_round;
+                if (rc != B2G_OK) return rc;
+                total[i] += ms;
             }
         }
-        (knob == 0 ? best.coop_per_sm : knob == 1 ? best.collide_block : best.traverse_block) = best_v;
+        int best_i = 0;
+        for (int i = 1; i < nc; ++i)
+            if (total[i] < total[best_i]) best_i = i;
+        (knob == 0 ? best.coop_per_sm : knob == 1 ? best.collide_block : best.traverse_block) = cand[best_i];
     }
     w->cfg = best;
+    w->tuning_steps = tuned;
     apply_launch_config(w);
     drop_graphs(w);
     {

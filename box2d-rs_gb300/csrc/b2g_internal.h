@@ -78,7 +78,10 @@ enum {
     CNT_COLOURINGS = 19,  /* colourings done so far: the stamp of colours kept in contacts (mids.w) */
     CNT_DYN_EXTENT = 20,  /* largest half-extent of a dynamic body's fat AABB (float bits), this pass */
     CNT_INTERIOR = 21,    /* constraint slots solved part-locally this step (slots [0, n)) */
-    CNT_PARTS = 22,       /* parts of this step's colouring (= blocks of the solver), 0 if off */
+    CNT_PARTS = 22,       /* parts of this step's colouring (at most the solver's blocks), 0 if off */
+    CNT_PART_NCACHE = 23, /* constraint bodies of the current partition (entries of cache_body) */
+    CNT_PART_P = 24,      /* parts of the current partition (0: none) */
+    CNT_PART_NF = 25,     /* proxies when the current partition was made */
     CNT_SIZE = 32
 };
 
@@ -180,6 +183,8 @@ struct DevWorld {
     int* cache_body;             /* constraint bodies in rank order */
     int* part_cbeg;              /* kMaxParts: each part's first entry of cache_body */
     int* part_cend;              /* kMaxParts: one past its last */
+    int* part_rbeg;              /* kMaxParts: each part's first Morton rank when the partition was
+                                    made (ascending); places bodies outside it by their rank */
     int4* vc_idx;                /* ia, ib, point count, flags (bit0 A dynamic, bit1 B dynamic) */
     float4 *vc_inv, *vc_nf, *vc_r0, *vc_r1, *vc_m0, *vc_m1, *vc_imp, *vc_k;
     float4 *pc_lp, *pc_geo, *pc_lc, *pc_inv, *pc_meta;
@@ -215,6 +220,8 @@ void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cud
 /* parts: allow the part-local solve (used where the world's size suits it) */
 void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms, bool parts);
 int launch_solver(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms, bool parts);
+/* whether the part-local solve applies to this world (parts allowed and the world's size suits it) */
+bool use_parts(const DevWorld& w, int num_sms, bool allowed);
 /* after_tree (optional) is called between the tree pass (keys, sort, build, refit, traverse)
  * and the contact merge, so the caller can record a profiling event there */
 void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms,

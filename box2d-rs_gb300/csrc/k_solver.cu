@@ -231,7 +231,13 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
     /* every 16th colouring starts afresh, so kept colours do not stay fragmented after the
      * contact graph has changed (a fresh colouring of a settled stack needs fewer colours) */
     const bool keep = stamp != 0u && (stamp & 15u) != 0u;
-    if (P > 0) {
+    /* the partition is made afresh every 4th colouring (and when the part or proxy count changed)
+     * and kept in between: a body stays in its part, and a body outside the partition goes to the
+     * part whose rank range its Morton rank falls in. (Kept colours stay proper across a new
+     * partition: interior constraints that share a body are always in the same part.) */
+    const bool rebalance = P > 0 && ((stamp & 3u) == 0u || w.cnt[CNT_PART_P] != P || w.cnt[CNT_PART_NF] != nf);
+    int ncache = w.cnt[CNT_PART_NCACHE];  /* read before any barrier; a rebalance rewrites it below */
+    if (rebalance) {
         /* Parts of equal work: weigh each Morton rank by the constraint endpoints of its body and
          * cut the weight prefix into P equal ranges. rank_x was zeroed by the broadphase. */
         for (int k = gtid; k < n; k += gsize) {
@@ -242,6 +248,7 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
         for (int q = gtid; q < P; q += gsize) {
             w.part_cbeg[q] = 0;
             w.part_cend[q] = 0;
+            w.part_rbeg[q] = INT_MAX;
         }
         if (!grid_barrier(w)) return;
         /* each block scans its chunk of ranks: (weight << 32 | has weight), exclusive */
@@ -285,23 +292,51 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
         }
         if (!grid_barrier(w)) return;
         /* each part's range of constraint bodies */
-        const int ncache = min(nf, (int)(uint32_t)all);
+        ncache = min(nf, (int)(uint32_t)all);
         for (int c = gtid; c < ncache; c += gsize) {
             const int part = w.b_part[w.cache_body[c]];
-            if (c == 0 || w.b_part[w.cache_body[c - 1]] != part) w.part_cbeg[part] = c;
+            if (c == 0 || w.b_part[w.cache_body[c - 1]] != part) {
+                w.part_cbeg[part] = c;
+                if (part > 0) w.part_rbeg[part] = w.b_rank[w.cache_body[c]];
+            }
             if (c == ncache - 1 || w.b_part[w.cache_body[c + 1]] != part) w.part_cend[part] = c + 1;
         }
+        if (gtid == 0) {
+            w.cnt[CNT_PART_NCACHE] = ncache;
+            w.cnt[CNT_PART_NF] = nf;
+            w.cnt[CNT_PART_P] = P;
+        }
     }
+    if (gtid == 0 && P == 0) w.cnt[CNT_PART_P] = 0;
+    /* a body's part: its own if the partition holds it, else the part whose rank range its
+     * current Morton rank falls in (the block of that part then reads it in global memory) */
+    auto part_of = [&](int b) {
+        const int c = w.b_cidx[b];
+        if (c >= 0 && c < ncache && w.cache_body[c] == b) return w.b_part[b];
+        const int r = w.b_rank[b];
+        if (r >= nf) return -2;
+        int lo = 0, hi = P - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (w.part_rbeg[mid] <= r) lo = mid;
+            else hi = mid - 1;
+        }
+        return lo;
+    };
     for (int k = gtid; k < n; k += gsize) {
         const int ci = w.cons_contact[k];
         int part = -1;
         if (P > 0) {
             const int2 bd = w.c.body[ci];
             const bool da = is_dynamic(w.b_flags[bd.x]), db = is_dynamic(w.b_flags[bd.y]);
-            const int pa = !da ? -1 : (w.b_rank[bd.x] < nf ? w.b_part[bd.x] : -2);
-            const int pb = !db ? -1 : (w.b_rank[bd.y] < nf ? w.b_part[bd.y] : -2);
-            part = !da ? pb : (!db ? pa : (pa == pb ? pa : -1));
-            if (part < 0) part = -1;
+            if (P == 1) {
+                part = 0;  /* one part holds everything; bodies outside its cache stay in global memory */
+            } else {
+                const int pa = !da ? -1 : part_of(bd.x);
+                const int pb = !db ? -1 : part_of(bd.y);
+                part = !da ? pb : (!db ? pa : (pa == pb ? pa : -1));
+                if (part < 0) part = -1;
+            }
         }
         w.cons_part[k] = part;
         const uint32_t cls = part < 0 ? 1u : 0u;
@@ -423,6 +458,15 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
                 w.cnt[CNT_COLOURS] = ndense;
                 w.cnt[CNT_INTERIOR] = base;
                 w.cnt[CNT_PARTS] = P;
+                if (rebalance) {
+                    /* rank starts ascending: part 0 from rank 0, an empty part as wide as nothing */
+                    int next = nf;
+                    for (int q = P - 1; q > 0; --q) {
+                        if (w.part_rbeg[q] == INT_MAX) w.part_rbeg[q] = next;
+                        else next = w.part_rbeg[q];
+                    }
+                    w.part_rbeg[0] = 0;
+                }
             }
         }
     }
@@ -599,7 +643,7 @@ struct PosSlot {
     int4 idx;
     float4 lp, geo, lc, inv, meta;
     int island;
-    int pad[3];
+    int pad[3];        /* pad[0]: cached early-exit flag of the island (part-local solve) */
 };
 
 __device__ __forceinline__ VelSlot vel_slot(const DevWorld& w, int k) {
@@ -625,6 +669,7 @@ __device__ __forceinline__ PosSlot pos_slot(const DevWorld& w, int k) {
     s.inv = w.pc_inv[k];
     s.meta = w.pc_meta[k];
     s.island = w.vc_island[k];
+    s.pad[0] = s.pad[1] = s.pad[2] = 0;  /* pad[0]: the island's early-exit flag (part-local solve) */
     return s;
 }
 
@@ -869,7 +914,80 @@ struct PartCtx {
     float4* state;     /* shared: cached velocities or positions */
     int* body;         /* shared: the cached bodies */
     void* slots;       /* shared: VelSlot[cap_vel] or PosSlot[cap_pos] */
+    void* bslots;      /* shared: this block's boundary slots, VelSlot or PosSlot[kBndSlots] */
+    const int* bco;    /* shared: boundary colour offsets */
+    const int* boff;   /* shared: per boundary colour, this block's first entry of bslots */
 };
+
+/* Boundary slots cached per block: each boundary colour is split evenly over the blocks, and a
+ * block keeps its share of every colour (with global body indices) in shared memory. */
+constexpr int kBndSlots = 128;
+constexpr int kBndBytes = kBndSlots * (int)sizeof(VelSlot);
+
+__device__ __forceinline__ void bnd_range(const PartCtx& pc, int c, int* lo, int* hi) {
+    const int len = pc.bco[c + 1] - pc.bco[c];
+    *lo = (int)((long long)len * blockIdx.x / gridDim.x);
+    *hi = (int)((long long)len * (blockIdx.x + 1) / gridDim.x);
+}
+
+/* whether an island stopped before position iteration `it` (some earlier iteration ended with
+ * min separation >= -3 slop) */
+__device__ __forceinline__ bool island_done(const DevWorld& w, int isl, int it, float tol) {
+    bool done = false;
+    for (int q = 0; q < it && !done; ++q) done = __uint_as_float(w.isl_minsep[(size_t)q * w.body_cap + isl]) <= tol;
+    return done;
+}
+
+/* one boundary colour of the warm start or a velocity iteration, this block's share; `last`: the
+ * final velocity sweep, whose impulses go to global memory for store_impulses */
+__device__ void bnd_vel_sweep(const DevWorld& w, const PartCtx& pc, int c, bool warm, bool last) {
+    int lo, hi;
+    bnd_range(pc, c, &lo, &hi);
+    VelSlot* bs = (VelSlot*)pc.bslots;
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const int k = pc.bco[c] + i, j = pc.boff[c] + i - lo;
+        const bool cached = j < kBndSlots;
+        const VelSlot sl = cached ? bs[j] : vel_slot(w, k);
+        float4 va = w.b_vel[sl.idx.x], vb = w.b_vel[sl.idx.y];
+        if (warm) {
+            warm_math(sl, va, vb);
+        } else {
+            float4 imp = sl.imp;
+            solve_velocity_math(sl, imp, va, vb);
+            if (cached && !last) bs[j].imp = imp;
+            else w.vc_imp[k] = imp;
+        }
+        if (sl.idx.w & 1) w.b_vel[sl.idx.x] = va;
+        if (sl.idx.w & 2) w.b_vel[sl.idx.y] = vb;
+    }
+}
+
+/* one boundary colour of position iteration `it`, this block's share (cached slots carry their
+ * island's early-exit flag in pad[0]) */
+__device__ void bnd_pos_sweep(const DevWorld& w, const PartCtx& pc, int c, int it, uint32_t* cur, float tol) {
+    int lo, hi;
+    bnd_range(pc, c, &lo, &hi);
+    const PosSlot* bs = (const PosSlot*)pc.bslots;
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const int k = pc.bco[c] + i, j = pc.boff[c] + i - lo;
+        const bool cached = j < kBndSlots;
+        const PosSlot sl = cached ? bs[j] : pos_slot(w, k);
+        if (cached ? sl.pad[0] != 0 : island_done(w, sl.island, it, tol)) continue;
+        float4 pa = w.b_pos[sl.idx.x], pb = w.b_pos[sl.idx.y];
+        const float ms = solve_position_math(sl, pa, pb);
+        if (sl.idx.w & 1) w.b_pos[sl.idx.x] = pa;
+        if (sl.idx.w & 2) w.b_pos[sl.idx.y] = pb;
+        if (ms < 0.0f) atomicMax(&cur[sl.island], __float_as_uint(-ms));
+    }
+}
+
+/* early-exit flags of the block's cached interior and boundary position slots for iteration `it` */
+__device__ void part_done_flags(const DevWorld& w, const PartCtx& pc, int nbnd, int it, float tol) {
+    PosSlot* ps = (PosSlot*)pc.slots;
+    PosSlot* bs = (PosSlot*)pc.bslots;
+    for (int j = threadIdx.x; j < pc.cap_pos; j += blockDim.x) ps[j].pad[0] = island_done(w, ps[j].island, it, tol) ? 1 : 0;
+    for (int j = threadIdx.x; j < nbnd; j += blockDim.x) bs[j].pad[0] = island_done(w, bs[j].island, it, tol) ? 1 : 0;
+}
 
 __device__ __forceinline__ int body_code(const DevWorld& w, const PartCtx& pc, int b, bool dyn) {
     if (dyn) {
@@ -934,11 +1052,9 @@ __device__ void part_pos_sweeps(const DevWorld& w, const PartCtx& pc, int it, ui
         const int beg = pc.off[c], end = pc.off[c + 1];
         for (int k = beg + threadIdx.x; k < end; k += blockDim.x) {
             const int j = k - pc.ibeg;
-            const PosSlot sl = j < pc.cap_pos ? ps[j] : part_pos_slot(w, pc, k);
-            bool done = false;
-            for (int q = 0; q < it && !done; ++q)
-                done = __uint_as_float(w.isl_minsep[(size_t)q * w.body_cap + sl.island]) <= tol;
-            if (done) continue;
+            const bool cached = j < pc.cap_pos;
+            const PosSlot sl = cached ? ps[j] : part_pos_slot(w, pc, k);
+            if (cached ? sl.pad[0] != 0 : island_done(w, sl.island, it, tol)) continue;
             float4 pa = ld_body(pc.state, w.b_pos, sl.idx.x), pb = ld_body(pc.state, w.b_pos, sl.idx.y);
             const float ms = solve_position_math(sl, pa, pb);
             if (sl.idx.w & 1) st_body(pc.state, w.b_pos, sl.idx.x, pa);
@@ -1043,6 +1159,8 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
     }
     extern __shared__ float4 s_part[];
     __shared__ int s_off[kMaxColours + 1];
+    __shared__ int s_bco[kMaxColours + 1];
+    __shared__ int s_boff[kMaxColours + 1];
     PartCtx pc{};
     if (parts) {
         /* this block's part: its rank range, colour offsets and shared-memory caches (blocks
@@ -1057,12 +1175,27 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
         pc.off = s_off;
         pc.state = s_part;
         pc.body = (int*)(s_part + sp.part_bodies);
-        pc.slots = (void*)(s_part + sp.part_bodies + (sp.part_bodies + 3) / 4);
+        pc.bslots = (void*)(s_part + sp.part_bodies + (sp.part_bodies + 3) / 4);
+        pc.slots = (void*)((char*)pc.bslots + kBndBytes);
+        pc.bco = s_bco;
+        pc.boff = s_boff;
+        for (int i = threadIdx.x; i <= ncol; i += blockDim.x) s_bco[i] = w.col_off[i];
         __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int c = 0; c < ncol; ++c) {
+                int lo, hi;
+                bnd_range(pc, c, &lo, &hi);
+                s_boff[c] = acc;
+                acc += hi - lo;
+            }
+            s_boff[ncol] = acc;
+        }
         pc.ibeg = pc.ncol > 0 ? s_off[0] : 0;
         const int nint = pc.ncol > 0 ? s_off[pc.ncol] - pc.ibeg : 0;
-        pc.cap_vel = min(nint, sp.part_slot_bytes / (int)sizeof(VelSlot));
-        pc.cap_pos = min(nint, sp.part_slot_bytes / (int)sizeof(PosSlot));
+        const int islot_bytes = max(0, sp.part_slot_bytes - kBndBytes);
+        pc.cap_vel = min(nint, islot_bytes / (int)sizeof(VelSlot));
+        pc.cap_pos = min(nint, islot_bytes / (int)sizeof(PosSlot));
         for (int l = threadIdx.x; l < pc.nloc; l += blockDim.x) {
             const int b = w.cache_body[pc.cbeg + l];
             pc.body[l] = b;
@@ -1071,6 +1204,14 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
         __syncthreads();
         VelSlot* vs = (VelSlot*)pc.slots;
         for (int j = threadIdx.x; j < pc.cap_vel; j += blockDim.x) vs[j] = part_vel_slot(w, pc, pc.ibeg + j);
+        for (int c = 0; c < ncol; ++c) {
+            int lo, hi;
+            bnd_range(pc, c, &lo, &hi);
+            for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+                const int j = s_boff[c] + i - lo;
+                if (j < kBndSlots) ((VelSlot*)pc.bslots)[j] = vel_slot(w, s_bco[c] + i);
+            }
+        }
         __syncthreads();
         /* phases 2 and 3: the warm start and each velocity iteration sweep the interior colours
          * of every part, then the boundary colours grid-wide */
@@ -1085,11 +1226,7 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
             if (ncol > 0) {
                 if (!grid_barrier(w)) return;
                 for (int c = 0; c < ncol; ++c) {
-                    const int beg = w.col_off[c], end = w.col_off[c + 1];
-                    for (int k = beg + gtid; k < end; k += gsize) {
-                        if (warm) warm_slot(w, k);
-                        else solve_velocity_slot(w, k);
-                    }
+                    bnd_vel_sweep(w, pc, c, warm, last);
                     if (!grid_barrier(w)) return;
                 }
                 if (!last) {
@@ -1171,16 +1308,38 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
         }
         PosSlot* ps = (PosSlot*)pc.slots;
         for (int j = threadIdx.x; j < pc.cap_pos; j += blockDim.x) ps[j] = part_pos_slot(w, pc, pc.ibeg + j);
+        for (int c = 0; c < ncol; ++c) {
+            int lo, hi;
+            bnd_range(pc, c, &lo, &hi);
+            for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+                const int j = s_boff[c] + i - lo;
+                if (j < kBndSlots) ((PosSlot*)pc.bslots)[j] = pos_slot(w, s_bco[c] + i);
+            }
+        }
         __syncthreads();
     }
+    const int nbnd = parts ? min(s_boff[ncol], kBndSlots) : 0;
     for (int it = 0; it < sp.pi; ++it) {
         uint32_t* cur = w.isl_minsep + (size_t)it * w.body_cap;
         if (parts) {
             /* the interior colours, then a barrier: islands span parts, and the next iteration's
              * early exit reads this iteration's buffer */
+            if (it > 0) {
+                part_done_flags(w, pc, nbnd, it, tol);
+                __syncthreads();
+            }
             part_pos_sweeps(w, pc, it, cur, tol);
             part_store(pc, w.b_pos);
             if (!grid_barrier(w)) return;
+            for (int c = 0; c < ncol; ++c) {
+                bnd_pos_sweep(w, pc, c, it, cur, tol);
+                if (!grid_barrier(w)) return;
+            }
+            if (it < sp.pi - 1) {
+                part_load(pc, w.b_pos);
+                __syncthreads();
+            }
+            continue;
         }
         for (int c = 0; c < ncol; ++c) {
             const int beg = w.col_off[c], end = w.col_off[c + 1];
@@ -1194,10 +1353,6 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
                 if (ms < 0.0f) atomicMax(&cur[isl], __float_as_uint(-ms));
             }
             if (!grid_barrier(w)) return;
-        }
-        if (parts && it < sp.pi - 1) {
-            part_load(pc, w.b_pos);
-            __syncthreads();
         }
     }
     /* phase 6a: copy back (synchronize_transform), sleep bookkeeping, clear forces */

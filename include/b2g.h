@@ -347,7 +347,7 @@ typedef struct b2g_launch_config {
     int32_t coop_blocks_per_sm;   /* persistent colouring/solver kernels: 1 or 2 blocks per SM */
     int32_t collide_block;        /* narrowphase threads per block: 32..256, power of two */
     int32_t traverse_block;       /* broadphase traversal threads per block: 32..256, power of two */
-    int32_t pad;
+    int32_t tuning_steps;         /* out: steps the world's last b2g_autotune ran (ignored on set) */
 } b2g_launch_config;
 int b2g_get_launch_config(void* world, b2g_launch_config* out);
 int b2g_set_launch_config(void* world, const b2g_launch_config* config);

@@ -42,7 +42,8 @@ def test_autotune_steps_are_ordinary_steps(built):
     cfg = b.autotune(s["dt"], s["vi"], s["pi"], per)
     assert cfg["coop_blocks_per_sm"] in (1, 2)
     assert cfg["collide_block"] in (64, 128, 256) and cfg["traverse_block"] in (64, 128, 256)
-    n = b2g.B2world.AUTOTUNE_CANDIDATES * (1 + per)
+    n = b.tuning_steps()
+    assert n >= 2 * 3 * (1 + per // 2)  # at least the two block-size knobs, every candidate stepped
     for _ in range(n):
         a.step(s["dt"], s["vi"], s["pi"])
     sa, sb = a.get_body_states(), b.get_body_states()
