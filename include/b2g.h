@@ -261,7 +261,8 @@ int b2g_collide_pairs_noalloc(const b2g_fixture_def* shape_a, const float* xf_a,
 typedef struct b2g_tape_slot {           /* one solver constraint of one taped step (144 bytes) */
     int32_t body_a, body_b;
     int32_t count_type_flags;            /* point count | manifold type << 8 | dynamic A/B << 16 */
-    int32_t colour;
+    int32_t colour;                      /* its boundary colour (0 for a part's interior slot); the
+                                            solve order is the slot order */
     float local_normal[2], local_point[2];
     float points[4];                     /* manifold points (local) */
     float inv_mass_a, inv_mass_b, inv_inertia_a, inv_inertia_b;
