@@ -542,6 +542,7 @@ int allocate(World* w, int nb, int nf) {
     A(d.bp_key, fix_cap); A(d.bp_val, fix_cap); A(d.bp_key_alt, fix_cap); A(d.bp_val_alt, fix_cap);
     A(d.bp_leaf, fix_cap); A(d.bp_node_b0, fix_cap); A(d.bp_node_b1, fix_cap); A(d.bp_node_child, fix_cap);
     A(d.bp_parent, 2 * (size_t)fix_cap); A(d.bp_flag, fix_cap);
+    A(d.bp_quad_box, 4 * (size_t)fix_cap); A(d.bp_quad_child, fix_cap);
     A(d.bp_world_root, 2 * (size_t)w->num_worlds); A(d.bp_world_first, 2 * (size_t)w->num_worlds);
     A(d.events, d.event_cap);
     A(d.pairs, pair_cap);

@@ -200,6 +200,9 @@ struct DevWorld {
     int2* bp_node_child;         /* child indices; leaves encoded as ~leaf */
     int* bp_parent;              /* parent of internal nodes [0,n-1) and leaves [n-1, 2n-1) */
     uint32_t* bp_flag;           /* refit arrival counters */
+    float4* bp_quad_box;         /* internal node: its grandchildren's boxes (4 per node; a leaf child
+                                    stands for itself), so a walk descends two levels per fetch */
+    int4* bp_quad_child;         /* the 4 entries (encoded like children; INT_MIN: none) */
     int* bp_world_root;          /* per key world (2 x num_worlds): root node (encoded like children), or
                                     INT_MIN if empty; key world w + num_worlds holds world w's large
                                     static proxies (see k_bp_keys) */

@@ -14,8 +14,8 @@
  *      walls form a small hierarchy of their own instead of inflating every ancestor box;
  *      a single world then sorts 31 key bits, four 8-bit passes),
  *   3. Karras (2012) hierarchy over the sorted keys (ties broken by position) — every
- *      internal node stores both children's boxes, so a traversal step is one 48-byte
- *      fetch and two overlap tests,
+ *      internal node stores both children's boxes, and after the refit a four-way record of
+ *      its grandchildren, so a traversal step is one 80-byte fetch and four overlap tests,
  *   4. bottom-up refit with per-node arrival counters,
  *   5. one thread per moved proxy walks its world's two subtrees with a short stack and
  *      applies the reference's rule: skip itself; skip a moved partner whose proxy id is
@@ -224,6 +224,37 @@ __global__ void k_bp_refit(DevWorld w) {
 
 __device__ __forceinline__ bool box_overlap(float4 a, float4 b) { return overlap4(a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w); }
 
+/* After the refit: each internal node's four-way record, its children's children (a leaf child
+ * stands for itself). A traversal then tests four boxes per dependent fetch and descends two
+ * levels at a time; the pairs found do not depend on the hierarchy's shape. */
+__global__ void k_bp_quad(DevWorld w) {
+    const int n = w.n_fixtures;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
+        const int2 ch = w.bp_node_child[i];
+        const int kids[2] = {ch.x, ch.y};
+        const float4 boxes[2] = {w.bp_node_b0[i], w.bp_node_b1[i]};
+        int ids[4] = {INT_MIN, INT_MIN, INT_MIN, INT_MIN};
+        float4 qb[4];
+        int m = 0;
+        for (int c = 0; c < 2; ++c) {
+            const int k = kids[c];
+            if (k < 0) {
+                ids[m] = k;
+                qb[m++] = boxes[c];
+            } else {
+                const int2 g = w.bp_node_child[k];
+                ids[m] = g.x;
+                qb[m++] = w.bp_node_b0[k];
+                ids[m] = g.y;
+                qb[m++] = w.bp_node_b1[k];
+            }
+        }
+        for (; m < 4; ++m) qb[m] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        w.bp_quad_child[i] = make_int4(ids[0], ids[1], ids[2], ids[3]);
+        for (int j = 0; j < 4; ++j) w.bp_quad_box[4 * (size_t)i + j] = qb[j];
+    }
+}
+
 /* register table of b2_contact_registers.rs:67-103: +1 keep order, -1 swap, 0 no contact */
 __device__ __forceinline__ int register_kind(int ta, int tb) {
     const int table[9] = {+1, -1, -1, +1, 0, +1, +1, -1, +1};
@@ -316,46 +347,62 @@ __device__ void handle_pair(const DevWorld& w, const StepParams& sp, int f, int 
     }
 }
 
+/* One lane per moved proxy walks the hierarchies, but a warp walks in step: a lane only queues
+ * the leaves its query box overlaps (in shared memory), and whenever a warp has 32 or more queued
+ * the whole warp checks them, one leaf per lane: the partner rules, the existing-contact row scan
+ * and add_pair's filters are chains of dependent loads, and the lanes with the most leaves would
+ * otherwise run them one after another while the rest of the warp waits. */
+constexpr int kLeafQueue = 224;  /* 31 left over + 32 lanes x 6 leaves in one round */
+
 __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams sp) {
+    __shared__ uint2 s_queue[kBlock / 32][kLeafQueue];
     const int n = w.n_fixtures;
     const int n_contacts = w.cnt[CNT_CONTACTS];
     const uint32_t nw = (uint32_t)w.num_worlds;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        const int f = (int)w.bp_val[p];
-        if (!w.f_moved[f]) continue;
-        const float4 q = w.bp_leaf[p];
-        uint32_t wd = (uint32_t)(w.bp_key[p] >> kMortonBits);
-        if (wd >= nw) wd -= nw;
-        const uint32_t rq = w.f_refid[f];
-        auto leaf = [&](int l) {
-            const int g = (int)w.bp_val[l];
-            if (g == f) return;
-            if (w.f_moved[g] && w.f_refid[g] > rq) return;
-            handle_pair(w, sp, f, g, rq, n_contacts);
-        };
-        /* the world's hierarchy, then the one of its large static proxies */
-        for (int h = 0; h < 2; ++h) {
-            const int root = w.bp_world_root[wd + (h ? nw : 0u)];
-            if (root == INT_MIN) continue;
-            if (root < 0) {  /* a single proxy */
-                if (box_overlap(w.bp_leaf[~root], q)) leaf(~root);
-                continue;
+    const int lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    uint2* queue = s_queue[threadIdx.x >> 5];
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+        const int p = base + lane;
+        int f = -1;
+        if (p < n) {
+            f = (int)w.bp_val[p];
+            if (!w.f_moved[f]) f = -1;
+        }
+        int stack[kStack];
+        int sp_top = 0;
+        int found[6];
+        int nfound = 0;
+        float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (f >= 0) {
+            q = w.bp_leaf[p];
+            uint32_t wd = (uint32_t)(w.bp_key[p] >> kMortonBits);
+            if (wd >= nw) wd -= nw;
+            /* the world's hierarchy and the one of its large static proxies */
+            for (int h = 0; h < 2; ++h) {
+                const int root = w.bp_world_root[wd + (h ? nw : 0u)];
+                if (root == INT_MIN) continue;
+                if (root < 0) {  /* a single proxy */
+                    if (box_overlap(w.bp_leaf[~root], q)) found[nfound++] = ~root;
+                } else {
+                    stack[sp_top++] = root;
+                }
             }
-            int stack[kStack];
-            int sp_top = 0;
-            stack[sp_top++] = root;
-            while (sp_top > 0) {
+        }
+        int nq = 0;
+        for (;;) {
+            if (sp_top > 0) {
                 const int node = stack[--sp_top];
-                const int2 ch = w.bp_node_child[node];
-                const float4 b0 = w.bp_node_b0[node];
-                const float4 b1 = w.bp_node_b1[node];
-                const int kids[2] = {ch.x, ch.y};
-                const bool hit[2] = {box_overlap(b0, q), box_overlap(b1, q)};
-                for (int c = 0; c < 2; ++c) {
-                    if (!hit[c]) continue;
+                const int4 ch = w.bp_quad_child[node];
+                const float4* qb = w.bp_quad_box + 4 * (size_t)node;
+                const float4 bx[4] = {qb[0], qb[1], qb[2], qb[3]};
+                const int kids[4] = {ch.x, ch.y, ch.z, ch.w};
+                for (int c = 0; c < 4; ++c) {
+                    if (kids[c] == INT_MIN || !box_overlap(bx[c], q)) continue;
                     const int id = kids[c];
                     if (id < 0) {
-                        leaf(~id);
+                        found[nfound++] = ~id;
                     } else if (sp_top < kStack) {
                         stack[sp_top++] = id;
                     } else {
@@ -363,6 +410,31 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
                     }
                 }
             }
+            /* queue this round's leaves: a warp prefix sum gives each lane its place */
+            int incl = nfound;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(full, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const int total = __shfl_sync(full, incl, 31);
+            for (int i = 0; i < nfound; ++i) queue[nq + incl - nfound + i] = make_uint2((uint32_t)f, (uint32_t)found[i]);
+            nfound = 0;
+            nq += total;
+            const bool more = __any_sync(full, sp_top > 0);
+            if (nq >= 32 || (!more && nq > 0)) {
+                __syncwarp();
+                for (int i = lane; i < nq; i += 32) {
+                    const uint2 e = queue[i];
+                    const int ff = (int)e.x, g = (int)w.bp_val[e.y];
+                    if (g == ff) continue;
+                    const uint32_t rf = w.f_refid[ff];
+                    if (w.f_moved[g] && w.f_refid[g] > rf) continue;
+                    handle_pair(w, sp, ff, g, rf, n_contacts);
+                }
+                __syncwarp();
+                nq = 0;
+            }
+            if (!more) break;
         }
     }
 }
@@ -470,6 +542,9 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
         }
         k_bp_leaves<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_refit<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        if (n > 1) {
+            k_bp_quad<<<grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        }
         k_bp_rows<<<grid_for(w.contact_cap, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         const int tb = w.cfg_traverse_block;
         k_bp_traverse<<<grid_for(n, tb, num_sms * 2048 / tb), tb, 0, s>>>(w, sp); B2G_LAUNCHED(1);
