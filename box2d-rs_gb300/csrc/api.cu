@@ -529,7 +529,7 @@ int allocate(World* w, int nb, int nf) {
     A(d.n_key, pair_cap); A(d.n_fix, pair_cap); A(d.n_idx, pair_cap); A(d.n_key_alt, pair_cap); A(d.n_idx_alt, pair_cap);
     A(d.cons_contact, contact_cap); A(d.cons_colour, contact_cap); A(d.cons_island, contact_cap);
     A(d.s_contact, contact_cap); A(d.s_cons, contact_cap); A(d.s_fix, contact_cap);
-    A(d.cons_part, contact_cap);
+    A(d.cons_part, contact_cap); A(d.col_tail, kColourTail);
     A(d.col_off, kMaxColours + 1); A(d.col_hist, (size_t)(kMaxParts + 1) * kMaxColours);
     A(d.part_off, (size_t)kMaxParts * (kMaxColours + 1)); A(d.part_ncol, kMaxParts); A(d.part_tot, kMaxParts + 1);
     A(d.rank_x, fix_cap); A(d.blk_tot, kMaxParts); A(d.cache_body, fix_cap);

@@ -82,11 +82,13 @@ enum {
     CNT_PART_NCACHE = 23, /* constraint bodies of the current partition (entries of cache_body) */
     CNT_PART_P = 24,      /* parts of the current partition (0: none) */
     CNT_PART_NF = 25,     /* proxies when the current partition was made */
+    CNT_TAIL = 26,        /* colouring: constraints left to the single-block rounds */
     CNT_SIZE = 32
 };
 
 constexpr int kMaxColours = 256;   /* first-fit colours 0..63, then one per colouring round */
 constexpr int kFirstFitColours = 64;
+constexpr int kColourTail = 256;   /* uncoloured constraints one block finishes colouring (one per thread) */
 constexpr int kMaxParts = 1024;    /* body parts of the part-local solve (at most one per solver block) */
 constexpr int kMaxPosIters = 64;
 
@@ -170,6 +172,7 @@ struct DevWorld {
     int* s_cons;                 /* slot -> constraint */
     int2* s_fix;                 /* slot -> (fixture A, fixture B): the solve order exported to the host */
     int* cons_part;              /* part of an interior constraint, -1 for a boundary one */
+    int* col_tail;               /* kColourTail: the constraints the last colouring rounds took */
     int* col_off;                /* kMaxColours + 1 offsets of non-empty boundary colours */
     int* col_hist;               /* (kMaxParts + 1) x kMaxColours counts, then slot cursors:
                                     rows of the parts' interior colours, last row the boundary's */

@@ -195,6 +195,94 @@ __device__ __forceinline__ unsigned long long block_scan_excl64(unsigned long lo
 
 constexpr uint32_t kStampMask = 0x1ffffffu;  /* colouring stamps kept in contacts: 25 bits */
 
+/* The last colouring rounds in one block (block 0), on the listed uncoloured constraints: the
+ * rounds of k_colour with block barriers. Offers of both round parities at the listed
+ * constraints' bodies are cleared first (earlier rounds may have left them). Returns the next
+ * round number and records the rounds. */
+__device__ int colour_tail(const DevWorld& w, int round) {
+    __shared__ int s_list[kColourTail];
+    __shared__ int s_left[2];
+    const int m = min(w.cnt[CNT_TAIL], kColourTail);
+    const size_t bc = (size_t)w.body_cap;
+    const unsigned long long kNone = ~0ull;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) s_list[i] = w.col_tail[i];
+    __syncthreads();
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int k = s_list[i];
+        const int2 bd = w.c.body[w.cons_contact[k]];
+        const size_t cm = w.cons_part[k] < 0 ? bc : 0;
+        for (int par = 0; par < 2; ++par) {
+            w.b_cmin[(size_t)par * 2 * bc + cm + bd.x] = kNone;
+            w.b_cmin[(size_t)par * 2 * bc + cm + bd.y] = kNone;
+        }
+    }
+    if (threadIdx.x == 0) s_left[0] = s_left[1] = 0;
+    __syncthreads();
+    int r = round;
+    for (;;) {
+        if (r >= kMaxColours - kFirstFitColours) {
+            for (int i = threadIdx.x; i < m; i += blockDim.x)
+                if (w.cons_colour[s_list[i]] < 0) w.cons_colour[s_list[i]] = kMaxColours - 1;
+            if (threadIdx.x == 0) atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_COLOUR_OVERFLOW);
+            break;
+        }
+        unsigned long long* offer = w.b_cmin + (size_t)(r & 1) * 2 * bc;
+        unsigned long long* stale = w.b_cmin + (size_t)((r + 1) & 1) * 2 * bc;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const int k = s_list[i];
+            const int2 bd = w.c.body[w.cons_contact[k]];
+            const size_t cm = w.cons_part[k] < 0 ? bc : 0;
+            if (r > round) {
+                stale[cm + bd.x] = kNone;
+                stale[cm + bd.y] = kNone;
+            }
+            if (w.cons_colour[k] >= 0) continue;
+            const unsigned long long key = ((unsigned long long)hash32((uint32_t)k) << 32) | (uint32_t)k;
+            if (is_dynamic(w.b_flags[bd.x])) atomicMin(&offer[cm + bd.x], key);
+            if (is_dynamic(w.b_flags[bd.y])) atomicMin(&offer[cm + bd.y], key);
+        }
+        if (threadIdx.x == 0) s_left[(r + 1) & 1] = 0;
+        __syncthreads();
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const int k = s_list[i];
+            if (w.cons_colour[k] >= 0) continue;
+            const int2 bd = w.c.body[w.cons_contact[k]];
+            const size_t cm = w.cons_part[k] < 0 ? bc : 0;
+            const unsigned long long key = ((unsigned long long)hash32((uint32_t)k) << 32) | (uint32_t)k;
+            const bool da = is_dynamic(w.b_flags[bd.x]), db = is_dynamic(w.b_flags[bd.y]);
+            const bool winA = !da || offer[cm + bd.x] == key;
+            const bool winB = !db || offer[cm + bd.y] == key;
+            if (winA && winB) {
+                const unsigned long long used =
+                    (da ? w.b_cmask[cm + bd.x] : 0ull) | (db ? w.b_cmask[cm + bd.y] : 0ull);
+                int colour;
+                if (~used != 0ull) {
+                    colour = __ffsll((long long)~used) - 1;
+                    const unsigned long long bit = 1ull << colour;
+                    if (da) w.b_cmask[cm + bd.x] |= bit;
+                    if (db) w.b_cmask[cm + bd.y] |= bit;
+                } else {
+                    colour = kFirstFitColours + r;
+                    if (colour >= kMaxColours) {
+                        colour = kMaxColours - 1;
+                        atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_COLOUR_OVERFLOW);
+                    }
+                }
+                w.cons_colour[k] = colour;
+            } else {
+                atomicAdd(&s_left[r & 1], 1);
+            }
+        }
+        __syncthreads();
+        const int left = s_left[r & 1];
+        __syncthreads();  /* every thread has read it before the next round clears the other counter */
+        ++r;
+        if (left == 0) break;
+    }
+    if (threadIdx.x == 0) w.cnt[CNT_ROUNDS] = r;
+    return r;
+}
+
 /* Colouring. Constraints are of two classes. With the part-local solve, the dynamic bodies are
  * split into parts (one per solver block, by Morton rank); a constraint whose dynamic bodies all
  * lie in one part is interior, the others are boundary. Interior constraints are solved by their
@@ -361,12 +449,26 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
         w.cnt[CNT_UNCOLOURED] = 0;
         w.cnt[CNT_UNCOLOURED + 1] = n;
         w.cnt[CNT_ROUNDS] = 0;
+        w.cnt[CNT_TAIL] = 0;
     }
     if (!grid_barrier(w)) return;
     int round = 0;
     for (;;) {
         const int remaining = ((volatile int*)w.cnt)[CNT_UNCOLOURED + ((round + 1) & 1)];
         if (remaining <= 0) break;
+        if (remaining <= kColourTail) {
+            /* Few left: list them and let one block finish the rounds with block barriers. Its
+             * rounds are the same rounds (priorities, first fit, overflow colours by round). */
+            for (int k = gtid; k < n; k += gsize)
+                if (w.cons_colour[k] < 0) {
+                    const int at = atomicAdd(&w.cnt[CNT_TAIL], 1);
+                    if (at < kColourTail) w.col_tail[at] = k;
+                }
+            if (!grid_barrier(w)) return;
+            if (blockIdx.x == 0) round = colour_tail(w, round);
+            if (!grid_barrier(w)) return;
+            break;
+        }
         if (round >= kMaxColours - kFirstFitColours) {
             /* cannot happen for rounds bounded by the maximum body degree; keep the kernel finite */
             for (int k = gtid; k < n; k += gsize)
@@ -424,7 +526,7 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
         ++round;
         if (!grid_barrier(w)) return;
     }
-    if (gtid == 0) w.cnt[CNT_ROUNDS] = round;
+    if (gtid == 0 && w.cnt[CNT_TAIL] == 0) w.cnt[CNT_ROUNDS] = round;
     /* histogram rows: part p's interior colours are row p, the boundary colours row P */
     for (int k = gtid; k < n; k += gsize) {
         const int part = w.cons_part[k];
