@@ -286,49 +286,36 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_coop(unsigned long long* k
         return;
     }
     const int tiles = (n + kSortTile - 1) / kSortTile;
-    uint32_t* dtot = hist + (size_t)256 * tiles;
     unsigned long long *kin = ka, *kout = kb;
     uint32_t *vin = va, *vout = vb;
     for (int p = 0; p < passes; ++p) {
         const int shift = 8 * p;
-        /* H: per-tile digit counts, digit-major */
+        /* H: per-tile digit counts, tile-major */
         for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
             tile_histogram(kin, n, shift, t * kSortTile, s_cnt);
-            hist[threadIdx.x * tiles + t] = s_cnt[threadIdx.x];
+            hist[(size_t)t * 256 + threadIdx.x] = s_cnt[threadIdx.x];
             __syncthreads();
         }
         if (!grid_barrier(cnt)) return;
-        /* S: exclusive scan of each digit's column over the tiles; column totals to dtot */
-        for (int d = blockIdx.x; d < 256; d += gridDim.x) {
-            uint32_t* col = hist + (size_t)d * tiles;
-            __shared__ uint32_t carry;
-            if (threadIdx.x == 0) carry = 0;
-            __syncthreads();
-            for (int base = 0; base < tiles; base += blockDim.x) {
-                const int i = base + threadIdx.x;
-                const uint32_t v = i < tiles ? col[i] : 0u;
-                uint32_t total;
-                const uint32_t ex = block_exclusive_scan(v, &total);
-                if (i < tiles) col[i] = carry + ex;
+        /* X: a block with tiles derives its digit bases itself (thread d sums digit d over the
+         * tiles: the digit's total and the counts of the tiles before each of its own), then
+         * scatters its tiles stably; no separate scan phase and barrier */
+        if ((int)blockIdx.x < tiles) {
+            const int d = threadIdx.x;
+            uint32_t tot = 0;
+#pragma unroll 8
+            for (int t = 0; t < tiles; ++t) tot += hist[(size_t)t * 256 + d];
+            uint32_t total;
+            const uint32_t digit_base = block_exclusive_scan(tot, &total);
+            uint32_t before = 0;
+            int next = 0;
+            for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+                for (; next < t; ++next) before += hist[(size_t)next * 256 + d];
+                s_base[d] = digit_base + before;
                 __syncthreads();
-                if (threadIdx.x == 0) carry += total;
+                scatter_tile(kin, vin, kout, vout, n, shift, t * kSortTile, s_base, s_run, s_warp);
                 __syncthreads();
             }
-            if (threadIdx.x == 0) dtot[d] = carry;
-            __syncthreads();
-        }
-        if (!grid_barrier(cnt)) return;
-        /* X: digit bases (each block scans the 256 totals), then stable scatter of its tiles */
-        {
-            uint32_t total;
-            const uint32_t ex = block_exclusive_scan(dtot[threadIdx.x], &total);
-            s_cnt[threadIdx.x] = ex;
-            __syncthreads();
-        }
-        for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
-            s_base[threadIdx.x] = s_cnt[threadIdx.x] + hist[threadIdx.x * tiles + t];
-            __syncthreads();
-            scatter_tile(kin, vin, kout, vout, n, shift, t * kSortTile, s_base, s_run, s_warp);
         }
         if (!grid_barrier(cnt)) return;
         unsigned long long* tk = kin; kin = kout; kout = tk;
