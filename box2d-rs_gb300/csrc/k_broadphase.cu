@@ -347,21 +347,27 @@ __device__ void handle_pair(const DevWorld& w, const StepParams& sp, int f, int 
     }
 }
 
-/* One lane per moved proxy walks the hierarchies, but a warp walks in step: a lane only queues
- * the leaves its query box overlaps (in shared memory), and whenever a warp has 32 or more queued
- * the whole warp checks them, one leaf per lane: the partner rules, the existing-contact row scan
- * and add_pair's filters are chains of dependent loads, and the lanes with the most leaves would
- * otherwise run them one after another while the rest of the warp waits. */
-constexpr int kLeafQueue = 224;  /* 31 left over + 32 lanes x 6 leaves in one round */
+/* One lane per moved proxy starts a walk of the hierarchies, and a warp walks in step:
+ *  - a lane only queues the leaves its query box overlaps (in shared memory), and whenever a warp
+ *    has 32 or more queued the whole warp checks them, one leaf per lane (the partner rules, the
+ *    existing-contact row scan and add_pair's filters are chains of dependent loads);
+ *  - a lane whose walk is done takes over the oldest pending node of a lane with two or more,
+ *    with that lane's query box, so a warp's rounds follow its total work rather than its longest
+ *    walk. */
+constexpr int kLeafQueue = 224;  /* 31 left over + 32 lanes x 4 leaves in one round, or the setup's
+                                    2 single-proxy roots per lane */
 
 __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams sp) {
     __shared__ uint2 s_queue[kBlock / 32][kLeafQueue];
+    __shared__ int s_give_node[kBlock / 32][32];
+    __shared__ int s_give_f[kBlock / 32][32];
+    __shared__ float4 s_give_q[kBlock / 32][32];
     const int n = w.n_fixtures;
     const int n_contacts = w.cnt[CNT_CONTACTS];
     const uint32_t nw = (uint32_t)w.num_worlds;
-    const int lane = threadIdx.x & 31;
-    const unsigned full = 0xffffffffu;
-    uint2* queue = s_queue[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+    const unsigned full = 0xffffffffu, lt = (1u << lane) - 1u;
+    uint2* queue = s_queue[wq];
     const int stride = gridDim.x * blockDim.x;
     for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
         const int p = base + lane;
@@ -371,7 +377,7 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
             if (!w.f_moved[f]) f = -1;
         }
         int stack[kStack];
-        int sp_top = 0;
+        int bot = 0, top = 0;  /* pending nodes [bot, top) of the current query */
         int found[6];
         int nfound = 0;
         float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -386,31 +392,13 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
                 if (root < 0) {  /* a single proxy */
                     if (box_overlap(w.bp_leaf[~root], q)) found[nfound++] = ~root;
                 } else {
-                    stack[sp_top++] = root;
+                    stack[top++] = root;
                 }
             }
         }
         int nq = 0;
-        for (;;) {
-            if (sp_top > 0) {
-                const int node = stack[--sp_top];
-                const int4 ch = w.bp_quad_child[node];
-                const float4* qb = w.bp_quad_box + 4 * (size_t)node;
-                const float4 bx[4] = {qb[0], qb[1], qb[2], qb[3]};
-                const int kids[4] = {ch.x, ch.y, ch.z, ch.w};
-                for (int c = 0; c < 4; ++c) {
-                    if (kids[c] == INT_MIN || !box_overlap(bx[c], q)) continue;
-                    const int id = kids[c];
-                    if (id < 0) {
-                        found[nfound++] = ~id;
-                    } else if (sp_top < kStack) {
-                        stack[sp_top++] = id;
-                    } else {
-                        atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_STACK_OVERFLOW);
-                    }
-                }
-            }
-            /* queue this round's leaves: a warp prefix sum gives each lane its place */
+        /* queue the leaves found so far: a warp prefix sum gives each lane its place */
+        auto enqueue = [&]() {
             int incl = nfound;
             for (int o = 1; o < 32; o <<= 1) {
                 const int y = __shfl_up_sync(full, incl, o);
@@ -420,7 +408,56 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
             for (int i = 0; i < nfound; ++i) queue[nq + incl - nfound + i] = make_uint2((uint32_t)f, (uint32_t)found[i]);
             nfound = 0;
             nq += total;
-            const bool more = __any_sync(full, sp_top > 0);
+        };
+        enqueue();  /* single-proxy roots, before this lane may take over another query */
+        for (;;) {
+            /* idle lanes take the oldest pending node of lanes with two or more */
+            const unsigned idle = __ballot_sync(full, top == bot);
+            const unsigned donors = __ballot_sync(full, top - bot >= 2);
+            if (idle != 0u && donors != 0u) {
+                const int pairs = min(__popc(idle), __popc(donors));
+                if ((donors >> lane) & 1u) {
+                    const int r = __popc(donors & lt);
+                    if (r < pairs) {
+                        s_give_node[wq][r] = stack[bot++];
+                        s_give_f[wq][r] = f;
+                        s_give_q[wq][r] = q;
+                    }
+                }
+                __syncwarp();
+                if ((idle >> lane) & 1u) {
+                    const int r = __popc(idle & lt);
+                    if (r < pairs) {
+                        f = s_give_f[wq][r];
+                        q = s_give_q[wq][r];
+                        bot = 0;
+                        top = 0;
+                        stack[top++] = s_give_node[wq][r];
+                    }
+                }
+                __syncwarp();
+            }
+            if (top > bot) {
+                const int node = stack[--top];
+                const int4 ch = w.bp_quad_child[node];
+                const float4* qb = w.bp_quad_box + 4 * (size_t)node;
+                const float4 bx[4] = {qb[0], qb[1], qb[2], qb[3]};
+                const int kids[4] = {ch.x, ch.y, ch.z, ch.w};
+                for (int c = 0; c < 4; ++c) {
+                    if (kids[c] == INT_MIN || !box_overlap(bx[c], q)) continue;
+                    const int id = kids[c];
+                    if (id < 0) {
+                        found[nfound++] = ~id;
+                    } else if (top < kStack) {
+                        stack[top++] = id;
+                    } else {
+                        atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_STACK_OVERFLOW);
+                    }
+                }
+                if (top == bot) bot = top = 0;
+            }
+            enqueue();
+            const bool more = __any_sync(full, top > bot);
             if (nq >= 32 || (!more && nq > 0)) {
                 __syncwarp();
                 for (int i = lane; i < nq; i += 32) {
