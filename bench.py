@@ -11,8 +11,10 @@ Legs
               each step bracketed by CUDA events on the world's stream; an L2 flush
               (a 256 MiB write) runs between steps outside the timed events.
   e2e         the same steps through the public API with host buffers: b2g_step plus a
-              read of every body's state (position, angle, velocities) into host memory,
-              timed on the host clock around the whole loop.
+              read of every body's state (position, angle, velocities) into host memory
+              after every step (b2g_get_body_states_async: the copy of step k overlaps
+              step k + 1; the last copy is waited for), timed on the host clock around the
+              whole loop.
   cpu_baseline the oracle (a faithful single-threaded CPU restatement of box2d-rs's step,
               libm sin/cos) timed on this host on a bounded sample of the same workload.
   --impl reference  times that CPU restatement alone (the real Rust crate cannot be built
@@ -442,7 +444,7 @@ def main():
     w.close()
 
     # e2e: a fresh world over the same step window, stepped through the API with every body's
-    # state read back into host memory each step
+    # state read back into host memory each step (b2g_get_body_states_async)
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else args.steps
     w = b2g.B2world(gravity=scene["gravity"], device=local_rank)
     w.set_allow_sleeping(False)
@@ -452,11 +454,14 @@ def main():
     for _ in range(args.warmup):
         w.step(dt, vi, pi)
     w.synchronize()
-    states = np.zeros(w.body_count, b2g.BODY_STATE)
+    # every step's states are copied into host memory (two buffers alternate); the copy of step k
+    # runs on a second stream while step k + 1 is computed, and the last one is waited for
+    states = [np.zeros(w.body_count, b2g.BODY_STATE) for _ in range(2)]
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    for k in range(e2e_steps):
         w.step(dt, vi, pi)
-        w.get_body_states(out=states)
+        w.get_body_states_async(states[k & 1])
+    w.wait_body_states()
     e2e_s = time.perf_counter() - t0
     d2h = w.body_count * 32  # one b2g_body_state (32 bytes) per body
     w.close()

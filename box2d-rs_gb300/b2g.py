@@ -364,6 +364,8 @@ def load_library(path=LIB_PATH):
         "b2g_step": [vp, f32, i32, i32],
         "b2g_synchronize": [vp],
         "b2g_get_body_states": [vp, u32, u32, vp],
+        "b2g_get_body_states_async": [vp, u32, u32, vp],
+        "b2g_wait_body_states": [vp],
         "b2g_get_mass_data": [vp, u32, u32, vp],
         "b2g_set_transform": [vp, u32, Vec2, f32],
         "b2g_set_linear_velocity": [vp, u32, Vec2],
@@ -520,6 +522,17 @@ class B2world:
             out = np.zeros(count, BODY_STATE)
         self._check(self._lib.b2g_get_body_states(self._h, first, count, _ptr(out)))
         return out
+
+    def get_body_states_async(self, out, first=0):
+        """Start copying body states [first, first + len(out)) into `out` without waiting; the copy
+        overlaps the next steps. `out` must not be read or freed before wait_body_states()."""
+        if out.dtype != BODY_STATE or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a contiguous BODY_STATE array")
+        self._check(self._lib.b2g_get_body_states_async(self._h, first, len(out), _ptr(out)))
+        return out
+
+    def wait_body_states(self):
+        self._check(self._lib.b2g_wait_body_states(self._h))
 
     def get_mass_data(self, first=0, count=None):
         """(n, 6) float32: mass, 1/mass, inertia about the centre, its inverse, local centre x, y."""

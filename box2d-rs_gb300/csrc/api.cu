@@ -133,6 +133,12 @@ struct World {
     bool pageable = false;   /* the device reads/writes pageable host memory coherently */
     b2g_body_state* d_states = nullptr;  /* packing buffer for b2g_get_body_states otherwise */
     int d_states_cap = 0;
+    /* b2g_get_body_states_async: two device snapshots, copied out on a second stream */
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_packed[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
+    b2g_body_state* d_ring[2] = {nullptr, nullptr};
+    int ring_cap = 0, ring_next = 0;
+    bool ring_used[2] = {false, false};
 };
 
 /* bucket: log2 of the bodies per world (batched worlds of uneven size use the mean), and
@@ -884,6 +890,13 @@ __global__ void k_pack_states(DevWorld d, uint32_t first, uint32_t count, b2g_bo
     }
 }
 
+/* the snapshot of b2g_get_body_states_async into the caller's buffer (host memory the device
+ * reaches coherently), 16 bytes per thread */
+__global__ void k_copy_states(const float4* __restrict__ in, float4* out, size_t n4) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = in[i];
+}
+
 /* small body edits after the device became authoritative */
 /* One edit of one body (src/b2_body.rs): 0 set_linear_velocity (:684-694), 1 set_angular_velocity
  * (:696-705), 2 apply_force, 3 apply_linear_impulse, 4 apply_force_to_center, 5 apply_torque,
@@ -1002,6 +1015,15 @@ int b2g_world_destroy(void* p) {
     World* w = W(p);
     if (!w) return B2G_ERR_INVALID_ARG;
     cudaStreamSynchronize(w->stream);
+    if (w->copy_stream) {
+        cudaStreamSynchronize(w->copy_stream);
+        for (int i = 0; i < 2; ++i) {
+            if (w->d_ring[i]) cudaFree(w->d_ring[i]);
+            cudaEventDestroy(w->ev_packed[i]);
+            cudaEventDestroy(w->ev_copied[i]);
+        }
+        cudaStreamDestroy(w->copy_stream);
+    }
     tape_free(w);
     if (w->d_states) cudaFree(w->d_states);
     free_all(w);
@@ -1118,6 +1140,63 @@ int b2g_step(void* p, float dt, int32_t vi, int32_t pi) {
 int b2g_synchronize(void* p) {
     World* w = W(p);
     if (!w) return B2G_ERR_INVALID_ARG;
+    return check_status(w);
+}
+
+int b2g_get_body_states_async(void* p, uint32_t first, uint32_t count, b2g_body_state* out) {
+    World* w = W(p);
+    if (!w || (!out && count > 0)) return B2G_ERR_INVALID_ARG;
+    if ((size_t)first + count > w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body range out of bounds");
+    if (count == 0) return B2G_OK;
+    if (!(w->device_authoritative && (int)(first + count) <= w->uploaded_bodies))
+        return b2g_get_body_states(p, first, count, out);  /* the host holds the state: nothing to overlap */
+    if (!w->copy_stream) {
+        CUDA_OK(w, cudaStreamCreateWithFlags(&w->copy_stream, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; ++i) {
+            CUDA_OK(w, cudaEventCreateWithFlags(&w->ev_packed[i], cudaEventDisableTiming));
+            CUDA_OK(w, cudaEventCreateWithFlags(&w->ev_copied[i], cudaEventDisableTiming));
+        }
+    }
+    if (w->ring_cap < (int)count) {
+        CUDA_OK(w, cudaStreamSynchronize(w->copy_stream));
+        for (int i = 0; i < 2; ++i) {
+            if (w->d_ring[i]) cudaFree(w->d_ring[i]);
+            w->d_ring[i] = nullptr;
+            w->ring_used[i] = false;
+        }
+        w->ring_cap = 0;
+        for (int i = 0; i < 2; ++i) CUDA_OK(w, cudaMalloc((void**)&w->d_ring[i], count * sizeof(b2g_body_state)));
+        w->ring_cap = (int)count;
+    }
+    const int i = w->ring_next;
+    w->ring_next ^= 1;
+    /* the snapshot is taken in stream order after the last issued step; the copy out of this
+     * buffer two requests ago must have finished before it is overwritten */
+    if (w->ring_used[i]) CUDA_OK(w, cudaStreamWaitEvent(w->stream, w->ev_copied[i], 0));
+    const int grid = grid_for((int)count, 256, w->num_sms * 8);
+    k_pack_states<<<grid, 256, 0, w->stream>>>(w->d, first, count, w->d_ring[i], nullptr);
+    B2G_LAUNCHED(1);
+    CUDA_OK(w, cudaEventRecord(w->ev_packed[i], w->stream));
+    CUDA_OK(w, cudaStreamWaitEvent(w->copy_stream, w->ev_packed[i], 0));
+    if (w->pageable) {
+        const size_t n4 = (size_t)count * sizeof(b2g_body_state) / sizeof(float4);
+        k_copy_states<<<grid_for((int)std::min<size_t>(n4, 1u << 30), 256, w->num_sms * 4), 256, 0, w->copy_stream>>>(
+            (const float4*)w->d_ring[i], (float4*)out, n4);
+        B2G_LAUNCHED(1);
+    } else {
+        CUDA_OK(w, cudaMemcpyAsync(out, w->d_ring[i], count * sizeof(b2g_body_state), cudaMemcpyDeviceToHost,
+                                   w->copy_stream));
+    }
+    CUDA_OK(w, cudaEventRecord(w->ev_copied[i], w->copy_stream));
+    w->ring_used[i] = true;
+    CUDA_OK(w, cudaGetLastError());
+    return B2G_OK;
+}
+
+int b2g_wait_body_states(void* p) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    if (w->copy_stream) CUDA_OK(w, cudaStreamSynchronize(w->copy_stream));
     return check_status(w);
 }
 

@@ -169,6 +169,15 @@ int b2g_synchronize(void* world);
 
 /* ---- state I/O (src/b2_body.rs getters/setters) ---- */
 int b2g_get_body_states(void* world, uint32_t first, uint32_t count, b2g_body_state* out);
+/* The same states without waiting (not in the reference: pipelined read-back). A snapshot is
+ * taken on the world's stream after the last issued step and copied into `out` on a second
+ * stream while the next steps run; at most two requests are in flight (a third waits, on the
+ * device, for the first copy). `out` must stay valid and untouched until b2g_wait_body_states
+ * returns; it must be host memory the device can write asynchronously: page-locked memory, or
+ * any memory on systems with coherent access to pageable memory (Grace). */
+int b2g_get_body_states_async(void* world, uint32_t first, uint32_t count, b2g_body_state* out);
+/* Wait for the asynchronous copies and the world's stream; reports device-side errors. */
+int b2g_wait_body_states(void* world);
 /* B2body::get_mass_data / get_local_center: 6 floats per body: mass, 1/mass, rotational inertia
  * about the centre of mass (get_inertia adds mass * |local centre|^2), its inverse, local centre. */
 int b2g_get_mass_data(void* world, uint32_t first, uint32_t count, float* out);
