@@ -137,6 +137,12 @@ CONTACT_INFO = np.dtype(
 
 EVENT = np.dtype([("kind", "<i4"), ("fixture_a", "<u4"), ("fixture_b", "<u4")])
 
+# B2Sweep (src/b2_math.rs): local centre, centre and angle at the start (c0, a0) and the end (c, a)
+SWEEP = np.dtype([("local_center", "<f4", (2,)), ("c0", "<f4", (2,)), ("c", "<f4", (2,)), ("a0", "<f4"),
+                  ("a", "<f4"), ("alpha0", "<f4"), ("pad", "<f4")])
+TOI_OUTPUT = np.dtype([("state", "<i4"), ("t", "<f4")])
+TOI_UNKNOWN, TOI_FAILED, TOI_OVERLAPPED, TOI_TOUCHING, TOI_SEPARATED = range(5)
+
 RAY_HIT = np.dtype([("fixture", "<i4"), ("point", "<f4", (2,)), ("normal", "<f4", (2,)), ("fraction", "<f4")])
 assert RAY_HIT.itemsize == 24
 
@@ -416,6 +422,8 @@ def load_library(path=LIB_PATH):
     lib.b2g_last_error.restype = ctypes.c_char_p
     lib.b2g_collide_pairs.argtypes = [vp, vp, vp, vp, i32, vp]
     lib.b2g_collide_pairs.restype = ctypes.c_int
+    lib.b2g_time_of_impact.argtypes = [vp, vp, vp, vp, vp, i32, vp]
+    lib.b2g_time_of_impact.restype = ctypes.c_int
     lib.b2g_get_launch_count.argtypes = []
     lib.b2g_get_launch_count.restype = ctypes.c_int64
     _lib = lib
@@ -433,6 +441,23 @@ def collide_pairs(defs_a, xf_a, defs_b, xf_b):
     rc = lib.b2g_collide_pairs(_ptr(da), _ptr(xa), _ptr(db), _ptr(xb), len(da), _ptr(out))
     if rc != OK:
         raise B2GError(rc, "b2g_collide_pairs")
+    return out
+
+
+def time_of_impact(defs_a, sweeps_a, defs_b, sweeps_b, t_max=None):
+    """GPU time of impact of independent pairs of moving shapes (b2_time_of_impact): a TOI_OUTPUT
+    (state TOI_*, t) per pair; t_max per pair (default 1)."""
+    lib = load_library()
+    da = np.ascontiguousarray(defs_a, FIXTURE_DEF)
+    db = np.ascontiguousarray(defs_b, FIXTURE_DEF)
+    sa = np.ascontiguousarray(sweeps_a, SWEEP)
+    sb = np.ascontiguousarray(sweeps_b, SWEEP)
+    tm = None if t_max is None else np.ascontiguousarray(t_max, np.float32)
+    out = np.zeros(len(da), TOI_OUTPUT)
+    rc = lib.b2g_time_of_impact(_ptr(da), _ptr(sa), _ptr(db), _ptr(sb), None if tm is None else _ptr(tm), len(da),
+                                _ptr(out))
+    if rc != OK:
+        raise B2GError(rc, "b2g_time_of_impact")
     return out
 
 

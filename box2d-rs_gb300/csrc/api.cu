@@ -1664,6 +1664,57 @@ int b2g_collide_pairs(const b2g_fixture_def* da, const float* xfa, const b2g_fix
 
 }  // extern "C"
 
+int b2g_time_of_impact(const b2g_fixture_def* da, const b2g_sweep* swa, const b2g_fixture_def* db,
+                       const b2g_sweep* swb, const float* t_max, int32_t n, b2g_toi_output* out) {
+    if (n < 0 || (n > 0 && (!da || !db || !swa || !swb || !out))) return B2G_ERR_INVALID_ARG;
+    if (n == 0) return B2G_OK;
+    std::vector<ShapeRec> sa(n), sb(n);
+    std::vector<float4> wa(2 * (size_t)n), wb(2 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        for (const b2g_fixture_def* d : {&da[i], &db[i]})
+            if (d->shape_type != B2G_SHAPE_CIRCLE && d->shape_type != B2G_SHAPE_POLYGON && d->shape_type != B2G_SHAPE_EDGE)
+                return B2G_ERR_INVALID_ARG;
+        build_shape(da[i], sa[i]);
+        build_shape(db[i], sb[i]);
+        const b2g_sweep& a = swa[i];
+        const b2g_sweep& b = swb[i];
+        wa[2 * i] = make_float4(a.local_center.x, a.local_center.y, a.c0.x, a.c0.y);
+        wa[2 * i + 1] = make_float4(a.c.x, a.c.y, a.a0, a.a);
+        wb[2 * i] = make_float4(b.local_center.x, b.local_center.y, b.c0.x, b.c0.y);
+        wb[2 * i + 1] = make_float4(b.c.x, b.c.y, b.a0, b.a);
+    }
+    ShapeRec *d_sa = nullptr, *d_sb = nullptr;
+    float4 *d_wa = nullptr, *d_wb = nullptr;
+    float* d_t = nullptr;
+    int2* d_out = nullptr;
+    int rc = B2G_OK;
+    if (cudaMalloc(&d_sa, n * sizeof(ShapeRec)) != cudaSuccess || cudaMalloc(&d_sb, n * sizeof(ShapeRec)) != cudaSuccess ||
+        cudaMalloc(&d_wa, 2 * n * sizeof(float4)) != cudaSuccess || cudaMalloc(&d_wb, 2 * n * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&d_out, n * sizeof(int2)) != cudaSuccess || (t_max && cudaMalloc(&d_t, n * sizeof(float)) != cudaSuccess))
+        rc = B2G_ERR_OUT_OF_MEMORY;
+    if (rc == B2G_OK) {
+        cudaMemcpy(d_sa, sa.data(), n * sizeof(ShapeRec), cudaMemcpyHostToDevice);
+        cudaMemcpy(d_sb, sb.data(), n * sizeof(ShapeRec), cudaMemcpyHostToDevice);
+        cudaMemcpy(d_wa, wa.data(), 2 * n * sizeof(float4), cudaMemcpyHostToDevice);
+        cudaMemcpy(d_wb, wb.data(), 2 * n * sizeof(float4), cudaMemcpyHostToDevice);
+        if (t_max) cudaMemcpy(d_t, t_max, n * sizeof(float), cudaMemcpyHostToDevice);
+        launch_time_of_impact(d_sa, d_wa, d_sb, d_wb, d_t, n, d_out, 0);
+        std::vector<int2> res(n);
+        if (cudaMemcpy(res.data(), d_out, n * sizeof(int2), cudaMemcpyDeviceToHost) != cudaSuccess) rc = B2G_ERR_CUDA;
+        for (int i = 0; rc == B2G_OK && i < n; ++i) {
+            out[i].state = res[i].x;
+            memcpy(&out[i].t, &res[i].y, sizeof(float));
+        }
+    }
+    cudaFree(d_sa);
+    cudaFree(d_sb);
+    cudaFree(d_wa);
+    cudaFree(d_wb);
+    cudaFree(d_t);
+    cudaFree(d_out);
+    return rc;
+}
+
 /* ---- allocation-free variant of b2g_collide_pairs ----
  * For callers that must not allocate (a frame loop with a fixed time budget, where freeing
  * device memory can wait for the whole device, or a program whose device memory belongs to

@@ -226,6 +226,9 @@ void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cud
 /* parts: allow the part-local solve (used where the world's size suits it) */
 void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms, bool parts);
 int launch_solver(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms, bool parts);
+/* time of impact of n shape pairs (sweeps as 2 float4: (lc, c0), (c, a0, a)); out = (state, t bits) */
+void launch_time_of_impact(const ShapeRec* sa, const float4* swa, const ShapeRec* sb, const float4* swb,
+                           const float* t_max, int n, int2* out, cudaStream_t s);
 /* whether the part-local solve applies to this world (parts allowed and the world's size suits it) */
 bool use_parts(const DevWorld& w, int num_sms, bool allowed);
 /* after_tree (optional) is called between the tree pass (keys, sort, build, refit, traverse)

@@ -234,6 +234,29 @@ int b2g_set_contact_events(void* world, int32_t flag);
 int b2g_collide_pairs(const b2g_fixture_def* shape_a, const float* xf_a, const b2g_fixture_def* shape_b,
                       const float* xf_b, int32_t n, b2g_contact_info* out);
 
+/* Time of impact of n independent pairs of moving shapes on the GPU (not used by b2g_step: the
+ * step runs without continuous physics), like the reference's public b2_time_of_impact
+ * (src/b2_time_of_impact.rs:48-50, private/collision/b2_time_of_impact.rs:191-463) with its GJK
+ * distance (private/collision/b2_distance.rs:331-440). A sweep is a body's motion over the
+ * interval (B2Sweep, src/b2_math.rs): local centre of mass, centre and angle at the start
+ * (c0, a0) and at the end (c, a); alpha0 is carried for the caller and not read. t_max: per pair
+ * (NULL: 1). Shapes are circles, polygons or edges. out[i] is the state (B2G_TOI_*) and the time
+ * in [0, t_max]. */
+enum { B2G_TOI_UNKNOWN = 0, B2G_TOI_FAILED = 1, B2G_TOI_OVERLAPPED = 2, B2G_TOI_TOUCHING = 3, B2G_TOI_SEPARATED = 4 };
+typedef struct b2g_sweep {
+    b2g_vec2 local_center;
+    b2g_vec2 c0, c;
+    float a0, a;
+    float alpha0;
+    float pad;
+} b2g_sweep;
+typedef struct b2g_toi_output {
+    int32_t state;
+    float t;
+} b2g_toi_output;
+int b2g_time_of_impact(const b2g_fixture_def* shape_a, const b2g_sweep* sweep_a, const b2g_fixture_def* shape_b,
+                       const b2g_sweep* sweep_b, const float* t_max, int32_t n, b2g_toi_output* out);
+
 /* Run steady-state steps as captured CUDA graphs (on by default). A step is captured once
  * per contact-buffer parity and replayed while dt, iterations, flags, gravity and the body
  * and fixture counts stay the same; any change re-captures. */

@@ -19,6 +19,8 @@
 
 #include "b2_oracle_math.h"
 
+struct b2g_fixture_def;
+
 namespace ora {
 
 enum { SHAPE_CIRCLE = 0, SHAPE_EDGE = 1, SHAPE_POLYGON = 2 };
@@ -45,6 +47,9 @@ struct Shape {
     Vec2 normals[kMaxPolygonVertices];
     Vec2 centroid{0, 0};
 };
+
+/* the shape of a fixture definition (b2_oracle_world.cpp) */
+void shape_from_def(const ::b2g_fixture_def& d, Shape& s);
 
 struct MassData {
     float mass;

@@ -274,6 +274,9 @@ static void build_shape(const b2g_fixture_def& d, Shape& s) {
     }
 }
 
+/* the fixture definition's shape, for the stand-alone routines (time of impact) */
+void shape_from_def(const b2g_fixture_def& d, Shape& s) { build_shape(d, s); }
+
 /* create_fixture, private/dynamics/b2_body.rs:155-200; create_proxies, private/dynamics/b2_fixture.rs:114-133 */
 static int create_fixture(World& w, const b2g_fixture_def& d) {
     Fixture f;

@@ -69,6 +69,7 @@ def load():
         "ora_polygon_mass": [vp, vp],
         "ora_sincos": [vp, vp, vp, i32],
         "ora_collide": [vp, vp, vp, vp, vp],
+        "ora_time_of_impact": [vp, vp, vp, vp, vp, i32, vp],
         "ora_import_state": [vp, vp, i32, vp, i32, vp, i32, f32],
     }
     for name, args in sig.items():
@@ -115,6 +116,20 @@ def collide(def_a, xf_a, def_b, xf_b):
     if rc != 0:
         raise ValueError("unsupported shape pair")
     return out[0]
+
+
+def time_of_impact(defs_a, sweeps_a, defs_b, sweeps_b, t_max=None):
+    """Time of impact of independent pairs of moving shapes (b2_time_of_impact), same layout as
+    b2g.time_of_impact."""
+    da = np.ascontiguousarray(defs_a, b2g.FIXTURE_DEF)
+    db = np.ascontiguousarray(defs_b, b2g.FIXTURE_DEF)
+    sa = np.ascontiguousarray(sweeps_a, b2g.SWEEP)
+    sb = np.ascontiguousarray(sweeps_b, b2g.SWEEP)
+    tm = None if t_max is None else np.ascontiguousarray(t_max, np.float32)
+    out = np.zeros(len(da), b2g.TOI_OUTPUT)
+    load().ora_time_of_impact(_ptr(da), _ptr(sa), _ptr(db), _ptr(sb), None if tm is None else _ptr(tm), len(da),
+                              _ptr(out))
+    return out
 
 
 class OracleWorld:
