@@ -288,6 +288,75 @@ def _stack_loss_grad(world, scene):
     return d
 
 
+def _toi_pairs(n, seed):
+    """n random pairs of moving shapes for the time-of-impact leg: circles (r 0.1-0.6), 3-8-gons
+    (radius 0.2-0.7 with jitter) and edges (up to 3 m), sweeps moving up to 4 m and turning up to
+    3 rad; the same mix as tests/test_toi.py, generated with array operations."""
+    rng = np.random.default_rng(seed)
+
+    def defs():
+        d = b2g.fixture_defs(n)
+        kind = rng.integers(0, 3, n)
+        c, p, e = kind == 0, kind == 1, kind == 2
+        d["shape_type"][c] = b2g.CIRCLE
+        d["radius"][c] = rng.uniform(0.1, 0.6, int(c.sum()))
+        d["vertices"][c, 0] = rng.uniform(-0.2, 0.2, (int(c.sum()), 2))
+        d["shape_type"][p] = b2g.POLYGON
+        d["polygon_mode"][p] = b2g.POLYGON_HULL
+        k = rng.integers(3, 9, n)
+        ang = np.sort(rng.uniform(0, 2 * np.pi, (n, 8)), axis=1)
+        rad = rng.uniform(0.2, 0.7, (n, 8))
+        verts = np.stack([rad * np.cos(ang), rad * np.sin(ang)], 2).astype(np.float32)
+        verts[np.arange(8)[None, :] >= k[:, None]] = 0.0
+        d["vertices"][p] = verts[p]
+        d["vertex_count"][p] = k[p]
+        d["shape_type"][e] = b2g.EDGE
+        a = rng.uniform(-2, 2, (n, 2)).astype(np.float32)
+        d["vertices"][e, 1] = a[e]
+        d["vertices"][e, 2] = (a + rng.uniform(-3, 3, (n, 2)))[e]
+        return d
+
+    def sweeps(spread):
+        s = np.zeros(n, b2g.SWEEP)
+        s["local_center"] = rng.uniform(-0.1, 0.1, (n, 2))
+        s["c0"] = rng.uniform(-spread, spread, (n, 2))
+        s["c"] = s["c0"] + rng.uniform(-spread, spread, (n, 2))
+        s["a0"] = rng.uniform(-10, 10, n)
+        s["a"] = s["a0"] + rng.uniform(-3, 3, n)
+        return s
+
+    return defs(), sweeps(4.0), defs(), sweeps(1.0)
+
+
+def run_toi(n=1_000_000, sample=100_000, repeats=3):
+    """Batched time of impact (b2g_time_of_impact): pairs per second through the C ABI (host shape
+    set-up, copies and the kernel, host clock), the oracle's single-thread rate on a sample, and
+    whether the sample's results are bit-identical."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    da, sa, db, sb = _toi_pairs(n, 11)
+    b2g.time_of_impact(da[:1000], sa[:1000], db[:1000], sb[:1000])  # load and warm up
+    best = float("inf")
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        got = b2g.time_of_impact(da, sa, db, sb)
+        best = min(best, time.perf_counter() - t0)
+    oracle.build()
+    oracle.set_trig(False)
+    try:
+        t0 = time.perf_counter()
+        ref = oracle.time_of_impact(da[:sample], sa[:sample], db[:sample], sb[:sample])
+        cpu = time.perf_counter() - t0
+    finally:
+        oracle.set_trig(True)
+    same = bool(np.array_equal(got[:sample]["state"], ref["state"]) and
+                np.array_equal(got[:sample]["t"].view(np.uint32), ref["t"].view(np.uint32)))
+    return {"pairs": n, "pairs_per_s": n / best, "cpu_pairs_per_s": sample / cpu, "cpu_sample": sample,
+            "cpu_cores": 1, "sample_bit_identical": same,
+            "states": np.bincount(got["state"], minlength=5).tolist()}
+
+
 def run_adjoint(torch, flush, device, steps=240, seeds=512, repeats=3):
     """Differentiable throw-and-stack (64 boxes + a circle projectile, loss = squared distance of the
     stack's centre of mass from a target after `steps` steps): device time of the plain forward
@@ -351,6 +420,7 @@ def main():
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels directly instead of CUDA graphs")
     ap.add_argument("--batched-steps", type=int, default=300, help="steps of the 4096-world leg (0 skips it)")
     ap.add_argument("--adjoint-steps", type=int, default=240, help="steps of the differentiable leg (0 skips it)")
+    ap.add_argument("--toi-pairs", type=int, default=1_000_000, help="pairs of the time-of-impact leg (0 skips it)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
     ap.add_argument("--skip-steps", type=int, default=0,
                     help="untimed steps before the warm-up (profiling a later window of the scene)")
@@ -512,6 +582,8 @@ def main():
                                       rank=rank, world_size=world_size, autotune=not args.no_autotune)
     if args.adjoint_steps > 0 and rank == 0:
         line["adjoint"] = run_adjoint(torch, flush, local_rank, steps=args.adjoint_steps)
+    if args.toi_pairs > 0 and rank == 0:
+        line["time_of_impact"] = run_toi(args.toi_pairs)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = run_cpu_on_snapshots(scene, snaps)
     if rank == 0:
