@@ -195,6 +195,25 @@ def timed_steps(world, scene, steps, flush, torch):
     return total
 
 
+def tune_blocks_per_sm(torch, flush, t, dt, vi, pi, turns=3, steps=3):
+    """After b2g_autotune (which times back-to-back steps): choose the persistent kernels' blocks
+    per SM on the scratch world `t` the way this bench times a step (device time, L2 flushed before
+    it); the two settings take turns. Returns the launch configuration to use."""
+    base = t.get_launch_config()
+    total = {1: 0.0, 2: 0.0}
+    for _ in range(turns):
+        for c in (1, 2):
+            t.set_launch_config(c, base["collide_block"], base["traverse_block"])
+            for _ in range(2):  # the step graph's captures for both contact-buffer parities
+                t.step(dt, vi, pi)
+            for _ in range(steps):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                t.step(dt, vi, pi)
+                total[c] += t.get_profile()["step"]  # device time (CUDA events), as timed_steps
+    return dict(base, coop_blocks_per_sm=min(total, key=total.get))
+
+
 def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_bucket=6, rank=0, world_size=1,
                 autotune=True):
     """Batched uneven worlds: one world batch stepped together vs. the same worlds stepped one
@@ -210,11 +229,14 @@ def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_
         scenes.build_world(t, part)
         for _ in range(warmup + steps // 2):
             t.step(part["dt"], part["vi"], part["pi"])
-        t.autotune(part["dt"], part["vi"], part["pi"], 3)
+        t.autotune(part["dt"], part["vi"], part["pi"], 6)
+        tuned = tune_blocks_per_sm(torch, flush, t, part["dt"], part["vi"], part["pi"])
         t.close()
     w = b2g.B2world(gravity=part["gravity"], num_worlds=part["num_worlds"], device=device)
     w.set_allow_sleeping(False)
     scenes.build_world(w, part)
+    if autotune:
+        w.set_launch_config(**tuned)
     for _ in range(warmup):
         w.step(part["dt"], part["vi"], part["pi"])
     w.synchronize()
@@ -468,12 +490,15 @@ def main():
         scenes.build_world(t, scene)
         for _ in range(args.skip_steps + args.warmup + args.steps // 2):
             t.step(dt, vi, pi)
-        t.autotune(dt, vi, pi, 3)
+        t.autotune(dt, vi, pi, 6)
+        tuned = tune_blocks_per_sm(torch, flush, t, dt, vi, pi)
         t.close()
     w = b2g.B2world(gravity=scene["gravity"], device=local_rank)
     w.set_allow_sleeping(False)
     w.set_continuous_physics(False)
     w.set_graph_capture(not args.no_graphs)
+    if not args.no_autotune:
+        w.set_launch_config(**tuned)
     scenes.build_world(w, scene)
     for _ in range(args.skip_steps + args.warmup):
         w.step(dt, vi, pi)
@@ -520,6 +545,8 @@ def main():
     w.set_allow_sleeping(False)
     w.set_continuous_physics(False)
     w.set_graph_capture(not args.no_graphs)
+    if not args.no_autotune:
+        w.set_launch_config(**tuned)
     scenes.build_world(w, scene)
     for _ in range(args.warmup):
         w.step(dt, vi, pi)

@@ -1989,8 +1989,9 @@ extern "C" {
 
 /* Coordinate search over the launch configuration on the world's own next steps: for each knob in
  * turn (persistent-kernel blocks per SM, narrowphase block, traversal block) the candidates take
- * turns over up to four rounds, each turn one untimed step (graph capture) and its share of
- * `steps_per_candidate` timed steps; the fastest in total is kept. With the part-local solve the
+ * turns over up to four rounds, each turn two untimed steps (the step graph's captures for both
+ * contact-buffer parities) and its share of `steps_per_candidate` timed steps; the fastest in
+ * total is kept. With the part-local solve the
  * persistent kernels keep one block per SM.
  * The steps are real steps of the world (the configuration never changes results). The choice is
  * applied to the world and remembered for later worlds of the same size bucket in this process. */
@@ -2006,7 +2007,7 @@ int b2g_autotune(void* p, float dt, int32_t vi, int32_t pi, int32_t steps_per_ca
     const int ncoop = use_parts(w->d, w->num_sms, w->part_solve) ? 1 : 2;
     /* the world keeps evolving while candidates are timed, so the candidates take turns over
      * several rounds (a step each) instead of running one after another */
-    const int rounds = std::max(1, std::min(steps_per_candidate, 4));
+    const int rounds = std::max(1, std::min(steps_per_candidate / 2, 4));
     const int per_round = std::max(1, steps_per_candidate / rounds);
     int tuned = 0;
     for (int knob = 0; knob < 3; ++knob) {
@@ -2025,9 +2026,10 @@ int b2g_autotune(void* p, float dt, int32_t vi, int32_t pi, int32_t steps_per_ca
                 apply_launch_config(w);
                 drop_graphs(w);
                 double ms = 0.0;
-                int rc = timed_steps(w, dt, vi, pi, 1, &ms);  /* graph capture, untimed */
+                /* untimed: the captures of the step graph for both contact-buffer parities */
+                int rc = timed_steps(w, dt, vi, pi, 2, &ms);
                 if (rc == B2G_OK) rc = timed_steps(w, dt, vi, pi, per_round, &ms);
-                tuned += 1 + per_round;
+                tuned += 2 + per_round;
                 if (rc != B2G_OK) return rc;
                 total[i] += ms;
             }

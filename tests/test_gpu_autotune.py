@@ -43,7 +43,7 @@ def test_autotune_steps_are_ordinary_steps(built):
     assert cfg["coop_blocks_per_sm"] in (1, 2)
     assert cfg["collide_block"] in (64, 128, 256) and cfg["traverse_block"] in (64, 128, 256)
     n = b.tuning_steps()
-    assert n >= 2 * 3 * (1 + per // 2)  # at least the two block-size knobs, every candidate stepped
+    assert n >= 2 * 3 * 3  # at least the two block-size knobs, every candidate stepped 2 + 1 times
     for _ in range(n):
         a.step(s["dt"], s["vi"], s["pi"])
     sa, sb = a.get_body_states(), b.get_body_states()
