@@ -625,9 +625,15 @@ __device__ void init_slot(const DevWorld& w, const StepParams& sp, int k) {
     const V2 cA = v2of(pA.x, pA.y), cB = v2of(pB.x, pB.y);
     const V2 vA = v2of(vA4.x, vA4.y), vB = v2of(vB4.x, vB4.y);
     const float wA = vA4.z, wB = vB4.z;
+    /* xf.q = rot(angle): the bodies' transforms hold exactly that rotation of their current angles
+     * (written from the same angle by the last copy-back, set_transform or creation), so it is
+     * read instead of evaluating sin/cos again for every constraint */
+    const float4 xa4 = w.b_xf[bd.x], xb4 = w.b_xf[bd.y];
     Xf xfA, xfB;
-    xfA.q = rot(pA.z);
-    xfB.q = rot(pB.z);
+    xfA.q.s = xa4.z;
+    xfA.q.c = xa4.w;
+    xfB.q.s = xb4.z;
+    xfB.q.c = xb4.w;
     xfA.p = sub(cA, mul(xfA.q, mk(lcA.x, lcA.y)));
     xfB.p = sub(cB, mul(xfB.q, mk(lcB.x, lcB.y)));
     /* b2_world_manifold_initialize, private/collision/b2_collision.rs:7-68 */
