@@ -189,3 +189,51 @@ def test_one_sided_edges_and_kinematic(built):
     recs, _, _ = parity.lockstep(s, 200)
     for r in recs:
         _assert_step(r)
+
+
+def test_kinematic_bodies_across_parts_lockstep(built):
+    """3000 mixed bodies (several parts of the part-local solve) with six kinematic paddles
+    sweeping through them: kinematic bodies are in no part (their velocities are read, never
+    written), and the constraints at them follow their dynamic body's part."""
+    s = scenes.mixed(n_circles=1500, n_polygons=1500, size=40.0, seed=17)
+    nb = len(s["bodies"])
+    kin = b2g.body_defs(6)
+    kin["type"] = b2g.KINEMATIC
+    kin["allow_sleep"] = 0
+    kin["position"][:, 0] = np.linspace(6.0, 34.0, 6)
+    kin["position"][:, 1] = 5.0
+    kin["linear_velocity"][:, 0] = np.array([1.5, -1.5] * 3)
+    kin["angular_velocity"] = np.array([0.7, -0.7] * 3)
+    fx = np.concatenate([b2g.box_fixture(nb + i, 2.0, 0.15, density=1.0) for i in range(6)])
+    s = dict(s, bodies=np.concatenate([s["bodies"], kin]), fixtures=np.concatenate([s["fixtures"], fx]))
+    recs, _, _ = parity.lockstep(s, 60)
+    for r in recs:
+        _assert_step(r)
+    assert max(r["constraints"] for r in recs) > 500
+
+
+def test_compound_bodies_lockstep(built):
+    """1500 bodies with two fixtures each (a box and an offset circle): a body's Morton rank is its
+    first fixture's, its fixtures may lie far apart in that order, and pairs within a body are
+    never made."""
+    rng = np.random.default_rng(23)
+    n = 1500
+    bodies = b2g.body_defs(n + 1)
+    bodies["allow_sleep"] = 0
+    bodies[1:]["type"] = b2g.DYNAMIC
+    bodies[1:]["position"][:, 0] = rng.uniform(2.0, 48.0, n)
+    bodies[1:]["position"][:, 1] = rng.uniform(2.0, 60.0, n)
+    bodies[1:]["angle"] = rng.uniform(0.0, 6.28, n)
+    walls = [b2g.edge_fixture(0, (0.0, 0.0), (50.0, 0.0)), b2g.edge_fixture(0, (0.0, 0.0), (0.0, 80.0)),
+             b2g.edge_fixture(0, (50.0, 0.0), (50.0, 80.0))]
+    fx = []
+    for i in range(n):
+        fx.append(b2g.box_fixture(i + 1, 0.3, 0.15, density=1.0, friction=0.5))
+        fx.append(b2g.circle_fixture(i + 1, 0.2, center=(0.45, 0.0), density=1.0, friction=0.5))
+    s = {"name": "compound", "bodies": bodies, "fixtures": np.concatenate(walls + fx), "gravity": (0.0, -10.0),
+         "dt": np.float32(1.0 / 60.0), "vi": 8, "pi": 3, "steps": 60, "num_worlds": 1, "allow_sleep": False,
+         "n_dynamic": n}
+    recs, _, _ = parity.lockstep(s, 60)
+    for r in recs:
+        _assert_step(r)
+    assert max(r["constraints"] for r in recs) > 300
