@@ -392,6 +392,7 @@ def load_library(path=LIB_PATH):
         "b2g_clear_forces": [vp],
         "b2g_get_profile": [vp, ctypes.POINTER(Profile)],
         "b2g_get_counts": [vp, ctypes.POINTER(Counts)],
+        "b2g_get_toi_stats": [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)],
         "b2g_get_contacts": [vp, vp, i32, ctypes.POINTER(i32)],
         "b2g_get_events": [vp, vp, i32, ctypes.POINTER(i32)],
         "b2g_get_pairs": [vp, vp, i32, ctypes.POINTER(i32)],
@@ -652,6 +653,12 @@ class B2world:
         c = Counts()
         self._check(self._lib.b2g_get_counts(self._h, ctypes.byref(c)))
         return c.as_dict()
+
+    def get_toi_stats(self):
+        """(solid time-of-impact events since creation, iterations of the last step's pass)."""
+        e, it = ctypes.c_int32(0), ctypes.c_int32(0)
+        self._check(self._lib.b2g_get_toi_stats(self._h, ctypes.byref(e), ctypes.byref(it)))
+        return int(e.value), int(it.value)
 
     def _get_list(self, fn, dtype, cap_hint, width=1):
         n = ctypes.c_int32(0)

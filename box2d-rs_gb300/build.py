@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libb2g.so")
 OBJDIR = os.path.join(HERE, "_build")
-SOURCES = ["api.cu", "k_collide.cu", "k_solver.cu", "k_broadphase.cu", "k_prims.cu", "k_adjoint.cu", "k_query.cu", "k_toi.cu"]
+SOURCES = ["api.cu", "k_collide.cu", "k_solver.cu", "k_broadphase.cu", "k_prims.cu", "k_adjoint.cu", "k_query.cu", "k_toi.cu", "k_continuous.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = [
     "-O3", "-std=c++17", "-lineinfo",

@@ -40,7 +40,7 @@ namespace {
 constexpr int kVersion = 1;
 
 struct Timer {
-    cudaEvent_t e[8] = {};
+    cudaEvent_t e[9] = {};
     bool valid = false;
 };
 
@@ -105,6 +105,7 @@ struct World {
     std::vector<std::vector<int>> body_fixtures;  /* newest first, like the reference's fixture list */
     std::vector<ShapeRec> h_shape;
     std::vector<int> h_fbody;
+    std::vector<int> h_fix_off, h_fix;  /* body -> fixtures, uploaded with the fixtures */
     std::vector<float4> h_fmat, h_fat;
     std::vector<uint32_t> h_filter, h_group, h_refid;
     std::vector<uint8_t> h_moved;
@@ -550,6 +551,14 @@ int allocate(World* w, int nb, int nf) {
     A(d.bp_parent, 2 * (size_t)fix_cap); A(d.bp_flag, fix_cap);
     A(d.bp_quad_box, 4 * (size_t)fix_cap); A(d.bp_quad_child, fix_cap);
     A(d.bp_world_root, 2 * (size_t)w->num_worlds); A(d.bp_world_first, 2 * (size_t)w->num_worlds);
+    A(d.b_fix_off, (size_t)body_cap + 1); A(d.b_fix, fix_cap);
+    A(d.b_alpha0, body_cap); A(d.b_stamp, body_cap); A(d.b_inval, body_cap); A(d.b_sync, body_cap);
+    A(d.f_pmoved, fix_cap);
+    A(d.t_toi, contact_cap); A(d.t_when, contact_cap); A(d.t_count, contact_cap); A(d.t_stamp, contact_cap);
+    A(d.t_elig, contact_cap); A(d.t_hits, contact_cap); A(d.t_sync, body_cap);
+    A(d.t_moved, kToiMovedCap); A(d.t_pmoved, kToiPassMovedCap); A(d.t_nkey, kToiNewCap); A(d.t_nslot, kToiNewCap);
+    A(d.tw_alpha, w->num_worlds); A(d.tw_key, w->num_worlds); A(d.tw_event, w->num_worlds);
+    A(d.tw_ealpha, w->num_worlds); A(d.tw_cand, (size_t)w->num_worlds * (kToiCand + 1));
     A(d.events, d.event_cap);
     A(d.pairs, pair_cap);
     A(d.scan_tmp, 2 * (size_t)contact_cap + scan_tmp_size(contact_cap) + 64);
@@ -576,6 +585,17 @@ int upload(World* w) {
         U(d.f_shape, w->h_shape); U(d.f_body, w->h_fbody); U(d.f_mat, w->h_fmat); U(d.f_filter, w->h_filter);
         U(d.f_group, w->h_group); U(d.f_refid, w->h_refid); U(d.f_fat, w->h_fat); U(d.f_moved, w->h_moved);
     }
+    /* body -> fixtures (the continuous pass synchronises an island body's proxies) */
+    w->h_fix_off.assign((size_t)nb + 1, 0);
+    for (int f = 0; f < nf; ++f) ++w->h_fix_off[(size_t)w->h_fbody[f] + 1];
+    for (int b = 0; b < nb; ++b) w->h_fix_off[(size_t)b + 1] += w->h_fix_off[b];
+    w->h_fix.assign((size_t)std::max(nf, 1), 0);
+    {
+        std::vector<int> fill(w->h_fix_off.begin(), w->h_fix_off.end() - 1);
+        for (int f = 0; f < nf; ++f) w->h_fix[(size_t)fill[w->h_fbody[f]]++] = f;
+    }
+    U(d.b_fix_off, w->h_fix_off);
+    if (nf > 0) U(d.b_fix, w->h_fix);
 #undef U
     CUDA_OK(w, cudaStreamSynchronize(s));
     w->uploaded_bodies = nb;
@@ -703,6 +723,10 @@ int status_error(World* w, int status) {
                     "contact_capacity / pair_capacity in b2g_world_def");
     if (status & ST_EVENT_OVERFLOW) return fail(w, B2G_ERR_CAPACITY, "contact event buffer overflowed");
     if (status & ST_RECORD_OVERFLOW) return fail(w, B2G_ERR_CAPACITY, "recorded pair buffer overflowed");
+    if (status & ST_TOI_OVERFLOW)
+        return fail(w, B2G_ERR_CAPACITY,
+                    "a list of the continuous pass overflowed (time-of-impact island of more than 64 bodies or 64 "
+                    "partner contacts, or more than 4096 new contacts or moved proxies in one step)");
     if (status & ST_PART_MISMATCH)
         return fail(w, B2G_ERR_CUDA, "the solver ran with a block count other than its colouring's");
     return B2G_OK;
@@ -762,6 +786,9 @@ void issue_step(World* w, const StepParams& sp, float dt, bool capturing = false
         mark(t.e[4]);
         launch_broadphase(w->d, sp, s, w->num_sms, [&]() { mark(t.e[7]); });
         swap_contacts(w);
+        mark(t.e[8]);
+        /* B2world::solve_toi (private/dynamics/b2_world.rs:946-950) */
+        if (w->continuous) launch_continuous(w->d, sp, s, w->num_sms);
         mark(t.e[5]);
         w->inv_dt0 = sp.inv_dt;
     } else {
@@ -770,6 +797,7 @@ void issue_step(World* w, const StepParams& sp, float dt, bool capturing = false
         mark(t.e[4]);
         mark(t.e[7]);
         if (w->auto_clear) launch_clear_forces(w->d, s);
+        mark(t.e[8]);
         mark(t.e[5]);
     }
 }
@@ -822,7 +850,8 @@ int step(World* w, float dt, int vi, int pi) {
         key.vi = vi;
         key.pi = pi;
         key.flags = sp.warm | (sp.allow_sleep << 1) | (sp.auto_clear << 2) | (sp.record_events << 3) |
-                    (sp.record_pairs << 4) | ((w->tape && w->tape->recording) ? (1 << 5) : 0);
+                    (sp.record_pairs << 4) | ((w->tape && w->tape->recording) ? (1 << 5) : 0) |
+                    (w->continuous ? (1 << 6) : 0);
         key.generation = w->alloc_generation;
         key.n_bodies = w->d.n_bodies;
         key.n_fixtures = w->d.n_fixtures;
@@ -1132,8 +1161,8 @@ int b2g_create_fixtures(void* p, const b2g_fixture_def* defs, int32_t n, uint32_
 int b2g_step(void* p, float dt, int32_t vi, int32_t pi) {
     World* w = W(p);
     if (!w) return B2G_ERR_INVALID_ARG;
-    if (w->continuous)
-        return fail(w, B2G_ERR_UNSUPPORTED, "continuous physics (time of impact) is not on the GPU path; call b2g_set_continuous_physics(world, 0)");
+    if (w->continuous && w->tape && w->tape->recording)
+        return fail(w, B2G_ERR_UNSUPPORTED, "the tape does not record the continuous pass; call b2g_set_continuous_physics(world, 0) while taping");
     return step(w, dt, vi, pi);
 }
 
@@ -1422,14 +1451,19 @@ int b2g_get_profile(void* p, b2g_profile* out) {
             return fail(w, B2G_ERR_CUDA, "profile events could not be timed");
         }
     }
+    float toi = 0.0f;
+    if (cudaEventElapsedTime(&toi, w->timer.e[0], w->timer.e[8]) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(w, B2G_ERR_CUDA, "profile events could not be timed");
+    }
     out->collide = ms[2] - ms[1];
     out->solve_init = ms[3] - ms[2];
     out->solve_velocity = ms[4] - ms[3];  /* the persistent solver kernel: velocity and position iterations */
     out->solve_position = 0.0f;
-    out->broadphase = (ms[5] - ms[4]) + ms[1];
-    out->solve = ms[5] - ms[2];
+    out->broadphase = (toi - ms[4]) + ms[1];
+    out->solve = toi - ms[2];
+    out->solve_toi = ms[5] - toi;
     out->step = ms[5];
-    out->solve_toi = 0.0f;
     return B2G_OK;
 }
 
@@ -1478,6 +1512,21 @@ int b2g_get_counts(void* p, b2g_counts* out) {
         out->touching_contacts = t;
     }
     out->islands_solved = cnt[CNT_CONS];
+    return B2G_OK;
+}
+
+int b2g_get_toi_stats(void* p, int32_t* events, int32_t* last_iterations) {
+    World* w = W(p);
+    if (!w || !events || !last_iterations) return B2G_ERR_INVALID_ARG;
+    *events = 0;
+    *last_iterations = 0;
+    if (!w->allocated) return B2G_OK;
+    int rc = check_status(w);
+    if (rc != B2G_OK) return rc;
+    int cnt[CNT_SIZE];
+    CUDA_OK(w, cudaMemcpy(cnt, w->d.cnt, sizeof(cnt), cudaMemcpyDeviceToHost));
+    *events = cnt[CNT_TOI_EVENTS];
+    *last_iterations = cnt[CNT_TOI_ITERS];
     return B2G_OK;
 }
 

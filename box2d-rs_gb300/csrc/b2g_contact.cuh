@@ -1,0 +1,172 @@
+/*
+ * b2g_contact.cuh — B2contact::update on the device, shared by the narrowphase pass
+ * (k_collide.cu) and the continuous-physics pass (k_continuous.cu).
+ *
+ * Reference: b2_contact_update, src/private/dynamics/b2_contact.rs:103-218; set_awake,
+ * src/b2_body.rs:783-801.
+ */
+#ifndef B2G_CONTACT_CUH
+#define B2G_CONTACT_CUH
+
+#include "b2g_internal.h"
+
+namespace b2g {
+namespace {
+
+/* set_awake(true): a static body is left alone; any other is flagged awake with its sleep time
+ * reset (the reference resets it whether or not the body slept) */
+__device__ __forceinline__ void wake_body(const DevWorld& w, int b) {
+    const uint32_t f = w.b_flags[b];
+    if ((f & BF_TYPE_MASK) == BODY_STATIC) return;
+    if (!(f & BF_AWAKE)) atomicOr(&w.b_flags[b], BF_AWAKE);
+    w.b_vel[b].w = 0.0f;  /* sleep_time = 0 */
+}
+
+__device__ __forceinline__ void push_event(const DevWorld& w, int kind, int fa, int fb) {
+    int slot = atomicAdd(&w.cnt[CNT_EVENTS], 1);
+    if (slot < w.event_cap) w.events[slot] = make_int4(kind, fa, fb, 0);
+    else atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_EVENT_OVERFLOW);
+}
+
+__device__ __forceinline__ Xf load_xf(const DevWorld& w, int b) {
+    float4 x = w.b_xf[b];
+    Xf r;
+    r.p = mk(x.x, x.y);
+    r.q.s = x.z;
+    r.q.c = x.w;
+    return r;
+}
+
+/* B2contact::update of contact i (flags: its current flags; fx, bd: its fixtures and bodies; ids:
+ * its manifold ids word): re-enable it, evaluate the manifold on the bodies' transforms, carry
+ * impulses from old points with the same feature id, update the touching flag, wake both bodies
+ * when it changes, and record begin/end events. Returns whether the contact touches. */
+__device__ __forceinline__ bool contact_update(const DevWorld& w, bool record_events, int i, uint32_t flags, int2 fx,
+                                               int2 bd, uint4 ids) {
+    const bool was_touching = (flags & CF_TOUCHING) != 0;
+    const int old_count = (int)((ids.z >> 8) & 0xffu);
+    flags |= CF_ENABLED;
+    bool touching = false;
+    if (flags & CF_SENSOR) {
+        /* sensor overlap tests (GJK) are outside the GPU path: sensors never touch */
+        w.c.mids[i] = make_uint4(ids.x, ids.y, ids.z & 0xffu, ids.w);
+    } else {
+        const int kind = (int)((flags >> CF_KIND_SHIFT) & 7u);
+        const Xf xfA = load_xf(w, bd.x);
+        const Xf xfB = load_xf(w, bd.y);
+        const ShapeRec sa = w.f_shape[fx.x];
+        const ShapeRec sb = w.f_shape[fx.y];
+        Manifold m;
+        m.type = MANIFOLD_CIRCLES;
+        m.count = 0;
+        m.ln = mk(0.0f, 0.0f);
+        m.lp = mk(0.0f, 0.0f);
+        m.p[0] = m.p[1] = mk(0.0f, 0.0f);
+        m.id[0] = m.id[1] = 0u;
+        evaluate(kind, m, sa, xfA, sb, xfB);
+        const float4 oldimp = w.c.mimp[i];
+        float ni[2] = {0.0f, 0.0f}, ti[2] = {0.0f, 0.0f};
+        for (int p = 0; p < m.count; ++p) {
+            if (old_count > 0 && ids.x == m.id[p]) {
+                ni[p] = oldimp.x;
+                ti[p] = oldimp.y;
+            } else if (old_count > 1 && ids.y == m.id[p]) {
+                ni[p] = oldimp.z;
+                ti[p] = oldimp.w;
+            }
+        }
+        touching = m.count > 0;
+        w.c.mgeo[i] = make_float4(m.ln.x, m.ln.y, m.lp.x, m.lp.y);
+        w.c.mpts[i] = make_float4(m.p[0].x, m.p[0].y, m.p[1].x, m.p[1].y);
+        w.c.mimp[i] = make_float4(ni[0], ti[0], ni[1], ti[1]);
+        w.c.mids[i] = make_uint4(m.id[0], m.id[1], (uint32_t)m.type | ((uint32_t)m.count << 8), ids.w);
+        if (touching != was_touching) {
+            wake_body(w, bd.x);
+            wake_body(w, bd.y);
+        }
+    }
+    w.c.flags[i] = touching ? (flags | CF_TOUCHING) : (flags & ~CF_TOUCHING);
+    if (record_events) {
+        if (!was_touching && touching) push_event(w, 0, fx.x, fx.y);
+        if (was_touching && !touching) push_event(w, 1, fx.x, fx.y);
+    }
+    return touching;
+}
+
+/* register table of b2_contact_registers.rs:67-103: +1 keep order, -1 swap, 0 no contact */
+__device__ __forceinline__ int register_kind(int ta, int tb) {
+    const int table[9] = {+1, -1, -1, +1, 0, +1, +1, -1, +1};
+    return table[ta * 3 + tb];
+}
+__device__ __forceinline__ int contact_kind(int ta, int tb) {
+    if (ta == SHAPE_CIRCLE) return KIND_CIRCLES;
+    if (ta == SHAPE_POLYGON) return tb == SHAPE_CIRCLE ? KIND_POLYGON_CIRCLE : KIND_POLYGONS;
+    return tb == SHAPE_CIRCLE ? KIND_EDGE_CIRCLE : KIND_EDGE_POLYGON;
+}
+
+/* b2_contact_manager_add_pair's rejections after the existing-contact check
+ * (private/dynamics/b2_contact_manager.rs:178-302): same body, no dynamic body, the default
+ * filter (private/dynamics/b2_world_callbacks.rs:6-18), no manifold routine for the two shape types
+ * (b2_contact_registers.rs:67-103). f is the fixture with the smaller proxy id. On acceptance
+ * (fa, fb) is the contact's fixture pair, fixture A the one of the primary shape type. */
+__device__ __forceinline__ bool pair_accept(const DevWorld& w, int f, int g, int& fa, int& fb) {
+    fa = f;
+    fb = g;
+    const int ba = w.f_body[fa], bb = w.f_body[fb];
+    if (ba == bb) return false;
+    const uint32_t fla = w.b_flags[ba], flb = w.b_flags[bb];
+    if ((fla & BF_TYPE_MASK) != BODY_DYNAMIC && (flb & BF_TYPE_MASK) != BODY_DYNAMIC) return false;
+    /* f_filter = category | mask << 16, f_group = group (int16) | sensor << 16 */
+    const uint32_t xa = w.f_filter[fa], xb = w.f_filter[fb];
+    const int grp_a = (int)(int16_t)(w.f_group[fa] & 0xffffu);
+    const int grp_b = (int)(int16_t)(w.f_group[fb] & 0xffffu);
+    if (grp_a == grp_b && grp_a != 0) {
+        if (grp_a <= 0) return false;
+    } else if (((xa >> 16) & (xb & 0xffffu)) == 0u || ((xa & 0xffffu) & (xb >> 16)) == 0u) {
+        return false;
+    }
+    const int reg = register_kind(shape_type(w.f_shape[fa]), shape_type(w.f_shape[fb]));
+    if (reg == 0) return false;
+    if (reg < 0) {
+        fa = g;
+        fb = f;
+    }
+    return true;
+}
+
+/* b2_contact_create + B2contact::new (private/dynamics/b2_contact.rs:11-60) into slot pos of d:
+ * enabled, not touching, an empty manifold, the mixing laws of src/b2_contact.rs:29-46 */
+__device__ __forceinline__ void init_contact(const DevWorld& w, const Contacts& d, int pos, unsigned long long key,
+                                             int2 fx) {
+    const float4 ma = w.f_mat[fx.x], mb = w.f_mat[fx.y];
+    const int kind = contact_kind(shape_type(w.f_shape[fx.x]), shape_type(w.f_shape[fx.y]));
+    const bool sensor = ((w.f_group[fx.x] | w.f_group[fx.y]) & 0x10000u) != 0u;
+    d.key[pos] = key;
+    d.fix[pos] = fx;
+    d.body[pos] = make_int2(w.f_body[fx.x], w.f_body[fx.y]);
+    d.flags[pos] = CF_ENABLED | (sensor ? CF_SENSOR : 0u) | ((uint32_t)kind << CF_KIND_SHIFT);
+    const float friction = fsqrt(ma.x * mb.x);
+    const float restitution = ma.y > mb.y ? ma.y : mb.y;
+    const float threshold = ma.z < mb.z ? ma.z : mb.z;
+    d.mat[pos] = make_float4(friction, restitution, threshold, 0.0f);
+    d.mgeo[pos] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    d.mpts[pos] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    d.mimp[pos] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    d.mids[pos] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+__device__ __forceinline__ void copy_contact(const Contacts& s, int i, const Contacts& d, int o) {
+    d.key[o] = s.key[i];
+    d.fix[o] = s.fix[i];
+    d.body[o] = s.body[i];
+    d.flags[o] = s.flags[i];
+    d.mat[o] = s.mat[i];
+    d.mgeo[o] = s.mgeo[i];
+    d.mpts[o] = s.mpts[i];
+    d.mimp[o] = s.mimp[i];
+    d.mids[o] = s.mids[i];
+}
+
+}  // namespace
+}  // namespace b2g
+#endif

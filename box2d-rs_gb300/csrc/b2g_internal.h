@@ -57,6 +57,8 @@ enum : uint32_t {
     ST_STACK_OVERFLOW = 1u << 5,
     ST_RECORD_OVERFLOW = 1u << 6,
     ST_PART_MISMATCH = 1u << 7,   /* the solver ran with other parts than its colouring */
+    ST_TOI_OVERFLOW = 1u << 8,    /* a time-of-impact island, candidate, moved-proxy or new-contact
+                                     list of the continuous pass overflowed */
 };
 
 /* device counters (d_cnt[]) */
@@ -83,7 +85,17 @@ enum {
     CNT_PART_P = 24,      /* parts of the current partition (0: none) */
     CNT_PART_NF = 25,     /* proxies when the current partition was made */
     CNT_TAIL = 26,        /* colouring: constraints left to the single-block rounds */
-    CNT_SIZE = 32
+    CNT_TOI_EVENTS = 27,  /* solid time-of-impact events solved since the world was made */
+    CNT_TOI_ITERS = 28,   /* iterations of the last continuous pass */
+    /* continuous pass (k_continuous.cu), zeroed before every pass: */
+    CNT_TOI_FIRST = 32,
+    CNT_TOI_NEW = 32,     /* contacts created by the pass (table slots [n, n + this)) */
+    CNT_TOI_SYNC = 33,    /* bodies with a pending sweep advance */
+    CNT_TOI_MOVED = 34,   /* proxies moved by this iteration's islands */
+    CNT_TOI_HITS = 35,    /* contacts whose time of impact is an event candidate this iteration */
+    CNT_TOI_PMOVED = 36,  /* proxies moved so far in the pass */
+    CNT_TOI_LAST = 37,
+    CNT_SIZE = 48
 };
 
 constexpr int kMaxColours = 256;   /* first-fit colours 0..63, then one per colouring round */
@@ -91,6 +103,12 @@ constexpr int kFirstFitColours = 64;
 constexpr int kColourTail = 256;   /* uncoloured constraints one block finishes colouring (one per thread) */
 constexpr int kMaxParts = 1024;    /* body parts of the part-local solve (at most one per solver block) */
 constexpr int kMaxPosIters = 64;
+/* continuous pass lists (k_continuous.cu): partner contacts of one event, proxies moved in one
+ * iteration and in one pass, contacts created in one pass */
+constexpr int kToiCand = 64;
+constexpr int kToiMovedCap = 4096;
+constexpr int kToiPassMovedCap = 8192;
+constexpr int kToiNewCap = 4096;
 
 struct Contacts {
     unsigned long long* key;
@@ -210,6 +228,31 @@ struct DevWorld {
                                     INT_MIN if empty; key world w + num_worlds holds world w's large
                                     static proxies (see k_bp_keys) */
     int* bp_world_first;         /* per key world: first sorted leaf */
+    /* continuous physics: the time-of-impact pass (k_continuous.cu) */
+    int* b_fix_off;              /* body -> fixtures: offsets into b_fix (n_bodies + 1) */
+    int* b_fix;                  /* fixtures grouped by body */
+    float* b_alpha0;             /* the body sweep's alpha0 during the pass */
+    int* b_stamp;                /* pass iteration that last put the body in an event's island */
+    int* b_inval;                /* pass iteration whose island displaced the body (its contacts' times
+                                    of impact are stale) */
+    uint32_t* b_sync;            /* pending advance of the body's sweep (alpha bits; 0: none) */
+    uint8_t* f_pmoved;           /* the proxy moved earlier in the pass (its LBVH leaf is stale) */
+    float* t_toi;                /* per contact: cached time of impact (alpha) */
+    int* t_when;                 /* per contact: iteration that computed t_toi, -1 none */
+    int* t_count;                /* per contact: time-of-impact events (toi_count) */
+    int* t_stamp;                /* per contact: iteration that put it in an event's island */
+    uint8_t* t_elig;             /* per contact: non-sensor with a bullet or non-dynamic body */
+    int* t_hits;                 /* contacts with an event-candidate alpha this iteration */
+    int* t_sync;                 /* bodies with a pending sweep advance */
+    int* t_moved;                /* proxies moved by this iteration's islands */
+    int* t_pmoved;               /* proxies moved in this pass */
+    unsigned long long* t_nkey;  /* the pass's new contacts sorted by key (key, then table slot) */
+    int* t_nslot;
+    uint32_t* tw_alpha;          /* per world: smallest event alpha of the iteration (bits; ~0: none) */
+    unsigned long long* tw_key;  /* per world: smallest contact key with that alpha */
+    int4* tw_event;              /* per world: (contact, body A, body B, iteration if solid else -1) */
+    float* tw_ealpha;            /* per world: the event's alpha */
+    int* tw_cand;                /* per world: count, then the other contacts of the event's bodies */
     /* outputs for the host */
     int4* events;                /* kind, fixture a, fixture b, - */
     uint2* pairs;                /* recorded emitted pairs (fixture ids) */
@@ -229,6 +272,8 @@ int launch_solver(const DevWorld& w, const StepParams& sp, cudaStream_t s, int n
 /* time of impact of n shape pairs (sweeps as 2 float4: (lc, c0), (c, a0, a)); out = (state, t bits) */
 void launch_time_of_impact(const ShapeRec* sa, const float4* swa, const ShapeRec* sb, const float4* swb,
                            const float* t_max, int n, int2* out, cudaStream_t s);
+/* continuous physics of a step (B2world::solve_toi) as one cooperative launch; returns a CUDA error */
+int launch_continuous(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms);
 /* whether the part-local solve applies to this world (parts allowed and the world's size suits it) */
 bool use_parts(const DevWorld& w, int num_sms, bool allowed);
 /* after_tree (optional) is called between the tree pass (keys, sort, build, refit, traverse)

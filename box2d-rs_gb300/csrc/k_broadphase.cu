@@ -29,7 +29,7 @@
  */
 #include <climits>
 
-#include "b2g_internal.h"
+#include "b2g_contact.cuh"
 
 namespace b2g {
 
@@ -255,17 +255,6 @@ __global__ void k_bp_quad(DevWorld w) {
     }
 }
 
-/* register table of b2_contact_registers.rs:67-103: +1 keep order, -1 swap, 0 no contact */
-__device__ __forceinline__ int register_kind(int ta, int tb) {
-    const int table[9] = {+1, -1, -1, +1, 0, +1, +1, -1, +1};
-    return table[ta * 3 + tb];
-}
-__device__ __forceinline__ int contact_kind(int ta, int tb) {
-    if (ta == SHAPE_CIRCLE) return KIND_CIRCLES;
-    if (ta == SHAPE_POLYGON) return tb == SHAPE_CIRCLE ? KIND_POLYGON_CIRCLE : KIND_POLYGONS;
-    return tb == SHAPE_CIRCLE ? KIND_EDGE_CIRCLE : KIND_EDGE_POLYGON;
-}
-
 __device__ __forceinline__ int lower_bound_u64(const unsigned long long* a, int n, unsigned long long key) {
     int lo = 0, hi = n;
     while (lo < hi) {
@@ -314,29 +303,8 @@ __device__ void handle_pair(const DevWorld& w, const StepParams& sp, int f, int 
     const unsigned long long key = ((unsigned long long)lo << w.key_bits) | hi;
     if (contact_exists(w, lo, key, n_contacts)) return;
     /* add_pair: fixture A is the one with the smaller proxy id */
-    int fa = rf < rg ? f : g, fb = rf < rg ? g : f;
-    const int ba = w.f_body[fa], bb = w.f_body[fb];
-    if (ba == bb) return;
-    const uint32_t fla = w.b_flags[ba], flb = w.b_flags[bb];
-    if ((fla & BF_TYPE_MASK) != BODY_DYNAMIC && (flb & BF_TYPE_MASK) != BODY_DYNAMIC) return;
-    /* default contact filter, private/dynamics/b2_world_callbacks.rs:6-18
-     * f_filter = category | mask << 16, f_group = group (int16) | sensor << 16 */
-    const uint32_t xa = w.f_filter[fa], xb = w.f_filter[fb];
-    const int grp_a = (int)(int16_t)(w.f_group[fa] & 0xffffu);
-    const int grp_b = (int)(int16_t)(w.f_group[fb] & 0xffffu);
-    if (grp_a == grp_b && grp_a != 0) {
-        if (grp_a <= 0) return;
-    } else if (((xa >> 16) & (xb & 0xffffu)) == 0u || ((xa & 0xffffu) & (xb >> 16)) == 0u) {
-        return;
-    }
-    const int ta = shape_type(w.f_shape[fa]), tb = shape_type(w.f_shape[fb]);
-    const int reg = register_kind(ta, tb);
-    if (reg == 0) return;
-    if (reg < 0) {
-        const int t = fa;
-        fa = fb;
-        fb = t;
-    }
+    int fa, fb;
+    if (!pair_accept(w, rf < rg ? f : g, rf < rg ? g : f, fa, fb)) return;
     const int slot = atomicAdd(&w.cnt[CNT_NEW], 1);
     if (slot < w.pair_cap) {
         w.n_key[slot] = key;
@@ -491,18 +459,6 @@ __global__ void k_merge_flags(DevWorld w, uint32_t* flag) {
         flag[i] = (w.c.flags[i] & CF_DEAD) ? 0u : 1u;
 }
 
-__device__ __forceinline__ void copy_contact(const Contacts& s, int i, const Contacts& d, int o) {
-    d.key[o] = s.key[i];
-    d.fix[o] = s.fix[i];
-    d.body[o] = s.body[i];
-    d.flags[o] = s.flags[i];
-    d.mat[o] = s.mat[i];
-    d.mgeo[o] = s.mgeo[i];
-    d.mpts[o] = s.mpts[i];
-    d.mimp[o] = s.mimp[i];
-    d.mids[o] = s.mids[i];
-}
-
 __global__ void k_merge_old(DevWorld w, const uint32_t* flag, const uint32_t* rank) {
     const int n = w.cnt[CNT_CONTACTS];
     const int nn = w.cnt[CNT_NEW];
@@ -529,24 +485,7 @@ __global__ void k_merge_new(DevWorld w, const uint32_t* rank) {
             atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_CONTACT_OVERFLOW);
             continue;
         }
-        const float4 ma = w.f_mat[fx.x], mb = w.f_mat[fx.y];
-        const ShapeRec& sa = w.f_shape[fx.x];
-        const ShapeRec& sb = w.f_shape[fx.y];
-        const int kind = contact_kind(shape_type(sa), shape_type(sb));
-        const bool sensor = ((w.f_group[fx.x] | w.f_group[fx.y]) & 0x10000u) != 0u;
-        const Contacts& d = w.c_alt;
-        d.key[pos] = key;
-        d.fix[pos] = fx;
-        d.body[pos] = make_int2(w.f_body[fx.x], w.f_body[fx.y]);
-        d.flags[pos] = CF_ENABLED | (sensor ? CF_SENSOR : 0u) | ((uint32_t)kind << CF_KIND_SHIFT);
-        const float friction = fsqrt(ma.x * mb.x);
-        const float restitution = ma.y > mb.y ? ma.y : mb.y;
-        const float threshold = ma.z < mb.z ? ma.z : mb.z;
-        d.mat[pos] = make_float4(friction, restitution, threshold, 0.0f);
-        d.mgeo[pos] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        d.mpts[pos] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        d.mimp[pos] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        d.mids[pos] = make_uint4(0u, 0u, 0u, 0u);
+        init_contact(w, w.c_alt, pos, key, fx);
     }
 }
 

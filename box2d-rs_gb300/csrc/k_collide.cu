@@ -15,33 +15,9 @@
  * Algorithmic bytes per evaluated contact: ~116 B of contact/manifold state + two
  * 144-byte shape records + two body transforms.
  */
-#include "b2g_internal.h"
+#include "b2g_contact.cuh"
 
 namespace b2g {
-
-__device__ __forceinline__ void wake_body(const DevWorld& w, int b) {
-    uint32_t f = w.b_flags[b];
-    if ((f & BF_TYPE_MASK) == BODY_STATIC) return;
-    if (!(f & BF_AWAKE)) {
-        atomicOr(&w.b_flags[b], BF_AWAKE);
-        w.b_vel[b].w = 0.0f;  /* sleep_time = 0 */
-    }
-}
-
-__device__ __forceinline__ void push_event(const DevWorld& w, int kind, int fa, int fb) {
-    int slot = atomicAdd(&w.cnt[CNT_EVENTS], 1);
-    if (slot < w.event_cap) w.events[slot] = make_int4(kind, fa, fb, 0);
-    else atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_EVENT_OVERFLOW);
-}
-
-__device__ __forceinline__ Xf load_xf(const DevWorld& w, int b) {
-    float4 x = w.b_xf[b];
-    Xf r;
-    r.p = mk(x.x, x.y);
-    r.q.s = x.z;
-    r.q.c = x.w;
-    return r;
-}
 
 __global__ void __launch_bounds__(256) k_collide(DevWorld w, StepParams sp) {
     const int n = w.cnt[CNT_CONTACTS];
@@ -69,51 +45,7 @@ __global__ void __launch_bounds__(256) k_collide(DevWorld w, StepParams sp) {
             w.c.flags[i] = (flags | CF_DEAD) & ~CF_TOUCHING;
             continue;
         }
-        flags |= CF_ENABLED;
-        bool touching = false;
-        if (flags & CF_SENSOR) {
-            /* sensor overlap tests (GJK) are outside the GPU path: sensors never touch */
-            w.c.mids[i] = make_uint4(ids.x, ids.y, ids.z & 0xffu, ids.w);
-        } else {
-            const int kind = (int)((flags >> CF_KIND_SHIFT) & 7u);
-            const Xf xfA = load_xf(w, bd.x);
-            const Xf xfB = load_xf(w, bd.y);
-            const ShapeRec sa = w.f_shape[fx.x];
-            const ShapeRec sb = w.f_shape[fx.y];
-            Manifold m;
-            m.type = MANIFOLD_CIRCLES;
-            m.count = 0;
-            m.ln = mk(0.0f, 0.0f);
-            m.lp = mk(0.0f, 0.0f);
-            m.p[0] = m.p[1] = mk(0.0f, 0.0f);
-            m.id[0] = m.id[1] = 0u;
-            evaluate(kind, m, sa, xfA, sb, xfB);
-            const float4 oldimp = w.c.mimp[i];
-            float ni[2] = {0.0f, 0.0f}, ti[2] = {0.0f, 0.0f};
-            for (int p = 0; p < m.count; ++p) {
-                if (old_count > 0 && ids.x == m.id[p]) {
-                    ni[p] = oldimp.x;
-                    ti[p] = oldimp.y;
-                } else if (old_count > 1 && ids.y == m.id[p]) {
-                    ni[p] = oldimp.z;
-                    ti[p] = oldimp.w;
-                }
-            }
-            touching = m.count > 0;
-            w.c.mgeo[i] = make_float4(m.ln.x, m.ln.y, m.lp.x, m.lp.y);
-            w.c.mpts[i] = make_float4(m.p[0].x, m.p[0].y, m.p[1].x, m.p[1].y);
-            w.c.mimp[i] = make_float4(ni[0], ti[0], ni[1], ti[1]);
-            w.c.mids[i] = make_uint4(m.id[0], m.id[1], (uint32_t)m.type | ((uint32_t)m.count << 8), ids.w);
-            if (touching != was_touching) {
-                wake_body(w, bd.x);
-                wake_body(w, bd.y);
-            }
-        }
-        w.c.flags[i] = touching ? (flags | CF_TOUCHING) : (flags & ~CF_TOUCHING);
-        if (sp.record_events) {
-            if (!was_touching && touching) push_event(w, 0, fx.x, fx.y);
-            if (was_touching && !touching) push_event(w, 1, fx.x, fx.y);
-        }
+        contact_update(w, sp.record_events != 0, i, flags, fx, bd, ids);
     }
 }
 

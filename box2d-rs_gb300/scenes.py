@@ -13,6 +13,7 @@ stream, so the GPU world and the CPU oracle receive identical f32 inputs.
                  3-8-gons of size 0.1-0.6) above their own ground
   throw_stack    8 x 8 stack of boxes (half-extent 0.25) and a circle projectile (r 0.5)
   hello_world    box2d-rs tests/test.rs:26-102
+  toi_rain       fast bodies (60-250 m/s) onto thin static plates, for continuous physics
 """
 from __future__ import annotations
 
@@ -348,6 +349,101 @@ def hello_world():
     s = _scene("hello_world", bodies, fixtures, 60, vi=6, pi=2)
     s["allow_sleep"] = True
     return s
+
+
+def toi_rain(n=64, seed=7, steps=120, bullets=2, kinematic=True):
+    """Fast bodies rained onto thin static plates (continuous physics): circles, boxes and 3-8-gons
+    with downward speeds of 60-250 m/s over 0.1 m thick static boxes and an edge floor, so that a
+    step without time of impact would carry them through; a few bullets and a sliding kinematic
+    plate add the dynamic-versus-bullet and kinematic cases."""
+    rng = SplitMix64(seed)
+    nk = 1 if kinematic else 0
+    ns = 4
+    bodies = b2g.body_defs(ns + nk + n)
+    bodies["allow_sleep"] = 0
+    fixtures = []
+    # statics: floor edge, thin plate, two thin walls
+    f = b2g.fixture_defs(1)
+    f["body"] = 0
+    f["shape_type"] = b2g.EDGE
+    f["vertices"][0, 1] = (-30.0, -4.0)
+    f["vertices"][0, 2] = (30.0, -4.0)
+    f["friction"] = 0.5
+    fixtures.append(f)
+    for b, pos, half in ((1, (0.0, 0.0), (20.0, 0.05)), (2, (-20.0, 10.0), (0.05, 12.0)), (3, (20.0, 10.0), (0.05, 12.0))):
+        bodies[b]["position"] = pos
+        f = b2g.fixture_defs(1)
+        f["body"] = b
+        f["shape_type"] = b2g.POLYGON
+        f["polygon_mode"] = b2g.POLYGON_BOX
+        f["box_half_extents"] = half
+        f["friction"] = 0.5
+        fixtures.append(f)
+    if kinematic:
+        k = ns
+        bodies[k]["type"] = b2g.KINEMATIC
+        bodies[k]["position"] = (-8.0, 6.0)
+        bodies[k]["linear_velocity"] = (3.0, 0.0)
+        bodies[k]["angular_velocity"] = 0.2
+        f = b2g.fixture_defs(1)
+        f["body"] = k
+        f["shape_type"] = b2g.POLYGON
+        f["polygon_mode"] = b2g.POLYGON_BOX
+        f["box_half_extents"] = (3.0, 0.05)
+        f["friction"] = 0.5
+        fixtures.append(f)
+    first = ns + nk
+    idx = np.arange(first, first + n)
+    bodies["type"][idx] = b2g.DYNAMIC
+    px = rng.uniform(n, -18.0, 18.0)
+    py = rng.uniform(n, 8.0, 40.0)
+    vx = rng.uniform(n, -20.0, 20.0)
+    vy = -rng.uniform(n, 60.0, 250.0)
+    ang = rng.uniform(n, 0.0, 2.0 * math.pi)
+    bodies["position"][idx] = np.stack([px, py], 1).astype(F32)
+    bodies["angle"][idx] = ang.astype(F32)
+    bodies["linear_velocity"][idx] = np.stack([vx, vy], 1).astype(F32)
+    bodies["angular_velocity"][idx] = rng.uniform(n, -5.0, 5.0).astype(F32)
+    if bullets:
+        bodies["bullet"][idx[:bullets]] = 1
+    kind = rng.integers(n, 0, 2)
+    size = rng.uniform(n, 0.15, 0.5)
+    nv = rng.integers(n, 3, 8)
+    verts = _polygon_vertices(rng, n, size, nv)
+    f = b2g.fixture_defs(n)
+    f["body"] = idx
+    f["density"] = 1.0
+    f["friction"] = 0.4
+    for i in range(n):
+        if kind[i] == 0:
+            f[i]["shape_type"] = b2g.CIRCLE
+            f[i]["radius"] = size[i]
+        elif kind[i] == 1:
+            f[i]["shape_type"] = b2g.POLYGON
+            f[i]["polygon_mode"] = b2g.POLYGON_BOX
+            f[i]["box_half_extents"] = (size[i], 0.6 * size[i])
+        else:
+            f[i]["shape_type"] = b2g.POLYGON
+            f[i]["vertex_count"] = nv[i]
+            f[i]["vertices"][: nv[i]] = verts[i, : nv[i]]
+    fixtures.append(f)
+    return _scene("toi_rain", bodies, np.concatenate(fixtures), steps, continuous=True)
+
+
+def toi_rain_batch(seeds=(7, 8, 9, 10), n=32, steps=90):
+    """Independent toi_rain worlds in one batch (continuous physics per world)."""
+    bodies, fixtures, offset = [], [], 0
+    for w, seed in enumerate(seeds):
+        s = toi_rain(n=n, seed=seed, steps=steps)
+        b = s["bodies"].copy()
+        b["world_index"] = w
+        f = s["fixtures"].copy()
+        f["body"] += offset
+        offset += len(b)
+        bodies.append(b)
+        fixtures.append(f)
+    return _scene("toi_rain_batch", np.concatenate(bodies), np.concatenate(fixtures), steps, num_worlds=len(seeds),
+                  continuous=True)
 
 
 def build_world(world, scene):

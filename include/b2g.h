@@ -200,6 +200,11 @@ int b2g_set_awake(void* world, uint32_t body, int32_t flag);
 int b2g_set_gravity(void* world, b2g_vec2 gravity);
 int b2g_set_allow_sleeping(void* world, int32_t flag);
 int b2g_set_warm_starting(void* world, int32_t flag);
+/* Continuous physics (B2world::solve_toi, private/dynamics/b2_world.rs:534-901): after the
+ * discrete solve, time-of-impact events against static, kinematic and bullet bodies are solved
+ * in order of time. Off by default in this ABI (the reference's B2world starts with it on: a
+ * wrapper mirroring B2world::new sets it); not recorded by the tape (b2g_step fails while a tape
+ * records with it on). */
 int b2g_set_continuous_physics(void* world, int32_t flag);
 int b2g_set_auto_clear_forces(void* world, int32_t flag);
 int b2g_clear_forces(void* world);
@@ -214,6 +219,9 @@ int b2g_set_part_solve(void* world, int32_t flag);
 /* ---- introspection ---- */
 int b2g_get_profile(void* world, b2g_profile* out);       /* B2world::get_profile, src/b2_world.rs:268-270 */
 int b2g_get_counts(void* world, b2g_counts* out);         /* get_body_count / get_contact_count / get_proxy_count */
+/* Continuous physics: solid time-of-impact events solved since the world was made, and the
+ * iterations (events per world, at most) of the last step's pass. */
+int b2g_get_toi_stats(void* world, int32_t* events, int32_t* last_iterations);
 /* Device times (ms, CUDA events) of the last step's phases, n >= 7: initial broadphase (only
  * after fixtures were added), collide, islands + constraint list, colouring, solver kernel,
  * broadphase tree pass (keys, sort, hierarchy, traversal), contact merge. */
@@ -234,8 +242,8 @@ int b2g_set_contact_events(void* world, int32_t flag);
 int b2g_collide_pairs(const b2g_fixture_def* shape_a, const float* xf_a, const b2g_fixture_def* shape_b,
                       const float* xf_b, int32_t n, b2g_contact_info* out);
 
-/* Time of impact of n independent pairs of moving shapes on the GPU (not used by b2g_step: the
- * step runs without continuous physics), like the reference's public b2_time_of_impact
+/* Time of impact of n independent pairs of moving shapes on the GPU (the routine the step's
+ * continuous pass runs per contact), like the reference's public b2_time_of_impact
  * (src/b2_time_of_impact.rs:48-50, private/collision/b2_time_of_impact.rs:191-463) with its GJK
  * distance (private/collision/b2_distance.rs:331-440). A sweep is a body's motion over the
  * interval (B2Sweep, src/b2_math.rs): local centre of mass, centre and angle at the start

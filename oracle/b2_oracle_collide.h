@@ -97,5 +97,9 @@ void collide_polygons(Manifold& m, const Shape& a, const Xf& xfA, const Shape& b
 void collide_edge_circle(Manifold& m, const Shape& a, const Xf& xfA, const Shape& b, const Xf& xfB);
 void collide_edge_polygon(Manifold& m, const Shape& a, const Xf& xfA, const Shape& b, const Xf& xfB);
 
+/* b2_time_of_impact of two shapes (child 0) on their sweeps; state as B2G_TOI_* (b2_oracle_toi.cpp) */
+void time_of_impact_shapes(const Shape& a, const Sweep& sa, const Shape& b, const Sweep& sb, float t_max, int& state,
+                           float& t);
+
 }  // namespace ora
 #endif

@@ -29,6 +29,9 @@ constexpr float kMaxTranslationSquared = kMaxTranslation * kMaxTranslation;
 constexpr float kMaxRotation = 0.5f * kPi;
 constexpr float kMaxRotationSquared = kMaxRotation * kMaxRotation;
 constexpr float kBaumgarte = 0.2f;
+constexpr float kToiBaumgarte = 0.75f;
+constexpr int kMaxSubSteps = 8;
+constexpr int kMaxToiContacts = 32;
 constexpr float kTimeToSleep = 0.5f;
 constexpr float kLinearSleepTolerance = 0.01f;
 constexpr float kAngularSleepTolerance = 2.0f / 180.0f * kPi;

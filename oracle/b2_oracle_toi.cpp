@@ -477,6 +477,14 @@ Sweep sweep_of(const b2g_sweep& s) {
 }
 
 }  // namespace
+
+/* the time of impact of two shapes (child 0) on their sweeps, for the world's solve_toi */
+void time_of_impact_shapes(const Shape& a, const Sweep& sa, const Shape& b, const Sweep& sb, float t_max, int& state,
+                           float& t) {
+    const Proxy pa = proxy_of(a), pb = proxy_of(b);
+    time_of_impact(pa, sa, pb, sb, t_max, state, t);
+}
+
 }  // namespace ora
 
 extern "C" int ora_time_of_impact(const b2g_fixture_def* da, const b2g_sweep* sa, const b2g_fixture_def* db,

@@ -83,6 +83,9 @@ struct Contact {
     int fa = -1, fb = -1;
     Manifold m;
     bool touching = false, enabled = true, island_flag = false;
+    bool toi_flag = false;   /* solve_toi: toi holds a valid time of impact */
+    int toi_count = 0;
+    float toi = 1.0f;
     float friction = 0, restitution = 0, threshold = 0, tangent_speed = 0;
     int prev = -1, next = -1;
     bool alive = false;
@@ -150,6 +153,8 @@ struct World {
     int hook_misses = 0;
     std::vector<uint64_t> last_order;  /* island contact order solved last step */
     int islands_solved = 0;
+    int toi_events = 0;                /* solid time-of-impact events solved so far */
+    bool toi_key_order = false;        /* solve_toi takes ties and island contacts in key order */
     /* island scratch */
     std::vector<int> isl_bodies, isl_contacts, stack;
     std::vector<Position> pos;
@@ -998,6 +1003,313 @@ static void solve(World& w, const Step& step) {
     w.profile.broadphase = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
+/* ---- continuous physics ---- */
+
+/* B2Sweep::advance, src/b2_math.rs:773-779 */
+static void sweep_advance(Sweep& s, float alpha) {
+    const float beta = (alpha - s.alpha0) / (1.0f - s.alpha0);
+    s.c0 += beta * (s.c - s.c0);
+    s.a0 += beta * (s.a - s.a0);
+    s.alpha0 = alpha;
+}
+
+/* B2body::advance, src/b2_body.rs:979-986 */
+static void body_advance(Body& b, float alpha) {
+    sweep_advance(b.sweep, alpha);
+    b.sweep.c = b.sweep.c0;
+    b.sweep.a = b.sweep.a0;
+    b.xf.q = rot(b.sweep.a);
+    b.xf.p = b.sweep.c - mul(b.xf.q, b.sweep.local_center);
+}
+
+/* the contact's key in the GPU's contact table: (smaller proxy id, larger proxy id) */
+static uint64_t contact_proxy_key(const World& w, const Contact& c) {
+    uint32_t p = (uint32_t)w.fixtures[c.fa].proxy, q = (uint32_t)w.fixtures[c.fb].proxy;
+    if (p > q) std::swap(p, q);
+    return ((uint64_t)p << 32) | q;
+}
+
+/* solve_toi_position_constraints, b2_contact_solver_private.rs:733-823: only the two bodies of
+ * the event move */
+static bool solve_toi_position(World& w, int toiA, int toiB) {
+    float minSeparation = 0.0f;
+    for (const PositionConstraint& pc : w.pcs) {
+        Vec2 lcA = pc.lcA, lcB = pc.lcB;
+        float mA = 0.0f, iA = 0.0f;
+        if (pc.ia == toiA || pc.ia == toiB) {
+            mA = pc.ma;
+            iA = pc.IA;
+        }
+        float mB = 0.0f, iB = 0.0f;
+        if (pc.ib == toiA || pc.ib == toiB) {
+            mB = pc.mb;
+            iB = pc.IB;
+        }
+        Vec2 cA = w.pos[pc.ia].c;
+        float aA = w.pos[pc.ia].a;
+        Vec2 cB = w.pos[pc.ib].c;
+        float aB = w.pos[pc.ib].a;
+        for (int j = 0; j < pc.count; ++j) {
+            Xf xfA, xfB;
+            xfA.q = rot(aA);
+            xfB.q = rot(aB);
+            xfA.p = cA - mul(xfA.q, lcA);
+            xfB.p = cB - mul(xfB.q, lcB);
+            Vec2 normal, point;
+            float separation;
+            position_manifold(pc, xfA, xfB, j, normal, point, separation);
+            Vec2 rA = point - cA;
+            Vec2 rB = point - cB;
+            minSeparation = bmin(minSeparation, separation);
+            float C = bclamp(kToiBaumgarte * (separation + kLinearSlop), -kMaxLinearCorrection, 0.0f);
+            float rnA = cross(rA, normal);
+            float rnB = cross(rB, normal);
+            float K = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+            float impulse = K > 0.0f ? -C / K : 0.0f;
+            Vec2 P = impulse * normal;
+            cA -= mA * P;
+            aA -= iA * cross(rA, P);
+            cB += mB * P;
+            aB += iB * cross(rB, P);
+        }
+        w.pos[pc.ia].c = cA;
+        w.pos[pc.ia].a = aA;
+        w.pos[pc.ib].c = cB;
+        w.pos[pc.ib].a = aB;
+    }
+    return minSeparation >= -1.5f * kLinearSlop;
+}
+
+/* B2island::solve_toi, b2_island_private.rs:330-458 */
+static void solve_toi_island(World& w, const Step& sub, int toiA, int toiB) {
+    const int nb = (int)w.isl_bodies.size();
+    w.pos.resize(nb);
+    w.vel.resize(nb);
+    for (int i = 0; i < nb; ++i) {
+        const Body& b = w.bodies[w.isl_bodies[i]];
+        w.pos[i].c = b.sweep.c;
+        w.pos[i].a = b.sweep.a;
+        w.vel[i].v = b.v;
+        w.vel[i].w = b.w;
+    }
+    /* B2contactSolver::new (the velocity part is initialised again below, after the position
+     * iterations move the bodies; without warm starting both passes start from zero impulses) */
+    init_constraints(w, sub);
+    for (int it = 0; it < sub.pi; ++it)
+        if (solve_toi_position(w, toiA, toiB)) break;
+    /* leap of faith to the new safe state */
+    Body& A = w.bodies[w.isl_bodies[toiA]];
+    Body& B = w.bodies[w.isl_bodies[toiB]];
+    A.sweep.c0 = w.pos[toiA].c;
+    A.sweep.a0 = w.pos[toiA].a;
+    B.sweep.c0 = w.pos[toiB].c;
+    B.sweep.a0 = w.pos[toiB].a;
+    init_constraints(w, sub);
+    for (int it = 0; it < sub.vi; ++it) solve_velocity(w);
+    const float h = sub.dt;
+    for (int i = 0; i < nb; ++i) {
+        Vec2 c = w.pos[i].c;
+        float a = w.pos[i].a;
+        Vec2 v = w.vel[i].v;
+        float wv = w.vel[i].w;
+        Vec2 translation = h * v;
+        if (dot(translation, translation) > kMaxTranslationSquared) {
+            float ratio = kMaxTranslation / length(translation);
+            v *= ratio;
+        }
+        float rotation = h * wv;
+        if (rotation * rotation > kMaxRotationSquared) {
+            float ratio = kMaxRotation / std::fabs(rotation);
+            wv *= ratio;
+        }
+        c += h * v;
+        a += h * wv;
+        w.pos[i].c = c;
+        w.pos[i].a = a;
+        w.vel[i].v = v;
+        w.vel[i].w = wv;
+        Body& b = w.bodies[w.isl_bodies[i]];
+        b.sweep.c = c;
+        b.sweep.a = a;
+        b.v = v;
+        b.w = wv;
+        synchronize_transform(b);
+    }
+}
+
+/* B2world::solve_toi, private/dynamics/b2_world.rs:534-901 (no sub-stepping: every step is
+ * complete). With toi_key_order set, two list-order choices follow the GPU's order instead: the
+ * first time of impact is the smallest (alpha, contact key), and an event's island takes its
+ * other contacts in key order. */
+static void solve_toi(World& w, const Step& step) {
+    for (int b = w.body_head; b >= 0; b = w.bodies[b].next) {
+        w.bodies[b].island_flag = false;
+        w.bodies[b].sweep.alpha0 = 0.0f;
+    }
+    for (int c = w.contact_head; c >= 0; c = w.contacts[c].next) {
+        Contact& C = w.contacts[c];
+        C.toi_flag = false;
+        C.island_flag = false;
+        C.toi_count = 0;
+        C.toi = 1.0f;
+    }
+    const bool key_order = w.toi_key_order;
+    for (;;) {
+        int minContact = -1;
+        float minAlpha = 1.0f;
+        uint64_t minKey = 0;
+        for (int id = w.contact_head; id >= 0; id = w.contacts[id].next) {
+            Contact& c = w.contacts[id];
+            if (!c.enabled) continue;
+            if (c.toi_count > kMaxSubSteps) continue;
+            float alpha;
+            if (c.toi_flag) {
+                alpha = c.toi;
+            } else {
+                const Fixture& FA = w.fixtures[c.fa];
+                const Fixture& FB = w.fixtures[c.fb];
+                if (FA.sensor || FB.sensor) continue;
+                Body& bA = w.bodies[FA.body];
+                Body& bB = w.bodies[FB.body];
+                const bool activeA = bA.awake && bA.type != STATIC;
+                const bool activeB = bB.awake && bB.type != STATIC;
+                if (!activeA && !activeB) continue;
+                const bool collideA = bA.bullet || bA.type != DYNAMIC;
+                const bool collideB = bB.bullet || bB.type != DYNAMIC;
+                if (!collideA && !collideB) continue;
+                float alpha0 = bA.sweep.alpha0;
+                if (bA.sweep.alpha0 < bB.sweep.alpha0) {
+                    alpha0 = bB.sweep.alpha0;
+                    sweep_advance(bA.sweep, alpha0);
+                } else if (bB.sweep.alpha0 < bA.sweep.alpha0) {
+                    alpha0 = bA.sweep.alpha0;
+                    sweep_advance(bB.sweep, alpha0);
+                }
+                int state;
+                float beta;
+                time_of_impact_shapes(FA.shape, bA.sweep, FB.shape, bB.sweep, 1.0f, state, beta);
+                if (state == B2G_TOI_TOUCHING) alpha = bmin(alpha0 + (1.0f - alpha0) * beta, 1.0f);
+                else alpha = 1.0f;
+                c.toi = alpha;
+                c.toi_flag = true;
+            }
+            if (alpha < minAlpha) {
+                minContact = id;
+                minAlpha = alpha;
+                minKey = contact_proxy_key(w, c);
+            } else if (key_order && minContact >= 0 && alpha == minAlpha) {
+                const uint64_t k = contact_proxy_key(w, c);
+                if (k < minKey) {
+                    minContact = id;
+                    minKey = k;
+                }
+            }
+        }
+        if (minContact < 0 || 1.0f - 10.0f * kEpsilon < minAlpha) break;
+
+        Contact& mc = w.contacts[minContact];
+        const int ia = w.fixtures[mc.fa].body, ib = w.fixtures[mc.fb].body;
+        Body& bA = w.bodies[ia];
+        Body& bB = w.bodies[ib];
+        const Sweep backup1 = bA.sweep, backup2 = bB.sweep;
+        body_advance(bA, minAlpha);
+        body_advance(bB, minAlpha);
+        update_contact(w, minContact);
+        mc.toi_flag = false;
+        ++mc.toi_count;
+        if (!mc.enabled || !mc.touching) {
+            mc.enabled = false;
+            bA.sweep = backup1;
+            bB.sweep = backup2;
+            synchronize_transform(bA);
+            synchronize_transform(bB);
+            continue;
+        }
+        set_awake(bA, true);
+        set_awake(bB, true);
+        w.isl_bodies.clear();
+        w.isl_contacts.clear();
+        bA.island_index = 0;
+        w.isl_bodies.push_back(ia);
+        bB.island_index = 1;
+        w.isl_bodies.push_back(ib);
+        w.isl_contacts.push_back(minContact);
+        bA.island_flag = true;
+        bB.island_flag = true;
+        mc.island_flag = true;
+
+        /* the contacts of the event's dynamic bodies: (body, edge) in list order, body A's first */
+        std::vector<std::pair<int, int>> cand;
+        for (int bi : {ia, ib}) {
+            if (w.bodies[bi].type != DYNAMIC) continue;
+            for (int e = w.bodies[bi].edge_head; e >= 0; e = w.edges[e].next) cand.emplace_back(bi, e);
+        }
+        if (key_order) {
+            /* each contact once (a second visit through the other body changes nothing), by key */
+            std::vector<std::pair<int, int>> uniq;
+            for (const auto& be : cand) {
+                bool seen = false;
+                for (const auto& u : uniq)
+                    if (w.edges[u.second].contact == w.edges[be.second].contact) seen = true;
+                if (!seen) uniq.push_back(be);
+            }
+            std::stable_sort(uniq.begin(), uniq.end(), [&](const std::pair<int, int>& x, const std::pair<int, int>& y) {
+                return contact_proxy_key(w, w.contacts[w.edges[x.second].contact]) <
+                       contact_proxy_key(w, w.contacts[w.edges[y.second].contact]);
+            });
+            cand.swap(uniq);
+        }
+        for (const auto& be : cand) {
+            Body& body = w.bodies[be.first];
+            const int ci = w.edges[be.second].contact;
+            const int oi = w.edges[be.second].other;
+            Contact& c = w.contacts[ci];
+            if (c.island_flag) continue;
+            Body& other = w.bodies[oi];
+            if (other.type == DYNAMIC && !body.bullet && !other.bullet) continue;
+            if (w.fixtures[c.fa].sensor || w.fixtures[c.fb].sensor) continue;
+            const Sweep backup = other.sweep;
+            if (!other.island_flag) body_advance(other, minAlpha);
+            update_contact(w, ci);
+            if (!c.enabled || !c.touching) {
+                other.sweep = backup;
+                synchronize_transform(other);
+                continue;
+            }
+            c.island_flag = true;
+            w.isl_contacts.push_back(ci);
+            if (other.island_flag) continue;
+            other.island_flag = true;
+            if (other.type != STATIC) set_awake(other, true);
+            other.island_index = (int)w.isl_bodies.size();
+            w.isl_bodies.push_back(oi);
+        }
+
+        Step sub;
+        sub.dt = (1.0f - minAlpha) * step.dt;
+        sub.inv_dt = 1.0f / sub.dt;
+        sub.dt_ratio = 1.0f;
+        sub.pi = 20;
+        sub.vi = step.vi;
+        sub.warm = false;
+        solve_toi_island(w, sub, bA.island_index, bB.island_index);
+        ++w.toi_events;
+
+        for (int bi : w.isl_bodies) {
+            Body& b = w.bodies[bi];
+            b.island_flag = false;
+            if (b.type != DYNAMIC) continue;
+            synchronize_fixtures(w, b);
+            for (int e = b.edge_head; e >= 0; e = w.edges[e].next) {
+                Contact& c = w.contacts[w.edges[e].contact];
+                c.toi_flag = false;
+                c.island_flag = false;
+            }
+        }
+        find_new_contacts(w);
+    }
+}
+
 /* B2world::step, private/dynamics/b2_world.rs:903-959 */
 static void step(World& w, float dt, int vi, int pi) {
     auto t0 = std::chrono::steady_clock::now();
@@ -1020,6 +1332,14 @@ static void step(World& w, float dt, int vi, int pi) {
     if (dt > 0.0f) {
         solve(w, s);
         w.profile.solve = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t2).count();
+    }
+    if (w.continuous && dt > 0.0f) {
+        /* the recorded pair set stays the one of the step's own pair update */
+        std::vector<Pair> pairs = w.last_pairs;
+        std::vector<uint8_t> moved = w.last_moved;
+        solve_toi(w, s);
+        w.last_pairs.swap(pairs);
+        w.last_moved.swap(moved);
     }
     if (dt > 0.0f) w.inv_dt0 = s.inv_dt;
     if (w.auto_clear) {
@@ -1057,10 +1377,9 @@ int ora_world_destroy(void* p) {
 
 int ora_set_flags(void* p, int allow_sleep, int warm_starting, int continuous, int auto_clear) {
     World& w = *(World*)p;
-    if (continuous) return B2G_ERR_UNSUPPORTED;
     w.allow_sleep = allow_sleep != 0;
     w.warm_starting = warm_starting != 0;
-    w.continuous = false;
+    w.continuous = continuous != 0;
     w.auto_clear = auto_clear != 0;
     return 0;
 }
@@ -1242,6 +1561,17 @@ int ora_set_solver_order(void* p, const uint32_t* pairs, int n) {
 }
 
 int ora_get_hook_misses(void* p) { return ((World*)p)->hook_misses; }
+
+/* solid time-of-impact events solved since the world was made */
+int ora_get_toi_events(void* p) { return ((World*)p)->toi_events; }
+
+/* Ordering hook of solve_toi: ties of the first time of impact go to the smallest contact key and
+ * an event's island takes its other contacts in key order (the GPU's order), instead of the
+ * contact-list order. */
+int ora_set_toi_key_order(void* p, int flag) {
+    ((World*)p)->toi_key_order = flag != 0;
+    return 0;
+}
 
 int ora_get_solver_order(void* p, uint32_t* out, int cap, int* n) {
     World& w = *(World*)p;

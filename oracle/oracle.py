@@ -64,6 +64,8 @@ def load():
         "ora_get_proxies": [vp, vp, vp, vp, i32],
         "ora_set_solver_order": [vp, vp, i32],
         "ora_get_hook_misses": [vp],
+        "ora_get_toi_events": [vp],
+        "ora_set_toi_key_order": [vp, i32],
         "ora_get_solver_order": [vp, vp, i32, pi32],
         "ora_get_events": [vp, vp, i32, pi32],
         "ora_polygon_mass": [vp, vp],
@@ -135,8 +137,10 @@ def time_of_impact(defs_a, sweeps_a, defs_b, sweeps_b, t_max=None):
 class OracleWorld:
     """The CPU restatement of B2world; same method names as b2g.B2world."""
 
-    def __init__(self, gravity=(0.0, -10.0), allow_sleep=False, warm_starting=True, record_events=False):
+    def __init__(self, gravity=(0.0, -10.0), allow_sleep=False, warm_starting=True, record_events=False,
+                 continuous=False):
         self._lib = load()
+        self._continuous = continuous
         h = ctypes.c_void_p()
         self._lib.ora_world_create(gravity[0], gravity[1], ctypes.byref(h))
         self._h = h
@@ -148,7 +152,7 @@ class OracleWorld:
         self._lib.ora_set_record_events(self._h, int(record_events))
 
     def _apply_flags(self):
-        rc = self._lib.ora_set_flags(self._h, int(self._allow_sleep), int(self._warm), 0, 1)
+        rc = self._lib.ora_set_flags(self._h, int(self._allow_sleep), int(self._warm), int(self._continuous), 1)
         assert rc == 0
 
     def close(self):
@@ -169,6 +173,18 @@ class OracleWorld:
     def set_warm_starting(self, flag):
         self._warm = bool(flag)
         self._apply_flags()
+
+    def set_continuous_physics(self, flag):
+        self._continuous = bool(flag)
+        self._apply_flags()
+
+    def set_toi_key_order(self, flag):
+        """solve_toi breaks ties and orders an event's island contacts by contact key (the GPU's order)."""
+        self._lib.ora_set_toi_key_order(self._h, int(bool(flag)))
+
+    def toi_events(self):
+        """Solid time-of-impact events solved since the world was made."""
+        return self._lib.ora_get_toi_events(self._h)
 
     def create_bodies(self, defs):
         defs = np.ascontiguousarray(defs, b2g.BODY_DEF)

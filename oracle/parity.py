@@ -68,6 +68,13 @@ class MultiOracle:
     def hook_misses(self):
         return sum(o.hook_misses() for o, _, _ in self.worlds)
 
+    def set_toi_key_order(self, flag):
+        for o, _, _ in self.worlds:
+            o.set_toi_key_order(flag)
+
+    def toi_events(self):
+        return sum(o.toi_events() for o, _, _ in self.worlds)
+
     def get_body_states(self):
         out = np.zeros(self.n_bodies, b2g.BODY_STATE)
         for o, bidx, _ in self.worlds:
@@ -106,17 +113,22 @@ def make_pair(scene, record_pairs=True, record_events=False, warm_starting=True)
     gpu = b2g.B2world(gravity=scene["gravity"], num_worlds=scene.get("num_worlds", 1))
     gpu.set_allow_sleeping(scene.get("allow_sleep", False))
     gpu.set_warm_starting(warm_starting)
-    gpu.set_continuous_physics(False)
+    continuous = bool(scene.get("continuous", False))
+    gpu.set_continuous_physics(continuous)
     gpu.set_record_pairs(record_pairs)
     gpu.set_contact_events(record_events)
     gpu.set_part_solve(scene.get("part_solve", True))
-    kw = dict(allow_sleep=scene.get("allow_sleep", False), warm_starting=warm_starting, record_events=record_events)
+    kw = dict(allow_sleep=scene.get("allow_sleep", False), warm_starting=warm_starting, record_events=record_events,
+              continuous=continuous)
     scenes.build_world(gpu, scene)
     if scene.get("num_worlds", 1) > 1:
         ora = MultiOracle(scene, **kw)
     else:
         ora = oracle.OracleWorld(gravity=scene["gravity"], **kw)
         scenes.build_world(ora, scene)
+    # solve_toi's list-order choices (ties of the first time of impact, an event's island order)
+    # follow the GPU's key order
+    ora.set_toi_key_order(True)
     return gpu, ora
 
 

@@ -68,15 +68,21 @@ def test_empty_and_zero_dt(built):
     assert np.array_equal(before["position"], after["position"])
 
 
-def test_continuous_physics_is_refused(built):
+def test_continuous_physics_refused_while_taping(built):
+    """The tape does not record the continuous pass: stepping with both on is refused (-6), and
+    the world steps again once continuous physics is off."""
     w = b2g.B2world()
+    w.set_allow_sleeping(False)
     scenes.build_world(w, scenes.pyramid(rows=2))
+    w.step(np.float32(1 / 60), 8, 3)
+    w.tape_begin(4)
     w.set_continuous_physics(True)
     with pytest.raises(b2g.B2GError) as e:
         w.step(np.float32(1 / 60), 8, 3)
     assert e.value.code == -6
     w.set_continuous_physics(False)
     w.step(np.float32(1 / 60), 8, 3)
+    w.tape_end()
 
 
 def test_contact_capacity_overflow_reports(built):

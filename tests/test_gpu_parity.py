@@ -237,3 +237,60 @@ def test_compound_bodies_lockstep(built):
     for r in recs:
         _assert_step(r)
     assert max(r["constraints"] for r in recs) > 300
+
+
+def _toi_lockstep(s, steps):
+    recs, gpu, ora = parity.lockstep(s, steps)
+    for r in recs:
+        _assert_step(r)
+    events, _ = gpu.get_toi_stats()
+    assert events == ora.toi_events()
+    return recs, gpu, ora, events
+
+
+def test_continuous_rain_lockstep(built):
+    """Continuous physics: fast circles, boxes and polygons (2 bullets) onto thin static plates and
+    a kinematic plate. Every step bit-exact with the oracle's solve_toi, the same number of
+    time-of-impact events, and no body passes the plate."""
+    s = scenes.toi_rain(n=64, seed=7, steps=120)
+    _, gpu, _, events = _toi_lockstep(s, 120)
+    assert events > 100
+    st = gpu.get_body_states()
+    dyn = s["bodies"]["type"] == b2g.DYNAMIC
+    x, y = st["position"][dyn, 0], st["position"][dyn, 1]
+    assert not np.any((np.abs(x) < 19.5) & (y < 0.0))
+
+
+def test_continuous_equal_times_lockstep(built):
+    """A row of identical boxes with identical velocities meets the plate at identical times: the
+    event among equal times of impact is the smallest contact key on both sides."""
+    n = 12
+    bodies = b2g.body_defs(n + 1)
+    bodies["allow_sleep"] = 0
+    bodies[0]["position"] = (0.0, 0.0)
+    bodies[1:]["type"] = b2g.DYNAMIC
+    bodies[1:]["position"][:, 0] = np.linspace(-9.0, 9.0, n).astype(np.float32)
+    bodies[1:]["position"][:, 1] = 6.0
+    bodies[1:]["linear_velocity"] = (0.0, -150.0)
+    fx = [b2g.box_fixture(0, 12.0, 0.05, friction=0.5)]
+    fx += [b2g.box_fixture(i + 1, 0.3, 0.2, density=1.0, friction=0.5) for i in range(n)]
+    s = {"name": "toi_row", "bodies": bodies, "fixtures": np.concatenate(fx), "gravity": (0.0, -10.0),
+         "dt": np.float32(1.0 / 60.0), "vi": 8, "pi": 3, "steps": 40, "num_worlds": 1, "allow_sleep": False,
+         "n_dynamic": n, "continuous": True}
+    _, gpu, _, events = _toi_lockstep(s, 40)
+    assert events >= n
+    assert np.all(gpu.get_body_states()["position"][1:, 1] > 0.0)
+
+
+def test_continuous_batched_worlds_lockstep(built):
+    """Four toi_rain worlds in one batch: events of different worlds are solved side by side."""
+    s = scenes.toi_rain_batch(seeds=(7, 8, 9, 10), n=32, steps=90)
+    _, _, _, events = _toi_lockstep(s, 90)
+    assert events > 100
+
+
+def test_continuous_pyramid_lockstep(built):
+    """A settling pyramid with continuous physics on: every box-ground contact gets a time of impact
+    each step (slow landings may make events); bit-exact with the oracle's solve_toi."""
+    s = dict(scenes.pyramid(rows=8), continuous=True)
+    _toi_lockstep(s, 120)

@@ -101,3 +101,27 @@ def test_gpu_time_of_impact_matches_the_oracle(built, oracle_lib):
     assert np.array_equal(got["t"].view(np.uint32), ref["t"].view(np.uint32))
     states = np.bincount(ref["state"], minlength=5)
     assert states[b2g.TOI_TOUCHING] > 1000 and states[b2g.TOI_SEPARATED] > 1000 and states[b2g.TOI_OVERLAPPED] > 100
+
+
+def _rain_below_plate(continuous):
+    import scenes
+
+    s = scenes.toi_rain(n=64, seed=7, steps=120)
+    o = oracle.OracleWorld(gravity=s["gravity"], continuous=continuous)
+    o.set_toi_key_order(True)
+    scenes.build_world(o, s)
+    o.steps(s["dt"], s["vi"], s["pi"], s["steps"])
+    st = o.get_body_states()
+    dyn = s["bodies"]["type"] == b2g.DYNAMIC
+    x, y = st["position"][dyn, 0], st["position"][dyn, 1]
+    return int(((np.abs(x) < 19.5) & (y < 0.0)).sum()), o.toi_events()
+
+
+def test_oracle_solve_toi_stops_tunnelling(oracle_lib):
+    """B2world::solve_toi in the oracle: bodies at 60-250 m/s pass a 0.1 m static plate in a
+    discrete step, and none does with continuous physics on (hundreds of time-of-impact events)."""
+    oracle.set_trig(False)
+    passed, events = _rain_below_plate(False)
+    assert passed > 10 and events == 0
+    passed, events = _rain_below_plate(True)
+    assert passed == 0 and events > 100
