@@ -142,6 +142,7 @@ SWEEP = np.dtype([("local_center", "<f4", (2,)), ("c0", "<f4", (2,)), ("c", "<f4
                   ("a", "<f4"), ("alpha0", "<f4"), ("pad", "<f4")])
 TOI_OUTPUT = np.dtype([("state", "<i4"), ("t", "<f4")])
 TOI_UNKNOWN, TOI_FAILED, TOI_OVERLAPPED, TOI_TOUCHING, TOI_SEPARATED = range(5)
+TOI_SIDE_BY_SIDE, TOI_ONE_AT_A_TIME, TOI_RESTART_ON_ADVANCE = range(3)  # b2g_set_toi_schedule
 
 RAY_HIT = np.dtype([("fixture", "<i4"), ("point", "<f4", (2,)), ("normal", "<f4", (2,)), ("fraction", "<f4")])
 assert RAY_HIT.itemsize == 24
@@ -392,7 +393,9 @@ def load_library(path=LIB_PATH):
         "b2g_clear_forces": [vp],
         "b2g_get_profile": [vp, ctypes.POINTER(Profile)],
         "b2g_get_counts": [vp, ctypes.POINTER(Counts)],
-        "b2g_get_toi_stats": [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)],
+        "b2g_get_toi_stats": [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                              ctypes.POINTER(ctypes.c_int32)],
+        "b2g_set_toi_schedule": [vp, i32],
         "b2g_get_contacts": [vp, vp, i32, ctypes.POINTER(i32)],
         "b2g_get_events": [vp, vp, i32, ctypes.POINTER(i32)],
         "b2g_get_pairs": [vp, vp, i32, ctypes.POINTER(i32)],
@@ -655,10 +658,15 @@ class B2world:
         return c.as_dict()
 
     def get_toi_stats(self):
-        """(solid time-of-impact events since creation, iterations of the last step's pass)."""
-        e, it = ctypes.c_int32(0), ctypes.c_int32(0)
-        self._check(self._lib.b2g_get_toi_stats(self._h, ctypes.byref(e), ctypes.byref(it)))
-        return int(e.value), int(it.value)
+        """(solid time-of-impact events since creation, iterations of the last step's pass,
+        passes restarted one event at a time)."""
+        e, it, r = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
+        self._check(self._lib.b2g_get_toi_stats(self._h, ctypes.byref(e), ctypes.byref(it), ctypes.byref(r)))
+        return int(e.value), int(it.value), int(r.value)
+
+    def set_toi_schedule(self, schedule):
+        """TOI_SIDE_BY_SIDE (default), TOI_ONE_AT_A_TIME or TOI_RESTART_ON_ADVANCE."""
+        self._check(self._lib.b2g_set_toi_schedule(self._h, int(schedule)))
 
     def _get_list(self, fn, dtype, cap_hint, width=1):
         n = ctypes.c_int32(0)

@@ -93,6 +93,7 @@ struct World {
     b2g_vec2 gravity{0.0f, -10.0f};
     int num_worlds = 1;
     bool warm = true, continuous = false, allow_sleep = true, auto_clear = true;
+    int toi_schedule = 0;  /* B2G_TOI_SCHEDULE_* */
     bool record_events = false, record_pairs = false;
     bool new_contacts = false;
     float inv_dt0 = 0.0f;
@@ -552,13 +553,17 @@ int allocate(World* w, int nb, int nf) {
     A(d.bp_quad_box, 4 * (size_t)fix_cap); A(d.bp_quad_child, fix_cap);
     A(d.bp_world_root, 2 * (size_t)w->num_worlds); A(d.bp_world_first, 2 * (size_t)w->num_worlds);
     A(d.b_fix_off, (size_t)body_cap + 1); A(d.b_fix, fix_cap);
-    A(d.b_alpha0, body_cap); A(d.b_stamp, body_cap); A(d.b_inval, body_cap); A(d.b_sync, body_cap);
-    A(d.f_pmoved, fix_cap);
-    A(d.t_toi, contact_cap); A(d.t_when, contact_cap); A(d.t_count, contact_cap); A(d.t_stamp, contact_cap);
-    A(d.t_elig, contact_cap); A(d.t_hits, contact_cap); A(d.t_sync, body_cap);
-    A(d.t_moved, kToiMovedCap); A(d.t_pmoved, kToiPassMovedCap); A(d.t_nkey, kToiNewCap); A(d.t_nslot, kToiNewCap);
-    A(d.tw_alpha, w->num_worlds); A(d.tw_key, w->num_worlds); A(d.tw_event, w->num_worlds);
-    A(d.tw_ealpha, w->num_worlds); A(d.tw_cand, (size_t)w->num_worlds * (kToiCand + 1));
+    A(d.b_alpha0, body_cap); A(d.b_stamp, body_cap); A(d.b_event, body_cap); A(d.b_inval, body_cap);
+    A(d.b_cx, body_cap); A(d.b_sync, body_cap); A(d.b_best, body_cap); A(d.b_bkey, body_cap);
+    A(d.f_leaf, fix_cap);
+    A(d.t_toi, contact_cap); A(d.t_when, contact_cap); A(d.t_count, contact_cap);
+    A(d.t_elig, contact_cap); A(d.t_hits, contact_cap); A(d.t_hitx, contact_cap); A(d.t_sync, body_cap);
+    A(d.t_moved, fix_cap); A(d.t_nkey, kToiNewCap); A(d.t_nslot, kToiNewCap);
+    A(d.ev_contact, kToiEvCap); A(d.ev_alpha, kToiEvCap); A(d.ev_solid, kToiEvCap);
+    A(d.ev_cand, (size_t)kToiEvCap * (kToiCand + 1));
+    A(d.tw_alpha, w->num_worlds); A(d.tw_key, w->num_worlds); A(d.tw_salpha, w->num_worlds); A(d.tw_skey, w->num_worlds);
+    A(d.s_xf, body_cap); A(d.s_pos, body_cap); A(d.s_pos0, body_cap); A(d.s_vel, body_cap); A(d.s_flags, body_cap);
+    A(d.s_fat, fix_cap);
     A(d.events, d.event_cap);
     A(d.pairs, pair_cap);
     A(d.scan_tmp, 2 * (size_t)contact_cap + scan_tmp_size(contact_cap) + 64);
@@ -751,6 +756,7 @@ StepParams make_params(World* w, float dt, int vi, int pi) {
     sp.auto_clear = w->auto_clear ? 1 : 0;
     sp.record_events = w->record_events ? 1 : 0;
     sp.record_pairs = w->record_pairs ? 1 : 0;
+    sp.toi_schedule = w->toi_schedule;
     return sp;
 }
 
@@ -851,7 +857,7 @@ int step(World* w, float dt, int vi, int pi) {
         key.pi = pi;
         key.flags = sp.warm | (sp.allow_sleep << 1) | (sp.auto_clear << 2) | (sp.record_events << 3) |
                     (sp.record_pairs << 4) | ((w->tape && w->tape->recording) ? (1 << 5) : 0) |
-                    (w->continuous ? (1 << 6) : 0);
+                    (w->continuous ? (1 << 6) : 0) | (sp.toi_schedule << 7);
         key.generation = w->alloc_generation;
         key.n_bodies = w->d.n_bodies;
         key.n_fixtures = w->d.n_fixtures;
@@ -1402,6 +1408,14 @@ int b2g_set_continuous_physics(void* p, int32_t flag) {
     W(p)->continuous = flag != 0;
     return B2G_OK;
 }
+int b2g_set_toi_schedule(void* p, int32_t schedule) {
+    if (!p) return B2G_ERR_INVALID_ARG;
+    if (schedule < B2G_TOI_SCHEDULE_SIDE_BY_SIDE || schedule > B2G_TOI_SCHEDULE_RESTART_ON_ADVANCE)
+        return fail(W(p), B2G_ERR_INVALID_ARG, "unknown time-of-impact schedule");
+    W(p)->toi_schedule = schedule;
+    return B2G_OK;
+}
+
 int b2g_set_auto_clear_forces(void* p, int32_t flag) {
     if (!p) return B2G_ERR_INVALID_ARG;
     W(p)->auto_clear = flag != 0;
@@ -1515,11 +1529,12 @@ int b2g_get_counts(void* p, b2g_counts* out) {
     return B2G_OK;
 }
 
-int b2g_get_toi_stats(void* p, int32_t* events, int32_t* last_iterations) {
+int b2g_get_toi_stats(void* p, int32_t* events, int32_t* last_iterations, int32_t* restarts) {
     World* w = W(p);
-    if (!w || !events || !last_iterations) return B2G_ERR_INVALID_ARG;
+    if (!w || !events || !last_iterations || !restarts) return B2G_ERR_INVALID_ARG;
     *events = 0;
     *last_iterations = 0;
+    *restarts = 0;
     if (!w->allocated) return B2G_OK;
     int rc = check_status(w);
     if (rc != B2G_OK) return rc;
@@ -1527,6 +1542,7 @@ int b2g_get_toi_stats(void* p, int32_t* events, int32_t* last_iterations) {
     CUDA_OK(w, cudaMemcpy(cnt, w->d.cnt, sizeof(cnt), cudaMemcpyDeviceToHost));
     *events = cnt[CNT_TOI_EVENTS];
     *last_iterations = cnt[CNT_TOI_ITERS];
+    *restarts = cnt[CNT_TOI_ROLLBACKS];
     return B2G_OK;
 }
 

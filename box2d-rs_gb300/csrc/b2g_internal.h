@@ -87,14 +87,19 @@ enum {
     CNT_TAIL = 26,        /* colouring: constraints left to the single-block rounds */
     CNT_TOI_EVENTS = 27,  /* solid time-of-impact events solved since the world was made */
     CNT_TOI_ITERS = 28,   /* iterations of the last continuous pass */
+    CNT_TOI_PASSES = 29,  /* continuous passes run (their body marks are stamped with it) */
+    CNT_TOI_ROLLBACKS = 30, /* passes restarted in sequential order after a conflict */
     /* continuous pass (k_continuous.cu), zeroed before every pass: */
     CNT_TOI_FIRST = 32,
     CNT_TOI_NEW = 32,     /* contacts created by the pass (table slots [n, n + this)) */
     CNT_TOI_SYNC = 33,    /* bodies with a pending sweep advance */
     CNT_TOI_MOVED = 34,   /* proxies moved by this iteration's islands */
     CNT_TOI_HITS = 35,    /* contacts whose time of impact is an event candidate this iteration */
-    CNT_TOI_PMOVED = 36,  /* proxies moved so far in the pass */
-    CNT_TOI_LAST = 37,
+    CNT_TOI_NEV = 36,     /* events of this iteration */
+    CNT_TOI_CONFLICT = 37, /* two events of one iteration asked to advance one body to different alphas */
+    CNT_TOI_SNAP_EV = 38, /* CNT_EVENTS and CNT_TOI_EVENTS when the pass's snapshot was taken */
+    CNT_TOI_SNAP_TE = 39,
+    CNT_TOI_LAST = 40,
     CNT_SIZE = 48
 };
 
@@ -103,11 +108,10 @@ constexpr int kFirstFitColours = 64;
 constexpr int kColourTail = 256;   /* uncoloured constraints one block finishes colouring (one per thread) */
 constexpr int kMaxParts = 1024;    /* body parts of the part-local solve (at most one per solver block) */
 constexpr int kMaxPosIters = 64;
-/* continuous pass lists (k_continuous.cu): partner contacts of one event, proxies moved in one
- * iteration and in one pass, contacts created in one pass */
+/* continuous pass lists (k_continuous.cu): partner contacts of one event, events of one
+ * iteration, contacts created in one pass */
 constexpr int kToiCand = 64;
-constexpr int kToiMovedCap = 4096;
-constexpr int kToiPassMovedCap = 8192;
+constexpr int kToiEvCap = 4096;
 constexpr int kToiNewCap = 4096;
 
 struct Contacts {
@@ -134,6 +138,7 @@ struct StepParams {
     int record_pairs;
     int part_bodies;      /* part-local solve: bodies cached in shared memory per block */
     int part_slot_bytes;  /* part-local solve: shared memory per block for constraint slots */
+    int toi_schedule;     /* continuous pass: B2G_TOI_SCHEDULE_* */
 };
 
 struct DevWorld {
@@ -233,26 +238,36 @@ struct DevWorld {
     int* b_fix;                  /* fixtures grouped by body */
     float* b_alpha0;             /* the body sweep's alpha0 during the pass */
     int* b_stamp;                /* pass iteration that last put the body in an event's island */
+    int* b_event;                /* that event's slot */
     int* b_inval;                /* pass iteration whose island displaced the body (its contacts' times
                                     of impact are stale) */
+    int* b_cx;                   /* the pass (CNT_TOI_PASSES) in which the body was found touching a
+                                    kinematic or bullet body: its events are solved one at a time */
     uint32_t* b_sync;            /* pending advance of the body's sweep (alpha bits; 0: none) */
-    uint8_t* f_pmoved;           /* the proxy moved earlier in the pass (its LBVH leaf is stale) */
+    uint32_t* b_best;            /* the body's earliest event candidate this iteration (alpha bits) */
+    unsigned long long* b_bkey;  /* and its contact key */
+    int* f_leaf;                 /* the proxy's leaf in the step's LBVH */
     float* t_toi;                /* per contact: cached time of impact (alpha) */
     int* t_when;                 /* per contact: iteration that computed t_toi, -1 none */
     int* t_count;                /* per contact: time-of-impact events (toi_count) */
-    int* t_stamp;                /* per contact: iteration that put it in an event's island */
     uint8_t* t_elig;             /* per contact: non-sensor with a bullet or non-dynamic body */
     int* t_hits;                 /* contacts with an event-candidate alpha this iteration */
+    int* t_hitx;                 /* per hit: the dynamic body of a simple hit, -1 for others */
     int* t_sync;                 /* bodies with a pending sweep advance */
     int* t_moved;                /* proxies moved by this iteration's islands */
-    int* t_pmoved;               /* proxies moved in this pass */
     unsigned long long* t_nkey;  /* the pass's new contacts sorted by key (key, then table slot) */
     int* t_nslot;
-    uint32_t* tw_alpha;          /* per world: smallest event alpha of the iteration (bits; ~0: none) */
-    unsigned long long* tw_key;  /* per world: smallest contact key with that alpha */
-    int4* tw_event;              /* per world: (contact, body A, body B, iteration if solid else -1) */
-    float* tw_ealpha;            /* per world: the event's alpha */
-    int* tw_cand;                /* per world: count, then the other contacts of the event's bodies */
+    int* ev_contact;             /* per event of the iteration: its contact, alpha, and the iteration */
+    float* ev_alpha;             /* if the contact touched (a solid event), else -1 */
+    int* ev_solid;
+    int* ev_cand;                /* per event: count, then its bodies' partner contacts */
+    uint32_t* tw_alpha;          /* per world: earliest one-at-a-time candidate (alpha bits; ~0: none) */
+    unsigned long long* tw_key;  /* and its key */
+    uint32_t* tw_salpha;         /* per world: earliest candidate of a body solved side by side */
+    unsigned long long* tw_skey;
+    float4 *s_xf, *s_pos, *s_pos0, *s_vel;  /* the pass's snapshot of the bodies and proxies */
+    uint32_t* s_flags;
+    float4* s_fat;
     /* outputs for the host */
     int4* events;                /* kind, fixture a, fixture b, - */
     uint2* pairs;                /* recorded emitted pairs (fixture ids) */

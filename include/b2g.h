@@ -206,6 +206,16 @@ int b2g_set_warm_starting(void* world, int32_t flag);
  * wrapper mirroring B2world::new sets it); not recorded by the tape (b2g_step fails while a tape
  * records with it on). */
 int b2g_set_continuous_physics(void* world, int32_t flag);
+/* How the continuous pass orders its time-of-impact events (not in the reference: a schedule).
+ * Side by side (default): the earliest events of bodies that touch only static bodies are solved
+ * together, the others one at a time; a pass whose side-by-side events would advance one body's
+ * sweep to two different times restarts one event at a time. One at a time: every event alone, in
+ * the reference's order. Restart on advance: side by side, but the first sweep advance restarts the
+ * pass (exercises the restart). Bodies and manifolds are the same under all three. */
+#define B2G_TOI_SCHEDULE_SIDE_BY_SIDE 0
+#define B2G_TOI_SCHEDULE_ONE_AT_A_TIME 1
+#define B2G_TOI_SCHEDULE_RESTART_ON_ADVANCE 2
+int b2g_set_toi_schedule(void* world, int32_t schedule);
 int b2g_set_auto_clear_forces(void* world, int32_t flag);
 int b2g_clear_forces(void* world);
 /* Part-local solve (default on; not in the reference: a solver schedule). Each solver block owns a
@@ -219,9 +229,9 @@ int b2g_set_part_solve(void* world, int32_t flag);
 /* ---- introspection ---- */
 int b2g_get_profile(void* world, b2g_profile* out);       /* B2world::get_profile, src/b2_world.rs:268-270 */
 int b2g_get_counts(void* world, b2g_counts* out);         /* get_body_count / get_contact_count / get_proxy_count */
-/* Continuous physics: solid time-of-impact events solved since the world was made, and the
- * iterations (events per world, at most) of the last step's pass. */
-int b2g_get_toi_stats(void* world, int32_t* events, int32_t* last_iterations);
+/* Continuous physics: solid time-of-impact events solved since the world was made, the
+ * iterations of the last step's pass, and the passes restarted one event at a time. */
+int b2g_get_toi_stats(void* world, int32_t* events, int32_t* last_iterations, int32_t* restarts);
 /* Device times (ms, CUDA events) of the last step's phases, n >= 7: initial broadphase (only
  * after fixtures were added), collide, islands + constraint list, colouring, solver kernel,
  * broadphase tree pass (keys, sort, hierarchy, traversal), contact merge. */

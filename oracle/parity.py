@@ -115,6 +115,7 @@ def make_pair(scene, record_pairs=True, record_events=False, warm_starting=True)
     gpu.set_warm_starting(warm_starting)
     continuous = bool(scene.get("continuous", False))
     gpu.set_continuous_physics(continuous)
+    gpu.set_toi_schedule(scene.get("toi_schedule", b2g.TOI_SIDE_BY_SIDE))
     gpu.set_record_pairs(record_pairs)
     gpu.set_contact_events(record_events)
     gpu.set_part_solve(scene.get("part_solve", True))
@@ -184,9 +185,26 @@ def manifold_diff(gpu_contacts, ora_contacts):
     return key_mismatch, id_mismatch, worst
 
 
+def drop_transient(contacts, aabbs):
+    """Contacts without a manifold whose two fat AABBs no longer overlap are left out. With
+    continuous physics the GPU solves independent time-of-impact events side by side, and a pair of
+    two such bodies can be found (or missed) at a moment their fat AABBs overlap in one order of the
+    events and not in the other; such a contact never gets a manifold and the next collide removes
+    it. Contacts that overlap at the end of the step are found in either order."""
+    c = np.asarray(contacts)
+    if len(c) == 0:
+        return c
+    a = aabbs[c["fixture_a"].astype(np.int64)]
+    b = aabbs[c["fixture_b"].astype(np.int64)]
+    apart = (b[:, 0] - a[:, 2] > 0) | (b[:, 1] - a[:, 3] > 0) | (a[:, 0] - b[:, 2] > 0) | (a[:, 1] - b[:, 3] > 0)
+    keep = ~apart | (c["touching"] != 0) | (c["point_count"] > 0)
+    return c[keep]
+
+
 def lockstep(scene, steps, check_pairs=True, check_contacts=True, resync=False, on_step=None):
     """Step GPU and oracle in lockstep; returns per-step records of the differences."""
     gpu, ora = make_pair(scene, record_pairs=check_pairs)
+    continuous = bool(scene.get("continuous", False))
     dt, vi, pi = scene["dt"], scene["vi"], scene["pi"]
     out = []
     for k in range(steps):
@@ -204,14 +222,17 @@ def lockstep(scene, steps, check_pairs=True, check_contacts=True, resync=False, 
             rec["pairs_equal"] = gp == op
             rec["pairs"] = len(gp)
             rec["pair_sym_diff"] = len(gp ^ op)
-        if check_contacts:
-            km, im, worst = manifold_diff(gpu.get_contacts(), ora.get_contacts())
-            rec["contact_key_mismatch"] = len(km)
-            rec["contact_id_mismatch"] = im
-            rec["manifold_max_diff"] = worst
         ga, _ = gpu.get_proxies()
         oa, _, _ = ora.get_proxies()
         rec["fat_aabb_equal"] = bool(np.array_equal(ga, oa))
+        if check_contacts:
+            gc, oc = gpu.get_contacts(), ora.get_contacts()
+            if continuous:
+                gc, oc = drop_transient(gc, ga), drop_transient(oc, oa)
+            km, im, worst = manifold_diff(gc, oc)
+            rec["contact_key_mismatch"] = len(km)
+            rec["contact_id_mismatch"] = im
+            rec["manifold_max_diff"] = worst
         out.append(rec)
         if on_step is not None:
             on_step(rec)

@@ -239,13 +239,23 @@ def test_compound_bodies_lockstep(built):
     assert max(r["constraints"] for r in recs) > 300
 
 
-def _toi_lockstep(s, steps):
-    recs, gpu, ora = parity.lockstep(s, steps)
+def _toi_lockstep(s, steps, schedule=b2g.TOI_SIDE_BY_SIDE):
+    recs, gpu, ora = parity.lockstep(dict(s, toi_schedule=schedule), steps)
     for r in recs:
         _assert_step(r)
-    events, _ = gpu.get_toi_stats()
+    events, _, restarts = gpu.get_toi_stats()
     assert events == ora.toi_events()
     return recs, gpu, ora, events
+
+
+@pytest.mark.parametrize("schedule", [b2g.TOI_ONE_AT_A_TIME, b2g.TOI_RESTART_ON_ADVANCE])
+def test_continuous_rain_schedules_lockstep(built, schedule):
+    """The same rain, every event alone, and side by side with a restart at the first sweep
+    advance (the path a conflict takes): the same bits as the oracle each step."""
+    s = scenes.toi_rain(n=64, seed=7, steps=80)
+    _, gpu, _, _ = _toi_lockstep(s, 80, schedule)
+    if schedule == b2g.TOI_RESTART_ON_ADVANCE:
+        assert gpu.get_toi_stats()[2] > 0
 
 
 def test_continuous_rain_lockstep(built):
@@ -294,3 +304,12 @@ def test_continuous_pyramid_lockstep(built):
     each step (slow landings may make events); bit-exact with the oracle's solve_toi."""
     s = dict(scenes.pyramid(rows=8), continuous=True)
     _toi_lockstep(s, 120)
+
+
+def test_continuous_mixed_side_by_side_lockstep(built):
+    """3000 circles and polygons falling in a 60 x 60 m box of one-sided-free edges: many bodies
+    cross an edge within a step at once, so most iterations of the pass solve many events side by
+    side. Bit-exact with the oracle's one-event-at-a-time solve_toi."""
+    s = dict(scenes.mixed(n_circles=1500, n_polygons=1500, size=60.0, seed=29), continuous=True)
+    _, gpu, _, events = _toi_lockstep(s, 150)
+    assert events > 50
