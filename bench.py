@@ -379,6 +379,65 @@ def run_toi(n=1_000_000, sample=100_000, repeats=3):
             "states": np.bincount(got["state"], minlength=5).tolist()}
 
 
+def run_continuous(torch, flush, device, skip=300, steps=60, warmup=3, cpu_budget_s=8.0):
+    """The mixed-100k scene with continuous physics on (B2world::solve_toi after every step, the
+    reference's default): bodies reach the floor edge at up to ~100 m/s, hundreds of
+    time-of-impact events per step. GPU: device time of `steps` steps after `skip` untimed ones
+    (L2 flushed between steps). CPU: the oracle (libm sin/cos, 1 thread, continuous on) stepped from
+    the GPU's state at the start of the window."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    scene = scenes.mixed()
+    w = b2g.B2world(gravity=scene["gravity"], device=device)
+    w.set_allow_sleeping(False)
+    w.set_continuous_physics(True)
+    scenes.build_world(w, scene)
+    dt, vi, pi = scene["dt"], scene["vi"], scene["pi"]
+    for _ in range(skip):
+        w.step(dt, vi, pi)
+    w.synchronize()
+    aabbs, _ = w.get_proxies()
+    snap = {"bodies": w.get_body_states(), "aabbs": aabbs, "contacts": w.get_contacts()}
+    for _ in range(warmup):
+        w.step(dt, vi, pi)
+    w.synchronize()
+    e0 = w.get_toi_stats()[0]
+    total, toi_ms, iters = 0.0, 0.0, []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        w.step(dt, vi, pi)
+        prof = w.get_profile()
+        total += prof["step"]
+        toi_ms += prof["solve_toi"]
+        iters.append(w.get_toi_stats()[1])
+    events = w.get_toi_stats()[0] - e0
+    restarts = w.get_toi_stats()[2]
+    n_dyn = scene["n_dynamic"]
+    w.close()
+
+    oracle.set_trig(True)
+    o = oracle.OracleWorld(gravity=scene["gravity"], allow_sleep=False, continuous=True)
+    scenes.build_world(o, scene)
+    o.import_state(snap["bodies"], snap["aabbs"], snap["contacts"], np.float32(1.0) / dt)
+    n, t0 = 0, time.perf_counter()
+    while n < 5 and (n < 1 or time.perf_counter() - t0 < cpu_budget_s):
+        o.step(dt, vi, pi)
+        n += 1
+    cpu_s = time.perf_counter() - t0
+    cpu_events = o.toi_events()
+    o.close()
+    return {"metric": "body-steps/s with continuous physics", "value": n_dyn * steps / (total / 1000.0),
+            "unit": "body-steps/s", "ms_per_step": total / steps, "solve_toi_ms_per_step": toi_ms / steps,
+            "window": f"steps {skip + warmup}-{skip + warmup + steps} of the mixed-100k scene",
+            "toi_events_per_step": events / steps, "pass_iterations_max": max(iters), "restarts": restarts,
+            "cpu_baseline": {"value": n_dyn * n / cpu_s, "unit": "body-steps/s", "cores": 1, "kind": "port",
+                             "sample": f"oracle (libm sin/cos, 1 thread, solve_toi on) stepped {n} steps from the "
+                                       f"GPU's state at step {skip}: {cpu_events / n:.0f} events per step, "
+                                       f"{cpu_s:.1f} s"}}
+
+
 def run_adjoint(torch, flush, device, steps=240, seeds=512, repeats=3):
     """Differentiable throw-and-stack (64 boxes + a circle projectile, loss = squared distance of the
     stack's centre of mass from a target after `steps` steps): device time of the plain forward
@@ -443,6 +502,8 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=300, help="steps of the 4096-world leg (0 skips it)")
     ap.add_argument("--adjoint-steps", type=int, default=240, help="steps of the differentiable leg (0 skips it)")
     ap.add_argument("--toi-pairs", type=int, default=1_000_000, help="pairs of the time-of-impact leg (0 skips it)")
+    ap.add_argument("--continuous-steps", type=int, default=60,
+                    help="timed steps of the continuous-physics leg (0 skips it)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
     ap.add_argument("--skip-steps", type=int, default=0,
                     help="untimed steps before the warm-up (profiling a later window of the scene)")
@@ -611,6 +672,9 @@ def main():
         line["adjoint"] = run_adjoint(torch, flush, local_rank, steps=args.adjoint_steps)
     if args.toi_pairs > 0 and rank == 0:
         line["time_of_impact"] = run_toi(args.toi_pairs)
+    if args.continuous_steps > 0 and rank == 0:
+        line["continuous"] = run_continuous(torch, flush, local_rank, steps=args.continuous_steps,
+                                            warmup=args.warmup)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = run_cpu_on_snapshots(scene, snaps)
     if rank == 0:
