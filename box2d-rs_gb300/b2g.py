@@ -396,6 +396,7 @@ def load_library(path=LIB_PATH):
         "b2g_get_toi_stats": [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
                               ctypes.POINTER(ctypes.c_int32)],
         "b2g_set_toi_schedule": [vp, i32],
+        "b2g_get_awake": [vp, u32, u32, vp],
         "b2g_get_contacts": [vp, vp, i32, ctypes.POINTER(i32)],
         "b2g_get_events": [vp, vp, i32, ctypes.POINTER(i32)],
         "b2g_get_pairs": [vp, vp, i32, ctypes.POINTER(i32)],
@@ -663,6 +664,14 @@ class B2world:
         e, it, r = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
         self._check(self._lib.b2g_get_toi_stats(self._h, ctypes.byref(e), ctypes.byref(it), ctypes.byref(r)))
         return int(e.value), int(it.value), int(r.value)
+
+    def get_awake(self, first=0, count=None):
+        """B2body::is_awake of bodies [first, first + count) as a uint8 array."""
+        if count is None:
+            count = self.body_count - first
+        out = np.zeros(count, np.uint8)
+        self._check(self._lib.b2g_get_awake(self._h, int(first), int(count), out.ctypes.data_as(ctypes.c_void_p)))
+        return out
 
     def set_toi_schedule(self, schedule):
         """TOI_SIDE_BY_SIDE (default), TOI_ONE_AT_A_TIME or TOI_RESTART_ON_ADVANCE."""

@@ -94,6 +94,7 @@ struct World {
     int num_worlds = 1;
     bool warm = true, continuous = false, allow_sleep = true, auto_clear = true;
     int toi_schedule = 0;  /* B2G_TOI_SCHEDULE_* */
+    bool asleep_seen = false;  /* a body was created asleep or put to sleep by the caller */
     bool record_events = false, record_pairs = false;
     bool new_contacts = false;
     float inv_dt0 = 0.0f;
@@ -525,6 +526,8 @@ int allocate(World* w, int nb, int nf) {
      * uses the second as its "has an awake member" flag) */
     w->minsep_buffers = std::max(2, w->minsep_buffers);
     A(d.isl_minsep, (size_t)w->minsep_buffers * body_cap); A(d.isl_done, body_cap); A(d.isl_sleep, body_cap);
+    A(d.b_wake, body_cap); A(d.b_dwake, body_cap); A(d.c_done, contact_cap);
+    cudaMemsetAsync(d.b_wake, 0x7f, (size_t)body_cap * sizeof(int), w->stream);  /* kNoWake */
     A(d.f_shape, fix_cap); A(d.f_body, fix_cap); A(d.f_mat, fix_cap); A(d.f_filter, fix_cap);
     A(d.f_group, fix_cap); A(d.f_refid, fix_cap); A(d.f_fat, fix_cap); A(d.f_moved, fix_cap);
     Contacts* cs[2] = {&d.c, &d.c_alt};
@@ -778,7 +781,7 @@ void issue_step(World* w, const StepParams& sp, float dt, bool capturing = false
         w->new_contacts = false;
     }
     mark(t.e[1]);
-    launch_collide(w->d, sp, s);
+    launch_collide(w->d, sp, s, w->allow_sleep || w->asleep_seen, w->num_sms);
     mark(t.e[2]);
     if (dt > 0.0f) {
         launch_islands_and_constraints(w->d, sp, s);
@@ -857,7 +860,7 @@ int step(World* w, float dt, int vi, int pi) {
         key.pi = pi;
         key.flags = sp.warm | (sp.allow_sleep << 1) | (sp.auto_clear << 2) | (sp.record_events << 3) |
                     (sp.record_pairs << 4) | ((w->tape && w->tape->recording) ? (1 << 5) : 0) |
-                    (w->continuous ? (1 << 6) : 0) | (sp.toi_schedule << 7);
+                    (w->continuous ? (1 << 6) : 0) | (sp.toi_schedule << 7) | (w->asleep_seen ? (1 << 9) : 0);
         key.generation = w->alloc_generation;
         key.n_bodies = w->d.n_bodies;
         key.n_fixtures = w->d.n_fixtures;
@@ -1091,6 +1094,7 @@ int b2g_create_bodies(void* p, const b2g_body_def* defs, int32_t n, uint32_t* id
         const b2g_body_def& d = defs[i];
         uint32_t fl = (uint32_t)d.type;
         if (d.awake && d.type != B2G_STATIC_BODY) fl |= BF_AWAKE;
+        if (!d.awake && d.type != B2G_STATIC_BODY) w->asleep_seen = true;
         if (d.enabled) fl |= BF_ENABLED;
         if (d.allow_sleep) fl |= BF_AUTO_SLEEP;
         if (d.fixed_rotation) fl |= BF_FIXED_ROTATION;
@@ -1377,7 +1381,26 @@ int b2g_apply_angular_impulse(void* p, uint32_t b, float impulse, int32_t wake) 
     return p ? body_op(W(p), 7, b, 0.0f, 0.0f, impulse, 0.0f, 0.0f, wake) : B2G_ERR_INVALID_ARG;
 }
 int b2g_set_awake(void* p, uint32_t b, int32_t flag) {
-    return p ? body_op(W(p), 8, b, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, flag) : B2G_ERR_INVALID_ARG;
+    if (!p) return B2G_ERR_INVALID_ARG;
+    if (!flag) W(p)->asleep_seen = true;
+    return body_op(W(p), 8, b, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, flag);
+}
+
+int b2g_get_awake(void* p, uint32_t first, uint32_t count, uint8_t* out) {
+    World* w = W(p);
+    if (!w || (!out && count)) return B2G_ERR_INVALID_ARG;
+    if ((size_t)first + count > w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body range out of bounds");
+    if (count == 0) return B2G_OK;
+    std::vector<uint32_t> fl(count);
+    if (w->device_authoritative) {
+        int rc = check_status(w);
+        if (rc != B2G_OK) return rc;
+        CUDA_OK(w, cudaMemcpy(fl.data(), w->d.b_flags + first, count * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    } else {
+        std::copy(w->h_flags.begin() + first, w->h_flags.begin() + first + count, fl.begin());
+    }
+    for (uint32_t i = 0; i < count; ++i) out[i] = (fl[i] & BF_AWAKE) ? 1 : 0;
+    return B2G_OK;
 }
 
 int b2g_set_gravity(void* p, b2g_vec2 g) {

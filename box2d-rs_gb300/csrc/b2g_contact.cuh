@@ -22,6 +22,14 @@ __device__ __forceinline__ void wake_body(const DevWorld& w, int b) {
     w.b_vel[b].w = 0.0f;  /* sleep_time = 0 */
 }
 
+/* set_awake(true) recorded for the collide pass of a world whose bodies may sleep: the reference's
+ * collide sees, at each contact of its list, the bodies woken by the contacts before it, so a wake
+ * is noted with the waking contact's place in the (key-sorted) table and applied when the pass ends */
+__device__ __forceinline__ void wake_body_at(const DevWorld& w, int b, int at) {
+    if ((w.b_flags[b] & BF_TYPE_MASK) == BODY_STATIC) return;
+    atomicMin(&w.b_wake[b], at);
+}
+
 __device__ __forceinline__ void push_event(const DevWorld& w, int kind, int fa, int fb) {
     int slot = atomicAdd(&w.cnt[CNT_EVENTS], 1);
     if (slot < w.event_cap) w.events[slot] = make_int4(kind, fa, fb, 0);
@@ -40,9 +48,10 @@ __device__ __forceinline__ Xf load_xf(const DevWorld& w, int b) {
 /* B2contact::update of contact i (flags: its current flags; fx, bd: its fixtures and bodies; ids:
  * its manifold ids word): re-enable it, evaluate the manifold on the bodies' transforms, carry
  * impulses from old points with the same feature id, update the touching flag, wake both bodies
- * when it changes, and record begin/end events. Returns whether the contact touches. */
+ * when it changes (at once, or noted at table place wake_at >= 0: wake_body_at), and record
+ * begin/end events. Returns whether the contact touches. */
 __device__ __forceinline__ bool contact_update(const DevWorld& w, bool record_events, int i, uint32_t flags, int2 fx,
-                                               int2 bd, uint4 ids) {
+                                               int2 bd, uint4 ids, int wake_at = -1) {
     const bool was_touching = (flags & CF_TOUCHING) != 0;
     const int old_count = (int)((ids.z >> 8) & 0xffu);
     flags |= CF_ENABLED;
@@ -81,8 +90,13 @@ __device__ __forceinline__ bool contact_update(const DevWorld& w, bool record_ev
         w.c.mimp[i] = make_float4(ni[0], ti[0], ni[1], ti[1]);
         w.c.mids[i] = make_uint4(m.id[0], m.id[1], (uint32_t)m.type | ((uint32_t)m.count << 8), ids.w);
         if (touching != was_touching) {
-            wake_body(w, bd.x);
-            wake_body(w, bd.y);
+            if (wake_at < 0) {
+                wake_body(w, bd.x);
+                wake_body(w, bd.y);
+            } else {
+                wake_body_at(w, bd.x, wake_at);
+                wake_body_at(w, bd.y, wake_at);
+            }
         }
     }
     w.c.flags[i] = touching ? (flags | CF_TOUCHING) : (flags & ~CF_TOUCHING);

@@ -89,6 +89,8 @@ enum {
     CNT_TOI_ITERS = 28,   /* iterations of the last continuous pass */
     CNT_TOI_PASSES = 29,  /* continuous passes run (their body marks are stamped with it) */
     CNT_TOI_ROLLBACKS = 30, /* passes restarted in sequential order after a conflict */
+    CNT_CASCADE = 40,     /* 3 ints: contacts collided per round of the wake cascade (rotating) */
+    CNT_CASCADE_ROUNDS = 43, /* rounds of the last wake cascade */
     /* continuous pass (k_continuous.cu), zeroed before every pass: */
     CNT_TOI_FIRST = 32,
     CNT_TOI_NEW = 32,     /* contacts created by the pass (table slots [n, n + this)) */
@@ -108,6 +110,7 @@ constexpr int kFirstFitColours = 64;
 constexpr int kColourTail = 256;   /* uncoloured constraints one block finishes colouring (one per thread) */
 constexpr int kMaxParts = 1024;    /* body parts of the part-local solve (at most one per solver block) */
 constexpr int kMaxPosIters = 64;
+constexpr int kNoWake = 0x7f7f7f7f;  /* b_wake's "not woken" (a byte-wise memset value) */
 /* continuous pass lists (k_continuous.cu): partner contacts of one event, events of one
  * iteration, contacts created in one pass */
 constexpr int kToiCand = 64;
@@ -165,6 +168,10 @@ struct DevWorld {
                                     2 round parities x 2 classes x body_cap */
     unsigned long long* b_cmask; /* colouring: colours used at this body, 2 classes x body_cap */
     uint32_t* isl_minsep;        /* 2 x body_cap: per-island max(-separation) bits, double-buffered */
+    int* b_wake;                 /* collide pass of a world whose bodies may sleep: the smallest table
+                                    place of a contact whose update woke the body (kNoWake: none) */
+    uint8_t* b_dwake;            /* woken by a destroyed contact (applied after the pass) */
+    uint8_t* c_done;             /* per contact: collided in this pass */
     uint8_t* isl_done;
     float* isl_sleep;            /* per island root: min sleep time (as ordered uint bits) */
     /* fixtures */
@@ -279,7 +286,9 @@ struct DevWorld {
 };
 
 /* kernel-file launchers */
-void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s);
+/* may_sleep: some body may be asleep (sleeping allowed, or a body made asleep): contacts then see
+ * the bodies woken by contacts before them in the table's key order, as in the reference's list */
+void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s, bool may_sleep, int num_sms);
 void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cudaStream_t s);
 /* parts: allow the part-local solve (used where the world's size suits it) */
 void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms, bool parts);

@@ -5,7 +5,12 @@
  * and b2_contact_update, src/private/dynamics/b2_contact.rs:103-218.
  *
  * One thread per contact of the (key-sorted) contact table:
- *   - skip when neither body is awake and non-static;
+ *   - skip when neither body is awake and non-static. The reference's loop sees, at each contact
+ *     of its list, the bodies woken by the updates before it; where bodies may sleep, a wake is
+ *     noted with the waking contact's table place, a contact counts a body woken at an earlier
+ *     place as awake, and the contacts a wake makes active are collided in further rounds until
+ *     none is left (the table's key order standing for the list order); the wakes are applied
+ *     after the pass;
  *   - if the two fat AABBs stopped overlapping, flag the contact dead (the next merge
  *     drops it), emit an end event if it was touching, and wake both bodies if its
  *     manifold had points (B2contact::destroy);
@@ -16,42 +21,119 @@
  * 144-byte shape records + two body transforms.
  */
 #include "b2g_contact.cuh"
+#include "b2g_sync.cuh"
 
 namespace b2g {
 
-__global__ void __launch_bounds__(256) k_collide(DevWorld w, StepParams sp) {
-    const int n = w.cnt[CNT_CONTACTS];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t flags = w.c.flags[i];
-        if (flags & CF_DEAD) continue;
-        const int2 fx = w.c.fix[i];
-        const int2 bd = w.c.body[i];
-        const uint32_t fa_flags = w.b_flags[bd.x];
-        const uint32_t fb_flags = w.b_flags[bd.y];
-        const bool activeA = (fa_flags & BF_AWAKE) && (fa_flags & BF_TYPE_MASK) != BODY_STATIC;
-        const bool activeB = (fb_flags & BF_AWAKE) && (fb_flags & BF_TYPE_MASK) != BODY_STATIC;
-        if (!activeA && !activeB) continue;
-        const float4 A = w.f_fat[fx.x];
-        const float4 B = w.f_fat[fx.y];
-        const bool was_touching = (flags & CF_TOUCHING) != 0;
-        const uint4 ids = w.c.mids[i];
-        const int old_count = (int)((ids.z >> 8) & 0xffu);
-        if (!overlap4(A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w)) {
-            if (sp.record_events && was_touching) push_event(w, 1, fx.x, fx.y);
-            if (old_count > 0 && !(flags & CF_SENSOR)) {
+namespace {
+
+/* Body b counts as active for contact i (table place i): awake and not static. With deferred
+ * wakes (the world's bodies may sleep), "awake" is awake when the pass began, or woken by the
+ * update of a contact earlier in the table than i. */
+__device__ __forceinline__ bool active_for(const DevWorld& w, int b, uint32_t f, int i, bool deferred) {
+    if ((f & BF_TYPE_MASK) == BODY_STATIC) return false;
+    if (f & BF_AWAKE) return true;
+    return deferred && ((volatile int*)w.b_wake)[b] < i;
+}
+
+/* b2_contact_manager_collide for contact i; false if it was skipped as inactive */
+__device__ __forceinline__ bool collide_contact(const DevWorld& w, const StepParams& sp, int i, bool deferred) {
+    uint32_t flags = w.c.flags[i];
+    if (flags & CF_DEAD) return true;
+    const int2 fx = w.c.fix[i];
+    const int2 bd = w.c.body[i];
+    const uint32_t fa_flags = w.b_flags[bd.x];
+    const uint32_t fb_flags = w.b_flags[bd.y];
+    if (!active_for(w, bd.x, fa_flags, i, deferred) && !active_for(w, bd.y, fb_flags, i, deferred)) return false;
+    const float4 A = w.f_fat[fx.x];
+    const float4 B = w.f_fat[fx.y];
+    const bool was_touching = (flags & CF_TOUCHING) != 0;
+    const uint4 ids = w.c.mids[i];
+    const int old_count = (int)((ids.z >> 8) & 0xffu);
+    if (!overlap4(A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w)) {
+        /* destroyed after the pass (the reference collects them and destroys them after its loop) */
+        if (sp.record_events && was_touching) push_event(w, 1, fx.x, fx.y);
+        if (old_count > 0 && !(flags & CF_SENSOR)) {
+            if (deferred) {
+                if ((fa_flags & BF_TYPE_MASK) != BODY_STATIC) w.b_dwake[bd.x] = 1;
+                if ((fb_flags & BF_TYPE_MASK) != BODY_STATIC) w.b_dwake[bd.y] = 1;
+            } else {
                 wake_body(w, bd.x);
                 wake_body(w, bd.y);
             }
-            w.c.flags[i] = (flags | CF_DEAD) & ~CF_TOUCHING;
-            continue;
         }
-        contact_update(w, sp.record_events != 0, i, flags, fx, bd, ids);
+        w.c.flags[i] = (flags | CF_DEAD) & ~CF_TOUCHING;
+        return true;
+    }
+    contact_update(w, sp.record_events != 0, i, flags, fx, bd, ids, deferred ? i : -1);
+    return true;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(256) k_collide(DevWorld w, StepParams sp, int deferred) {
+    const int n = w.cnt[CNT_CONTACTS];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const bool done = collide_contact(w, sp, i, deferred != 0);
+        if (deferred) w.c_done[i] = done ? 1 : 0;
     }
 }
 
-void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s) {
+/* The contacts skipped as inactive whose body a contact earlier in the table woke: collided in
+ * rounds until a round finds none (a chain of wakes along the table's order). */
+__global__ void __launch_bounds__(256) k_collide_cascade(DevWorld w, StepParams sp) {
+    grid_barrier_start();
+    const int n = w.cnt[CNT_CONTACTS];
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    volatile int* vcnt = w.cnt;
+    int round = 0;
+    for (; round < n + 1; ++round) {
+        if (gtid == 0) vcnt[CNT_CASCADE + (round + 1) % 3] = 0;
+        int mine = 0;
+        for (int i = gtid; i < n; i += gridDim.x * blockDim.x) {
+            if (w.c_done[i]) continue;
+            const int2 bd = w.c.body[i];
+            const uint32_t fa = w.b_flags[bd.x], fb = w.b_flags[bd.y];
+            if (!active_for(w, bd.x, fa, i, true) && !active_for(w, bd.y, fb, i, true)) continue;
+            collide_contact(w, sp, i, true);
+            w.c_done[i] = 1;
+            ++mine;
+        }
+        if (mine) atomicAdd(&w.cnt[CNT_CASCADE + round % 3], mine);
+        if (!grid_barrier(w)) return;
+        if (vcnt[CNT_CASCADE + round % 3] == 0) break;
+    }
+    if (gtid == 0) vcnt[CNT_CASCADE_ROUNDS] = round;
+}
+
+/* apply the pass's wakes (set_awake(true): awake, sleep time 0) and clear the records */
+__global__ void k_collide_wake(DevWorld w) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x) {
+        if (w.b_wake[b] != kNoWake || w.b_dwake[b]) {
+            const uint32_t f = w.b_flags[b];
+            if ((f & BF_TYPE_MASK) != BODY_STATIC) {
+                w.b_flags[b] = f | BF_AWAKE;
+                w.b_vel[b].w = 0.0f;
+            }
+            w.b_wake[b] = kNoWake;
+            w.b_dwake[b] = 0;
+        }
+    }
+}
+
+void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s, bool may_sleep, int num_sms) {
     const int block = w.cfg_collide_block;
-    k_collide<<<grid_for(w.contact_cap, block, 152 * 2048 / block), block, 0, s>>>(w, sp); B2G_LAUNCHED(1);
+    k_collide<<<grid_for(w.contact_cap, block, 152 * 2048 / block), block, 0, s>>>(w, sp, may_sleep ? 1 : 0);
+    B2G_LAUNCHED(1);
+    if (!may_sleep) return;
+    DevWorld wc = w;
+    StepParams p = sp;
+    void* args[] = {&wc, &p};
+    cudaMemsetAsync(w.cnt + CNT_BARRIER, 0, sizeof(int), s);
+    cudaMemsetAsync(w.cnt + CNT_CASCADE, 0, 3 * sizeof(int), s);
+    cudaLaunchCooperativeKernel((const void*)k_collide_cascade, dim3(num_sms), dim3(256), args, 0, s);
+    k_collide_wake<<<grid_for(w.n_bodies, 256, num_sms * 8), 256, 0, s>>>(w);
+    B2G_LAUNCHED(2);
 }
 
 /* Stand-alone manifolds of independent shape pairs (the public b2_collide_* functions,

@@ -195,6 +195,8 @@ int b2g_apply_torque(void* world, uint32_t body, float torque, int32_t wake);
 int b2g_apply_linear_impulse_to_center(void* world, uint32_t body, b2g_vec2 impulse, int32_t wake);
 int b2g_apply_angular_impulse(void* world, uint32_t body, float impulse, int32_t wake);
 int b2g_set_awake(void* world, uint32_t body, int32_t flag);
+/* B2body::is_awake (src/b2_body.rs:803-805) of bodies [first, first + count): 1 awake, 0 asleep */
+int b2g_get_awake(void* world, uint32_t first, uint32_t count, uint8_t* out);
 
 /* ---- world flags, src/b2_world.rs:163-193, :232-253 ---- */
 int b2g_set_gravity(void* world, b2g_vec2 gravity);

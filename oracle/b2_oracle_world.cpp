@@ -154,7 +154,7 @@ struct World {
     std::vector<uint64_t> last_order;  /* island contact order solved last step */
     int islands_solved = 0;
     int toi_events = 0;                /* solid time-of-impact events solved so far */
-    bool toi_key_order = false;        /* solve_toi takes ties and island contacts in key order */
+    bool key_order = false;            /* collide and solve_toi take contacts in key order */
     /* island scratch */
     std::vector<int> isl_bodies, isl_contacts, stack;
     std::vector<Position> pos;
@@ -507,10 +507,20 @@ static void update_contact(World& w, int id) {
     }
 }
 
-/* b2_contact_manager_collide, private/dynamics/b2_contact_manager.rs:83-171 */
+static uint64_t contact_proxy_key(const World& w, const Contact& c);
+
+/* b2_contact_manager_collide, private/dynamics/b2_contact_manager.rs:83-171. The loop sees, at
+ * each contact, the bodies woken by the updates before it; with key_order set it goes through the
+ * contacts in key order (the GPU's table order) instead of the list order. */
 static void collide(World& w) {
     std::vector<int> to_destroy;
-    for (int id = w.contact_head; id >= 0; id = w.contacts[id].next) {
+    std::vector<int> order;
+    for (int id = w.contact_head; id >= 0; id = w.contacts[id].next) order.push_back(id);
+    if (w.key_order)
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+            return contact_proxy_key(w, w.contacts[x]) < contact_proxy_key(w, w.contacts[y]);
+        });
+    for (int id : order) {
         Contact& c = w.contacts[id];
         const Fixture& FA = w.fixtures[c.fa];
         const Fixture& FB = w.fixtures[c.fb];
@@ -1138,7 +1148,7 @@ static void solve_toi_island(World& w, const Step& sub, int toiA, int toiB) {
 }
 
 /* B2world::solve_toi, private/dynamics/b2_world.rs:534-901 (no sub-stepping: every step is
- * complete). With toi_key_order set, two list-order choices follow the GPU's order instead: the
+ * complete). With key_order set, two list-order choices follow the GPU's order instead: the
  * first time of impact is the smallest (alpha, contact key), and an event's island takes its
  * other contacts in key order. */
 static void solve_toi(World& w, const Step& step) {
@@ -1153,7 +1163,7 @@ static void solve_toi(World& w, const Step& step) {
         C.toi_count = 0;
         C.toi = 1.0f;
     }
-    const bool key_order = w.toi_key_order;
+    const bool key_order = w.key_order;
     for (;;) {
         int minContact = -1;
         float minAlpha = 1.0f;
@@ -1565,11 +1575,19 @@ int ora_get_hook_misses(void* p) { return ((World*)p)->hook_misses; }
 /* solid time-of-impact events solved since the world was made */
 int ora_get_toi_events(void* p) { return ((World*)p)->toi_events; }
 
-/* Ordering hook of solve_toi: ties of the first time of impact go to the smallest contact key and
- * an event's island takes its other contacts in key order (the GPU's order), instead of the
- * contact-list order. */
-int ora_set_toi_key_order(void* p, int flag) {
-    ((World*)p)->toi_key_order = flag != 0;
+/* Ordering hook for the contact list: collide goes through the contacts in key order, and in
+ * solve_toi ties of the first time of impact go to the smallest contact key and an event's island
+ * takes its other contacts in key order (the GPU's order), instead of the contact-list order. */
+int ora_set_key_order(void* p, int flag) {
+    ((World*)p)->key_order = flag != 0;
+    return 0;
+}
+
+/* B2body::is_awake of bodies [first, first + count) */
+int ora_get_awake(void* p, uint32_t first, uint32_t count, uint8_t* out) {
+    World& w = *(World*)p;
+    if ((size_t)first + count > w.bodies.size()) return -1;
+    for (uint32_t i = 0; i < count; ++i) out[i] = w.bodies[first + i].awake ? 1 : 0;
     return 0;
 }
 

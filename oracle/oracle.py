@@ -65,7 +65,8 @@ def load():
         "ora_set_solver_order": [vp, vp, i32],
         "ora_get_hook_misses": [vp],
         "ora_get_toi_events": [vp],
-        "ora_set_toi_key_order": [vp, i32],
+        "ora_set_key_order": [vp, i32],
+        "ora_get_awake": [vp, u32, u32, vp],
         "ora_get_solver_order": [vp, vp, i32, pi32],
         "ora_get_events": [vp, vp, i32, pi32],
         "ora_polygon_mass": [vp, vp],
@@ -178,9 +179,18 @@ class OracleWorld:
         self._continuous = bool(flag)
         self._apply_flags()
 
-    def set_toi_key_order(self, flag):
-        """solve_toi breaks ties and orders an event's island contacts by contact key (the GPU's order)."""
-        self._lib.ora_set_toi_key_order(self._h, int(bool(flag)))
+    def set_key_order(self, flag):
+        """collide and solve_toi take contacts in key order (the GPU's table order) instead of the
+        contact-list order: ties of solve_toi's first time of impact, an event's island order, and
+        which contacts see the bodies woken by collide's earlier updates."""
+        self._lib.ora_set_key_order(self._h, int(bool(flag)))
+
+    def get_awake(self, first=0, count=None):
+        if count is None:
+            count = self.body_count - first
+        out = np.zeros(count, np.uint8)
+        self._lib.ora_get_awake(self._h, first, count, _ptr(out))
+        return out
 
     def toi_events(self):
         """Solid time-of-impact events solved since the world was made."""

@@ -68,9 +68,15 @@ class MultiOracle:
     def hook_misses(self):
         return sum(o.hook_misses() for o, _, _ in self.worlds)
 
-    def set_toi_key_order(self, flag):
+    def set_key_order(self, flag):
         for o, _, _ in self.worlds:
-            o.set_toi_key_order(flag)
+            o.set_key_order(flag)
+
+    def get_awake(self):
+        out = np.zeros(self.n_bodies, np.uint8)
+        for o, bidx, _ in self.worlds:
+            out[bidx] = o.get_awake()
+        return out
 
     def toi_events(self):
         return sum(o.toi_events() for o, _, _ in self.worlds)
@@ -127,9 +133,9 @@ def make_pair(scene, record_pairs=True, record_events=False, warm_starting=True)
     else:
         ora = oracle.OracleWorld(gravity=scene["gravity"], **kw)
         scenes.build_world(ora, scene)
-    # solve_toi's list-order choices (ties of the first time of impact, an event's island order)
+    # the contact-list order choices (collide's wake order, solve_toi's ties and island order)
     # follow the GPU's key order
-    ora.set_toi_key_order(True)
+    ora.set_key_order(True)
     return gpu, ora
 
 
@@ -217,6 +223,8 @@ def lockstep(scene, steps, check_pairs=True, check_contacts=True, resync=False, 
         os_ = ora.get_body_states()
         rec["body_abs"], rec["body_rel"] = body_diff(gs, os_)
         rec["bitexact_bodies"] = all(np.array_equal(gs[f], os_[f]) for f in BODY_FIELDS)
+        rec["awake_equal"] = bool(np.array_equal(gpu.get_awake(), ora.get_awake()))
+        rec["awake"] = int(gpu.get_awake().sum())
         if check_pairs:
             gp, op = pair_set(gpu.get_pairs()), pair_set(ora.get_pairs())
             rec["pairs_equal"] = gp == op

@@ -31,6 +31,7 @@ def _assert_step(r, bitexact=True):
     assert r["body_rel"] <= TOL, r
     if bitexact:
         assert r["bitexact_bodies"], r
+        assert r["awake_equal"], r
 
 
 def test_narrowphase_golden(built):
@@ -313,3 +314,41 @@ def test_continuous_mixed_side_by_side_lockstep(built):
     s = dict(scenes.mixed(n_circles=1500, n_polygons=1500, size=60.0, seed=29), continuous=True)
     _, gpu, _, events = _toi_lockstep(s, 150)
     assert events > 50
+
+
+def _sleepy(s):
+    s = dict(s, allow_sleep=True)
+    b = s["bodies"].copy()
+    b["allow_sleep"] = 1
+    return dict(s, bodies=b)
+
+
+def test_sleeping_pyramid_lockstep(built):
+    """Sleeping on: a 10-row pyramid settles and falls asleep island by island (sleep timers,
+    the per-island position-solved test, set_awake(false) zeroing velocities); bodies and awake
+    flags bit-exact with the oracle every step."""
+    s = _sleepy(scenes.pyramid(rows=10))
+    recs, gpu, _ = parity.lockstep(s, 300)
+    for r in recs:
+        _assert_step(r)
+    assert recs[-1]["awake"] == 0
+
+
+def test_sleeping_pile_woken_lockstep(built):
+    """A pile of 40 boxes falls asleep, then a heavy box dropped from 145 m lands on it: the
+    sleeping pile's contacts become active as the wake spreads, in the reference's order within
+    each collide pass (its list order, here the key order on both sides)."""
+    s = scenes.pile(n_boxes=40, width=4.0, height=4.0, seed=11, spacing=0.45)
+    nb = len(s["bodies"])
+    drop = b2g.body_defs(1)
+    drop["type"] = b2g.DYNAMIC
+    drop["position"] = (0.3, 145.0)
+    fx = b2g.box_fixture(nb, 0.6, 0.6, density=20.0, friction=0.6)
+    s = _sleepy(dict(s, bodies=np.concatenate([s["bodies"], drop]), fixtures=np.concatenate([s["fixtures"], fx]),
+                     n_dynamic=s["n_dynamic"] + 1))
+    recs, gpu, _ = parity.lockstep(s, 440)
+    for r in recs:
+        _assert_step(r)
+    awake = [r["awake"] for r in recs]
+    assert min(awake[230:320]) <= 1      # the pile slept before the box arrived
+    assert max(awake[340:]) > 30         # and woke up

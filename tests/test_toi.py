@@ -108,7 +108,7 @@ def _rain_below_plate(continuous):
 
     s = scenes.toi_rain(n=64, seed=7, steps=120)
     o = oracle.OracleWorld(gravity=s["gravity"], continuous=continuous)
-    o.set_toi_key_order(True)
+    o.set_key_order(True)
     scenes.build_world(o, s)
     o.steps(s["dt"], s["vi"], s["pi"], s["steps"])
     st = o.get_body_states()
