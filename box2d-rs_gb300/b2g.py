@@ -397,6 +397,9 @@ def load_library(path=LIB_PATH):
                               ctypes.POINTER(ctypes.c_int32)],
         "b2g_set_toi_schedule": [vp, i32],
         "b2g_get_awake": [vp, u32, u32, vp],
+        "b2g_state_size": [vp, ctypes.POINTER(ctypes.c_uint64)],
+        "b2g_state_save": [vp, vp, ctypes.c_uint64],
+        "b2g_state_load": [vp, vp, ctypes.c_uint64],
         "b2g_get_contacts": [vp, vp, i32, ctypes.POINTER(i32)],
         "b2g_get_events": [vp, vp, i32, ctypes.POINTER(i32)],
         "b2g_get_pairs": [vp, vp, i32, ctypes.POINTER(i32)],
@@ -672,6 +675,19 @@ class B2world:
         out = np.zeros(count, np.uint8)
         self._check(self._lib.b2g_get_awake(self._h, int(first), int(count), out.ctypes.data_as(ctypes.c_void_p)))
         return out
+
+    def save_state(self):
+        """The world's exact state (b2g_state_save) as a uint8 array."""
+        n = ctypes.c_uint64(0)
+        self._check(self._lib.b2g_state_size(self._h, ctypes.byref(n)))
+        out = np.empty(n.value, np.uint8)
+        self._check(self._lib.b2g_state_save(self._h, out.ctypes.data_as(ctypes.c_void_p), n.value))
+        return out
+
+    def load_state(self, state):
+        """Continue from a state of save_state (this world, or one built the same way)."""
+        state = np.ascontiguousarray(state, np.uint8)
+        self._check(self._lib.b2g_state_load(self._h, state.ctypes.data_as(ctypes.c_void_p), len(state)))
 
     def set_toi_schedule(self, schedule):
         """TOI_SIDE_BY_SIDE (default), TOI_ONE_AT_A_TIME or TOI_RESTART_ON_ADVANCE."""

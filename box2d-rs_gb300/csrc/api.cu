@@ -118,6 +118,7 @@ struct World {
     int uploaded_bodies = 0, uploaded_fixtures = 0;
     bool device_authoritative = false;
     std::vector<void*> allocations;
+    std::vector<size_t> alloc_bytes;  /* byte size of each entry of allocations */
     int user_contact_cap = 0, user_pair_cap = 0;
     Timer timer;
     b2g_profile profile{};
@@ -218,6 +219,7 @@ int dalloc(World* w, T** p, size_t n) {
         return B2G_ERR_OUT_OF_MEMORY;
     }
     w->allocations.push_back((void*)*p);
+    w->alloc_bytes.push_back(n * sizeof(T));
     cudaMemsetAsync(*p, 0, n * sizeof(T), w->stream);
     return B2G_OK;
 }
@@ -228,6 +230,7 @@ void free_all(World* w) {
     drop_graphs(w);
     for (void* p : w->allocations) cudaFree(p);
     w->allocations.clear();
+    w->alloc_bytes.clear();
     w->allocated = false;
     ++w->alloc_generation;
 }
@@ -816,7 +819,10 @@ int ensure_minsep_buffers(World* w, int pi) {
     if (pi <= w->minsep_buffers) return B2G_OK;
     CUDA_OK(w, cudaStreamSynchronize(w->stream));
     auto it = std::find(w->allocations.begin(), w->allocations.end(), (void*)w->d.isl_minsep);
-    if (it != w->allocations.end()) w->allocations.erase(it);
+    if (it != w->allocations.end()) {
+        w->alloc_bytes.erase(w->alloc_bytes.begin() + (it - w->allocations.begin()));
+        w->allocations.erase(it);
+    }
     cudaFree(w->d.isl_minsep);
     w->minsep_buffers = pi;
     int rc = dalloc(w, &w->d.isl_minsep, (size_t)pi * w->d.body_cap);
@@ -1549,6 +1555,150 @@ int b2g_get_counts(void* p, b2g_counts* out) {
         out->touching_contacts = t;
     }
     out->islands_solved = cnt[CNT_CONS];
+    return B2G_OK;
+}
+
+/* ---- exact checkpoint: every device buffer of the world and its stepping state ---- */
+
+namespace {
+
+constexpr uint32_t kStateMagic = 0x53473242u;  /* "B2GS" */
+constexpr uint32_t kStateVersion = 1;
+
+struct StateHeader {
+    uint32_t magic, version;
+    int32_t n_bodies, n_fixtures, body_cap, fix_cap, contact_cap, pair_cap, num_worlds, key_bits, morton_world_bits;
+    int32_t minsep_buffers, n_alloc;
+    uint64_t buffer_bytes;
+    float inv_dt0;
+    int32_t steps, swaps_parity, new_contacts, warm, continuous, allow_sleep, auto_clear, toi_schedule, asleep_seen,
+        part_solve, proxies_created;
+    b2g_vec2 gravity;
+};
+
+/* the device holds the world (bodies, fixtures) and nothing is in flight */
+int state_ready(World* w) {
+    if (w->h_flags.empty()) return fail(w, B2G_ERR_INVALID_ARG, "the world has no bodies");
+    if (w->tape && w->tape->recording) return fail(w, B2G_ERR_UNSUPPORTED, "a tape is recording");
+    int rc = prepare(w);
+    if (rc != B2G_OK) return rc;
+    CUDA_OK(w, cudaStreamSynchronize(w->stream));
+    return check_status(w);
+}
+
+uint64_t state_bytes(const World* w) {
+    uint64_t n = sizeof(StateHeader) + w->alloc_bytes.size() * sizeof(uint64_t);
+    for (size_t b : w->alloc_bytes) n += b;
+    return n;
+}
+
+}  // namespace
+
+int b2g_state_size(void* p, uint64_t* bytes) {
+    World* w = W(p);
+    if (!w || !bytes) return B2G_ERR_INVALID_ARG;
+    int rc = state_ready(w);
+    if (rc != B2G_OK) return rc;
+    *bytes = state_bytes(w);
+    return B2G_OK;
+}
+
+int b2g_state_save(void* p, void* out, uint64_t bytes) {
+    World* w = W(p);
+    if (!w || !out) return B2G_ERR_INVALID_ARG;
+    int rc = state_ready(w);
+    if (rc != B2G_OK) return rc;
+    if (bytes < state_bytes(w)) return fail(w, B2G_ERR_INVALID_ARG, "buffer smaller than b2g_state_size");
+    StateHeader h{};
+    h.magic = kStateMagic;
+    h.version = kStateVersion;
+    h.n_bodies = w->d.n_bodies;
+    h.n_fixtures = w->d.n_fixtures;
+    h.body_cap = w->d.body_cap;
+    h.fix_cap = w->d.fix_cap;
+    h.contact_cap = w->d.contact_cap;
+    h.pair_cap = w->d.pair_cap;
+    h.num_worlds = w->num_worlds;
+    h.key_bits = w->d.key_bits;
+    h.morton_world_bits = w->d.morton_world_bits;
+    h.minsep_buffers = w->minsep_buffers;
+    h.n_alloc = (int32_t)w->allocations.size();
+    h.buffer_bytes = state_bytes(w);
+    h.inv_dt0 = w->inv_dt0;
+    h.steps = w->steps;
+    h.swaps_parity = w->swaps & 1;
+    h.new_contacts = w->new_contacts;
+    h.warm = w->warm;
+    h.continuous = w->continuous;
+    h.allow_sleep = w->allow_sleep;
+    h.auto_clear = w->auto_clear;
+    h.toi_schedule = w->toi_schedule;
+    h.asleep_seen = w->asleep_seen;
+    h.part_solve = w->part_solve;
+    h.proxies_created = w->proxies_created;
+    h.gravity = w->gravity;
+    unsigned char* o = (unsigned char*)out;
+    memcpy(o, &h, sizeof(h));
+    o += sizeof(h);
+    for (size_t b : w->alloc_bytes) {
+        const uint64_t v = b;
+        memcpy(o, &v, sizeof(v));
+        o += sizeof(v);
+    }
+    for (size_t i = 0; i < w->allocations.size(); ++i) {
+        CUDA_OK(w, cudaMemcpy(o, w->allocations[i], w->alloc_bytes[i], cudaMemcpyDeviceToHost));
+        o += w->alloc_bytes[i];
+    }
+    return B2G_OK;
+}
+
+int b2g_state_load(void* p, const void* in, uint64_t bytes) {
+    World* w = W(p);
+    if (!w || !in) return B2G_ERR_INVALID_ARG;
+    if (bytes < sizeof(StateHeader)) return fail(w, B2G_ERR_INVALID_ARG, "not a world state");
+    StateHeader h;
+    memcpy(&h, in, sizeof(h));
+    if (h.magic != kStateMagic || h.version != kStateVersion || h.buffer_bytes != bytes)
+        return fail(w, B2G_ERR_INVALID_ARG, "not a world state of this version");
+    int rc = state_ready(w);
+    if (rc != B2G_OK) return rc;
+    rc = ensure_minsep_buffers(w, h.minsep_buffers);
+    if (rc != B2G_OK) return rc;
+    const unsigned char* src = (const unsigned char*)in + sizeof(h);
+    bool same = h.n_bodies == w->d.n_bodies && h.n_fixtures == w->d.n_fixtures && h.body_cap == w->d.body_cap &&
+                h.fix_cap == w->d.fix_cap && h.contact_cap == w->d.contact_cap && h.pair_cap == w->d.pair_cap &&
+                h.num_worlds == w->num_worlds && h.n_alloc == (int32_t)w->allocations.size() &&
+                h.minsep_buffers == w->minsep_buffers;
+    for (int32_t i = 0; same && i < h.n_alloc; ++i) {
+        uint64_t v;
+        memcpy(&v, src + (size_t)i * sizeof(v), sizeof(v));
+        same = v == w->alloc_bytes[i];
+    }
+    if (!same)
+        return fail(w, B2G_ERR_INVALID_ARG,
+                    "the state was saved from a world of another layout (bodies, fixtures, capacities or worlds)");
+    src += (size_t)h.n_alloc * sizeof(uint64_t);
+    for (size_t i = 0; i < w->allocations.size(); ++i) {
+        CUDA_OK(w, cudaMemcpy(w->allocations[i], src, w->alloc_bytes[i], cudaMemcpyHostToDevice));
+        src += w->alloc_bytes[i];
+    }
+    /* the contact table is the buffer that was current when saved */
+    if ((w->swaps & 1) != h.swaps_parity) swap_contacts(w);
+    w->d.key_bits = h.key_bits;
+    w->d.morton_world_bits = h.morton_world_bits;
+    w->inv_dt0 = h.inv_dt0;
+    w->steps = h.steps;
+    w->new_contacts = h.new_contacts != 0;
+    w->warm = h.warm != 0;
+    w->continuous = h.continuous != 0;
+    w->allow_sleep = h.allow_sleep != 0;
+    w->auto_clear = h.auto_clear != 0;
+    w->toi_schedule = h.toi_schedule;
+    w->asleep_seen = h.asleep_seen != 0;
+    w->part_solve = h.part_solve != 0;
+    w->proxies_created = h.proxies_created;
+    w->gravity = h.gravity;
+    w->device_authoritative = true;
     return B2G_OK;
 }
 

@@ -231,6 +231,16 @@ int b2g_set_part_solve(void* world, int32_t flag);
 /* ---- introspection ---- */
 int b2g_get_profile(void* world, b2g_profile* out);       /* B2world::get_profile, src/b2_world.rs:268-270 */
 int b2g_get_counts(void* world, b2g_counts* out);         /* get_body_count / get_contact_count / get_proxy_count */
+/* Exact checkpoint and resume (not in the reference's API, which serialises a world through serde,
+ * src/serialize/): the world's device buffers (bodies, fixtures, the contact table with its
+ * manifolds and impulses, the colouring and partition the next steps reuse) and its stepping state,
+ * written to caller memory of b2g_state_size bytes. A world loaded from it continues bit for bit
+ * like the saved one: load into the same world, or one built with the same world definition, bodies
+ * and fixtures (B2G_ERR_INVALID_ARG otherwise). Not while a tape records. */
+int b2g_state_size(void* world, uint64_t* bytes);
+int b2g_state_save(void* world, void* out, uint64_t bytes);
+int b2g_state_load(void* world, const void* in, uint64_t bytes);
+
 /* Continuous physics: solid time-of-impact events solved since the world was made, the
  * iterations of the last step's pass, and the passes restarted one event at a time. */
 int b2g_get_toi_stats(void* world, int32_t* events, int32_t* last_iterations, int32_t* restarts);
