@@ -140,6 +140,46 @@ EVENT = np.dtype([("kind", "<i4"), ("fixture_a", "<u4"), ("fixture_b", "<u4")])
 # B2Sweep (src/b2_math.rs): local centre, centre and angle at the start (c0, a0) and the end (c, a)
 SWEEP = np.dtype([("local_center", "<f4", (2,)), ("c0", "<f4", (2,)), ("c", "<f4", (2,)), ("a0", "<f4"),
                   ("a", "<f4"), ("alpha0", "<f4"), ("pad", "<f4")])
+JOINT_REVOLUTE = 1
+JOINT_DEF = np.dtype(
+    [
+        ("type", "<i4"),
+        ("body_a", "<u4"),
+        ("body_b", "<u4"),
+        ("collide_connected", "<i4"),
+        ("local_anchor_a", "<f4", (2,)),
+        ("local_anchor_b", "<f4", (2,)),
+        ("reference_angle", "<f4"),
+        ("enable_limit", "<i4"),
+        ("lower_angle", "<f4"),
+        ("upper_angle", "<f4"),
+        ("enable_motor", "<i4"),
+        ("motor_speed", "<f4"),
+        ("max_motor_torque", "<f4"),
+        ("pad_", "<u4"),
+    ]
+)
+
+
+def revolute_joint(body_a, body_b, anchor_a, anchor_b, reference_angle=0.0, collide_connected=False,
+                   limits=None, motor=None):
+    """B2revoluteJointDef: local anchors on each body; limits = (lower, upper) radians;
+    motor = (speed, max torque)."""
+    d = np.zeros(1, JOINT_DEF)
+    d["type"] = JOINT_REVOLUTE
+    d["body_a"], d["body_b"] = body_a, body_b
+    d["collide_connected"] = int(bool(collide_connected))
+    d["local_anchor_a"], d["local_anchor_b"] = anchor_a, anchor_b
+    d["reference_angle"] = reference_angle
+    if limits is not None:
+        d["enable_limit"] = 1
+        d["lower_angle"], d["upper_angle"] = limits
+    if motor is not None:
+        d["enable_motor"] = 1
+        d["motor_speed"], d["max_motor_torque"] = motor
+    return d
+
+
 TOI_OUTPUT = np.dtype([("state", "<i4"), ("t", "<f4")])
 TOI_UNKNOWN, TOI_FAILED, TOI_OVERLAPPED, TOI_TOUCHING, TOI_SEPARATED = range(5)
 TOI_SIDE_BY_SIDE, TOI_ONE_AT_A_TIME, TOI_RESTART_ON_ADVANCE = range(3)  # b2g_set_toi_schedule
@@ -397,6 +437,9 @@ def load_library(path=LIB_PATH):
                               ctypes.POINTER(ctypes.c_int32)],
         "b2g_set_toi_schedule": [vp, i32],
         "b2g_get_awake": [vp, u32, u32, vp],
+        "b2g_create_joints": [vp, vp, i32, vp],
+        "b2g_get_joint_impulses": [vp, u32, u32, vp],
+        "b2g_get_joint_order": [vp, vp, i32, ctypes.POINTER(ctypes.c_int32)],
         "b2g_state_size": [vp, ctypes.POINTER(ctypes.c_uint64)],
         "b2g_state_save": [vp, vp, ctypes.c_uint64],
         "b2g_state_load": [vp, vp, ctypes.c_uint64],
@@ -675,6 +718,30 @@ class B2world:
         out = np.zeros(count, np.uint8)
         self._check(self._lib.b2g_get_awake(self._h, int(first), int(count), out.ctypes.data_as(ctypes.c_void_p)))
         return out
+
+    def create_joints(self, defs):
+        defs = np.ascontiguousarray(defs, JOINT_DEF)
+        ids = np.zeros(len(defs), np.uint32)
+        self._check(self._lib.b2g_create_joints(self._h, defs.ctypes.data_as(ctypes.c_void_p), len(defs),
+                                                ids.ctypes.data_as(ctypes.c_void_p)))
+        self.joint_count = getattr(self, "joint_count", 0) + len(defs)
+        return ids
+
+    def get_joint_impulses(self):
+        """(joints, 5): accumulated impulse x, y, motor, lower limit, upper limit."""
+        n = getattr(self, "joint_count", 0)
+        out = np.zeros((n, 5), np.float32)
+        if n:
+            self._check(self._lib.b2g_get_joint_impulses(self._h, 0, n, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def get_joint_order(self):
+        n = getattr(self, "joint_count", 0)
+        out = np.zeros(max(n, 1), np.uint32)
+        got = ctypes.c_int32(0)
+        self._check(self._lib.b2g_get_joint_order(self._h, out.ctypes.data_as(ctypes.c_void_p), len(out),
+                                                  ctypes.byref(got)))
+        return out[: got.value]
 
     def save_state(self):
         """The world's exact state (b2g_state_save) as a uint8 array."""

@@ -95,6 +95,13 @@ struct World {
     bool warm = true, continuous = false, allow_sleep = true, auto_clear = true;
     int toi_schedule = 0;  /* B2G_TOI_SCHEDULE_* */
     bool asleep_seen = false;  /* a body was created asleep or put to sleep by the caller */
+    /* joints: definitions, host copies of their impulses, the colouring, body -> joints */
+    std::vector<b2g_joint_def> joints;
+    std::vector<float4> h_jimp, h_jimp2;
+    std::vector<int> h_jorder, h_jcoff, h_jnt_off, h_jnt;
+    bool joints_dirty = false;          /* joints changed since the device copy */
+    bool joint_filter_pending = false;  /* contacts of newly joined bodies to flag for filtering */
+    int joint_cap = 0;                  /* joints the device arrays hold */
     bool record_events = false, record_pairs = false;
     bool new_contacts = false;
     float inv_dt0 = 0.0f;
@@ -226,11 +233,26 @@ int dalloc(World* w, T** p, size_t n) {
 
 void drop_graphs(World* w);
 
+/* frees one dalloc'd buffer */
+template <class T>
+void dfree(World* w, T** p) {
+    if (!*p) return;
+    auto it = std::find(w->allocations.begin(), w->allocations.end(), (void*)*p);
+    if (it != w->allocations.end()) {
+        w->alloc_bytes.erase(w->alloc_bytes.begin() + (it - w->allocations.begin()));
+        w->allocations.erase(it);
+    }
+    cudaFree(*p);
+    *p = nullptr;
+}
+
 void free_all(World* w) {
     drop_graphs(w);
     for (void* p : w->allocations) cudaFree(p);
     w->allocations.clear();
     w->alloc_bytes.clear();
+    w->joint_cap = 0;
+    w->d.j_body = nullptr;  /* the joint arrays went with the rest */
     w->allocated = false;
     ++w->alloc_generation;
 }
@@ -559,6 +581,7 @@ int allocate(World* w, int nb, int nf) {
     A(d.bp_quad_box, 4 * (size_t)fix_cap); A(d.bp_quad_child, fix_cap);
     A(d.bp_world_root, 2 * (size_t)w->num_worlds); A(d.bp_world_first, 2 * (size_t)w->num_worlds);
     A(d.b_fix_off, (size_t)body_cap + 1); A(d.b_fix, fix_cap);
+    A(d.b_jnt_off, (size_t)body_cap + 1);
     A(d.b_alpha0, body_cap); A(d.b_stamp, body_cap); A(d.b_event, body_cap); A(d.b_inval, body_cap);
     A(d.b_cx, body_cap); A(d.b_sync, body_cap); A(d.b_best, body_cap); A(d.b_bkey, body_cap);
     A(d.f_leaf, fix_cap);
@@ -635,11 +658,123 @@ int download_state(World* w) {
     return B2G_OK;
 }
 
+inline float __uint_as_float_host(uint32_t u) {
+    float f;
+    memcpy(&f, &u, sizeof(f));
+    return f;
+}
+
+/* The joints' impulses from the device into the host copies (before the device arrays change) */
+int download_joint_impulses(World* w) {
+    const int n = w->d.n_joints;
+    if (w->joint_cap == 0 || n == 0 || !w->device_authoritative) return B2G_OK;
+    CUDA_OK(w, cudaMemcpy(w->h_jimp.data(), w->d.j_imp, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    CUDA_OK(w, cudaMemcpy(w->h_jimp2.data(), w->d.j_imp2, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    return B2G_OK;
+}
+
+/* Uploads the joints: definitions, impulses, the colouring (greedy, in creation order: a joint takes
+ * the first colour no earlier joint on one of its dynamic bodies has, so joints of a colour share no
+ * body the solver writes) and body -> joints. */
+int upload_joints(World* w) {
+    DevWorld& d = w->d;
+    const int nj = (int)w->joints.size();
+    const int nb = (int)w->h_flags.size();
+    cudaStream_t s = w->stream;
+    if (nj > w->joint_cap) {
+        dfree(w, &d.j_body); dfree(w, &d.j_anchor); dfree(w, &d.j_lim); dfree(w, &d.j_par); dfree(w, &d.j_imp);
+        dfree(w, &d.j_imp2); dfree(w, &d.j_rr); dfree(w, &d.j_k); dfree(w, &d.j_m); dfree(w, &d.j_s);
+        dfree(w, &d.j_order); dfree(w, &d.j_coff); dfree(w, &d.b_jnt);
+        int rc = B2G_OK;
+        const int cap = nj;
+        if ((rc = dalloc(w, &d.j_body, cap)) || (rc = dalloc(w, &d.j_anchor, cap)) || (rc = dalloc(w, &d.j_lim, cap)) ||
+            (rc = dalloc(w, &d.j_par, cap)) || (rc = dalloc(w, &d.j_imp, cap)) || (rc = dalloc(w, &d.j_imp2, cap)) ||
+            (rc = dalloc(w, &d.j_rr, cap)) || (rc = dalloc(w, &d.j_k, cap)) || (rc = dalloc(w, &d.j_m, cap)) ||
+            (rc = dalloc(w, &d.j_s, cap)) || (rc = dalloc(w, &d.j_order, cap)) ||
+            (rc = dalloc(w, &d.j_coff, kMaxJointColours + 1)) || (rc = dalloc(w, &d.b_jnt, 2 * (size_t)cap)))
+            return rc;
+        w->joint_cap = cap;
+        drop_graphs(w);
+        ++w->alloc_generation;
+    }
+    std::vector<int> colour(nj, 0);
+    std::vector<uint64_t> used(nb, 0);
+    int ncol = 0;
+    for (int j = 0; j < nj; ++j) {
+        const uint32_t a = w->joints[j].body_a, b = w->joints[j].body_b;
+        const bool da = (w->h_flags[a] & BF_TYPE_MASK) == BODY_DYNAMIC, db = (w->h_flags[b] & BF_TYPE_MASK) == BODY_DYNAMIC;
+        const uint64_t busy = (da ? used[a] : 0ull) | (db ? used[b] : 0ull);
+        int c = 0;
+        while (c < kMaxJointColours && (busy >> c) & 1ull) ++c;
+        if (c == kMaxJointColours) return fail(w, B2G_ERR_CAPACITY, "a body has more joints than the joint colouring holds (64)");
+        colour[j] = c;
+        if (da) used[a] |= 1ull << c;
+        if (db) used[b] |= 1ull << c;
+        ncol = std::max(ncol, c + 1);
+    }
+    w->h_jcoff.assign(kMaxJointColours + 1, 0);
+    for (int j = 0; j < nj; ++j) ++w->h_jcoff[colour[j] + 1];
+    for (int c = 0; c < kMaxJointColours; ++c) w->h_jcoff[c + 1] += w->h_jcoff[c];
+    w->h_jorder.assign(nj, 0);
+    {
+        std::vector<int> fill(w->h_jcoff.begin(), w->h_jcoff.end() - 1);
+        for (int j = 0; j < nj; ++j) w->h_jorder[fill[colour[j]]++] = j;
+    }
+    w->h_jnt_off.assign((size_t)nb + 1, 0);
+    for (int j = 0; j < nj; ++j) {
+        ++w->h_jnt_off[(size_t)w->joints[j].body_a + 1];
+        ++w->h_jnt_off[(size_t)w->joints[j].body_b + 1];
+    }
+    for (int b = 0; b < nb; ++b) w->h_jnt_off[(size_t)b + 1] += w->h_jnt_off[b];
+    w->h_jnt.assign(std::max(2 * nj, 1), 0);
+    {
+        std::vector<int> fill(w->h_jnt_off.begin(), w->h_jnt_off.end() - 1);
+        for (int j = 0; j < nj; ++j) {
+            w->h_jnt[(size_t)fill[w->joints[j].body_a]++] = j;
+            w->h_jnt[(size_t)fill[w->joints[j].body_b]++] = j;
+        }
+    }
+#define U(dst, src, n) CUDA_OK(w, cudaMemcpyAsync((dst), (src), (size_t)(n) * sizeof(*(dst)), cudaMemcpyHostToDevice, s))
+    U(d.b_jnt_off, w->h_jnt_off.data(), nb + 1);
+    if (nj > 0) {
+        std::vector<int2> jb(nj);
+        std::vector<float4> an(nj), lim(nj), par(nj);
+        for (int j = 0; j < nj; ++j) {
+            const b2g_joint_def& jd = w->joints[j];
+            jb[j] = make_int2((int)jd.body_a, (int)jd.body_b);
+            an[j] = make_float4(jd.local_anchor_a.x, jd.local_anchor_a.y, jd.local_anchor_b.x, jd.local_anchor_b.y);
+            lim[j] = make_float4(jd.reference_angle, jd.lower_angle, jd.upper_angle, jd.motor_speed);
+            const uint32_t fl = (jd.enable_limit ? JF_LIMIT : 0u) | (jd.enable_motor ? JF_MOTOR : 0u) |
+                                (jd.collide_connected ? JF_COLLIDE : 0u);
+            par[j] = make_float4(jd.max_motor_torque, __uint_as_float_host(fl), 0.0f, 0.0f);
+        }
+        U(d.j_body, jb.data(), nj);
+        U(d.j_anchor, an.data(), nj);
+        U(d.j_lim, lim.data(), nj);
+        U(d.j_par, par.data(), nj);
+        U(d.j_imp, w->h_jimp.data(), nj);
+        U(d.j_imp2, w->h_jimp2.data(), nj);
+        U(d.j_order, w->h_jorder.data(), nj);
+        U(d.j_coff, w->h_jcoff.data(), kMaxJointColours + 1);
+        U(d.b_jnt, w->h_jnt.data(), 2 * nj);
+    }
+#undef U
+    CUDA_OK(w, cudaStreamSynchronize(s));
+    d.n_joints = nj;
+    d.n_jcolours = ncol;
+    w->joints_dirty = false;
+    return B2G_OK;
+}
+
 /* Makes the device hold every created body and fixture; grows capacities by rebuilding. */
 int prepare(World* w) {
     const int nb = (int)w->h_flags.size();
     const int nf = (int)w->h_fbody.size();
-    if (w->allocated && nb == w->uploaded_bodies && nf == w->uploaded_fixtures) return B2G_OK;
+    if (w->allocated && nb == w->uploaded_bodies && nf == w->uploaded_fixtures && !w->joints_dirty) return B2G_OK;
+    {
+        int rc = download_joint_impulses(w);
+        if (rc != B2G_OK) return rc;
+    }
     if (w->allocated && (nb > w->d.body_cap || nf > w->d.fix_cap)) {
         /* rebuild: keep the current contact table (its keys and impulses) across the reallocation */
         CUDA_OK(w, cudaStreamSynchronize(w->stream));
@@ -704,7 +839,9 @@ int prepare(World* w) {
         w->d.key_bits = kb;
     }
     w->d.morton_world_bits = bits_for((uint64_t)(2 * w->num_worlds - 1));  /* key worlds: 2 per world */
-    return upload(w);
+    int rc = upload(w);
+    if (rc != B2G_OK) return rc;
+    return upload_joints(w);
 }
 
 int status_error(World* w, int status);
@@ -840,6 +977,11 @@ int step(World* w, float dt, int vi, int pi) {
     if (rc != B2G_OK) return rc;
     rc = ensure_minsep_buffers(w, pi);
     if (rc != B2G_OK) return rc;
+    if (w->joint_filter_pending) {
+        /* B2world::create_joint flags the contacts of the joined bodies (b2_world.rs:258-271) */
+        launch_flag_joint_contacts(w->d, w->stream, w->num_sms);
+        w->joint_filter_pending = false;
+    }
     w->device_authoritative = true;
     if (w->tape && w->tape->recording) {
         if (dt > 0.0f) ++w->tape->steps;
@@ -1171,6 +1313,67 @@ int b2g_create_fixtures(void* p, const b2g_fixture_def* defs, int32_t n, uint32_
         w->new_contacts = true;
         if (ids) ids[i] = (uint32_t)f;
     }
+    return B2G_OK;
+}
+
+int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* ids) {
+    World* w = W(p);
+    if (!w || (!defs && n > 0) || n < 0) return B2G_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i) {
+        const b2g_joint_def& d = defs[i];
+        if (d.type != B2G_JOINT_REVOLUTE) return fail(w, B2G_ERR_UNSUPPORTED, "only revolute joints are on the GPU path");
+        if (d.body_a >= w->h_flags.size() || d.body_b >= w->h_flags.size() || d.body_a == d.body_b)
+            return fail(w, B2G_ERR_INVALID_ARG, "joint body ids out of range or equal");
+    }
+    if (n > 0) tape_touch(w);
+    if (w->device_authoritative) {
+        int rc = download_joint_impulses(w);
+        if (rc != B2G_OK) return rc;
+    }
+    for (int i = 0; i < n; ++i) {
+        if (ids) ids[i] = (uint32_t)w->joints.size();
+        w->joints.push_back(defs[i]);
+        w->h_jimp.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        w->h_jimp2.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        if (!defs[i].collide_connected) w->joint_filter_pending = true;
+    }
+    if (n > 0) w->joints_dirty = true;
+    return B2G_OK;
+}
+
+int b2g_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) {
+    World* w = W(p);
+    if (!w || (!out && count)) return B2G_ERR_INVALID_ARG;
+    if ((size_t)first + count > w->joints.size()) return fail(w, B2G_ERR_INVALID_ARG, "joint range out of bounds");
+    if (count == 0) return B2G_OK;
+    if (w->device_authoritative && !w->joints_dirty) {
+        int rc = check_status(w);
+        if (rc != B2G_OK) return rc;
+        rc = download_joint_impulses(w);
+        if (rc != B2G_OK) return rc;
+    }
+    for (uint32_t i = 0; i < count; ++i) {
+        const float4 a = w->h_jimp[first + i], b = w->h_jimp2[first + i];
+        out[5 * i + 0] = a.x;
+        out[5 * i + 1] = a.y;
+        out[5 * i + 2] = a.z;
+        out[5 * i + 3] = a.w;
+        out[5 * i + 4] = b.x;
+    }
+    return B2G_OK;
+}
+
+int b2g_get_joint_order(void* p, uint32_t* out, int32_t cap, int32_t* n) {
+    World* w = W(p);
+    if (!w || !n || (!out && cap > 0)) return B2G_ERR_INVALID_ARG;
+    if (!w->h_flags.empty()) {
+        int rc = prepare(w);
+        if (rc != B2G_OK) return rc;
+    }
+    const int nj = (int)w->h_jorder.size();
+    *n = nj;
+    if (cap < nj) return fail(w, B2G_ERR_CAPACITY, "joint order buffer too small");
+    for (int i = 0; i < nj; ++i) out[i] = (uint32_t)w->h_jorder[i];
     return B2G_OK;
 }
 
@@ -2386,6 +2589,7 @@ int b2g_tape_begin(void* p, int32_t max_steps, int32_t every, int64_t max_slots)
     if (w->h_flags.empty()) return fail(w, B2G_ERR_INVALID_ARG, "the world has no bodies");
     if (w->allow_sleep)
         return fail(w, B2G_ERR_UNSUPPORTED, "the tape needs sleeping off: call b2g_set_allow_sleeping(world, 0)");
+    if (!w->joints.empty()) return fail(w, B2G_ERR_UNSUPPORTED, "the tape does not record joints");
     int rc = prepare(w);
     if (rc != B2G_OK) return rc;
     tape_free(w);

@@ -118,8 +118,21 @@ __device__ __forceinline__ int contact_kind(int ta, int tb) {
     return tb == SHAPE_CIRCLE ? KIND_EDGE_CIRCLE : KIND_EDGE_POLYGON;
 }
 
+/* the joint part of B2body::should_collide (private/dynamics/b2_body.rs:399-413): no joint between
+ * the two bodies keeps them from colliding */
+__device__ __forceinline__ bool joint_allows(const DevWorld& w, int a, int b) {
+    for (int e = w.b_jnt_off[a]; e < w.b_jnt_off[a + 1]; ++e) {
+        const int j = w.b_jnt[e];
+        const int2 jb = w.j_body[j];
+        const int other = jb.x == a ? jb.y : jb.x;
+        if (other == b && !(__float_as_uint(w.j_par[j].y) & JF_COLLIDE)) return false;
+    }
+    return true;
+}
+
 /* b2_contact_manager_add_pair's rejections after the existing-contact check
- * (private/dynamics/b2_contact_manager.rs:178-302): same body, no dynamic body, the default
+ * (private/dynamics/b2_contact_manager.rs:178-302): same body, no dynamic body, a joint that keeps
+ * the bodies apart, the default
  * filter (private/dynamics/b2_world_callbacks.rs:6-18), no manifold routine for the two shape types
  * (b2_contact_registers.rs:67-103). f is the fixture with the smaller proxy id. On acceptance
  * (fa, fb) is the contact's fixture pair, fixture A the one of the primary shape type. */
@@ -130,6 +143,7 @@ __device__ __forceinline__ bool pair_accept(const DevWorld& w, int f, int g, int
     if (ba == bb) return false;
     const uint32_t fla = w.b_flags[ba], flb = w.b_flags[bb];
     if ((fla & BF_TYPE_MASK) != BODY_DYNAMIC && (flb & BF_TYPE_MASK) != BODY_DYNAMIC) return false;
+    if (!joint_allows(w, bb, ba)) return false;
     /* f_filter = category | mask << 16, f_group = group (int16) | sensor << 16 */
     const uint32_t xa = w.f_filter[fa], xb = w.f_filter[fb];
     const int grp_a = (int)(int16_t)(w.f_group[fa] & 0xffffu);

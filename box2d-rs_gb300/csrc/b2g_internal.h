@@ -44,7 +44,15 @@ enum : uint32_t {
     CF_ENABLED = 1u << 1,
     CF_DEAD = 1u << 2,
     CF_SENSOR = 1u << 3,
+    CF_FILTER = 1u << 4,   /* E_FILTER_FLAG: re-check should_collide at the next collide */
     CF_KIND_SHIFT = 8,
+};
+
+/* revolute joint flag bits (j_par.y) */
+enum : uint32_t {
+    JF_LIMIT = 1u << 0,
+    JF_MOTOR = 1u << 1,
+    JF_COLLIDE = 1u << 2,  /* collide_connected */
 };
 
 /* device status bits (sticky until read by the host) */
@@ -113,6 +121,7 @@ constexpr int kMaxPosIters = 64;
 constexpr int kNoWake = 0x7f7f7f7f;  /* b_wake's "not woken" (a byte-wise memset value) */
 /* continuous pass lists (k_continuous.cu): partner contacts of one event, events of one
  * iteration, contacts created in one pass */
+constexpr int kMaxJointColours = 64;  /* colours of the joint colouring */
 constexpr int kToiCand = 64;
 constexpr int kToiEvCap = 4096;
 constexpr int kToiNewCap = 4096;
@@ -240,6 +249,14 @@ struct DevWorld {
                                     INT_MIN if empty; key world w + num_worlds holds world w's large
                                     static proxies (see k_bp_keys) */
     int* bp_world_first;         /* per key world: first sorted leaf */
+    /* joints (revolute): definitions, impulses kept across steps, the step's temporaries, the
+     * joints sorted by colour (j_order, j_coff: n_jcolours + 1 offsets) and body -> joints */
+    int n_joints, n_jcolours;
+    int2* j_body;
+    float4 *j_anchor, *j_lim, *j_par, *j_imp, *j_imp2, *j_rr, *j_k, *j_m;
+    float2* j_s;
+    int *j_order, *j_coff;
+    int *b_jnt_off, *b_jnt;
     /* continuous physics: the time-of-impact pass (k_continuous.cu) */
     int* b_fix_off;              /* body -> fixtures: offsets into b_fix (n_bodies + 1) */
     int* b_fix;                  /* fixtures grouped by body */
@@ -289,6 +306,8 @@ struct DevWorld {
 /* may_sleep: some body may be asleep (sleeping allowed, or a body made asleep): contacts then see
  * the bodies woken by contacts before them in the table's key order, as in the reference's list */
 void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s, bool may_sleep, int num_sms);
+/* flags the contacts of bodies a joint keeps apart (after joints were created) */
+void launch_flag_joint_contacts(const DevWorld& w, cudaStream_t s, int num_sms);
 void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cudaStream_t s);
 /* parts: allow the part-local solve (used where the world's size suits it) */
 void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms, bool parts);

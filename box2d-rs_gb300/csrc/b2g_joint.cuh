@@ -1,0 +1,232 @@
+/*
+ * b2g_joint.cuh — the revolute joint on the device (B2revoluteJoint,
+ * private/dynamics/joints/b2_revolute_joint.rs:21-287): init_velocity_constraints (anchors,
+ * effective masses, warm start), solve_velocity_constraints (motor, lower and upper limits, the
+ * point constraint) and solve_position_constraints (angular limit, then the point), each the
+ * reference's sequence of IEEE f32 operations (built without fused multiply-add).
+ *
+ * Joint j's definition: j_body (A, B), j_anchor (local anchor A, local anchor B), j_lim
+ * (reference angle, lower, upper, motor speed), j_par (max motor torque, flag bits); its impulses
+ * (kept across steps for warm starting): j_imp (x, y, motor, lower), j_imp2.x (upper); the
+ * step's temporaries: j_rr (rA, rB), j_k (K ex.x, ex.y, ey.x, ey.y), j_m (1/mA, 1/mB, 1/IA, 1/IB),
+ * j_s (axial mass, angle). Bodies are read and written in the global arrays; only dynamic bodies
+ * are written (the others have zero inverse mass, so the reference leaves them unchanged).
+ */
+#ifndef B2G_JOINT_CUH
+#define B2G_JOINT_CUH
+
+#include "b2g_internal.h"
+
+namespace b2g {
+namespace {
+
+constexpr float kAngularSlop = 2.0f / 180.0f * kPi;           /* B2_ANGULAR_SLOP */
+constexpr float kMaxAngularCorrection = 8.0f / 180.0f * kPi;  /* B2_MAX_ANGULAR_CORRECTION */
+
+__device__ __forceinline__ bool joint_body_dynamic(const DevWorld& w, int b) {
+    return (w.b_flags[b] & BF_TYPE_MASK) == BODY_DYNAMIC;
+}
+
+/* B2Mat22::solve, src/b2_math.rs:278-293 */
+__device__ __forceinline__ V2 mat22_solve(float a11, float a21, float a12, float a22, V2 b) {
+    float det = a11 * a22 - a12 * a21;
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    return mk(det * (a22 * b.x - a12 * b.y), det * (a11 * b.y - a21 * b.x));
+}
+
+/* init_velocity_constraints, b2_revolute_joint.rs:21-116 */
+__device__ void joint_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 an = w.j_anchor[j];
+    const float4 lim = w.j_lim[j];
+    const uint32_t jf = __float_as_uint(w.j_par[j].y);
+    const float4 massA = w.b_mass[bd.x], massB = w.b_mass[bd.y];
+    const float2 lcA = w.b_lc[bd.x], lcB = w.b_lc[bd.y];
+    const float mA = massA.y, mB = massB.y, iA = massA.w, iB = massB.w;
+    const float aA = w.b_pos[bd.x].z, aB = w.b_pos[bd.y].z;
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = rot(aA), qB = rot(aB);
+    const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+    const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+    float4 K;
+    K.x = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;     /* ex.x */
+    K.z = -rA.y * rA.x * iA - rB.y * rB.x * iB;              /* ey.x */
+    K.y = K.z;                                               /* ex.y */
+    K.w = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;     /* ey.y */
+    float axial = iA + iB;
+    bool fixed_rotation;
+    if (axial > 0.0f) {
+        axial = fdiv(1.0f, axial);
+        fixed_rotation = false;
+    } else {
+        fixed_rotation = true;
+    }
+    const float angle = aB - aA - lim.x;
+    float4 imp = w.j_imp[j];
+    float upper = w.j_imp2[j].x;
+    if (!(jf & JF_LIMIT) || fixed_rotation) {
+        imp.w = 0.0f;
+        upper = 0.0f;
+    }
+    if (!(jf & JF_MOTOR) || fixed_rotation) imp.z = 0.0f;
+    if (sp.warm) {
+        imp.x *= sp.dt_ratio;
+        imp.y *= sp.dt_ratio;
+        imp.z *= sp.dt_ratio;
+        imp.w *= sp.dt_ratio;
+        upper *= sp.dt_ratio;
+        const float axial_impulse = imp.z + imp.w - upper;
+        const V2 P = mk(imp.x, imp.y);
+        vA = sub(vA, scale(mA, P));
+        wA -= iA * (cross(rA, P) + axial_impulse);
+        vB = add(vB, scale(mB, P));
+        wB += iB * (cross(rB, P) + axial_impulse);
+    } else {
+        imp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        upper = 0.0f;
+    }
+    w.j_imp[j] = imp;
+    w.j_imp2[j] = make_float4(upper, 0.0f, 0.0f, 0.0f);
+    w.j_rr[j] = make_float4(rA.x, rA.y, rB.x, rB.y);
+    w.j_k[j] = K;
+    w.j_m[j] = make_float4(mA, mB, iA, iB);
+    w.j_s[j] = make_float2(axial, angle);
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+/* solve_velocity_constraints, b2_revolute_joint.rs:118-208 */
+__device__ void joint_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 lim = w.j_lim[j];
+    const float4 par = w.j_par[j];
+    const uint32_t jf = __float_as_uint(par.y);
+    const float4 m = w.j_m[j];
+    const float mA = m.x, mB = m.y, iA = m.z, iB = m.w;
+    const float4 rr = w.j_rr[j];
+    const V2 rA = mk(rr.x, rr.y), rB = mk(rr.z, rr.w);
+    const float2 s = w.j_s[j];
+    const float axial = s.x, angle = s.y;
+    float4 imp = w.j_imp[j];
+    float upper = w.j_imp2[j].x;
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const bool fixed_rotation = iA + iB == 0.0f;
+    if ((jf & JF_MOTOR) && !fixed_rotation) {
+        const float cdot = wB - wA - lim.w;
+        float impulse = -axial * cdot;
+        const float old_impulse = imp.z;
+        const float max_impulse = sp.dt * par.x;
+        imp.z = fclampr(imp.z + impulse, -max_impulse, max_impulse);
+        impulse = imp.z - old_impulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    if ((jf & JF_LIMIT) && !fixed_rotation) {
+        {
+            const float C = angle - lim.y;
+            const float cdot = wB - wA;
+            float impulse = -axial * (cdot + fmaxr(C, 0.0f) * sp.inv_dt);
+            const float old_impulse = imp.w;
+            imp.w = fmaxr(imp.w + impulse, 0.0f);
+            impulse = imp.w - old_impulse;
+            wA -= iA * impulse;
+            wB += iB * impulse;
+        }
+        {
+            const float C = lim.z - angle;
+            const float cdot = wA - wB;
+            float impulse = -axial * (cdot + fmaxr(C, 0.0f) * sp.inv_dt);
+            const float old_impulse = upper;
+            upper = fmaxr(upper + impulse, 0.0f);
+            impulse = upper - old_impulse;
+            wA += iA * impulse;
+            wB -= iB * impulse;
+        }
+    }
+    {
+        const V2 cdot = sub(sub(add(vB, cross_sv(wB, rB)), vA), cross_sv(wA, rA));
+        const float4 K = w.j_k[j];
+        const V2 impulse = mat22_solve(K.x, K.y, K.z, K.w, neg(cdot));
+        imp.x += impulse.x;
+        imp.y += impulse.y;
+        vA = sub(vA, scale(mA, impulse));
+        wA -= iA * cross(rA, impulse);
+        vB = add(vB, scale(mB, impulse));
+        wB += iB * cross(rB, impulse);
+    }
+    w.j_imp[j] = imp;
+    w.j_imp2[j].x = upper;
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+/* solve_position_constraints, b2_revolute_joint.rs:210-287; returns whether the joint is
+ * within the linear and angular slop */
+__device__ bool joint_solve_position(const DevWorld& w, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 an = w.j_anchor[j];
+    const float4 lim = w.j_lim[j];
+    const uint32_t jf = __float_as_uint(w.j_par[j].y);
+    const float4 m = w.j_m[j];
+    const float mA = m.x, mB = m.y, iA = m.z, iB = m.w;
+    const float axial = w.j_s[j].x;
+    const float2 lcA = w.b_lc[bd.x], lcB = w.b_lc[bd.y];
+    float4 pa = w.b_pos[bd.x], pb = w.b_pos[bd.y];
+    V2 cA = mk(pa.x, pa.y), cB = mk(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    float angular_error = 0.0f;
+    const bool fixed_rotation = iA + iB == 0.0f;
+    if ((jf & JF_LIMIT) && !fixed_rotation) {
+        const float angle = aB - aA - lim.x;
+        float C = 0.0f;
+        if (fabsr(lim.z - lim.y) < 2.0f * kAngularSlop) {
+            C = fclampr(angle - lim.y, -kMaxAngularCorrection, kMaxAngularCorrection);
+        } else if (angle <= lim.y) {
+            C = fclampr(angle - lim.y + kAngularSlop, -kMaxAngularCorrection, 0.0f);
+        } else if (angle >= lim.z) {
+            C = fclampr(angle - lim.z - kAngularSlop, 0.0f, kMaxAngularCorrection);
+        }
+        const float limit_impulse = -axial * C;
+        aA -= iA * limit_impulse;
+        aB += iB * limit_impulse;
+        angular_error = fabsr(C);
+    }
+    float position_error;
+    {
+        const Rot qA = rot(aA), qB = rot(aB);
+        const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+        const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+        const V2 C = sub(sub(add(cB, rB), cA), rA);
+        position_error = length(C);
+        const float kxx = mA + mB + iA * rA.y * rA.y + iB * rB.y * rB.y;
+        const float kxy = -iA * rA.x * rA.y - iB * rB.x * rB.y;
+        const float kyy = mA + mB + iA * rA.x * rA.x + iB * rB.x * rB.x;
+        const V2 impulse = neg(mat22_solve(kxx, kxy, kxy, kyy, C));
+        cA = sub(cA, scale(mA, impulse));
+        aA -= iA * cross(rA, impulse);
+        cB = add(cB, scale(mB, impulse));
+        aB += iB * cross(rB, impulse);
+    }
+    if (joint_body_dynamic(w, bd.x)) w.b_pos[bd.x] = make_float4(cA.x, cA.y, aA, pa.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_pos[bd.y] = make_float4(cB.x, cB.y, aB, pb.w);
+    return position_error <= kLinearSlop && angular_error <= kAngularSlop;
+}
+
+/* the joint belongs to an island solved this step (a body of it is non-static and in one); both
+ * bodies enabled (private/dynamics/b2_world.rs:476-479) */
+__device__ __forceinline__ int joint_island(const DevWorld& w, int j) {
+    const int2 bd = w.j_body[j];
+    const uint32_t fa = w.b_flags[bd.x], fb = w.b_flags[bd.y];
+    if (!(fa & BF_ENABLED) || !(fb & BF_ENABLED)) return -1;
+    if ((fa & BF_TYPE_MASK) != BODY_STATIC && (fa & BF_ISLAND)) return w.b_island[bd.x];
+    if ((fb & BF_TYPE_MASK) != BODY_STATIC && (fb & BF_ISLAND)) return w.b_island[bd.y];
+    return -1;
+}
+
+}  // namespace
+}  // namespace b2g
+#endif

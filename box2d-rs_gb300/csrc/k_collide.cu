@@ -44,13 +44,21 @@ __device__ __forceinline__ bool collide_contact(const DevWorld& w, const StepPar
     const int2 bd = w.c.body[i];
     const uint32_t fa_flags = w.b_flags[bd.x];
     const uint32_t fb_flags = w.b_flags[bd.y];
-    if (!active_for(w, bd.x, fa_flags, i, deferred) && !active_for(w, bd.y, fb_flags, i, deferred)) return false;
+    bool destroy = false;
+    if (flags & CF_FILTER) {
+        /* flagged by a new joint: should these bodies collide? (the default filter's answer does
+         * not change) */
+        if (!joint_allows(w, bd.y, bd.x)) destroy = true;
+        else w.c.flags[i] = flags = flags & ~CF_FILTER;
+    }
+    if (!destroy && !active_for(w, bd.x, fa_flags, i, deferred) && !active_for(w, bd.y, fb_flags, i, deferred))
+        return false;
     const float4 A = w.f_fat[fx.x];
     const float4 B = w.f_fat[fx.y];
     const bool was_touching = (flags & CF_TOUCHING) != 0;
     const uint4 ids = w.c.mids[i];
     const int old_count = (int)((ids.z >> 8) & 0xffu);
-    if (!overlap4(A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w)) {
+    if (destroy || !overlap4(A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w)) {
         /* destroyed after the pass (the reference collects them and destroys them after its loop) */
         if (sp.record_events && was_touching) push_event(w, 1, fx.x, fx.y);
         if (old_count > 0 && !(flags & CF_SENSOR)) {
@@ -119,6 +127,21 @@ __global__ void k_collide_wake(DevWorld w) {
             w.b_dwake[b] = 0;
         }
     }
+}
+
+/* B2world::create_joint (private/dynamics/b2_world.rs:258-271): the contacts between two bodies
+ * joined without collide_connected are flagged for filtering at the next collide */
+__global__ void k_flag_joint_contacts(DevWorld w) {
+    const int n = w.cnt[CNT_CONTACTS];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int2 bd = w.c.body[i];
+        if (!joint_allows(w, bd.y, bd.x)) w.c.flags[i] |= CF_FILTER;
+    }
+}
+
+void launch_flag_joint_contacts(const DevWorld& w, cudaStream_t s, int num_sms) {
+    k_flag_joint_contacts<<<grid_for(w.contact_cap, 256, num_sms * 8), 256, 0, s>>>(w);
+    B2G_LAUNCHED(1);
 }
 
 void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s, bool may_sleep, int num_sms) {

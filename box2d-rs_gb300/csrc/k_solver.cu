@@ -29,6 +29,7 @@
  * gives bit-identical bodies, because each operation is the same IEEE f32 operation.
  */
 #include "b2g_internal.h"
+#include "b2g_joint.cuh"
 #include "b2g_solver_math.cuh"
 #include "b2g_sync.cuh"
 
@@ -83,6 +84,13 @@ __global__ void k_island_union(DevWorld w) {
         if (!contact_is_constraint(w.c.flags[i])) continue;
         const int2 bd = w.c.body[i];
         if (is_static(w.b_flags[bd.x]) || is_static(w.b_flags[bd.y])) continue;
+        uf_union(w.b_island, bd.x, bd.y);
+    }
+    /* joints join islands too, unless a body is disabled (private/dynamics/b2_world.rs:466-489) */
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.n_joints; j += gridDim.x * blockDim.x) {
+        const int2 bd = w.j_body[j];
+        const uint32_t fa = w.b_flags[bd.x], fb = w.b_flags[bd.y];
+        if (is_static(fa) || is_static(fb) || !(fa & BF_ENABLED) || !(fb & BF_ENABLED)) continue;
         uf_union(w.b_island, bd.x, bd.y);
     }
 }
@@ -1049,8 +1057,24 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
                 if (!grid_barrier(w)) return;
             }
         }
-        /* phase 3: velocity iterations */
+        /* phase 2b: the joints' init_velocity_constraints (with their warm start) follow the
+         * contacts' warm start, joint colour by joint colour (b2_island_private.rs:196-201) */
+        for (int c = 0; c < w.n_jcolours; ++c) {
+            for (int q = w.j_coff[c] + gtid; q < w.j_coff[c + 1]; q += gsize) {
+                const int j = w.j_order[q];
+                if (joint_island(w, j) >= 0) joint_init_velocity(w, sp, j);
+            }
+            if (!grid_barrier(w)) return;
+        }
+        /* phase 3: velocity iterations, joints before contacts (:205-215) */
         for (int it = 0; it < sp.vi; ++it) {
+            for (int c = 0; c < w.n_jcolours; ++c) {
+                for (int q = w.j_coff[c] + gtid; q < w.j_coff[c + 1]; q += gsize) {
+                    const int j = w.j_order[q];
+                    if (joint_island(w, j) >= 0) joint_solve_velocity(w, sp, j);
+                }
+                if (!grid_barrier(w)) return;
+            }
             for (int c = 0; c < ncol; ++c) {
                 const int beg = w.col_off[c], end = w.col_off[c + 1];
                 for (int k = beg + gtid; k < end; k += gsize) solve_velocity_slot(w, k);
@@ -1154,6 +1178,21 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
                 if (done) continue;
                 const float ms = solve_position_slot(w, k);
                 if (ms < 0.0f) atomicMax(&cur[isl], __float_as_uint(-ms));
+            }
+            if (!grid_barrier(w)) return;
+        }
+        /* the joints after the contacts; a joint out of its slop keeps its island going
+         * (contacts_okay && joints_okay, b2_island_private.rs:257-274) */
+        for (int c = 0; c < w.n_jcolours; ++c) {
+            for (int q = w.j_coff[c] + gtid; q < w.j_coff[c + 1]; q += gsize) {
+                const int j = w.j_order[q];
+                const int isl = joint_island(w, j);
+                if (isl < 0) continue;
+                bool done = false;
+                for (int jt = 0; jt < it && !done; ++jt)
+                    done = __uint_as_float(w.isl_minsep[(size_t)jt * w.body_cap + isl]) <= tol;
+                if (done) continue;
+                if (!joint_solve_position(w, j)) atomicMax(&cur[isl], __float_as_uint(kMaxFloat));
             }
             if (!grid_barrier(w)) return;
         }
@@ -1293,7 +1332,10 @@ int part_count(const DevWorld& w, int num_sms) {
 constexpr int kPartMaxProxiesPerSm = 2048;
 
 bool use_parts(const DevWorld& w, int num_sms, bool allowed) {
-    return allowed && w.n_fixtures > 0 && (long long)w.n_fixtures <= (long long)num_sms * kPartMaxProxiesPerSm;
+    /* joints are solved grid-wide before each contact sweep, so a world with joints runs the
+     * grid-wide colour schedule */
+    return allowed && w.n_joints == 0 && w.n_fixtures > 0 &&
+           (long long)w.n_fixtures <= (long long)num_sms * kPartMaxProxiesPerSm;
 }
 
 void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms, bool parts) {

@@ -14,6 +14,7 @@ stream, so the GPU world and the CPU oracle receive identical f32 inputs.
   throw_stack    8 x 8 stack of boxes (half-extent 0.25) and a circle projectile (r 0.5)
   hello_world    box2d-rs tests/test.rs:26-102
   toi_rain       fast bodies (60-250 m/s) onto thin static plates, for continuous physics
+  bridge         30 planks joined by revolute joints, bodies dropped on it, a motor and limits
 """
 from __future__ import annotations
 
@@ -446,8 +447,55 @@ def toi_rain_batch(seeds=(7, 8, 9, 10), n=32, steps=90):
                   continuous=True)
 
 
+def bridge(planks=30, seed=13, steps=240, drops=24):
+    """A bridge of planks joined by revolute joints between two static posts (box2d-rs testbed
+    bridge), with circles and boxes dropped on it; a motorised wheel and a hinged flap with limits
+    on the side."""
+    rng = SplitMix64(seed)
+    n_extra = 2
+    bodies = b2g.body_defs(1 + planks + drops + n_extra)
+    bodies["allow_sleep"] = 0
+    fixtures = [b2g.edge_fixture(0, (-40.0, 0.0), (40.0, 0.0))]
+    joints = []
+    x0 = -14.5
+    for i in range(planks):
+        b = 1 + i
+        bodies[b]["type"] = b2g.DYNAMIC
+        bodies[b]["position"] = (x0 + 1.0 * i, 5.0)
+        fixtures.append(b2g.box_fixture(b, 0.5, 0.125, density=20.0, friction=0.2))
+        prev = 0 if i == 0 else b - 1
+        anchor = (x0 - 0.5 + 1.0 * i, 5.0)
+        la = anchor if prev == 0 else (0.5, 0.0)
+        joints.append(b2g.revolute_joint(prev, b, la, (-0.5, 0.0)))
+    joints.append(b2g.revolute_joint(planks, 0, (0.5, 0.0), (x0 - 0.5 + 1.0 * planks, 5.0)))
+    first = 1 + planks
+    px = rng.uniform(drops, -12.0, 12.0)
+    py = rng.uniform(drops, 8.0, 20.0)
+    for k in range(drops):
+        b = first + k
+        bodies[b]["type"] = b2g.DYNAMIC
+        bodies[b]["position"] = (px[k], py[k])
+        if k % 2:
+            fixtures.append(b2g.circle_fixture(b, 0.4, density=1.0, friction=0.4))
+        else:
+            fixtures.append(b2g.box_fixture(b, 0.4, 0.3, density=1.0, friction=0.4))
+    wheel, flap = first + drops, first + drops + 1
+    bodies[wheel]["type"] = b2g.DYNAMIC
+    bodies[wheel]["position"] = (22.0, 3.0)
+    fixtures.append(b2g.box_fixture(wheel, 2.0, 0.2, density=2.0, friction=0.5))
+    joints.append(b2g.revolute_joint(0, wheel, (22.0, 3.0), (0.0, 0.0), motor=(2.0, 500.0)))
+    bodies[flap]["type"] = b2g.DYNAMIC
+    bodies[flap]["position"] = (-22.0, 6.0)
+    fixtures.append(b2g.box_fixture(flap, 1.5, 0.1, density=1.0, friction=0.5))
+    joints.append(b2g.revolute_joint(0, flap, (-23.5, 6.0), (-1.5, 0.0), limits=(-0.6, 0.3),
+                                     motor=(-1.0, 5.0)))
+    return _scene("bridge", bodies, np.concatenate(fixtures), steps, joints=np.concatenate(joints))
+
+
 def build_world(world, scene):
-    """Create a scene's bodies and fixtures in a B2world or OracleWorld."""
+    """Create a scene's bodies, fixtures and joints in a B2world or OracleWorld."""
     world.create_bodies(scene["bodies"])
     world.create_fixtures(scene["fixtures"])
+    if scene.get("joints") is not None and len(scene["joints"]):
+        world.create_joints(scene["joints"])
     return world

@@ -30,6 +30,8 @@ constexpr float kMaxRotation = 0.5f * kPi;
 constexpr float kMaxRotationSquared = kMaxRotation * kMaxRotation;
 constexpr float kBaumgarte = 0.2f;
 constexpr float kToiBaumgarte = 0.75f;
+constexpr float kAngularSlop = 2.0f / 180.0f * kPi;
+constexpr float kMaxAngularCorrection = 8.0f / 180.0f * kPi;
 constexpr int kMaxSubSteps = 8;
 constexpr int kMaxToiContacts = 32;
 constexpr float kTimeToSleep = 0.5f;
@@ -122,6 +124,13 @@ struct Mat22 {
     Vec2 ex, ey;
 };
 inline Vec2 mul(const Mat22& a, Vec2 v) { return Vec2{a.ex.x * v.x + a.ey.x * v.y, a.ex.y * v.x + a.ey.y * v.y}; }
+/* B2Mat22::solve, src/b2_math.rs:278-293 */
+inline Vec2 solve(const Mat22& m, Vec2 b) {
+    float a11 = m.ex.x, a12 = m.ey.x, a21 = m.ex.y, a22 = m.ey.y;
+    float det = a11 * a22 - a12 * a21;
+    if (det != 0.0f) det = 1.0f / det;
+    return Vec2{det * (a22 * b.x - a12 * b.y), det * (a11 * b.y - a21 * b.x)};
+}
 /* B2Mat22::get_inverse, src/b2_math.rs:261-276 */
 inline Mat22 inverse(const Mat22& m) {
     float a = m.ex.x, b = m.ey.x, c = m.ex.y, d = m.ey.y;

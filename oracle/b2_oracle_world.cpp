@@ -60,6 +60,7 @@ struct Body {
     int prev = -1, next = -1;
     int fixture_head = -1;
     int edge_head = -1;
+    int jedge_head = -1;  /* joint edges, newest first */
 };
 
 struct Fixture {
@@ -83,12 +84,37 @@ struct Contact {
     int fa = -1, fb = -1;
     Manifold m;
     bool touching = false, enabled = true, island_flag = false;
+    bool filter_flag = false;  /* E_FILTER_FLAG: re-check should_collide at the next collide */
     bool toi_flag = false;   /* solve_toi: toi holds a valid time of impact */
     int toi_count = 0;
     float toi = 1.0f;
     float friction = 0, restitution = 0, threshold = 0, tangent_speed = 0;
     int prev = -1, next = -1;
     bool alive = false;
+};
+
+/* B2revoluteJoint (src/joints/b2_revolute_joint.rs:97-140) with the B2joint base */
+struct Joint {
+    int body_a = -1, body_b = -1;
+    bool collide_connected = false, island_flag = false;
+    Vec2 local_anchor_a{0, 0}, local_anchor_b{0, 0};
+    float reference_angle = 0;
+    bool enable_limit = false, enable_motor = false;
+    float lower_angle = 0, upper_angle = 0, motor_speed = 0, max_motor_torque = 0;
+    Vec2 impulse{0, 0};
+    float motor_impulse = 0, lower_impulse = 0, upper_impulse = 0;
+    /* solver temporaries */
+    int index_a = 0, index_b = 0;
+    Vec2 r_a{0, 0}, r_b{0, 0}, lc_a{0, 0}, lc_b{0, 0};
+    float inv_mass_a = 0, inv_mass_b = 0, inv_ia = 0, inv_ib = 0, axial_mass = 0, angle = 0;
+    Mat22 k{};
+    int prev = -1, next = -1;
+};
+
+struct JointEdge {
+    int joint = -1;
+    int other = -1;
+    int next = -1;
 };
 
 struct Position {
@@ -134,6 +160,11 @@ struct World {
     std::vector<Contact> contacts;
     std::vector<int> free_contacts;
     std::vector<Edge> edges;  /* 2 per contact slot: [2c] = node A, [2c+1] = node B */
+    std::vector<Joint> joints;
+    std::vector<JointEdge> jedges;  /* 2 per joint: [2j] = body A's, [2j+1] = body B's */
+    int joint_head = -1;
+    std::vector<int> joint_rank;    /* joint ordering hook: rank of each joint, -1 none */
+    std::vector<int> isl_joints;
     int body_head = -1;
     int contact_head = -1;
     int contact_count = 0;
@@ -377,6 +408,15 @@ static int register_kind(int t1, int t2) {
     return table[t1][t2];
 }
 
+/* B2body::should_collide, private/dynamics/b2_body.rs:391-416: one body dynamic, and no joint
+ * between them that keeps them from colliding */
+static bool should_collide(const World& w, int self, int other) {
+    if (w.bodies[self].type != DYNAMIC && w.bodies[other].type != DYNAMIC) return false;
+    for (int e = w.bodies[self].jedge_head; e >= 0; e = w.jedges[e].next)
+        if (w.jedges[e].other == other && !w.joints[w.jedges[e].joint].collide_connected) return false;
+    return true;
+}
+
 /* b2_contact_manager_add_pair, private/dynamics/b2_contact_manager.rs:178-302 */
 static void add_pair(World& w, int fixA, int fixB) {
     int bodyA = w.fixtures[fixA].body;
@@ -389,8 +429,7 @@ static void add_pair(World& w, int fixA, int fixB) {
             if (c.fa == fixB && c.fb == fixA) return;
         }
     }
-    /* should_collide: at least one dynamic body (joints are not restated) */
-    if (w.bodies[bodyB].type != DYNAMIC && w.bodies[bodyA].type != DYNAMIC) return;
+    if (!should_collide(w, bodyB, bodyA)) return;
     if (!filter_should_collide(w.fixtures[fixA], w.fixtures[fixB])) return;
     int kind = register_kind(w.fixtures[fixA].shape.type, w.fixtures[fixB].shape.type);
     if (kind == 0) return;
@@ -524,6 +563,14 @@ static void collide(World& w) {
         Contact& c = w.contacts[id];
         const Fixture& FA = w.fixtures[c.fa];
         const Fixture& FB = w.fixtures[c.fb];
+        if (c.filter_flag) {
+            /* should these bodies collide? (the default filter's answer does not change) */
+            if (!should_collide(w, FB.body, FA.body)) {
+                to_destroy.push_back(id);
+                continue;
+            }
+            c.filter_flag = false;
+        }
         const Body& bA = w.bodies[FA.body];
         const Body& bB = w.bodies[FB.body];
         bool activeA = bA.awake && bA.type != STATIC;
@@ -859,6 +906,176 @@ static bool solve_position(World& w) {
     return minSeparation >= -3.0f * kLinearSlop;
 }
 
+/* ---- revolute joint, private/dynamics/joints/b2_revolute_joint.rs ---- */
+
+/* init_velocity_constraints (:21-116): anchors, effective masses, warm start */
+static void joint_init_velocity(World& w, Joint& j, const Step& step) {
+    const Body& A = w.bodies[j.body_a];
+    const Body& B = w.bodies[j.body_b];
+    j.index_a = A.island_index;
+    j.index_b = B.island_index;
+    j.lc_a = A.sweep.local_center;
+    j.lc_b = B.sweep.local_center;
+    j.inv_mass_a = A.inv_mass;
+    j.inv_mass_b = B.inv_mass;
+    j.inv_ia = A.inv_I;
+    j.inv_ib = B.inv_I;
+    const float aA = w.pos[j.index_a].a;
+    const float aB = w.pos[j.index_b].a;
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const Rot qA = rot(aA), qB = rot(aB);
+    j.r_a = mul(qA, j.local_anchor_a - j.lc_a);
+    j.r_b = mul(qB, j.local_anchor_b - j.lc_b);
+    const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+    j.k.ex.x = mA + mB + j.r_a.y * j.r_a.y * iA + j.r_b.y * j.r_b.y * iB;
+    j.k.ey.x = -j.r_a.y * j.r_a.x * iA - j.r_b.y * j.r_b.x * iB;
+    j.k.ex.y = j.k.ey.x;
+    j.k.ey.y = mA + mB + j.r_a.x * j.r_a.x * iA + j.r_b.x * j.r_b.x * iB;
+    j.axial_mass = iA + iB;
+    bool fixed_rotation;
+    if (j.axial_mass > 0.0f) {
+        j.axial_mass = 1.0f / j.axial_mass;
+        fixed_rotation = false;
+    } else {
+        fixed_rotation = true;
+    }
+    j.angle = aB - aA - j.reference_angle;
+    if (!j.enable_limit || fixed_rotation) {
+        j.lower_impulse = 0.0f;
+        j.upper_impulse = 0.0f;
+    }
+    if (!j.enable_motor || fixed_rotation) j.motor_impulse = 0.0f;
+    if (step.warm) {
+        j.impulse *= step.dt_ratio;
+        j.motor_impulse *= step.dt_ratio;
+        j.lower_impulse *= step.dt_ratio;
+        j.upper_impulse *= step.dt_ratio;
+        const float axial = j.motor_impulse + j.lower_impulse - j.upper_impulse;
+        const Vec2 P = v2(j.impulse.x, j.impulse.y);
+        vA -= mA * P;
+        wA -= iA * (cross(j.r_a, P) + axial);
+        vB += mB * P;
+        wB += iB * (cross(j.r_b, P) + axial);
+    } else {
+        j.impulse = v2(0, 0);
+        j.motor_impulse = 0.0f;
+        j.lower_impulse = 0.0f;
+        j.upper_impulse = 0.0f;
+    }
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+/* solve_velocity_constraints (:118-208): motor, lower and upper limits, point */
+static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+    const bool fixed_rotation = iA + iB == 0.0f;
+    if (j.enable_motor && !fixed_rotation) {
+        const float cdot = wB - wA - j.motor_speed;
+        float impulse = -j.axial_mass * cdot;
+        const float old_impulse = j.motor_impulse;
+        const float max_impulse = step.dt * j.max_motor_torque;
+        j.motor_impulse = bclamp(j.motor_impulse + impulse, -max_impulse, max_impulse);
+        impulse = j.motor_impulse - old_impulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    if (j.enable_limit && !fixed_rotation) {
+        {
+            const float C = j.angle - j.lower_angle;
+            const float cdot = wB - wA;
+            float impulse = -j.axial_mass * (cdot + bmax(C, 0.0f) * step.inv_dt);
+            const float old_impulse = j.lower_impulse;
+            j.lower_impulse = bmax(j.lower_impulse + impulse, 0.0f);
+            impulse = j.lower_impulse - old_impulse;
+            wA -= iA * impulse;
+            wB += iB * impulse;
+        }
+        {
+            const float C = j.upper_angle - j.angle;
+            const float cdot = wA - wB;
+            float impulse = -j.axial_mass * (cdot + bmax(C, 0.0f) * step.inv_dt);
+            const float old_impulse = j.upper_impulse;
+            j.upper_impulse = bmax(j.upper_impulse + impulse, 0.0f);
+            impulse = j.upper_impulse - old_impulse;
+            wA += iA * impulse;
+            wB -= iB * impulse;
+        }
+    }
+    {
+        const Vec2 cdot = vB + cross_sv(wB, j.r_b) - vA - cross_sv(wA, j.r_a);
+        const Vec2 impulse = solve(j.k, -cdot);
+        j.impulse.x += impulse.x;
+        j.impulse.y += impulse.y;
+        vA -= mA * impulse;
+        wA -= iA * cross(j.r_a, impulse);
+        vB += mB * impulse;
+        wB += iB * cross(j.r_b, impulse);
+    }
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+/* solve_position_constraints (:210-287): angular limit, then the point */
+static bool joint_solve_position(World& w, Joint& j) {
+    Vec2 cA = w.pos[j.index_a].c;
+    float aA = w.pos[j.index_a].a;
+    Vec2 cB = w.pos[j.index_b].c;
+    float aB = w.pos[j.index_b].a;
+    float angular_error = 0.0f;
+    const bool fixed_rotation = j.inv_ia + j.inv_ib == 0.0f;
+    if (j.enable_limit && !fixed_rotation) {
+        const float angle = aB - aA - j.reference_angle;
+        float C = 0.0f;
+        if (std::fabs(j.upper_angle - j.lower_angle) < 2.0f * kAngularSlop) {
+            C = bclamp(angle - j.lower_angle, -kMaxAngularCorrection, kMaxAngularCorrection);
+        } else if (angle <= j.lower_angle) {
+            C = bclamp(angle - j.lower_angle + kAngularSlop, -kMaxAngularCorrection, 0.0f);
+        } else if (angle >= j.upper_angle) {
+            C = bclamp(angle - j.upper_angle - kAngularSlop, 0.0f, kMaxAngularCorrection);
+        }
+        const float limit_impulse = -j.axial_mass * C;
+        aA -= j.inv_ia * limit_impulse;
+        aB += j.inv_ib * limit_impulse;
+        angular_error = std::fabs(C);
+    }
+    float position_error;
+    {
+        const Rot qA = rot(aA), qB = rot(aB);
+        const Vec2 rA = mul(qA, j.local_anchor_a - j.lc_a);
+        const Vec2 rB = mul(qB, j.local_anchor_b - j.lc_b);
+        const Vec2 C = cB + rB - cA - rA;
+        position_error = length(C);
+        const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+        Mat22 K;
+        K.ex.x = mA + mB + iA * rA.y * rA.y + iB * rB.y * rB.y;
+        K.ex.y = -iA * rA.x * rA.y - iB * rB.x * rB.y;
+        K.ey.x = K.ex.y;
+        K.ey.y = mA + mB + iA * rA.x * rA.x + iB * rB.x * rB.x;
+        const Vec2 impulse = -solve(K, C);
+        cA -= mA * impulse;
+        aA -= iA * cross(rA, impulse);
+        cB += mB * impulse;
+        aB += iB * cross(rB, impulse);
+    }
+    w.pos[j.index_a].c = cA;
+    w.pos[j.index_a].a = aA;
+    w.pos[j.index_b].c = cB;
+    w.pos[j.index_b].a = aB;
+    return position_error <= kLinearSlop && angular_error <= kAngularSlop;
+}
+
 /* B2island::solve, b2_island_private.rs:129-328 */
 static void solve_island(World& w, const Step& step) {
     float h = step.dt;
@@ -886,7 +1103,11 @@ static void solve_island(World& w, const Step& step) {
     }
     init_constraints(w, step);
     if (step.warm) warm_start(w);
-    for (int it = 0; it < step.vi; ++it) solve_velocity(w);
+    for (int ji : w.isl_joints) joint_init_velocity(w, w.joints[ji], step);
+    for (int it = 0; it < step.vi; ++it) {
+        for (int ji : w.isl_joints) joint_solve_velocity(w, w.joints[ji], step);
+        solve_velocity(w);
+    }
     store_impulses(w);
     for (int i = 0; i < nb; ++i) {
         Vec2 c = w.pos[i].c;
@@ -912,7 +1133,13 @@ static void solve_island(World& w, const Step& step) {
     }
     bool positionSolved = false;
     for (int it = 0; it < step.pi; ++it) {
-        if (solve_position(w)) {
+        const bool contacts_okay = solve_position(w);
+        bool joints_okay = true;
+        for (int ji : w.isl_joints) {
+            const bool ok = joint_solve_position(w, w.joints[ji]);
+            joints_okay = joints_okay && ok;
+        }
+        if (contacts_okay && joints_okay) {
             positionSolved = true;
             break;
         }
@@ -950,6 +1177,7 @@ static void solve_island(World& w, const Step& step) {
 static void solve(World& w, const Step& step) {
     for (int b = w.body_head; b >= 0; b = w.bodies[b].next) w.bodies[b].island_flag = false;
     for (int c = w.contact_head; c >= 0; c = w.contacts[c].next) w.contacts[c].island_flag = false;
+    for (int j = w.joint_head; j >= 0; j = w.joints[j].next) w.joints[j].island_flag = false;
     w.last_order.clear();
     w.islands_solved = 0;
     for (int seed = w.body_head; seed >= 0; seed = w.bodies[seed].next) {
@@ -959,6 +1187,7 @@ static void solve(World& w, const Step& step) {
         if (S.type == STATIC) continue;
         w.isl_bodies.clear();
         w.isl_contacts.clear();
+        w.isl_joints.clear();
         w.stack.clear();
         w.stack.push_back(seed);
         S.island_flag = true;
@@ -983,6 +1212,22 @@ static void solve(World& w, const Step& step) {
                 w.stack.push_back(other);
                 w.bodies[other].island_flag = true;
             }
+            for (int e = b.jedge_head; e >= 0; e = w.jedges[e].next) {
+                Joint& J = w.joints[w.jedges[e].joint];
+                if (J.island_flag) continue;
+                const int other = w.jedges[e].other;
+                if (!w.bodies[other].enabled) continue;
+                w.isl_joints.push_back(w.jedges[e].joint);
+                J.island_flag = true;
+                if (w.bodies[other].island_flag) continue;
+                w.stack.push_back(other);
+                w.bodies[other].island_flag = true;
+            }
+        }
+        if (!w.joint_rank.empty()) {
+            /* joint ordering hook: this island's joints in the caller's order */
+            std::stable_sort(w.isl_joints.begin(), w.isl_joints.end(),
+                             [&](int x, int y) { return w.joint_rank[x] < w.joint_rank[y]; });
         }
         if (w.hook) {
             /* ordering hook: solve this island's contacts in the caller's order */
@@ -1567,6 +1812,69 @@ int ora_set_solver_order(void* p, const uint32_t* pairs, int n) {
     w.hook = n > 0;
     w.hook_rank.reserve((size_t)n * 2);
     for (int i = 0; i < n; ++i) w.hook_rank[pair_key((int)pairs[2 * i], (int)pairs[2 * i + 1])] = i;
+    return 0;
+}
+
+/* B2world::create_joint, private/dynamics/b2_world.rs:156-276 (revolute joints) */
+int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) {
+    World& w = *(World*)p;
+    for (int i = 0; i < n; ++i) {
+        const b2g_joint_def& d = defs[i];
+        if (d.type != B2G_JOINT_REVOLUTE || d.body_a >= w.bodies.size() || d.body_b >= w.bodies.size()) return -1;
+        const int id = (int)w.joints.size();
+        Joint j;
+        j.body_a = (int)d.body_a;
+        j.body_b = (int)d.body_b;
+        j.collide_connected = d.collide_connected != 0;
+        j.local_anchor_a = v2(d.local_anchor_a.x, d.local_anchor_a.y);
+        j.local_anchor_b = v2(d.local_anchor_b.x, d.local_anchor_b.y);
+        j.reference_angle = d.reference_angle;
+        j.enable_limit = d.enable_limit != 0;
+        j.lower_angle = d.lower_angle;
+        j.upper_angle = d.upper_angle;
+        j.enable_motor = d.enable_motor != 0;
+        j.motor_speed = d.motor_speed;
+        j.max_motor_torque = d.max_motor_torque;
+        j.next = w.joint_head;
+        if (w.joint_head >= 0) w.joints[w.joint_head].prev = id;
+        w.joint_head = id;
+        w.joints.push_back(j);
+        w.jedges.push_back(JointEdge{id, j.body_b, w.bodies[j.body_a].jedge_head});
+        w.bodies[j.body_a].jedge_head = 2 * id;
+        w.jedges.push_back(JointEdge{id, j.body_a, w.bodies[j.body_b].jedge_head});
+        w.bodies[j.body_b].jedge_head = 2 * id + 1;
+        if (!j.collide_connected) {
+            for (int e = w.bodies[j.body_b].edge_head; e >= 0; e = w.edges[e].next)
+                if (w.edges[e].other == j.body_a) w.contacts[w.edges[e].contact].filter_flag = true;
+        }
+        if (ids) ids[i] = (uint32_t)id;
+    }
+    return 0;
+}
+
+/* per joint: impulse x, y, motor, lower, upper */
+int ora_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) {
+    World& w = *(World*)p;
+    if ((size_t)first + count > w.joints.size()) return -1;
+    for (uint32_t i = 0; i < count; ++i) {
+        const Joint& j = w.joints[first + i];
+        out[5 * i + 0] = j.impulse.x;
+        out[5 * i + 1] = j.impulse.y;
+        out[5 * i + 2] = j.motor_impulse;
+        out[5 * i + 3] = j.lower_impulse;
+        out[5 * i + 4] = j.upper_impulse;
+    }
+    return 0;
+}
+
+/* Joint ordering hook: each island solves its joints in this order of joint ids (n = 0 clears) */
+int ora_set_joint_order(void* p, const uint32_t* order, int n) {
+    World& w = *(World*)p;
+    w.joint_rank.clear();
+    if (n <= 0) return 0;
+    w.joint_rank.assign(w.joints.size(), 0x7fffffff);
+    for (int i = 0; i < n; ++i)
+        if (order[i] < w.joint_rank.size()) w.joint_rank[order[i]] = i;
     return 0;
 }
 

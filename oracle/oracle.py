@@ -65,6 +65,9 @@ def load():
         "ora_set_solver_order": [vp, vp, i32],
         "ora_get_hook_misses": [vp],
         "ora_get_toi_events": [vp],
+        "ora_create_joints": [vp, vp, i32, vp],
+        "ora_get_joint_impulses": [vp, u32, u32, vp],
+        "ora_set_joint_order": [vp, vp, i32],
         "ora_set_key_order": [vp, i32],
         "ora_get_awake": [vp, u32, u32, vp],
         "ora_get_solver_order": [vp, vp, i32, pi32],
@@ -210,6 +213,26 @@ class OracleWorld:
         assert rc == 0, rc
         self.fixture_count += len(defs)
         return ids
+
+    def create_joints(self, defs):
+        defs = np.ascontiguousarray(defs, b2g.JOINT_DEF)
+        ids = np.zeros(len(defs), np.uint32)
+        rc = self._lib.ora_create_joints(self._h, _ptr(defs), len(defs), _ptr(ids))
+        assert rc == 0, rc
+        self.joint_count = getattr(self, "joint_count", 0) + len(defs)
+        return ids
+
+    def get_joint_impulses(self):
+        n = getattr(self, "joint_count", 0)
+        out = np.zeros((n, 5), np.float32)
+        if n:
+            self._lib.ora_get_joint_impulses(self._h, 0, n, _ptr(out))
+        return out
+
+    def set_joint_order(self, order):
+        """Ordering hook: islands solve their joints in this order of joint ids."""
+        o = np.ascontiguousarray(order, np.uint32)
+        self._lib.ora_set_joint_order(self._h, _ptr(o) if len(o) else None, len(o))
 
     def step(self, dt, vi, pi):
         self._lib.ora_step(self._h, dt, vi, pi)

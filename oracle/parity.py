@@ -136,6 +136,9 @@ def make_pair(scene, record_pairs=True, record_events=False, warm_starting=True)
     # the contact-list order choices (collide's wake order, solve_toi's ties and island order)
     # follow the GPU's key order
     ora.set_key_order(True)
+    if scene.get("joints") is not None and len(scene["joints"]):
+        assert scene.get("num_worlds", 1) == 1, "joints are checked on single worlds"
+        ora.set_joint_order(gpu.get_joint_order())
     return gpu, ora
 
 
@@ -224,6 +227,8 @@ def lockstep(scene, steps, check_pairs=True, check_contacts=True, resync=False, 
         rec["body_abs"], rec["body_rel"] = body_diff(gs, os_)
         rec["bitexact_bodies"] = all(np.array_equal(gs[f], os_[f]) for f in BODY_FIELDS)
         rec["awake_equal"] = bool(np.array_equal(gpu.get_awake(), ora.get_awake()))
+        if getattr(gpu, "joint_count", 0):
+            rec["joint_impulses_equal"] = bool(np.array_equal(gpu.get_joint_impulses(), ora.get_joint_impulses()))
         rec["awake"] = int(gpu.get_awake().sum())
         if check_pairs:
             gp, op = pair_set(gpu.get_pairs()), pair_set(ora.get_pairs())
