@@ -770,7 +770,13 @@ int upload_joints(World* w) {
 int prepare(World* w) {
     const int nb = (int)w->h_flags.size();
     const int nf = (int)w->h_fbody.size();
-    if (w->allocated && nb == w->uploaded_bodies && nf == w->uploaded_fixtures && !w->joints_dirty) return B2G_OK;
+    if (w->allocated && nb == w->uploaded_bodies && nf == w->uploaded_fixtures) {
+        if (!w->joints_dirty) return B2G_OK;
+        /* only joints were added: the device's bodies and fixtures stay as they are */
+        int rc = download_joint_impulses(w);
+        if (rc != B2G_OK) return rc;
+        return upload_joints(w);
+    }
     {
         int rc = download_joint_impulses(w);
         if (rc != B2G_OK) return rc;

@@ -200,6 +200,28 @@ def _continue(w, s, steps):
     return w.get_body_states().copy(), c.copy(), w.get_awake().copy()
 
 
+def test_state_checkpoint_with_joints(built):
+    """A bridge of revolute joints resumes bit for bit from a checkpoint, joint impulses included."""
+    s = scenes.bridge(steps=60)
+
+    def make():
+        w = b2g.B2world(gravity=s["gravity"])
+        w.set_allow_sleeping(False)
+        scenes.build_world(w, s)
+        return w
+
+    a = make()
+    _continue(a, s, 25)
+    state = a.save_state()
+    ref = _continue(a, s, 20) + (a.get_joint_impulses(),)
+    b = make()
+    b.load_state(state)
+    got = _continue(b, s, 20) + (b.get_joint_impulses(),)
+    for f in b2g.BODY_STATE.names:
+        assert np.array_equal(ref[0][f], got[0][f]), f
+    assert np.array_equal(ref[1], got[1]) and np.array_equal(ref[3], got[3])
+
+
 @pytest.mark.parametrize("continuous,sleep", [(False, False), (True, True)])
 def test_state_checkpoint_resumes_bit_for_bit(built, continuous, sleep):
     """b2g_state_save / b2g_state_load: after a checkpoint at step 25, the next 30 steps are the

@@ -372,3 +372,68 @@ def test_revolute_bridge_lockstep(built):
         assert not (a in planks and b in planks and abs(a - b) == 1)
     st = gpu.get_body_states()
     assert abs(float(st["angular_velocity"][1 + 30 + 24]) - 2.0) < 1e-3  # the motor holds its speed
+
+
+def test_revolute_chain_sleeps_lockstep(built):
+    """Sleeping on: a hanging chain of 8 links (revolute joints, the first to a static hook) is
+    set swinging, comes to rest and falls asleep as one island (the joints keep it together)."""
+    n = 8
+    bodies = b2g.body_defs(n + 1)
+    bodies["allow_sleep"] = 1
+    bodies[1:]["type"] = b2g.DYNAMIC
+    bodies[1:]["position"][:, 1] = 19.5 - np.arange(n, dtype=np.float32)
+    bodies[1:]["angle"] = np.float32(-np.pi / 2)
+    bodies[1:]["angular_damping"] = 4.0
+    bodies[1:]["linear_damping"] = 4.0
+    bodies[n]["linear_velocity"] = (3.0, 0.0)
+    fx = [b2g.edge_fixture(0, (-30.0, 0.0), (30.0, 0.0))]
+    fx += [b2g.box_fixture(i + 1, 0.5, 0.1, density=1.0, friction=0.2) for i in range(n)]
+    joints = [b2g.revolute_joint(0, 1, (0.0, 20.0), (-0.5, 0.0))]
+    joints += [b2g.revolute_joint(i, i + 1, (0.5, 0.0), (-0.5, 0.0)) for i in range(1, n)]
+    s = {"name": "chain", "bodies": bodies, "fixtures": np.concatenate(fx), "joints": np.concatenate(joints),
+         "gravity": (0.0, -10.0), "dt": np.float32(1.0 / 60.0), "vi": 8, "pi": 3, "steps": 480, "num_worlds": 1,
+         "allow_sleep": True, "n_dynamic": n}
+    recs, _, _ = parity.lockstep(s, 480)
+    for r in recs:
+        _assert_step(r)
+        assert r["joint_impulses_equal"], r
+    assert recs[-1]["awake"] == 0
+
+
+def test_joint_created_mid_run_filters_contacts(built):
+    """Two overlapping boxes collide; a revolute joint between them (collide_connected off) made
+    after 20 steps flags their contact, which the next collide destroys (B2world::create_joint's
+    filtering), on the GPU as in the oracle."""
+    bodies = b2g.body_defs(3)
+    bodies["allow_sleep"] = 0
+    bodies[1:]["type"] = b2g.DYNAMIC
+    bodies[1]["position"] = (0.0, 1.0)
+    bodies[2]["position"] = (0.8, 2.1)
+    fx = np.concatenate([b2g.edge_fixture(0, (-10.0, 0.0), (10.0, 0.0)),
+                         b2g.box_fixture(1, 0.5, 0.5, density=1.0, friction=0.5),
+                         b2g.box_fixture(2, 0.5, 0.5, density=1.0, friction=0.5)])
+    s = {"name": "mid_joint", "bodies": bodies, "fixtures": fx, "gravity": (0.0, -10.0), "dt": np.float32(1 / 60),
+         "vi": 8, "pi": 3, "steps": 60, "num_worlds": 1, "allow_sleep": False, "n_dynamic": 2}
+    gpu, ora = parity.make_pair(s, record_pairs=False)
+    dt, vi, pi = s["dt"], s["vi"], s["pi"]
+
+    def step_both(k):
+        for _ in range(k):
+            gpu.step(dt, vi, pi)
+            ora.set_solver_order(gpu.get_solver_order())
+            ora.step(dt, vi, pi)
+            for f in parity.BODY_FIELDS:
+                assert np.array_equal(gpu.get_body_states()[f], ora.get_body_states()[f]), f
+            km, im, _ = parity.manifold_diff(gpu.get_contacts(), ora.get_contacts())
+            assert not km and im == 0
+
+    step_both(20)
+    pair = (1, 2)
+    assert any(tuple(sorted((int(c["fixture_a"]), int(c["fixture_b"])))) == pair for c in gpu.get_contacts())
+    j = b2g.revolute_joint(1, 2, (0.4, 0.5), (-0.4, -0.6))
+    gpu.create_joints(j)
+    ora.create_joints(j)
+    ora.set_joint_order(gpu.get_joint_order())
+    step_both(40)
+    assert not any(tuple(sorted((int(c["fixture_a"]), int(c["fixture_b"])))) == pair for c in gpu.get_contacts())
+    assert np.array_equal(gpu.get_joint_impulses(), ora.get_joint_impulses())
