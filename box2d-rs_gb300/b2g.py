@@ -156,9 +156,30 @@ JOINT_DEF = np.dtype(
         ("enable_motor", "<i4"),
         ("motor_speed", "<f4"),
         ("max_motor_torque", "<f4"),
-        ("pad_", "<u4"),
+        ("length", "<f4"),
+        ("min_length", "<f4"),
+        ("max_length", "<f4"),
+        ("stiffness", "<f4"),
+        ("damping", "<f4"),
+        ("pad_", "<u4", (3,)),
     ]
 )
+JOINT_DISTANCE = 3
+
+
+def distance_joint(body_a, body_b, anchor_a, anchor_b, length, min_length=None, max_length=None, stiffness=0.0,
+                   damping=0.0, collide_connected=False):
+    """B2distanceJointDef with local anchors; min/max length default to the rest length (rigid)."""
+    d = np.zeros(1, JOINT_DEF)
+    d["type"] = JOINT_DISTANCE
+    d["body_a"], d["body_b"] = body_a, body_b
+    d["collide_connected"] = int(bool(collide_connected))
+    d["local_anchor_a"], d["local_anchor_b"] = anchor_a, anchor_b
+    d["length"] = length
+    d["min_length"] = length if min_length is None else min_length
+    d["max_length"] = length if max_length is None else max_length
+    d["stiffness"], d["damping"] = stiffness, damping
+    return d
 
 
 def revolute_joint(body_a, body_b, anchor_a, anchor_b, reference_angle=0.0, collide_connected=False,

@@ -743,10 +743,19 @@ int upload_joints(World* w) {
             const b2g_joint_def& jd = w->joints[j];
             jb[j] = make_int2((int)jd.body_a, (int)jd.body_b);
             an[j] = make_float4(jd.local_anchor_a.x, jd.local_anchor_a.y, jd.local_anchor_b.x, jd.local_anchor_b.y);
-            lim[j] = make_float4(jd.reference_angle, jd.lower_angle, jd.upper_angle, jd.motor_speed);
-            const uint32_t fl = (jd.enable_limit ? JF_LIMIT : 0u) | (jd.enable_motor ? JF_MOTOR : 0u) |
-                                (jd.collide_connected ? JF_COLLIDE : 0u);
-            par[j] = make_float4(jd.max_motor_torque, __uint_as_float_host(fl), 0.0f, 0.0f);
+            uint32_t fl = ((uint32_t)jd.type << JF_TYPE_SHIFT) | (jd.collide_connected ? JF_COLLIDE : 0u);
+            if (jd.type == B2G_JOINT_DISTANCE) {
+                /* b2_distance_joint_new (private/dynamics/joints/b2_distance_joint.rs:42-76) */
+                const float len = std::max(jd.length, kLinearSlop);
+                const float lo = std::max(jd.min_length, kLinearSlop);
+                const float hi = std::max(jd.max_length, lo);
+                lim[j] = make_float4(len, lo, hi, jd.stiffness);
+                par[j] = make_float4(jd.damping, __uint_as_float_host(fl), 0.0f, 0.0f);
+            } else {
+                lim[j] = make_float4(jd.reference_angle, jd.lower_angle, jd.upper_angle, jd.motor_speed);
+                fl |= (jd.enable_limit ? JF_LIMIT : 0u) | (jd.enable_motor ? JF_MOTOR : 0u);
+                par[j] = make_float4(jd.max_motor_torque, __uint_as_float_host(fl), 0.0f, 0.0f);
+            }
         }
         U(d.j_body, jb.data(), nj);
         U(d.j_anchor, an.data(), nj);
@@ -1327,7 +1336,8 @@ int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* i
     if (!w || (!defs && n > 0) || n < 0) return B2G_ERR_INVALID_ARG;
     for (int i = 0; i < n; ++i) {
         const b2g_joint_def& d = defs[i];
-        if (d.type != B2G_JOINT_REVOLUTE) return fail(w, B2G_ERR_UNSUPPORTED, "only revolute joints are on the GPU path");
+        if (d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE)
+            return fail(w, B2G_ERR_UNSUPPORTED, "only revolute and distance joints are on the GPU path");
         if (d.body_a >= w->h_flags.size() || d.body_b >= w->h_flags.size() || d.body_a == d.body_b)
             return fail(w, B2G_ERR_INVALID_ARG, "joint body ids out of range or equal");
     }
@@ -1360,6 +1370,14 @@ int b2g_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) 
     }
     for (uint32_t i = 0; i < count; ++i) {
         const float4 a = w->h_jimp[first + i], b = w->h_jimp2[first + i];
+        if (w->joints[first + i].type == B2G_JOINT_DISTANCE) {
+            out[5 * i + 0] = a.x;
+            out[5 * i + 1] = a.y;
+            out[5 * i + 2] = a.z;
+            out[5 * i + 3] = 0.0f;
+            out[5 * i + 4] = 0.0f;
+            continue;
+        }
         out[5 * i + 0] = a.x;
         out[5 * i + 1] = a.y;
         out[5 * i + 2] = a.z;

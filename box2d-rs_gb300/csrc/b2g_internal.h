@@ -53,6 +53,7 @@ enum : uint32_t {
     JF_LIMIT = 1u << 0,
     JF_MOTOR = 1u << 1,
     JF_COLLIDE = 1u << 2,  /* collide_connected */
+    JF_TYPE_SHIFT = 8,     /* the joint type (B2G_JOINT_*) sits in bits 8-15 */
 };
 
 /* device status bits (sticky until read by the host) */

@@ -1,5 +1,5 @@
 /*
- * b2g_joint.cuh — the revolute joint on the device (B2revoluteJoint,
+ * b2g_joint.cuh — the revolute and distance joints on the device. The revolute joint (B2revoluteJoint,
  * private/dynamics/joints/b2_revolute_joint.rs:21-287): init_velocity_constraints (anchors,
  * effective masses, warm start), solve_velocity_constraints (motor, lower and upper limits, the
  * point constraint) and solve_position_constraints (angular limit, then the point), each the
@@ -15,6 +15,7 @@
 #ifndef B2G_JOINT_CUH
 #define B2G_JOINT_CUH
 
+#include "b2g.h"
 #include "b2g_internal.h"
 
 namespace b2g {
@@ -34,8 +35,187 @@ __device__ __forceinline__ V2 mat22_solve(float a11, float a21, float a12, float
     return mk(det * (a22 * b.x - a12 * b.y), det * (a11 * b.y - a21 * b.x));
 }
 
+/* ---- distance joint (B2distanceJoint, private/dynamics/joints/b2_distance_joint.rs:78-319) ----
+ * j_lim = (rest length, min length, max length, stiffness), j_par.x = damping, j_imp = (impulse,
+ * lower, upper, -); the step's temporaries j_rr (rA, rB), j_k (u, current length, mass), j_s
+ * (gamma, bias), j_imp2.y (soft mass). */
+
+__device__ __forceinline__ void distance_apply(V2& vA, float& wA, V2& vB, float& wB, const float4& m, V2 rA, V2 rB,
+                                               V2 P) {
+    vA = sub(vA, scale(m.x, P));
+    wA -= m.z * cross(rA, P);
+    vB = add(vB, scale(m.y, P));
+    wB += m.w * cross(rB, P);
+}
+
+/* init_velocity_constraints, :78-181 */
+__device__ void distance_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 an = w.j_anchor[j];
+    const float4 lim = w.j_lim[j];
+    const float damping = w.j_par[j].x;
+    const float4 massA = w.b_mass[bd.x], massB = w.b_mass[bd.y];
+    const float2 lcA = w.b_lc[bd.x], lcB = w.b_lc[bd.y];
+    const float4 m = make_float4(massA.y, massB.y, massA.w, massB.w);
+    const float4 pa = w.b_pos[bd.x], pb = w.b_pos[bd.y];
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = rot(pa.z), qB = rot(pb.z);
+    const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+    const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+    V2 u = sub(sub(add(mk(pb.x, pb.y), rB), mk(pa.x, pa.y)), rA);
+    float4 imp = w.j_imp[j];
+    const float current = length(u);
+    if (current > kLinearSlop) {
+        const float inv = fdiv(1.0f, current);
+        u.x *= inv;
+        u.y *= inv;
+    } else {
+        u = mk(0.0f, 0.0f);
+        imp.x = 0.0f;
+        imp.y = 0.0f;
+        imp.z = 0.0f;
+    }
+    const float crAu = cross(rA, u);
+    const float crBu = cross(rB, u);
+    float inv_mass = m.x + m.z * crAu * crAu + m.y + m.w * crBu * crBu;
+    const float mass = inv_mass != 0.0f ? fdiv(1.0f, inv_mass) : 0.0f;
+    float gamma, bias, soft_mass;
+    if (lim.w > 0.0f && lim.y < lim.z) {
+        const float C = current - lim.x;
+        const float d = damping;
+        const float k = lim.w;
+        const float h = sp.dt;
+        gamma = h * (d + h * k);
+        gamma = gamma != 0.0f ? fdiv(1.0f, gamma) : 0.0f;
+        bias = C * h * k * gamma;
+        inv_mass += gamma;
+        soft_mass = inv_mass != 0.0f ? fdiv(1.0f, inv_mass) : 0.0f;
+    } else {
+        gamma = 0.0f;
+        bias = 0.0f;
+        soft_mass = mass;
+    }
+    if (sp.warm) {
+        imp.x *= sp.dt_ratio;
+        imp.y *= sp.dt_ratio;
+        imp.z *= sp.dt_ratio;
+        const V2 P = scale(imp.x + imp.y - imp.z, u);
+        distance_apply(vA, wA, vB, wB, m, rA, rB, P);
+    } else {
+        imp.x = 0.0f;  /* the reference zeroes only the spring impulse here */
+    }
+    w.j_imp[j] = imp;
+    w.j_rr[j] = make_float4(rA.x, rA.y, rB.x, rB.y);
+    w.j_k[j] = make_float4(u.x, u.y, current, mass);
+    w.j_m[j] = m;
+    w.j_s[j] = make_float2(gamma, bias);
+    w.j_imp2[j].y = soft_mass;
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+/* solve_velocity_constraints, :183-274 */
+__device__ void distance_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 lim = w.j_lim[j];
+    const float4 m = w.j_m[j];
+    const float4 rr = w.j_rr[j];
+    const V2 rA = mk(rr.x, rr.y), rB = mk(rr.z, rr.w);
+    const float4 uk = w.j_k[j];
+    const V2 u = mk(uk.x, uk.y);
+    const float current = uk.z, mass = uk.w;
+    const float2 gb = w.j_s[j];
+    const float soft_mass = w.j_imp2[j].y;
+    float4 imp = w.j_imp[j];
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    if (lim.y < lim.z) {
+        if (lim.w > 0.0f) {
+            const V2 vpA = add(vA, cross_sv(wA, rA));
+            const V2 vpB = add(vB, cross_sv(wB, rB));
+            const float cdot = dot(u, sub(vpB, vpA));
+            const float impulse = -soft_mass * (cdot + gb.y + gb.x * imp.x);
+            imp.x += impulse;
+            distance_apply(vA, wA, vB, wB, m, rA, rB, scale(impulse, u));
+        }
+        {
+            const float C = current - lim.y;
+            const float bias = fmaxr(0.0f, C) * sp.inv_dt;
+            const V2 vpA = add(vA, cross_sv(wA, rA));
+            const V2 vpB = add(vB, cross_sv(wB, rB));
+            const float cdot = dot(u, sub(vpB, vpA));
+            float impulse = -mass * (cdot + bias);
+            const float old_impulse = imp.y;
+            imp.y = fmaxr(0.0f, imp.y + impulse);
+            impulse = imp.y - old_impulse;
+            distance_apply(vA, wA, vB, wB, m, rA, rB, scale(impulse, u));
+        }
+        {
+            const float C = lim.z - current;
+            const float bias = fmaxr(0.0f, C) * sp.inv_dt;
+            const V2 vpA = add(vA, cross_sv(wA, rA));
+            const V2 vpB = add(vB, cross_sv(wB, rB));
+            const float cdot = dot(u, sub(vpA, vpB));
+            float impulse = -mass * (cdot + bias);
+            const float old_impulse = imp.z;
+            imp.z = fmaxr(0.0f, imp.z + impulse);
+            impulse = imp.z - old_impulse;
+            distance_apply(vA, wA, vB, wB, m, rA, rB, scale(-impulse, u));
+        }
+    } else {
+        const V2 vpA = add(vA, cross_sv(wA, rA));
+        const V2 vpB = add(vB, cross_sv(wB, rB));
+        const float cdot = dot(u, sub(vpB, vpA));
+        const float impulse = -mass * cdot;
+        imp.x += impulse;
+        distance_apply(vA, wA, vB, wB, m, rA, rB, scale(impulse, u));
+    }
+    w.j_imp[j] = imp;
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+/* solve_position_constraints, :276-319 */
+__device__ bool distance_solve_position(const DevWorld& w, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 an = w.j_anchor[j];
+    const float4 lim = w.j_lim[j];
+    const float4 m = w.j_m[j];
+    const float mass = w.j_k[j].w;
+    const float2 lcA = w.b_lc[bd.x], lcB = w.b_lc[bd.y];
+    const float4 pa = w.b_pos[bd.x], pb = w.b_pos[bd.y];
+    V2 cA = mk(pa.x, pa.y), cB = mk(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    const Rot qA = rot(aA), qB = rot(aB);
+    const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+    const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+    V2 u = sub(sub(add(cB, rB), cA), rA);
+    const float len = normalize(u);
+    float C;
+    if (lim.y == lim.z) C = len - lim.y;
+    else if (len < lim.y) C = len - lim.y;
+    else if (lim.z < len) C = len - lim.z;
+    else return true;
+    const float impulse = -mass * C;
+    const V2 P = scale(impulse, u);
+    cA = sub(cA, scale(m.x, P));
+    aA -= m.z * cross(rA, P);
+    cB = add(cB, scale(m.y, P));
+    aB += m.w * cross(rB, P);
+    if (joint_body_dynamic(w, bd.x)) w.b_pos[bd.x] = make_float4(cA.x, cA.y, aA, pa.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_pos[bd.y] = make_float4(cB.x, cB.y, aB, pb.w);
+    return fabsr(C) < kLinearSlop;
+}
+
+__device__ __forceinline__ bool joint_is_distance(const DevWorld& w, int j) {
+    return ((__float_as_uint(w.j_par[j].y) >> JF_TYPE_SHIFT) & 0xffu) == B2G_JOINT_DISTANCE;
+}
+
 /* init_velocity_constraints, b2_revolute_joint.rs:21-116 */
-__device__ void joint_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
+__device__ void revolute_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
     const int2 bd = w.j_body[j];
     const float4 an = w.j_anchor[j];
     const float4 lim = w.j_lim[j];
@@ -98,7 +278,7 @@ __device__ void joint_init_velocity(const DevWorld& w, const StepParams& sp, int
 }
 
 /* solve_velocity_constraints, b2_revolute_joint.rs:118-208 */
-__device__ void joint_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
+__device__ void revolute_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
     const int2 bd = w.j_body[j];
     const float4 lim = w.j_lim[j];
     const float4 par = w.j_par[j];
@@ -166,7 +346,7 @@ __device__ void joint_solve_velocity(const DevWorld& w, const StepParams& sp, in
 
 /* solve_position_constraints, b2_revolute_joint.rs:210-287; returns whether the joint is
  * within the linear and angular slop */
-__device__ bool joint_solve_position(const DevWorld& w, int j) {
+__device__ bool revolute_solve_position(const DevWorld& w, int j) {
     const int2 bd = w.j_body[j];
     const float4 an = w.j_anchor[j];
     const float4 lim = w.j_lim[j];
@@ -214,6 +394,19 @@ __device__ bool joint_solve_position(const DevWorld& w, int j) {
     if (joint_body_dynamic(w, bd.x)) w.b_pos[bd.x] = make_float4(cA.x, cA.y, aA, pa.w);
     if (joint_body_dynamic(w, bd.y)) w.b_pos[bd.y] = make_float4(cB.x, cB.y, aB, pb.w);
     return position_error <= kLinearSlop && angular_error <= kAngularSlop;
+}
+
+/* the joint routines by type */
+__device__ __forceinline__ void joint_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    if (joint_is_distance(w, j)) distance_init_velocity(w, sp, j);
+    else revolute_init_velocity(w, sp, j);
+}
+__device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    if (joint_is_distance(w, j)) distance_solve_velocity(w, sp, j);
+    else revolute_solve_velocity(w, sp, j);
+}
+__device__ __forceinline__ bool joint_solve_position(const DevWorld& w, int j) {
+    return joint_is_distance(w, j) ? distance_solve_position(w, j) : revolute_solve_position(w, j);
 }
 
 /* the joint belongs to an island solved this step (a body of it is non-static and in one); both

@@ -110,11 +110,16 @@ typedef struct b2g_fixture_def {
     uint64_t user_data;
 } b2g_fixture_def;
 
-/* B2revoluteJointDef (src/joints/b2_revolute_joint.rs:10-72, defaults :10-27) with the B2jointDef
- * base (bodies, collide_connected). Anchors are in the bodies' local frames. */
+/* A joint definition: the B2jointDef base (bodies, collide_connected) and the fields of its type.
+ * Anchors are in the bodies' local frames.
+ *   B2G_JOINT_REVOLUTE: B2revoluteJointDef (src/joints/b2_revolute_joint.rs:10-72): reference angle,
+ *     limit (enable_limit, lower/upper angle), motor (enable_motor, speed, max torque)
+ *   B2G_JOINT_DISTANCE: B2distanceJointDef (src/joints/b2_distance_joint.rs): rest length, min and
+ *     max length, stiffness and damping (a spring when stiffness > 0 and min < max) */
 #define B2G_JOINT_REVOLUTE 1
+#define B2G_JOINT_DISTANCE 3
 typedef struct b2g_joint_def {
-    int32_t type;              /* B2G_JOINT_REVOLUTE */
+    int32_t type;              /* B2G_JOINT_* */
     uint32_t body_a, body_b;
     int32_t collide_connected;
     b2g_vec2 local_anchor_a, local_anchor_b;
@@ -123,7 +128,8 @@ typedef struct b2g_joint_def {
     float lower_angle, upper_angle;
     int32_t enable_motor;
     float motor_speed, max_motor_torque;
-    uint32_t pad_;
+    float length, min_length, max_length, stiffness, damping;
+    uint32_t pad_[3];
 } b2g_joint_def;
 
 /* Body state read back after a step (B2body getters, src/b2_body.rs:650-680). */
@@ -177,11 +183,12 @@ int64_t b2g_get_launch_count(void);
  *                B2body::create_fixture (src/b2_body.rs:233) ---- */
 int b2g_create_bodies(void* world, const b2g_body_def* defs, int32_t n, uint32_t* out_ids);
 int b2g_create_fixtures(void* world, const b2g_fixture_def* defs, int32_t n, uint32_t* out_ids);
-/* B2world::create_joint (private/dynamics/b2_world.rs:156-276): revolute joints. A joint that
+/* B2world::create_joint (private/dynamics/b2_world.rs:156-276): revolute and distance joints. A joint that
  * does not let its bodies collide flags their contacts for the next collide, which destroys them.
  * A world with joints runs the grid-wide colour schedule (no part-local solve) and cannot be taped. */
 int b2g_create_joints(void* world, const b2g_joint_def* defs, int32_t n, uint32_t* out_ids);
-/* B2revoluteJoint impulses (accumulated, for warm starting): per joint x, y, motor, lower, upper */
+/* Accumulated joint impulses (for warm starting), 5 per joint: revolute x, y, motor, lower, upper;
+ * distance impulse, lower, upper, 0, 0 */
 int b2g_get_joint_impulses(void* world, uint32_t first, uint32_t count, float* out);
 /* The order the GPU solves joints in (ids, colour by colour): the oracle's joint ordering hook */
 int b2g_get_joint_order(void* world, uint32_t* out, int32_t cap, int32_t* n);

@@ -95,7 +95,12 @@ struct Contact {
 
 /* B2revoluteJoint (src/joints/b2_revolute_joint.rs:97-140) with the B2joint base */
 struct Joint {
+    int type = B2G_JOINT_REVOLUTE;
     int body_a = -1, body_b = -1;
+    /* B2distanceJoint (private/dynamics/joints/b2_distance_joint.rs:42-76) */
+    float length = 0, min_length = 0, max_length = 0, stiffness = 0, damping = 0;
+    float dist_impulse = 0, gamma = 0, bias = 0, current_length = 0, mass = 0, soft_mass = 0;
+    Vec2 u{0, 0};
     bool collide_connected = false, island_flag = false;
     Vec2 local_anchor_a{0, 0}, local_anchor_b{0, 0};
     float reference_angle = 0;
@@ -908,8 +913,173 @@ static bool solve_position(World& w) {
 
 /* ---- revolute joint, private/dynamics/joints/b2_revolute_joint.rs ---- */
 
+/* ---- distance joint, private/dynamics/joints/b2_distance_joint.rs ---- */
+
+/* init_velocity_constraints (:78-181) */
+static void distance_init_velocity(World& w, Joint& j, const Step& step) {
+    const Body& A = w.bodies[j.body_a];
+    const Body& B = w.bodies[j.body_b];
+    j.index_a = A.island_index;
+    j.index_b = B.island_index;
+    j.lc_a = A.sweep.local_center;
+    j.lc_b = B.sweep.local_center;
+    j.inv_mass_a = A.inv_mass;
+    j.inv_mass_b = B.inv_mass;
+    j.inv_ia = A.inv_I;
+    j.inv_ib = B.inv_I;
+    const Vec2 cA = w.pos[j.index_a].c;
+    const float aA = w.pos[j.index_a].a;
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    const Vec2 cB = w.pos[j.index_b].c;
+    const float aB = w.pos[j.index_b].a;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const Rot qA = rot(aA), qB = rot(aB);
+    j.r_a = mul(qA, j.local_anchor_a - j.lc_a);
+    j.r_b = mul(qB, j.local_anchor_b - j.lc_b);
+    j.u = cB + j.r_b - cA - j.r_a;
+    j.current_length = length(j.u);
+    if (j.current_length > kLinearSlop) {
+        j.u *= 1.0f / j.current_length;
+    } else {
+        j.u = v2(0.0f, 0.0f);
+        j.mass = 0.0f;
+        j.dist_impulse = 0.0f;
+        j.lower_impulse = 0.0f;
+        j.upper_impulse = 0.0f;
+    }
+    const float crAu = cross(j.r_a, j.u);
+    const float crBu = cross(j.r_b, j.u);
+    float inv_mass = j.inv_mass_a + j.inv_ia * crAu * crAu + j.inv_mass_b + j.inv_ib * crBu * crBu;
+    j.mass = inv_mass != 0.0f ? 1.0f / inv_mass : 0.0f;
+    if (j.stiffness > 0.0f && j.min_length < j.max_length) {
+        const float C = j.current_length - j.length;
+        const float d = j.damping;
+        const float k = j.stiffness;
+        const float h = step.dt;
+        j.gamma = h * (d + h * k);
+        j.gamma = j.gamma != 0.0f ? 1.0f / j.gamma : 0.0f;
+        j.bias = C * h * k * j.gamma;
+        inv_mass += j.gamma;
+        j.soft_mass = inv_mass != 0.0f ? 1.0f / inv_mass : 0.0f;
+    } else {
+        j.gamma = 0.0f;
+        j.bias = 0.0f;
+        j.soft_mass = j.mass;
+    }
+    if (step.warm) {
+        j.dist_impulse *= step.dt_ratio;
+        j.lower_impulse *= step.dt_ratio;
+        j.upper_impulse *= step.dt_ratio;
+        const Vec2 P = (j.dist_impulse + j.lower_impulse - j.upper_impulse) * j.u;
+        vA -= j.inv_mass_a * P;
+        wA -= j.inv_ia * cross(j.r_a, P);
+        vB += j.inv_mass_b * P;
+        wB += j.inv_ib * cross(j.r_b, P);
+    } else {
+        j.dist_impulse = 0.0f;
+    }
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+/* solve_velocity_constraints (:183-274) */
+static void distance_solve_velocity(World& w, Joint& j, const Step& step) {
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    auto apply = [&](Vec2 P) {
+        vA -= j.inv_mass_a * P;
+        wA -= j.inv_ia * cross(j.r_a, P);
+        vB += j.inv_mass_b * P;
+        wB += j.inv_ib * cross(j.r_b, P);
+    };
+    if (j.min_length < j.max_length) {
+        if (j.stiffness > 0.0f) {
+            const Vec2 vpA = vA + cross_sv(wA, j.r_a);
+            const Vec2 vpB = vB + cross_sv(wB, j.r_b);
+            const float cdot = dot(j.u, vpB - vpA);
+            const float impulse = -j.soft_mass * (cdot + j.bias + j.gamma * j.dist_impulse);
+            j.dist_impulse += impulse;
+            apply(impulse * j.u);
+        }
+        {
+            const float C = j.current_length - j.min_length;
+            const float bias = bmax(0.0f, C) * step.inv_dt;
+            const Vec2 vpA = vA + cross_sv(wA, j.r_a);
+            const Vec2 vpB = vB + cross_sv(wB, j.r_b);
+            const float cdot = dot(j.u, vpB - vpA);
+            float impulse = -j.mass * (cdot + bias);
+            const float old_impulse = j.lower_impulse;
+            j.lower_impulse = bmax(0.0f, j.lower_impulse + impulse);
+            impulse = j.lower_impulse - old_impulse;
+            apply(impulse * j.u);
+        }
+        {
+            const float C = j.max_length - j.current_length;
+            const float bias = bmax(0.0f, C) * step.inv_dt;
+            const Vec2 vpA = vA + cross_sv(wA, j.r_a);
+            const Vec2 vpB = vB + cross_sv(wB, j.r_b);
+            const float cdot = dot(j.u, vpA - vpB);
+            float impulse = -j.mass * (cdot + bias);
+            const float old_impulse = j.upper_impulse;
+            j.upper_impulse = bmax(0.0f, j.upper_impulse + impulse);
+            impulse = j.upper_impulse - old_impulse;
+            apply(-impulse * j.u);
+        }
+    } else {
+        const Vec2 vpA = vA + cross_sv(wA, j.r_a);
+        const Vec2 vpB = vB + cross_sv(wB, j.r_b);
+        const float cdot = dot(j.u, vpB - vpA);
+        const float impulse = -j.mass * cdot;
+        j.dist_impulse += impulse;
+        apply(impulse * j.u);
+    }
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+/* solve_position_constraints (:276-319) */
+static bool distance_solve_position(World& w, Joint& j) {
+    Vec2 cA = w.pos[j.index_a].c;
+    float aA = w.pos[j.index_a].a;
+    Vec2 cB = w.pos[j.index_b].c;
+    float aB = w.pos[j.index_b].a;
+    const Rot qA = rot(aA), qB = rot(aB);
+    const Vec2 rA = mul(qA, j.local_anchor_a - j.lc_a);
+    const Vec2 rB = mul(qB, j.local_anchor_b - j.lc_b);
+    Vec2 u = cB + rB - cA - rA;
+    const float len = normalize(u);
+    float C;
+    if (j.min_length == j.max_length) C = len - j.min_length;
+    else if (len < j.min_length) C = len - j.min_length;
+    else if (j.max_length < len) C = len - j.max_length;
+    else return true;
+    const float impulse = -j.mass * C;
+    const Vec2 P = impulse * u;
+    cA -= j.inv_mass_a * P;
+    aA -= j.inv_ia * cross(rA, P);
+    cB += j.inv_mass_b * P;
+    aB += j.inv_ib * cross(rB, P);
+    w.pos[j.index_a].c = cA;
+    w.pos[j.index_a].a = aA;
+    w.pos[j.index_b].c = cB;
+    w.pos[j.index_b].a = aB;
+    return std::fabs(C) < kLinearSlop;
+}
+
 /* init_velocity_constraints (:21-116): anchors, effective masses, warm start */
 static void joint_init_velocity(World& w, Joint& j, const Step& step) {
+    if (j.type == B2G_JOINT_DISTANCE) {
+        distance_init_velocity(w, j, step);
+        return;
+    }
     const Body& A = w.bodies[j.body_a];
     const Body& B = w.bodies[j.body_b];
     j.index_a = A.island_index;
@@ -973,6 +1143,10 @@ static void joint_init_velocity(World& w, Joint& j, const Step& step) {
 
 /* solve_velocity_constraints (:118-208): motor, lower and upper limits, point */
 static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
+    if (j.type == B2G_JOINT_DISTANCE) {
+        distance_solve_velocity(w, j, step);
+        return;
+    }
     Vec2 vA = w.vel[j.index_a].v;
     float wA = w.vel[j.index_a].w;
     Vec2 vB = w.vel[j.index_b].v;
@@ -1029,6 +1203,7 @@ static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
 
 /* solve_position_constraints (:210-287): angular limit, then the point */
 static bool joint_solve_position(World& w, Joint& j) {
+    if (j.type == B2G_JOINT_DISTANCE) return distance_solve_position(w, j);
     Vec2 cA = w.pos[j.index_a].c;
     float aA = w.pos[j.index_a].a;
     Vec2 cB = w.pos[j.index_b].c;
@@ -1820,9 +1995,18 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
     World& w = *(World*)p;
     for (int i = 0; i < n; ++i) {
         const b2g_joint_def& d = defs[i];
-        if (d.type != B2G_JOINT_REVOLUTE || d.body_a >= w.bodies.size() || d.body_b >= w.bodies.size()) return -1;
+        if ((d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE) || d.body_a >= w.bodies.size() ||
+            d.body_b >= w.bodies.size())
+            return -1;
         const int id = (int)w.joints.size();
         Joint j;
+        j.type = d.type;
+        /* b2_distance_joint_new (b2_distance_joint.rs:42-76) */
+        j.length = bmax(d.length, kLinearSlop);
+        j.min_length = bmax(d.min_length, kLinearSlop);
+        j.max_length = bmax(d.max_length, j.min_length);
+        j.stiffness = d.stiffness;
+        j.damping = d.damping;
         j.body_a = (int)d.body_a;
         j.body_b = (int)d.body_b;
         j.collide_connected = d.collide_connected != 0;
@@ -1858,6 +2042,14 @@ int ora_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) 
     if ((size_t)first + count > w.joints.size()) return -1;
     for (uint32_t i = 0; i < count; ++i) {
         const Joint& j = w.joints[first + i];
+        if (j.type == B2G_JOINT_DISTANCE) {
+            out[5 * i + 0] = j.dist_impulse;
+            out[5 * i + 1] = j.lower_impulse;
+            out[5 * i + 2] = j.upper_impulse;
+            out[5 * i + 3] = 0.0f;
+            out[5 * i + 4] = 0.0f;
+            continue;
+        }
         out[5 * i + 0] = j.impulse.x;
         out[5 * i + 1] = j.impulse.y;
         out[5 * i + 2] = j.motor_impulse;

@@ -437,3 +437,50 @@ def test_joint_created_mid_run_filters_contacts(built):
     step_both(40)
     assert not any(tuple(sorted((int(c["fixture_a"]), int(c["fixture_b"])))) == pair for c in gpu.get_contacts())
     assert np.array_equal(gpu.get_joint_impulses(), ora.get_joint_impulses())
+
+
+def test_distance_joints_lockstep(built):
+    """Distance joints: a rigid pendulum, a damped spring with min and max length, a rope (max
+    length only), and a chain of boxes hung on rigid distance joints with bodies dropped on it;
+    bodies, manifolds and joint impulses bit-exact every step."""
+    n_chain, n_drop = 10, 12
+    nb = 1 + 3 + n_chain + n_drop
+    bodies = b2g.body_defs(nb)
+    bodies["allow_sleep"] = 0
+    bodies[1:]["type"] = b2g.DYNAMIC
+    bodies[1]["position"] = (-10.0, 7.0)
+    bodies[2]["position"] = (-6.0, 9.0)
+    bodies[3]["position"] = (-2.0, 12.0)
+    bodies[3]["linear_velocity"] = (4.0, 0.0)
+    fx = [b2g.edge_fixture(0, (-30.0, 0.0), (30.0, 0.0)),
+          b2g.box_fixture(1, 0.3, 0.3, density=2.0), b2g.circle_fixture(2, 0.4, density=2.0),
+          b2g.box_fixture(3, 0.4, 0.2, density=2.0)]
+    joints = [b2g.distance_joint(0, 1, (-10.0, 10.0), (0.0, 0.3), 3.0),
+              b2g.distance_joint(0, 2, (-6.0, 12.0), (0.0, 0.0), 3.0, min_length=1.0, max_length=5.0,
+                                 stiffness=20.0, damping=0.5),
+              b2g.distance_joint(0, 3, (-2.0, 14.0), (-0.4, 0.0), 4.0, min_length=0.0, max_length=4.0)]
+    first = 4
+    for i in range(n_chain):
+        b = first + i
+        bodies[b]["position"] = (2.0 + 1.0 * i, 8.0)
+        fx.append(b2g.box_fixture(b, 0.4, 0.1, density=5.0, friction=0.3))
+        if i == 0:
+            joints.append(b2g.distance_joint(0, b, (1.0, 8.0), (-0.4, 0.0), 0.6))
+        else:
+            joints.append(b2g.distance_joint(b - 1, b, (0.4, 0.0), (-0.4, 0.0), 0.2))
+    joints.append(b2g.distance_joint(first + n_chain - 1, 0, (0.4, 0.0), (12.0, 8.0), 0.6))
+    rng = np.random.default_rng(31)
+    for k in range(n_drop):
+        b = first + n_chain + k
+        bodies[b]["position"] = (rng.uniform(2.5, 11.0), rng.uniform(10.0, 16.0))
+        fx.append(b2g.circle_fixture(b, 0.25, density=1.0, friction=0.4) if k % 2 else
+                  b2g.box_fixture(b, 0.25, 0.2, density=1.0, friction=0.4))
+    s = {"name": "distance", "bodies": bodies, "fixtures": np.concatenate(fx), "joints": np.concatenate(joints),
+         "gravity": (0.0, -10.0), "dt": np.float32(1.0 / 60.0), "vi": 8, "pi": 3, "steps": 200, "num_worlds": 1,
+         "allow_sleep": False, "n_dynamic": nb - 1}
+    recs, gpu, _ = parity.lockstep(s, 200)
+    for r in recs:
+        _assert_step(r)
+        assert r["joint_impulses_equal"], r
+    st = gpu.get_body_states()
+    assert abs(float(np.linalg.norm(st["position"][1] + np.array([10.0, -10.0]) - [0.0, 0.0]) ) - 3.0) < 0.35
