@@ -95,6 +95,7 @@ struct World {
     bool warm = true, continuous = false, allow_sleep = true, auto_clear = true;
     int toi_schedule = 0;  /* B2G_TOI_SCHEDULE_* */
     bool asleep_seen = false;  /* a body was created asleep or put to sleep by the caller */
+    bool kinematic_or_bullet = false;  /* a kinematic or bullet body exists */
     /* joints: definitions, host copies of their impulses, the colouring, body -> joints */
     std::vector<b2g_joint_def> joints;
     std::vector<float4> h_jimp, h_jimp2;
@@ -915,6 +916,7 @@ StepParams make_params(World* w, float dt, int vi, int pi) {
     sp.record_events = w->record_events ? 1 : 0;
     sp.record_pairs = w->record_pairs ? 1 : 0;
     sp.toi_schedule = w->toi_schedule;
+    sp.toi_may_conflict = w->kinematic_or_bullet ? 1 : 0;
     return sp;
 }
 
@@ -1023,7 +1025,8 @@ int step(World* w, float dt, int vi, int pi) {
         key.pi = pi;
         key.flags = sp.warm | (sp.allow_sleep << 1) | (sp.auto_clear << 2) | (sp.record_events << 3) |
                     (sp.record_pairs << 4) | ((w->tape && w->tape->recording) ? (1 << 5) : 0) |
-                    (w->continuous ? (1 << 6) : 0) | (sp.toi_schedule << 7) | (w->asleep_seen ? (1 << 9) : 0);
+                    (w->continuous ? (1 << 6) : 0) | (sp.toi_schedule << 7) | (w->asleep_seen ? (1 << 9) : 0) |
+                    (sp.toi_may_conflict << 10);
         key.generation = w->alloc_generation;
         key.n_bodies = w->d.n_bodies;
         key.n_fixtures = w->d.n_fixtures;
@@ -1262,6 +1265,7 @@ int b2g_create_bodies(void* p, const b2g_body_def* defs, int32_t n, uint32_t* id
         if (d.allow_sleep) fl |= BF_AUTO_SLEEP;
         if (d.fixed_rotation) fl |= BF_FIXED_ROTATION;
         if (d.bullet) fl |= BF_BULLET;
+        if (d.type == B2G_KINEMATIC_BODY || (d.type == B2G_DYNAMIC_BODY && d.bullet)) w->kinematic_or_bullet = true;
         const Rot q = rot(d.angle);
         const int id = (int)w->h_flags.size();
         w->h_flags.push_back(fl);

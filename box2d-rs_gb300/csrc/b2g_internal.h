@@ -152,6 +152,8 @@ struct StepParams {
     int part_bodies;      /* part-local solve: bodies cached in shared memory per block */
     int part_slot_bytes;  /* part-local solve: shared memory per block for constraint slots */
     int toi_schedule;     /* continuous pass: B2G_TOI_SCHEDULE_* */
+    int toi_may_conflict; /* continuous pass: a kinematic or bullet body exists, so side-by-side events
+                             can conflict and the pass keeps a snapshot to restart from */
 };
 
 struct DevWorld {

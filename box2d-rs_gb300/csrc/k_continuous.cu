@@ -549,6 +549,7 @@ __global__ void __launch_bounds__(kTBlock) k_continuous(DevWorld w, StepParams s
     volatile int* vcnt = w.cnt;
     int epoch = w.cnt[CNT_TOI_PASSES] * 2 + 1;  /* odd, never 0 (the marks' initial value) */
     bool batched = sp.toi_schedule != B2G_TOI_SCHEDULE_ONE_AT_A_TIME;
+    bool snapshot = false;  /* the pass's snapshot was taken (uniform across blocks) */
 
     pass_init(w, n_tab, epoch, gtid, gstride);
     if (!grid_barrier(w)) return;
@@ -635,6 +636,11 @@ __global__ void __launch_bounds__(kTBlock) k_continuous(DevWorld w, StepParams s
         const int hits = min(vcnt[CNT_TOI_HITS], w.contact_cap);
         if (hits == 0) break;
 
+        if (batched && vcnt[CNT_TOI_CONFLICT] && !snapshot) {
+            /* a conflict where none can arise: report it rather than restart from nothing */
+            if (gtid == 0) toi_overflow(w);
+            batched = false;
+        }
         if (batched && vcnt[CNT_TOI_CONFLICT]) {
             /* two side-by-side events asked one body for different alphas: back to the snapshot,
              * then every event alone */
@@ -671,8 +677,10 @@ __global__ void __launch_bounds__(kTBlock) k_continuous(DevWorld w, StepParams s
             iter = -1;
             continue;
         }
-        if (iter == 0 && batched) {
-            /* the snapshot a conflict goes back to (nothing has moved yet) */
+        if (iter == 0 && batched && (sp.toi_may_conflict || sp.toi_schedule == B2G_TOI_SCHEDULE_RESTART_ON_ADVANCE)) {
+            /* the snapshot a conflict goes back to (nothing has moved yet). Without kinematic and
+             * bullet bodies every event is with a static body and no sweep is ever advanced for a
+             * time of impact, so no conflict can arise and none is kept. */
             for (int b = gtid; b < w.n_bodies; b += gstride) {
                 w.s_xf[b] = w.b_xf[b];
                 w.s_pos[b] = w.b_pos[b];
@@ -692,6 +700,7 @@ __global__ void __launch_bounds__(kTBlock) k_continuous(DevWorld w, StepParams s
                 vcnt[CNT_TOI_SNAP_EV] = vcnt[CNT_EVENTS];
                 vcnt[CNT_TOI_SNAP_TE] = vcnt[CNT_TOI_EVENTS];
             }
+            snapshot = true;
         }
 
         /* 2: commit the sweep advances; ties of the minima go to the smallest key */
