@@ -165,6 +165,20 @@ JOINT_DEF = np.dtype(
     ]
 )
 JOINT_DISTANCE = 3
+JOINT_WELD = 8
+
+
+def weld_joint(body_a, body_b, anchor_a, anchor_b, reference_angle=0.0, stiffness=0.0, damping=0.0,
+               collide_connected=False):
+    """B2weldJointDef with local anchors; stiffness > 0 makes the angular part a spring."""
+    d = np.zeros(1, JOINT_DEF)
+    d["type"] = JOINT_WELD
+    d["body_a"], d["body_b"] = body_a, body_b
+    d["collide_connected"] = int(bool(collide_connected))
+    d["local_anchor_a"], d["local_anchor_b"] = anchor_a, anchor_b
+    d["reference_angle"] = reference_angle
+    d["stiffness"], d["damping"] = stiffness, damping
+    return d
 
 
 def distance_joint(body_a, body_b, anchor_a, anchor_b, length, min_length=None, max_length=None, stiffness=0.0,

@@ -256,7 +256,7 @@ struct DevWorld {
      * joints sorted by colour (j_order, j_coff: n_jcolours + 1 offsets) and body -> joints */
     int n_joints, n_jcolours;
     int2* j_body;
-    float4 *j_anchor, *j_lim, *j_par, *j_imp, *j_imp2, *j_rr, *j_k, *j_m;
+    float4 *j_anchor, *j_lim, *j_par, *j_imp, *j_imp2, *j_rr, *j_k, *j_m, *j_x;
     float2* j_s;
     int *j_order, *j_coff;
     int *b_jnt_off, *b_jnt;

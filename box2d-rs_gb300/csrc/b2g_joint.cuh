@@ -210,6 +210,234 @@ __device__ bool distance_solve_position(const DevWorld& w, int j) {
     return fabsr(C) < kLinearSlop;
 }
 
+/* ---- weld joint (B2weldJoint, private/dynamics/joints/b2_weld_joint.rs) with B2Mat33
+ * (src/b2_math.rs:569-608, private/common/b2_math.rs:5-71) ----
+ * j_lim = (reference angle, stiffness, damping, -), j_imp = (x, y, angular, -); the step's mass
+ * matrix: columns ex = j_k.xyz, ey = (j_k.w, j_imp2.x, j_imp2.y), ez = (j_imp2.z, j_imp2.w, j_x.x);
+ * j_s = (gamma, bias). */
+
+struct V3 {
+    float x, y, z;
+};
+__device__ __forceinline__ V3 v3(float x, float y, float z) {
+    V3 r;
+    r.x = x;
+    r.y = y;
+    r.z = z;
+    return r;
+}
+__device__ __forceinline__ V3 v3add(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 v3scale(float s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float v3dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 v3cross(V3 a, V3 b) {
+    return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+struct M33 {
+    V3 ex, ey, ez;
+};
+__device__ __forceinline__ M33 weld_k(float mA, float mB, float iA, float iB, V2 rA, V2 rB) {
+    M33 k;
+    k.ex.x = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
+    k.ey.x = -rA.y * rA.x * iA - rB.y * rB.x * iB;
+    k.ez.x = -rA.y * iA - rB.y * iB;
+    k.ex.y = k.ey.x;
+    k.ey.y = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
+    k.ez.y = rA.x * iA + rB.x * iB;
+    k.ex.z = k.ez.x;
+    k.ey.z = k.ez.y;
+    k.ez.z = iA + iB;
+    return k;
+}
+__device__ __forceinline__ void m33_inverse22(const M33& a, M33& m) {
+    const float A = a.ex.x, B = a.ey.x, C = a.ex.y, D = a.ey.y;
+    float det = A * D - B * C;
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    m.ex = v3(det * D, -det * C, 0.0f);
+    m.ey = v3(-det * B, det * A, 0.0f);
+    m.ez = v3(0.0f, 0.0f, 0.0f);
+}
+__device__ __forceinline__ void m33_sym_inverse33(const M33& a, M33& m) {
+    float det = v3dot(a.ex, v3cross(a.ey, a.ez));
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    const float a11 = a.ex.x, a12 = a.ey.x, a13 = a.ez.x, a22 = a.ey.y, a23 = a.ez.y, a33 = a.ez.z;
+    m.ex = v3(det * (a22 * a33 - a23 * a23), det * (a13 * a23 - a12 * a33), det * (a12 * a23 - a13 * a22));
+    m.ey = v3(m.ex.y, det * (a11 * a33 - a13 * a13), det * (a13 * a12 - a11 * a23));
+    m.ez = v3(m.ex.z, m.ey.z, det * (a11 * a22 - a12 * a12));
+}
+__device__ __forceinline__ V3 m33_solve33(const M33& a, V3 b) {
+    float det = v3dot(a.ex, v3cross(a.ey, a.ez));
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    return v3(det * v3dot(b, v3cross(a.ey, a.ez)), det * v3dot(a.ex, v3cross(b, a.ez)),
+              det * v3dot(a.ex, v3cross(a.ey, b)));
+}
+
+/* init_velocity_constraints */
+__device__ void weld_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 an = w.j_anchor[j];
+    const float4 lim = w.j_lim[j];
+    const float4 massA = w.b_mass[bd.x], massB = w.b_mass[bd.y];
+    const float2 lcA = w.b_lc[bd.x], lcB = w.b_lc[bd.y];
+    const float mA = massA.y, mB = massB.y, iA = massA.w, iB = massB.w;
+    const float aA = w.b_pos[bd.x].z, aB = w.b_pos[bd.y].z;
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = rot(aA), qB = rot(aB);
+    const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+    const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+    const M33 k = weld_k(mA, mB, iA, iB, rA, rB);
+    M33 mass;
+    float gamma, bias;
+    if (lim.y > 0.0f) {
+        m33_inverse22(k, mass);
+        float inv_m = iA + iB;
+        const float C = aB - aA - lim.x;
+        const float d = lim.z;
+        const float kk = lim.y;
+        const float h = sp.dt;
+        gamma = h * (d + h * kk);
+        gamma = gamma != 0.0f ? fdiv(1.0f, gamma) : 0.0f;
+        bias = C * h * kk * gamma;
+        inv_m += gamma;
+        mass.ez.z = inv_m != 0.0f ? fdiv(1.0f, inv_m) : 0.0f;
+    } else if (k.ez.z == 0.0f) {
+        m33_inverse22(k, mass);
+        gamma = 0.0f;
+        bias = 0.0f;
+    } else {
+        m33_sym_inverse33(k, mass);
+        gamma = 0.0f;
+        bias = 0.0f;
+    }
+    float4 imp = w.j_imp[j];
+    if (sp.warm) {
+        imp.x *= sp.dt_ratio;
+        imp.y *= sp.dt_ratio;
+        imp.z *= sp.dt_ratio;
+        const V2 P = mk(imp.x, imp.y);
+        vA = sub(vA, scale(mA, P));
+        wA -= iA * (cross(rA, P) + imp.z);
+        vB = add(vB, scale(mB, P));
+        wB += iB * (cross(rB, P) + imp.z);
+    } else {
+        imp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    w.j_imp[j] = imp;
+    w.j_rr[j] = make_float4(rA.x, rA.y, rB.x, rB.y);
+    w.j_k[j] = make_float4(mass.ex.x, mass.ex.y, mass.ex.z, mass.ey.x);
+    w.j_imp2[j] = make_float4(mass.ey.y, mass.ey.z, mass.ez.x, mass.ez.y);
+    w.j_x[j] = make_float4(mass.ez.z, 0.0f, 0.0f, 0.0f);
+    w.j_m[j] = make_float4(mA, mB, iA, iB);
+    w.j_s[j] = make_float2(gamma, bias);
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+/* solve_velocity_constraints */
+__device__ void weld_solve_velocity(const DevWorld& w, int j) {
+    const int2 bd = w.j_body[j];
+    const float stiffness = w.j_lim[j].y;
+    const float4 m = w.j_m[j];
+    const float mA = m.x, mB = m.y, iA = m.z, iB = m.w;
+    const float4 rr = w.j_rr[j];
+    const V2 rA = mk(rr.x, rr.y), rB = mk(rr.z, rr.w);
+    const float4 k0 = w.j_k[j], k1 = w.j_imp2[j];
+    M33 mass;
+    mass.ex = v3(k0.x, k0.y, k0.z);
+    mass.ey = v3(k0.w, k1.x, k1.y);
+    mass.ez = v3(k1.z, k1.w, w.j_x[j].x);
+    const float2 gb = w.j_s[j];
+    float4 imp = w.j_imp[j];
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    if (stiffness > 0.0f) {
+        const float cdot2 = wB - wA;
+        const float impulse2 = -mass.ez.z * (cdot2 + gb.y + gb.x * imp.z);
+        imp.z += impulse2;
+        wA -= iA * impulse2;
+        wB += iB * impulse2;
+        const V2 cdot1 = sub(sub(add(vB, cross_sv(wB, rB)), vA), cross_sv(wA, rA));
+        const V2 impulse1 = neg(mk(mass.ex.x * cdot1.x + mass.ey.x * cdot1.y, mass.ex.y * cdot1.x + mass.ey.y * cdot1.y));
+        imp.x += impulse1.x;
+        imp.y += impulse1.y;
+        vA = sub(vA, scale(mA, impulse1));
+        wA -= iA * cross(rA, impulse1);
+        vB = add(vB, scale(mB, impulse1));
+        wB += iB * cross(rB, impulse1);
+    } else {
+        const V2 cdot1 = sub(sub(add(vB, cross_sv(wB, rB)), vA), cross_sv(wA, rA));
+        const float cdot2 = wB - wA;
+        const V3 mc = v3add(v3add(v3scale(cdot1.x, mass.ex), v3scale(cdot1.y, mass.ey)), v3scale(cdot2, mass.ez));
+        const V3 impulse = v3(-mc.x, -mc.y, -mc.z);
+        imp.x += impulse.x;
+        imp.y += impulse.y;
+        imp.z += impulse.z;
+        const V2 P = mk(impulse.x, impulse.y);
+        vA = sub(vA, scale(mA, P));
+        wA -= iA * (cross(rA, P) + impulse.z);
+        vB = add(vB, scale(mB, P));
+        wB += iB * (cross(rB, P) + impulse.z);
+    }
+    w.j_imp[j] = imp;
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+/* solve_position_constraints, b2_weld_joint.rs:230-287 */
+__device__ bool weld_solve_position(const DevWorld& w, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 an = w.j_anchor[j];
+    const float4 lim = w.j_lim[j];
+    const float4 m = w.j_m[j];
+    const float mA = m.x, mB = m.y, iA = m.z, iB = m.w;
+    const float2 lcA = w.b_lc[bd.x], lcB = w.b_lc[bd.y];
+    const float4 pa = w.b_pos[bd.x], pb = w.b_pos[bd.y];
+    V2 cA = mk(pa.x, pa.y), cB = mk(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    const Rot qA = rot(aA), qB = rot(aB);
+    const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+    const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+    float position_error, angular_error;
+    const M33 K = weld_k(mA, mB, iA, iB, rA, rB);
+    if (lim.y > 0.0f) {
+        const V2 C1 = sub(sub(add(cB, rB), cA), rA);
+        position_error = length(C1);
+        angular_error = 0.0f;
+        const V2 P = neg(mat22_solve(K.ex.x, K.ex.y, K.ey.x, K.ey.y, C1));
+        cA = sub(cA, scale(mA, P));
+        aA -= iA * cross(rA, P);
+        cB = add(cB, scale(mB, P));
+        aB += iB * cross(rB, P);
+    } else {
+        const V2 C1 = sub(sub(add(cB, rB), cA), rA);
+        const float C2 = aB - aA - lim.x;
+        position_error = length(C1);
+        angular_error = fabsr(C2);
+        V3 impulse;
+        if (K.ez.z > 0.0f) {
+            const V3 x = m33_solve33(K, v3(C1.x, C1.y, C2));
+            impulse = v3(-x.x, -x.y, -x.z);
+        } else {
+            const V2 i2 = neg(mat22_solve(K.ex.x, K.ex.y, K.ey.x, K.ey.y, C1));
+            impulse = v3(i2.x, i2.y, 0.0f);
+        }
+        const V2 P = mk(impulse.x, impulse.y);
+        cA = sub(cA, scale(mA, P));
+        aA -= iA * (cross(rA, P) + impulse.z);
+        cB = add(cB, scale(mB, P));
+        aB += iB * (cross(rB, P) + impulse.z);
+    }
+    if (joint_body_dynamic(w, bd.x)) w.b_pos[bd.x] = make_float4(cA.x, cA.y, aA, pa.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_pos[bd.y] = make_float4(cB.x, cB.y, aB, pb.w);
+    return position_error <= kLinearSlop && angular_error <= kAngularSlop;
+}
+
+__device__ __forceinline__ uint32_t joint_type(const DevWorld& w, int j) {
+    return (__float_as_uint(w.j_par[j].y) >> JF_TYPE_SHIFT) & 0xffu;
+}
+
 __device__ __forceinline__ bool joint_is_distance(const DevWorld& w, int j) {
     return ((__float_as_uint(w.j_par[j].y) >> JF_TYPE_SHIFT) & 0xffu) == B2G_JOINT_DISTANCE;
 }
@@ -398,15 +626,22 @@ __device__ bool revolute_solve_position(const DevWorld& w, int j) {
 
 /* the joint routines by type */
 __device__ __forceinline__ void joint_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
-    if (joint_is_distance(w, j)) distance_init_velocity(w, sp, j);
+    const uint32_t t = joint_type(w, j);
+    if (t == B2G_JOINT_DISTANCE) distance_init_velocity(w, sp, j);
+    else if (t == B2G_JOINT_WELD) weld_init_velocity(w, sp, j);
     else revolute_init_velocity(w, sp, j);
 }
 __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
-    if (joint_is_distance(w, j)) distance_solve_velocity(w, sp, j);
+    const uint32_t t = joint_type(w, j);
+    if (t == B2G_JOINT_DISTANCE) distance_solve_velocity(w, sp, j);
+    else if (t == B2G_JOINT_WELD) weld_solve_velocity(w, j);
     else revolute_solve_velocity(w, sp, j);
 }
 __device__ __forceinline__ bool joint_solve_position(const DevWorld& w, int j) {
-    return joint_is_distance(w, j) ? distance_solve_position(w, j) : revolute_solve_position(w, j);
+    const uint32_t t = joint_type(w, j);
+    if (t == B2G_JOINT_DISTANCE) return distance_solve_position(w, j);
+    if (t == B2G_JOINT_WELD) return weld_solve_position(w, j);
+    return revolute_solve_position(w, j);
 }
 
 /* the joint belongs to an island solved this step (a body of it is non-static and in one); both

@@ -101,6 +101,9 @@ struct Joint {
     float length = 0, min_length = 0, max_length = 0, stiffness = 0, damping = 0;
     float dist_impulse = 0, gamma = 0, bias = 0, current_length = 0, mass = 0, soft_mass = 0;
     Vec2 u{0, 0};
+    /* B2weldJoint (private/dynamics/joints/b2_weld_joint.rs): impulse (x, y, angular), mass matrix */
+    float weld_impulse[3] = {0, 0, 0};
+    float weld_mass[9] = {0};  /* ex, ey, ez columns */
     bool collide_connected = false, island_flag = false;
     Vec2 local_anchor_a{0, 0}, local_anchor_b{0, 0};
     float reference_angle = 0;
@@ -1074,8 +1077,240 @@ static bool distance_solve_position(World& w, Joint& j) {
     return std::fabs(C) < kLinearSlop;
 }
 
+/* ---- weld joint, private/dynamics/joints/b2_weld_joint.rs (with B2Mat33, src/b2_math.rs and
+ * private/common/b2_math.rs:5-71) ---- */
+
+struct V3 {
+    float x, y, z;
+};
+static V3 v3add(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+static V3 v3scale(float s, V3 a) { return V3{s * a.x, s * a.y, s * a.z}; }
+static float v3dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static V3 v3cross(V3 a, V3 b) { return V3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+struct M33 {
+    V3 ex, ey, ez;
+};
+/* K of the weld joint (b2_weld_joint.rs init and position solve share its expressions) */
+static M33 weld_k(float mA, float mB, float iA, float iB, Vec2 rA, Vec2 rB) {
+    M33 k;
+    k.ex.x = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
+    k.ey.x = -rA.y * rA.x * iA - rB.y * rB.x * iB;
+    k.ez.x = -rA.y * iA - rB.y * iB;
+    k.ex.y = k.ey.x;
+    k.ey.y = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
+    k.ez.y = rA.x * iA + rB.x * iB;
+    k.ex.z = k.ez.x;
+    k.ey.z = k.ez.y;
+    k.ez.z = iA + iB;
+    return k;
+}
+static void m33_inverse22(const M33& a, M33& m) {
+    const float A = a.ex.x, B = a.ey.x, C = a.ex.y, D = a.ey.y;
+    float det = A * D - B * C;
+    if (det != 0.0f) det = 1.0f / det;
+    m.ex.x = det * D;
+    m.ey.x = -det * B;
+    m.ex.z = 0.0f;
+    m.ex.y = -det * C;
+    m.ey.y = det * A;
+    m.ey.z = 0.0f;
+    m.ez.x = 0.0f;
+    m.ez.y = 0.0f;
+    m.ez.z = 0.0f;
+}
+static void m33_sym_inverse33(const M33& a, M33& m) {
+    float det = v3dot(a.ex, v3cross(a.ey, a.ez));
+    if (det != 0.0f) det = 1.0f / det;
+    const float a11 = a.ex.x, a12 = a.ey.x, a13 = a.ez.x, a22 = a.ey.y, a23 = a.ez.y, a33 = a.ez.z;
+    m.ex.x = det * (a22 * a33 - a23 * a23);
+    m.ex.y = det * (a13 * a23 - a12 * a33);
+    m.ex.z = det * (a12 * a23 - a13 * a22);
+    m.ey.x = m.ex.y;
+    m.ey.y = det * (a11 * a33 - a13 * a13);
+    m.ey.z = det * (a13 * a12 - a11 * a23);
+    m.ez.x = m.ex.z;
+    m.ez.y = m.ey.z;
+    m.ez.z = det * (a11 * a22 - a12 * a12);
+}
+static V3 m33_solve33(const M33& a, V3 b) {
+    float det = v3dot(a.ex, v3cross(a.ey, a.ez));
+    if (det != 0.0f) det = 1.0f / det;
+    return V3{det * v3dot(b, v3cross(a.ey, a.ez)), det * v3dot(a.ex, v3cross(b, a.ez)), det * v3dot(a.ex, v3cross(a.ey, b))};
+}
+static Vec2 m33_solve22(const M33& a, Vec2 b) {
+    const float a11 = a.ex.x, a12 = a.ey.x, a21 = a.ex.y, a22 = a.ey.y;
+    float det = a11 * a22 - a12 * a21;
+    if (det != 0.0f) det = 1.0f / det;
+    return v2(det * (a22 * b.x - a12 * b.y), det * (a11 * b.y - a21 * b.x));
+}
+static M33 weld_mass_of(const Joint& j) {
+    M33 m;
+    m.ex = V3{j.weld_mass[0], j.weld_mass[1], j.weld_mass[2]};
+    m.ey = V3{j.weld_mass[3], j.weld_mass[4], j.weld_mass[5]};
+    m.ez = V3{j.weld_mass[6], j.weld_mass[7], j.weld_mass[8]};
+    return m;
+}
+
+/* init_velocity_constraints */
+static void weld_init_velocity(World& w, Joint& j, const Step& step) {
+    const Body& A = w.bodies[j.body_a];
+    const Body& B = w.bodies[j.body_b];
+    j.index_a = A.island_index;
+    j.index_b = B.island_index;
+    j.lc_a = A.sweep.local_center;
+    j.lc_b = B.sweep.local_center;
+    j.inv_mass_a = A.inv_mass;
+    j.inv_mass_b = B.inv_mass;
+    j.inv_ia = A.inv_I;
+    j.inv_ib = B.inv_I;
+    const float aA = w.pos[j.index_a].a, aB = w.pos[j.index_b].a;
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const Rot qA = rot(aA), qB = rot(aB);
+    j.r_a = mul(qA, j.local_anchor_a - j.lc_a);
+    j.r_b = mul(qB, j.local_anchor_b - j.lc_b);
+    const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+    const M33 k = weld_k(mA, mB, iA, iB, j.r_a, j.r_b);
+    M33 mass{};
+    if (j.stiffness > 0.0f) {
+        m33_inverse22(k, mass);
+        float inv_m = iA + iB;
+        const float C = aB - aA - j.reference_angle;
+        const float d = j.damping;
+        const float kk = j.stiffness;
+        const float h = step.dt;
+        j.gamma = h * (d + h * kk);
+        j.gamma = j.gamma != 0.0f ? 1.0f / j.gamma : 0.0f;
+        j.bias = C * h * kk * j.gamma;
+        inv_m += j.gamma;
+        mass.ez.z = inv_m != 0.0f ? 1.0f / inv_m : 0.0f;
+    } else if (k.ez.z == 0.0f) {
+        m33_inverse22(k, mass);
+        j.gamma = 0.0f;
+        j.bias = 0.0f;
+    } else {
+        m33_sym_inverse33(k, mass);
+        j.gamma = 0.0f;
+        j.bias = 0.0f;
+    }
+    const float mm[9] = {mass.ex.x, mass.ex.y, mass.ex.z, mass.ey.x, mass.ey.y, mass.ey.z, mass.ez.x, mass.ez.y, mass.ez.z};
+    for (int q = 0; q < 9; ++q) j.weld_mass[q] = mm[q];
+    if (step.warm) {
+        for (float& x : j.weld_impulse) x *= step.dt_ratio;
+        const Vec2 P = v2(j.weld_impulse[0], j.weld_impulse[1]);
+        vA -= mA * P;
+        wA -= iA * (cross(j.r_a, P) + j.weld_impulse[2]);
+        vB += mB * P;
+        wB += iB * (cross(j.r_b, P) + j.weld_impulse[2]);
+    } else {
+        j.weld_impulse[0] = j.weld_impulse[1] = j.weld_impulse[2] = 0.0f;
+    }
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+/* solve_velocity_constraints */
+static void weld_solve_velocity(World& w, Joint& j) {
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+    const M33 mass = weld_mass_of(j);
+    if (j.stiffness > 0.0f) {
+        const float cdot2 = wB - wA;
+        const float impulse2 = -mass.ez.z * (cdot2 + j.bias + j.gamma * j.weld_impulse[2]);
+        j.weld_impulse[2] += impulse2;
+        wA -= iA * impulse2;
+        wB += iB * impulse2;
+        const Vec2 cdot1 = vB + cross_sv(wB, j.r_b) - vA - cross_sv(wA, j.r_a);
+        const Vec2 impulse1 = -v2(mass.ex.x * cdot1.x + mass.ey.x * cdot1.y, mass.ex.y * cdot1.x + mass.ey.y * cdot1.y);
+        j.weld_impulse[0] += impulse1.x;
+        j.weld_impulse[1] += impulse1.y;
+        const Vec2 P = impulse1;
+        vA -= mA * P;
+        wA -= iA * cross(j.r_a, P);
+        vB += mB * P;
+        wB += iB * cross(j.r_b, P);
+    } else {
+        const Vec2 cdot1 = vB + cross_sv(wB, j.r_b) - vA - cross_sv(wA, j.r_a);
+        const float cdot2 = wB - wA;
+        const V3 cdot{cdot1.x, cdot1.y, cdot2};
+        const V3 mc = v3add(v3add(v3scale(cdot.x, mass.ex), v3scale(cdot.y, mass.ey)), v3scale(cdot.z, mass.ez));
+        const V3 impulse{-mc.x, -mc.y, -mc.z};
+        j.weld_impulse[0] += impulse.x;
+        j.weld_impulse[1] += impulse.y;
+        j.weld_impulse[2] += impulse.z;
+        const Vec2 P = v2(impulse.x, impulse.y);
+        vA -= mA * P;
+        wA -= iA * (cross(j.r_a, P) + impulse.z);
+        vB += mB * P;
+        wB += iB * (cross(j.r_b, P) + impulse.z);
+    }
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+/* solve_position_constraints (:230-287) */
+static bool weld_solve_position(World& w, Joint& j) {
+    Vec2 cA = w.pos[j.index_a].c;
+    float aA = w.pos[j.index_a].a;
+    Vec2 cB = w.pos[j.index_b].c;
+    float aB = w.pos[j.index_b].a;
+    const Rot qA = rot(aA), qB = rot(aB);
+    const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+    const Vec2 rA = mul(qA, j.local_anchor_a - j.lc_a);
+    const Vec2 rB = mul(qB, j.local_anchor_b - j.lc_b);
+    float position_error, angular_error;
+    const M33 K = weld_k(mA, mB, iA, iB, rA, rB);
+    if (j.stiffness > 0.0f) {
+        const Vec2 C1 = cB + rB - cA - rA;
+        position_error = length(C1);
+        angular_error = 0.0f;
+        const Vec2 P = -m33_solve22(K, C1);
+        cA -= mA * P;
+        aA -= iA * cross(rA, P);
+        cB += mB * P;
+        aB += iB * cross(rB, P);
+    } else {
+        const Vec2 C1 = cB + rB - cA - rA;
+        const float C2 = aB - aA - j.reference_angle;
+        position_error = length(C1);
+        angular_error = std::fabs(C2);
+        const V3 C{C1.x, C1.y, C2};
+        V3 impulse;
+        if (K.ez.z > 0.0f) {
+            const V3 x = m33_solve33(K, C);
+            impulse = V3{-x.x, -x.y, -x.z};
+        } else {
+            const Vec2 i2 = -m33_solve22(K, C1);
+            impulse = V3{i2.x, i2.y, 0.0f};
+        }
+        const Vec2 P = v2(impulse.x, impulse.y);
+        cA -= mA * P;
+        aA -= iA * (cross(rA, P) + impulse.z);
+        cB += mB * P;
+        aB += iB * (cross(rB, P) + impulse.z);
+    }
+    w.pos[j.index_a].c = cA;
+    w.pos[j.index_a].a = aA;
+    w.pos[j.index_b].c = cB;
+    w.pos[j.index_b].a = aB;
+    return position_error <= kLinearSlop && angular_error <= kAngularSlop;
+}
+
 /* init_velocity_constraints (:21-116): anchors, effective masses, warm start */
 static void joint_init_velocity(World& w, Joint& j, const Step& step) {
+    if (j.type == B2G_JOINT_WELD) {
+        weld_init_velocity(w, j, step);
+        return;
+    }
     if (j.type == B2G_JOINT_DISTANCE) {
         distance_init_velocity(w, j, step);
         return;
@@ -1143,6 +1378,10 @@ static void joint_init_velocity(World& w, Joint& j, const Step& step) {
 
 /* solve_velocity_constraints (:118-208): motor, lower and upper limits, point */
 static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
+    if (j.type == B2G_JOINT_WELD) {
+        weld_solve_velocity(w, j);
+        return;
+    }
     if (j.type == B2G_JOINT_DISTANCE) {
         distance_solve_velocity(w, j, step);
         return;
@@ -1204,6 +1443,7 @@ static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
 /* solve_position_constraints (:210-287): angular limit, then the point */
 static bool joint_solve_position(World& w, Joint& j) {
     if (j.type == B2G_JOINT_DISTANCE) return distance_solve_position(w, j);
+    if (j.type == B2G_JOINT_WELD) return weld_solve_position(w, j);
     Vec2 cA = w.pos[j.index_a].c;
     float aA = w.pos[j.index_a].a;
     Vec2 cB = w.pos[j.index_b].c;
@@ -1995,7 +2235,8 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
     World& w = *(World*)p;
     for (int i = 0; i < n; ++i) {
         const b2g_joint_def& d = defs[i];
-        if ((d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE) || d.body_a >= w.bodies.size() ||
+        if ((d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE && d.type != B2G_JOINT_WELD) ||
+            d.body_a >= w.bodies.size() ||
             d.body_b >= w.bodies.size())
             return -1;
         const int id = (int)w.joints.size();
@@ -2042,6 +2283,14 @@ int ora_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) 
     if ((size_t)first + count > w.joints.size()) return -1;
     for (uint32_t i = 0; i < count; ++i) {
         const Joint& j = w.joints[first + i];
+        if (j.type == B2G_JOINT_WELD) {
+            out[5 * i + 0] = j.weld_impulse[0];
+            out[5 * i + 1] = j.weld_impulse[1];
+            out[5 * i + 2] = j.weld_impulse[2];
+            out[5 * i + 3] = 0.0f;
+            out[5 * i + 4] = 0.0f;
+            continue;
+        }
         if (j.type == B2G_JOINT_DISTANCE) {
             out[5 * i + 0] = j.dist_impulse;
             out[5 * i + 1] = j.lower_impulse;

@@ -484,3 +484,43 @@ def test_distance_joints_lockstep(built):
         assert r["joint_impulses_equal"], r
     st = gpu.get_body_states()
     assert abs(float(np.linalg.norm(st["position"][1] + np.array([10.0, -10.0]) - [0.0, 0.0]) ) - 3.0) < 0.35
+
+
+def test_weld_joints_lockstep(built):
+    """Weld joints: a rigid cantilever of 8 welded boxes from a static wall, and a soft-welded
+    beam (angular spring, stiffness 30, damping 1) on a revolute hinge, with bodies dropped on both;
+    bodies, manifolds and joint impulses bit-exact every step."""
+    n, n_drop = 8, 10
+    nb = 1 + 2 * n + n_drop
+    bodies = b2g.body_defs(nb)
+    bodies["allow_sleep"] = 0
+    bodies[1:]["type"] = b2g.DYNAMIC
+    fx = [b2g.edge_fixture(0, (-30.0, 0.0), (30.0, 0.0))]
+    joints = []
+    for i in range(n):
+        a, b = 1 + i, 1 + n + i
+        bodies[a]["position"] = (-12.0 + 1.0 * i, 8.0)
+        bodies[b]["position"] = (3.0 + 1.0 * i, 8.0)
+        fx.append(b2g.box_fixture(a, 0.5, 0.125, density=5.0, friction=0.4))
+        fx.append(b2g.box_fixture(b, 0.5, 0.125, density=5.0, friction=0.4))
+        if i == 0:
+            joints.append(b2g.weld_joint(0, a, (-12.5, 8.0), (-0.5, 0.0)))
+            joints.append(b2g.revolute_joint(0, b, (2.5, 8.0), (-0.5, 0.0)))
+        else:
+            joints.append(b2g.weld_joint(a - 1, a, (0.5, 0.0), (-0.5, 0.0)))
+            joints.append(b2g.weld_joint(b - 1, b, (0.5, 0.0), (-0.5, 0.0), stiffness=30.0, damping=1.0))
+    rng = np.random.default_rng(37)
+    for k in range(n_drop):
+        b = 1 + 2 * n + k
+        bodies[b]["position"] = (rng.uniform(-12.0, 10.0), rng.uniform(10.0, 16.0))
+        fx.append(b2g.circle_fixture(b, 0.3, density=1.0, friction=0.4) if k % 2 else
+                  b2g.box_fixture(b, 0.3, 0.2, density=1.0, friction=0.4))
+    s = {"name": "weld", "bodies": bodies, "fixtures": np.concatenate(fx), "joints": np.concatenate(joints),
+         "gravity": (0.0, -10.0), "dt": np.float32(1.0 / 60.0), "vi": 8, "pi": 3, "steps": 200, "num_worlds": 1,
+         "allow_sleep": False, "n_dynamic": nb - 1}
+    recs, gpu, _ = parity.lockstep(s, 200)
+    for r in recs:
+        _assert_step(r)
+        assert r["joint_impulses_equal"], r
+    st = gpu.get_body_states()
+    assert float(st["position"][n, 1]) > 4.5  # the rigid cantilever holds up (welds sag a little)
