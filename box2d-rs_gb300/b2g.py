@@ -161,11 +161,25 @@ JOINT_DEF = np.dtype(
         ("max_length", "<f4"),
         ("stiffness", "<f4"),
         ("damping", "<f4"),
-        ("pad_", "<u4", (3,)),
+        ("max_force", "<f4"),
+        ("max_torque", "<f4"),
+        ("pad_", "<u4"),
     ]
 )
 JOINT_DISTANCE = 3
 JOINT_WELD = 8
+JOINT_FRICTION = 9
+
+
+def friction_joint(body_a, body_b, anchor_a, anchor_b, max_force, max_torque, collide_connected=False):
+    """B2frictionJointDef: top-down friction (linear and angular) between two bodies."""
+    d = np.zeros(1, JOINT_DEF)
+    d["type"] = JOINT_FRICTION
+    d["body_a"], d["body_b"] = body_a, body_b
+    d["collide_connected"] = int(bool(collide_connected))
+    d["local_anchor_a"], d["local_anchor_b"] = anchor_a, anchor_b
+    d["max_force"], d["max_torque"] = max_force, max_torque
+    return d
 
 
 def weld_joint(body_a, body_b, anchor_a, anchor_b, reference_angle=0.0, stiffness=0.0, damping=0.0,

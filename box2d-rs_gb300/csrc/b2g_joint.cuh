@@ -434,6 +434,103 @@ __device__ bool weld_solve_position(const DevWorld& w, int j) {
     return position_error <= kLinearSlop && angular_error <= kAngularSlop;
 }
 
+/* ---- friction joint (B2frictionJoint, private/dynamics/joints/b2_friction_joint.rs) ----
+ * j_lim = (max force, max torque, -, -), j_imp = (linear x, y, angular, -); the step's linear mass
+ * (B2Mat22::get_inverse of K) in j_k (ex.x, ex.y, ey.x, ey.y), angular mass in j_s.x. No position
+ * correction. */
+
+__device__ void friction_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 an = w.j_anchor[j];
+    const float4 massA = w.b_mass[bd.x], massB = w.b_mass[bd.y];
+    const float2 lcA = w.b_lc[bd.x], lcB = w.b_lc[bd.y];
+    const float mA = massA.y, mB = massB.y, iA = massA.w, iB = massB.w;
+    const float aA = w.b_pos[bd.x].z, aB = w.b_pos[bd.y].z;
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = rot(aA), qB = rot(aB);
+    const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+    const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+    const float kxx = mA + mB + iA * rA.y * rA.y + iB * rB.y * rB.y;
+    const float kxy = -iA * rA.x * rA.y - iB * rB.x * rB.y;
+    const float kyy = mA + mB + iA * rA.x * rA.x + iB * rB.x * rB.x;
+    /* B2Mat22::get_inverse, src/b2_math.rs:261-276 (a = ex.x, b = ey.x, c = ex.y, d = ey.y) */
+    float det = kxx * kyy - kxy * kxy;
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    const float4 lm = make_float4(det * kyy, -det * kxy, -det * kxy, det * kxx);  /* ex.x, ex.y, ey.x, ey.y */
+    float angular_mass = iA + iB;
+    if (angular_mass > 0.0f) angular_mass = fdiv(1.0f, angular_mass);
+    float4 imp = w.j_imp[j];
+    if (sp.warm) {
+        imp.x *= sp.dt_ratio;
+        imp.y *= sp.dt_ratio;
+        imp.z *= sp.dt_ratio;
+        const V2 P = mk(imp.x, imp.y);
+        vA = sub(vA, scale(mA, P));
+        wA -= iA * (cross(rA, P) + imp.z);
+        vB = add(vB, scale(mB, P));
+        wB += iB * (cross(rB, P) + imp.z);
+    } else {
+        imp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    w.j_imp[j] = imp;
+    w.j_rr[j] = make_float4(rA.x, rA.y, rB.x, rB.y);
+    w.j_k[j] = lm;
+    w.j_m[j] = make_float4(mA, mB, iA, iB);
+    w.j_s[j] = make_float2(angular_mass, 0.0f);
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+__device__ void friction_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 lim = w.j_lim[j];
+    const float4 m = w.j_m[j];
+    const float mA = m.x, mB = m.y, iA = m.z, iB = m.w;
+    const float4 rr = w.j_rr[j];
+    const V2 rA = mk(rr.x, rr.y), rB = mk(rr.z, rr.w);
+    const float4 lm = w.j_k[j];
+    const float angular_mass = w.j_s[j].x;
+    float4 imp = w.j_imp[j];
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const float h = sp.dt;
+    {
+        const float cdot = wB - wA;
+        float impulse = -angular_mass * cdot;
+        const float old_impulse = imp.z;
+        const float max_impulse = h * lim.y;
+        imp.z = fclampr(imp.z + impulse, -max_impulse, max_impulse);
+        impulse = imp.z - old_impulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    {
+        const V2 cdot = sub(sub(add(vB, cross_sv(wB, rB)), vA), cross_sv(wA, rA));
+        V2 impulse = neg(mk(lm.x * cdot.x + lm.z * cdot.y, lm.y * cdot.x + lm.w * cdot.y));
+        const V2 old_impulse = mk(imp.x, imp.y);
+        V2 li = add(old_impulse, impulse);
+        const float max_impulse = h * lim.x;
+        if (dot(li, li) > max_impulse * max_impulse) {
+            normalize(li);
+            li.x *= max_impulse;
+            li.y *= max_impulse;
+        }
+        impulse = sub(li, old_impulse);
+        imp.x = li.x;
+        imp.y = li.y;
+        vA = sub(vA, scale(mA, impulse));
+        wA -= iA * cross(rA, impulse);
+        vB = add(vB, scale(mB, impulse));
+        wB += iB * cross(rB, impulse);
+    }
+    w.j_imp[j] = imp;
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
 __device__ __forceinline__ uint32_t joint_type(const DevWorld& w, int j) {
     return (__float_as_uint(w.j_par[j].y) >> JF_TYPE_SHIFT) & 0xffu;
 }
@@ -629,18 +726,21 @@ __device__ __forceinline__ void joint_init_velocity(const DevWorld& w, const Ste
     const uint32_t t = joint_type(w, j);
     if (t == B2G_JOINT_DISTANCE) distance_init_velocity(w, sp, j);
     else if (t == B2G_JOINT_WELD) weld_init_velocity(w, sp, j);
+    else if (t == B2G_JOINT_FRICTION) friction_init_velocity(w, sp, j);
     else revolute_init_velocity(w, sp, j);
 }
 __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
     const uint32_t t = joint_type(w, j);
     if (t == B2G_JOINT_DISTANCE) distance_solve_velocity(w, sp, j);
     else if (t == B2G_JOINT_WELD) weld_solve_velocity(w, j);
+    else if (t == B2G_JOINT_FRICTION) friction_solve_velocity(w, sp, j);
     else revolute_solve_velocity(w, sp, j);
 }
 __device__ __forceinline__ bool joint_solve_position(const DevWorld& w, int j) {
     const uint32_t t = joint_type(w, j);
     if (t == B2G_JOINT_DISTANCE) return distance_solve_position(w, j);
     if (t == B2G_JOINT_WELD) return weld_solve_position(w, j);
+    if (t == B2G_JOINT_FRICTION) return true;
     return revolute_solve_position(w, j);
 }
 

@@ -117,10 +117,12 @@ typedef struct b2g_fixture_def {
  *   B2G_JOINT_DISTANCE: B2distanceJointDef (src/joints/b2_distance_joint.rs): rest length, min and
  *     max length, stiffness and damping (a spring when stiffness > 0 and min < max)
  *   B2G_JOINT_WELD: B2weldJointDef (src/joints/b2_weld_joint.rs): reference angle, stiffness and
- *     damping (an angular spring when stiffness > 0) */
+ *     damping (an angular spring when stiffness > 0)
+ *   B2G_JOINT_FRICTION: B2frictionJointDef (src/joints/b2_friction_joint.rs): max force, max torque */
 #define B2G_JOINT_REVOLUTE 1
 #define B2G_JOINT_DISTANCE 3
 #define B2G_JOINT_WELD 8
+#define B2G_JOINT_FRICTION 9
 typedef struct b2g_joint_def {
     int32_t type;              /* B2G_JOINT_* */
     uint32_t body_a, body_b;
@@ -132,7 +134,8 @@ typedef struct b2g_joint_def {
     int32_t enable_motor;
     float motor_speed, max_motor_torque;
     float length, min_length, max_length, stiffness, damping;
-    uint32_t pad_[3];
+    float max_force, max_torque;
+    uint32_t pad_;
 } b2g_joint_def;
 
 /* Body state read back after a step (B2body getters, src/b2_body.rs:650-680). */
@@ -191,7 +194,7 @@ int b2g_create_fixtures(void* world, const b2g_fixture_def* defs, int32_t n, uin
  * A world with joints runs the grid-wide colour schedule (no part-local solve) and cannot be taped. */
 int b2g_create_joints(void* world, const b2g_joint_def* defs, int32_t n, uint32_t* out_ids);
 /* Accumulated joint impulses (for warm starting), 5 per joint: revolute x, y, motor, lower, upper;
- * distance impulse, lower, upper, 0, 0; weld x, y, angular, 0, 0 */
+ * distance impulse, lower, upper, 0, 0; weld x, y, angular, 0, 0; friction x, y, angular, 0, 0 */
 int b2g_get_joint_impulses(void* world, uint32_t first, uint32_t count, float* out);
 /* The order the GPU solves joints in (ids, colour by colour): the oracle's joint ordering hook */
 int b2g_get_joint_order(void* world, uint32_t* out, int32_t cap, int32_t* n);

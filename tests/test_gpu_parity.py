@@ -524,3 +524,39 @@ def test_weld_joints_lockstep(built):
         assert r["joint_impulses_equal"], r
     st = gpu.get_body_states()
     assert float(st["position"][n, 1]) > 4.5  # the rigid cantilever holds up (welds sag a little)
+
+
+def test_friction_joints_lockstep(built):
+    """Friction joints (top-down friction): boxes and circles sliding and spinning over a static
+    body with no gravity are slowed by friction joints to it, one pair drags each other through a
+    friction joint, and they collide with each other and the walls; bit-exact every step."""
+    n = 16
+    bodies = b2g.body_defs(n + 1)
+    bodies["allow_sleep"] = 0
+    bodies[1:]["type"] = b2g.DYNAMIC
+    rng = np.random.default_rng(41)
+    bodies[1:]["position"][:, 0] = rng.uniform(-8.0, 8.0, n)
+    bodies[1:]["position"][:, 1] = rng.uniform(-8.0, 8.0, n)
+    bodies[1:]["linear_velocity"][:, 0] = rng.uniform(-6.0, 6.0, n)
+    bodies[1:]["linear_velocity"][:, 1] = rng.uniform(-6.0, 6.0, n)
+    bodies[1:]["angular_velocity"] = rng.uniform(-4.0, 4.0, n)
+    corners = [(-10.0, -10.0), (10.0, -10.0), (10.0, 10.0), (-10.0, 10.0)]
+    fx = [b2g.edge_fixture(0, corners[i], corners[(i + 1) % 4]) for i in range(4)]
+    joints = []
+    for i in range(n):
+        b = i + 1
+        fx.append(b2g.box_fixture(b, 0.5, 0.3, density=1.0, friction=0.3) if i % 2 else
+                  b2g.circle_fixture(b, 0.4, density=1.0, friction=0.3))
+        if i < n - 2:
+            joints.append(b2g.friction_joint(0, b, (0.0, 0.0), (0.0, 0.0), max_force=2.0, max_torque=0.5,
+                                             collide_connected=True))
+    joints.append(b2g.friction_joint(n - 1, n, (0.0, 0.0), (0.0, 0.0), max_force=4.0, max_torque=1.0))
+    s = {"name": "friction", "bodies": bodies, "fixtures": np.concatenate(fx), "joints": np.concatenate(joints),
+         "gravity": (0.0, 0.0), "dt": np.float32(1.0 / 60.0), "vi": 8, "pi": 3, "steps": 240, "num_worlds": 1,
+         "allow_sleep": False, "n_dynamic": n}
+    recs, gpu, _ = parity.lockstep(s, 240)
+    for r in recs:
+        _assert_step(r)
+        assert r["joint_impulses_equal"], r
+    v = gpu.get_body_states()["linear_velocity"][1:n - 1]
+    assert float(np.abs(v).max()) < 1.0  # friction stopped them
