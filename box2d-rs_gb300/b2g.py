@@ -163,12 +163,15 @@ JOINT_DEF = np.dtype(
         ("damping", "<f4"),
         ("max_force", "<f4"),
         ("max_torque", "<f4"),
-        ("pad_", "<u4"),
+        ("correction_factor", "<f4"),
+        ("angular_offset", "<f4"),
+        ("linear_offset", "<f4", (2,)),
     ]
 )
 JOINT_DISTANCE = 3
 JOINT_WELD = 8
 JOINT_FRICTION = 9
+JOINT_MOTOR = 11
 
 
 def friction_joint(body_a, body_b, anchor_a, anchor_b, max_force, max_torque, collide_connected=False):
@@ -179,6 +182,19 @@ def friction_joint(body_a, body_b, anchor_a, anchor_b, max_force, max_torque, co
     d["collide_connected"] = int(bool(collide_connected))
     d["local_anchor_a"], d["local_anchor_b"] = anchor_a, anchor_b
     d["max_force"], d["max_torque"] = max_force, max_torque
+    return d
+
+
+def motor_joint(body_a, body_b, linear_offset=(0.0, 0.0), angular_offset=0.0, max_force=1.0, max_torque=1.0,
+                correction_factor=0.3, collide_connected=False):
+    """B2motorJointDef: drives body B to body A's position plus linear_offset (in A's frame) and A's
+    angle plus angular_offset, with bounded force and torque."""
+    d = np.zeros(1, JOINT_DEF)
+    d["type"] = JOINT_MOTOR
+    d["body_a"], d["body_b"] = body_a, body_b
+    d["collide_connected"] = int(bool(collide_connected))
+    d["linear_offset"], d["angular_offset"] = linear_offset, angular_offset
+    d["max_force"], d["max_torque"], d["correction_factor"] = max_force, max_torque, correction_factor
     return d
 
 

@@ -745,7 +745,11 @@ int upload_joints(World* w) {
             jb[j] = make_int2((int)jd.body_a, (int)jd.body_b);
             an[j] = make_float4(jd.local_anchor_a.x, jd.local_anchor_a.y, jd.local_anchor_b.x, jd.local_anchor_b.y);
             uint32_t fl = ((uint32_t)jd.type << JF_TYPE_SHIFT) | (jd.collide_connected ? JF_COLLIDE : 0u);
-            if (jd.type == B2G_JOINT_FRICTION) {
+            if (jd.type == B2G_JOINT_MOTOR) {
+                an[j] = make_float4(jd.linear_offset.x, jd.linear_offset.y, 0.0f, 0.0f);
+                lim[j] = make_float4(jd.max_force, jd.max_torque, jd.correction_factor, jd.angular_offset);
+                par[j] = make_float4(0.0f, __uint_as_float_host(fl), 0.0f, 0.0f);
+            } else if (jd.type == B2G_JOINT_FRICTION) {
                 lim[j] = make_float4(jd.max_force, jd.max_torque, 0.0f, 0.0f);
                 par[j] = make_float4(0.0f, __uint_as_float_host(fl), 0.0f, 0.0f);
             } else if (jd.type == B2G_JOINT_WELD) {
@@ -1347,8 +1351,9 @@ int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* i
     for (int i = 0; i < n; ++i) {
         const b2g_joint_def& d = defs[i];
         if (d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE && d.type != B2G_JOINT_WELD &&
-            d.type != B2G_JOINT_FRICTION)
-            return fail(w, B2G_ERR_UNSUPPORTED, "only revolute, distance, weld and friction joints are on the GPU path");
+            d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR)
+            return fail(w, B2G_ERR_UNSUPPORTED,
+                        "only revolute, distance, weld, friction and motor joints are on the GPU path");
         if (d.body_a >= w->h_flags.size() || d.body_b >= w->h_flags.size() || d.body_a == d.body_b)
             return fail(w, B2G_ERR_INVALID_ARG, "joint body ids out of range or equal");
     }

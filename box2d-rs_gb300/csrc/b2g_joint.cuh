@@ -531,6 +531,110 @@ __device__ void friction_solve_velocity(const DevWorld& w, const StepParams& sp,
     if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
 }
 
+/* ---- motor joint (B2motorJoint, private/dynamics/joints/b2_motor_joint.rs) ----
+ * j_anchor = (linear offset x, y, -, -), j_lim = (max force, max torque, correction factor, angular
+ * offset), j_imp = (linear x, y, angular, -); the step's linear mass (B2Mat22::get_inverse of K) in
+ * j_k, (angular mass, angular error) in j_s, linear error in j_x.xy. No position correction. */
+
+__device__ void motor_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 an = w.j_anchor[j];
+    const float4 lim = w.j_lim[j];
+    const float4 massA = w.b_mass[bd.x], massB = w.b_mass[bd.y];
+    const float2 lcA = w.b_lc[bd.x], lcB = w.b_lc[bd.y];
+    const float mA = massA.y, mB = massB.y, iA = massA.w, iB = massB.w;
+    const float4 pa = w.b_pos[bd.x], pb = w.b_pos[bd.y];
+    const float aA = pa.z, aB = pb.z;
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = rot(aA), qB = rot(aB);
+    const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+    const V2 rB = mul(qB, mk(-lcB.x, -lcB.y));
+    const float kxx = mA + mB + iA * rA.y * rA.y + iB * rB.y * rB.y;
+    const float kxy = -iA * rA.x * rA.y - iB * rB.x * rB.y;
+    const float kyy = mA + mB + iA * rA.x * rA.x + iB * rB.x * rB.x;
+    float det = kxx * kyy - kxy * kxy;
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    const float4 lm = make_float4(det * kyy, -det * kxy, -det * kxy, det * kxx);  /* ex.x, ex.y, ey.x, ey.y */
+    float angular_mass = iA + iB;
+    if (angular_mass > 0.0f) angular_mass = fdiv(1.0f, angular_mass);
+    const V2 linear_error = sub(sub(add(mk(pb.x, pb.y), rB), mk(pa.x, pa.y)), rA);
+    const float angular_error = aB - aA - lim.w;
+    float4 imp = w.j_imp[j];
+    if (sp.warm) {
+        imp.x *= sp.dt_ratio;
+        imp.y *= sp.dt_ratio;
+        imp.z *= sp.dt_ratio;
+        const V2 P = mk(imp.x, imp.y);
+        vA = sub(vA, scale(mA, P));
+        wA -= iA * (cross(rA, P) + imp.z);
+        vB = add(vB, scale(mB, P));
+        wB += iB * (cross(rB, P) + imp.z);
+    } else {
+        imp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    w.j_imp[j] = imp;
+    w.j_rr[j] = make_float4(rA.x, rA.y, rB.x, rB.y);
+    w.j_k[j] = lm;
+    w.j_m[j] = make_float4(mA, mB, iA, iB);
+    w.j_s[j] = make_float2(angular_mass, angular_error);
+    w.j_x[j] = make_float4(linear_error.x, linear_error.y, 0.0f, 0.0f);
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+__device__ void motor_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 lim = w.j_lim[j];
+    const float4 m = w.j_m[j];
+    const float mA = m.x, mB = m.y, iA = m.z, iB = m.w;
+    const float4 rr = w.j_rr[j];
+    const V2 rA = mk(rr.x, rr.y), rB = mk(rr.z, rr.w);
+    const float4 lm = w.j_k[j];
+    const float2 as = w.j_s[j];
+    const float4 le = w.j_x[j];
+    const float cf = lim.z;
+    float4 imp = w.j_imp[j];
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const float h = sp.dt, inv_h = sp.inv_dt;
+    {
+        const float cdot = wB - wA + inv_h * cf * as.y;
+        float impulse = -as.x * cdot;
+        const float old_impulse = imp.z;
+        const float max_impulse = h * lim.y;
+        imp.z = fclampr(imp.z + impulse, -max_impulse, max_impulse);
+        impulse = imp.z - old_impulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    {
+        const float s = inv_h * cf;
+        const V2 cdot = add(sub(sub(add(vB, cross_sv(wB, rB)), vA), cross_sv(wA, rA)), mk(s * le.x, s * le.y));
+        V2 impulse = neg(mk(lm.x * cdot.x + lm.z * cdot.y, lm.y * cdot.x + lm.w * cdot.y));
+        const V2 old_impulse = mk(imp.x, imp.y);
+        V2 li = add(old_impulse, impulse);
+        const float max_impulse = h * lim.x;
+        if (dot(li, li) > max_impulse * max_impulse) {
+            normalize(li);
+            li.x *= max_impulse;
+            li.y *= max_impulse;
+        }
+        impulse = sub(li, old_impulse);
+        imp.x = li.x;
+        imp.y = li.y;
+        vA = sub(vA, scale(mA, impulse));
+        wA -= iA * cross(rA, impulse);
+        vB = add(vB, scale(mB, impulse));
+        wB += iB * cross(rB, impulse);
+    }
+    w.j_imp[j] = imp;
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
 __device__ __forceinline__ uint32_t joint_type(const DevWorld& w, int j) {
     return (__float_as_uint(w.j_par[j].y) >> JF_TYPE_SHIFT) & 0xffu;
 }
@@ -727,6 +831,7 @@ __device__ __forceinline__ void joint_init_velocity(const DevWorld& w, const Ste
     if (t == B2G_JOINT_DISTANCE) distance_init_velocity(w, sp, j);
     else if (t == B2G_JOINT_WELD) weld_init_velocity(w, sp, j);
     else if (t == B2G_JOINT_FRICTION) friction_init_velocity(w, sp, j);
+    else if (t == B2G_JOINT_MOTOR) motor_init_velocity(w, sp, j);
     else revolute_init_velocity(w, sp, j);
 }
 __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
@@ -734,13 +839,14 @@ __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const St
     if (t == B2G_JOINT_DISTANCE) distance_solve_velocity(w, sp, j);
     else if (t == B2G_JOINT_WELD) weld_solve_velocity(w, j);
     else if (t == B2G_JOINT_FRICTION) friction_solve_velocity(w, sp, j);
+    else if (t == B2G_JOINT_MOTOR) motor_solve_velocity(w, sp, j);
     else revolute_solve_velocity(w, sp, j);
 }
 __device__ __forceinline__ bool joint_solve_position(const DevWorld& w, int j) {
     const uint32_t t = joint_type(w, j);
     if (t == B2G_JOINT_DISTANCE) return distance_solve_position(w, j);
     if (t == B2G_JOINT_WELD) return weld_solve_position(w, j);
-    if (t == B2G_JOINT_FRICTION) return true;
+    if (t == B2G_JOINT_FRICTION || t == B2G_JOINT_MOTOR) return true;
     return revolute_solve_position(w, j);
 }
 

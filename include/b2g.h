@@ -118,11 +118,15 @@ typedef struct b2g_fixture_def {
  *     max length, stiffness and damping (a spring when stiffness > 0 and min < max)
  *   B2G_JOINT_WELD: B2weldJointDef (src/joints/b2_weld_joint.rs): reference angle, stiffness and
  *     damping (an angular spring when stiffness > 0)
- *   B2G_JOINT_FRICTION: B2frictionJointDef (src/joints/b2_friction_joint.rs): max force, max torque */
+ *   B2G_JOINT_FRICTION: B2frictionJointDef (src/joints/b2_friction_joint.rs): max force, max torque
+ *   B2G_JOINT_MOTOR: B2motorJointDef (src/joints/b2_motor_joint.rs): linear offset (in body A's frame),
+ *     angular offset, max force, max torque, correction factor (the anchors are not used)
+ * The type numbers follow Box2D's C++ b2JointType. */
 #define B2G_JOINT_REVOLUTE 1
 #define B2G_JOINT_DISTANCE 3
 #define B2G_JOINT_WELD 8
 #define B2G_JOINT_FRICTION 9
+#define B2G_JOINT_MOTOR 11
 typedef struct b2g_joint_def {
     int32_t type;              /* B2G_JOINT_* */
     uint32_t body_a, body_b;
@@ -135,7 +139,8 @@ typedef struct b2g_joint_def {
     float motor_speed, max_motor_torque;
     float length, min_length, max_length, stiffness, damping;
     float max_force, max_torque;
-    uint32_t pad_;
+    float correction_factor, angular_offset;
+    b2g_vec2 linear_offset;
 } b2g_joint_def;
 
 /* Body state read back after a step (B2body getters, src/b2_body.rs:650-680). */

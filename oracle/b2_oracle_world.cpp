@@ -107,6 +107,10 @@ struct Joint {
     float max_force = 0, max_torque = 0, angular_impulse = 0, angular_mass = 0;
     Vec2 linear_impulse{0, 0};
     Mat22 linear_mass{};
+    /* B2motorJoint (private/dynamics/joints/b2_motor_joint.rs): shares max_force, max_torque, the
+     * linear and angular impulses and masses with the friction joint */
+    Vec2 linear_offset{0, 0}, linear_error{0, 0};
+    float angular_offset = 0, correction_factor = 0, angular_error = 0;
     float weld_mass[9] = {0};  /* ex, ey, ez columns */
     bool collide_connected = false, island_flag = false;
     Vec2 local_anchor_a{0, 0}, local_anchor_b{0, 0};
@@ -1396,8 +1400,103 @@ static void friction_solve_velocity(World& w, Joint& j, const Step& step) {
     w.vel[j.index_b].w = wB;
 }
 
+/* ---- motor joint, private/dynamics/joints/b2_motor_joint.rs ---- */
+
+static void motor_init_velocity(World& w, Joint& j, const Step& step) {
+    const Body& A = w.bodies[j.body_a];
+    const Body& B = w.bodies[j.body_b];
+    j.index_a = A.island_index;
+    j.index_b = B.island_index;
+    j.lc_a = A.sweep.local_center;
+    j.lc_b = B.sweep.local_center;
+    j.inv_mass_a = A.inv_mass;
+    j.inv_mass_b = B.inv_mass;
+    j.inv_ia = A.inv_I;
+    j.inv_ib = B.inv_I;
+    const Vec2 cA = w.pos[j.index_a].c, cB = w.pos[j.index_b].c;
+    const float aA = w.pos[j.index_a].a, aB = w.pos[j.index_b].a;
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const Rot qA = rot(aA), qB = rot(aB);
+    j.r_a = mul(qA, j.linear_offset - j.lc_a);
+    j.r_b = mul(qB, -j.lc_b);
+    const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+    Mat22 K;
+    K.ex.x = mA + mB + iA * j.r_a.y * j.r_a.y + iB * j.r_b.y * j.r_b.y;
+    K.ex.y = -iA * j.r_a.x * j.r_a.y - iB * j.r_b.x * j.r_b.y;
+    K.ey.x = K.ex.y;
+    K.ey.y = mA + mB + iA * j.r_a.x * j.r_a.x + iB * j.r_b.x * j.r_b.x;
+    j.linear_mass = inverse(K);
+    j.angular_mass = iA + iB;
+    if (j.angular_mass > 0.0f) j.angular_mass = 1.0f / j.angular_mass;
+    j.linear_error = cB + j.r_b - cA - j.r_a;
+    j.angular_error = aB - aA - j.angular_offset;
+    if (step.warm) {
+        j.linear_impulse *= step.dt_ratio;
+        j.angular_impulse *= step.dt_ratio;
+        const Vec2 P = v2(j.linear_impulse.x, j.linear_impulse.y);
+        vA -= mA * P;
+        wA -= iA * (cross(j.r_a, P) + j.angular_impulse);
+        vB += mB * P;
+        wB += iB * (cross(j.r_b, P) + j.angular_impulse);
+    } else {
+        j.linear_impulse = v2(0, 0);
+        j.angular_impulse = 0.0f;
+    }
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+static void motor_solve_velocity(World& w, Joint& j, const Step& step) {
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+    const float h = step.dt, inv_h = step.inv_dt;
+    {
+        const float cdot = wB - wA + inv_h * j.correction_factor * j.angular_error;
+        float impulse = -j.angular_mass * cdot;
+        const float old_impulse = j.angular_impulse;
+        const float max_impulse = h * j.max_torque;
+        j.angular_impulse = bclamp(j.angular_impulse + impulse, -max_impulse, max_impulse);
+        impulse = j.angular_impulse - old_impulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    {
+        const Vec2 cdot = vB + cross_sv(wB, j.r_b) - vA - cross_sv(wA, j.r_a) +
+                          (inv_h * j.correction_factor) * j.linear_error;
+        Vec2 impulse = -mul(j.linear_mass, cdot);
+        const Vec2 old_impulse = j.linear_impulse;
+        j.linear_impulse += impulse;
+        const float max_impulse = h * j.max_force;
+        if (dot(j.linear_impulse, j.linear_impulse) > max_impulse * max_impulse) {
+            normalize(j.linear_impulse);
+            j.linear_impulse *= max_impulse;
+        }
+        impulse = j.linear_impulse - old_impulse;
+        vA -= mA * impulse;
+        wA -= iA * cross(j.r_a, impulse);
+        vB += mB * impulse;
+        wB += iB * cross(j.r_b, impulse);
+    }
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
 /* init_velocity_constraints (:21-116): anchors, effective masses, warm start */
 static void joint_init_velocity(World& w, Joint& j, const Step& step) {
+    if (j.type == B2G_JOINT_MOTOR) {
+        motor_init_velocity(w, j, step);
+        return;
+    }
     if (j.type == B2G_JOINT_FRICTION) {
         friction_init_velocity(w, j, step);
         return;
@@ -1473,6 +1572,10 @@ static void joint_init_velocity(World& w, Joint& j, const Step& step) {
 
 /* solve_velocity_constraints (:118-208): motor, lower and upper limits, point */
 static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
+    if (j.type == B2G_JOINT_MOTOR) {
+        motor_solve_velocity(w, j, step);
+        return;
+    }
     if (j.type == B2G_JOINT_FRICTION) {
         friction_solve_velocity(w, j, step);
         return;
@@ -1543,7 +1646,8 @@ static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
 static bool joint_solve_position(World& w, Joint& j) {
     if (j.type == B2G_JOINT_DISTANCE) return distance_solve_position(w, j);
     if (j.type == B2G_JOINT_WELD) return weld_solve_position(w, j);
-    if (j.type == B2G_JOINT_FRICTION) return true;  /* b2_friction_joint.rs: no position correction */
+    /* b2_friction_joint.rs and b2_motor_joint.rs: no position correction */
+    if (j.type == B2G_JOINT_FRICTION || j.type == B2G_JOINT_MOTOR) return true;
     Vec2 cA = w.pos[j.index_a].c;
     float aA = w.pos[j.index_a].a;
     Vec2 cB = w.pos[j.index_b].c;
@@ -2336,7 +2440,7 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
     for (int i = 0; i < n; ++i) {
         const b2g_joint_def& d = defs[i];
         if ((d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE && d.type != B2G_JOINT_WELD &&
-             d.type != B2G_JOINT_FRICTION) ||
+             d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR) ||
             d.body_a >= w.bodies.size() ||
             d.body_b >= w.bodies.size())
             return -1;
@@ -2351,6 +2455,9 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
         j.damping = d.damping;
         j.max_force = d.max_force;
         j.max_torque = d.max_torque;
+        j.linear_offset = v2(d.linear_offset.x, d.linear_offset.y);
+        j.angular_offset = d.angular_offset;
+        j.correction_factor = d.correction_factor;
         j.body_a = (int)d.body_a;
         j.body_b = (int)d.body_b;
         j.collide_connected = d.collide_connected != 0;
@@ -2386,7 +2493,7 @@ int ora_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) 
     if ((size_t)first + count > w.joints.size()) return -1;
     for (uint32_t i = 0; i < count; ++i) {
         const Joint& j = w.joints[first + i];
-        if (j.type == B2G_JOINT_FRICTION) {
+        if (j.type == B2G_JOINT_FRICTION || j.type == B2G_JOINT_MOTOR) {
             out[5 * i + 0] = j.linear_impulse.x;
             out[5 * i + 1] = j.linear_impulse.y;
             out[5 * i + 2] = j.angular_impulse;

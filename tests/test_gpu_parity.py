@@ -560,3 +560,39 @@ def test_friction_joints_lockstep(built):
         assert r["joint_impulses_equal"], r
     v = gpu.get_body_states()["linear_velocity"][1:n - 1]
     assert float(np.abs(v).max()) < 1.0  # friction stopped them
+
+
+@pytest.mark.gpu
+def test_motor_joints_lockstep(built):
+    """Motor joints: boxes hanging under gravity are driven by motor joints to offsets from a static
+    body and to angles, two dynamic bodies are held apart by a motor joint between them, and the
+    driven boxes collide with each other on the way; bit-exact every step."""
+    n = 12
+    bodies = b2g.body_defs(n + 1)
+    bodies["allow_sleep"] = 0
+    bodies[1:]["type"] = b2g.DYNAMIC
+    rng = np.random.default_rng(43)
+    bodies[1:]["position"][:, 0] = rng.uniform(-6.0, 6.0, n)
+    bodies[1:]["position"][:, 1] = rng.uniform(1.0, 8.0, n)
+    bodies[1:]["angle"] = rng.uniform(-1.0, 1.0, n)
+    fx = [b2g.edge_fixture(0, (-20.0, 0.0), (20.0, 0.0))]
+    joints = []
+    for i in range(n):
+        b = i + 1
+        fx.append(b2g.box_fixture(b, 0.5, 0.3, center=(0.1, 0.0), density=1.0, friction=0.3) if i % 2 else
+                  b2g.circle_fixture(b, 0.4, density=1.0, friction=0.3))
+        if i < n - 2:
+            joints.append(b2g.motor_joint(0, b, linear_offset=(-5.0 + i, 4.0), angular_offset=0.25 * i,
+                                          max_force=float(60 + 10 * i), max_torque=float(5 + i),
+                                          correction_factor=0.2 + 0.05 * i))
+    joints.append(b2g.motor_joint(n - 1, n, linear_offset=(1.5, 0.5), angular_offset=0.5, max_force=40.0,
+                                  max_torque=10.0, collide_connected=True))
+    s = {"name": "motor", "bodies": bodies, "fixtures": np.concatenate(fx), "joints": np.concatenate(joints),
+         "gravity": (0.0, -10.0), "dt": np.float32(1.0 / 60.0), "vi": 8, "pi": 3, "steps": 240, "num_worlds": 1,
+         "allow_sleep": False, "n_dynamic": n}
+    recs, gpu, _ = parity.lockstep(s, 240)
+    for r in recs:
+        _assert_step(r)
+        assert r["joint_impulses_equal"], r
+    st = gpu.get_body_states()
+    assert abs(float(st["position"][1, 0]) + 5.0) < 0.2 and abs(float(st["position"][1, 1]) - 4.0) < 0.2
