@@ -166,12 +166,14 @@ JOINT_DEF = np.dtype(
         ("correction_factor", "<f4"),
         ("angular_offset", "<f4"),
         ("linear_offset", "<f4", (2,)),
+        ("target", "<f4", (2,)),
     ]
 )
 JOINT_DISTANCE = 3
 JOINT_WELD = 8
 JOINT_FRICTION = 9
 JOINT_MOTOR = 11
+JOINT_MOUSE = 5
 
 
 def friction_joint(body_a, body_b, anchor_a, anchor_b, max_force, max_torque, collide_connected=False):
@@ -195,6 +197,18 @@ def motor_joint(body_a, body_b, linear_offset=(0.0, 0.0), angular_offset=0.0, ma
     d["collide_connected"] = int(bool(collide_connected))
     d["linear_offset"], d["angular_offset"] = linear_offset, angular_offset
     d["max_force"], d["max_torque"], d["correction_factor"] = max_force, max_torque, correction_factor
+    return d
+
+
+def mouse_joint(body_a, body_b, target, max_force, stiffness=0.0, damping=0.0, collide_connected=False):
+    """B2mouseJointDef: pulls body B's point under `target` (world) towards the target; body A only ties
+    the joint into the world."""
+    d = np.zeros(1, JOINT_DEF)
+    d["type"] = JOINT_MOUSE
+    d["body_a"], d["body_b"] = body_a, body_b
+    d["collide_connected"] = int(bool(collide_connected))
+    d["target"] = target
+    d["max_force"], d["stiffness"], d["damping"] = max_force, stiffness, damping
     return d
 
 
@@ -503,6 +517,7 @@ def load_library(path=LIB_PATH):
         "b2g_set_toi_schedule": [vp, i32],
         "b2g_get_awake": [vp, u32, u32, vp],
         "b2g_create_joints": [vp, vp, i32, vp],
+        "b2g_set_mouse_target": [vp, u32, Vec2],
         "b2g_get_joint_impulses": [vp, u32, u32, vp],
         "b2g_get_joint_order": [vp, vp, i32, ctypes.POINTER(ctypes.c_int32)],
         "b2g_state_size": [vp, ctypes.POINTER(ctypes.c_uint64)],
@@ -799,6 +814,9 @@ class B2world:
         if n:
             self._check(self._lib.b2g_get_joint_impulses(self._h, 0, n, out.ctypes.data_as(ctypes.c_void_p)))
         return out
+
+    def set_mouse_target(self, joint, target):
+        self._check(self._lib.b2g_set_mouse_target(self._h, joint, Vec2(*target)))
 
     def get_joint_order(self):
         n = getattr(self, "joint_count", 0)

@@ -745,7 +745,11 @@ int upload_joints(World* w) {
             jb[j] = make_int2((int)jd.body_a, (int)jd.body_b);
             an[j] = make_float4(jd.local_anchor_a.x, jd.local_anchor_a.y, jd.local_anchor_b.x, jd.local_anchor_b.y);
             uint32_t fl = ((uint32_t)jd.type << JF_TYPE_SHIFT) | (jd.collide_connected ? JF_COLLIDE : 0u);
-            if (jd.type == B2G_JOINT_MOTOR) {
+            if (jd.type == B2G_JOINT_MOUSE) {
+                an[j] = make_float4(jd.target.x, jd.target.y, jd.local_anchor_b.x, jd.local_anchor_b.y);
+                lim[j] = make_float4(jd.max_force, jd.stiffness, jd.damping, 0.0f);
+                par[j] = make_float4(0.0f, __uint_as_float_host(fl), 0.0f, 0.0f);
+            } else if (jd.type == B2G_JOINT_MOTOR) {
                 an[j] = make_float4(jd.linear_offset.x, jd.linear_offset.y, 0.0f, 0.0f);
                 lim[j] = make_float4(jd.max_force, jd.max_torque, jd.correction_factor, jd.angular_offset);
                 par[j] = make_float4(0.0f, __uint_as_float_host(fl), 0.0f, 0.0f);
@@ -1351,9 +1355,9 @@ int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* i
     for (int i = 0; i < n; ++i) {
         const b2g_joint_def& d = defs[i];
         if (d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE && d.type != B2G_JOINT_WELD &&
-            d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR)
+            d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR && d.type != B2G_JOINT_MOUSE)
             return fail(w, B2G_ERR_UNSUPPORTED,
-                        "only revolute, distance, weld, friction and motor joints are on the GPU path");
+                        "only revolute, distance, weld, friction, motor and mouse joints are on the GPU path");
         if (d.body_a >= w->h_flags.size() || d.body_b >= w->h_flags.size() || d.body_a == d.body_b)
             return fail(w, B2G_ERR_INVALID_ARG, "joint body ids out of range or equal");
     }
@@ -1361,10 +1365,18 @@ int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* i
     if (w->device_authoritative) {
         int rc = download_joint_impulses(w);
         if (rc != B2G_OK) return rc;
+        for (int i = 0; i < n && rc == B2G_OK; ++i)
+            if (defs[i].type == B2G_JOINT_MOUSE) rc = download_state(w);  /* body B's transform */
+        if (rc != B2G_OK) return rc;
     }
     for (int i = 0; i < n; ++i) {
         if (ids) ids[i] = (uint32_t)w->joints.size();
         w->joints.push_back(defs[i]);
+        if (defs[i].type == B2G_JOINT_MOUSE) {
+            /* b2_mouse_joint_new (src/joints/b2_mouse_joint.rs:140-160): the target in body B's frame */
+            const V2 la = mul_t(host_xf(w, (int)defs[i].body_b), mk(defs[i].target.x, defs[i].target.y));
+            w->joints.back().local_anchor_b = b2g_vec2{la.x, la.y};
+        }
         w->h_jimp.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         w->h_jimp2.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         if (!defs[i].collide_connected) w->joint_filter_pending = true;
@@ -1629,6 +1641,24 @@ int b2g_apply_linear_impulse_to_center(void* p, uint32_t b, b2g_vec2 impulse, in
 int b2g_apply_angular_impulse(void* p, uint32_t b, float impulse, int32_t wake) {
     return p ? body_op(W(p), 7, b, 0.0f, 0.0f, impulse, 0.0f, 0.0f, wake) : B2G_ERR_INVALID_ARG;
 }
+int b2g_set_mouse_target(void* p, uint32_t j, b2g_vec2 target) {
+    World* w = W(p);
+    if (!w || j >= w->joints.size() || w->joints[j].type != B2G_JOINT_MOUSE)
+        return w ? fail(w, B2G_ERR_INVALID_ARG, "not a mouse joint") : B2G_ERR_INVALID_ARG;
+    b2g_joint_def& jd = w->joints[j];
+    if (target.x == jd.target.x && target.y == jd.target.y) return B2G_OK;
+    tape_touch(w);
+    int rc = body_op(w, 8, jd.body_b, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1);  /* set_awake(true) */
+    if (rc != B2G_OK) return rc;
+    if (w->device_authoritative && !w->joints_dirty) {
+        rc = download_joint_impulses(w);
+        if (rc != B2G_OK) return rc;
+    }
+    jd.target = target;
+    w->joints_dirty = true;
+    return B2G_OK;
+}
+
 int b2g_set_awake(void* p, uint32_t b, int32_t flag) {
     if (!p) return B2G_ERR_INVALID_ARG;
     if (!flag) W(p)->asleep_seen = true;

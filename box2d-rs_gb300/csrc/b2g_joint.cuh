@@ -635,6 +635,90 @@ __device__ void motor_solve_velocity(const DevWorld& w, const StepParams& sp, in
     if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
 }
 
+/* ---- mouse joint (B2mouseJoint, private/dynamics/joints/b2_mouse_joint.rs) ----
+ * j_anchor = (target x, y, local anchor B x, y), j_lim = (max force, stiffness, damping, -),
+ * j_imp = (x, y, -, -); the step's mass (B2Mat22::get_inverse of K + gamma I) in j_k, r_b in j_rr.zw,
+ * gamma in j_s.x, beta-scaled position error in j_x.xy. Acts on body B only; no position correction. */
+
+__device__ void mouse_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int b = w.j_body[j].y;
+    const float4 an = w.j_anchor[j];
+    const float4 lim = w.j_lim[j];
+    const float4 massB = w.b_mass[b];
+    const float2 lcB = w.b_lc[b];
+    const float mB = massB.y, iB = massB.w;
+    const float4 pb = w.b_pos[b];
+    float4 vb = w.b_vel[b];
+    V2 vB = mk(vb.x, vb.y);
+    float wB = vb.z;
+    const Rot qB = rot(pb.z);
+    const float d = lim.z, k = lim.y, h = sp.dt;
+    float gamma = h * (d + h * k);
+    if (gamma != 0.0f) gamma = fdiv(1.0f, gamma);
+    const float beta = h * k * gamma;
+    const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+    const float kxx = mB + iB * rB.y * rB.y + gamma;
+    const float kxy = -iB * rB.x * rB.y;
+    const float kyy = mB + iB * rB.x * rB.x + gamma;
+    float det = kxx * kyy - kxy * kxy;
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    const float4 lm = make_float4(det * kyy, -det * kxy, -det * kxy, det * kxx);  /* ex.x, ex.y, ey.x, ey.y */
+    V2 C = sub(add(mk(pb.x, pb.y), rB), mk(an.x, an.y));
+    C = mk(C.x * beta, C.y * beta);
+    wB *= 0.98f;
+    float4 imp = w.j_imp[j];
+    if (sp.warm) {
+        imp.x *= sp.dt_ratio;
+        imp.y *= sp.dt_ratio;
+        const V2 P = mk(imp.x, imp.y);
+        vB = add(vB, scale(mB, P));
+        wB += iB * cross(rB, P);
+    } else {
+        imp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    w.j_imp[j] = imp;
+    w.j_rr[j] = make_float4(0.0f, 0.0f, rB.x, rB.y);
+    w.j_k[j] = lm;
+    w.j_m[j] = make_float4(0.0f, mB, 0.0f, iB);
+    w.j_s[j] = make_float2(gamma, 0.0f);
+    w.j_x[j] = make_float4(C.x, C.y, 0.0f, 0.0f);
+    if (joint_body_dynamic(w, b)) w.b_vel[b] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+__device__ void mouse_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int b = w.j_body[j].y;
+    const float4 lim = w.j_lim[j];
+    const float4 m = w.j_m[j];
+    const float mB = m.y, iB = m.w;
+    const float4 rr = w.j_rr[j];
+    const V2 rB = mk(rr.z, rr.w);
+    const float4 lm = w.j_k[j];
+    const float gamma = w.j_s[j].x;
+    const float4 C = w.j_x[j];
+    float4 imp = w.j_imp[j];
+    float4 vb = w.b_vel[b];
+    V2 vB = mk(vb.x, vb.y);
+    float wB = vb.z;
+    const V2 cdot = add(vB, cross_sv(wB, rB));
+    const V2 rhs = neg(add(add(cdot, mk(C.x, C.y)), mk(gamma * imp.x, gamma * imp.y)));
+    V2 impulse = mk(lm.x * rhs.x + lm.z * rhs.y, lm.y * rhs.x + lm.w * rhs.y);
+    const V2 old_impulse = mk(imp.x, imp.y);
+    V2 li = add(old_impulse, impulse);
+    const float max_impulse = sp.dt * lim.x;
+    if (dot(li, li) > max_impulse * max_impulse) {
+        const float s = fdiv(max_impulse, length(li));
+        li.x *= s;
+        li.y *= s;
+    }
+    impulse = sub(li, old_impulse);
+    imp.x = li.x;
+    imp.y = li.y;
+    vB = add(vB, scale(mB, impulse));
+    wB += iB * cross(rB, impulse);
+    w.j_imp[j] = imp;
+    if (joint_body_dynamic(w, b)) w.b_vel[b] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
 __device__ __forceinline__ uint32_t joint_type(const DevWorld& w, int j) {
     return (__float_as_uint(w.j_par[j].y) >> JF_TYPE_SHIFT) & 0xffu;
 }
@@ -832,6 +916,7 @@ __device__ __forceinline__ void joint_init_velocity(const DevWorld& w, const Ste
     else if (t == B2G_JOINT_WELD) weld_init_velocity(w, sp, j);
     else if (t == B2G_JOINT_FRICTION) friction_init_velocity(w, sp, j);
     else if (t == B2G_JOINT_MOTOR) motor_init_velocity(w, sp, j);
+    else if (t == B2G_JOINT_MOUSE) mouse_init_velocity(w, sp, j);
     else revolute_init_velocity(w, sp, j);
 }
 __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
@@ -840,13 +925,14 @@ __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const St
     else if (t == B2G_JOINT_WELD) weld_solve_velocity(w, j);
     else if (t == B2G_JOINT_FRICTION) friction_solve_velocity(w, sp, j);
     else if (t == B2G_JOINT_MOTOR) motor_solve_velocity(w, sp, j);
+    else if (t == B2G_JOINT_MOUSE) mouse_solve_velocity(w, sp, j);
     else revolute_solve_velocity(w, sp, j);
 }
 __device__ __forceinline__ bool joint_solve_position(const DevWorld& w, int j) {
     const uint32_t t = joint_type(w, j);
     if (t == B2G_JOINT_DISTANCE) return distance_solve_position(w, j);
     if (t == B2G_JOINT_WELD) return weld_solve_position(w, j);
-    if (t == B2G_JOINT_FRICTION || t == B2G_JOINT_MOTOR) return true;
+    if (t == B2G_JOINT_FRICTION || t == B2G_JOINT_MOTOR || t == B2G_JOINT_MOUSE) return true;
     return revolute_solve_position(w, j);
 }
 

@@ -111,6 +111,10 @@ struct Joint {
      * linear and angular impulses and masses with the friction joint */
     Vec2 linear_offset{0, 0}, linear_error{0, 0};
     float angular_offset = 0, correction_factor = 0, angular_error = 0;
+    /* B2mouseJoint (private/dynamics/joints/b2_mouse_joint.rs): shares the linear impulse and mass, gamma,
+     * max_force, stiffness and damping */
+    Vec2 target{0, 0}, mouse_c{0, 0};
+    float beta = 0;
     float weld_mass[9] = {0};  /* ex, ey, ez columns */
     bool collide_connected = false, island_flag = false;
     Vec2 local_anchor_a{0, 0}, local_anchor_b{0, 0};
@@ -1491,10 +1495,69 @@ static void motor_solve_velocity(World& w, Joint& j, const Step& step) {
     w.vel[j.index_b].w = wB;
 }
 
+/* ---- mouse joint, private/dynamics/joints/b2_mouse_joint.rs ---- */
+
+static void mouse_init_velocity(World& w, Joint& j, const Step& step) {
+    const Body& B = w.bodies[j.body_b];
+    j.index_b = B.island_index;
+    j.lc_b = B.sweep.local_center;
+    j.inv_mass_b = B.inv_mass;
+    j.inv_ib = B.inv_I;
+    const Vec2 cB = w.pos[j.index_b].c;
+    const float aB = w.pos[j.index_b].a;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const Rot qB = rot(aB);
+    const float d = j.damping, k = j.stiffness, h = step.dt;
+    j.gamma = h * (d + h * k);
+    if (j.gamma != 0.0f) j.gamma = 1.0f / j.gamma;
+    j.beta = h * k * j.gamma;
+    j.r_b = mul(qB, j.local_anchor_b - j.lc_b);
+    Mat22 K;
+    K.ex.x = j.inv_mass_b + j.inv_ib * j.r_b.y * j.r_b.y + j.gamma;
+    K.ex.y = -j.inv_ib * j.r_b.x * j.r_b.y;
+    K.ey.x = K.ex.y;
+    K.ey.y = j.inv_mass_b + j.inv_ib * j.r_b.x * j.r_b.x + j.gamma;
+    j.linear_mass = inverse(K);
+    j.mouse_c = cB + j.r_b - j.target;
+    j.mouse_c *= j.beta;
+    wB *= 0.98f;
+    if (step.warm) {
+        j.linear_impulse *= step.dt_ratio;
+        vB += j.inv_mass_b * j.linear_impulse;
+        wB += j.inv_ib * cross(j.r_b, j.linear_impulse);
+    } else {
+        j.linear_impulse = v2(0, 0);
+    }
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+static void mouse_solve_velocity(World& w, Joint& j, const Step& step) {
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const Vec2 cdot = vB + cross_sv(wB, j.r_b);
+    Vec2 impulse = mul(j.linear_mass, -(cdot + j.mouse_c + j.gamma * j.linear_impulse));
+    const Vec2 old_impulse = j.linear_impulse;
+    j.linear_impulse += impulse;
+    const float max_impulse = step.dt * j.max_force;
+    if (dot(j.linear_impulse, j.linear_impulse) > max_impulse * max_impulse)
+        j.linear_impulse *= max_impulse / length(j.linear_impulse);
+    impulse = j.linear_impulse - old_impulse;
+    vB += j.inv_mass_b * impulse;
+    wB += j.inv_ib * cross(j.r_b, impulse);
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
 /* init_velocity_constraints (:21-116): anchors, effective masses, warm start */
 static void joint_init_velocity(World& w, Joint& j, const Step& step) {
     if (j.type == B2G_JOINT_MOTOR) {
         motor_init_velocity(w, j, step);
+        return;
+    }
+    if (j.type == B2G_JOINT_MOUSE) {
+        mouse_init_velocity(w, j, step);
         return;
     }
     if (j.type == B2G_JOINT_FRICTION) {
@@ -1576,6 +1639,10 @@ static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
         motor_solve_velocity(w, j, step);
         return;
     }
+    if (j.type == B2G_JOINT_MOUSE) {
+        mouse_solve_velocity(w, j, step);
+        return;
+    }
     if (j.type == B2G_JOINT_FRICTION) {
         friction_solve_velocity(w, j, step);
         return;
@@ -1646,8 +1713,8 @@ static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
 static bool joint_solve_position(World& w, Joint& j) {
     if (j.type == B2G_JOINT_DISTANCE) return distance_solve_position(w, j);
     if (j.type == B2G_JOINT_WELD) return weld_solve_position(w, j);
-    /* b2_friction_joint.rs and b2_motor_joint.rs: no position correction */
-    if (j.type == B2G_JOINT_FRICTION || j.type == B2G_JOINT_MOTOR) return true;
+    /* b2_friction_joint.rs, b2_motor_joint.rs and b2_mouse_joint.rs: no position correction */
+    if (j.type == B2G_JOINT_FRICTION || j.type == B2G_JOINT_MOTOR || j.type == B2G_JOINT_MOUSE) return true;
     Vec2 cA = w.pos[j.index_a].c;
     float aA = w.pos[j.index_a].a;
     Vec2 cB = w.pos[j.index_b].c;
@@ -2440,7 +2507,7 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
     for (int i = 0; i < n; ++i) {
         const b2g_joint_def& d = defs[i];
         if ((d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE && d.type != B2G_JOINT_WELD &&
-             d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR) ||
+             d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR && d.type != B2G_JOINT_MOUSE) ||
             d.body_a >= w.bodies.size() ||
             d.body_b >= w.bodies.size())
             return -1;
@@ -2458,11 +2525,14 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
         j.linear_offset = v2(d.linear_offset.x, d.linear_offset.y);
         j.angular_offset = d.angular_offset;
         j.correction_factor = d.correction_factor;
+        j.target = v2(d.target.x, d.target.y);
         j.body_a = (int)d.body_a;
         j.body_b = (int)d.body_b;
         j.collide_connected = d.collide_connected != 0;
         j.local_anchor_a = v2(d.local_anchor_a.x, d.local_anchor_a.y);
         j.local_anchor_b = v2(d.local_anchor_b.x, d.local_anchor_b.y);
+        /* b2_mouse_joint_new (src/joints/b2_mouse_joint.rs:140-160): the target in body B's frame */
+        if (j.type == B2G_JOINT_MOUSE) j.local_anchor_b = mul_t(w.bodies[j.body_b].xf, j.target);
         j.reference_angle = d.reference_angle;
         j.enable_limit = d.enable_limit != 0;
         j.lower_angle = d.lower_angle;
@@ -2493,7 +2563,7 @@ int ora_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) 
     if ((size_t)first + count > w.joints.size()) return -1;
     for (uint32_t i = 0; i < count; ++i) {
         const Joint& j = w.joints[first + i];
-        if (j.type == B2G_JOINT_FRICTION || j.type == B2G_JOINT_MOTOR) {
+        if (j.type == B2G_JOINT_FRICTION || j.type == B2G_JOINT_MOTOR || j.type == B2G_JOINT_MOUSE) {
             out[5 * i + 0] = j.linear_impulse.x;
             out[5 * i + 1] = j.linear_impulse.y;
             out[5 * i + 2] = j.angular_impulse;
@@ -2527,6 +2597,18 @@ int ora_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) 
 }
 
 /* Joint ordering hook: each island solves its joints in this order of joint ids (n = 0 clears) */
+/* B2mouseJoint::set_target (src/joints/b2_mouse_joint.rs:114-119) */
+int ora_set_mouse_target(void* p, uint32_t id, float x, float y) {
+    World& w = *(World*)p;
+    if (id >= w.joints.size() || w.joints[id].type != B2G_JOINT_MOUSE) return -1;
+    Joint& j = w.joints[id];
+    if (x != j.target.x || y != j.target.y) {
+        set_awake(w.bodies[j.body_b], true);
+        j.target = v2(x, y);
+    }
+    return 0;
+}
+
 int ora_set_joint_order(void* p, const uint32_t* order, int n) {
     World& w = *(World*)p;
     w.joint_rank.clear();

@@ -68,6 +68,7 @@ def load():
         "ora_create_joints": [vp, vp, i32, vp],
         "ora_get_joint_impulses": [vp, u32, u32, vp],
         "ora_set_joint_order": [vp, vp, i32],
+        "ora_set_mouse_target": [vp, u32, f32, f32],
         "ora_set_key_order": [vp, i32],
         "ora_get_awake": [vp, u32, u32, vp],
         "ora_get_solver_order": [vp, vp, i32, pi32],
@@ -228,6 +229,9 @@ class OracleWorld:
         if n:
             self._lib.ora_get_joint_impulses(self._h, 0, n, _ptr(out))
         return out
+
+    def set_mouse_target(self, joint, target):
+        assert self._lib.ora_set_mouse_target(self._h, joint, float(target[0]), float(target[1])) == 0
 
     def set_joint_order(self, order):
         """Ordering hook: islands solve their joints in this order of joint ids."""

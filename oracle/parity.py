@@ -210,13 +210,15 @@ def drop_transient(contacts, aabbs):
     return c[keep]
 
 
-def lockstep(scene, steps, check_pairs=True, check_contacts=True, resync=False, on_step=None):
+def lockstep(scene, steps, check_pairs=True, check_contacts=True, resync=False, on_step=None, before_step=None):
     """Step GPU and oracle in lockstep; returns per-step records of the differences."""
     gpu, ora = make_pair(scene, record_pairs=check_pairs)
     continuous = bool(scene.get("continuous", False))
     dt, vi, pi = scene["dt"], scene["vi"], scene["pi"]
     out = []
     for k in range(steps):
+        if before_step is not None:
+            before_step(k, gpu, ora)  # the same world edits on both sides
         gpu.step(dt, vi, pi)
         order = gpu.get_solver_order()
         ora.set_solver_order(order)

@@ -596,3 +596,39 @@ def test_motor_joints_lockstep(built):
         assert r["joint_impulses_equal"], r
     st = gpu.get_body_states()
     assert abs(float(st["position"][1, 0]) + 5.0) < 0.2 and abs(float(st["position"][1, 1]) - 4.0) < 0.2
+
+
+@pytest.mark.gpu
+def test_mouse_joints_lockstep(built):
+    """Mouse joints: boxes resting on the ground, some held by soft mouse joints at a point of their
+    own; the free ones fall asleep, then new targets drag jointed boxes up and sideways (each new
+    target wakes its body) and back down onto the others; bit-exact bodies, impulses and awake flags
+    every step."""
+    n = 8
+    bodies = b2g.body_defs(n + 1)
+    bodies[1:]["type"] = b2g.DYNAMIC
+    bodies[1:]["position"][:, 0] = np.arange(n) * 2.0 - 7.0
+    bodies[1:]["position"][:, 1] = 0.5
+    fx = [b2g.edge_fixture(0, (-20.0, 0.0), (20.0, 0.0))]
+    fx += [b2g.box_fixture(i + 1, 0.5, 0.5, density=1.0, friction=0.6) for i in range(n)]
+    held = [1, 3, 4, 6]
+    joints = [b2g.mouse_joint(0, b, (float(bodies[b]["position"][0]) + 0.2, 0.8), max_force=400.0,
+                              stiffness=150.0, damping=12.0 + b) for b in held]
+    moves = {90: [(0, (-5.5, 3.0)), (2, (-2.0, 4.0))], 150: [(1, (-1.0, 2.5)), (0, (-4.0, 1.2))],
+             200: [(3, (4.0, 5.0)), (2, (-2.5, 1.0))]}
+
+    def before_step(k, gpu, ora):
+        for j, t in moves.get(k, []):
+            gpu.set_mouse_target(j, t)
+            ora.set_mouse_target(j, t)
+
+    s = {"name": "mouse", "bodies": bodies, "fixtures": np.concatenate(fx), "joints": np.concatenate(joints),
+         "gravity": (0.0, -10.0), "dt": np.float32(1.0 / 60.0), "vi": 8, "pi": 3, "steps": 260, "num_worlds": 1,
+         "allow_sleep": True, "n_dynamic": n}
+    recs, gpu, _ = parity.lockstep(s, 260, before_step=before_step)
+    for r in recs:
+        _assert_step(r)
+        assert r["joint_impulses_equal"], r
+    assert min(r["awake"] for r in recs[60:90]) < n  # free boxes slept before the drags
+    st = gpu.get_body_states()
+    assert st["position"][held[3], 1] > 3.5  # dragged up to its last target
