@@ -167,6 +167,10 @@ JOINT_DEF = np.dtype(
         ("angular_offset", "<f4"),
         ("linear_offset", "<f4", (2,)),
         ("target", "<f4", (2,)),
+        ("local_axis_a", "<f4", (2,)),
+        ("lower_translation", "<f4"),
+        ("upper_translation", "<f4"),
+        ("max_motor_force", "<f4"),
     ]
 )
 JOINT_DISTANCE = 3
@@ -174,6 +178,7 @@ JOINT_WELD = 8
 JOINT_FRICTION = 9
 JOINT_MOTOR = 11
 JOINT_MOUSE = 5
+JOINT_PRISMATIC = 2
 
 
 def friction_joint(body_a, body_b, anchor_a, anchor_b, max_force, max_torque, collide_connected=False):
@@ -209,6 +214,25 @@ def mouse_joint(body_a, body_b, target, max_force, stiffness=0.0, damping=0.0, c
     d["collide_connected"] = int(bool(collide_connected))
     d["target"] = target
     d["max_force"], d["stiffness"], d["damping"] = max_force, stiffness, damping
+    return d
+
+
+def prismatic_joint(body_a, body_b, anchor_a, anchor_b, axis, reference_angle=0.0, limits=None, motor=None,
+                    collide_connected=False):
+    """B2prismaticJointDef: body B slides along `axis` (body A's frame); limits = (lower, upper)
+    translation; motor = (speed, max force)."""
+    d = np.zeros(1, JOINT_DEF)
+    d["type"] = JOINT_PRISMATIC
+    d["body_a"], d["body_b"] = body_a, body_b
+    d["collide_connected"] = int(bool(collide_connected))
+    d["local_anchor_a"], d["local_anchor_b"] = anchor_a, anchor_b
+    d["local_axis_a"], d["reference_angle"] = axis, reference_angle
+    if limits is not None:
+        d["enable_limit"] = 1
+        d["lower_translation"], d["upper_translation"] = limits
+    if motor is not None:
+        d["enable_motor"] = 1
+        d["motor_speed"], d["max_motor_force"] = motor
     return d
 
 

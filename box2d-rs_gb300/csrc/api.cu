@@ -745,7 +745,14 @@ int upload_joints(World* w) {
             jb[j] = make_int2((int)jd.body_a, (int)jd.body_b);
             an[j] = make_float4(jd.local_anchor_a.x, jd.local_anchor_a.y, jd.local_anchor_b.x, jd.local_anchor_b.y);
             uint32_t fl = ((uint32_t)jd.type << JF_TYPE_SHIFT) | (jd.collide_connected ? JF_COLLIDE : 0u);
-            if (jd.type == B2G_JOINT_MOUSE) {
+            if (jd.type == B2G_JOINT_PRISMATIC) {
+                /* B2prismaticJoint::new (private/dynamics/joints/b2_prismatic_joint.rs:54-60): unit axis */
+                V2 ax = mk(jd.local_axis_a.x, jd.local_axis_a.y);
+                normalize(ax);
+                lim[j] = make_float4(jd.lower_translation, jd.upper_translation, jd.motor_speed, jd.max_motor_force);
+                fl |= (jd.enable_limit ? JF_LIMIT : 0u) | (jd.enable_motor ? JF_MOTOR : 0u);
+                par[j] = make_float4(jd.reference_angle, __uint_as_float_host(fl), ax.x, ax.y);
+            } else if (jd.type == B2G_JOINT_MOUSE) {
                 an[j] = make_float4(jd.target.x, jd.target.y, jd.local_anchor_b.x, jd.local_anchor_b.y);
                 lim[j] = make_float4(jd.max_force, jd.stiffness, jd.damping, 0.0f);
                 par[j] = make_float4(0.0f, __uint_as_float_host(fl), 0.0f, 0.0f);
@@ -1355,9 +1362,10 @@ int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* i
     for (int i = 0; i < n; ++i) {
         const b2g_joint_def& d = defs[i];
         if (d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE && d.type != B2G_JOINT_WELD &&
-            d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR && d.type != B2G_JOINT_MOUSE)
-            return fail(w, B2G_ERR_UNSUPPORTED,
-                        "only revolute, distance, weld, friction, motor and mouse joints are on the GPU path");
+            d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR && d.type != B2G_JOINT_MOUSE &&
+            d.type != B2G_JOINT_PRISMATIC)
+            return fail(w, B2G_ERR_UNSUPPORTED, "only revolute, prismatic, distance, weld, friction, motor "
+                                                "and mouse joints are on the GPU path");
         if (d.body_a >= w->h_flags.size() || d.body_b >= w->h_flags.size() || d.body_a == d.body_b)
             return fail(w, B2G_ERR_INVALID_ARG, "joint body ids out of range or equal");
     }
@@ -1398,7 +1406,7 @@ int b2g_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) 
     }
     for (uint32_t i = 0; i < count; ++i) {
         const float4 a = w->h_jimp[first + i], b = w->h_jimp2[first + i];
-        if (w->joints[first + i].type != B2G_JOINT_REVOLUTE) {
+        if (w->joints[first + i].type != B2G_JOINT_REVOLUTE && w->joints[first + i].type != B2G_JOINT_PRISMATIC) {
             out[5 * i + 0] = a.x;
             out[5 * i + 1] = a.y;
             out[5 * i + 2] = a.z;

@@ -719,6 +719,230 @@ __device__ void mouse_solve_velocity(const DevWorld& w, const StepParams& sp, in
     if (joint_body_dynamic(w, b)) w.b_vel[b] = make_float4(vB.x, vB.y, wB, vb.w);
 }
 
+/* ---- prismatic joint (B2prismaticJoint, private/dynamics/joints/b2_prismatic_joint.rs:120-460) ----
+ * j_lim = (lower, upper translation, motor speed, max motor force), j_par = (reference angle, flags,
+ * unit local axis x, y), j_imp = (x, y, motor, lower), j_imp2.x = upper; the step's axis and perp in
+ * j_rr, (a1, a2, s1, s2) in j_k, (k11, k12, k22, axial mass) in j_x, translation in j_s.x. */
+
+__device__ void prismatic_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 an = w.j_anchor[j];
+    const float4 par = w.j_par[j];
+    const uint32_t jf = __float_as_uint(par.y);
+    const float4 massA = w.b_mass[bd.x], massB = w.b_mass[bd.y];
+    const float2 lcA = w.b_lc[bd.x], lcB = w.b_lc[bd.y];
+    const float mA = massA.y, mB = massB.y, iA = massA.w, iB = massB.w;
+    const float4 pa = w.b_pos[bd.x], pb = w.b_pos[bd.y];
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = rot(pa.z), qB = rot(pb.z);
+    const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+    const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+    const V2 d = sub(add(sub(mk(pb.x, pb.y), mk(pa.x, pa.y)), rB), rA);
+    const V2 xaxis = mk(par.z, par.w);
+    const V2 axis = mul(qA, xaxis);
+    const float a1 = cross(add(d, rA), axis), a2 = cross(rB, axis);
+    float axial_mass = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+    if (axial_mass > 0.0f) axial_mass = fdiv(1.0f, axial_mass);
+    const V2 perp = mul(qA, cross_sv(1.0f, xaxis));
+    const float s1 = cross(add(d, rA), perp), s2 = cross(rB, perp);
+    const float k11 = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+    const float k12 = iA * s1 + iB * s2;
+    float k22 = iA + iB;
+    if (k22 == 0.0f) k22 = 1.0f;
+    float4 imp = w.j_imp[j];
+    float4 imp2 = w.j_imp2[j];
+    float translation = 0.0f;
+    if (jf & JF_LIMIT) {
+        translation = dot(axis, d);
+    } else {
+        imp.w = 0.0f;
+        imp2.x = 0.0f;
+    }
+    if (!(jf & JF_MOTOR)) imp.z = 0.0f;
+    if (sp.warm) {
+        imp.x *= sp.dt_ratio;
+        imp.y *= sp.dt_ratio;
+        imp.z *= sp.dt_ratio;
+        imp.w *= sp.dt_ratio;
+        imp2.x *= sp.dt_ratio;
+        const float axial = imp.z + imp.w - imp2.x;
+        const V2 P = add(scale(imp.x, perp), scale(axial, axis));
+        const float LA = imp.x * s1 + imp.y + axial * a1;
+        const float LB = imp.x * s2 + imp.y + axial * a2;
+        vA = sub(vA, scale(mA, P));
+        wA -= iA * LA;
+        vB = add(vB, scale(mB, P));
+        wB += iB * LB;
+    } else {
+        imp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        imp2.x = 0.0f;
+    }
+    w.j_imp[j] = imp;
+    w.j_imp2[j] = imp2;
+    w.j_rr[j] = make_float4(axis.x, axis.y, perp.x, perp.y);
+    w.j_k[j] = make_float4(a1, a2, s1, s2);
+    w.j_x[j] = make_float4(k11, k12, k22, axial_mass);
+    w.j_m[j] = make_float4(mA, mB, iA, iB);
+    w.j_s[j] = make_float2(translation, 0.0f);
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+__device__ void prismatic_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 lim = w.j_lim[j];
+    const uint32_t jf = __float_as_uint(w.j_par[j].y);
+    const float4 m = w.j_m[j];
+    const float mA = m.x, mB = m.y, iA = m.z, iB = m.w;
+    const float4 rr = w.j_rr[j];
+    const V2 axis = mk(rr.x, rr.y), perp = mk(rr.z, rr.w);
+    const float4 ak = w.j_k[j];
+    const float a1 = ak.x, a2 = ak.y, s1 = ak.z, s2 = ak.w;
+    const float4 kx = w.j_x[j];
+    const float axial_mass = kx.w, translation = w.j_s[j].x;
+    float4 imp = w.j_imp[j];
+    float4 imp2 = w.j_imp2[j];
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    if (jf & JF_MOTOR) {
+        const float cdot = dot(axis, sub(vB, vA)) + a2 * wB - a1 * wA;
+        float impulse = axial_mass * (lim.z - cdot);
+        const float old_impulse = imp.z;
+        const float max_impulse = sp.dt * lim.w;
+        imp.z = fclampr(imp.z + impulse, -max_impulse, max_impulse);
+        impulse = imp.z - old_impulse;
+        const V2 P = scale(impulse, axis);
+        const float LA = impulse * a1, LB = impulse * a2;
+        vA = sub(vA, scale(mA, P));
+        wA -= iA * LA;
+        vB = add(vB, scale(mB, P));
+        wB += iB * LB;
+    }
+    if (jf & JF_LIMIT) {
+        {
+            const float C = translation - lim.x;
+            const float cdot = dot(axis, sub(vB, vA)) + a2 * wB - a1 * wA;
+            float impulse = -axial_mass * (cdot + fmaxr(C, 0.0f) * sp.inv_dt);
+            const float old_impulse = imp.w;
+            imp.w = fmaxr(imp.w + impulse, 0.0f);
+            impulse = imp.w - old_impulse;
+            const V2 P = scale(impulse, axis);
+            const float LA = impulse * a1, LB = impulse * a2;
+            vA = sub(vA, scale(mA, P));
+            wA -= iA * LA;
+            vB = add(vB, scale(mB, P));
+            wB += iB * LB;
+        }
+        {
+            const float C = lim.y - translation;
+            const float cdot = dot(axis, sub(vA, vB)) + a1 * wA - a2 * wB;
+            float impulse = -axial_mass * (cdot + fmaxr(C, 0.0f) * sp.inv_dt);
+            const float old_impulse = imp2.x;
+            imp2.x = fmaxr(imp2.x + impulse, 0.0f);
+            impulse = imp2.x - old_impulse;
+            const V2 P = scale(impulse, axis);
+            const float LA = impulse * a1, LB = impulse * a2;
+            vA = add(vA, scale(mA, P));
+            wA += iA * LA;
+            vB = sub(vB, scale(mB, P));
+            wB -= iB * LB;
+        }
+    }
+    {
+        const V2 cdot = mk(dot(perp, sub(vB, vA)) + s2 * wB - s1 * wA, wB - wA);
+        const V2 df = mat22_solve(kx.x, kx.y, kx.y, kx.z, neg(cdot));
+        imp.x += df.x;
+        imp.y += df.y;
+        const V2 P = scale(df.x, perp);
+        const float LA = df.x * s1 + df.y, LB = df.x * s2 + df.y;
+        vA = sub(vA, scale(mA, P));
+        wA -= iA * LA;
+        vB = add(vB, scale(mB, P));
+        wB += iB * LB;
+    }
+    w.j_imp[j] = imp;
+    w.j_imp2[j] = imp2;
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+__device__ bool prismatic_solve_position(const DevWorld& w, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 an = w.j_anchor[j];
+    const float4 lim = w.j_lim[j];
+    const float4 par = w.j_par[j];
+    const uint32_t jf = __float_as_uint(par.y);
+    const float4 m = w.j_m[j];
+    const float mA = m.x, mB = m.y, iA = m.z, iB = m.w;
+    const float2 lcA = w.b_lc[bd.x], lcB = w.b_lc[bd.y];
+    const float4 pa = w.b_pos[bd.x], pb = w.b_pos[bd.y];
+    V2 cA = mk(pa.x, pa.y), cB = mk(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    const Rot qA = rot(aA), qB = rot(aB);
+    const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+    const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+    const V2 d = sub(sub(add(cB, rB), cA), rA);
+    const V2 xaxis = mk(par.z, par.w);
+    const V2 axis = mul(qA, xaxis);
+    const float a1 = cross(add(d, rA), axis), a2 = cross(rB, axis);
+    const V2 perp = mul(qA, cross_sv(1.0f, xaxis));
+    const float s1 = cross(add(d, rA), perp), s2 = cross(rB, perp);
+    const V2 C1 = mk(dot(perp, d), aB - aA - par.x);
+    float linear_error = fabsr(C1.x);
+    const float angular_error = fabsr(C1.y);
+    bool active = false;
+    float C2 = 0.0f;
+    if (jf & JF_LIMIT) {
+        const float translation = dot(axis, d);
+        if (fabsr(lim.y - lim.x) < 2.0f * kLinearSlop) {
+            C2 = translation;
+            linear_error = fmaxr(linear_error, fabsr(translation));
+            active = true;
+        } else if (translation <= lim.x) {
+            C2 = fminr(translation - lim.x, 0.0f);
+            linear_error = fmaxr(linear_error, lim.x - translation);
+            active = true;
+        } else if (translation >= lim.y) {
+            C2 = fmaxr(translation - lim.y, 0.0f);
+            linear_error = fmaxr(linear_error, translation - lim.y);
+            active = true;
+        }
+    }
+    V3 impulse;
+    const float k11 = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+    const float k12 = iA * s1 + iB * s2;
+    if (active) {
+        const float k13 = iA * s1 * a1 + iB * s2 * a2;
+        float k22 = iA + iB;
+        if (k22 == 0.0f) k22 = 1.0f;
+        const float k23 = iA * a1 + iB * a2;
+        const float k33 = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+        M33 K;
+        K.ex = v3(k11, k12, k13);
+        K.ey = v3(k12, k22, k23);
+        K.ez = v3(k13, k23, k33);
+        impulse = m33_solve33(K, v3(-C1.x, -C1.y, -C2));
+    } else {
+        float k22 = iA + iB;
+        if (k22 == 0.0f) k22 = 1.0f;
+        const V2 i1 = mat22_solve(k11, k12, k12, k22, neg(C1));
+        impulse = v3(i1.x, i1.y, 0.0f);
+    }
+    const V2 P = add(scale(impulse.x, perp), scale(impulse.z, axis));
+    const float LA = impulse.x * s1 + impulse.y + impulse.z * a1;
+    const float LB = impulse.x * s2 + impulse.y + impulse.z * a2;
+    cA = sub(cA, scale(mA, P));
+    aA -= iA * LA;
+    cB = add(cB, scale(mB, P));
+    aB += iB * LB;
+    if (joint_body_dynamic(w, bd.x)) w.b_pos[bd.x] = make_float4(cA.x, cA.y, aA, pa.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_pos[bd.y] = make_float4(cB.x, cB.y, aB, pb.w);
+    return linear_error <= kLinearSlop && angular_error <= kAngularSlop;
+}
+
 __device__ __forceinline__ uint32_t joint_type(const DevWorld& w, int j) {
     return (__float_as_uint(w.j_par[j].y) >> JF_TYPE_SHIFT) & 0xffu;
 }
@@ -917,6 +1141,7 @@ __device__ __forceinline__ void joint_init_velocity(const DevWorld& w, const Ste
     else if (t == B2G_JOINT_FRICTION) friction_init_velocity(w, sp, j);
     else if (t == B2G_JOINT_MOTOR) motor_init_velocity(w, sp, j);
     else if (t == B2G_JOINT_MOUSE) mouse_init_velocity(w, sp, j);
+    else if (t == B2G_JOINT_PRISMATIC) prismatic_init_velocity(w, sp, j);
     else revolute_init_velocity(w, sp, j);
 }
 __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
@@ -926,6 +1151,7 @@ __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const St
     else if (t == B2G_JOINT_FRICTION) friction_solve_velocity(w, sp, j);
     else if (t == B2G_JOINT_MOTOR) motor_solve_velocity(w, sp, j);
     else if (t == B2G_JOINT_MOUSE) mouse_solve_velocity(w, sp, j);
+    else if (t == B2G_JOINT_PRISMATIC) prismatic_solve_velocity(w, sp, j);
     else revolute_solve_velocity(w, sp, j);
 }
 __device__ __forceinline__ bool joint_solve_position(const DevWorld& w, int j) {
@@ -933,6 +1159,7 @@ __device__ __forceinline__ bool joint_solve_position(const DevWorld& w, int j) {
     if (t == B2G_JOINT_DISTANCE) return distance_solve_position(w, j);
     if (t == B2G_JOINT_WELD) return weld_solve_position(w, j);
     if (t == B2G_JOINT_FRICTION || t == B2G_JOINT_MOTOR || t == B2G_JOINT_MOUSE) return true;
+    if (t == B2G_JOINT_PRISMATIC) return prismatic_solve_position(w, j);
     return revolute_solve_position(w, j);
 }
 

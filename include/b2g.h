@@ -124,11 +124,15 @@ typedef struct b2g_fixture_def {
  *   B2G_JOINT_MOUSE: B2mouseJointDef (src/joints/b2_mouse_joint.rs): a world target that body B's point
  *     under it at creation is pulled to by a soft constraint (max force, stiffness, damping); body A only
  *     ties the joint into the world (usually a static body)
+ *   B2G_JOINT_PRISMATIC: B2prismaticJointDef (src/joints/b2_prismatic_joint.rs): local axis in body A
+ *     (normalized at creation), reference angle, limit (enable_limit, lower/upper translation), motor
+ *     (enable_motor, motor_speed, max_motor_force)
  * The type numbers follow Box2D's C++ b2JointType. */
 #define B2G_JOINT_REVOLUTE 1
 #define B2G_JOINT_DISTANCE 3
 #define B2G_JOINT_WELD 8
 #define B2G_JOINT_FRICTION 9
+#define B2G_JOINT_PRISMATIC 2
 #define B2G_JOINT_MOUSE 5
 #define B2G_JOINT_MOTOR 11
 typedef struct b2g_joint_def {
@@ -146,6 +150,8 @@ typedef struct b2g_joint_def {
     float correction_factor, angular_offset;
     b2g_vec2 linear_offset;
     b2g_vec2 target;
+    b2g_vec2 local_axis_a;
+    float lower_translation, upper_translation, max_motor_force;
 } b2g_joint_def;
 
 /* Body state read back after a step (B2body getters, src/b2_body.rs:650-680). */
@@ -204,7 +210,8 @@ int b2g_create_fixtures(void* world, const b2g_fixture_def* defs, int32_t n, uin
  * A world with joints runs the grid-wide colour schedule (no part-local solve) and cannot be taped. */
 int b2g_create_joints(void* world, const b2g_joint_def* defs, int32_t n, uint32_t* out_ids);
 /* Accumulated joint impulses (for warm starting), 5 per joint: revolute x, y, motor, lower, upper;
- * distance impulse, lower, upper, 0, 0; weld, friction and motor x, y, angular, 0, 0; mouse x, y, 0, 0, 0 */
+ * prismatic x, y, motor, lower, upper; distance impulse, lower, upper, 0, 0; weld, friction and motor x, y,
+ * angular, 0, 0; mouse x, y, 0, 0, 0 */
 int b2g_get_joint_impulses(void* world, uint32_t first, uint32_t count, float* out);
 /* B2mouseJoint::set_target (src/joints/b2_mouse_joint.rs:114-119): a new target wakes body B */
 int b2g_set_mouse_target(void* world, uint32_t joint, b2g_vec2 target);

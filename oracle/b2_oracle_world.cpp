@@ -115,6 +115,11 @@ struct Joint {
      * max_force, stiffness and damping */
     Vec2 target{0, 0}, mouse_c{0, 0};
     float beta = 0;
+    /* B2prismaticJoint (private/dynamics/joints/b2_prismatic_joint.rs): shares the point impulse, motor and
+     * limit impulses, axial mass and K with the revolute joint */
+    Vec2 local_xaxis_a{1, 0}, local_yaxis_a{0, 1}, axis{0, 0}, perp{0, 0};
+    float a1 = 0, a2 = 0, s1 = 0, s2 = 0, translation = 0;
+    float lower_translation = 0, upper_translation = 0, max_motor_force = 0;
     float weld_mass[9] = {0};  /* ex, ey, ez columns */
     bool collide_connected = false, island_flag = false;
     Vec2 local_anchor_a{0, 0}, local_anchor_b{0, 0};
@@ -1550,6 +1555,217 @@ static void mouse_solve_velocity(World& w, Joint& j, const Step& step) {
     w.vel[j.index_b].w = wB;
 }
 
+/* ---- prismatic joint, private/dynamics/joints/b2_prismatic_joint.rs:120-460 ---- */
+
+static void prismatic_init_velocity(World& w, Joint& j, const Step& step) {
+    const Body& A = w.bodies[j.body_a];
+    const Body& B = w.bodies[j.body_b];
+    j.index_a = A.island_index;
+    j.index_b = B.island_index;
+    j.lc_a = A.sweep.local_center;
+    j.lc_b = B.sweep.local_center;
+    j.inv_mass_a = A.inv_mass;
+    j.inv_mass_b = B.inv_mass;
+    j.inv_ia = A.inv_I;
+    j.inv_ib = B.inv_I;
+    const Vec2 cA = w.pos[j.index_a].c, cB = w.pos[j.index_b].c;
+    const float aA = w.pos[j.index_a].a, aB = w.pos[j.index_b].a;
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const Rot qA = rot(aA), qB = rot(aB);
+    const Vec2 rA = mul(qA, j.local_anchor_a - j.lc_a);
+    const Vec2 rB = mul(qB, j.local_anchor_b - j.lc_b);
+    const Vec2 d = (cB - cA) + rB - rA;
+    const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+    j.axis = mul(qA, j.local_xaxis_a);
+    j.a1 = cross(d + rA, j.axis);
+    j.a2 = cross(rB, j.axis);
+    j.axial_mass = mA + mB + iA * j.a1 * j.a1 + iB * j.a2 * j.a2;
+    if (j.axial_mass > 0.0f) j.axial_mass = 1.0f / j.axial_mass;
+    j.perp = mul(qA, j.local_yaxis_a);
+    j.s1 = cross(d + rA, j.perp);
+    j.s2 = cross(rB, j.perp);
+    const float k11 = mA + mB + iA * j.s1 * j.s1 + iB * j.s2 * j.s2;
+    const float k12 = iA * j.s1 + iB * j.s2;
+    float k22 = iA + iB;
+    if (k22 == 0.0f) k22 = 1.0f;
+    j.k.ex = v2(k11, k12);
+    j.k.ey = v2(k12, k22);
+    if (j.enable_limit) {
+        j.translation = dot(j.axis, d);
+    } else {
+        j.lower_impulse = 0.0f;
+        j.upper_impulse = 0.0f;
+    }
+    if (!j.enable_motor) j.motor_impulse = 0.0f;
+    if (step.warm) {
+        j.impulse *= step.dt_ratio;
+        j.motor_impulse *= step.dt_ratio;
+        j.lower_impulse *= step.dt_ratio;
+        j.upper_impulse *= step.dt_ratio;
+        const float axial = j.motor_impulse + j.lower_impulse - j.upper_impulse;
+        const Vec2 P = j.impulse.x * j.perp + axial * j.axis;
+        const float LA = j.impulse.x * j.s1 + j.impulse.y + axial * j.a1;
+        const float LB = j.impulse.x * j.s2 + j.impulse.y + axial * j.a2;
+        vA -= mA * P;
+        wA -= iA * LA;
+        vB += mB * P;
+        wB += iB * LB;
+    } else {
+        j.impulse = v2(0, 0);
+        j.motor_impulse = 0.0f;
+        j.lower_impulse = 0.0f;
+        j.upper_impulse = 0.0f;
+    }
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+static void prismatic_solve_velocity(World& w, Joint& j, const Step& step) {
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+    if (j.enable_motor) {
+        const float cdot = dot(j.axis, vB - vA) + j.a2 * wB - j.a1 * wA;
+        float impulse = j.axial_mass * (j.motor_speed - cdot);
+        const float old_impulse = j.motor_impulse;
+        const float max_impulse = step.dt * j.max_motor_force;
+        j.motor_impulse = bclamp(j.motor_impulse + impulse, -max_impulse, max_impulse);
+        impulse = j.motor_impulse - old_impulse;
+        const Vec2 P = impulse * j.axis;
+        const float LA = impulse * j.a1, LB = impulse * j.a2;
+        vA -= mA * P;
+        wA -= iA * LA;
+        vB += mB * P;
+        wB += iB * LB;
+    }
+    if (j.enable_limit) {
+        {
+            const float C = j.translation - j.lower_translation;
+            const float cdot = dot(j.axis, vB - vA) + j.a2 * wB - j.a1 * wA;
+            float impulse = -j.axial_mass * (cdot + bmax(C, 0.0f) * step.inv_dt);
+            const float old_impulse = j.lower_impulse;
+            j.lower_impulse = bmax(j.lower_impulse + impulse, 0.0f);
+            impulse = j.lower_impulse - old_impulse;
+            const Vec2 P = impulse * j.axis;
+            const float LA = impulse * j.a1, LB = impulse * j.a2;
+            vA -= mA * P;
+            wA -= iA * LA;
+            vB += mB * P;
+            wB += iB * LB;
+        }
+        {
+            const float C = j.upper_translation - j.translation;
+            const float cdot = dot(j.axis, vA - vB) + j.a1 * wA - j.a2 * wB;
+            float impulse = -j.axial_mass * (cdot + bmax(C, 0.0f) * step.inv_dt);
+            const float old_impulse = j.upper_impulse;
+            j.upper_impulse = bmax(j.upper_impulse + impulse, 0.0f);
+            impulse = j.upper_impulse - old_impulse;
+            const Vec2 P = impulse * j.axis;
+            const float LA = impulse * j.a1, LB = impulse * j.a2;
+            vA += mA * P;
+            wA += iA * LA;
+            vB -= mB * P;
+            wB -= iB * LB;
+        }
+    }
+    {
+        const Vec2 cdot = v2(dot(j.perp, vB - vA) + j.s2 * wB - j.s1 * wA, wB - wA);
+        const Vec2 df = solve(j.k, -cdot);
+        j.impulse += df;
+        const Vec2 P = df.x * j.perp;
+        const float LA = df.x * j.s1 + df.y, LB = df.x * j.s2 + df.y;
+        vA -= mA * P;
+        wA -= iA * LA;
+        vB += mB * P;
+        wB += iB * LB;
+    }
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+static bool prismatic_solve_position(World& w, Joint& j) {
+    Vec2 cA = w.pos[j.index_a].c;
+    float aA = w.pos[j.index_a].a;
+    Vec2 cB = w.pos[j.index_b].c;
+    float aB = w.pos[j.index_b].a;
+    const Rot qA = rot(aA), qB = rot(aB);
+    const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+    const Vec2 rA = mul(qA, j.local_anchor_a - j.lc_a);
+    const Vec2 rB = mul(qB, j.local_anchor_b - j.lc_b);
+    const Vec2 d = cB + rB - cA - rA;
+    const Vec2 axis = mul(qA, j.local_xaxis_a);
+    const float a1 = cross(d + rA, axis), a2 = cross(rB, axis);
+    const Vec2 perp = mul(qA, j.local_yaxis_a);
+    const float s1 = cross(d + rA, perp), s2 = cross(rB, perp);
+    const Vec2 C1 = v2(dot(perp, d), aB - aA - j.reference_angle);
+    float linear_error = std::fabs(C1.x);
+    const float angular_error = std::fabs(C1.y);
+    bool active = false;
+    float C2 = 0.0f;
+    if (j.enable_limit) {
+        const float translation = dot(axis, d);
+        if (std::fabs(j.upper_translation - j.lower_translation) < 2.0f * kLinearSlop) {
+            C2 = translation;
+            linear_error = bmax(linear_error, std::fabs(translation));
+            active = true;
+        } else if (translation <= j.lower_translation) {
+            C2 = bmin(translation - j.lower_translation, 0.0f);
+            linear_error = bmax(linear_error, j.lower_translation - translation);
+            active = true;
+        } else if (translation >= j.upper_translation) {
+            C2 = bmax(translation - j.upper_translation, 0.0f);
+            linear_error = bmax(linear_error, translation - j.upper_translation);
+            active = true;
+        }
+    }
+    V3 impulse;
+    if (active) {
+        const float k11 = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+        const float k12 = iA * s1 + iB * s2;
+        const float k13 = iA * s1 * a1 + iB * s2 * a2;
+        float k22 = iA + iB;
+        if (k22 == 0.0f) k22 = 1.0f;
+        const float k23 = iA * a1 + iB * a2;
+        const float k33 = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+        M33 K;
+        K.ex = V3{k11, k12, k13};
+        K.ey = V3{k12, k22, k23};
+        K.ez = V3{k13, k23, k33};
+        impulse = m33_solve33(K, V3{-C1.x, -C1.y, -C2});
+    } else {
+        const float k11 = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+        const float k12 = iA * s1 + iB * s2;
+        float k22 = iA + iB;
+        if (k22 == 0.0f) k22 = 1.0f;
+        Mat22 K;
+        K.ex = v2(k11, k12);
+        K.ey = v2(k12, k22);
+        const Vec2 i1 = solve(K, -C1);
+        impulse = V3{i1.x, i1.y, 0.0f};
+    }
+    const Vec2 P = impulse.x * perp + impulse.z * axis;
+    const float LA = impulse.x * s1 + impulse.y + impulse.z * a1;
+    const float LB = impulse.x * s2 + impulse.y + impulse.z * a2;
+    cA -= mA * P;
+    aA -= iA * LA;
+    cB += mB * P;
+    aB += iB * LB;
+    w.pos[j.index_a].c = cA;
+    w.pos[j.index_a].a = aA;
+    w.pos[j.index_b].c = cB;
+    w.pos[j.index_b].a = aB;
+    return linear_error <= kLinearSlop && angular_error <= kAngularSlop;
+}
+
 /* init_velocity_constraints (:21-116): anchors, effective masses, warm start */
 static void joint_init_velocity(World& w, Joint& j, const Step& step) {
     if (j.type == B2G_JOINT_MOTOR) {
@@ -1558,6 +1774,10 @@ static void joint_init_velocity(World& w, Joint& j, const Step& step) {
     }
     if (j.type == B2G_JOINT_MOUSE) {
         mouse_init_velocity(w, j, step);
+        return;
+    }
+    if (j.type == B2G_JOINT_PRISMATIC) {
+        prismatic_init_velocity(w, j, step);
         return;
     }
     if (j.type == B2G_JOINT_FRICTION) {
@@ -1643,6 +1863,10 @@ static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
         mouse_solve_velocity(w, j, step);
         return;
     }
+    if (j.type == B2G_JOINT_PRISMATIC) {
+        prismatic_solve_velocity(w, j, step);
+        return;
+    }
     if (j.type == B2G_JOINT_FRICTION) {
         friction_solve_velocity(w, j, step);
         return;
@@ -1715,6 +1939,7 @@ static bool joint_solve_position(World& w, Joint& j) {
     if (j.type == B2G_JOINT_WELD) return weld_solve_position(w, j);
     /* b2_friction_joint.rs, b2_motor_joint.rs and b2_mouse_joint.rs: no position correction */
     if (j.type == B2G_JOINT_FRICTION || j.type == B2G_JOINT_MOTOR || j.type == B2G_JOINT_MOUSE) return true;
+    if (j.type == B2G_JOINT_PRISMATIC) return prismatic_solve_position(w, j);
     Vec2 cA = w.pos[j.index_a].c;
     float aA = w.pos[j.index_a].a;
     Vec2 cB = w.pos[j.index_b].c;
@@ -2507,7 +2732,8 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
     for (int i = 0; i < n; ++i) {
         const b2g_joint_def& d = defs[i];
         if ((d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE && d.type != B2G_JOINT_WELD &&
-             d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR && d.type != B2G_JOINT_MOUSE) ||
+             d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR && d.type != B2G_JOINT_MOUSE &&
+             d.type != B2G_JOINT_PRISMATIC) ||
             d.body_a >= w.bodies.size() ||
             d.body_b >= w.bodies.size())
             return -1;
@@ -2526,6 +2752,13 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
         j.angular_offset = d.angular_offset;
         j.correction_factor = d.correction_factor;
         j.target = v2(d.target.x, d.target.y);
+        /* B2prismaticJoint::new (b2_prismatic_joint.rs:54-60) */
+        j.local_xaxis_a = v2(d.local_axis_a.x, d.local_axis_a.y);
+        normalize(j.local_xaxis_a);
+        j.local_yaxis_a = cross_sv(1.0f, j.local_xaxis_a);
+        j.lower_translation = d.lower_translation;
+        j.upper_translation = d.upper_translation;
+        j.max_motor_force = d.max_motor_force;
         j.body_a = (int)d.body_a;
         j.body_b = (int)d.body_b;
         j.collide_connected = d.collide_connected != 0;

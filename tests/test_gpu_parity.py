@@ -632,3 +632,42 @@ def test_mouse_joints_lockstep(built):
     assert min(r["awake"] for r in recs[60:90]) < n  # free boxes slept before the drags
     st = gpu.get_body_states()
     assert st["position"][held[3], 1] > 3.5  # dragged up to its last target
+
+
+@pytest.mark.gpu
+def test_prismatic_joints_lockstep(built):
+    """Prismatic joints: boxes on slides at several angles to a static body (limits, motors, a
+    locked slide with equal limits, a free slide), a dynamic pair on a motorised slide, and the
+    sliders collide with one another and a falling box; bit-exact every step."""
+    n = 10
+    bodies = b2g.body_defs(n + 1)
+    bodies["allow_sleep"] = 0
+    bodies[1:]["type"] = b2g.DYNAMIC
+    bodies[1:]["position"][:, 0] = np.arange(n) * 1.3 - 6.0
+    bodies[1:]["position"][:, 1] = 3.0 + 0.4 * (np.arange(n) % 3)
+    bodies[1:]["angle"] = 0.1 * np.arange(n)
+    bodies[n]["position"] = (0.2, 8.0)
+    fx = [b2g.edge_fixture(0, (-20.0, 0.0), (20.0, 0.0))]
+    fx += [b2g.box_fixture(i + 1, 0.5, 0.25, density=1.0, friction=0.4) for i in range(n)]
+    joints = []
+    for i in range(n - 3):
+        b = i + 1
+        ang = -0.6 + 0.2 * i
+        p = bodies[b]["position"]
+        limits = [(-1.0, 1.5), None, (0.0, 0.0), (-0.5, 2.0), (-2.0, 0.3), None, (-1.0, 1.0)][i]
+        motor = [None, (1.0, 30.0), None, (-2.0, 50.0), (3.0, 5.0), None, (0.5, 100.0)][i]
+        joints.append(b2g.prismatic_joint(0, b, (float(p[0]), float(p[1])), (0.0, 0.0), (np.cos(ang), np.sin(ang)),
+                                          reference_angle=float(bodies[b]["angle"]), limits=limits, motor=motor))
+    joints.append(b2g.prismatic_joint(n - 2, n - 1, (0.6, 0.0), (-0.6, 0.0), (1.0, 0.5), reference_angle=-0.1,
+                                      limits=(-0.5, 0.8), motor=(-1.5, 20.0)))
+    s = {"name": "prismatic", "bodies": bodies, "fixtures": np.concatenate(fx), "joints": np.concatenate(joints),
+         "gravity": (0.0, -10.0), "dt": np.float32(1.0 / 60.0), "vi": 8, "pi": 3, "steps": 240, "num_worlds": 1,
+         "allow_sleep": False, "n_dynamic": n}
+    recs, gpu, _ = parity.lockstep(s, 240)
+    for r in recs:
+        _assert_step(r)
+        assert r["joint_impulses_equal"], r
+    st = gpu.get_body_states()
+    assert np.all(np.isfinite(st["position"]))
+    locked = st["position"][3] - bodies[3]["position"]
+    assert float(np.abs(locked).max()) < 0.05  # equal limits hold the slide in place
