@@ -179,6 +179,7 @@ JOINT_FRICTION = 9
 JOINT_MOTOR = 11
 JOINT_MOUSE = 5
 JOINT_PRISMATIC = 2
+JOINT_WHEEL = 7
 
 
 def friction_joint(body_a, body_b, anchor_a, anchor_b, max_force, max_torque, collide_connected=False):
@@ -233,6 +234,26 @@ def prismatic_joint(body_a, body_b, anchor_a, anchor_b, axis, reference_angle=0.
     if motor is not None:
         d["enable_motor"] = 1
         d["motor_speed"], d["max_motor_force"] = motor
+    return d
+
+
+def wheel_joint(body_a, body_b, anchor_a, anchor_b, axis, stiffness=0.0, damping=0.0, limits=None, motor=None,
+                collide_connected=False):
+    """B2wheelJointDef: body B rides a spring along `axis` (body A's frame) and spins freely;
+    limits = (lower, upper) translation; motor = (speed, max torque)."""
+    d = np.zeros(1, JOINT_DEF)
+    d["type"] = JOINT_WHEEL
+    d["body_a"], d["body_b"] = body_a, body_b
+    d["collide_connected"] = int(bool(collide_connected))
+    d["local_anchor_a"], d["local_anchor_b"] = anchor_a, anchor_b
+    d["local_axis_a"] = axis
+    d["stiffness"], d["damping"] = stiffness, damping
+    if limits is not None:
+        d["enable_limit"] = 1
+        d["lower_translation"], d["upper_translation"] = limits
+    if motor is not None:
+        d["enable_motor"] = 1
+        d["motor_speed"], d["max_motor_torque"] = motor
     return d
 
 

@@ -745,7 +745,11 @@ int upload_joints(World* w) {
             jb[j] = make_int2((int)jd.body_a, (int)jd.body_b);
             an[j] = make_float4(jd.local_anchor_a.x, jd.local_anchor_a.y, jd.local_anchor_b.x, jd.local_anchor_b.y);
             uint32_t fl = ((uint32_t)jd.type << JF_TYPE_SHIFT) | (jd.collide_connected ? JF_COLLIDE : 0u);
-            if (jd.type == B2G_JOINT_PRISMATIC) {
+            if (jd.type == B2G_JOINT_WHEEL) {
+                lim[j] = make_float4(jd.lower_translation, jd.upper_translation, jd.motor_speed, jd.max_motor_torque);
+                fl |= (jd.enable_limit ? JF_LIMIT : 0u) | (jd.enable_motor ? JF_MOTOR : 0u);
+                par[j] = make_float4(jd.stiffness, __uint_as_float_host(fl), jd.local_axis_a.x, jd.local_axis_a.y);
+            } else if (jd.type == B2G_JOINT_PRISMATIC) {
                 /* B2prismaticJoint::new (private/dynamics/joints/b2_prismatic_joint.rs:54-60): unit axis */
                 V2 ax = mk(jd.local_axis_a.x, jd.local_axis_a.y);
                 normalize(ax);
@@ -1363,8 +1367,8 @@ int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* i
         const b2g_joint_def& d = defs[i];
         if (d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE && d.type != B2G_JOINT_WELD &&
             d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR && d.type != B2G_JOINT_MOUSE &&
-            d.type != B2G_JOINT_PRISMATIC)
-            return fail(w, B2G_ERR_UNSUPPORTED, "only revolute, prismatic, distance, weld, friction, motor "
+            d.type != B2G_JOINT_PRISMATIC && d.type != B2G_JOINT_WHEEL)
+            return fail(w, B2G_ERR_UNSUPPORTED, "only revolute, prismatic, wheel, distance, weld, friction, motor "
                                                 "and mouse joints are on the GPU path");
         if (d.body_a >= w->h_flags.size() || d.body_b >= w->h_flags.size() || d.body_a == d.body_b)
             return fail(w, B2G_ERR_INVALID_ARG, "joint body ids out of range or equal");
@@ -1386,7 +1390,8 @@ int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* i
             w->joints.back().local_anchor_b = b2g_vec2{la.x, la.y};
         }
         w->h_jimp.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
-        w->h_jimp2.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        /* the wheel joint's damping rides in the w slot of its second impulse record */
+        w->h_jimp2.push_back(make_float4(0.0f, 0.0f, 0.0f, defs[i].type == B2G_JOINT_WHEEL ? defs[i].damping : 0.0f));
         if (!defs[i].collide_connected) w->joint_filter_pending = true;
     }
     if (n > 0) w->joints_dirty = true;
@@ -1406,7 +1411,8 @@ int b2g_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) 
     }
     for (uint32_t i = 0; i < count; ++i) {
         const float4 a = w->h_jimp[first + i], b = w->h_jimp2[first + i];
-        if (w->joints[first + i].type != B2G_JOINT_REVOLUTE && w->joints[first + i].type != B2G_JOINT_PRISMATIC) {
+        const int jt = w->joints[first + i].type;
+        if (jt != B2G_JOINT_REVOLUTE && jt != B2G_JOINT_PRISMATIC && jt != B2G_JOINT_WHEEL) {
             out[5 * i + 0] = a.x;
             out[5 * i + 1] = a.y;
             out[5 * i + 2] = a.z;

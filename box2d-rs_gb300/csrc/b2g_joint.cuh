@@ -943,6 +943,245 @@ __device__ bool prismatic_solve_position(const DevWorld& w, int j) {
     return linear_error <= kLinearSlop && angular_error <= kAngularSlop;
 }
 
+/* ---- wheel joint (B2wheelJoint, private/dynamics/joints/b2_wheel_joint.rs:24-398) ----
+ * j_lim = (lower, upper translation, motor speed, max motor torque), j_par = (stiffness, flags, local
+ * axis x, y), j_imp = (impulse, spring, motor, lower), j_imp2 = (upper, translation, -, damping); the
+ * step's ax and ay in j_rr, (s_ax, s_bx, s_ay, s_by) in j_k, (mass, axial mass, spring mass, motor
+ * mass) in j_x, (bias, gamma) in j_s. As the reference does: the warm start does not scale the limit
+ * impulses, and the position pass reuses the step's ax, s_ay and s_by where it says so. */
+
+__device__ void wheel_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 an = w.j_anchor[j];
+    const float4 par = w.j_par[j];
+    const uint32_t jf = __float_as_uint(par.y);
+    const float4 massA = w.b_mass[bd.x], massB = w.b_mass[bd.y];
+    const float2 lcA = w.b_lc[bd.x], lcB = w.b_lc[bd.y];
+    const float mA = massA.y, mB = massB.y, iA = massA.w, iB = massB.w;
+    const float4 pa = w.b_pos[bd.x], pb = w.b_pos[bd.y];
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = rot(pa.z), qB = rot(pb.z);
+    const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+    const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+    const V2 d = sub(sub(add(mk(pb.x, pb.y), rB), mk(pa.x, pa.y)), rA);
+    const V2 xaxis = mk(par.z, par.w);
+    const V2 ay = mul(qA, cross_sv(1.0f, xaxis));
+    const float s_ay = cross(add(d, rA), ay), s_by = cross(rB, ay);
+    float mass = mA + mB + iA * s_ay * s_ay + iB * s_by * s_by;
+    if (mass > 0.0f) mass = fdiv(1.0f, mass);
+    const V2 ax = mul(qA, xaxis);
+    const float s_ax = cross(add(d, rA), ax), s_bx = cross(rB, ax);
+    const float inv_mass = mA + mB + iA * s_ax * s_ax + iB * s_bx * s_bx;
+    const float axial_mass = inv_mass > 0.0f ? fdiv(1.0f, inv_mass) : 0.0f;
+    float4 imp = w.j_imp[j];
+    float4 imp2 = w.j_imp2[j];
+    const float stiffness = par.x, damping = imp2.w;
+    float spring_mass = 0.0f, bias = 0.0f, gamma = 0.0f;
+    if (stiffness > 0.0f && inv_mass > 0.0f) {
+        const float C = dot(d, ax);
+        const float h = sp.dt;
+        gamma = h * (damping + h * stiffness);
+        if (gamma > 0.0f) gamma = fdiv(1.0f, gamma);
+        bias = C * h * stiffness * gamma;
+        spring_mass = inv_mass + gamma;
+        if (spring_mass > 0.0f) spring_mass = fdiv(1.0f, spring_mass);
+    } else {
+        imp.y = 0.0f;
+    }
+    if (jf & JF_LIMIT) {
+        imp2.y = dot(ax, d);
+    } else {
+        imp.w = 0.0f;
+        imp2.x = 0.0f;
+    }
+    float motor_mass = 0.0f;
+    if (jf & JF_MOTOR) {
+        motor_mass = iA + iB;
+        if (motor_mass > 0.0f) motor_mass = fdiv(1.0f, motor_mass);
+    } else {
+        imp.z = 0.0f;
+    }
+    if (sp.warm) {
+        imp.x *= sp.dt_ratio;
+        imp.y *= sp.dt_ratio;
+        imp.z *= sp.dt_ratio;
+        const float axial = imp.y + imp.w - imp2.x;
+        const V2 P = add(scale(imp.x, ay), scale(axial, ax));
+        const float LA = imp.x * s_ay + axial * s_ax + imp.z;
+        const float LB = imp.x * s_by + axial * s_bx + imp.z;
+        vA = sub(vA, scale(mA, P));
+        wA -= iA * LA;
+        vB = add(vB, scale(mB, P));
+        wB += iB * LB;
+    } else {
+        imp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        imp2.x = 0.0f;
+    }
+    w.j_imp[j] = imp;
+    w.j_imp2[j] = imp2;
+    w.j_rr[j] = make_float4(ax.x, ax.y, ay.x, ay.y);
+    w.j_k[j] = make_float4(s_ax, s_bx, s_ay, s_by);
+    w.j_x[j] = make_float4(mass, axial_mass, spring_mass, motor_mass);
+    w.j_m[j] = make_float4(mA, mB, iA, iB);
+    w.j_s[j] = make_float2(bias, gamma);
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+__device__ void wheel_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 lim = w.j_lim[j];
+    const uint32_t jf = __float_as_uint(w.j_par[j].y);
+    const float4 m = w.j_m[j];
+    const float mA = m.x, mB = m.y, iA = m.z, iB = m.w;
+    const float4 rr = w.j_rr[j];
+    const V2 ax = mk(rr.x, rr.y), ay = mk(rr.z, rr.w);
+    const float4 sk = w.j_k[j];
+    const float s_ax = sk.x, s_bx = sk.y, s_ay = sk.z, s_by = sk.w;
+    const float4 ms = w.j_x[j];
+    const float2 bg = w.j_s[j];
+    float4 imp = w.j_imp[j];
+    float4 imp2 = w.j_imp2[j];
+    const float translation = imp2.y;
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    {
+        const float cdot = dot(ax, sub(vB, vA)) + s_bx * wB - s_ax * wA;
+        const float impulse = -ms.z * (cdot + bg.x + bg.y * imp.y);
+        imp.y += impulse;
+        const V2 P = scale(impulse, ax);
+        const float LA = impulse * s_ax, LB = impulse * s_bx;
+        vA = sub(vA, scale(mA, P));
+        wA -= iA * LA;
+        vB = add(vB, scale(mB, P));
+        wB += iB * LB;
+    }
+    {
+        const float cdot = wB - wA - lim.z;
+        float impulse = -ms.w * cdot;
+        const float old_impulse = imp.z;
+        const float max_impulse = sp.dt * lim.w;
+        imp.z = fclampr(imp.z + impulse, -max_impulse, max_impulse);
+        impulse = imp.z - old_impulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    if (jf & JF_LIMIT) {
+        {
+            const float C = translation - lim.x;
+            const float cdot = dot(ax, sub(vB, vA)) + s_bx * wB - s_ax * wA;
+            float impulse = -ms.y * (cdot + fmaxr(C, 0.0f) * sp.inv_dt);
+            const float old_impulse = imp.w;
+            imp.w = fmaxr(imp.w + impulse, 0.0f);
+            impulse = imp.w - old_impulse;
+            const V2 P = scale(impulse, ax);
+            const float LA = impulse * s_ax, LB = impulse * s_bx;
+            vA = sub(vA, scale(mA, P));
+            wA -= iA * LA;
+            vB = add(vB, scale(mB, P));
+            wB += iB * LB;
+        }
+        {
+            const float C = lim.y - translation;
+            const float cdot = dot(ax, sub(vA, vB)) + s_ax * wA - s_bx * wB;
+            float impulse = -ms.y * (cdot + fmaxr(C, 0.0f) * sp.inv_dt);
+            const float old_impulse = imp2.x;
+            imp2.x = fmaxr(imp2.x + impulse, 0.0f);
+            impulse = imp2.x - old_impulse;
+            const V2 P = scale(impulse, ax);
+            const float LA = impulse * s_ax, LB = impulse * s_bx;
+            vA = add(vA, scale(mA, P));
+            wA += iA * LA;
+            vB = sub(vB, scale(mB, P));
+            wB -= iB * LB;
+        }
+    }
+    {
+        const float cdot = dot(ay, sub(vB, vA)) + s_by * wB - s_ay * wA;
+        const float impulse = -ms.x * cdot;
+        imp.x += impulse;
+        const V2 P = scale(impulse, ay);
+        const float LA = impulse * s_ay, LB = impulse * s_by;
+        vA = sub(vA, scale(mA, P));
+        wA -= iA * LA;
+        vB = add(vB, scale(mB, P));
+        wB += iB * LB;
+    }
+    w.j_imp[j] = imp;
+    w.j_imp2[j] = imp2;
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+__device__ bool wheel_solve_position(const DevWorld& w, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 an = w.j_anchor[j];
+    const float4 lim = w.j_lim[j];
+    const float4 par = w.j_par[j];
+    const uint32_t jf = __float_as_uint(par.y);
+    const float4 m = w.j_m[j];
+    const float mA = m.x, mB = m.y, iA = m.z, iB = m.w;
+    const float4 rr = w.j_rr[j];
+    const V2 step_ax = mk(rr.x, rr.y);
+    const float4 sk = w.j_k[j];
+    const float2 lcA = w.b_lc[bd.x], lcB = w.b_lc[bd.y];
+    const float4 pa = w.b_pos[bd.x], pb = w.b_pos[bd.y];
+    V2 cA = mk(pa.x, pa.y), cB = mk(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    const V2 xaxis = mk(par.z, par.w);
+    float linear_error = 0.0f;
+    if (jf & JF_LIMIT) {
+        const Rot qA = rot(aA), qB = rot(aB);
+        const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+        const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+        const V2 d = sub(add(sub(cB, cA), rB), rA);
+        const V2 ax = mul(qA, xaxis);
+        const float s_ax = cross(add(d, rA), step_ax), s_bx = cross(rB, step_ax);
+        float C = 0.0f;
+        const float translation = dot(ax, d);
+        if (fabsr(lim.y - lim.x) < 2.0f * kLinearSlop) C = translation;
+        else if (translation <= lim.x) C = fminr(translation - lim.x, 0.0f);
+        else if (translation >= lim.y) C = fmaxr(translation - lim.y, 0.0f);
+        if (C != 0.0f) {
+            const float inv_mass = mA + mB + iA * s_ax * s_ax + iB * s_bx * s_bx;
+            float impulse = 0.0f;
+            if (inv_mass != 0.0f) impulse = fdiv(-C, inv_mass);
+            const V2 P = scale(impulse, ax);
+            const float LA = impulse * s_ax, LB = impulse * s_bx;
+            cA = sub(cA, scale(mA, P));
+            aA -= iA * LA;
+            cB = add(cB, scale(mB, P));
+            aB += iB * LB;
+            linear_error = fabsr(C);
+        }
+    }
+    {
+        const Rot qA = rot(aA), qB = rot(aB);
+        const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+        const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+        const V2 d = sub(add(sub(cB, cA), rB), rA);
+        const V2 ay = mul(qA, cross_sv(1.0f, xaxis));
+        const float s_ay = cross(add(d, rA), ay), s_by = cross(rB, ay);
+        const float C = dot(d, ay);
+        const float inv_mass = mA + mB + iA * sk.z * sk.z + iB * sk.w * sk.w;
+        float impulse = 0.0f;
+        if (inv_mass != 0.0f) impulse = fdiv(-C, inv_mass);
+        const V2 P = scale(impulse, ay);
+        const float LA = impulse * s_ay, LB = impulse * s_by;
+        cA = sub(cA, scale(mA, P));
+        aA -= iA * LA;
+        cB = add(cB, scale(mB, P));
+        aB += iB * LB;
+        linear_error = fmaxr(linear_error, fabsr(C));
+    }
+    if (joint_body_dynamic(w, bd.x)) w.b_pos[bd.x] = make_float4(cA.x, cA.y, aA, pa.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_pos[bd.y] = make_float4(cB.x, cB.y, aB, pb.w);
+    return linear_error <= kLinearSlop;
+}
+
 __device__ __forceinline__ uint32_t joint_type(const DevWorld& w, int j) {
     return (__float_as_uint(w.j_par[j].y) >> JF_TYPE_SHIFT) & 0xffu;
 }
@@ -1142,6 +1381,7 @@ __device__ __forceinline__ void joint_init_velocity(const DevWorld& w, const Ste
     else if (t == B2G_JOINT_MOTOR) motor_init_velocity(w, sp, j);
     else if (t == B2G_JOINT_MOUSE) mouse_init_velocity(w, sp, j);
     else if (t == B2G_JOINT_PRISMATIC) prismatic_init_velocity(w, sp, j);
+    else if (t == B2G_JOINT_WHEEL) wheel_init_velocity(w, sp, j);
     else revolute_init_velocity(w, sp, j);
 }
 __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
@@ -1152,6 +1392,7 @@ __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const St
     else if (t == B2G_JOINT_MOTOR) motor_solve_velocity(w, sp, j);
     else if (t == B2G_JOINT_MOUSE) mouse_solve_velocity(w, sp, j);
     else if (t == B2G_JOINT_PRISMATIC) prismatic_solve_velocity(w, sp, j);
+    else if (t == B2G_JOINT_WHEEL) wheel_solve_velocity(w, sp, j);
     else revolute_solve_velocity(w, sp, j);
 }
 __device__ __forceinline__ bool joint_solve_position(const DevWorld& w, int j) {
@@ -1160,6 +1401,7 @@ __device__ __forceinline__ bool joint_solve_position(const DevWorld& w, int j) {
     if (t == B2G_JOINT_WELD) return weld_solve_position(w, j);
     if (t == B2G_JOINT_FRICTION || t == B2G_JOINT_MOTOR || t == B2G_JOINT_MOUSE) return true;
     if (t == B2G_JOINT_PRISMATIC) return prismatic_solve_position(w, j);
+    if (t == B2G_JOINT_WHEEL) return wheel_solve_position(w, j);
     return revolute_solve_position(w, j);
 }
 

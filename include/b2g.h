@@ -127,6 +127,8 @@ typedef struct b2g_fixture_def {
  *   B2G_JOINT_PRISMATIC: B2prismaticJointDef (src/joints/b2_prismatic_joint.rs): local axis in body A
  *     (normalized at creation), reference angle, limit (enable_limit, lower/upper translation), motor
  *     (enable_motor, motor_speed, max_motor_force)
+ *   B2G_JOINT_WHEEL: B2wheelJointDef (src/joints/b2_wheel_joint.rs): local axis in body A (used as given),
+ *     suspension spring (stiffness, damping), limit (lower/upper translation), motor (speed, max torque)
  * The type numbers follow Box2D's C++ b2JointType. */
 #define B2G_JOINT_REVOLUTE 1
 #define B2G_JOINT_DISTANCE 3
@@ -134,6 +136,7 @@ typedef struct b2g_fixture_def {
 #define B2G_JOINT_FRICTION 9
 #define B2G_JOINT_PRISMATIC 2
 #define B2G_JOINT_MOUSE 5
+#define B2G_JOINT_WHEEL 7
 #define B2G_JOINT_MOTOR 11
 typedef struct b2g_joint_def {
     int32_t type;              /* B2G_JOINT_* */
@@ -210,7 +213,7 @@ int b2g_create_fixtures(void* world, const b2g_fixture_def* defs, int32_t n, uin
  * A world with joints runs the grid-wide colour schedule (no part-local solve) and cannot be taped. */
 int b2g_create_joints(void* world, const b2g_joint_def* defs, int32_t n, uint32_t* out_ids);
 /* Accumulated joint impulses (for warm starting), 5 per joint: revolute x, y, motor, lower, upper;
- * prismatic x, y, motor, lower, upper; distance impulse, lower, upper, 0, 0; weld, friction and motor x, y,
+ * prismatic x, y, motor, lower, upper; wheel impulse, spring, motor, lower, upper; distance impulse, lower, upper, 0, 0; weld, friction and motor x, y,
  * angular, 0, 0; mouse x, y, 0, 0, 0 */
 int b2g_get_joint_impulses(void* world, uint32_t first, uint32_t count, float* out);
 /* B2mouseJoint::set_target (src/joints/b2_mouse_joint.rs:114-119): a new target wakes body B */

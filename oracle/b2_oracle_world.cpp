@@ -120,6 +120,9 @@ struct Joint {
     Vec2 local_xaxis_a{1, 0}, local_yaxis_a{0, 1}, axis{0, 0}, perp{0, 0};
     float a1 = 0, a2 = 0, s1 = 0, s2 = 0, translation = 0;
     float lower_translation = 0, upper_translation = 0, max_motor_force = 0;
+    /* B2wheelJoint (private/dynamics/joints/b2_wheel_joint.rs): ax, ay in axis, perp; s_ax, s_bx in a1, a2;
+     * s_ay, s_by in s1, s2; shares the motor and limit impulses, axial mass, bias and gamma */
+    float wheel_impulse = 0, spring_impulse = 0, wheel_mass = 0, spring_mass = 0, motor_mass = 0;
     float weld_mass[9] = {0};  /* ex, ey, ez columns */
     bool collide_connected = false, island_flag = false;
     Vec2 local_anchor_a{0, 0}, local_anchor_b{0, 0};
@@ -1766,6 +1769,225 @@ static bool prismatic_solve_position(World& w, Joint& j) {
     return linear_error <= kLinearSlop && angular_error <= kAngularSlop;
 }
 
+/* ---- wheel joint, private/dynamics/joints/b2_wheel_joint.rs:24-398 ---- */
+
+static void wheel_init_velocity(World& w, Joint& j, const Step& step) {
+    const Body& A = w.bodies[j.body_a];
+    const Body& B = w.bodies[j.body_b];
+    j.index_a = A.island_index;
+    j.index_b = B.island_index;
+    j.lc_a = A.sweep.local_center;
+    j.lc_b = B.sweep.local_center;
+    j.inv_mass_a = A.inv_mass;
+    j.inv_mass_b = B.inv_mass;
+    j.inv_ia = A.inv_I;
+    j.inv_ib = B.inv_I;
+    const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+    const Vec2 cA = w.pos[j.index_a].c, cB = w.pos[j.index_b].c;
+    const float aA = w.pos[j.index_a].a, aB = w.pos[j.index_b].a;
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const Rot qA = rot(aA), qB = rot(aB);
+    const Vec2 rA = mul(qA, j.local_anchor_a - j.lc_a);
+    const Vec2 rB = mul(qB, j.local_anchor_b - j.lc_b);
+    const Vec2 d = cB + rB - cA - rA;
+    j.perp = mul(qA, j.local_yaxis_a);
+    j.s1 = cross(d + rA, j.perp);
+    j.s2 = cross(rB, j.perp);
+    j.wheel_mass = mA + mB + iA * j.s1 * j.s1 + iB * j.s2 * j.s2;
+    if (j.wheel_mass > 0.0f) j.wheel_mass = 1.0f / j.wheel_mass;
+    j.axis = mul(qA, j.local_xaxis_a);
+    j.a1 = cross(d + rA, j.axis);
+    j.a2 = cross(rB, j.axis);
+    const float inv_mass = mA + mB + iA * j.a1 * j.a1 + iB * j.a2 * j.a2;
+    j.axial_mass = inv_mass > 0.0f ? 1.0f / inv_mass : 0.0f;
+    j.spring_mass = 0.0f;
+    j.bias = 0.0f;
+    j.gamma = 0.0f;
+    if (j.stiffness > 0.0f && inv_mass > 0.0f) {
+        j.spring_mass = 1.0f / inv_mass;
+        const float C = dot(d, j.axis);
+        const float h = step.dt;
+        j.gamma = h * (j.damping + h * j.stiffness);
+        if (j.gamma > 0.0f) j.gamma = 1.0f / j.gamma;
+        j.bias = C * h * j.stiffness * j.gamma;
+        j.spring_mass = inv_mass + j.gamma;
+        if (j.spring_mass > 0.0f) j.spring_mass = 1.0f / j.spring_mass;
+    } else {
+        j.spring_impulse = 0.0f;
+    }
+    if (j.enable_limit) {
+        j.translation = dot(j.axis, d);
+    } else {
+        j.lower_impulse = 0.0f;
+        j.upper_impulse = 0.0f;
+    }
+    if (j.enable_motor) {
+        j.motor_mass = iA + iB;
+        if (j.motor_mass > 0.0f) j.motor_mass = 1.0f / j.motor_mass;
+    } else {
+        j.motor_mass = 0.0f;
+        j.motor_impulse = 0.0f;
+    }
+    if (step.warm) {
+        j.wheel_impulse *= step.dt_ratio;
+        j.spring_impulse *= step.dt_ratio;
+        j.motor_impulse *= step.dt_ratio;
+        const float axial = j.spring_impulse + j.lower_impulse - j.upper_impulse;
+        const Vec2 P = j.wheel_impulse * j.perp + axial * j.axis;
+        const float LA = j.wheel_impulse * j.s1 + axial * j.a1 + j.motor_impulse;
+        const float LB = j.wheel_impulse * j.s2 + axial * j.a2 + j.motor_impulse;
+        vA -= mA * P;
+        wA -= iA * LA;
+        vB += mB * P;
+        wB += iB * LB;
+    } else {
+        j.wheel_impulse = 0.0f;
+        j.spring_impulse = 0.0f;
+        j.motor_impulse = 0.0f;
+        j.lower_impulse = 0.0f;
+        j.upper_impulse = 0.0f;
+    }
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+static void wheel_solve_velocity(World& w, Joint& j, const Step& step) {
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+    {
+        const float cdot = dot(j.axis, vB - vA) + j.a2 * wB - j.a1 * wA;
+        const float impulse = -j.spring_mass * (cdot + j.bias + j.gamma * j.spring_impulse);
+        j.spring_impulse += impulse;
+        const Vec2 P = impulse * j.axis;
+        const float LA = impulse * j.a1, LB = impulse * j.a2;
+        vA -= mA * P;
+        wA -= iA * LA;
+        vB += mB * P;
+        wB += iB * LB;
+    }
+    {
+        const float cdot = wB - wA - j.motor_speed;
+        float impulse = -j.motor_mass * cdot;
+        const float old_impulse = j.motor_impulse;
+        const float max_impulse = step.dt * j.max_motor_torque;
+        j.motor_impulse = bclamp(j.motor_impulse + impulse, -max_impulse, max_impulse);
+        impulse = j.motor_impulse - old_impulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    if (j.enable_limit) {
+        {
+            const float C = j.translation - j.lower_translation;
+            const float cdot = dot(j.axis, vB - vA) + j.a2 * wB - j.a1 * wA;
+            float impulse = -j.axial_mass * (cdot + bmax(C, 0.0f) * step.inv_dt);
+            const float old_impulse = j.lower_impulse;
+            j.lower_impulse = bmax(j.lower_impulse + impulse, 0.0f);
+            impulse = j.lower_impulse - old_impulse;
+            const Vec2 P = impulse * j.axis;
+            const float LA = impulse * j.a1, LB = impulse * j.a2;
+            vA -= mA * P;
+            wA -= iA * LA;
+            vB += mB * P;
+            wB += iB * LB;
+        }
+        {
+            const float C = j.upper_translation - j.translation;
+            const float cdot = dot(j.axis, vA - vB) + j.a1 * wA - j.a2 * wB;
+            float impulse = -j.axial_mass * (cdot + bmax(C, 0.0f) * step.inv_dt);
+            const float old_impulse = j.upper_impulse;
+            j.upper_impulse = bmax(j.upper_impulse + impulse, 0.0f);
+            impulse = j.upper_impulse - old_impulse;
+            const Vec2 P = impulse * j.axis;
+            const float LA = impulse * j.a1, LB = impulse * j.a2;
+            vA += mA * P;
+            wA += iA * LA;
+            vB -= mB * P;
+            wB -= iB * LB;
+        }
+    }
+    {
+        const float cdot = dot(j.perp, vB - vA) + j.s2 * wB - j.s1 * wA;
+        const float impulse = -j.wheel_mass * cdot;
+        j.wheel_impulse += impulse;
+        const Vec2 P = impulse * j.perp;
+        const float LA = impulse * j.s1, LB = impulse * j.s2;
+        vA -= mA * P;
+        wA -= iA * LA;
+        vB += mB * P;
+        wB += iB * LB;
+    }
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+static bool wheel_solve_position(World& w, Joint& j) {
+    Vec2 cA = w.pos[j.index_a].c;
+    float aA = w.pos[j.index_a].a;
+    Vec2 cB = w.pos[j.index_b].c;
+    float aB = w.pos[j.index_b].a;
+    const float mA = j.inv_mass_a, mB = j.inv_mass_b, iA = j.inv_ia, iB = j.inv_ib;
+    float linear_error = 0.0f;
+    if (j.enable_limit) {
+        const Rot qA = rot(aA), qB = rot(aB);
+        const Vec2 rA = mul(qA, j.local_anchor_a - j.lc_a);
+        const Vec2 rB = mul(qB, j.local_anchor_b - j.lc_b);
+        const Vec2 d = (cB - cA) + rB - rA;
+        const Vec2 ax = mul(qA, j.local_xaxis_a);
+        const float s_ax = cross(d + rA, j.axis), s_bx = cross(rB, j.axis);
+        float C = 0.0f;
+        const float translation = dot(ax, d);
+        if (std::fabs(j.upper_translation - j.lower_translation) < 2.0f * kLinearSlop) C = translation;
+        else if (translation <= j.lower_translation) C = bmin(translation - j.lower_translation, 0.0f);
+        else if (translation >= j.upper_translation) C = bmax(translation - j.upper_translation, 0.0f);
+        if (C != 0.0f) {
+            const float inv_mass = mA + mB + iA * s_ax * s_ax + iB * s_bx * s_bx;
+            float impulse = 0.0f;
+            if (inv_mass != 0.0f) impulse = -C / inv_mass;
+            const Vec2 P = impulse * ax;
+            const float LA = impulse * s_ax, LB = impulse * s_bx;
+            cA -= mA * P;
+            aA -= iA * LA;
+            cB += mB * P;
+            aB += iB * LB;
+            linear_error = std::fabs(C);
+        }
+    }
+    {
+        const Rot qA = rot(aA), qB = rot(aB);
+        const Vec2 rA = mul(qA, j.local_anchor_a - j.lc_a);
+        const Vec2 rB = mul(qB, j.local_anchor_b - j.lc_b);
+        const Vec2 d = (cB - cA) + rB - rA;
+        const Vec2 ay = mul(qA, j.local_yaxis_a);
+        const float s_ay = cross(d + rA, ay), s_by = cross(rB, ay);
+        const float C = dot(d, ay);
+        const float inv_mass = mA + mB + iA * j.s1 * j.s1 + iB * j.s2 * j.s2;
+        float impulse = 0.0f;
+        if (inv_mass != 0.0f) impulse = -C / inv_mass;
+        const Vec2 P = impulse * ay;
+        const float LA = impulse * s_ay, LB = impulse * s_by;
+        cA -= mA * P;
+        aA -= iA * LA;
+        cB += mB * P;
+        aB += iB * LB;
+        linear_error = bmax(linear_error, std::fabs(C));
+    }
+    w.pos[j.index_a].c = cA;
+    w.pos[j.index_a].a = aA;
+    w.pos[j.index_b].c = cB;
+    w.pos[j.index_b].a = aB;
+    return linear_error <= kLinearSlop;
+}
+
 /* init_velocity_constraints (:21-116): anchors, effective masses, warm start */
 static void joint_init_velocity(World& w, Joint& j, const Step& step) {
     if (j.type == B2G_JOINT_MOTOR) {
@@ -1778,6 +2000,10 @@ static void joint_init_velocity(World& w, Joint& j, const Step& step) {
     }
     if (j.type == B2G_JOINT_PRISMATIC) {
         prismatic_init_velocity(w, j, step);
+        return;
+    }
+    if (j.type == B2G_JOINT_WHEEL) {
+        wheel_init_velocity(w, j, step);
         return;
     }
     if (j.type == B2G_JOINT_FRICTION) {
@@ -1867,6 +2093,10 @@ static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
         prismatic_solve_velocity(w, j, step);
         return;
     }
+    if (j.type == B2G_JOINT_WHEEL) {
+        wheel_solve_velocity(w, j, step);
+        return;
+    }
     if (j.type == B2G_JOINT_FRICTION) {
         friction_solve_velocity(w, j, step);
         return;
@@ -1940,6 +2170,7 @@ static bool joint_solve_position(World& w, Joint& j) {
     /* b2_friction_joint.rs, b2_motor_joint.rs and b2_mouse_joint.rs: no position correction */
     if (j.type == B2G_JOINT_FRICTION || j.type == B2G_JOINT_MOTOR || j.type == B2G_JOINT_MOUSE) return true;
     if (j.type == B2G_JOINT_PRISMATIC) return prismatic_solve_position(w, j);
+    if (j.type == B2G_JOINT_WHEEL) return wheel_solve_position(w, j);
     Vec2 cA = w.pos[j.index_a].c;
     float aA = w.pos[j.index_a].a;
     Vec2 cB = w.pos[j.index_b].c;
@@ -2733,7 +2964,7 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
         const b2g_joint_def& d = defs[i];
         if ((d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE && d.type != B2G_JOINT_WELD &&
              d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR && d.type != B2G_JOINT_MOUSE &&
-             d.type != B2G_JOINT_PRISMATIC) ||
+             d.type != B2G_JOINT_PRISMATIC && d.type != B2G_JOINT_WHEEL) ||
             d.body_a >= w.bodies.size() ||
             d.body_b >= w.bodies.size())
             return -1;
@@ -2759,6 +2990,10 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
         j.lower_translation = d.lower_translation;
         j.upper_translation = d.upper_translation;
         j.max_motor_force = d.max_motor_force;
+        if (j.type == B2G_JOINT_WHEEL) {  /* b2_wheel_joint.rs:334-335: the axis as given */
+            j.local_xaxis_a = v2(d.local_axis_a.x, d.local_axis_a.y);
+            j.local_yaxis_a = cross_sv(1.0f, j.local_xaxis_a);
+        }
         j.body_a = (int)d.body_a;
         j.body_b = (int)d.body_b;
         j.collide_connected = d.collide_connected != 0;
@@ -2796,6 +3031,14 @@ int ora_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) 
     if ((size_t)first + count > w.joints.size()) return -1;
     for (uint32_t i = 0; i < count; ++i) {
         const Joint& j = w.joints[first + i];
+        if (j.type == B2G_JOINT_WHEEL) {
+            out[5 * i + 0] = j.wheel_impulse;
+            out[5 * i + 1] = j.spring_impulse;
+            out[5 * i + 2] = j.motor_impulse;
+            out[5 * i + 3] = j.lower_impulse;
+            out[5 * i + 4] = j.upper_impulse;
+            continue;
+        }
         if (j.type == B2G_JOINT_FRICTION || j.type == B2G_JOINT_MOTOR || j.type == B2G_JOINT_MOUSE) {
             out[5 * i + 0] = j.linear_impulse.x;
             out[5 * i + 1] = j.linear_impulse.y;

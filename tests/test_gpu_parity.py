@@ -671,3 +671,40 @@ def test_prismatic_joints_lockstep(built):
     assert np.all(np.isfinite(st["position"]))
     locked = st["position"][3] - bodies[3]["position"]
     assert float(np.abs(locked).max()) < 0.05  # equal limits hold the slide in place
+
+
+@pytest.mark.gpu
+def test_wheel_joints_lockstep(built):
+    """Wheel joints: two cars (a chassis on two sprung wheels, rear wheel motorised, one car with
+    suspension limits and an axis not of unit length) drive over bumps and into each other; bit-exact
+    bodies and joint impulses every step."""
+    bodies = b2g.body_defs(7)
+    bodies["allow_sleep"] = 0
+    bodies[1:]["type"] = b2g.DYNAMIC
+    pos = [(-6.0, 1.2), (-7.0, 0.6), (-5.0, 0.6), (6.0, 1.3), (5.0, 0.65), (7.0, 0.65)]
+    for i, p in enumerate(pos):
+        bodies[i + 1]["position"] = p
+    fx = [b2g.edge_fixture(0, (-20.0, 0.0), (-2.0, 0.0)), b2g.edge_fixture(0, (-2.0, 0.0), (-1.0, 0.3)),
+          b2g.edge_fixture(0, (-1.0, 0.3), (1.0, 0.0)), b2g.edge_fixture(0, (1.0, 0.0), (20.0, 0.0))]
+    for c in (1, 4):
+        fx.append(b2g.box_fixture(c, 1.5, 0.25, density=1.0, friction=0.4))
+        fx.append(b2g.circle_fixture(c + 1, 0.4, density=1.0, friction=0.9))
+        fx.append(b2g.circle_fixture(c + 2, 0.4, density=1.0, friction=0.9))
+    joints = [
+        b2g.wheel_joint(1, 2, (-1.0, -0.6), (0.0, 0.0), (0.0, 1.0), stiffness=40.0, damping=2.0, motor=(-12.0, 40.0)),
+        b2g.wheel_joint(1, 3, (1.0, -0.6), (0.0, 0.0), (0.0, 1.0), stiffness=40.0, damping=2.0),
+        b2g.wheel_joint(4, 5, (-1.0, -0.65), (0.0, 0.0), (0.3, 1.2), stiffness=25.0, damping=1.0,
+                        limits=(-0.15, 0.1)),
+        b2g.wheel_joint(4, 6, (1.0, -0.65), (0.0, 0.0), (0.0, 1.0), stiffness=25.0, damping=1.0, limits=(-0.15, 0.1),
+                        motor=(10.0, 30.0)),
+    ]
+    s = {"name": "wheel", "bodies": bodies, "fixtures": np.concatenate(fx), "joints": np.concatenate(joints),
+         "gravity": (0.0, -10.0), "dt": np.float32(1.0 / 60.0), "vi": 8, "pi": 3, "steps": 240, "num_worlds": 1,
+         "allow_sleep": False, "n_dynamic": 6}
+    recs, gpu, _ = parity.lockstep(s, 240)
+    for r in recs:
+        _assert_step(r)
+        assert r["joint_impulses_equal"], r
+    st = gpu.get_body_states()
+    assert np.all(np.isfinite(st["position"]))
+    assert float(st["position"][1, 0]) > -6.0  # the motorised car moved forward
