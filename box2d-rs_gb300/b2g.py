@@ -171,6 +171,11 @@ JOINT_DEF = np.dtype(
         ("lower_translation", "<f4"),
         ("upper_translation", "<f4"),
         ("max_motor_force", "<f4"),
+        ("ground_anchor_a", "<f4", (2,)),
+        ("ground_anchor_b", "<f4", (2,)),
+        ("length_a", "<f4"),
+        ("length_b", "<f4"),
+        ("ratio", "<f4"),
     ]
 )
 JOINT_DISTANCE = 3
@@ -180,6 +185,7 @@ JOINT_MOTOR = 11
 JOINT_MOUSE = 5
 JOINT_PRISMATIC = 2
 JOINT_WHEEL = 7
+JOINT_PULLEY = 4
 
 
 def friction_joint(body_a, body_b, anchor_a, anchor_b, max_force, max_torque, collide_connected=False):
@@ -254,6 +260,20 @@ def wheel_joint(body_a, body_b, anchor_a, anchor_b, axis, stiffness=0.0, damping
     if motor is not None:
         d["enable_motor"] = 1
         d["motor_speed"], d["max_motor_torque"] = motor
+    return d
+
+
+def pulley_joint(body_a, body_b, ground_a, ground_b, anchor_a, anchor_b, length_a, length_b, ratio=1.0,
+                 collide_connected=True):
+    """B2pulleyJointDef: ropes from world ground anchors to local anchors on each body, with
+    length_a + ratio * length_b held constant."""
+    d = np.zeros(1, JOINT_DEF)
+    d["type"] = JOINT_PULLEY
+    d["body_a"], d["body_b"] = body_a, body_b
+    d["collide_connected"] = int(bool(collide_connected))
+    d["local_anchor_a"], d["local_anchor_b"] = anchor_a, anchor_b
+    d["ground_anchor_a"], d["ground_anchor_b"] = ground_a, ground_b
+    d["length_a"], d["length_b"], d["ratio"] = length_a, length_b, ratio
     return d
 
 

@@ -745,7 +745,11 @@ int upload_joints(World* w) {
             jb[j] = make_int2((int)jd.body_a, (int)jd.body_b);
             an[j] = make_float4(jd.local_anchor_a.x, jd.local_anchor_a.y, jd.local_anchor_b.x, jd.local_anchor_b.y);
             uint32_t fl = ((uint32_t)jd.type << JF_TYPE_SHIFT) | (jd.collide_connected ? JF_COLLIDE : 0u);
-            if (jd.type == B2G_JOINT_WHEEL) {
+            if (jd.type == B2G_JOINT_PULLEY) {
+                /* the constant length_a + ratio * length_b (b2_pulley_joint.rs:33) is formed on the device */
+                lim[j] = make_float4(jd.ground_anchor_a.x, jd.ground_anchor_a.y, jd.ground_anchor_b.x, jd.ground_anchor_b.y);
+                par[j] = make_float4(jd.ratio, __uint_as_float_host(fl), jd.length_a, jd.length_b);
+            } else if (jd.type == B2G_JOINT_WHEEL) {
                 lim[j] = make_float4(jd.lower_translation, jd.upper_translation, jd.motor_speed, jd.max_motor_torque);
                 fl |= (jd.enable_limit ? JF_LIMIT : 0u) | (jd.enable_motor ? JF_MOTOR : 0u);
                 par[j] = make_float4(jd.stiffness, __uint_as_float_host(fl), jd.local_axis_a.x, jd.local_axis_a.y);
@@ -1367,9 +1371,8 @@ int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* i
         const b2g_joint_def& d = defs[i];
         if (d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE && d.type != B2G_JOINT_WELD &&
             d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR && d.type != B2G_JOINT_MOUSE &&
-            d.type != B2G_JOINT_PRISMATIC && d.type != B2G_JOINT_WHEEL)
-            return fail(w, B2G_ERR_UNSUPPORTED, "only revolute, prismatic, wheel, distance, weld, friction, motor "
-                                                "and mouse joints are on the GPU path");
+            d.type != B2G_JOINT_PRISMATIC && d.type != B2G_JOINT_WHEEL && d.type != B2G_JOINT_PULLEY)
+            return fail(w, B2G_ERR_UNSUPPORTED, "the gear joint is not on the GPU path");
         if (d.body_a >= w->h_flags.size() || d.body_b >= w->h_flags.size() || d.body_a == d.body_b)
             return fail(w, B2G_ERR_INVALID_ARG, "joint body ids out of range or equal");
     }

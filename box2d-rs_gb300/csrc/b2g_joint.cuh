@@ -1182,6 +1182,131 @@ __device__ bool wheel_solve_position(const DevWorld& w, int j) {
     return linear_error <= kLinearSlop;
 }
 
+/* ---- pulley joint (B2pulleyJoint, private/dynamics/joints/b2_pulley_joint.rs) ----
+ * j_lim = (ground anchor A x, y, ground anchor B x, y), j_par = (ratio, flags, length A, length B), j_imp.x =
+ * impulse; the step's r_a, r_b in j_rr, u_a, u_b in j_k, mass in j_s.x. */
+
+struct PulleyFrame {
+    V2 rA, rB, uA, uB;
+    float lenA, lenB, mass;
+};
+
+__device__ __forceinline__ PulleyFrame pulley_frame(const DevWorld& w, int j, V2 cA, float aA, V2 cB, float aB,
+                                                    float mA, float mB, float iA, float iB) {
+    const int2 bd = w.j_body[j];
+    const float4 an = w.j_anchor[j];
+    const float4 g = w.j_lim[j];
+    const float ratio = w.j_par[j].x;
+    const float2 lcA = w.b_lc[bd.x], lcB = w.b_lc[bd.y];
+    PulleyFrame f;
+    f.rA = mul(rot(aA), sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+    f.rB = mul(rot(aB), sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+    f.uA = sub(add(cA, f.rA), mk(g.x, g.y));
+    f.uB = sub(add(cB, f.rB), mk(g.z, g.w));
+    f.lenA = length(f.uA);
+    f.lenB = length(f.uB);
+    if (f.lenA > 10.0f * kLinearSlop) {
+        const float s = fdiv(1.0f, f.lenA);
+        f.uA = mk(f.uA.x * s, f.uA.y * s);
+    } else {
+        f.uA = mk(0.0f, 0.0f);
+    }
+    if (f.lenB > 10.0f * kLinearSlop) {
+        const float s = fdiv(1.0f, f.lenB);
+        f.uB = mk(f.uB.x * s, f.uB.y * s);
+    } else {
+        f.uB = mk(0.0f, 0.0f);
+    }
+    const float ruA = cross(f.rA, f.uA), ruB = cross(f.rB, f.uB);
+    const float mAe = mA + iA * ruA * ruA, mBe = mB + iB * ruB * ruB;
+    f.mass = mAe + ratio * ratio * mBe;
+    if (f.mass > 0.0f) f.mass = fdiv(1.0f, f.mass);
+    return f;
+}
+
+__device__ void pulley_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 bd = w.j_body[j];
+    const float ratio = w.j_par[j].x;
+    const float4 massA = w.b_mass[bd.x], massB = w.b_mass[bd.y];
+    const float mA = massA.y, mB = massB.y, iA = massA.w, iB = massB.w;
+    const float4 pa = w.b_pos[bd.x], pb = w.b_pos[bd.y];
+    const PulleyFrame f = pulley_frame(w, j, mk(pa.x, pa.y), pa.z, mk(pb.x, pb.y), pb.z, mA, mB, iA, iB);
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    float4 imp = w.j_imp[j];
+    if (sp.warm) {
+        imp.x *= sp.dt_ratio;
+        const V2 PA = scale(-imp.x, f.uA);
+        const V2 PB = scale(-ratio * imp.x, f.uB);
+        vA = add(vA, scale(mA, PA));
+        wA += iA * cross(f.rA, PA);
+        vB = add(vB, scale(mB, PB));
+        wB += iB * cross(f.rB, PB);
+    } else {
+        imp.x = 0.0f;
+    }
+    w.j_imp[j] = imp;
+    w.j_rr[j] = make_float4(f.rA.x, f.rA.y, f.rB.x, f.rB.y);
+    w.j_k[j] = make_float4(f.uA.x, f.uA.y, f.uB.x, f.uB.y);
+    w.j_m[j] = make_float4(mA, mB, iA, iB);
+    w.j_s[j] = make_float2(f.mass, 0.0f);
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+__device__ void pulley_solve_velocity(const DevWorld& w, int j) {
+    const int2 bd = w.j_body[j];
+    const float ratio = w.j_par[j].x;
+    const float4 m = w.j_m[j];
+    const float mA = m.x, mB = m.y, iA = m.z, iB = m.w;
+    const float4 rr = w.j_rr[j], uu = w.j_k[j];
+    const V2 rA = mk(rr.x, rr.y), rB = mk(rr.z, rr.w), uA = mk(uu.x, uu.y), uB = mk(uu.z, uu.w);
+    const float mass = w.j_s[j].x;
+    float4 imp = w.j_imp[j];
+    float4 va = w.b_vel[bd.x], vb = w.b_vel[bd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const V2 vpA = add(vA, cross_sv(wA, rA)), vpB = add(vB, cross_sv(wB, rB));
+    const float cdot = -dot(uA, vpA) - ratio * dot(uB, vpB);
+    const float impulse = -mass * cdot;
+    imp.x += impulse;
+    const V2 PA = scale(-impulse, uA);
+    const V2 PB = scale(-ratio * impulse, uB);
+    vA = add(vA, scale(mA, PA));
+    wA += iA * cross(rA, PA);
+    vB = add(vB, scale(mB, PB));
+    wB += iB * cross(rB, PB);
+    w.j_imp[j] = imp;
+    if (joint_body_dynamic(w, bd.x)) w.b_vel[bd.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_vel[bd.y] = make_float4(vB.x, vB.y, wB, vb.w);
+}
+
+__device__ bool pulley_solve_position(const DevWorld& w, int j) {
+    const int2 bd = w.j_body[j];
+    const float4 par = w.j_par[j];
+    const float ratio = par.x;
+    const float4 m = w.j_m[j];
+    const float mA = m.x, mB = m.y, iA = m.z, iB = m.w;
+    const float4 pa = w.b_pos[bd.x], pb = w.b_pos[bd.y];
+    V2 cA = mk(pa.x, pa.y), cB = mk(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    const PulleyFrame f = pulley_frame(w, j, cA, aA, cB, aB, mA, mB, iA, iB);
+    const float constant = par.z + ratio * par.w;
+    const float C = constant - f.lenA - ratio * f.lenB;
+    const float linear_error = fabsr(C);
+    const float impulse = -f.mass * C;
+    const V2 PA = scale(-impulse, f.uA);
+    const V2 PB = scale(-ratio * impulse, f.uB);
+    cA = add(cA, scale(mA, PA));
+    aA += iA * cross(f.rA, PA);
+    cB = add(cB, scale(mB, PB));
+    aB += iB * cross(f.rB, PB);
+    if (joint_body_dynamic(w, bd.x)) w.b_pos[bd.x] = make_float4(cA.x, cA.y, aA, pa.w);
+    if (joint_body_dynamic(w, bd.y)) w.b_pos[bd.y] = make_float4(cB.x, cB.y, aB, pb.w);
+    return linear_error < kLinearSlop;
+}
+
 __device__ __forceinline__ uint32_t joint_type(const DevWorld& w, int j) {
     return (__float_as_uint(w.j_par[j].y) >> JF_TYPE_SHIFT) & 0xffu;
 }
@@ -1382,6 +1507,7 @@ __device__ __forceinline__ void joint_init_velocity(const DevWorld& w, const Ste
     else if (t == B2G_JOINT_MOUSE) mouse_init_velocity(w, sp, j);
     else if (t == B2G_JOINT_PRISMATIC) prismatic_init_velocity(w, sp, j);
     else if (t == B2G_JOINT_WHEEL) wheel_init_velocity(w, sp, j);
+    else if (t == B2G_JOINT_PULLEY) pulley_init_velocity(w, sp, j);
     else revolute_init_velocity(w, sp, j);
 }
 __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
@@ -1393,6 +1519,7 @@ __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const St
     else if (t == B2G_JOINT_MOUSE) mouse_solve_velocity(w, sp, j);
     else if (t == B2G_JOINT_PRISMATIC) prismatic_solve_velocity(w, sp, j);
     else if (t == B2G_JOINT_WHEEL) wheel_solve_velocity(w, sp, j);
+    else if (t == B2G_JOINT_PULLEY) pulley_solve_velocity(w, j);
     else revolute_solve_velocity(w, sp, j);
 }
 __device__ __forceinline__ bool joint_solve_position(const DevWorld& w, int j) {
@@ -1402,6 +1529,7 @@ __device__ __forceinline__ bool joint_solve_position(const DevWorld& w, int j) {
     if (t == B2G_JOINT_FRICTION || t == B2G_JOINT_MOTOR || t == B2G_JOINT_MOUSE) return true;
     if (t == B2G_JOINT_PRISMATIC) return prismatic_solve_position(w, j);
     if (t == B2G_JOINT_WHEEL) return wheel_solve_position(w, j);
+    if (t == B2G_JOINT_PULLEY) return pulley_solve_position(w, j);
     return revolute_solve_position(w, j);
 }
 

@@ -129,12 +129,15 @@ typedef struct b2g_fixture_def {
  *     (enable_motor, motor_speed, max_motor_force)
  *   B2G_JOINT_WHEEL: B2wheelJointDef (src/joints/b2_wheel_joint.rs): local axis in body A (used as given),
  *     suspension spring (stiffness, damping), limit (lower/upper translation), motor (speed, max torque)
+ *   B2G_JOINT_PULLEY: B2pulleyJointDef (src/joints/b2_pulley_joint.rs): ground anchors (world), rope
+ *     lengths at rest, ratio (length_a + ratio * length_b stays constant)
  * The type numbers follow Box2D's C++ b2JointType. */
 #define B2G_JOINT_REVOLUTE 1
 #define B2G_JOINT_DISTANCE 3
 #define B2G_JOINT_WELD 8
 #define B2G_JOINT_FRICTION 9
 #define B2G_JOINT_PRISMATIC 2
+#define B2G_JOINT_PULLEY 4
 #define B2G_JOINT_MOUSE 5
 #define B2G_JOINT_WHEEL 7
 #define B2G_JOINT_MOTOR 11
@@ -155,6 +158,8 @@ typedef struct b2g_joint_def {
     b2g_vec2 target;
     b2g_vec2 local_axis_a;
     float lower_translation, upper_translation, max_motor_force;
+    b2g_vec2 ground_anchor_a, ground_anchor_b;
+    float length_a, length_b, ratio;
 } b2g_joint_def;
 
 /* Body state read back after a step (B2body getters, src/b2_body.rs:650-680). */
@@ -213,7 +218,7 @@ int b2g_create_fixtures(void* world, const b2g_fixture_def* defs, int32_t n, uin
  * A world with joints runs the grid-wide colour schedule (no part-local solve) and cannot be taped. */
 int b2g_create_joints(void* world, const b2g_joint_def* defs, int32_t n, uint32_t* out_ids);
 /* Accumulated joint impulses (for warm starting), 5 per joint: revolute x, y, motor, lower, upper;
- * prismatic x, y, motor, lower, upper; wheel impulse, spring, motor, lower, upper; distance impulse, lower, upper, 0, 0; weld, friction and motor x, y,
+ * prismatic x, y, motor, lower, upper; wheel impulse, spring, motor, lower, upper; pulley impulse, 0, 0, 0, 0; distance impulse, lower, upper, 0, 0; weld, friction and motor x, y,
  * angular, 0, 0; mouse x, y, 0, 0, 0 */
 int b2g_get_joint_impulses(void* world, uint32_t first, uint32_t count, float* out);
 /* B2mouseJoint::set_target (src/joints/b2_mouse_joint.rs:114-119): a new target wakes body B */

@@ -123,6 +123,9 @@ struct Joint {
     /* B2wheelJoint (private/dynamics/joints/b2_wheel_joint.rs): ax, ay in axis, perp; s_ax, s_bx in a1, a2;
      * s_ay, s_by in s1, s2; shares the motor and limit impulses, axial mass, bias and gamma */
     float wheel_impulse = 0, spring_impulse = 0, wheel_mass = 0, spring_mass = 0, motor_mass = 0;
+    /* B2pulleyJoint (private/dynamics/joints/b2_pulley_joint.rs) */
+    Vec2 ground_a{0, 0}, ground_b{0, 0}, u_a{0, 0}, u_b{0, 0};
+    float pulley_constant = 0, ratio = 1, pulley_impulse = 0, pulley_mass = 0;
     float weld_mass[9] = {0};  /* ex, ey, ez columns */
     bool collide_connected = false, island_flag = false;
     Vec2 local_anchor_a{0, 0}, local_anchor_b{0, 0};
@@ -1988,6 +1991,115 @@ static bool wheel_solve_position(World& w, Joint& j) {
     return linear_error <= kLinearSlop;
 }
 
+/* ---- pulley joint, private/dynamics/joints/b2_pulley_joint.rs ---- */
+
+static float pulley_dir(Vec2& u) {
+    const float len = length(u);
+    if (len > 10.0f * kLinearSlop) u *= 1.0f / len;
+    else u = v2(0, 0);
+    return len;
+}
+
+static void pulley_init_velocity(World& w, Joint& j, const Step& step) {
+    const Body& A = w.bodies[j.body_a];
+    const Body& B = w.bodies[j.body_b];
+    j.index_a = A.island_index;
+    j.index_b = B.island_index;
+    j.lc_a = A.sweep.local_center;
+    j.lc_b = B.sweep.local_center;
+    j.inv_mass_a = A.inv_mass;
+    j.inv_mass_b = B.inv_mass;
+    j.inv_ia = A.inv_I;
+    j.inv_ib = B.inv_I;
+    const Vec2 cA = w.pos[j.index_a].c, cB = w.pos[j.index_b].c;
+    const float aA = w.pos[j.index_a].a, aB = w.pos[j.index_b].a;
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const Rot qA = rot(aA), qB = rot(aB);
+    j.r_a = mul(qA, j.local_anchor_a - j.lc_a);
+    j.r_b = mul(qB, j.local_anchor_b - j.lc_b);
+    j.u_a = cA + j.r_a - j.ground_a;
+    j.u_b = cB + j.r_b - j.ground_b;
+    pulley_dir(j.u_a);
+    pulley_dir(j.u_b);
+    const float ruA = cross(j.r_a, j.u_a), ruB = cross(j.r_b, j.u_b);
+    const float mA = j.inv_mass_a + j.inv_ia * ruA * ruA;
+    const float mB = j.inv_mass_b + j.inv_ib * ruB * ruB;
+    j.pulley_mass = mA + j.ratio * j.ratio * mB;
+    if (j.pulley_mass > 0.0f) j.pulley_mass = 1.0f / j.pulley_mass;
+    if (step.warm) {
+        j.pulley_impulse *= step.dt_ratio;
+        const Vec2 PA = (-j.pulley_impulse) * j.u_a;
+        const Vec2 PB = (-j.ratio * j.pulley_impulse) * j.u_b;
+        vA += j.inv_mass_a * PA;
+        wA += j.inv_ia * cross(j.r_a, PA);
+        vB += j.inv_mass_b * PB;
+        wB += j.inv_ib * cross(j.r_b, PB);
+    } else {
+        j.pulley_impulse = 0.0f;
+    }
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+static void pulley_solve_velocity(World& w, Joint& j) {
+    Vec2 vA = w.vel[j.index_a].v;
+    float wA = w.vel[j.index_a].w;
+    Vec2 vB = w.vel[j.index_b].v;
+    float wB = w.vel[j.index_b].w;
+    const Vec2 vpA = vA + cross_sv(wA, j.r_a);
+    const Vec2 vpB = vB + cross_sv(wB, j.r_b);
+    const float cdot = -dot(j.u_a, vpA) - j.ratio * dot(j.u_b, vpB);
+    const float impulse = -j.pulley_mass * cdot;
+    j.pulley_impulse += impulse;
+    const Vec2 PA = -impulse * j.u_a;
+    const Vec2 PB = -j.ratio * impulse * j.u_b;
+    vA += j.inv_mass_a * PA;
+    wA += j.inv_ia * cross(j.r_a, PA);
+    vB += j.inv_mass_b * PB;
+    wB += j.inv_ib * cross(j.r_b, PB);
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+}
+
+static bool pulley_solve_position(World& w, Joint& j) {
+    Vec2 cA = w.pos[j.index_a].c;
+    float aA = w.pos[j.index_a].a;
+    Vec2 cB = w.pos[j.index_b].c;
+    float aB = w.pos[j.index_b].a;
+    const Rot qA = rot(aA), qB = rot(aB);
+    const Vec2 rA = mul(qA, j.local_anchor_a - j.lc_a);
+    const Vec2 rB = mul(qB, j.local_anchor_b - j.lc_b);
+    Vec2 uA = cA + rA - j.ground_a;
+    Vec2 uB = cB + rB - j.ground_b;
+    const float lenA = pulley_dir(uA), lenB = pulley_dir(uB);
+    const float ruA = cross(rA, uA), ruB = cross(rB, uB);
+    const float mA = j.inv_mass_a + j.inv_ia * ruA * ruA;
+    const float mB = j.inv_mass_b + j.inv_ib * ruB * ruB;
+    float mass = mA + j.ratio * j.ratio * mB;
+    if (mass > 0.0f) mass = 1.0f / mass;
+    const float C = j.pulley_constant - lenA - j.ratio * lenB;
+    const float linear_error = std::fabs(C);
+    const float impulse = -mass * C;
+    const Vec2 PA = -impulse * uA;
+    const Vec2 PB = -j.ratio * impulse * uB;
+    cA += j.inv_mass_a * PA;
+    aA += j.inv_ia * cross(rA, PA);
+    cB += j.inv_mass_b * PB;
+    aB += j.inv_ib * cross(rB, PB);
+    w.pos[j.index_a].c = cA;
+    w.pos[j.index_a].a = aA;
+    w.pos[j.index_b].c = cB;
+    w.pos[j.index_b].a = aB;
+    return linear_error < kLinearSlop;
+}
+
 /* init_velocity_constraints (:21-116): anchors, effective masses, warm start */
 static void joint_init_velocity(World& w, Joint& j, const Step& step) {
     if (j.type == B2G_JOINT_MOTOR) {
@@ -2004,6 +2116,10 @@ static void joint_init_velocity(World& w, Joint& j, const Step& step) {
     }
     if (j.type == B2G_JOINT_WHEEL) {
         wheel_init_velocity(w, j, step);
+        return;
+    }
+    if (j.type == B2G_JOINT_PULLEY) {
+        pulley_init_velocity(w, j, step);
         return;
     }
     if (j.type == B2G_JOINT_FRICTION) {
@@ -2097,6 +2213,10 @@ static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
         wheel_solve_velocity(w, j, step);
         return;
     }
+    if (j.type == B2G_JOINT_PULLEY) {
+        pulley_solve_velocity(w, j);
+        return;
+    }
     if (j.type == B2G_JOINT_FRICTION) {
         friction_solve_velocity(w, j, step);
         return;
@@ -2171,6 +2291,7 @@ static bool joint_solve_position(World& w, Joint& j) {
     if (j.type == B2G_JOINT_FRICTION || j.type == B2G_JOINT_MOTOR || j.type == B2G_JOINT_MOUSE) return true;
     if (j.type == B2G_JOINT_PRISMATIC) return prismatic_solve_position(w, j);
     if (j.type == B2G_JOINT_WHEEL) return wheel_solve_position(w, j);
+    if (j.type == B2G_JOINT_PULLEY) return pulley_solve_position(w, j);
     Vec2 cA = w.pos[j.index_a].c;
     float aA = w.pos[j.index_a].a;
     Vec2 cB = w.pos[j.index_b].c;
@@ -2964,7 +3085,7 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
         const b2g_joint_def& d = defs[i];
         if ((d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE && d.type != B2G_JOINT_WELD &&
              d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR && d.type != B2G_JOINT_MOUSE &&
-             d.type != B2G_JOINT_PRISMATIC && d.type != B2G_JOINT_WHEEL) ||
+             d.type != B2G_JOINT_PRISMATIC && d.type != B2G_JOINT_WHEEL && d.type != B2G_JOINT_PULLEY) ||
             d.body_a >= w.bodies.size() ||
             d.body_b >= w.bodies.size())
             return -1;
@@ -2990,6 +3111,11 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
         j.lower_translation = d.lower_translation;
         j.upper_translation = d.upper_translation;
         j.max_motor_force = d.max_motor_force;
+        /* b2_pulley_joint.rs:30-40 */
+        j.ground_a = v2(d.ground_anchor_a.x, d.ground_anchor_a.y);
+        j.ground_b = v2(d.ground_anchor_b.x, d.ground_anchor_b.y);
+        j.ratio = d.ratio;
+        j.pulley_constant = d.length_a + d.ratio * d.length_b;
         if (j.type == B2G_JOINT_WHEEL) {  /* b2_wheel_joint.rs:334-335: the axis as given */
             j.local_xaxis_a = v2(d.local_axis_a.x, d.local_axis_a.y);
             j.local_yaxis_a = cross_sv(1.0f, j.local_xaxis_a);
@@ -3031,6 +3157,11 @@ int ora_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) 
     if ((size_t)first + count > w.joints.size()) return -1;
     for (uint32_t i = 0; i < count; ++i) {
         const Joint& j = w.joints[first + i];
+        if (j.type == B2G_JOINT_PULLEY) {
+            out[5 * i + 0] = j.pulley_impulse;
+            for (int k = 1; k < 5; ++k) out[5 * i + k] = 0.0f;
+            continue;
+        }
         if (j.type == B2G_JOINT_WHEEL) {
             out[5 * i + 0] = j.wheel_impulse;
             out[5 * i + 1] = j.spring_impulse;
