@@ -107,22 +107,42 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def bytes_model(counts, scene_stats, vi, pi):
-    """Algorithmic HBM bytes of one step by phase (SoA layout of csrc/b2g_internal.h).
+SORT_PASSES = 4  # one world: 31 key bits (15-bit Morton cells per axis + the large-static bit), 8-bit digits
 
-    per dynamic body   integrate velocities 72 B, integrate positions 48 B, write-back 40 B,
-                       fixture sync 76 B + 16 B/vertex
-    per contact        collide: 116 B state + shape bytes (polygon 16 B/vertex + 12, circle 12, edge 36)
-    per constraint     init + warm start 320 B, velocity iteration 208 B, position iteration 128 B,
-                       store 16 B
-    per proxy          broadphase keys/sort/build/refit 16 B + 8 B per new pair
+
+def bytes_model(st, scene_stats, vi, pi):
+    """Algorithmic HBM bytes of one step by kernel phase (SoA layout of csrc/b2g_internal.h), from the
+    step's own device counts `st` (b2g_get_step_stats).
+
+    k_solve        per dynamic body: integrate velocities 72 B, integrate positions 48 B, write-back 40 B;
+                   per proxy: fixture sync 76 B + shape bytes; per constraint slot: init + warm start
+                   320 B, velocity iteration 208 B, position iteration 128 B, store 16 B
+    k_collide      per contact: 116 B state + 2 shape records (polygon 16 B/vertex + 12, circle 12, edge 36)
+    bp_sort        per proxy: bounds 24 B + keys 28 B + 4 radix passes x 24 B (key + payload read and
+                   written)
+    bp_hierarchy   per proxy: build 36 B, leaves 36 B, refit 68 B, four-way records 144 B; per contact:
+                   row index 12 B
+    bp_traverse    per fetched node 80 B (four child boxes + children), per checked leaf 32 B (its
+                   payload, proxy ids, moved flags, contact row and key), per proxy 5 B (payload and
+                   moved flag), per new pair 20 B
+    merge          per contact: 2 x 108 B (read and written)
     """
-    nb, nc, ncons = scene_stats["n_dynamic"], counts["contacts"], counts["islands_solved"]
+    nf, nb = scene_stats["n_fixtures"], scene_stats["n_dynamic"]
+    nc, ncons = st["contacts"], st["constraints"]
     shape = scene_stats["shape_bytes_mean"]
-    collide = nc * (116 + 2 * shape)
-    solver = nb * (72 + 48 + 40) + ncons * (320 + 208 * vi + 128 * pi + 16) + scene_stats["n_fixtures"] * (76 + shape)
-    broad = scene_stats["n_fixtures"] * 16 * 6 + counts["pairs"] * 8
-    return {"collide": collide, "solver": solver, "broadphase": broad}
+    return {
+        "solver": nb * (72 + 48 + 40) + ncons * (320 + 208 * vi + 128 * pi + 16) + nf * (76 + shape),
+        "collide": nc * (116 + 2 * shape),
+        "bp_sort": nf * (24 + 28 + SORT_PASSES * 24),
+        "bp_hierarchy": nf * (36 + 36 + 68 + 144) + nc * 12,
+        "bp_traverse": st["bp_node_visits"] * 80 + st["bp_leaf_checks"] * 32 + nf * 5 + st["new_pairs"] * 20,
+        "merge": nc * 2 * 108,
+    }
+
+
+# the kernel that dominates each phase (the phase's CUDA-event time is charged to it)
+PHASE_KERNEL = {"solver": "k_solve", "collide": "k_collide", "bp_sort": "k_radix_coop",
+                "bp_hierarchy": "k_bp_refit", "bp_traverse": "k_bp_traverse", "merge": "k_merge_old"}
 
 
 def scene_stats(scene):
@@ -132,22 +152,28 @@ def scene_stats(scene):
     return {"n_dynamic": scene["n_dynamic"], "n_fixtures": len(f), "shape_bytes_mean": float(shape.mean())}
 
 
-def run_cpu_baseline(scene, budget_s=15.0, max_steps=60):
-    """Time the oracle (libm trig, single thread) on the first steps of the same workload."""
+def run_cpu_baseline(scene, skip, budget_s=30.0, max_steps=60):
+    """Time the oracle (libm trig, single thread) on the bench's window of the same workload: the
+    oracle steps the scene `skip` steps untimed, then is timed for up to `max_steps` steps or
+    `budget_s` seconds (at least 3 steps)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
     oracle.set_trig(True)
     w = oracle.OracleWorld(gravity=scene["gravity"], allow_sleep=False)
     scenes.build_world(w, scene)
+    if skip > 0:
+        w.steps(scene["dt"], scene["vi"], scene["pi"], skip)
     steps = 0
     t0 = time.perf_counter()
-    while steps < max_steps and time.perf_counter() - t0 < budget_s:
+    while steps < max_steps and (steps < 3 or time.perf_counter() - t0 < budget_s):
         w.step(scene["dt"], scene["vi"], scene["pi"])
         steps += 1
     dt = time.perf_counter() - t0
+    w.close()
     return {"value": scene["n_dynamic"] * steps / dt, "unit": "body-steps/s", "cores": 1, "kind": "port",
-            "sample": f"first {steps} steps of the mixed-100k scene (oracle, libm sin/cos, 1 thread, {dt:.1f} s)"}
+            "sample": f"steps {skip + 1}-{skip + steps} of the mixed-100k scene after {skip} untimed steps "
+                      f"(oracle, libm sin/cos, 1 thread, {dt:.1f} s timed)"}
 
 
 def snapshot(world):
@@ -438,6 +464,73 @@ def run_continuous(torch, flush, device, skip=300, steps=60, warmup=3, cpu_budge
                                        f"{cpu_s:.1f} s"}}
 
 
+def run_pile(torch, flush, device, steps=20, warmup=3, cpu=True, n_boxes=250_000, scene_steps=1000,
+             cpu_budget_s=20.0):
+    """High-contact pile: 250k boxes (half-extents 0.05-0.2 m) dropped into a 100 x 400 m walled container,
+    1000 steps. The last `steps` steps of the 1000 are timed (device time, L2 flushed between steps),
+    when the pile holds its most contact points. CPU: the oracle (libm sin/cos, 1 thread) stepped from
+    the GPU's state at the start of the window. Contact and pair capacities are given explicitly."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    scene = scenes.pile(n_boxes=n_boxes, steps=scene_steps)
+    dt, vi, pi = scene["dt"], scene["vi"], scene["pi"]
+    w = b2g.B2world(gravity=scene["gravity"], device=device, contact_capacity=16_000_000, pair_capacity=4_000_000)
+    w.set_allow_sleeping(False)
+    scenes.build_world(w, scene)
+    skip = scene_steps - steps - warmup
+    for _ in range(skip):
+        w.step(dt, vi, pi)
+    w.synchronize()
+    snap = snapshot(w)
+    for _ in range(warmup):
+        w.step(dt, vi, pi)
+    w.synchronize()
+    total = 0.0
+    fine = dict.fromkeys(b2g.B2world.PHASES + b2g.B2world.TREE_PHASES, 0.0)
+    stats = scene_stats(scene)
+    byts = {}
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        w.step(dt, vi, pi)
+        total += w.get_profile()["step"]
+        for ph, v in w.get_phase_times(tree_split=True).items():
+            fine[ph] += v
+        for ph, v in bytes_model(w.get_step_stats(), stats, vi, pi).items():
+            byts[ph] = byts.get(ph, 0) + v
+    st = w.get_step_stats()
+    contacts = w.get_contacts()
+    points = int(contacts["point_count"][contacts["touching"] != 0].sum())
+    w.close()
+    peak, _ = load_peaks()
+    solver_ach = byts["solver"] / (fine["solver"] / 1e3) / 1e9 if fine["solver"] > 0 else None
+    out = {"metric": "body-steps/s, high-contact pile", "value": n_boxes * steps / (total / 1e3),
+           "unit": "body-steps/s", "ms_per_step": total / steps,
+           "window": f"steps {skip + warmup + 1}-{scene_steps} of the {scene_steps}-step pile",
+           "contact_points": points, "contacts": st["contacts"], "constraints": st["constraints"],
+           "colours": st["colours"], "parts": st["parts"],
+           "phase_ms_per_step": {k: v / steps for k, v in fine.items()},
+           "solver_roofline": {"achieved": solver_ach, "peak": peak, "unit": "GB/s",
+                               "frac": solver_ach / peak if solver_ach else None},
+           "capacities": {"contacts": 16_000_000, "pairs": 4_000_000}}
+    if cpu:
+        import oracle
+
+        oracle.set_trig(True)
+        o = oracle.OracleWorld(gravity=scene["gravity"], allow_sleep=False)
+        scenes.build_world(o, scene)
+        o.import_state(snap["bodies"], snap["aabbs"], snap["contacts"], np.float32(1.0) / dt)
+        n, t0 = 0, time.perf_counter()
+        while n < 10 and (n < 1 or time.perf_counter() - t0 < cpu_budget_s):
+            o.step(dt, vi, pi)
+            n += 1
+        cpu_s = time.perf_counter() - t0
+        o.close()
+        out["cpu_baseline"] = {"value": n_boxes * n / cpu_s, "unit": "body-steps/s", "cores": 1, "kind": "port",
+                               "sample": f"oracle (libm sin/cos, 1 thread) stepped {n} steps from the GPU's state at "
+                                         f"step {skip}: {cpu_s:.1f} s"}
+    return out
+
+
 def run_adjoint(torch, flush, device, steps=240, seeds=512, repeats=3):
     """Differentiable throw-and-stack (64 boxes + a circle projectile, loss = squared distance of the
     stack's centre of mass from a target after `steps` steps): device time of the plain forward
@@ -489,6 +582,17 @@ def dist_info():
     return rank, world, local
 
 
+SCENE_STEPS = 600  # the mixed-100k configuration runs 600 steps; the timed window is centred on its middle
+
+
+def window_skip(args):
+    """Untimed steps before the warm-up: --skip-steps, else the window of `steps` timed steps is centred
+    on step 300 of the 600-step scene (the whole trajectory when steps >= 600)."""
+    if args.skip_steps is not None:
+        return args.skip_steps
+    return max(0, SCENE_STEPS // 2 - args.warmup - args.steps // 2)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -504,9 +608,10 @@ def main():
     ap.add_argument("--toi-pairs", type=int, default=1_000_000, help="pairs of the time-of-impact leg (0 skips it)")
     ap.add_argument("--continuous-steps", type=int, default=60,
                     help="timed steps of the continuous-physics leg (0 skips it)")
+    ap.add_argument("--pile-steps", type=int, default=20, help="timed steps of the high-contact pile leg (0 skips it)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
-    ap.add_argument("--skip-steps", type=int, default=0,
-                    help="untimed steps before the warm-up (profiling a later window of the scene)")
+    ap.add_argument("--skip-steps", type=int, default=None,
+                    help="untimed steps before the warm-up (default: centre the timed window on step 300)")
     ap.add_argument("--profile-window", action="store_true",
                     help="bracket the timed steps with cudaProfilerStart/Stop (ncu --profile-from-start off)")
     args = ap.parse_args()
@@ -514,7 +619,11 @@ def main():
     n_half = int(50_000 * args.scale)
     scene = scenes.mixed(n_circles=n_half, n_polygons=n_half)
     stats = scene_stats(scene)
-    config = {"workload": WORKLOAD, "bodies": stats["n_dynamic"], "fixtures": stats["n_fixtures"],
+    skip = window_skip(args)
+    first = skip + args.warmup + 1
+    window = f"steps {first}-{first + args.steps - 1} of the {SCENE_STEPS}-step scene"
+    config = {"workload": f"{WORKLOAD}; timed window: {window}", "bodies": stats["n_dynamic"],
+              "fixtures": stats["n_fixtures"], "window": window,
               "velocity_iterations": 8, "position_iterations": 3, "dt": 1 / 60, "sleep": False,
               "continuous": False, "l2": "256 MiB flush between timed steps", "parallelism": "replicas",
               "cuda_graphs": not args.no_graphs}
@@ -522,13 +631,14 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = run_cpu_baseline(scene, budget_s=20.0, max_steps=max(args.steps, 1))
+        cb = run_cpu_baseline(scene, skip + args.warmup, budget_s=30.0, max_steps=max(args.steps, 3))
         line = {"metric": METRIC, "value": cb["value"], "unit": "body-steps/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
                 "dtype": "f32", "data": "synthetic (seeded splitmix64)", "config": config, "cpu_baseline": cb,
                 "e2e": {"value": cb["value"], "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                 "vs_baseline": None,
-                "note": "box2d-rs cannot be compiled here (no Rust toolchain); timed its faithful C++ restatement"}
+                "note": "box2d-rs cannot be compiled here (no Rust toolchain); timed its faithful C++ restatement "
+                        "on the same window of the same scene"}
         print(json.dumps(line))
         return
 
@@ -543,13 +653,12 @@ def main():
 
     dt, vi, pi = scene["dt"], scene["vi"], scene["pi"]
     if not args.no_autotune:
-        # tune on a scratch world of the same scene, advanced to the middle of the timed window
-        # (the scene is sparse in its first steps); the measured world inherits the choice
-        # through the size-bucket cache
+        # tune on a scratch world of the same scene, advanced to the middle of the timed window;
+        # the measured world inherits the choice through the size-bucket cache
         t = b2g.B2world(gravity=scene["gravity"], device=local_rank)
         t.set_allow_sleeping(False)
         scenes.build_world(t, scene)
-        for _ in range(args.skip_steps + args.warmup + args.steps // 2):
+        for _ in range(skip + args.warmup + args.steps // 2):
             t.step(dt, vi, pi)
         t.autotune(dt, vi, pi, 6)
         tuned = tune_blocks_per_sm(torch, flush, t, dt, vi, pi)
@@ -561,7 +670,7 @@ def main():
     if not args.no_autotune:
         w.set_launch_config(**tuned)
     scenes.build_world(w, scene)
-    for _ in range(args.skip_steps + args.warmup):
+    for _ in range(skip + args.warmup):
         w.step(dt, vi, pi)
     w.synchronize()
     config["launch_config"] = w.get_launch_config()
@@ -575,8 +684,9 @@ def main():
         torch.cuda.profiler.start()
     launches0 = w._lib.b2g_get_launch_count()
     total_ms = 0.0
-    phase_ms = {"collide": 0.0, "solve_init": 0.0, "solve_velocity": 0.0, "broadphase": 0.0}
-    fine_ms = dict.fromkeys(b2g.B2world.PHASES, 0.0)
+    fine_ms = dict.fromkeys(b2g.B2world.PHASES + b2g.B2world.TREE_PHASES, 0.0)
+    bytes_total = {}
+    work = {"bp_node_visits": 0, "bp_leaf_checks": 0, "new_pairs": 0, "contacts": 0, "constraints": 0}
     snap_at = set(int(x) for x in np.linspace(0, args.steps - 1, 4)) if rank == 0 and not args.no_cpu_baseline else set()
     snaps = []
     for k in range(args.steps):
@@ -585,12 +695,15 @@ def main():
         w.step(dt, vi, pi)
         p = w.get_profile()  # synchronizes the world's stream; event times of this step
         total_ms += p["step"]
-        for ph in phase_ms:
-            phase_ms[ph] += p[ph]
-        for ph, v in w.get_phase_times().items():
+        for ph, v in w.get_phase_times(tree_split=True).items():
             fine_ms[ph] += v
+        st = w.get_step_stats()  # this step's work counts (outside the timed events)
+        for key in work:
+            work[key] += st[key]
+        for ph, v in bytes_model(st, stats, vi, pi).items():
+            bytes_total[ph] = bytes_total.get(ph, 0) + v
         if k in snap_at:  # outside the timed events: the state after this step
-            snaps.append((args.warmup + k + 1, snapshot(w)))
+            snaps.append((skip + args.warmup + k + 1, snapshot(w)))
     launches = w._lib.b2g_get_launch_count() - launches0
     torch.cuda.synchronize()
     if args.profile_window:
@@ -609,7 +722,7 @@ def main():
     if not args.no_autotune:
         w.set_launch_config(**tuned)
     scenes.build_world(w, scene)
-    for _ in range(args.warmup):
+    for _ in range(skip + args.warmup):
         w.step(dt, vi, pi)
     w.synchronize()
     # every step's states are copied into host memory (two buffers alternate); the copy of step k
@@ -633,34 +746,45 @@ def main():
     e2e_value = stats["n_dynamic"] * e2e_steps * world_size / e2e_s
 
     peak, peak_kind = load_peaks()
-    bm = bytes_model(counts, stats, vi, pi)
-    # dominant kernel: the persistent solver k_solve (its own CUDA-event time, "solver" phase);
-    # achieved = its algorithmic bytes per launch / its mean launch time
-    ms_phase = {"collide": fine_ms["collide"], "solver": fine_ms["solver"],
-                "broadphase": fine_ms["broadphase_tree"] + fine_ms["contact_merge"]}
-    dominant = max(ms_phase, key=ms_phase.get)
-    achieved = bm[dominant] / (ms_phase[dominant] / args.steps / 1e3) / 1e9
-    traffic = None
+    # per phase: algorithmic bytes per step / the phase's mean CUDA-event time per step
+    phase_time = {"solver": fine_ms["solver"], "collide": fine_ms["collide"], "bp_sort": fine_ms["bp_sort"],
+                  "bp_hierarchy": fine_ms["bp_hierarchy"], "bp_traverse": fine_ms["bp_traverse"],
+                  "merge": fine_ms["contact_merge"]}
+    traffic_rec = {}
     tf = os.path.join(ROOT, "profiles", "roofline_traffic.json")
-    if dominant == "solver" and os.path.exists(tf):
+    if os.path.exists(tf):
         with open(tf) as f:
             rec = json.load(f)
-        if rec.get("kernel") == "k_solve" and rec.get("workload") == WORKLOAD:
-            traffic = rec["dram_bytes_per_launch"]
+        if rec.get("workload") == WORKLOAD and rec.get("window") == window:
+            traffic_rec = rec.get("dram_bytes_per_launch", {})
+    phases = {}
+    for ph, ms in phase_time.items():
+        if ms <= 0:
+            continue
+        b = bytes_total.get(ph, 0) / args.steps
+        ach = b / (ms / args.steps / 1e3) / 1e9
+        kern = PHASE_KERNEL[ph]
+        phases[ph] = {"kernel": kern, "ms_per_step": ms / args.steps, "algorithmic_bytes_per_step": b,
+                      "achieved": ach, "frac": ach / peak, "traffic": traffic_rec.get(kern)}
+    dominant = max(phases, key=lambda k: phases[k]["ms_per_step"])
+    d = phases[dominant]
     line = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded splitmix64)",
         "config": config,
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,
-                "steps": e2e_steps},
+                "steps": e2e_steps, "window": window,
+                "h2d_note": "B2world::step takes no per-step host input (dt and the iteration counts are scalar "
+                            "arguments of b2g_step); every body's state is read back to host memory every step"},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "k_solve" if dominant == "solver" else dominant,
-                     "kernel_phase": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": bm[dominant],
-                     "traffic_note": "DRAM bytes per launch from one ncu capture at step 603 "
-                                     "(profiles/k_solve_mixed100k_step603.md)" if traffic else None},
+        "roofline": {"bound": "hbm", "kernel": d["kernel"], "kernel_phase": dominant, "achieved": d["achieved"],
+                     "peak": peak, "unit": "GB/s", "frac": d["frac"], "peak_kind": peak_kind,
+                     "traffic": d["traffic"], "algorithmic_bytes_per_launch": d["algorithmic_bytes_per_step"],
+                     "traffic_note": ("DRAM bytes per launch from one ncu capture of the same window "
+                                      "(profiles/roofline_traffic.json)") if d["traffic"] else None},
+        "roofline_phases": phases,
+        "work_per_step": {k: v / args.steps for k, v in work.items()},
         "phase_ms_per_step": {k: v / args.steps for k, v in fine_ms.items()},
         "counts_last_step": counts,
         "clocks": clocks,
@@ -675,6 +799,9 @@ def main():
     if args.continuous_steps > 0 and rank == 0:
         line["continuous"] = run_continuous(torch, flush, local_rank, steps=args.continuous_steps,
                                             warmup=args.warmup)
+    if args.pile_steps > 0 and rank == 0:
+        line["c3_pile"] = run_pile(torch, flush, local_rank, steps=args.pile_steps, warmup=args.warmup,
+                                   cpu=not args.no_cpu_baseline)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = run_cpu_on_snapshots(scene, snaps)
     if rank == 0:

@@ -24,6 +24,7 @@ POLYGON_HULL, POLYGON_BOX, POLYGON_BOX_ORIENTED = 0, 1, 2
 POLYGON_RADIUS = np.float32(0.01)  # B2_POLYGON_RADIUS = 2 * linear slop
 
 OK = 0
+ERR_INVALID_ARG, ERR_OUT_OF_MEMORY, ERR_CAPACITY, ERR_TIMEOUT, ERR_CUDA, ERR_UNSUPPORTED = -1, -2, -3, -4, -5, -6
 ERRORS = {
     -1: "invalid argument",
     -2: "out of memory",
@@ -408,6 +409,40 @@ class Profile(ctypes.Structure):
         return {n: float(getattr(self, n)) for n, _ in self._fields_}
 
 
+CONTACT_IMPULSE = np.dtype([("fixture_a", np.uint32), ("fixture_b", np.uint32), ("normal_impulses", np.float32, 2),
+                            ("tangent_impulses", np.float32, 2), ("count", np.int32)])
+
+
+class ContactEdit(ctypes.Structure):
+    """b2g_contact_edit: what a pre_solve callback may change (B2contact's setters)."""
+    _fields_ = [("enabled", ctypes.c_int32), ("friction", ctypes.c_float), ("restitution", ctypes.c_float),
+                ("restitution_threshold", ctypes.c_float), ("tangent_speed", ctypes.c_float)]
+
+
+CONTACT_FILTER_FN = ctypes.CFUNCTYPE(ctypes.c_int32, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32)
+PRE_SOLVE_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ContactEdit))
+
+
+def contact_filter_callback(fn):
+    """A C contact filter calling fn(fixture_a, fixture_b) -> bool."""
+    return CONTACT_FILTER_FN(lambda user, a, b: 1 if fn(int(a), int(b)) else 0)
+
+
+def pre_solve_callback(fn):
+    """A C pre_solve callback calling fn(contact, old_manifold, edit): the first two are CONTACT_INFO
+    records, edit a ContactEdit to change in place."""
+    def call(user, c, old, edit):
+        info = np.frombuffer(ctypes.string_at(c, CONTACT_INFO.itemsize), CONTACT_INFO)[0]
+        prev = np.frombuffer(ctypes.string_at(old, CONTACT_INFO.itemsize), CONTACT_INFO)[0]
+        fn(info, prev, edit.contents)
+    return PRE_SOLVE_FN(call)
+
+
+class StepStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in ("bp_node_visits", "bp_leaf_checks", "new_pairs", "contacts", "constraints",
+                                               "interior_slots", "parts", "colours")]
+
+
 class Counts(ctypes.Structure):
     _fields_ = [
         (n, ctypes.c_int32)
@@ -592,11 +627,23 @@ def load_library(path=LIB_PATH):
         "b2g_get_events": [vp, vp, i32, ctypes.POINTER(i32)],
         "b2g_get_pairs": [vp, vp, i32, ctypes.POINTER(i32)],
         "b2g_get_proxies": [vp, vp, vp, i32],
+        "b2g_get_proxy_ids": [vp, vp, i32],
+        "b2g_get_post_solve": [vp, vp, i32, ctypes.POINTER(i32)],
+        "b2g_set_contact_filter": [vp, vp, vp],
+        "b2g_set_pre_solve": [vp, vp, vp],
+        "b2g_destroy_bodies": [vp, vp, i32],
+        "b2g_destroy_fixtures": [vp, vp, i32],
+        "b2g_destroy_joints": [vp, vp, i32],
+        "b2g_set_filter_data": [vp, u32, ctypes.c_uint16, ctypes.c_uint16, ctypes.c_int16],
+        "b2g_refilter": [vp, u32],
         "b2g_get_solver_order": [vp, vp, i32, ctypes.POINTER(i32)],
         "b2g_set_contact_events": [vp, i32],
         "b2g_set_record_pairs": [vp, i32],
         "b2g_set_graph_capture": [vp, i32],
+        "b2g_set_barrier_limit": [vp, ctypes.c_int64],
+        "b2g_debug_hold_barriers": [vp, i32],
         "b2g_get_phase_times": [vp, vp, i32],
+        "b2g_get_step_stats": [vp, ctypes.POINTER(StepStats)],
         "b2g_ray_cast_closest": [vp, vp, vp, i32, vp],
         "b2g_query_aabb": [vp, vp, vp, i32, vp, i32, ctypes.POINTER(i32)],
         "b2g_get_launch_config": [vp, ctypes.POINTER(LaunchConfig)],
@@ -830,6 +877,14 @@ class B2world:
     def set_graph_capture(self, flag):
         self._check(self._lib.b2g_set_graph_capture(self._h, int(flag)))
 
+    def set_barrier_limit(self, cycles):
+        """Grid-barrier wait limit of the world's persistent kernels in clock cycles (0: default)."""
+        self._check(self._lib.b2g_set_barrier_limit(self._h, int(cycles)))
+
+    def debug_hold_barriers(self, extra):
+        """Test hook: every grid barrier waits for `extra` arrivals that never come (0: off)."""
+        self._check(self._lib.b2g_debug_hold_barriers(self._h, int(extra)))
+
     # -- introspection --
     def get_profile(self):
         p = Profile()
@@ -837,12 +892,21 @@ class B2world:
         return p.as_dict()
 
     PHASES = ("initial_broadphase", "collide", "islands", "colouring", "solver", "broadphase_tree", "contact_merge")
+    TREE_PHASES = ("bp_sort", "bp_hierarchy", "bp_traverse")
 
-    def get_phase_times(self):
-        """Device milliseconds of the last step's phases (see b2g_get_phase_times)."""
-        out = np.zeros(7, np.float32)
-        self._check(self._lib.b2g_get_phase_times(self._h, _ptr(out), 7))
-        return dict(zip(self.PHASES, map(float, out)))
+    def get_phase_times(self, tree_split=False):
+        """Device milliseconds of the last step's phases (see b2g_get_phase_times); with tree_split
+        also the broadphase tree pass in three (keys + sort, hierarchy, traversal)."""
+        out = np.zeros(10, np.float32)
+        self._check(self._lib.b2g_get_phase_times(self._h, _ptr(out), 10))
+        names = self.PHASES + (self.TREE_PHASES if tree_split else ())
+        return dict(zip(names, map(float, out)))
+
+    def get_step_stats(self):
+        """Work counts of the last step (b2g_get_step_stats)."""
+        out = StepStats()
+        self._check(self._lib.b2g_get_step_stats(self._h, ctypes.byref(out)))
+        return {k: int(getattr(out, k)) for k, _ in StepStats._fields_}
 
     def get_counts(self):
         c = Counts()
@@ -1016,6 +1080,53 @@ class B2world:
         out = np.zeros((self.body_count, 8), np.float32)
         self._check(self._lib.b2g_tape_get_checkpoint(self._h, int(index), _ptr(out), self.body_count))
         return out
+
+    def set_contact_filter(self, fn):
+        """fn(fixture_a, fixture_b) -> bool replaces the default contact filter (None restores it)."""
+        self._filter_cb = None if fn is None else contact_filter_callback(fn)
+        ptr = None if fn is None else ctypes.cast(self._filter_cb, ctypes.c_void_p)
+        self._check(self._lib.b2g_set_contact_filter(self._h, ptr, None))
+
+    def set_pre_solve(self, fn):
+        """fn(contact, old_manifold, edit) is called after collide for every updated touching contact."""
+        self._pre_solve_cb = None if fn is None else pre_solve_callback(fn)
+        ptr = None if fn is None else ctypes.cast(self._pre_solve_cb, ctypes.c_void_p)
+        self._check(self._lib.b2g_set_pre_solve(self._h, ptr, None))
+
+    def get_post_solve(self):
+        """The last step's post_solve reports (b2g_get_post_solve), as a CONTACT_IMPULSE array."""
+        n = ctypes.c_int32(0)
+        self._check(self._lib.b2g_get_post_solve(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(max(n.value, 1), CONTACT_IMPULSE)
+        self._check(self._lib.b2g_get_post_solve(self._h, _ptr(out), n.value, ctypes.byref(n)))
+        return out[: n.value]
+
+    def get_proxy_ids(self):
+        """Each fixture's proxy id (the reference's dynamic-tree leaf id), -1 without a proxy."""
+        out = np.zeros(max(self.fixture_count, 1), np.int32)
+        self._check(self._lib.b2g_get_proxy_ids(self._h, _ptr(out), self.fixture_count))
+        return out[: self.fixture_count]
+
+    # -- destruction and filtering (B2world::destroy_body / destroy_joint, B2body::destroy_fixture,
+    #    B2fixture::set_filter_data / refilter) --
+    def destroy_bodies(self, ids):
+        ids = np.ascontiguousarray(np.atleast_1d(ids), np.uint32)
+        self._check(self._lib.b2g_destroy_bodies(self._h, _ptr(ids), len(ids)))
+
+    def destroy_fixtures(self, ids):
+        ids = np.ascontiguousarray(np.atleast_1d(ids), np.uint32)
+        self._check(self._lib.b2g_destroy_fixtures(self._h, _ptr(ids), len(ids)))
+
+    def destroy_joints(self, ids):
+        ids = np.ascontiguousarray(np.atleast_1d(ids), np.uint32)
+        self._check(self._lib.b2g_destroy_joints(self._h, _ptr(ids), len(ids)))
+
+    def set_filter_data(self, fixture, category_bits, mask_bits, group_index):
+        self._check(self._lib.b2g_set_filter_data(self._h, int(fixture), int(category_bits), int(mask_bits),
+                                                  int(group_index)))
+
+    def refilter(self, fixture):
+        self._check(self._lib.b2g_refilter(self._h, int(fixture)))
 
     def get_proxies(self):
         n = self.fixture_count

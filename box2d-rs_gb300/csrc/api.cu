@@ -14,14 +14,20 @@
  * Counts that vary per step live in device memory and every kernel reads them there.
  *
  * Proxy ids: the reference's proxy id is the node-pool index of the proxy's leaf in its
- * dynamic tree. Without destruction that index depends only on creation order (the k-th
- * proxy gets 0 for k = 0 and 2k - 1 afterwards, since every later insertion also takes
- * one internal node and moves return what they take), so it is reproduced exactly and
- * used for the same purposes: which fixture of a same-type pair is A, and the moved rule.
+ * dynamic tree (private/collision/b2_dynamic_tree.rs:28-99). That index depends only on the
+ * order of creations and destructions, not on the tree's shape: an insertion into a non-empty
+ * tree takes a leaf and an internal node from the pool's free list (or the next two fresh nodes),
+ * a removal returns the leaf's parent and then the leaf (so the list's head is the leaf), a move
+ * returns its parent and takes it back, and the root alone neither takes nor returns a parent.
+ * So the free list is a stack of (leaf, parent) pairs with the leaf on top, and a new proxy gets
+ * the most recently freed leaf id, else the next fresh node (0 for the first proxy, then two nodes
+ * per proxy). alloc_refid / free_refid keep that stack; the ids serve the same purposes as in the
+ * reference: which fixture of a same-type pair is A, the contact keys' order and the moved rule.
  */
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -40,7 +46,7 @@ namespace {
 constexpr int kVersion = 1;
 
 struct Timer {
-    cudaEvent_t e[9] = {};
+    cudaEvent_t e[11] = {};
     bool valid = false;
 };
 
@@ -119,7 +125,20 @@ struct World {
     std::vector<float4> h_fmat, h_fat;
     std::vector<uint32_t> h_filter, h_group, h_refid;
     std::vector<uint8_t> h_moved;
-    int proxies_created = 0;
+    int proxies_created = 0;       /* live proxies */
+    uint32_t next_node = 0;        /* the dynamic tree's next fresh node id */
+    std::vector<uint32_t> free_refids;  /* freed leaf ids, most recent last */
+    /* destroyed objects keep their ids (tombstones: a body turns static and disabled, a fixture
+     * loses its proxy, a joint leaves the joint colouring) */
+    std::vector<uint8_t> h_bdead, h_fdead, h_jdead;
+    bool host_dirty = false;       /* host mirrors were edited: the next prepare uploads them */
+    std::vector<int4> pending_events;  /* end events of destructions since the last b2g_get_events */
+    /* host callbacks: the user's contact filter (replacing the default one) and pre_solve */
+    b2g_contact_filter_fn filter_fn = nullptr;
+    void* filter_user = nullptr;
+    b2g_pre_solve_fn pre_solve_fn = nullptr;
+    void* pre_solve_user = nullptr;
+    int hook_rc = 0;               /* the first error of a host callback round trip during a step */
     /* device */
     DevWorld d{};
     bool allocated = false;
@@ -139,6 +158,8 @@ struct World {
     int swaps = 0;
     int alloc_generation = 0;
     int minsep_buffers = 2;  /* position-iteration separation buffers held in d.isl_minsep */
+    int barrier_limit_units = 0;  /* grid-barrier wait limit / 1024 cycles (0: the kernels' default) */
+    int barrier_hold = 0;         /* test hook: arrivals every grid barrier waits for in vain */
     TapeHost* tape = nullptr;
     LaunchCfg cfg;
     bool cfg_set = false;    /* chosen by the user or the autotuner: no bucket lookup */
@@ -208,6 +229,7 @@ int fail(World* w, int code, const char* msg) {
     if (w) w->err = msg;
     return code;
 }
+int fail(World* w, int code, const std::string& msg) { return fail(w, code, msg.c_str()); }
 
 #define CUDA_OK(w, call)                                                       \
     do {                                                                       \
@@ -498,6 +520,26 @@ void reset_mass_data(World* w, int b) {
     v.y += dv.y;
 }
 
+/* a new proxy's id: the most recently freed leaf, else the next fresh node (a leaf and, unless the tree
+ * is empty, its parent) */
+uint32_t alloc_refid(World* w) {
+    uint32_t id;
+    if (!w->free_refids.empty()) {
+        id = w->free_refids.back();
+        w->free_refids.pop_back();
+    } else {
+        id = w->next_node;
+        w->next_node += w->proxies_created == 0 ? 1u : 2u;
+    }
+    ++w->proxies_created;
+    return id;
+}
+
+void free_refid(World* w, uint32_t id) {
+    w->free_refids.push_back(id);
+    --w->proxies_created;
+}
+
 /* host copy of the fat-AABB rule of B2dynamicTree::move_proxy (private/collision/b2_dynamic_tree.rs:109-168) */
 void host_move_proxy(World* w, int f, const AABB& aabb, V2 disp) {
     const V2 r = mk(kAabbExtension, kAabbExtension);
@@ -522,6 +564,15 @@ void host_move_proxy(World* w, int f, const AABB& aabb, V2 disp) {
 }
 
 /* ---- device allocation, upload and download ---- */
+
+/* the grid-barrier settings into the device's counter block (read by every grid barrier) */
+int write_barrier_settings(World* w) {
+    if (!w->allocated) return B2G_OK;
+    const int v[2] = {w->barrier_limit_units, w->barrier_hold};
+    CUDA_OK(w, cudaMemcpyAsync(w->d.cnt + CNT_BARRIER_LIMIT, v, sizeof(v), cudaMemcpyHostToDevice, w->stream));
+    CUDA_OK(w, cudaStreamSynchronize(w->stream));
+    return B2G_OK;
+}
 
 int allocate(World* w, int nb, int nf) {
     DevWorld& d = w->d;
@@ -602,7 +653,7 @@ int allocate(World* w, int nb, int nf) {
     A(d.cnt, CNT_SIZE);
 #undef A
     w->allocated = true;
-    return B2G_OK;
+    return write_barrier_settings(w);
 }
 
 int upload(World* w) {
@@ -635,6 +686,7 @@ int upload(World* w) {
     CUDA_OK(w, cudaStreamSynchronize(s));
     w->uploaded_bodies = nb;
     w->uploaded_fixtures = nf;
+    w->host_dirty = false;
     d.n_bodies = nb;
     d.n_fixtures = nf;
     return B2G_OK;
@@ -701,7 +753,10 @@ int upload_joints(World* w) {
     std::vector<int> colour(nj, 0);
     std::vector<uint64_t> used(nb, 0);
     int ncol = 0;
+    int nlive = 0;
     for (int j = 0; j < nj; ++j) {
+        if (w->h_jdead[j]) continue;  /* a destroyed joint is in no colour */
+        ++nlive;
         const uint32_t a = w->joints[j].body_a, b = w->joints[j].body_b;
         const bool da = (w->h_flags[a] & BF_TYPE_MASK) == BODY_DYNAMIC, db = (w->h_flags[b] & BF_TYPE_MASK) == BODY_DYNAMIC;
         const uint64_t busy = (da ? used[a] : 0ull) | (db ? used[b] : 0ull);
@@ -714,15 +769,18 @@ int upload_joints(World* w) {
         ncol = std::max(ncol, c + 1);
     }
     w->h_jcoff.assign(kMaxJointColours + 1, 0);
-    for (int j = 0; j < nj; ++j) ++w->h_jcoff[colour[j] + 1];
+    for (int j = 0; j < nj; ++j)
+        if (!w->h_jdead[j]) ++w->h_jcoff[colour[j] + 1];
     for (int c = 0; c < kMaxJointColours; ++c) w->h_jcoff[c + 1] += w->h_jcoff[c];
-    w->h_jorder.assign(nj, 0);
+    w->h_jorder.assign(nlive, 0);
     {
         std::vector<int> fill(w->h_jcoff.begin(), w->h_jcoff.end() - 1);
-        for (int j = 0; j < nj; ++j) w->h_jorder[fill[colour[j]]++] = j;
+        for (int j = 0; j < nj; ++j)
+            if (!w->h_jdead[j]) w->h_jorder[fill[colour[j]]++] = j;
     }
     w->h_jnt_off.assign((size_t)nb + 1, 0);
     for (int j = 0; j < nj; ++j) {
+        if (w->h_jdead[j]) continue;
         ++w->h_jnt_off[(size_t)w->joints[j].body_a + 1];
         ++w->h_jnt_off[(size_t)w->joints[j].body_b + 1];
     }
@@ -731,6 +789,7 @@ int upload_joints(World* w) {
     {
         std::vector<int> fill(w->h_jnt_off.begin(), w->h_jnt_off.end() - 1);
         for (int j = 0; j < nj; ++j) {
+            if (w->h_jdead[j]) continue;
             w->h_jnt[(size_t)fill[w->joints[j].body_a]++] = j;
             w->h_jnt[(size_t)fill[w->joints[j].body_b]++] = j;
         }
@@ -742,7 +801,8 @@ int upload_joints(World* w) {
         std::vector<float4> an(nj), lim(nj), par(nj);
         for (int j = 0; j < nj; ++j) {
             const b2g_joint_def& jd = w->joints[j];
-            jb[j] = make_int2((int)jd.body_a, (int)jd.body_b);
+            /* a destroyed joint joins no islands: its body pair is (a, a) */
+            jb[j] = w->h_jdead[j] ? make_int2((int)jd.body_a, (int)jd.body_a) : make_int2((int)jd.body_a, (int)jd.body_b);
             an[j] = make_float4(jd.local_anchor_a.x, jd.local_anchor_a.y, jd.local_anchor_b.x, jd.local_anchor_b.y);
             uint32_t fl = ((uint32_t)jd.type << JF_TYPE_SHIFT) | (jd.collide_connected ? JF_COLLIDE : 0u);
             if (jd.type == B2G_JOINT_PULLEY) {
@@ -793,13 +853,14 @@ int upload_joints(World* w) {
         U(d.j_par, par.data(), nj);
         U(d.j_imp, w->h_jimp.data(), nj);
         U(d.j_imp2, w->h_jimp2.data(), nj);
-        U(d.j_order, w->h_jorder.data(), nj);
+        if (nlive > 0) U(d.j_order, w->h_jorder.data(), nlive);
         U(d.j_coff, w->h_jcoff.data(), kMaxJointColours + 1);
         U(d.b_jnt, w->h_jnt.data(), 2 * nj);
     }
 #undef U
     CUDA_OK(w, cudaStreamSynchronize(s));
     d.n_joints = nj;
+    if (d.n_jcolours != ncol) drop_graphs(w);  /* captured launches hold the colour count */
     d.n_jcolours = ncol;
     w->joints_dirty = false;
     return B2G_OK;
@@ -809,7 +870,7 @@ int upload_joints(World* w) {
 int prepare(World* w) {
     const int nb = (int)w->h_flags.size();
     const int nf = (int)w->h_fbody.size();
-    if (w->allocated && nb == w->uploaded_bodies && nf == w->uploaded_fixtures) {
+    if (w->allocated && nb == w->uploaded_bodies && nf == w->uploaded_fixtures && !w->host_dirty) {
         if (!w->joints_dirty) return B2G_OK;
         /* only joints were added: the device's bodies and fixtures stay as they are */
         int rc = download_joint_impulses(w);
@@ -867,7 +928,7 @@ int prepare(World* w) {
         if (rc != B2G_OK) return rc;
     }
     /* contact keys are refid_min << key_bits | refid_max; widening key_bits keeps their order */
-    const int kb = bits_for((uint64_t)std::max(1, 2 * w->proxies_created));
+    const int kb = bits_for((uint64_t)std::max(1u, w->next_node));
     if (kb != w->d.key_bits) {
         if (w->d.key_bits != 0) {
             /* re-key the current table: decode with the old width, encode with the new one */
@@ -887,6 +948,70 @@ int prepare(World* w) {
     int rc = upload(w);
     if (rc != B2G_OK) return rc;
     return upload_joints(w);
+}
+
+/* Host copy of the first n entries of the current contact table (n = the device's contact count). A
+ * contact destroyed between steps stays in the table, flagged CF_DEAD, until the next merge. */
+struct HostContacts {
+    int n = 0;
+    std::vector<int2> fix, body;
+    std::vector<uint32_t> flags;
+    std::vector<float4> mat, mgeo, mpts, mimp;
+    std::vector<uint4> mids;
+};
+
+int download_contacts(World* w, HostContacts& h, bool manifolds) {
+    CUDA_OK(w, cudaStreamSynchronize(w->stream));
+    CUDA_OK(w, cudaMemcpy(&h.n, w->d.cnt + CNT_CONTACTS, sizeof(int), cudaMemcpyDeviceToHost));
+    const int n = h.n;
+    const Contacts& c = w->d.c;
+    h.flags.resize(n);
+    h.fix.resize(n);
+    h.body.resize(n);
+    if (n == 0) return B2G_OK;
+    CUDA_OK(w, cudaMemcpy(h.flags.data(), c.flags, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    CUDA_OK(w, cudaMemcpy(h.fix.data(), c.fix, n * sizeof(int2), cudaMemcpyDeviceToHost));
+    CUDA_OK(w, cudaMemcpy(h.body.data(), c.body, n * sizeof(int2), cudaMemcpyDeviceToHost));
+    if (!manifolds) return B2G_OK;
+    h.mat.resize(n);
+    h.mgeo.resize(n);
+    h.mpts.resize(n);
+    h.mimp.resize(n);
+    h.mids.resize(n);
+    CUDA_OK(w, cudaMemcpy(h.mat.data(), c.mat, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    CUDA_OK(w, cudaMemcpy(h.mgeo.data(), c.mgeo, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    CUDA_OK(w, cudaMemcpy(h.mpts.data(), c.mpts, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    CUDA_OK(w, cudaMemcpy(h.mimp.data(), c.mimp, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    CUDA_OK(w, cudaMemcpy(h.mids.data(), c.mids, n * sizeof(uint4), cudaMemcpyDeviceToHost));
+    return B2G_OK;
+}
+
+void contact_info(const HostContacts& h, int i, b2g_contact_info& o) {
+    memset(&o, 0, sizeof(o));
+    o.fixture_a = (uint32_t)h.fix[i].x;
+    o.fixture_b = (uint32_t)h.fix[i].y;
+    o.touching = (h.flags[i] & CF_TOUCHING) ? 1 : 0;
+    o.manifold_type = (int)(h.mids[i].z & 0xffu);
+    o.point_count = (int)((h.mids[i].z >> 8) & 0xffu);
+    o.local_normal = b2g_vec2{h.mgeo[i].x, h.mgeo[i].y};
+    o.local_point = b2g_vec2{h.mgeo[i].z, h.mgeo[i].w};
+    o.point_local[0] = b2g_vec2{h.mpts[i].x, h.mpts[i].y};
+    o.point_local[1] = b2g_vec2{h.mpts[i].z, h.mpts[i].w};
+    o.normal_impulse[0] = h.mimp[i].x;
+    o.tangent_impulse[0] = h.mimp[i].y;
+    o.normal_impulse[1] = h.mimp[i].z;
+    o.tangent_impulse[1] = h.mimp[i].w;
+    o.point_id[0] = h.mids[i].x;
+    o.point_id[1] = h.mids[i].y;
+    o.friction = h.mat[i].x;
+    o.restitution = h.mat[i].y;
+    o.restitution_threshold = h.mat[i].z;
+}
+
+/* readers of a stepped world after a host-side edit: the edited mirrors go to the device first */
+int sync_host_edits(World* w) {
+    if (w->device_authoritative && w->host_dirty) return prepare(w);
+    return B2G_OK;
 }
 
 int status_error(World* w, int status);
@@ -910,10 +1035,16 @@ int status_error(World* w, int status) {
         cudaMemcpy(w->d.cnt + CNT_BARRIER, z2, sizeof(z2), cudaMemcpyHostToDevice);
         return fail(w, B2G_ERR_TIMEOUT, "a grid barrier wait timed out; the step's results are void");
     }
-    if (status & (ST_CONTACT_OVERFLOW | ST_PAIR_OVERFLOW | ST_STACK_OVERFLOW | ST_COLOUR_OVERFLOW))
+    if (status & (ST_CONTACT_OVERFLOW | ST_PAIR_OVERFLOW | ST_STACK_OVERFLOW | ST_COLOUR_OVERFLOW)) {
+        std::string what;
+        if (status & ST_CONTACT_OVERFLOW) what += " contacts";
+        if (status & ST_PAIR_OVERFLOW) what += " new-pairs";
+        if (status & ST_STACK_OVERFLOW) what += " traversal-stack";
+        if (status & ST_COLOUR_OVERFLOW) what += " colours";
         return fail(w, B2G_ERR_CAPACITY,
-                    "a device capacity overflowed (contacts, pairs, traversal stack or colours); raise "
-                    "contact_capacity / pair_capacity in b2g_world_def");
+                    "a device capacity overflowed (" + what.substr(1) +
+                        "); raise contact_capacity / pair_capacity in b2g_world_def");
+    }
     if (status & ST_EVENT_OVERFLOW) return fail(w, B2G_ERR_CAPACITY, "contact event buffer overflowed");
     if (status & ST_RECORD_OVERFLOW) return fail(w, B2G_ERR_CAPACITY, "recorded pair buffer overflowed");
     if (status & ST_TOI_OVERFLOW)
@@ -946,7 +1077,118 @@ StepParams make_params(World* w, float dt, int vi, int pi) {
     sp.record_pairs = w->record_pairs ? 1 : 0;
     sp.toi_schedule = w->toi_schedule;
     sp.toi_may_conflict = w->kinematic_or_bullet ? 1 : 0;
+    sp.custom_filter = w->filter_fn ? 1 : 0;
+    sp.pre_solve = w->pre_solve_fn ? 1 : 0;
     return sp;
+}
+
+/* ---- host callbacks inside a step ----
+ * The reference calls its contact filter from add_pair and from collide (for a flagged contact), and
+ * pre_solve from each contact's update. Here a world with such a callback runs its steps without
+ * graphs and stops at three points to run them on the host: before collide (the flagged contacts,
+ * whose answer goes to the device as CF_REJECT; the manifolds are also copied for pre_solve's old
+ * manifold), after collide (pre_solve of every updated, touching contact, in table order; its edits go
+ * back to the device before the solver), and after the broadphase's traversal (the new pairs, before
+ * they are sorted and merged). Each stop synchronises the world's stream: a slow path. */
+
+/* self.should_collide(other) on the host mirrors (B2body::should_collide, private/dynamics/b2_body.rs:391-416) */
+bool host_should_collide(const World* w, int self, int other) {
+    if ((w->h_flags[self] & BF_TYPE_MASK) != BODY_DYNAMIC && (w->h_flags[other] & BF_TYPE_MASK) != BODY_DYNAMIC)
+        return false;
+    for (size_t j = 0; j < w->joints.size(); ++j) {
+        if (w->h_jdead[j] || w->joints[j].collide_connected) continue;
+        const int a = (int)w->joints[j].body_a, b = (int)w->joints[j].body_b;
+        if ((a == self && b == other) || (a == other && b == self)) return false;
+    }
+    return true;
+}
+
+int hook_before_collide(World* w, HostContacts& old) {
+    int rc = download_contacts(w, old, w->pre_solve_fn != nullptr);
+    if (rc != B2G_OK || !w->filter_fn) return rc;
+    bool changed = false;
+    for (int i = 0; i < old.n; ++i) {
+        const uint32_t f = old.flags[i];
+        if (!(f & CF_FILTER) || (f & CF_DEAD)) continue;
+        if (!host_should_collide(w, old.body[i].y, old.body[i].x)) continue;  /* collide destroys it anyway */
+        const bool keep = w->filter_fn(w->filter_user, (uint32_t)old.fix[i].x, (uint32_t)old.fix[i].y) != 0;
+        const uint32_t nf = keep ? (f & ~CF_REJECT) : (f | CF_REJECT);
+        if (nf != f) {
+            old.flags[i] = nf;
+            changed = true;
+        }
+    }
+    if (changed && old.n > 0)
+        CUDA_OK(w, cudaMemcpy(w->d.c.flags, old.flags.data(), old.n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    return B2G_OK;
+}
+
+int hook_pre_solve(World* w, const HostContacts& old) {
+    HostContacts now;
+    int rc = download_contacts(w, now, true);
+    if (rc != B2G_OK) return rc;
+    bool changed = false;
+    for (int i = 0; i < now.n; ++i) {
+        const uint32_t f = now.flags[i];
+        if (!(f & CF_UPDATED) || !(f & CF_TOUCHING) || (f & CF_DEAD)) continue;
+        b2g_contact_info info, prev;
+        contact_info(now, i, info);
+        if (i < old.n) contact_info(old, i, prev);
+        else memset(&prev, 0, sizeof(prev));
+        b2g_contact_edit e;
+        e.enabled = (f & CF_ENABLED) ? 1 : 0;
+        e.friction = now.mat[i].x;
+        e.restitution = now.mat[i].y;
+        e.restitution_threshold = now.mat[i].z;
+        e.tangent_speed = now.mat[i].w;
+        w->pre_solve_fn(w->pre_solve_user, &info, &prev, &e);
+        const uint32_t nf = e.enabled ? (f | CF_ENABLED) : (f & ~CF_ENABLED);
+        const float4 nm = make_float4(e.friction, e.restitution, e.restitution_threshold, e.tangent_speed);
+        if (nf != f || memcmp(&nm, &now.mat[i], sizeof(nm)) != 0) {
+            now.flags[i] = nf;
+            now.mat[i] = nm;
+            changed = true;
+        }
+    }
+    if (changed) {
+        CUDA_OK(w, cudaMemcpy(w->d.c.flags, now.flags.data(), now.n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        CUDA_OK(w, cudaMemcpy(w->d.c.mat, now.mat.data(), now.n * sizeof(float4), cudaMemcpyHostToDevice));
+    }
+    return B2G_OK;
+}
+
+/* add_pair's call of the contact filter for the broadphase's new pairs (the fixtures of the smaller and
+ * the larger proxy id, as the pair was found); the pairs it rejects are removed before the merge */
+int hook_new_pairs(World* w) {
+    CUDA_OK(w, cudaStreamSynchronize(w->stream));
+    int n = 0;
+    CUDA_OK(w, cudaMemcpy(&n, w->d.cnt + CNT_NEW, sizeof(int), cudaMemcpyDeviceToHost));
+    n = std::min(n, w->d.pair_cap);
+    if (n <= 0) return B2G_OK;
+    std::vector<unsigned long long> key(n);
+    std::vector<int2> fix(n);
+    CUDA_OK(w, cudaMemcpy(key.data(), w->d.n_key, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    CUDA_OK(w, cudaMemcpy(fix.data(), w->d.n_fix, n * sizeof(int2), cudaMemcpyDeviceToHost));
+    int m = 0;
+    for (int i = 0; i < n; ++i) {
+        const int fa = fix[i].x, fb = fix[i].y;
+        const bool a_first = w->h_refid[fa] < w->h_refid[fb];
+        const bool keep = w->filter_fn(w->filter_user, (uint32_t)(a_first ? fa : fb), (uint32_t)(a_first ? fb : fa)) != 0;
+        if (!keep) continue;
+        key[m] = key[i];
+        fix[m] = fix[i];
+        ++m;
+    }
+    if (m == n) return B2G_OK;
+    std::vector<uint32_t> idx(std::max(m, 1));
+    for (int i = 0; i < m; ++i) idx[i] = (uint32_t)i;
+    if (m > 0) {
+        CUDA_OK(w, cudaMemcpy(w->d.n_key, key.data(), m * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+        CUDA_OK(w, cudaMemcpy(w->d.n_fix, fix.data(), m * sizeof(int2), cudaMemcpyHostToDevice));
+        CUDA_OK(w, cudaMemcpy(w->d.n_idx, idx.data(), m * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    }
+    CUDA_OK(w, cudaMemcpy(w->d.cnt + CNT_NEW, &m, sizeof(int), cudaMemcpyHostToDevice));
+    return B2G_OK;
 }
 
 /* The launch sequence of one step on the world's stream (captured into a graph or run directly).
@@ -959,15 +1201,25 @@ void issue_step(World* w, const StepParams& sp, float dt, bool capturing = false
         if (capturing) cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
         else cudaEventRecord(e, s);
     };
+    /* host callbacks (never under capture): the first failure is kept and the rest of the step skipped */
+    auto hook = [&](int rc) {
+        if (rc != B2G_OK && w->hook_rc == B2G_OK) w->hook_rc = rc;
+    };
+    auto pair_hook = [&](int k) {
+        if (k == 2 && w->filter_fn && w->hook_rc == B2G_OK) hook(hook_new_pairs(w));
+    };
     cudaMemsetAsync(w->d.cnt + CNT_EVENTS, 0, sizeof(int), s);
     mark(t.e[0]);
     if (w->new_contacts) {
-        launch_broadphase(w->d, sp, s, w->num_sms);
+        launch_broadphase(w->d, sp, s, w->num_sms, pair_hook);
         swap_contacts(w);
         w->new_contacts = false;
     }
     mark(t.e[1]);
+    HostContacts before;
+    if ((w->filter_fn || w->pre_solve_fn) && w->hook_rc == B2G_OK) hook(hook_before_collide(w, before));
     launch_collide(w->d, sp, s, w->allow_sleep || w->asleep_seen, w->num_sms);
+    if (w->pre_solve_fn && w->hook_rc == B2G_OK) hook(hook_pre_solve(w, before));
     mark(t.e[2]);
     if (dt > 0.0f) {
         launch_islands_and_constraints(w->d, sp, s);
@@ -979,7 +1231,10 @@ void issue_step(World* w, const StepParams& sp, float dt, bool capturing = false
         launch_solver(w->d, sp, s, w->num_sms, w->part_solve);
         if (taping) launch_tape_post(w->d, w->tape->d, sp, s, w->num_sms);
         mark(t.e[4]);
-        launch_broadphase(w->d, sp, s, w->num_sms, [&]() { mark(t.e[7]); });
+        launch_broadphase(w->d, sp, s, w->num_sms, [&](int k) {
+            mark(t.e[k == 0 ? 9 : k == 1 ? 10 : 7]);
+            pair_hook(k);
+        });
         swap_contacts(w);
         mark(t.e[8]);
         /* B2world::solve_toi (private/dynamics/b2_world.rs:946-950) */
@@ -990,6 +1245,8 @@ void issue_step(World* w, const StepParams& sp, float dt, bool capturing = false
         mark(t.e[6]);
         mark(t.e[3]);
         mark(t.e[4]);
+        mark(t.e[9]);
+        mark(t.e[10]);
         mark(t.e[7]);
         if (w->auto_clear) launch_clear_forces(w->d, s);
         mark(t.e[8]);
@@ -1043,7 +1300,8 @@ int step(World* w, float dt, int vi, int pi) {
     /* Steady state (no fixtures added since the last step, dt > 0, warm-start ratio already
      * set): the step's launch sequence depends only on the parameters, the allocation and the
      * contact-buffer parity, so it runs as one of two captured CUDA graphs. */
-    const bool graphable = w->use_graphs && !w->new_contacts && dt > 0.0f && w->steps > 0;
+    const bool graphable = w->use_graphs && !w->new_contacts && dt > 0.0f && w->steps > 0 && !w->filter_fn &&
+                           !w->pre_solve_fn;
     if (graphable) {
         GraphKey key{};
         key.dt = dt;
@@ -1098,7 +1356,12 @@ int step(World* w, float dt, int vi, int pi) {
         swap_contacts(w);
         w->inv_dt0 = sp.inv_dt;
     } else {
+        w->hook_rc = B2G_OK;
         issue_step(w, sp, dt);
+        if (w->hook_rc != B2G_OK) {
+            ++w->steps;
+            return w->hook_rc;
+        }
     }
     CUDA_OK(w, cudaGetLastError());
     ++w->steps;
@@ -1194,7 +1457,7 @@ __global__ void k_body_op(DevWorld d, int op, int b, float x, float y, float z, 
 }
 
 int body_op(World* w, int op, uint32_t b, float x, float y, float z, float px, float py, int wake) {
-    if (b >= w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body id out of range");
+    if (b >= w->h_flags.size() || w->h_bdead[b]) return fail(w, B2G_ERR_INVALID_ARG, "body id out of range or destroyed");
     tape_touch(w);
     if (w->device_authoritative) {
         int rc = prepare(w);
@@ -1234,6 +1497,7 @@ int b2g_world_create(const b2g_world_def* def, void** out) {
         return B2G_ERR_CUDA;
     }
     w->num_sms = prop.multiProcessorCount;
+    w->d.num_sms = w->num_sms;
     w->pageable = prop.pageableMemoryAccess != 0;
     if (!prop.cooperativeLaunch) {
         cudaStreamDestroy(w->stream);
@@ -1308,6 +1572,7 @@ int b2g_create_bodies(void* p, const b2g_body_def* defs, int32_t n, uint32_t* id
         w->h_damp.push_back(make_float4(d.linear_damping, d.angular_damping, d.gravity_scale, 0.0f));
         w->h_lc.push_back(make_float2(0.0f, 0.0f));
         w->body_fixtures.emplace_back();
+        w->h_bdead.push_back(0);
         if (ids) ids[i] = (uint32_t)id;
     }
     return B2G_OK;
@@ -1320,6 +1585,7 @@ int b2g_create_fixtures(void* p, const b2g_fixture_def* defs, int32_t n, uint32_
     for (int i = 0; i < n; ++i) {
         const b2g_fixture_def& d = defs[i];
         if (d.body >= w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "fixture body id out of range");
+        if (w->h_bdead[d.body]) return fail(w, B2G_ERR_INVALID_ARG, "fixture body was destroyed");
         if (d.shape_type < 0 || d.shape_type > 2)
             return fail(w, B2G_ERR_UNSUPPORTED, "shape type must be circle, edge or polygon (chain shapes are not supported)");
         if (!(d.density >= 0.0f) || !(d.friction >= 0.0f) || !(d.restitution >= 0.0f))
@@ -1348,8 +1614,7 @@ int b2g_create_fixtures(void* p, const b2g_fixture_def* defs, int32_t n, uint32_
             const V2 lo = sub(a.lo, r), hi = add(a.hi, r);
             w->h_fat.push_back(make_float4(lo.x, lo.y, hi.x, hi.y));
             w->h_moved.push_back(1);
-            w->h_refid.push_back(w->proxies_created == 0 ? 0u : (uint32_t)(2 * w->proxies_created - 1));
-            ++w->proxies_created;
+            w->h_refid.push_back(alloc_refid(w));
         } else {
             const float inf = INFINITY;
             w->h_fat.push_back(make_float4(inf, inf, -inf, -inf));
@@ -1357,6 +1622,7 @@ int b2g_create_fixtures(void* p, const b2g_fixture_def* defs, int32_t n, uint32_
             w->h_refid.push_back(0xffffffffu);
         }
         w->body_fixtures[b].insert(w->body_fixtures[b].begin(), f);
+        w->h_fdead.push_back(0);
         if (d.density > 0.0f) reset_mass_data(w, b);
         w->new_contacts = true;
         if (ids) ids[i] = (uint32_t)f;
@@ -1375,6 +1641,11 @@ int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* i
             return fail(w, B2G_ERR_UNSUPPORTED, "the gear joint is not on the GPU path");
         if (d.body_a >= w->h_flags.size() || d.body_b >= w->h_flags.size() || d.body_a == d.body_b)
             return fail(w, B2G_ERR_INVALID_ARG, "joint body ids out of range or equal");
+        if (w->h_bdead[d.body_a] || w->h_bdead[d.body_b]) return fail(w, B2G_ERR_INVALID_ARG, "a joint body was destroyed");
+        /* B2pulleyJointDef::initialize asserts ratio > B2_EPSILON (src/joints/b2_pulley_joint.rs:81) and
+         * the joint's constructor ratio != 0 (private/dynamics/joints/b2_pulley_joint.rs:30) */
+        if (d.type == B2G_JOINT_PULLEY && !(d.ratio > FLT_EPSILON))
+            return fail(w, B2G_ERR_INVALID_ARG, "a pulley joint's ratio must be greater than FLT_EPSILON");
     }
     if (n > 0) tape_touch(w);
     if (w->device_authoritative) {
@@ -1387,6 +1658,7 @@ int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* i
     for (int i = 0; i < n; ++i) {
         if (ids) ids[i] = (uint32_t)w->joints.size();
         w->joints.push_back(defs[i]);
+        w->h_jdead.push_back(0);
         if (defs[i].type == B2G_JOINT_MOUSE) {
             /* b2_mouse_joint_new (src/joints/b2_mouse_joint.rs:140-160): the target in body B's frame */
             const V2 la = mul_t(host_xf(w, (int)defs[i].body_b), mk(defs[i].target.x, defs[i].target.y));
@@ -1399,6 +1671,225 @@ int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* i
     }
     if (n > 0) w->joints_dirty = true;
     return B2G_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+/* The world's host mirrors made current before a host-side edit of a stepped world: first the edit's
+ * contact changes on the device (destroyed contacts, filtering flags), which may wake bodies, then the
+ * device's bodies and proxies are downloaded; the edited mirrors are uploaded by the next prepare. */
+int begin_host_edit(World* w, const std::vector<uint8_t>* fix_mark, const std::vector<int2>* body_pairs) {
+    if (!w->device_authoritative) {
+        w->host_dirty = true;
+        return B2G_OK;
+    }
+    int rc = prepare(w);
+    if (rc != B2G_OK) return rc;
+    rc = check_status(w);
+    if (rc != B2G_OK) return rc;
+    const bool any_mark = fix_mark && std::any_of(fix_mark->begin(), fix_mark->end(), [](uint8_t m) { return m != 0; });
+    const bool any_pair = body_pairs && !body_pairs->empty();
+    if (any_mark || any_pair) {
+        const int nf = (int)w->h_fbody.size();
+        const int np = any_pair ? (int)body_pairs->size() : 0;
+        uint8_t* d_mark = nullptr;
+        int2* d_pairs = nullptr;
+        if (cudaMalloc(&d_mark, (size_t)std::max(nf, 1)) != cudaSuccess ||
+            (np > 0 && cudaMalloc(&d_pairs, (size_t)np * sizeof(int2)) != cudaSuccess)) {
+            cudaFree(d_mark);
+            cudaGetLastError();
+            return fail(w, B2G_ERR_OUT_OF_MEMORY, "cudaMalloc for a contact edit failed");
+        }
+        int n_events0 = 0;
+        CUDA_OK(w, cudaMemcpy(&n_events0, w->d.cnt + CNT_EVENTS, sizeof(int), cudaMemcpyDeviceToHost));
+        cudaMemsetAsync(d_mark, 0, (size_t)std::max(nf, 1), w->stream);
+        if (any_mark) cudaMemcpyAsync(d_mark, fix_mark->data(), (size_t)nf, cudaMemcpyHostToDevice, w->stream);
+        if (np > 0) cudaMemcpyAsync(d_pairs, body_pairs->data(), (size_t)np * sizeof(int2), cudaMemcpyHostToDevice, w->stream);
+        launch_edit_contacts(w->d, d_mark, d_pairs, np, w->record_events, w->stream);
+        const cudaError_t e = cudaStreamSynchronize(w->stream);
+        cudaFree(d_mark);
+        cudaFree(d_pairs);
+        if (e != cudaSuccess) return fail(w, B2G_ERR_CUDA, cudaGetErrorString(e));
+        /* the destroyed contacts' end events wait on the host for the next b2g_get_events; the
+         * device list keeps only the last step's */
+        int n_events1 = 0;
+        CUDA_OK(w, cudaMemcpy(&n_events1, w->d.cnt + CNT_EVENTS, sizeof(int), cudaMemcpyDeviceToHost));
+        n_events1 = std::min(n_events1, w->d.event_cap);
+        if (n_events1 > n_events0) {
+            const size_t k = w->pending_events.size();
+            w->pending_events.resize(k + (size_t)(n_events1 - n_events0));
+            CUDA_OK(w, cudaMemcpy(w->pending_events.data() + k, w->d.events + n_events0,
+                                  (size_t)(n_events1 - n_events0) * sizeof(int4), cudaMemcpyDeviceToHost));
+            CUDA_OK(w, cudaMemcpy(w->d.cnt + CNT_EVENTS, &n_events0, sizeof(int), cudaMemcpyHostToDevice));
+        }
+        int status = 0;
+        CUDA_OK(w, cudaMemcpy(&status, w->d.cnt + CNT_STATUS, sizeof(int), cudaMemcpyDeviceToHost));
+        rc = status_error(w, status);
+        if (rc != B2G_OK) return rc;
+    }
+    rc = download_state(w);
+    if (rc != B2G_OK) return rc;
+    w->host_dirty = true;
+    return B2G_OK;
+}
+
+/* set_awake(true) on a host mirror (src/b2_body.rs:783-801): not for static bodies; sleep time 0 */
+void host_wake(World* w, int b) {
+    if ((w->h_flags[b] & BF_TYPE_MASK) == BODY_STATIC) return;
+    w->h_flags[b] |= BF_AWAKE;
+    w->h_vel[b].w = 0.0f;
+}
+
+/* a fixture's proxy is destroyed (B2fixture::destroy_proxies, private/dynamics/b2_fixture.rs:135-145) */
+void drop_proxy(World* w, int f) {
+    if (w->h_refid[f] != 0xffffffffu) free_refid(w, w->h_refid[f]);
+    w->h_refid[f] = 0xffffffffu;
+    const float inf = INFINITY;
+    w->h_fat[f] = make_float4(inf, inf, -inf, -inf);
+    w->h_moved[f] = 0;
+}
+
+bool has_duplicates(const uint32_t* ids, int n) {
+    std::vector<uint32_t> v(ids, ids + n);
+    std::sort(v.begin(), v.end());
+    return std::adjacent_find(v.begin(), v.end()) != v.end();
+}
+
+}  // namespace
+
+extern "C" {
+
+/* B2world::destroy_joint, private/dynamics/b2_world.rs:278-340, for each joint in the given order:
+ * both bodies woken, the joint leaves the solver and the islands, and without collide_connected the
+ * contacts between its bodies are flagged for filtering at the next collide. */
+int b2g_destroy_joints(void* p, const uint32_t* ids, int32_t n) {
+    World* w = W(p);
+    if (!w || n < 0 || (n > 0 && !ids)) return B2G_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i)
+        if (ids[i] >= w->joints.size() || w->h_jdead[ids[i]])
+            return fail(w, B2G_ERR_INVALID_ARG, "joint id out of range or already destroyed");
+    if (has_duplicates(ids, n)) return fail(w, B2G_ERR_INVALID_ARG, "a joint id appears twice");
+    if (n == 0) return B2G_OK;
+    tape_touch(w);
+    std::vector<int2> pairs;
+    for (int i = 0; i < n; ++i) {
+        const b2g_joint_def& j = w->joints[ids[i]];
+        if (!j.collide_connected) pairs.push_back(make_int2((int)j.body_a, (int)j.body_b));
+    }
+    int rc = download_joint_impulses(w);
+    if (rc != B2G_OK) return rc;
+    rc = begin_host_edit(w, nullptr, &pairs);
+    if (rc != B2G_OK) return rc;
+    for (int i = 0; i < n; ++i) {
+        const b2g_joint_def& j = w->joints[ids[i]];
+        host_wake(w, (int)j.body_a);
+        host_wake(w, (int)j.body_b);
+        w->h_jdead[ids[i]] = 1;
+    }
+    w->joints_dirty = true;
+    return B2G_OK;
+}
+
+/* B2body::destroy_fixture, private/dynamics/b2_body.rs:214-289, for each fixture in the given order:
+ * its contacts are destroyed (end events, wakes), its proxy is destroyed (the id returns to the
+ * tree's free list), it leaves its body's fixture list and the body's mass data is reset. */
+int b2g_destroy_fixtures(void* p, const uint32_t* ids, int32_t n) {
+    World* w = W(p);
+    if (!w || n < 0 || (n > 0 && !ids)) return B2G_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i)
+        if (ids[i] >= w->h_fbody.size() || w->h_fdead[ids[i]])
+            return fail(w, B2G_ERR_INVALID_ARG, "fixture id out of range or already destroyed");
+    if (has_duplicates(ids, n)) return fail(w, B2G_ERR_INVALID_ARG, "a fixture id appears twice");
+    if (n == 0) return B2G_OK;
+    tape_touch(w);
+    std::vector<uint8_t> mark(w->h_fbody.size(), 0);
+    for (int i = 0; i < n; ++i) mark[ids[i]] = 1;
+    int rc = begin_host_edit(w, &mark, nullptr);
+    if (rc != B2G_OK) return rc;
+    for (int i = 0; i < n; ++i) {
+        const int f = (int)ids[i];
+        const int b = w->h_fbody[f];
+        std::vector<int>& list = w->body_fixtures[b];
+        list.erase(std::remove(list.begin(), list.end(), f), list.end());
+        drop_proxy(w, f);
+        w->h_fdead[f] = 1;
+        reset_mass_data(w, b);
+    }
+    return B2G_OK;
+}
+
+/* B2world::destroy_body, private/dynamics/b2_world.rs:100-158, for each body in the given order: its
+ * joints are destroyed (newest first, waking their bodies), its contacts are destroyed (end events,
+ * wakes), its fixtures' proxies are destroyed in the body's fixture-list order (newest first). The
+ * body keeps its id as a static, disabled body without fixtures; its last state stays readable. */
+int b2g_destroy_bodies(void* p, const uint32_t* ids, int32_t n) {
+    World* w = W(p);
+    if (!w || n < 0 || (n > 0 && !ids)) return B2G_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i)
+        if (ids[i] >= w->h_flags.size() || w->h_bdead[ids[i]])
+            return fail(w, B2G_ERR_INVALID_ARG, "body id out of range or already destroyed");
+    if (has_duplicates(ids, n)) return fail(w, B2G_ERR_INVALID_ARG, "a body id appears twice");
+    if (n == 0) return B2G_OK;
+    tape_touch(w);
+    std::vector<uint8_t> dead_body(w->h_flags.size(), 0), mark(w->h_fbody.size(), 0);
+    for (int i = 0; i < n; ++i) dead_body[ids[i]] = 1;
+    for (size_t f = 0; f < w->h_fbody.size(); ++f)
+        if (!w->h_fdead[f] && dead_body[w->h_fbody[f]]) mark[f] = 1;
+    int rc = download_joint_impulses(w);
+    if (rc != B2G_OK) return rc;
+    rc = begin_host_edit(w, &mark, nullptr);
+    if (rc != B2G_OK) return rc;
+    bool joints_gone = false;
+    for (int i = 0; i < n; ++i) {
+        const uint32_t b = ids[i];
+        /* the body's joint list is newest first */
+        for (int j = (int)w->joints.size() - 1; j >= 0; --j) {
+            if (w->h_jdead[j] || (w->joints[j].body_a != b && w->joints[j].body_b != b)) continue;
+            host_wake(w, (int)w->joints[j].body_a);
+            host_wake(w, (int)w->joints[j].body_b);
+            w->h_jdead[j] = 1;
+            joints_gone = true;
+        }
+        for (int f : w->body_fixtures[b]) {
+            drop_proxy(w, f);
+            w->h_fdead[f] = 1;
+        }
+        w->body_fixtures[b].clear();
+        w->h_bdead[b] = 1;
+        w->h_flags[b] = (uint32_t)BODY_STATIC;  /* static, disabled, asleep: no step touches it */
+        w->h_mass[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    if (joints_gone) w->joints_dirty = true;
+    return B2G_OK;
+}
+
+/* B2fixture::set_filter_data + refilter (private/dynamics/b2_fixture.rs:175-211): the fixture's
+ * contacts are flagged for filtering at the next collide (destroyed there if the bodies or the
+ * filter no longer allow them) and its proxy is touched, so the next broadphase queries it and
+ * pairs the new filter allows are made. */
+int b2g_set_filter_data(void* p, uint32_t f, uint16_t category_bits, uint16_t mask_bits, int16_t group_index) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    if (f >= w->h_fbody.size() || w->h_fdead[f]) return fail(w, B2G_ERR_INVALID_ARG, "fixture id out of range or destroyed");
+    tape_touch(w);
+    std::vector<uint8_t> mark(w->h_fbody.size(), 0);
+    mark[f] = 2;
+    int rc = begin_host_edit(w, &mark, nullptr);
+    if (rc != B2G_OK) return rc;
+    w->h_filter[f] = (uint32_t)category_bits | ((uint32_t)mask_bits << 16);
+    w->h_group[f] = (uint32_t)(uint16_t)group_index | (w->h_group[f] & 0x10000u);
+    if (w->h_refid[f] != 0xffffffffu) w->h_moved[f] = 1;
+    return B2G_OK;
+}
+
+int b2g_refilter(void* p, uint32_t f) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    if (f >= w->h_fbody.size() || w->h_fdead[f]) return fail(w, B2G_ERR_INVALID_ARG, "fixture id out of range or destroyed");
+    const uint32_t x = w->h_filter[f];
+    return b2g_set_filter_data(p, f, (uint16_t)(x & 0xffffu), (uint16_t)(x >> 16), (int16_t)(w->h_group[f] & 0xffffu));
 }
 
 int b2g_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) {
@@ -1463,6 +1954,8 @@ int b2g_synchronize(void* p) {
 int b2g_get_body_states_async(void* p, uint32_t first, uint32_t count, b2g_body_state* out) {
     World* w = W(p);
     if (!w || (!out && count > 0)) return B2G_ERR_INVALID_ARG;
+    const int synced = sync_host_edits(w);
+    if (synced != B2G_OK) return synced;
     if ((size_t)first + count > w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body range out of bounds");
     if (count == 0) return B2G_OK;
     if (!(w->device_authoritative && (int)(first + count) <= w->uploaded_bodies))
@@ -1520,6 +2013,8 @@ int b2g_wait_body_states(void* p) {
 int b2g_get_body_states(void* p, uint32_t first, uint32_t count, b2g_body_state* out) {
     World* w = W(p);
     if (!w || (!out && count > 0)) return B2G_ERR_INVALID_ARG;
+    const int synced = sync_host_edits(w);
+    if (synced != B2G_OK) return synced;
     if ((size_t)first + count > w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body range out of bounds");
     if (count == 0) return B2G_OK;
     if (w->device_authoritative && (int)(first + count) <= w->uploaded_bodies) {
@@ -1578,6 +2073,8 @@ int b2g_get_body_states(void* p, uint32_t first, uint32_t count, b2g_body_state*
 int b2g_get_mass_data(void* p, uint32_t first, uint32_t count, float* out) {
     World* w = W(p);
     if (!w || (!out && count > 0)) return B2G_ERR_INVALID_ARG;
+    const int synced = sync_host_edits(w);
+    if (synced != B2G_OK) return synced;
     if ((size_t)first + count > w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body range out of bounds");
     std::vector<float4> m(count);
     std::vector<float2> lc(count);
@@ -1607,7 +2104,7 @@ int b2g_get_mass_data(void* p, uint32_t first, uint32_t count, float* out) {
 int b2g_set_transform(void* p, uint32_t b, b2g_vec2 position, float angle) {
     World* w = W(p);
     if (!w) return B2G_ERR_INVALID_ARG;
-    if (b >= w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body id out of range");
+    if (b >= w->h_flags.size() || w->h_bdead[b]) return fail(w, B2G_ERR_INVALID_ARG, "body id out of range or destroyed");
     tape_touch(w);
     if (w->device_authoritative) {
         int rc = prepare(w);
@@ -1685,6 +2182,8 @@ int b2g_set_awake(void* p, uint32_t b, int32_t flag) {
 int b2g_get_awake(void* p, uint32_t first, uint32_t count, uint8_t* out) {
     World* w = W(p);
     if (!w || (!out && count)) return B2G_ERR_INVALID_ARG;
+    const int synced = sync_host_edits(w);
+    if (synced != B2G_OK) return synced;
     if ((size_t)first + count > w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "body range out of bounds");
     if (count == 0) return B2G_OK;
     std::vector<uint32_t> fl(count);
@@ -1724,7 +2223,10 @@ int b2g_set_warm_starting(void* p, int32_t flag) {
 }
 int b2g_set_continuous_physics(void* p, int32_t flag) {
     if (!p) return B2G_ERR_INVALID_ARG;
-    W(p)->continuous = flag != 0;
+    World* w = W(p);
+    if (flag && (w->filter_fn || w->pre_solve_fn))
+        return fail(w, B2G_ERR_UNSUPPORTED, "host contact filters and pre_solve callbacks cannot run inside the continuous pass");
+    w->continuous = flag != 0;
     return B2G_OK;
 }
 int b2g_set_toi_schedule(void* p, int32_t schedule) {
@@ -1760,6 +2262,41 @@ int b2g_set_record_pairs(void* p, int32_t flag) {
     if (!p) return B2G_ERR_INVALID_ARG;
     W(p)->record_pairs = flag != 0;
     return B2G_OK;
+}
+
+int b2g_set_contact_filter(void* p, b2g_contact_filter_fn fn, void* user) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    if (fn && w->continuous)
+        return fail(w, B2G_ERR_UNSUPPORTED, "a host contact filter cannot run inside the continuous pass; turn continuous physics off");
+    w->filter_fn = fn;
+    w->filter_user = user;
+    return B2G_OK;
+}
+
+int b2g_set_pre_solve(void* p, b2g_pre_solve_fn fn, void* user) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    if (fn && w->continuous)
+        return fail(w, B2G_ERR_UNSUPPORTED, "a pre_solve callback cannot run inside the continuous pass; turn continuous physics off");
+    w->pre_solve_fn = fn;
+    w->pre_solve_user = user;
+    return B2G_OK;
+}
+
+int b2g_set_barrier_limit(void* p, int64_t cycles) {
+    World* w = W(p);
+    if (!w || cycles < 0) return B2G_ERR_INVALID_ARG;
+    const long long units = cycles == 0 ? 0 : std::max(1LL, std::min((long long)INT32_MAX, (long long)(cycles >> 10)));
+    w->barrier_limit_units = (int)units;
+    return write_barrier_settings(w);
+}
+
+int b2g_debug_hold_barriers(void* p, int32_t extra) {
+    World* w = W(p);
+    if (!w || extra < 0) return B2G_ERR_INVALID_ARG;
+    w->barrier_hold = extra;
+    return write_barrier_settings(w);
 }
 
 int b2g_set_graph_capture(void* p, int32_t flag) {
@@ -1805,8 +2342,18 @@ int b2g_get_phase_times(void* p, float* out, int32_t n) {
     if (!w || !out || n < 7) return B2G_ERR_INVALID_ARG;
     int rc = check_status(w);
     if (rc != B2G_OK) return rc;
-    for (int i = 0; i < 7; ++i) out[i] = 0.0f;
+    for (int i = 0; i < std::min(n, 10); ++i) out[i] = 0.0f;
     if (!w->timer.valid || w->steps == 0) return B2G_OK;
+    if (n >= 10) {
+        /* the tree pass in three: keys + sort, hierarchy, traversal (events 4, 9, 10, 7) */
+        const int sub[4] = {4, 9, 10, 7};
+        for (int i = 0; i < 3; ++i) {
+            if (cudaEventElapsedTime(&out[7 + i], w->timer.e[sub[i]], w->timer.e[sub[i + 1]]) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(w, B2G_ERR_CUDA, "profile events could not be timed");
+            }
+        }
+    }
     /* event order within a step: 0 start, 1 after the initial broadphase, 2 after collide,
      * 6 after islands, 3 after colouring, 4 after the solver, 7 after the tree pass, 5 end */
     const int order[8] = {0, 1, 2, 6, 3, 4, 7, 5};
@@ -1818,6 +2365,26 @@ int b2g_get_phase_times(void* p, float* out, int32_t n) {
         }
     }
     for (int i = 0; i < 7; ++i) out[i] = t[i + 1] - t[i];
+    return B2G_OK;
+}
+
+int b2g_get_step_stats(void* p, b2g_step_stats* out) {
+    World* w = W(p);
+    if (!w || !out) return B2G_ERR_INVALID_ARG;
+    memset(out, 0, sizeof(*out));
+    if (!w->allocated) return B2G_OK;
+    int rc = check_status(w);
+    if (rc != B2G_OK) return rc;
+    int cnt[CNT_SIZE];
+    CUDA_OK(w, cudaMemcpy(cnt, w->d.cnt, sizeof(cnt), cudaMemcpyDeviceToHost));
+    out->bp_node_visits = cnt[CNT_BP_VISITS];
+    out->bp_leaf_checks = cnt[CNT_BP_CANDIDATES];
+    out->new_pairs = cnt[CNT_NEW];
+    out->contacts = cnt[CNT_CONTACTS];
+    out->constraints = cnt[CNT_CONS];
+    out->interior_slots = cnt[CNT_INTERIOR];
+    out->parts = cnt[CNT_PARTS];
+    out->colours = cnt[CNT_COLOURS];
     return B2G_OK;
 }
 
@@ -1853,7 +2420,7 @@ int b2g_get_counts(void* p, b2g_counts* out) {
 namespace {
 
 constexpr uint32_t kStateMagic = 0x53473242u;  /* "B2GS" */
-constexpr uint32_t kStateVersion = 1;
+constexpr uint32_t kStateVersion = 2;
 
 struct StateHeader {
     uint32_t magic, version;
@@ -1876,10 +2443,91 @@ int state_ready(World* w) {
     return check_status(w);
 }
 
+/* The host-side part of a world's state, after the device buffers: destroyed-object marks, the
+ * joint definitions (a mouse joint's target moves), the proxy-id free list and the next fresh node. */
+std::vector<unsigned char> host_state(const World* w) {
+    std::vector<unsigned char> b;
+    auto put = [&b](const void* p, size_t n) {
+        const unsigned char* c = (const unsigned char*)p;
+        b.insert(b.end(), c, c + n);
+    };
+    const int32_t nb = (int32_t)w->h_bdead.size(), nf = (int32_t)w->h_fdead.size(), nj = (int32_t)w->joints.size();
+    const int32_t nfree = (int32_t)w->free_refids.size();
+    put(&nb, sizeof(nb));
+    put(w->h_bdead.data(), (size_t)nb);
+    put(&nf, sizeof(nf));
+    put(w->h_fdead.data(), (size_t)nf);
+    put(&nj, sizeof(nj));
+    put(w->joints.data(), (size_t)nj * sizeof(b2g_joint_def));
+    put(w->h_jdead.data(), (size_t)nj);
+    put(&nfree, sizeof(nfree));
+    put(w->free_refids.data(), (size_t)nfree * sizeof(uint32_t));
+    put(&w->next_node, sizeof(w->next_node));
+    return b;
+}
+
 uint64_t state_bytes(const World* w) {
     uint64_t n = sizeof(StateHeader) + w->alloc_bytes.size() * sizeof(uint64_t);
     for (size_t b : w->alloc_bytes) n += b;
-    return n;
+    return n + host_state(w).size();
+}
+
+/* After a load: every host mirror from the loaded device buffers, and the host part of the state. */
+int load_host_state(World* w, const unsigned char* src, const unsigned char* end) {
+    auto get = [&src, end](void* p, size_t n) {
+        if ((size_t)(end - src) < n) return false;
+        memcpy(p, src, n);
+        src += n;
+        return true;
+    };
+    int32_t nb = 0, nf = 0, nj = 0, nfree = 0;
+    if (!get(&nb, sizeof(nb)) || nb != (int32_t)w->h_flags.size()) return fail(w, B2G_ERR_INVALID_ARG, "state body count");
+    if (!get(w->h_bdead.data(), (size_t)nb)) return fail(w, B2G_ERR_INVALID_ARG, "truncated state");
+    if (!get(&nf, sizeof(nf)) || nf != (int32_t)w->h_fbody.size()) return fail(w, B2G_ERR_INVALID_ARG, "state fixture count");
+    if (!get(w->h_fdead.data(), (size_t)nf)) return fail(w, B2G_ERR_INVALID_ARG, "truncated state");
+    if (!get(&nj, sizeof(nj)) || nj != (int32_t)w->joints.size()) return fail(w, B2G_ERR_INVALID_ARG, "state joint count");
+    if (!get(w->joints.data(), (size_t)nj * sizeof(b2g_joint_def)) || !get(w->h_jdead.data(), (size_t)nj))
+        return fail(w, B2G_ERR_INVALID_ARG, "truncated state");
+    if (!get(&nfree, sizeof(nfree)) || nfree < 0) return fail(w, B2G_ERR_INVALID_ARG, "truncated state");
+    w->free_refids.resize((size_t)nfree);
+    if (!get(w->free_refids.data(), (size_t)nfree * sizeof(uint32_t)) || !get(&w->next_node, sizeof(w->next_node)))
+        return fail(w, B2G_ERR_INVALID_ARG, "truncated state");
+    DevWorld& d = w->d;
+#define D(src_, dst, n) CUDA_OK(w, cudaMemcpy((dst).data(), (src_), (size_t)(n) * sizeof((dst)[0]), cudaMemcpyDeviceToHost))
+    if (nb > 0) {
+        D(d.b_xf, w->h_xf, nb); D(d.b_pos, w->h_pos, nb); D(d.b_pos0, w->h_pos0, nb); D(d.b_vel, w->h_vel, nb);
+        D(d.b_force, w->h_force, nb); D(d.b_mass, w->h_mass, nb); D(d.b_damp, w->h_damp, nb); D(d.b_lc, w->h_lc, nb);
+        D(d.b_flags, w->h_flags, nb); D(d.b_world, w->h_world, nb);
+    }
+    if (nf > 0) {
+        D(d.f_shape, w->h_shape, nf); D(d.f_body, w->h_fbody, nf); D(d.f_mat, w->h_fmat, nf);
+        D(d.f_filter, w->h_filter, nf); D(d.f_group, w->h_group, nf); D(d.f_refid, w->h_refid, nf);
+        D(d.f_fat, w->h_fat, nf); D(d.f_moved, w->h_moved, nf);
+    }
+#undef D
+    /* fixture lists, newest first (fixtures are appended in creation order) */
+    for (auto& l : w->body_fixtures) l.clear();
+    for (int f = nf - 1; f >= 0; --f)
+        if (!w->h_fdead[f]) w->body_fixtures[w->h_fbody[f]].push_back(f);
+    int live = 0;
+    for (int f = 0; f < nf; ++f) live += w->h_refid[f] != 0xffffffffu ? 1 : 0;
+    w->proxies_created = live;
+    w->kinematic_or_bullet = false;
+    for (int b = 0; b < nb; ++b) {
+        const uint32_t fl = w->h_flags[b];
+        if ((fl & BF_TYPE_MASK) == BODY_KINEMATIC || ((fl & BF_TYPE_MASK) == BODY_DYNAMIC && (fl & BF_BULLET)))
+            w->kinematic_or_bullet = true;
+    }
+    /* the joints' host copies: impulses from the device, then the colouring and tables re-derived (and
+     * re-uploaded: the same contents the state holds) */
+    if (nj > 0) {
+        int rc = download_joint_impulses(w);
+        if (rc != B2G_OK) return rc;
+        rc = upload_joints(w);
+        if (rc != B2G_OK) return rc;
+    }
+    w->host_dirty = false;
+    return B2G_OK;
 }
 
 }  // namespace
@@ -1939,6 +2587,8 @@ int b2g_state_save(void* p, void* out, uint64_t bytes) {
         CUDA_OK(w, cudaMemcpy(o, w->allocations[i], w->alloc_bytes[i], cudaMemcpyDeviceToHost));
         o += w->alloc_bytes[i];
     }
+    const std::vector<unsigned char> hs = host_state(w);
+    memcpy(o, hs.data(), hs.size());
     return B2G_OK;
 }
 
@@ -1950,6 +2600,7 @@ int b2g_state_load(void* p, const void* in, uint64_t bytes) {
     memcpy(&h, in, sizeof(h));
     if (h.magic != kStateMagic || h.version != kStateVersion || h.buffer_bytes != bytes)
         return fail(w, B2G_ERR_INVALID_ARG, "not a world state of this version");
+    const unsigned char* end = (const unsigned char*)in + bytes;
     int rc = state_ready(w);
     if (rc != B2G_OK) return rc;
     rc = ensure_minsep_buffers(w, h.minsep_buffers);
@@ -1969,6 +2620,7 @@ int b2g_state_load(void* p, const void* in, uint64_t bytes) {
                     "the state was saved from a world of another layout (bodies, fixtures, capacities or worlds)");
     src += (size_t)h.n_alloc * sizeof(uint64_t);
     for (size_t i = 0; i < w->allocations.size(); ++i) {
+        if ((size_t)(end - src) < w->alloc_bytes[i]) return fail(w, B2G_ERR_INVALID_ARG, "truncated state");
         CUDA_OK(w, cudaMemcpy(w->allocations[i], src, w->alloc_bytes[i], cudaMemcpyHostToDevice));
         src += w->alloc_bytes[i];
     }
@@ -1989,7 +2641,10 @@ int b2g_state_load(void* p, const void* in, uint64_t bytes) {
     w->proxies_created = h.proxies_created;
     w->gravity = h.gravity;
     w->device_authoritative = true;
-    return B2G_OK;
+    rc = load_host_state(w, src, end);
+    if (rc != B2G_OK) return rc;
+    /* the barrier settings are the world's, not the saved state's */
+    return write_barrier_settings(w);
 }
 
 int b2g_get_toi_stats(void* p, int32_t* events, int32_t* last_iterations, int32_t* restarts) {
@@ -2016,44 +2671,16 @@ int b2g_get_contacts(void* p, b2g_contact_info* out, int32_t cap, int32_t* n) {
     if (!w->allocated) return B2G_OK;
     int rc = check_status(w);
     if (rc != B2G_OK) return rc;
-    int nc = 0;
-    CUDA_OK(w, cudaMemcpy(&nc, w->d.cnt + CNT_CONTACTS, sizeof(int), cudaMemcpyDeviceToHost));
-    *n = nc;
-    if (!out || cap < nc || nc == 0) return B2G_OK;
-    const Contacts& c = w->d.c;
-    std::vector<int2> fix(nc);
-    std::vector<uint32_t> flags(nc);
-    std::vector<float4> mat(nc), mgeo(nc), mpts(nc), mimp(nc);
-    std::vector<uint4> mids(nc);
-    cudaMemcpy(fix.data(), c.fix, nc * sizeof(int2), cudaMemcpyDeviceToHost);
-    cudaMemcpy(flags.data(), c.flags, nc * sizeof(uint32_t), cudaMemcpyDeviceToHost);
-    cudaMemcpy(mat.data(), c.mat, nc * sizeof(float4), cudaMemcpyDeviceToHost);
-    cudaMemcpy(mgeo.data(), c.mgeo, nc * sizeof(float4), cudaMemcpyDeviceToHost);
-    cudaMemcpy(mpts.data(), c.mpts, nc * sizeof(float4), cudaMemcpyDeviceToHost);
-    cudaMemcpy(mimp.data(), c.mimp, nc * sizeof(float4), cudaMemcpyDeviceToHost);
-    CUDA_OK(w, cudaMemcpy(mids.data(), c.mids, nc * sizeof(uint4), cudaMemcpyDeviceToHost));
-    for (int i = 0; i < nc; ++i) {
-        b2g_contact_info& o = out[i];
-        memset(&o, 0, sizeof(o));
-        o.fixture_a = (uint32_t)fix[i].x;
-        o.fixture_b = (uint32_t)fix[i].y;
-        o.touching = (flags[i] & CF_TOUCHING) ? 1 : 0;
-        o.manifold_type = (int)(mids[i].z & 0xffu);
-        o.point_count = (int)((mids[i].z >> 8) & 0xffu);
-        o.local_normal = b2g_vec2{mgeo[i].x, mgeo[i].y};
-        o.local_point = b2g_vec2{mgeo[i].z, mgeo[i].w};
-        o.point_local[0] = b2g_vec2{mpts[i].x, mpts[i].y};
-        o.point_local[1] = b2g_vec2{mpts[i].z, mpts[i].w};
-        o.normal_impulse[0] = mimp[i].x;
-        o.tangent_impulse[0] = mimp[i].y;
-        o.normal_impulse[1] = mimp[i].z;
-        o.tangent_impulse[1] = mimp[i].w;
-        o.point_id[0] = mids[i].x;
-        o.point_id[1] = mids[i].y;
-        o.friction = mat[i].x;
-        o.restitution = mat[i].y;
-        o.restitution_threshold = mat[i].z;
-    }
+    HostContacts h;
+    rc = download_contacts(w, h, out != nullptr);
+    if (rc != B2G_OK) return rc;
+    int live = 0;
+    for (int i = 0; i < h.n; ++i) live += (h.flags[i] & CF_DEAD) ? 0 : 1;
+    *n = live;
+    if (!out || cap < live || live == 0) return B2G_OK;
+    int k = 0;
+    for (int i = 0; i < h.n; ++i)
+        if (!(h.flags[i] & CF_DEAD)) contact_info(h, i, out[k++]);
     return B2G_OK;
 }
 
@@ -2064,13 +2691,17 @@ int b2g_get_events(void* p, b2g_contact_event* out, int32_t cap, int32_t* n) {
     if (!w->allocated) return B2G_OK;
     int rc = check_status(w);
     if (rc != B2G_OK) return rc;
-    int ne = 0;
-    CUDA_OK(w, cudaMemcpy(&ne, w->d.cnt + CNT_EVENTS, sizeof(int), cudaMemcpyDeviceToHost));
-    ne = std::min(ne, w->d.event_cap);
+    int nd = 0;
+    CUDA_OK(w, cudaMemcpy(&nd, w->d.cnt + CNT_EVENTS, sizeof(int), cudaMemcpyDeviceToHost));
+    nd = std::min(nd, w->d.event_cap);
+    const int np = (int)w->pending_events.size();
+    const int ne = nd + np;
     *n = ne;
     if (!out || cap < ne || ne == 0) return B2G_OK;
     std::vector<int4> ev(ne);
-    CUDA_OK(w, cudaMemcpy(ev.data(), w->d.events, ne * sizeof(int4), cudaMemcpyDeviceToHost));
+    std::copy(w->pending_events.begin(), w->pending_events.end(), ev.begin());
+    if (nd > 0) CUDA_OK(w, cudaMemcpy(ev.data() + np, w->d.events, nd * sizeof(int4), cudaMemcpyDeviceToHost));
+    w->pending_events.clear();
     std::sort(ev.begin(), ev.end(), [](const int4& a, const int4& b) {
         if (a.x != b.x) return a.x < b.x;
         if (a.y != b.y) return a.y < b.y;
@@ -2102,9 +2733,19 @@ int b2g_get_pairs(void* p, uint32_t* out, int32_t cap, int32_t* n) {
     return B2G_OK;
 }
 
+int b2g_get_proxy_ids(void* p, int32_t* out, int32_t cap) {
+    World* w = W(p);
+    if (!w || (!out && cap > 0)) return B2G_ERR_INVALID_ARG;
+    const int nf = std::min((int)w->h_refid.size(), (int)cap);
+    for (int f = 0; f < nf; ++f) out[f] = w->h_refid[f] == 0xffffffffu ? -1 : (int32_t)w->h_refid[f];
+    return B2G_OK;
+}
+
 int b2g_get_proxies(void* p, float* aabbs, uint8_t* moved, int32_t cap) {
     World* w = W(p);
     if (!w) return B2G_ERR_INVALID_ARG;
+    const int synced = sync_host_edits(w);
+    if (synced != B2G_OK) return synced;
     const int nf = std::min((int)w->h_fbody.size(), (int)cap);
     if (w->device_authoritative) {
         int rc = check_status(w);
@@ -2274,6 +2915,8 @@ alignas(256) unsigned char g_noalloc_host[kNoAllocBytes]; /* host staging, same 
 std::mutex g_noalloc_lock;
 constexpr int kNoAllocDevices = 64;
 void* g_noalloc_dev[kNoAllocDevices] = {}; /* device address of the scratch, per device ordinal */
+int noalloc_collide(int dev, const b2g_fixture_def* da, const float* xfa, const b2g_fixture_def* db, const float* xfb,
+                    int32_t n, b2g_contact_info* out);
 }  // namespace
 
 extern "C" {
@@ -2286,6 +2929,20 @@ int b2g_collide_pairs_noalloc(const b2g_fixture_def* da, const float* xfa, const
     std::lock_guard<std::mutex> guard(g_noalloc_lock);
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocDevices) return B2G_ERR_CUDA;
+    /* an error left pending on this thread by an earlier, unrelated call is not this call's */
+    (void)cudaGetLastError();
+    int rc = noalloc_collide(dev, da, xfa, db, xfb, n, out);
+    /* a failed call forgets the device address, so a call after a device reset looks it up again */
+    if (rc == B2G_ERR_CUDA) g_noalloc_dev[dev] = nullptr;
+    return rc;
+}
+
+}  // extern "C"
+
+namespace {
+
+int noalloc_collide(int dev, const b2g_fixture_def* da, const float* xfa, const b2g_fixture_def* db, const float* xfb,
+                    int32_t n, b2g_contact_info* out) {
     if (!g_noalloc_dev[dev]) {
         /* set-up on the first call on this device (the device is current here) */
         void* p = nullptr;
@@ -2344,6 +3001,46 @@ int b2g_collide_pairs_noalloc(const b2g_fixture_def* da, const float* xfa, const
         o.point_local[1] = b2g_vec2{pts[i].z, pts[i].w};
         o.point_id[0] = ids[i].x;
         o.point_id[1] = ids[i].y;
+    }
+    return B2G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+/* B2island::report (private/dynamics/b2_island_private.rs:460-487) of the last step's discrete solve:
+ * the constraint slots' fixture pairs, solved point counts and impulses after the velocity iterations
+ * (the velocity-constraint arrays keep them until the next step's constraint initialisation) */
+int b2g_get_post_solve(void* p, b2g_contact_impulse* out, int32_t cap, int32_t* n) {
+    World* w = W(p);
+    if (!w || !n || (!out && cap > 0)) return B2G_ERR_INVALID_ARG;
+    *n = 0;
+    if (!w->allocated || !w->device_authoritative) return B2G_OK;
+    int rc = check_status(w);
+    if (rc != B2G_OK) return rc;
+    int nc = 0;
+    CUDA_OK(w, cudaMemcpy(&nc, w->d.cnt + CNT_CONS, sizeof(int), cudaMemcpyDeviceToHost));
+    *n = nc;
+    if (!out || cap < nc || nc == 0) return B2G_OK;
+    std::vector<int2> fx(nc);
+    std::vector<int4> idx(nc);
+    std::vector<float4> imp(nc);
+    CUDA_OK(w, cudaMemcpy(fx.data(), w->d.s_fix, nc * sizeof(int2), cudaMemcpyDeviceToHost));
+    CUDA_OK(w, cudaMemcpy(idx.data(), w->d.vc_idx, nc * sizeof(int4), cudaMemcpyDeviceToHost));
+    CUDA_OK(w, cudaMemcpy(imp.data(), w->d.vc_imp, nc * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < nc; ++i) {
+        b2g_contact_impulse& r = out[i];
+        memset(&r, 0, sizeof(r));
+        r.fixture_a = (uint32_t)fx[i].x;
+        r.fixture_b = (uint32_t)fx[i].y;
+        r.count = idx[i].z;
+        r.normal_impulses[0] = imp[i].x;
+        r.tangent_impulses[0] = imp[i].y;
+        if (r.count > 1) {
+            r.normal_impulses[1] = imp[i].z;
+            r.tangent_impulses[1] = imp[i].w;
+        }
     }
     return B2G_OK;
 }

@@ -132,27 +132,35 @@ __device__ __forceinline__ bool joint_allows(const DevWorld& w, int a, int b) {
 
 /* b2_contact_manager_add_pair's rejections after the existing-contact check
  * (private/dynamics/b2_contact_manager.rs:178-302): same body, no dynamic body, a joint that keeps
- * the bodies apart, the default
- * filter (private/dynamics/b2_world_callbacks.rs:6-18), no manifold routine for the two shape types
- * (b2_contact_registers.rs:67-103). f is the fixture with the smaller proxy id. On acceptance
- * (fa, fb) is the contact's fixture pair, fixture A the one of the primary shape type. */
-__device__ __forceinline__ bool pair_accept(const DevWorld& w, int f, int g, int& fa, int& fb) {
+ * the bodies apart, the default filter (private/dynamics/b2_world_callbacks.rs:6-18; skipped when the
+ * host's contact filter replaces it and filters the new pairs itself), no manifold routine for the
+ * two shape types (b2_contact_registers.rs:67-103). f is the fixture with the smaller proxy id. On
+ * acceptance (fa, fb) is the contact's fixture pair, fixture A the one of the primary shape type. */
+/* the default contact filter, should_collide of private/dynamics/b2_world_callbacks.rs:6-18, on the
+ * fixtures' current filter data (f_filter = category | mask << 16, f_group = group (int16) | sensor << 16) */
+__device__ __forceinline__ bool filter_allows(const DevWorld& w, int fa, int fb) {
+    const uint32_t xa = w.f_filter[fa], xb = w.f_filter[fb];
+    const int grp_a = (int)(int16_t)(w.f_group[fa] & 0xffffu);
+    const int grp_b = (int)(int16_t)(w.f_group[fb] & 0xffffu);
+    if (grp_a == grp_b && grp_a != 0) return grp_a > 0;
+    return ((xa >> 16) & (xb & 0xffffu)) != 0u && ((xa & 0xffffu) & (xb >> 16)) != 0u;
+}
+
+/* self.should_collide(other), B2body::should_collide (private/dynamics/b2_body.rs:391-416): one body
+ * dynamic, no joint of self's keeping it from other */
+__device__ __forceinline__ bool bodies_collide(const DevWorld& w, int self, int other) {
+    const uint32_t fs = w.b_flags[self], fo = w.b_flags[other];
+    if ((fs & BF_TYPE_MASK) != BODY_DYNAMIC && (fo & BF_TYPE_MASK) != BODY_DYNAMIC) return false;
+    return joint_allows(w, self, other);
+}
+
+__device__ __forceinline__ bool pair_accept(const DevWorld& w, int f, int g, int& fa, int& fb, bool default_filter = true) {
     fa = f;
     fb = g;
     const int ba = w.f_body[fa], bb = w.f_body[fb];
     if (ba == bb) return false;
-    const uint32_t fla = w.b_flags[ba], flb = w.b_flags[bb];
-    if ((fla & BF_TYPE_MASK) != BODY_DYNAMIC && (flb & BF_TYPE_MASK) != BODY_DYNAMIC) return false;
-    if (!joint_allows(w, bb, ba)) return false;
-    /* f_filter = category | mask << 16, f_group = group (int16) | sensor << 16 */
-    const uint32_t xa = w.f_filter[fa], xb = w.f_filter[fb];
-    const int grp_a = (int)(int16_t)(w.f_group[fa] & 0xffffu);
-    const int grp_b = (int)(int16_t)(w.f_group[fb] & 0xffffu);
-    if (grp_a == grp_b && grp_a != 0) {
-        if (grp_a <= 0) return false;
-    } else if (((xa >> 16) & (xb & 0xffffu)) == 0u || ((xa & 0xffffu) & (xb >> 16)) == 0u) {
-        return false;
-    }
+    if (!bodies_collide(w, bb, ba)) return false;
+    if (default_filter && !filter_allows(w, fa, fb)) return false;
     const int reg = register_kind(shape_type(w.f_shape[fa]), shape_type(w.f_shape[fb]));
     if (reg == 0) return false;
     if (reg < 0) {

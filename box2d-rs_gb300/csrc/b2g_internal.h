@@ -45,6 +45,8 @@ enum : uint32_t {
     CF_DEAD = 1u << 2,
     CF_SENSOR = 1u << 3,
     CF_FILTER = 1u << 4,   /* E_FILTER_FLAG: re-check should_collide at the next collide */
+    CF_REJECT = 1u << 5,   /* the host's contact filter rejected this flagged contact (destroyed at collide) */
+    CF_UPDATED = 1u << 6,  /* updated by this step's collide (kept only while a pre_solve callback is set) */
     CF_KIND_SHIFT = 8,
 };
 
@@ -100,6 +102,10 @@ enum {
     CNT_TOI_ROLLBACKS = 30, /* passes restarted in sequential order after a conflict */
     CNT_CASCADE = 40,     /* 3 ints: contacts collided per round of the wake cascade (rotating) */
     CNT_CASCADE_ROUNDS = 43, /* rounds of the last wake cascade */
+    CNT_BARRIER_LIMIT = 44, /* grid-barrier wait limit in units of 1024 clock cycles (0: 2e9 cycles) */
+    CNT_BARRIER_HOLD = 45,  /* extra arrivals every grid barrier waits for (0; a test's timeout hook) */
+    CNT_BP_VISITS = 46,     /* hierarchy nodes the last broadphase traversal fetched */
+    CNT_BP_CANDIDATES = 47, /* leaves it checked against the pair rules */
     /* continuous pass (k_continuous.cu), zeroed before every pass: */
     CNT_TOI_FIRST = 32,
     CNT_TOI_NEW = 32,     /* contacts created by the pass (table slots [n, n + this)) */
@@ -152,6 +158,9 @@ struct StepParams {
     int part_bodies;      /* part-local solve: bodies cached in shared memory per block */
     int part_slot_bytes;  /* part-local solve: shared memory per block for constraint slots */
     int toi_schedule;     /* continuous pass: B2G_TOI_SCHEDULE_* */
+    int custom_filter;    /* the host's contact filter replaces the default one (new pairs are filtered on
+                             the host, flagged contacts carry its answer in CF_REJECT) */
+    int pre_solve;        /* contacts updated by collide are marked CF_UPDATED for the host's pre_solve */
     int toi_may_conflict; /* continuous pass: a kinematic or bullet body exists, so side-by-side events
                              can conflict and the pass keeps a snapshot to restart from */
 };
@@ -163,6 +172,7 @@ struct DevWorld {
     int cfg_collide_block;    /* threads per block of the narrowphase */
     int cfg_traverse_block;   /* threads per block of the broadphase traversal */
     int n_bodies, n_fixtures, num_worlds;
+    int num_sms;              /* multiprocessors of the world's device (grid caps of the launchers) */
     int key_bits;      /* bits of the contact key (2 x refid bits) */
     int morton_world_bits;
     /* bodies */
@@ -305,10 +315,27 @@ struct DevWorld {
     int* cnt;
 };
 
+/* After a grid-barrier wait ran out, the step's buffers may be half-written: every later kernel of
+ * the world returns at once (it reads no index another kernel computed) until the host reads and
+ * clears the status (B2G_ERR_TIMEOUT). The status word is written only by the world's own kernels and
+ * the host between launches, so all blocks of one launch see the same value. */
+__device__ __forceinline__ bool world_aborted(const int* cnt) {
+    return (((volatile const int*)cnt)[CNT_STATUS] & ST_BARRIER_TIMEOUT) != 0;
+}
+#define B2G_RETURN_IF_ABORTED(w) \
+    do {                          \
+        if (world_aborted((w).cnt)) return; \
+    } while (0)
+
 /* kernel-file launchers */
 /* may_sleep: some body may be asleep (sleeping allowed, or a body made asleep): contacts then see
  * the bodies woken by contacts before them in the table's key order, as in the reference's list */
 void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s, bool may_sleep, int num_sms);
+/* contact edits of destroy / refilter calls between steps (k_edit_contacts in k_collide.cu): fix_mark
+ * per fixture, bit 0 destroyed (its contacts are destroyed), bit 1 refiltered (its contacts are flagged
+ * for filtering); body_pairs: contacts between these bodies are flagged for filtering */
+void launch_edit_contacts(const DevWorld& w, const uint8_t* fix_mark, const int2* body_pairs, int n_pairs,
+                          bool record_events, cudaStream_t s);
 /* flags the contacts of bodies a joint keeps apart (after joints were created) */
 void launch_flag_joint_contacts(const DevWorld& w, cudaStream_t s, int num_sms);
 void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cudaStream_t s);
@@ -322,10 +349,11 @@ void launch_time_of_impact(const ShapeRec* sa, const float4* swa, const ShapeRec
 int launch_continuous(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms);
 /* whether the part-local solve applies to this world (parts allowed and the world's size suits it) */
 bool use_parts(const DevWorld& w, int num_sms, bool allowed);
-/* after_tree (optional) is called between the tree pass (keys, sort, build, refit, traverse)
- * and the contact merge, so the caller can record a profiling event there */
+/* mark (optional) is called with 0 after the keys and their sort, 1 after the hierarchy (build,
+ * refit, four-way records, contact rows), 2 after the traversal (before the contact merge), so the
+ * caller can record profiling events there */
 void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms,
-                       const std::function<void()>& after_tree = nullptr);
+                       const std::function<void(int)>& mark = nullptr);
 void launch_set_transform(const DevWorld& w, int body, float px, float py, float angle, cudaStream_t s);
 void launch_clear_forces(const DevWorld& w, cudaStream_t s);
 void launch_collide_pairs(const ShapeRec* a, const float4* xa, const ShapeRec* b, const float4* xb, const int* kind,
@@ -353,6 +381,10 @@ size_t scan_tmp_size(int max_n);
 /* Host-side count of the kernels this library has launched (bench.py reports it per step). */
 extern unsigned long long g_kernel_launches;
 #define B2G_LAUNCHED(n) (::b2g::g_kernel_launches += (unsigned long long)(n))
+
+/* multiprocessors of the current device, queried once per device ordinal (for the launchers of the
+ * stand-alone routines, which have no world) */
+int current_sm_count();
 
 inline int grid_for(int n, int block, int max_blocks) {
     int g = (n + block - 1) / block;

@@ -388,8 +388,10 @@ __device__ __forceinline__ bool move_proxy(const DevWorld& w, int f, const AABB&
     return true;
 }
 
-/* b2_fixture_synchronize, private/dynamics/b2_fixture.rs:147-173; returns whether the proxy moved */
+/* b2_fixture_synchronize, private/dynamics/b2_fixture.rs:147-173 (for each of the fixture's proxies:
+ * none for a destroyed fixture or one on a disabled body); returns whether the proxy moved */
 __device__ __forceinline__ bool sync_fixture(const DevWorld& w, int f, const Xf& xf1, const Xf& xf2) {
+    if (w.f_refid[f] == 0xffffffffu) return false;
     const ShapeRec s = w.f_shape[f];
     AABB a1, a2;
     shape_aabb(s, xf1, a1);

@@ -6,7 +6,10 @@
  * launch completes when the counter reaches (k + 1) x gridDim.x. Thread 0 of each block keeps k in
  * shared memory, arrives with one fire-and-forget release add and polls the counter with acquire
  * loads; nobody resets anything, so the last block to arrive waits for no extra round trip. Each
- * wait is bounded: a clock64 limit (~1 s at 2 GHz) checked every 256 polls. On timeout the block
+ * wait is bounded: a clock64 limit checked every 256 polls, cnt[CNT_BARRIER_LIMIT] x 1024 cycles
+ * (b2g_set_barrier_limit; 0 means 2e9 cycles, ~1 s at 2 GHz). cnt[CNT_BARRIER_HOLD] (0 unless a
+ * test sets it) is added to every wait's target: arrivals that never come, so the wait runs out
+ * its limit; it exists to test the timeout path without a fault. On timeout the block
  * sets ST_BARRIER_TIMEOUT in the status word; once set, every later barrier returns false at once,
  * so all blocks leave the kernel within one limit and the host reports B2G_ERR_TIMEOUT. Thread 0
  * decides for its block and broadcasts through shared memory, so all threads of a block see the
@@ -49,10 +52,16 @@ __device__ __forceinline__ bool grid_barrier(int* cnt) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        int ok = (((volatile int*)cnt)[CNT_STATUS] & ST_BARRIER_TIMEOUT) == 0;
+        /* two independent loads: the limit's latency hides under the status word's */
+        const int status = ((volatile int*)cnt)[CNT_STATUS];
+        int2 lim_hold;
+        asm volatile("ld.volatile.global.v2.s32 {%0, %1}, [%2];"
+                     : "=r"(lim_hold.x), "=r"(lim_hold.y) : "l"(&cnt[CNT_BARRIER_LIMIT]) : "memory");
+        int ok = (status & ST_BARRIER_TIMEOUT) == 0;
         if (ok) {
             unsigned* count = (unsigned*)&cnt[CNT_BARRIER];
-            const unsigned target = (b2g_barrier_epoch + 1u) * gridDim.x;
+            const unsigned target = (b2g_barrier_epoch + 1u) * gridDim.x + (unsigned)lim_hold.y;
+            const long long limit = lim_hold.x > 0 ? (long long)lim_hold.x << 10 : 2000000000LL;
             ++b2g_barrier_epoch;
             red_release_add_gpu(count, 1u);
             const long long t0 = clock64();
@@ -60,7 +69,7 @@ __device__ __forceinline__ bool grid_barrier(int* cnt) {
             while ((int)(ld_acquire_gpu(count) - target) < 0) {
                 if ((++polls & 255u) == 0u) {
                     if (((volatile int*)cnt)[CNT_STATUS] & ST_BARRIER_TIMEOUT) break;
-                    if (clock64() - t0 > 2000000000LL) {
+                    if (clock64() - t0 > limit) {
                         atomicOr((unsigned*)&cnt[CNT_STATUS], ST_BARRIER_TIMEOUT);
                         break;
                     }

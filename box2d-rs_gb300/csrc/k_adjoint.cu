@@ -50,6 +50,7 @@ __device__ __forceinline__ bool tape_ok(const TapeDev& t, long long step, long l
 }
 
 __global__ void k_tape_record(DevWorld w, TapeDev t, StepParams sp) {
+    B2G_RETURN_IF_ABORTED(w);
     const long long step = t.cnt[TAPE_CNT_STEPS];
     const long long base = t.cnt[TAPE_CNT_SLOTS];
     const int ncons = w.cnt[CNT_CONS];
@@ -188,6 +189,7 @@ __global__ void k_tape_record(DevWorld w, TapeDev t, StepParams sp) {
 }
 
 __global__ void k_tape_post(DevWorld w, TapeDev t, StepParams sp) {
+    B2G_RETURN_IF_ABORTED(w);
     const long long step = t.cnt[TAPE_CNT_STEPS];
     const long long base = t.cnt[TAPE_CNT_SLOTS];
     const int ncons = w.cnt[CNT_CONS];
@@ -207,6 +209,7 @@ __global__ void k_tape_post(DevWorld w, TapeDev t, StepParams sp) {
 }
 
 __global__ void k_tape_advance(DevWorld w, TapeDev t) {
+    B2G_RETURN_IF_ABORTED(w);
     const long long step = t.cnt[TAPE_CNT_STEPS];
     const long long base = t.cnt[TAPE_CNT_SLOTS];
     const int ncons = w.cnt[CNT_CONS];
@@ -216,6 +219,7 @@ __global__ void k_tape_advance(DevWorld w, TapeDev t) {
 }
 
 __global__ void k_tape_snapshot(DevWorld w, TapeDev t, int index) {
+    B2G_RETURN_IF_ABORTED(w);
     const size_t o = (size_t)index * t.n_bodies;
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < t.n_bodies; b += gridDim.x * blockDim.x) {
         const float4 p = w.b_pos[b], v = w.b_vel[b];
@@ -717,7 +721,7 @@ void launch_tape_post(const DevWorld& w, const TapeDev& t, const StepParams& sp,
 }
 
 void launch_tape_snapshot(const DevWorld& w, const TapeDev& t, int index, cudaStream_t s) {
-    k_tape_snapshot<<<grid_for(t.n_bodies, kBlock, 152 * 4), kBlock, 0, s>>>(w, t, index);
+    k_tape_snapshot<<<grid_for(t.n_bodies, kBlock, w.num_sms * 4), kBlock, 0, s>>>(w, t, index);
     B2G_LAUNCHED(1);
 }
 

@@ -56,6 +56,7 @@ __device__ __forceinline__ uint32_t spread16(uint32_t x) {
 }
 
 __global__ void k_bp_init(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t == 0) {
         w.cnt[CNT_BOUNDS + 0] = INT_MAX;
@@ -65,6 +66,8 @@ __global__ void k_bp_init(DevWorld w) {
         w.cnt[CNT_NEW] = 0;
         w.cnt[CNT_PAIRS] = 0;
         w.cnt[CNT_DYN_EXTENT] = 0;
+        w.cnt[CNT_BP_VISITS] = 0;
+        w.cnt[CNT_BP_CANDIDATES] = 0;
     }
     for (int i = t; i < 2 * w.num_worlds; i += gridDim.x * blockDim.x) {
         w.bp_world_first[i] = -1;
@@ -73,6 +76,7 @@ __global__ void k_bp_init(DevWorld w) {
 }
 
 __global__ void k_bp_bounds(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x)
         w.b_rank[b] = INT_MAX;
     int mnx = INT_MAX, mny = INT_MAX, mxx = INT_MIN, mxy = INT_MIN, dyn = 0;
@@ -105,6 +109,7 @@ __global__ void k_bp_bounds(DevWorld w) {
 }
 
 __global__ void k_bp_keys(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     float lx = 0.0f, ly = 0.0f, sx = 0.0f, sy = 0.0f;
     if (w.cnt[CNT_BOUNDS + 0] != INT_MAX) {
         lx = ord2f(w.cnt[CNT_BOUNDS + 0]);
@@ -144,6 +149,7 @@ __device__ __forceinline__ int delta(const unsigned long long* k, int n, int i, 
 
 /* Karras, "Maximizing parallelism in the construction of BVHs, octrees, and k-d trees" (HPG 2012) */
 __global__ void k_bp_build(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     const int n = w.n_fixtures;
     const unsigned long long* k = w.bp_key;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
@@ -181,6 +187,7 @@ __global__ void k_bp_build(DevWorld w) {
 }
 
 __global__ void k_bp_leaves(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     const int n = w.n_fixtures;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const uint32_t f = w.bp_val[p];
@@ -200,6 +207,7 @@ __device__ __forceinline__ float4 box_union(float4 a, float4 b) {
 }
 
 __global__ void k_bp_refit(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     const int n = w.n_fixtures;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         if (n < 2) break;
@@ -228,6 +236,7 @@ __device__ __forceinline__ bool box_overlap(float4 a, float4 b) { return overlap
  * stands for itself). A traversal then tests four boxes per dependent fetch and descends two
  * levels at a time; the pairs found do not depend on the hierarchy's shape. */
 __global__ void k_bp_quad(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     const int n = w.n_fixtures;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
         const int2 ch = w.bp_node_child[i];
@@ -269,6 +278,7 @@ __device__ __forceinline__ int lower_bound_u64(const unsigned long long* a, int 
  * that contact's key starts with r, which a stale entry cannot satisfy (ids with contacts are
  * rewritten every pass and the table is sorted). */
 __global__ void k_bp_rows(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const unsigned long long r = w.c.key[i] >> w.key_bits;
@@ -304,7 +314,7 @@ __device__ void handle_pair(const DevWorld& w, const StepParams& sp, int f, int 
     if (contact_exists(w, lo, key, n_contacts)) return;
     /* add_pair: fixture A is the one with the smaller proxy id */
     int fa, fb;
-    if (!pair_accept(w, rf < rg ? f : g, rf < rg ? g : f, fa, fb)) return;
+    if (!pair_accept(w, rf < rg ? f : g, rf < rg ? g : f, fa, fb, !sp.custom_filter)) return;
     const int slot = atomicAdd(&w.cnt[CNT_NEW], 1);
     if (slot < w.pair_cap) {
         w.n_key[slot] = key;
@@ -326,6 +336,7 @@ constexpr int kLeafQueue = 224;  /* 31 left over + 32 lanes x 4 leaves in one ro
                                     2 single-proxy roots per lane */
 
 __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams sp) {
+    B2G_RETURN_IF_ABORTED(w);
     __shared__ uint2 s_queue[kBlock / 32][kLeafQueue];
     __shared__ int s_give_node[kBlock / 32][32];
     __shared__ int s_give_f[kBlock / 32][32];
@@ -337,6 +348,7 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
     const unsigned full = 0xffffffffu, lt = (1u << lane) - 1u;
     uint2* queue = s_queue[wq];
     const int stride = gridDim.x * blockDim.x;
+    unsigned visits = 0, candidates = 0;  /* this lane's node fetches and leaf checks (traffic counters) */
     for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
         const int p = base + lane;
         int f = -1;
@@ -406,6 +418,7 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
                 __syncwarp();
             }
             if (top > bot) {
+                ++visits;
                 const int node = stack[--top];
                 const int4 ch = w.bp_quad_child[node];
                 const float4* qb = w.bp_quad_box + 4 * (size_t)node;
@@ -429,6 +442,7 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
             if (nq >= 32 || (!more && nq > 0)) {
                 __syncwarp();
                 for (int i = lane; i < nq; i += 32) {
+                    ++candidates;
                     const uint2 e = queue[i];
                     const int ff = (int)e.x, g = (int)w.bp_val[e.y];
                     if (g == ff) continue;
@@ -442,24 +456,34 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
             if (!more) break;
         }
     }
+    visits = __reduce_add_sync(0xffffffffu, visits);
+    candidates = __reduce_add_sync(0xffffffffu, candidates);
+    if (lane == 0 && (visits | candidates)) {
+        atomicAdd((unsigned*)&w.cnt[CNT_BP_VISITS], visits);
+        atomicAdd((unsigned*)&w.cnt[CNT_BP_CANDIDATES], candidates);
+    }
 }
 
 __global__ void k_bp_clear_moved(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < w.n_fixtures; f += gridDim.x * blockDim.x) w.f_moved[f] = 0;
 }
 
 __global__ void k_bp_clamp_new(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     if (blockIdx.x == 0 && threadIdx.x == 0 && w.cnt[CNT_NEW] > w.pair_cap) w.cnt[CNT_NEW] = w.pair_cap;
 }
 
 /* ---- merge of surviving contacts and new contacts (both key-sorted) ---- */
 __global__ void k_merge_flags(DevWorld w, uint32_t* flag) {
+    B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         flag[i] = (w.c.flags[i] & CF_DEAD) ? 0u : 1u;
 }
 
 __global__ void k_merge_old(DevWorld w, const uint32_t* flag, const uint32_t* rank) {
+    B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
     const int nn = w.cnt[CNT_NEW];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -472,6 +496,7 @@ __global__ void k_merge_old(DevWorld w, const uint32_t* flag, const uint32_t* ra
 
 /* b2_contact_create + B2contact::new (private/dynamics/b2_contact.rs:11-60): mixing laws of src/b2_contact.rs:29-46 */
 __global__ void k_merge_new(DevWorld w, const uint32_t* rank) {
+    B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
     const int nn = w.cnt[CNT_NEW];
     const int alive = w.cnt[CNT_ALIVE];
@@ -490,6 +515,7 @@ __global__ void k_merge_new(DevWorld w, const uint32_t* rank) {
 }
 
 __global__ void k_merge_finish(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         int total = w.cnt[CNT_ALIVE] + w.cnt[CNT_NEW];
         if (total > w.contact_cap) {
@@ -504,7 +530,7 @@ __global__ void k_merge_finish(DevWorld w) {
 
 /* Runs update_pairs + add_pair and merges: the caller swaps w.c and w.c_alt afterwards. */
 void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms,
-                       const std::function<void()>& after_tree) {
+                       const std::function<void(int)>& mark) {
     const int n = w.n_fixtures;
     const int gf = grid_for(n, kBlock, num_sms * 8);
     k_bp_init<<<grid_for(2 * w.num_worlds, kBlock, 64), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
@@ -513,6 +539,7 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
         k_bp_keys<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         radix_sort_pairs_coop(w.bp_key, w.bp_val, w.bp_key_alt, w.bp_val_alt, nullptr, n, kMortonBits + w.morton_world_bits,
                               w.sort_hist, w.cnt, s, num_sms);
+        if (mark) mark(0);
         if (n > 1) {
             k_bp_build<<<grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         }
@@ -522,12 +549,13 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
             k_bp_quad<<<grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         }
         k_bp_rows<<<grid_for(w.contact_cap, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        if (mark) mark(1);
         const int tb = w.cfg_traverse_block;
         k_bp_traverse<<<grid_for(n, tb, num_sms * 2048 / tb), tb, 0, s>>>(w, sp); B2G_LAUNCHED(1);
         k_bp_clear_moved<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
     }
     k_bp_clamp_new<<<1, 32, 0, s>>>(w); B2G_LAUNCHED(1);
-    if (after_tree) after_tree();
+    if (mark) mark(2);
     /* sort new keys; payload = emission slot */
     radix_sort_pairs_coop(w.n_key, w.n_idx, w.n_key_alt, w.n_idx_alt, &w.cnt[CNT_NEW], w.pair_cap, 2 * w.key_bits,
                           w.sort_hist, w.cnt, s, num_sms);

@@ -46,13 +46,16 @@ __device__ __forceinline__ bool collide_contact(const DevWorld& w, const StepPar
     const uint32_t fb_flags = w.b_flags[bd.y];
     bool destroy = false;
     if (flags & CF_FILTER) {
-        /* flagged by a new joint: should these bodies collide? (the default filter's answer does
-         * not change) */
-        if (!joint_allows(w, bd.y, bd.x)) destroy = true;
-        else w.c.flags[i] = flags = flags & ~CF_FILTER;
+        /* flagged for filtering (a joint made or destroyed, new filter data): should these bodies and
+         * fixtures collide? CF_REJECT: the host's contact filter said no before the step */
+        const bool allowed = sp.custom_filter ? !(flags & CF_REJECT) : filter_allows(w, fx.x, fx.y);
+        if (!bodies_collide(w, bd.y, bd.x) || !allowed) destroy = true;
+        else w.c.flags[i] = flags = flags & ~(CF_FILTER | CF_REJECT);
     }
-    if (!destroy && !active_for(w, bd.x, fa_flags, i, deferred) && !active_for(w, bd.y, fb_flags, i, deferred))
+    if (!destroy && !active_for(w, bd.x, fa_flags, i, deferred) && !active_for(w, bd.y, fb_flags, i, deferred)) {
+        if (sp.pre_solve && (flags & CF_UPDATED)) w.c.flags[i] = flags & ~CF_UPDATED;
         return false;
+    }
     const float4 A = w.f_fat[fx.x];
     const float4 B = w.f_fat[fx.y];
     const bool was_touching = (flags & CF_TOUCHING) != 0;
@@ -74,12 +77,14 @@ __device__ __forceinline__ bool collide_contact(const DevWorld& w, const StepPar
         return true;
     }
     contact_update(w, sp.record_events != 0, i, flags, fx, bd, ids, deferred ? i : -1);
+    if (sp.pre_solve) w.c.flags[i] |= CF_UPDATED;
     return true;
 }
 
 }  // namespace
 
 __global__ void __launch_bounds__(256) k_collide(DevWorld w, StepParams sp, int deferred) {
+    B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const bool done = collide_contact(w, sp, i, deferred != 0);
@@ -90,6 +95,7 @@ __global__ void __launch_bounds__(256) k_collide(DevWorld w, StepParams sp, int 
 /* The contacts skipped as inactive whose body a contact earlier in the table woke: collided in
  * rounds until a round finds none (a chain of wakes along the table's order). */
 __global__ void __launch_bounds__(256) k_collide_cascade(DevWorld w, StepParams sp) {
+    B2G_RETURN_IF_ABORTED(w);
     grid_barrier_start();
     const int n = w.cnt[CNT_CONTACTS];
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -116,6 +122,7 @@ __global__ void __launch_bounds__(256) k_collide_cascade(DevWorld w, StepParams 
 
 /* apply the pass's wakes (set_awake(true): awake, sleep time 0) and clear the records */
 __global__ void k_collide_wake(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x) {
         if (w.b_wake[b] != kNoWake || w.b_dwake[b]) {
             const uint32_t f = w.b_flags[b];
@@ -132,11 +139,59 @@ __global__ void k_collide_wake(DevWorld w) {
 /* B2world::create_joint (private/dynamics/b2_world.rs:258-271): the contacts between two bodies
  * joined without collide_connected are flagged for filtering at the next collide */
 __global__ void k_flag_joint_contacts(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int2 bd = w.c.body[i];
         if (!joint_allows(w, bd.y, bd.x)) w.c.flags[i] |= CF_FILTER;
     }
+}
+
+/* Contact edits of a host call between steps, one thread per contact of the table:
+ *  - fix_mark bit 0 (a destroyed fixture: B2body::destroy_fixture, B2world::destroy_body): the
+ *    contact is destroyed as B2contactManager::destroy does (private/dynamics/b2_contact_manager.rs:24-78
+ *    with b2_contact_destroy, private/dynamics/b2_contact.rs:33-46): an end event if it touches, both
+ *    bodies woken if its manifold has points and neither fixture is a sensor; it is then dead (collide
+ *    skips it and the next merge drops it);
+ *  - fix_mark bit 1 (B2fixture::refilter, private/dynamics/b2_fixture.rs:181-211) and the body pairs
+ *    of destroyed joints without collide_connected (B2world::destroy_joint,
+ *    private/dynamics/b2_world.rs:326-340): the contact is flagged for filtering at the next collide. */
+__global__ void k_edit_contacts(DevWorld w, const uint8_t* fix_mark, const int2* body_pairs, int n_pairs,
+                                int record_events) {
+    const int n = w.cnt[CNT_CONTACTS];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t flags = w.c.flags[i];
+        if (flags & CF_DEAD) continue;
+        const int2 fx = w.c.fix[i];
+        const uint8_t m = fix_mark[fx.x] | fix_mark[fx.y];
+        if (m & 1u) {
+            if (record_events && (flags & CF_TOUCHING)) push_event(w, 1, fx.x, fx.y);
+            const int old_count = (int)((w.c.mids[i].z >> 8) & 0xffu);
+            if (old_count > 0 && !(flags & CF_SENSOR)) {
+                const int2 bd = w.c.body[i];
+                wake_body(w, bd.x);
+                wake_body(w, bd.y);
+            }
+            w.c.flags[i] = (flags | CF_DEAD) & ~CF_TOUCHING;
+            continue;
+        }
+        bool flag = (m & 2u) != 0;
+        if (!flag && n_pairs > 0) {
+            const int2 bd = w.c.body[i];
+            for (int k = 0; k < n_pairs && !flag; ++k) {
+                const int2 p = body_pairs[k];
+                flag = (p.x == bd.x && p.y == bd.y) || (p.x == bd.y && p.y == bd.x);
+            }
+        }
+        if (flag) w.c.flags[i] = flags | CF_FILTER;
+    }
+}
+
+void launch_edit_contacts(const DevWorld& w, const uint8_t* fix_mark, const int2* body_pairs, int n_pairs,
+                          bool record_events, cudaStream_t s) {
+    k_edit_contacts<<<grid_for(w.contact_cap, 256, w.num_sms * 8), 256, 0, s>>>(w, fix_mark, body_pairs, n_pairs,
+                                                                                record_events ? 1 : 0);
+    B2G_LAUNCHED(1);
 }
 
 void launch_flag_joint_contacts(const DevWorld& w, cudaStream_t s, int num_sms) {
@@ -146,7 +201,7 @@ void launch_flag_joint_contacts(const DevWorld& w, cudaStream_t s, int num_sms) 
 
 void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s, bool may_sleep, int num_sms) {
     const int block = w.cfg_collide_block;
-    k_collide<<<grid_for(w.contact_cap, block, 152 * 2048 / block), block, 0, s>>>(w, sp, may_sleep ? 1 : 0);
+    k_collide<<<grid_for(w.contact_cap, block, w.num_sms * 2048 / block), block, 0, s>>>(w, sp, may_sleep ? 1 : 0);
     B2G_LAUNCHED(1);
     if (!may_sleep) return;
     DevWorld wc = w;
@@ -189,7 +244,7 @@ __global__ void k_collide_pairs(const ShapeRec* a, const float4* xa, const Shape
 
 void launch_collide_pairs(const ShapeRec* a, const float4* xa, const ShapeRec* b, const float4* xb, const int* kind,
                           int n, float4* geo, float4* pts, uint4* ids, cudaStream_t s) {
-    k_collide_pairs<<<grid_for(n, 128, 152 * 16), 128, 0, s>>>(a, xa, b, xb, kind, n, geo, pts, ids); B2G_LAUNCHED(1);
+    k_collide_pairs<<<grid_for(n, 128, current_sm_count() * 16), 128, 0, s>>>(a, xa, b, xb, kind, n, geo, pts, ids); B2G_LAUNCHED(1);
 }
 
 }  // namespace b2g

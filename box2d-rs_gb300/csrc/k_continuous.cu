@@ -538,6 +538,7 @@ __device__ __forceinline__ bool earlier(uint32_t a, unsigned long long ka, uint3
 }
 
 __global__ void __launch_bounds__(kTBlock) k_continuous(DevWorld w, StepParams sp) {
+    B2G_RETURN_IF_ABORTED(w);
     extern __shared__ __align__(16) unsigned char smem[];
     IslandScratch* scratch = reinterpret_cast<IslandScratch*>(smem);
     grid_barrier_start();

@@ -12,12 +12,30 @@
  *      __match_any_sync groups equal digits, and per-warp counts are prefixed across
  *      the 8 warps in shared memory, so every item's rank preserves input order.
  */
+#include <mutex>
+#include <vector>
+
 #include "b2g_internal.h"
 #include "b2g_sync.cuh"
 
 namespace b2g {
 
 unsigned long long g_kernel_launches = 0;
+
+int current_sm_count() {
+    static std::mutex m;
+    static std::vector<int> counts;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 1;
+    std::lock_guard<std::mutex> lock(m);
+    if ((int)counts.size() <= dev) counts.resize((size_t)dev + 1, 0);
+    if (counts[dev] == 0) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) return 1;
+        counts[dev] = n;
+    }
+    return counts[dev];
+}
 
 namespace {
 constexpr int kScanBlock = 256;
@@ -254,6 +272,7 @@ __device__ void tile_histogram(const unsigned long long* __restrict__ keys, int 
 __global__ void __launch_bounds__(kSortBlock) k_radix_coop(unsigned long long* ka, uint32_t* va, unsigned long long* kb,
                                                            uint32_t* vb, const int* d_n, int max_n, int bits,
                                                            uint32_t* hist, int* cnt) {
+    if (world_aborted(cnt)) return;
     grid_barrier_start();
     __shared__ uint32_t s_base[256];
     __shared__ uint32_t s_run[256];

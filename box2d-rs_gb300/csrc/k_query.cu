@@ -124,6 +124,7 @@ __device__ __forceinline__ Xf body_xf(const DevWorld& w, int b) {
  * out_b = (normal x, normal y, fraction, -) */
 __global__ void __launch_bounds__(kBlock) k_ray_cast(DevWorld w, const float4* rays, const uint32_t* ray_world, int n,
                                                      float4* out_a, float4* out_b) {
+    B2G_RETURN_IF_ABORTED(w);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 ray = rays[i];
         const V2 p1 = mk(ray.x, ray.y), p2 = mk(ray.z, ray.w);
@@ -189,6 +190,7 @@ __global__ void __launch_bounds__(kBlock) k_ray_cast(DevWorld w, const float4* r
 /* one thread per box: every fixture whose fat AABB overlaps it, as (query, fixture) pairs */
 __global__ void __launch_bounds__(kBlock) k_query_aabb(DevWorld w, const float4* boxes, const uint32_t* box_world,
                                                        int n, uint2* out, int cap, int* count) {
+    B2G_RETURN_IF_ABORTED(w);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 q = boxes[i];
         const uint32_t wd = box_world ? box_world[i] : 0u;
@@ -227,13 +229,13 @@ __global__ void __launch_bounds__(kBlock) k_query_aabb(DevWorld w, const float4*
 
 void launch_ray_cast(const DevWorld& w, const float4* rays, const uint32_t* ray_world, int n, float4* out_a,
                      float4* out_b, cudaStream_t s) {
-    k_ray_cast<<<grid_for(n, kBlock, 152 * 16), kBlock, 0, s>>>(w, rays, ray_world, n, out_a, out_b);
+    k_ray_cast<<<grid_for(n, kBlock, w.num_sms * 16), kBlock, 0, s>>>(w, rays, ray_world, n, out_a, out_b);
     B2G_LAUNCHED(1);
 }
 
 void launch_query_aabb(const DevWorld& w, const float4* boxes, const uint32_t* box_world, int n, uint2* out, int cap,
                        int* count, cudaStream_t s) {
-    k_query_aabb<<<grid_for(n, kBlock, 152 * 16), kBlock, 0, s>>>(w, boxes, box_world, n, out, cap, count);
+    k_query_aabb<<<grid_for(n, kBlock, w.num_sms * 16), kBlock, 0, s>>>(w, boxes, box_world, n, out, cap, count);
     B2G_LAUNCHED(1);
 }
 

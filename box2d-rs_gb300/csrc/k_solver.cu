@@ -67,6 +67,7 @@ __device__ __forceinline__ void uf_union(int* parent, int a, int b) {
 }
 
 __global__ void k_island_init(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x) {
         w.b_island[b] = b;
         w.isl_minsep[w.body_cap + b] = 0u;  /* "island has an awake member" */
@@ -79,6 +80,7 @@ __device__ __forceinline__ bool contact_is_constraint(uint32_t cf) {
 }
 
 __global__ void k_island_union(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (!contact_is_constraint(w.c.flags[i])) continue;
@@ -96,6 +98,7 @@ __global__ void k_island_union(DevWorld w) {
 }
 
 __global__ void k_island_compress(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x) {
         const int r = uf_find(w.b_island, b);
         const uint32_t f = w.b_flags[b];
@@ -104,6 +107,7 @@ __global__ void k_island_compress(DevWorld w) {
 }
 
 __global__ void k_island_mark(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x) {
         int r = w.b_island[b];
         r = w.b_island[r];  /* compress left every body at most one hop from its root */
@@ -116,6 +120,7 @@ __global__ void k_island_mark(DevWorld w) {
 
 /* flag[i] = 1 if contact i is a constraint of a solved island */
 __global__ void k_cons_flags(DevWorld w, uint32_t* flag) {
+    B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t sel = 0;
@@ -129,6 +134,7 @@ __global__ void k_cons_flags(DevWorld w, uint32_t* flag) {
 }
 
 __global__ void k_cons_scatter(DevWorld w, const uint32_t* flag, const uint32_t* pos) {
+    B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (!flag[i]) continue;
@@ -145,6 +151,7 @@ __global__ void k_cons_scatter(DevWorld w, const uint32_t* flag, const uint32_t*
 }
 
 __global__ void k_cons_clamp(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     if (threadIdx.x == 0 && blockIdx.x == 0 && w.cnt[CNT_CONS] > w.cons_cap) w.cnt[CNT_CONS] = w.cons_cap;
 }
 
@@ -309,6 +316,7 @@ __device__ int colour_tail(const DevWorld& w, int round) {
  * the parts concurrently is solving them one after the other, as no two parts share a dynamic
  * body, so this slot order is the sequential solve order. */
 __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
+    B2G_RETURN_IF_ABORTED(w);
     grid_barrier_start();
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsize = gridDim.x * blockDim.x;
@@ -924,6 +932,7 @@ __device__ __forceinline__ void part_load(const PartCtx& pc, const float4* glob)
 }
 
 __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
+    B2G_RETURN_IF_ABORTED(w);
     grid_barrier_start();
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gsize = gridDim.x * blockDim.x;
@@ -1263,6 +1272,7 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
 }
 
 __global__ void k_sleep_init(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x)
         w.isl_sleep[b] = kMaxFloat;
 }
@@ -1285,6 +1295,7 @@ __global__ void k_set_transform(DevWorld w, int body, float px, float py, float 
 }
 
 __global__ void k_clear_forces(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x)
         w.b_force[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
@@ -1303,8 +1314,8 @@ int coop_blocks(const void* fn, int num_sms) {
 }  // namespace
 
 void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cudaStream_t s) {
-    const int gb = grid_for(w.n_bodies, kBlock, 152 * 8);
-    const int gc = grid_for(w.contact_cap, kBlock, 152 * 8);
+    const int gb = grid_for(w.n_bodies, kBlock, w.num_sms * 8);
+    const int gc = grid_for(w.contact_cap, kBlock, w.num_sms * 8);
     k_island_init<<<gb, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
     k_island_union<<<gc, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
     k_island_compress<<<gb, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
@@ -1382,11 +1393,11 @@ int launch_solver(const DevWorld& w, const StepParams& sp, cudaStream_t s, int n
 }
 
 void launch_set_transform(const DevWorld& w, int body, float px, float py, float angle, cudaStream_t s) {
-    k_set_transform<<<grid_for(w.n_fixtures, kBlock, 152 * 4), kBlock, 0, s>>>(w, body, px, py, angle); B2G_LAUNCHED(1);
+    k_set_transform<<<grid_for(w.n_fixtures, kBlock, w.num_sms * 4), kBlock, 0, s>>>(w, body, px, py, angle); B2G_LAUNCHED(1);
 }
 
 void launch_clear_forces(const DevWorld& w, cudaStream_t s) {
-    k_clear_forces<<<grid_for(w.n_bodies, kBlock, 152 * 4), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+    k_clear_forces<<<grid_for(w.n_bodies, kBlock, w.num_sms * 4), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
 }
 
 }  // namespace b2g

@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(kBlock) k_time_of_impact(const ShapeRec* sa, c
 
 void launch_time_of_impact(const ShapeRec* sa, const float4* swa, const ShapeRec* sb, const float4* swb,
                            const float* t_max, int n, int2* out, cudaStream_t s) {
-    k_time_of_impact<<<grid_for(n, kBlock, 152 * 16), kBlock, 0, s>>>(sa, swa, sb, swb, t_max, n, out);
+    k_time_of_impact<<<grid_for(n, kBlock, current_sm_count() * 16), kBlock, 0, s>>>(sa, swa, sb, swb, t_max, n, out);
     B2G_LAUNCHED(1);
 }
 

@@ -217,6 +217,33 @@ int b2g_create_fixtures(void* world, const b2g_fixture_def* defs, int32_t n, uin
  * does not let its bodies collide flags their contacts for the next collide, which destroys them.
  * A world with joints runs the grid-wide colour schedule (no part-local solve) and cannot be taped. */
 int b2g_create_joints(void* world, const b2g_joint_def* defs, int32_t n, uint32_t* out_ids);
+
+/* ---- destruction and filtering ----
+ * Ids stay valid after a destruction: a destroyed body keeps its slot as a static, disabled body
+ * without fixtures (its last state stays readable), a destroyed fixture keeps its slot without a
+ * proxy, a destroyed joint leaves the solver; none is reused, and any further call that names one
+ * returns B2G_ERR_INVALID_ARG. Destroyed proxies return their ids to the dynamic tree's free list
+ * exactly as the reference's node pool does (private/collision/b2_dynamic_tree.rs:28-99), so proxy
+ * ids, which fixture of a same-type pair is A, and the contact order stay the reference's.
+ * End events of contacts a destruction removes are added to the event list of the last step
+ * (b2g_get_events); the next step clears the list. Not between b2g_tape_begin and b2g_tape_end. */
+/* B2world::destroy_body (src/b2_world.rs:72-74, private/dynamics/b2_world.rs:100-158), for each body
+ * in order: its joints (waking their bodies), its contacts (end events, wakes), its fixtures'
+ * proxies in fixture-list order. */
+int b2g_destroy_bodies(void* world, const uint32_t* ids, int32_t n);
+/* B2body::destroy_fixture (src/b2_body.rs:259-261, private/dynamics/b2_body.rs:214-289), for each
+ * fixture in order: its contacts, its proxy, then the body's mass data is reset. */
+int b2g_destroy_fixtures(void* world, const uint32_t* ids, int32_t n);
+/* B2world::destroy_joint (src/b2_world.rs:89-91, private/dynamics/b2_world.rs:278-340): both
+ * bodies woken; without collide_connected the contacts between them are flagged for filtering. */
+int b2g_destroy_joints(void* world, const uint32_t* ids, int32_t n);
+/* B2fixture::set_filter_data (src/b2_fixture.rs:179-181, private/dynamics/b2_fixture.rs:175-211):
+ * new filter data, then refilter: the fixture's contacts are flagged for filtering at the next
+ * collide and its proxy is touched so the next broadphase queries it. */
+int b2g_set_filter_data(void* world, uint32_t fixture, uint16_t category_bits, uint16_t mask_bits,
+                        int16_t group_index);
+/* B2fixture::refilter (src/b2_fixture.rs:183-189) with the fixture's current filter data. */
+int b2g_refilter(void* world, uint32_t fixture);
 /* Accumulated joint impulses (for warm starting), 5 per joint: revolute x, y, motor, lower, upper;
  * prismatic x, y, motor, lower, upper; wheel impulse, spring, motor, lower, upper; pulley impulse, 0, 0, 0, 0; distance impulse, lower, upper, 0, 0; weld, friction and motor x, y,
  * angular, 0, 0; mouse x, y, 0, 0, 0 */
@@ -295,6 +322,15 @@ int b2g_set_part_solve(void* world, int32_t flag);
 /* ---- introspection ---- */
 int b2g_get_profile(void* world, b2g_profile* out);       /* B2world::get_profile, src/b2_world.rs:268-270 */
 int b2g_get_counts(void* world, b2g_counts* out);         /* get_body_count / get_contact_count / get_proxy_count */
+/* Work counts of the last step, for traffic models of its kernels (not in the reference, whose
+ * B2Profile holds times only): hierarchy nodes the broadphase traversal fetched and leaves it
+ * checked, new contacts it found, the contact table's size, constraint slots solved (of them
+ * part-locally), the parts and colours of the colouring. */
+typedef struct b2g_step_stats {
+    int32_t bp_node_visits, bp_leaf_checks, new_pairs, contacts;
+    int32_t constraints, interior_slots, parts, colours;
+} b2g_step_stats;
+int b2g_get_step_stats(void* world, b2g_step_stats* out);
 /* Exact checkpoint and resume (not in the reference's API, which serialises a world through serde,
  * src/serialize/): the world's device buffers (bodies, fixtures, the contact table with its
  * manifolds and impulses, the colouring and partition the next steps reuse) and its stepping state,
@@ -310,11 +346,51 @@ int b2g_state_load(void* world, const void* in, uint64_t bytes);
 int b2g_get_toi_stats(void* world, int32_t* events, int32_t* last_iterations, int32_t* restarts);
 /* Device times (ms, CUDA events) of the last step's phases, n >= 7: initial broadphase (only
  * after fixtures were added), collide, islands + constraint list, colouring, solver kernel,
- * broadphase tree pass (keys, sort, hierarchy, traversal), contact merge. */
+ * broadphase tree pass (keys, sort, hierarchy, traversal), contact merge (with the continuous
+ * pass when it runs); with n >= 10 also the tree pass in three: keys + sort, hierarchy (build,
+ * refit, four-way records, contact rows), traversal. */
 int b2g_get_phase_times(void* world, float* out, int32_t n);
 int b2g_get_contacts(void* world, b2g_contact_info* out, int32_t capacity, int32_t* out_count);
 /* begin/end events produced since the previous call (B2contactListener, src/b2_world_callbacks.rs:68-104) */
 int b2g_get_events(void* world, b2g_contact_event* out, int32_t capacity, int32_t* out_count);
+/* B2contactImpulse (src/b2_world_callbacks.rs:52-58) of one contact, as B2contactListener::post_solve
+ * receives it. */
+typedef struct b2g_contact_impulse {
+    uint32_t fixture_a, fixture_b;
+    float normal_impulses[2];
+    float tangent_impulses[2];
+    int32_t count;                  /* points as solved: a 2-point manifold solved as 1 reports 1 */
+} b2g_contact_impulse;
+/* The post_solve reports of the last step (B2island::report, private/dynamics/b2_island_private.rs:
+ * 460-487): one per contact of the islands the discrete solve solved, in solve order, with the
+ * impulses after the velocity iterations. The reference calls post_solve only when a listener is
+ * set; here the records are always kept on the device and read on demand. The time-of-impact
+ * sub-steps of continuous physics are not reported. */
+int b2g_get_post_solve(void* world, b2g_contact_impulse* out, int32_t capacity, int32_t* out_count);
+
+/* ---- host callbacks (a slow path: the world's steps run without graphs and synchronise at each
+ * callback point; not with continuous physics, whose pass runs on the device alone) ----
+ * B2world::set_contact_filter (src/b2_world.rs:38-40) with a B2contactFilter::should_collide
+ * (src/b2_world_callbacks.rs:33-45) written on the host: it replaces the default filter. It is asked
+ * about every new pair the broadphase finds (with the fixtures of the smaller and the larger proxy
+ * id, after add_pair's body and joint checks), and about every contact flagged for filtering (a
+ * destroyed joint, new filter data) whose bodies still may collide, before collide; nonzero keeps the
+ * pair. fn = NULL restores the default filter. */
+typedef int32_t (*b2g_contact_filter_fn)(void* user, uint32_t fixture_a, uint32_t fixture_b);
+int b2g_set_contact_filter(void* world, b2g_contact_filter_fn fn, void* user);
+/* B2contactListener::pre_solve (src/b2_world_callbacks.rs:68-104; called from
+ * private/dynamics/b2_contact.rs:201-217): after collide, once for every contact the step updated that
+ * touches, in the contact table's key order, with the new manifold and the manifold before the update.
+ * The callback may edit the contact for this step's solve as B2contact's setters do: set_enabled,
+ * set_friction, set_restitution, set_restitution_threshold, set_tangent_speed (friction and
+ * restitution persist, as in the reference; enabled is set again by the next update). */
+typedef struct b2g_contact_edit {
+    int32_t enabled;
+    float friction, restitution, restitution_threshold, tangent_speed;
+} b2g_contact_edit;
+typedef void (*b2g_pre_solve_fn)(void* user, const b2g_contact_info* contact, const b2g_contact_info* old_manifold,
+                                 b2g_contact_edit* edit);
+int b2g_set_pre_solve(void* world, b2g_pre_solve_fn fn, void* user);
 
 /* Buffer begin/end contact events during steps (off by default: the reference only
  * calls a listener once one is installed, src/b2_world.rs:44-46). */
@@ -356,6 +432,16 @@ int b2g_time_of_impact(const b2g_fixture_def* shape_a, const b2g_sweep* sweep_a,
  * and fixture counts stay the same; any change re-captures. */
 int b2g_set_graph_capture(void* world, int32_t flag);
 
+/* Grid-barrier wait limit of the world's persistent kernels, in SM clock cycles (0 restores
+ * the default of 2e9 cycles, about 1 s at 2 GHz; the value is rounded down to a multiple of
+ * 1024). A wait that runs out sets the device status: the step's results are void, the next
+ * status check returns B2G_ERR_TIMEOUT and clears it, and the world can be restored with
+ * b2g_state_load. The reference has no device waits (it panics or loops on the host). */
+int b2g_set_barrier_limit(void* world, int64_t cycles);
+/* Test hook for the timeout path: every grid barrier of the world's kernels also waits for
+ * `extra` arrivals that never come, so each wait runs out its limit (0 turns it off). */
+int b2g_debug_hold_barriers(void* world, int32_t extra);
+
 /* The same stand-alone manifolds as b2g_collide_pairs, for callers that must not allocate
  * memory: a frame loop with a fixed time budget (freeing device memory can wait for the whole
  * device) or a host program whose device memory is owned by its own pool allocator. It calls
@@ -368,6 +454,9 @@ int b2g_set_graph_capture(void* world, int32_t flag);
  *   - All calls share the one scratch array. The function holds a process-wide lock and
  *     returns only after its results are copied back, because two calls running on the GPU
  *     at the same time would overwrite each other's data.
+ *   - It copies and launches on the legacy default stream of the current device. On entry it
+ *     clears a CUDA error left pending on the calling thread by an earlier call; after a failed
+ *     call it looks the scratch address up again (for example after a device reset).
  * It has no counterpart in the reference. */
 #define B2G_NOALLOC_MAX_PAIRS 16384
 int b2g_collide_pairs_noalloc(const b2g_fixture_def* shape_a, const float* xf_a, const b2g_fixture_def* shape_b,
@@ -495,6 +584,9 @@ int b2g_get_pairs(void* world, uint32_t* out_pairs, int32_t capacity, int32_t* o
 /* Fat AABBs (lower.x, lower.y, upper.x, upper.y per fixture) and moved flags
  * (B2dynamicTree::move_proxy, private/collision/b2_dynamic_tree.rs:109-168). */
 int b2g_get_proxies(void* world, float* out_aabbs, uint8_t* out_moved, int32_t capacity);
+/* Each fixture's proxy id (the reference's node index of its leaf in the dynamic tree,
+ * B2fixtureProxy::proxy_id, src/b2_fixture.rs:93-99), -1 for a fixture without a proxy. */
+int b2g_get_proxy_ids(void* world, int32_t* out_ids, int32_t capacity);
 /* The constraint order the GPU solved in during the last step: one (fixture_a, fixture_b)
  * pair per island contact, grouped by colour. Feeding it to the host reference solver as its
  * island contact order reproduces the GPU's Gauss-Seidel sweep

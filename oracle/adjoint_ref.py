@@ -38,6 +38,8 @@ def load():
         getattr(lib, name).restype = ctypes.c_int
     lib.ora_adj_backward_f64.argtypes = [vp, vp, vp, vp]
     lib.ora_adj_backward_f64.restype = ctypes.c_int
+    lib.ora_adj_backward_f64_anchored.argtypes = [vp, vp, vp]
+    lib.ora_adj_backward_f64_anchored.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -135,6 +137,15 @@ class AdjointRef:
         d_final = np.ascontiguousarray(d_final, np.float64)
         out = np.zeros((self.n, 6), np.float64)
         assert self._lib.ora_adj_backward_f64(self._h, _p(init), _p(d_final), _p(out)) == 0
+        return out
+
+    def backward_f64_anchored(self, d_final):
+        """The f64 reverse pass along the f32 replay's trajectory (call replay_f32 first): every step is
+        linearised at the f32 state it started from, so only the reverse pass's own rounding separates
+        it from the GPU's f32 gradient."""
+        d_final = np.ascontiguousarray(d_final, np.float64)
+        out = np.zeros((self.n, 6), np.float64)
+        assert self._lib.ora_adj_backward_f64_anchored(self._h, _p(d_final), _p(out)) == 0
         return out
 
 

@@ -58,6 +58,10 @@ struct Ref {
     std::vector<std::vector<int>> vcount, bias;       /* [t][k], [t][2k + j] */
     bool have_dec = false;
     long long carry_mismatch = 0;                     /* f32 replay: carried impulse != recorded one */
+    /* the f32 replay's trajectory: each step's starting state and the impulses carried into it, the
+     * points an anchored f64 pass linearises around */
+    std::vector<std::vector<Body<float>>> anchor_start;
+    std::vector<std::vector<float>> anchor_end_prev;
 };
 
 template <class T>
@@ -104,8 +108,12 @@ int pos_iters(const HSlot& t) {
     return n;
 }
 
+/* The taped steps. frozen = false: the f32 replay, which records every decision and its own
+ * trajectory; frozen = true: the frozen-decision model (any T). anchored (with frozen): every step
+ * starts from the f32 replay's state and carried impulses instead of the previous step's result, so a
+ * reverse pass over the trace is the f64-accurate gradient of the f32 trajectory's linearisation. */
 template <class T>
-void forward(Ref& R, bool frozen, std::vector<Body<T>>& st, Trace<T>* tr) {
+void forward(Ref& R, bool frozen, std::vector<Body<T>>& st, Trace<T>* tr, bool anchored = false) {
     if (!frozen) {
         R.vdec.assign(R.T, {});
         R.pdec.assign(R.T, {});
@@ -124,12 +132,36 @@ void forward(Ref& R, bool frozen, std::vector<Body<T>>& st, Trace<T>* tr) {
         tr->ww.assign(R.T, {});
         tr->wp.assign(R.T, {});
     }
+    if (!frozen) {
+        R.anchor_start.assign(R.T, {});
+        R.anchor_end_prev.assign(R.T, {});
+    }
     for (int t = 0; t < R.T; ++t) {
         const HStep& sp = R.steps[t];
         const std::vector<HSlot>& sl = R.slots[t];
         const std::vector<int>& co = R.col[t];
         const int ns = sp.nslots, ncol = sp.ncol;
         const T h = (T)sp.dt;
+        if (!frozen) {
+            R.anchor_start[t].resize(R.nb);
+            for (int b = 0; b < R.nb; ++b) {
+                Body<float>& a = R.anchor_start[t][b];
+                a.c = p2((float)st[b].c.x, (float)st[b].c.y);
+                a.a = (float)st[b].a;
+                a.v = p2((float)st[b].v.x, (float)st[b].v.y);
+                a.w = (float)st[b].w;
+            }
+            R.anchor_end_prev[t].assign(end_prev.begin(), end_prev.end());
+        } else if (anchored) {
+            for (int b = 0; b < R.nb; ++b) {
+                const Body<float>& a = R.anchor_start[t][b];
+                st[b].c = p2((T)a.c.x, (T)a.c.y);
+                st[b].a = (T)a.a;
+                st[b].v = p2((T)a.v.x, (T)a.v.y);
+                st[b].w = (T)a.w;
+            }
+            end_prev.assign(R.anchor_end_prev[t].begin(), R.anchor_end_prev[t].end());
+        }
         if (tr) tr->start[t] = st;
         for (int b = 0; b < R.nb; ++b)
             if (R.bs[b].type == 2) integrate_velocity(R.bs[b], h, (T)sp.gx, (T)sp.gy, st[b].v, st[b].w);
@@ -344,12 +376,25 @@ int ora_adj_forward_f64(void* h, const double* init, double* out) {
     return 0;
 }
 
+static int adj_backward(void* h, const double* init, const double* d_final, double* d_init, bool anchored);
+
 int ora_adj_backward_f64(void* h, const double* init, const double* d_final, double* d_init) {
+    return adj_backward(h, init, d_final, d_init, false);
+}
+
+/* the f64 reverse pass linearised around the f32 replay's trajectory (every step starts from the f32
+ * state): isolates the reverse pass's own arithmetic from the f32/f64 trajectories' divergence */
+int ora_adj_backward_f64_anchored(void* h, const double* d_final, double* d_init) {
+    return adj_backward(h, nullptr, d_final, d_init, true);
+}
+
+static int adj_backward(void* h, const double* init, const double* d_final, double* d_init, bool anchored) {
     Ref& R = *(Ref*)h;
-    if (!R.have_dec) return -1;
+    if (!R.have_dec || (anchored && (int)R.anchor_start.size() != R.T) || (!anchored && !init)) return -1;
     typedef double T;
     std::vector<Body<T>> st(R.nb);
     for (int b = 0; b < R.nb; ++b) {
+        if (anchored) continue;  /* the forward pass takes every step's start from the f32 replay */
         const double* p = init + 6 * (size_t)b;
         st[b].c = p2(p[0], p[1]);
         st[b].a = p[2];
@@ -357,7 +402,7 @@ int ora_adj_backward_f64(void* h, const double* init, const double* d_final, dou
         st[b].w = p[5];
     }
     Trace<T> tr;
-    forward<T>(R, true, st, &tr);
+    forward<T>(R, true, st, &tr, anchored);
     /* reverse */
     std::vector<Body<T>> g(R.nb);
     for (int b = 0; b < R.nb; ++b) {

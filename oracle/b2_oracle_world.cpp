@@ -44,6 +44,7 @@ namespace ora {
 enum { STATIC = 0, KINEMATIC = 1, DYNAMIC = 2 };
 
 struct Body {
+    bool alive = true;  /* false once destroyed (its slot keeps its last state) */
     int type = STATIC;
     Xf xf{};
     Sweep sweep{};
@@ -64,6 +65,7 @@ struct Body {
 };
 
 struct Fixture {
+    bool alive = true;
     int body = -1;
     Shape shape;
     float density = 0, friction = 0.2f, restitution = 0, threshold = 1.0f;
@@ -127,7 +129,7 @@ struct Joint {
     Vec2 ground_a{0, 0}, ground_b{0, 0}, u_a{0, 0}, u_b{0, 0};
     float pulley_constant = 0, ratio = 1, pulley_impulse = 0, pulley_mass = 0;
     float weld_mass[9] = {0};  /* ex, ey, ez columns */
-    bool collide_connected = false, island_flag = false;
+    bool collide_connected = false, island_flag = false, alive = true;
     Vec2 local_anchor_a{0, 0}, local_anchor_b{0, 0};
     float reference_angle = 0;
     bool enable_limit = false, enable_motor = false;
@@ -184,8 +186,17 @@ struct Step {
     bool warm;
 };
 
+typedef int (*ContactFilterFn)(void* user, uint32_t fixture_a, uint32_t fixture_b);
+typedef void (*PreSolveFn)(void* user, const b2g_contact_info* contact, const b2g_contact_info* old_manifold,
+                           b2g_contact_edit* edit);
+
 struct World {
     Vec2 gravity{0, -10};
+    ContactFilterFn filter_fn = nullptr;  /* the user's contact filter (nullptr: the default filter) */
+    std::vector<b2g_contact_impulse> post_solve;  /* the last step's island reports, in solve order */
+    PreSolveFn pre_solve_fn = nullptr;            /* the listener's pre_solve (nullptr: none) */
+    void* pre_solve_user = nullptr;
+    void* filter_user = nullptr;
     std::vector<Body> bodies;
     std::vector<Fixture> fixtures;
     std::vector<Contact> contacts;
@@ -427,6 +438,14 @@ static bool filter_should_collide(const Fixture& a, const Fixture& b) {
     return (a.mask & b.category) != 0 && (a.category & b.mask) != 0;
 }
 
+/* the world's contact filter: the user's (B2world::set_contact_filter, src/b2_world.rs:38-40, replacing
+ * the default) or the default one; called with the fixtures of the pair's smaller and larger proxy id
+ * in add_pair, with the contact's fixtures A and B for a flagged contact in collide */
+static bool contact_filter(const World& w, int fa, int fb) {
+    if (w.filter_fn) return w.filter_fn(w.filter_user, (uint32_t)fa, (uint32_t)fb) != 0;
+    return filter_should_collide(w.fixtures[fa], w.fixtures[fb]);
+}
+
 /* b2_contact_registers.rs:67-103: which (typeA, typeB) has a manifold routine with A first */
 static int register_kind(int t1, int t2) {
     /* +1 primary, -1 swap, 0 none */
@@ -461,7 +480,7 @@ static void add_pair(World& w, int fixA, int fixB) {
         }
     }
     if (!should_collide(w, bodyB, bodyA)) return;
-    if (!filter_should_collide(w.fixtures[fixA], w.fixtures[fixB])) return;
+    if (!contact_filter(w, fixA, fixB)) return;
     int kind = register_kind(w.fixtures[fixA].shape.type, w.fixtures[fixB].shape.type);
     if (kind == 0) return;
     if (kind < 0) std::swap(fixA, fixB);
@@ -534,6 +553,27 @@ static void evaluate(const Contact& c, const World& w, Manifold& m, const Xf& xf
     else collide_edge_polygon(m, sa, xfA, sb, xfB);
 }
 
+/* a contact (fixtures, touching flag, material) with manifold m, as the C ABI reports it */
+static void contact_info(const Contact& c, const Manifold& m, b2g_contact_info& o) {
+    memset(&o, 0, sizeof(o));
+    o.fixture_a = (uint32_t)c.fa;
+    o.fixture_b = (uint32_t)c.fb;
+    o.touching = c.touching ? 1 : 0;
+    o.manifold_type = m.type;
+    o.point_count = m.point_count;
+    o.local_normal = b2g_vec2{m.local_normal.x, m.local_normal.y};
+    o.local_point = b2g_vec2{m.local_point.x, m.local_point.y};
+    for (int j = 0; j < 2; ++j) {
+        o.point_local[j] = b2g_vec2{m.points[j].local_point.x, m.points[j].local_point.y};
+        o.normal_impulse[j] = m.points[j].normal_impulse;
+        o.tangent_impulse[j] = m.points[j].tangent_impulse;
+        o.point_id[j] = m.points[j].id;
+    }
+    o.friction = c.friction;
+    o.restitution = c.restitution;
+    o.restitution_threshold = c.threshold;
+}
+
 /* b2_contact_update, private/dynamics/b2_contact.rs:103-218 */
 static void update_contact(World& w, int id) {
     Contact& c = w.contacts[id];
@@ -575,6 +615,21 @@ static void update_contact(World& w, int id) {
         if (!wasTouching && touching) w.events.push_back(b2g_contact_event{B2G_EVENT_BEGIN, (uint32_t)c.fa, (uint32_t)c.fb});
         if (wasTouching && !touching) w.events.push_back(b2g_contact_event{B2G_EVENT_END, (uint32_t)c.fa, (uint32_t)c.fb});
     }
+    /* listener.pre_solve(contact, old_manifold) for a touching non-sensor contact (:215); the
+     * listener may disable the contact or change its material for this step */
+    if (!sensor && touching && w.pre_solve_fn) {
+        b2g_contact_info now, prev;
+        contact_info(c, c.m, now);
+        contact_info(c, old, prev);
+        prev.touching = wasTouching ? 1 : 0;
+        b2g_contact_edit e{c.enabled ? 1 : 0, c.friction, c.restitution, c.threshold, c.tangent_speed};
+        w.pre_solve_fn(w.pre_solve_user, &now, &prev, &e);
+        c.enabled = e.enabled != 0;
+        c.friction = e.friction;
+        c.restitution = e.restitution;
+        c.threshold = e.restitution_threshold;
+        c.tangent_speed = e.tangent_speed;
+    }
 }
 
 static uint64_t contact_proxy_key(const World& w, const Contact& c);
@@ -595,8 +650,8 @@ static void collide(World& w) {
         const Fixture& FA = w.fixtures[c.fa];
         const Fixture& FB = w.fixtures[c.fb];
         if (c.filter_flag) {
-            /* should these bodies collide? (the default filter's answer does not change) */
-            if (!should_collide(w, FB.body, FA.body)) {
+            /* should these bodies collide, and does the contact filter still allow the fixtures? */
+            if (!should_collide(w, FB.body, FA.body) || !contact_filter(w, c.fa, c.fb)) {
                 to_destroy.push_back(id);
                 continue;
             }
@@ -2372,6 +2427,20 @@ static void solve_island(World& w, const Step& step) {
         solve_velocity(w);
     }
     store_impulses(w);
+    /* B2island::report (b2_island_private.rs:460-487): each island contact's impulses after the
+     * velocity iterations, point count as solved (a 2-point manifold solved as 1 reports 1) */
+    for (const VelocityConstraint& vc : w.vcs) {
+        const Contact& c = w.contacts[w.isl_contacts[vc.contact]];
+        b2g_contact_impulse r{};
+        r.fixture_a = (uint32_t)c.fa;
+        r.fixture_b = (uint32_t)c.fb;
+        r.count = vc.count;
+        for (int j = 0; j < vc.count; ++j) {
+            r.normal_impulses[j] = vc.p[j].ni;
+            r.tangent_impulses[j] = vc.p[j].ti;
+        }
+        w.post_solve.push_back(r);
+    }
     for (int i = 0; i < nb; ++i) {
         Vec2 c = w.pos[i].c;
         float a = w.pos[i].a;
@@ -2829,8 +2898,95 @@ static void solve_toi(World& w, const Step& step) {
 }
 
 /* B2world::step, private/dynamics/b2_world.rs:903-959 */
+/* ---- destruction (src/b2_world.rs:72-91, src/b2_body.rs:259) and filtering (src/b2_fixture.rs:179-189) ---- */
+
+/* B2world::destroy_joint, private/dynamics/b2_world.rs:278-340 */
+static void destroy_joint(World& w, int id) {
+    Joint& J = w.joints[id];
+    if (J.prev >= 0) w.joints[J.prev].next = J.next;
+    else w.joint_head = J.next;
+    if (J.next >= 0) w.joints[J.next].prev = J.prev;
+    J.prev = J.next = -1;
+    set_awake(w.bodies[J.body_a], true);
+    set_awake(w.bodies[J.body_b], true);
+    for (int side = 0; side < 2; ++side) {  /* remove the joint edge from each body's singly linked list */
+        const int b = side == 0 ? J.body_a : J.body_b;
+        const int mine = 2 * id + side;
+        int* link = &w.bodies[b].jedge_head;
+        while (*link >= 0 && *link != mine) link = &w.jedges[*link].next;
+        if (*link == mine) *link = w.jedges[mine].next;
+    }
+    J.alive = false;
+    if (!J.collide_connected) {
+        for (int e = w.bodies[J.body_b].edge_head; e >= 0; e = w.edges[e].next)
+            if (w.edges[e].other == J.body_a) w.contacts[w.edges[e].contact].filter_flag = true;
+    }
+}
+
+/* B2fixture::destroy_proxies, private/dynamics/b2_fixture.rs:135-145 */
+static void destroy_proxies(World& w, Fixture& f) {
+    if (f.proxy < 0) return;
+    w.bp.destroy_proxy(f.proxy);
+    f.proxy = -1;
+}
+
+/* B2body::destroy_fixture, private/dynamics/b2_body.rs:214-289 */
+static void destroy_fixture(World& w, int fid) {
+    Fixture& F = w.fixtures[fid];
+    Body& b = w.bodies[F.body];
+    int* link = &b.fixture_head;
+    while (*link >= 0 && *link != fid) link = &w.fixtures[*link].next;
+    if (*link == fid) *link = F.next;
+    F.next = -1;
+    /* the body's contacts of this fixture (B2contactManager::destroy) */
+    for (int e = b.edge_head; e >= 0;) {
+        const int next = w.edges[e].next;
+        const Contact& c = w.contacts[w.edges[e].contact];
+        if (c.fa == fid || c.fb == fid) destroy_contact(w, w.edges[e].contact);
+        e = next;
+    }
+    if (b.enabled) destroy_proxies(w, F);
+    F.alive = false;
+    reset_mass_data(w, b);
+}
+
+/* B2world::destroy_body, private/dynamics/b2_world.rs:100-158 */
+static void destroy_body(World& w, int bid) {
+    Body& b = w.bodies[bid];
+    while (b.jedge_head >= 0) destroy_joint(w, w.jedges[b.jedge_head].joint);
+    while (b.edge_head >= 0) destroy_contact(w, w.edges[b.edge_head].contact);
+    for (int f = b.fixture_head; f >= 0;) {
+        const int next = w.fixtures[f].next;
+        destroy_proxies(w, w.fixtures[f]);
+        w.fixtures[f].alive = false;
+        w.fixtures[f].next = -1;
+        f = next;
+    }
+    b.fixture_head = -1;
+    if (b.prev >= 0) w.bodies[b.prev].next = b.next;
+    else w.body_head = b.next;
+    if (b.next >= 0) w.bodies[b.next].prev = b.prev;
+    b.prev = b.next = -1;
+    b.alive = false;
+    b.awake = false;  /* the slot reads as asleep, as the GPU's does */
+}
+
+/* B2fixture::set_filter_data + refilter, private/dynamics/b2_fixture.rs:175-211 */
+static void set_filter_data(World& w, int fid, uint16_t category, uint16_t mask, int16_t group) {
+    Fixture& F = w.fixtures[fid];
+    F.category = category;
+    F.mask = mask;
+    F.group = group;
+    for (int e = w.bodies[F.body].edge_head; e >= 0; e = w.edges[e].next) {
+        Contact& c = w.contacts[w.edges[e].contact];
+        if (c.fa == fid || c.fb == fid) c.filter_flag = true;
+    }
+    if (F.proxy >= 0) w.bp.touch_proxy(F.proxy);
+}
+
 static void step(World& w, float dt, int vi, int pi) {
     auto t0 = std::chrono::steady_clock::now();
+    w.post_solve.clear();
     if (w.new_contacts) {
         find_new_contacts(w);
         w.new_contacts = false;
@@ -3055,7 +3211,16 @@ int ora_get_proxies(void* p, float* aabbs, uint8_t* moved, int* proxy_ids, int c
     int n = (int)w.fixtures.size();
     for (int i = 0; i < n && i < cap; ++i) {
         const Fixture& f = w.fixtures[i];
-        if (f.proxy < 0) continue;
+        if (f.proxy < 0) {  /* no proxy (disabled or destroyed): an empty box, as the GPU reports it */
+            const float inf = INFINITY;
+            aabbs[4 * i + 0] = inf;
+            aabbs[4 * i + 1] = inf;
+            aabbs[4 * i + 2] = -inf;
+            aabbs[4 * i + 3] = -inf;
+            if (moved) moved[i] = 0;
+            if (proxy_ids) proxy_ids[i] = -1;
+            continue;
+        }
         const AABB& a = w.bp.tree.fat_aabb(f.proxy);
         aabbs[4 * i + 0] = a.lo.x;
         aabbs[4 * i + 1] = a.lo.y;
@@ -3223,6 +3388,58 @@ int ora_set_joint_order(void* p, const uint32_t* order, int n) {
     w.joint_rank.assign(w.joints.size(), 0x7fffffff);
     for (int i = 0; i < n; ++i)
         if (order[i] < w.joint_rank.size()) w.joint_rank[order[i]] = i;
+    return 0;
+}
+
+int ora_destroy_bodies(void* p, const uint32_t* ids, int n) {
+    World& w = *(World*)p;
+    for (int i = 0; i < n; ++i)
+        if (ids[i] >= w.bodies.size() || !w.bodies[ids[i]].alive) return -1;
+    for (int i = 0; i < n; ++i) destroy_body(w, (int)ids[i]);
+    return 0;
+}
+
+int ora_destroy_fixtures(void* p, const uint32_t* ids, int n) {
+    World& w = *(World*)p;
+    for (int i = 0; i < n; ++i)
+        if (ids[i] >= w.fixtures.size() || !w.fixtures[ids[i]].alive) return -1;
+    for (int i = 0; i < n; ++i) destroy_fixture(w, (int)ids[i]);
+    return 0;
+}
+
+int ora_destroy_joints(void* p, const uint32_t* ids, int n) {
+    World& w = *(World*)p;
+    for (int i = 0; i < n; ++i)
+        if (ids[i] >= w.joints.size() || !w.joints[ids[i]].alive) return -1;
+    for (int i = 0; i < n; ++i) destroy_joint(w, (int)ids[i]);
+    return 0;
+}
+
+int ora_set_filter_data(void* p, uint32_t f, int category, int mask, int group) {
+    World& w = *(World*)p;
+    if (f >= w.fixtures.size() || !w.fixtures[f].alive) return -1;
+    set_filter_data(w, (int)f, (uint16_t)category, (uint16_t)mask, (int16_t)group);
+    return 0;
+}
+
+int ora_set_contact_filter(void* p, ContactFilterFn fn, void* user) {
+    World& w = *(World*)p;
+    w.filter_fn = fn;
+    w.filter_user = user;
+    return 0;
+}
+
+int ora_set_pre_solve(void* p, PreSolveFn fn, void* user) {
+    World& w = *(World*)p;
+    w.pre_solve_fn = fn;
+    w.pre_solve_user = user;
+    return 0;
+}
+
+int ora_get_post_solve(void* p, b2g_contact_impulse* out, int cap, int* n) {
+    World& w = *(World*)p;
+    *n = (int)w.post_solve.size();
+    for (int i = 0; out && i < *n && i < cap; ++i) out[i] = w.post_solve[i];
     return 0;
 }
 

@@ -23,6 +23,7 @@ sys.path.insert(0, os.path.join(os.path.dirname(_HERE), "box2d-rs_gb300"))
 import b2g  # noqa: E402  (struct layouts of include/b2g.h)
 
 _lib = None
+CONTACT_FILTER_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32)
 
 
 def build(force=False):
@@ -78,6 +79,13 @@ def load():
         "ora_collide": [vp, vp, vp, vp, vp],
         "ora_time_of_impact": [vp, vp, vp, vp, vp, i32, vp],
         "ora_import_state": [vp, vp, i32, vp, i32, vp, i32, f32],
+        "ora_destroy_bodies": [vp, vp, i32],
+        "ora_destroy_fixtures": [vp, vp, i32],
+        "ora_destroy_joints": [vp, vp, i32],
+        "ora_set_filter_data": [vp, u32, i32, i32, i32],
+        "ora_set_contact_filter": [vp, vp, vp],
+        "ora_get_post_solve": [vp, vp, i32, pi32],
+        "ora_set_pre_solve": [vp, vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -284,6 +292,15 @@ class OracleWorld:
     def get_solver_order(self):
         return self._get_list(self._lib.ora_get_solver_order, np.uint32, 2).reshape(-1, 2)
 
+    def set_pre_solve(self, fn):
+        """fn(contact, old_manifold, edit) as b2g.B2world.set_pre_solve."""
+        self._pre_solve_cb = None if fn is None else b2g.pre_solve_callback(fn)
+        ptr = None if fn is None else ctypes.cast(self._pre_solve_cb, ctypes.c_void_p)
+        self._lib.ora_set_pre_solve(self._h, ptr, None)
+
+    def get_post_solve(self):
+        return self._get_list(self._lib.ora_get_post_solve, b2g.CONTACT_IMPULSE)
+
     def get_events(self):
         return self._get_list(self._lib.ora_get_events, b2g.EVENT)
 
@@ -329,6 +346,31 @@ class OracleWorld:
 
     def hook_misses(self):
         return self._lib.ora_get_hook_misses(self._h)
+
+    def destroy_bodies(self, ids):
+        ids = np.ascontiguousarray(ids, np.uint32)
+        assert self._lib.ora_destroy_bodies(self._h, _ptr(ids), len(ids)) == 0
+
+    def destroy_fixtures(self, ids):
+        ids = np.ascontiguousarray(ids, np.uint32)
+        assert self._lib.ora_destroy_fixtures(self._h, _ptr(ids), len(ids)) == 0
+
+    def destroy_joints(self, ids):
+        ids = np.ascontiguousarray(ids, np.uint32)
+        assert self._lib.ora_destroy_joints(self._h, _ptr(ids), len(ids)) == 0
+
+    def set_filter_data(self, fixture, category_bits, mask_bits, group_index):
+        assert self._lib.ora_set_filter_data(self._h, int(fixture), int(category_bits), int(mask_bits),
+                                             int(group_index)) == 0
+
+    def set_contact_filter(self, fn):
+        """fn(fixture_a, fixture_b) -> bool replaces the default contact filter (None restores it)."""
+        if fn is None:
+            self._filter_cb = None
+            self._lib.ora_set_contact_filter(self._h, None, None)
+            return
+        self._filter_cb = CONTACT_FILTER_FN(lambda user, a, b: 1 if fn(int(a), int(b)) else 0)
+        self._lib.ora_set_contact_filter(self._h, ctypes.cast(self._filter_cb, ctypes.c_void_p), None)
 
     def import_state(self, bodies, fat_aabbs, contacts, inv_dt0):
         """Continue from another engine's post-step state (see ora_import_state)."""

@@ -31,14 +31,17 @@ class MultiOracle:
     running each in its own oracle and mapping body/fixture ids. Creation order inside each
     world follows the batch's order, so proxy ids keep the same relative order."""
 
-    def __init__(self, scene, **kw):
+    def __init__(self, scene, worlds=None, **kw):
+        """worlds: the batch's worlds to restate (default all); the others are left out and their
+        bodies and fixtures read as zeros."""
         bodies, fixtures = scene["bodies"], scene["fixtures"]
         wi = bodies["world_index"]
         self.n_bodies, self.n_fixtures = len(bodies), len(fixtures)
         self.worlds = []
-        self.fix_world = np.zeros(len(fixtures), np.int64)
+        self.world_ids = list(range(scene["num_worlds"])) if worlds is None else [int(x) for x in worlds]
+        self.fix_world = np.full(len(fixtures), -1, np.int64)
         self.fix_local = np.zeros(len(fixtures), np.int64)
-        for w in range(scene["num_worlds"]):
+        for w in self.world_ids:
             bidx = np.nonzero(wi == w)[0]
             remap = np.full(len(bodies), -1, np.int64)
             remap[bidx] = np.arange(len(bidx))
@@ -58,11 +61,30 @@ class MultiOracle:
         for o, _, _ in self.worlds:
             o.step(dt, vi, pi)
 
+    def body_mask(self):
+        m = np.zeros(self.n_bodies, bool)
+        for _, bidx, _ in self.worlds:
+            m[bidx] = True
+        return m
+
+    def fixture_mask(self):
+        return self.fix_world >= 0
+
+    def import_state(self, bodies, fat_aabbs, contacts, inv_dt0):
+        """Each restated world continues from its part of a batch's post-step state."""
+        c = np.asarray(contacts)
+        cw = self.fix_world[c["fixture_a"].astype(np.int64)] if len(c) else np.zeros(0, np.int64)
+        for k, (o, bidx, fidx) in enumerate(self.worlds):
+            cc = c[cw == self.world_ids[k]].copy()
+            cc["fixture_a"] = self.fix_local[cc["fixture_a"].astype(np.int64)]
+            cc["fixture_b"] = self.fix_local[cc["fixture_b"].astype(np.int64)]
+            o.import_state(bodies[bidx], np.asarray(fat_aabbs)[fidx], cc, inv_dt0)
+
     def set_solver_order(self, pairs):
         p = np.asarray(pairs, np.int64).reshape(-1, 2)
         w = self.fix_world[p[:, 0]] if len(p) else np.zeros(0, np.int64)
         for k, (o, _, _) in enumerate(self.worlds):
-            sel = p[w == k]
+            sel = p[w == self.world_ids[k]]
             o.set_solver_order(np.stack([self.fix_local[sel[:, 0]], self.fix_local[sel[:, 1]]], 1) if len(sel) else None)
 
     def hook_misses(self):
@@ -80,6 +102,10 @@ class MultiOracle:
 
     def toi_events(self):
         return sum(o.toi_events() for o, _, _ in self.worlds)
+
+    def close(self):
+        for o, _, _ in self.worlds:
+            o.close()
 
     def get_body_states(self):
         out = np.zeros(self.n_bodies, b2g.BODY_STATE)
@@ -166,6 +192,46 @@ def contact_map(contacts):
     return {(int(c["fixture_a"]), int(c["fixture_b"])): c for c in contacts}
 
 
+def _sorted_by_pair(c):
+    c = np.asarray(c)
+    return c[np.lexsort((c["fixture_b"], c["fixture_a"]))] if len(c) else c
+
+
+def manifold_diff_fast(gpu_contacts, ora_contacts):
+    """manifold_diff with array operations, for tables of hundreds of thousands of contacts. Returns
+    (number of fixture pairs in one table only, id mismatches, max point/impulse difference)."""
+    g, o = _sorted_by_pair(gpu_contacts), _sorted_by_pair(ora_contacts)
+    kg = (g["fixture_a"].astype(np.uint64) << np.uint64(32)) | g["fixture_b"].astype(np.uint64)
+    ko = (o["fixture_a"].astype(np.uint64) << np.uint64(32)) | o["fixture_b"].astype(np.uint64)
+    common, ig, io = np.intersect1d(kg, ko, assume_unique=True, return_indices=True)
+    key_mismatch = len(kg) + len(ko) - 2 * len(common)
+    a, b = g[ig], o[io]
+    same_head = (a["touching"] == b["touching"]) & (a["point_count"] == b["point_count"])
+    n = a["point_count"]
+    typed = same_head & (n > 0)
+    type_ok = ~typed | (a["manifold_type"] == b["manifold_type"])
+    ids_ok = np.ones(len(a), bool)
+    for j in range(2):
+        sel = typed & type_ok & (n > j)
+        ids_ok &= ~sel | (a["point_id"][:, j] == b["point_id"][:, j])
+    id_mismatch = int((~same_head).sum() + (~type_ok).sum() + (same_head & type_ok & ~ids_ok).sum())
+    worst = 0.0
+    cmp = typed & type_ok
+    if cmp.any():
+        aa, bb = a[cmp], b[cmp]
+        for f in ("local_normal", "local_point"):
+            worst = max(worst, float(np.abs(aa[f].astype(np.float64) - bb[f]).max()))
+        nn = aa["point_count"]
+        for j in range(2):
+            sel = nn > j
+            if sel.any():
+                for f in ("point_local",):
+                    worst = max(worst, float(np.abs(aa[f][sel, j].astype(np.float64) - bb[f][sel, j]).max()))
+                for f in ("normal_impulse", "tangent_impulse"):
+                    worst = max(worst, float(np.abs(aa[f][sel, j].astype(np.float64) - bb[f][sel, j]).max()))
+    return key_mismatch, id_mismatch, worst
+
+
 def manifold_diff(gpu_contacts, ora_contacts):
     """Compare live contacts by fixture pair. Returns (missing/extra keys, id mismatches, max point diff)."""
     g = contact_map(gpu_contacts)
@@ -208,6 +274,87 @@ def drop_transient(contacts, aabbs):
     apart = (b[:, 0] - a[:, 2] > 0) | (b[:, 1] - a[:, 3] > 0) | (a[:, 0] - b[:, 2] > 0) | (a[:, 1] - b[:, 3] > 0)
     keep = ~apart | (c["touching"] != 0) | (c["point_count"] > 0)
     return c[keep]
+
+
+def _pair_keys(pairs, fix_mask=None):
+    p = np.asarray(pairs, np.int64).reshape(-1, 2)
+    if fix_mask is not None and len(p):
+        p = p[fix_mask[p[:, 0]] & fix_mask[p[:, 1]]]
+    if len(p) == 0:
+        return np.zeros(0, np.int64)
+    return np.unique(np.minimum(p[:, 0], p[:, 1]) << 32 | np.maximum(p[:, 0], p[:, 1]))
+
+
+def _restrict_contacts(c, fix_mask):
+    c = np.asarray(c)
+    if fix_mask is None or len(c) == 0:
+        return c
+    return c[fix_mask[c["fixture_a"].astype(np.int64)]]
+
+
+def lockstep_window(scene, steps, skip=0, worlds=None, check_pairs=True, part_solve=None):
+    """Lockstep parity on a window of a scene: the GPU steps `skip` steps alone, the oracle imports its
+    post-step state (bodies, fat AABBs, the contact table with manifolds and impulses, the warm-start
+    ratio), then both step `steps` more, the oracle in the GPU's solve order. For a batched scene,
+    `worlds` selects the worlds the oracle restates (the GPU steps every world); only those worlds'
+    bodies, proxies, pairs and contacts are compared. Array comparisons throughout, so it scales to
+    the configurations' full sizes. Returns per-step records."""
+    oracle.set_trig(False)
+    nw = scene.get("num_worlds", 1)
+    gpu = b2g.B2world(gravity=scene["gravity"], num_worlds=nw,
+                      contact_capacity=scene.get("contact_capacity", 0), pair_capacity=scene.get("pair_capacity", 0))
+    gpu.set_allow_sleeping(False)
+    gpu.set_record_pairs(check_pairs)
+    if part_solve is not None:
+        gpu.set_part_solve(part_solve)
+    scenes.build_world(gpu, scene)
+    dt, vi, pi = scene["dt"], scene["vi"], scene["pi"]
+    for _ in range(skip):
+        gpu.step(dt, vi, pi)
+    if nw > 1:
+        ora = MultiOracle(scene, worlds=worlds, allow_sleep=False)
+        bmask, fmask = ora.body_mask(), ora.fixture_mask()
+    else:
+        ora = oracle.OracleWorld(gravity=scene["gravity"], allow_sleep=False)
+        scenes.build_world(ora, scene)
+        bmask, fmask = None, None
+    ora.set_key_order(True)
+    if skip > 0:
+        aabbs, _ = gpu.get_proxies()
+        ora.import_state(gpu.get_body_states(), aabbs, gpu.get_contacts(), np.float32(1.0) / dt)
+    out = []
+    for k in range(steps):
+        gpu.step(dt, vi, pi)
+        order = gpu.get_solver_order()
+        ora.set_solver_order(order)
+        ora.step(dt, vi, pi)
+        rec = {"step": skip + k + 1, "hook_misses": ora.hook_misses(), "constraints": len(order)}
+        gs, os_ = gpu.get_body_states(), ora.get_body_states()
+        if bmask is not None:
+            gs, os_ = gs[bmask], os_[bmask]
+        rec["body_abs"], rec["body_rel"] = body_diff(gs, os_)
+        rec["bitexact_bodies"] = all(np.array_equal(gs[f], os_[f]) for f in BODY_FIELDS)
+        if check_pairs:
+            gp, op = _pair_keys(gpu.get_pairs(), fmask), _pair_keys(ora.get_pairs(), fmask)
+            rec["pairs_equal"] = bool(np.array_equal(gp, op))
+            rec["pairs"] = int(len(gp))
+        ga, _ = gpu.get_proxies()
+        oa, _, _ = ora.get_proxies()
+        if fmask is not None:
+            ga, oa = ga[fmask], oa[fmask]
+        rec["fat_aabb_equal"] = bool(np.array_equal(ga, oa))
+        gc = _restrict_contacts(gpu.get_contacts(), fmask)
+        oc = ora.get_contacts()
+        km, im, worst = manifold_diff_fast(gc, oc)
+        rec["contacts"] = int(len(gc))
+        rec["contact_key_mismatch"] = km
+        rec["contact_id_mismatch"] = im
+        rec["manifold_max_diff"] = worst
+        out.append(rec)
+    gpu.close()
+    if hasattr(ora, "close"):
+        ora.close()
+    return out
 
 
 def lockstep(scene, steps, check_pairs=True, check_contacts=True, resync=False, on_step=None, before_step=None):

@@ -79,3 +79,23 @@ def test_recorded_gpu_gradient_matches_f64(tape):
                       gg["linear_velocity"][:, 1], gg["angular_velocity"]], 1).astype(np.float64)
     rel = np.linalg.norm(g_gpu - g) / np.linalg.norm(g)
     assert rel <= 1e-3, rel
+
+
+def test_anchored_reverse_pass_matches_the_recorded_gpu_gradient(tape):
+    """The f64 reverse pass linearised along the f32 replay's own trajectory (every step starts from
+    the f32 state it started from on the GPU): only the reverse pass's rounding separates it from the
+    GPU's f32 gradient, so the two agree far below 1e-3."""
+    z, ref = tape
+    init = adjoint_ref.state_from_checkpoint(z["init"])
+    ref.replay_f32(init)
+    gd = np.zeros((len(init), 6))
+    gd[:, 0:2] = z["d_final"]["world_center"]
+    g = ref.backward_f64_anchored(gd)
+    gg = z["gpu_grad"]
+    g_gpu = np.stack([gg["world_center"][:, 0], gg["world_center"][:, 1], gg["angle"], gg["linear_velocity"][:, 0],
+                      gg["linear_velocity"][:, 1], gg["angular_velocity"]], 1).astype(np.float64)
+    rel = np.linalg.norm(g_gpu - g) / np.linalg.norm(g)
+    assert rel <= 1e-4, rel
+    # the unanchored f64 pass over this short tape lands on nearly the same gradient
+    g64 = ref.backward_f64(init.astype(np.float64), gd)
+    assert np.linalg.norm(g64 - g) / np.linalg.norm(g) <= 1e-3

@@ -254,3 +254,38 @@ def test_state_checkpoint_resumes_bit_for_bit(built, continuous, sleep):
         small = b2g.B2world(gravity=s["gravity"])
         scenes.build_world(small, scenes.pyramid(rows=3))
         small.load_state(state)
+
+
+def test_barrier_timeout_reports_and_world_recovers(built):
+    """A grid-barrier wait that runs out returns B2G_ERR_TIMEOUT instead of hanging: the world's
+    barriers are made to wait for arrivals that never come (b2g_debug_hold_barriers) under a short
+    limit (~0.5 ms); every block leaves its kernel and the host reports the timeout. The world is
+    then restored from a checkpoint and its next steps equal those of a world that never failed."""
+    s = scenes.mixed(n_circles=1500, n_polygons=1500, size=60.0, seed=3)
+
+    def make():
+        w = b2g.B2world(gravity=s["gravity"])
+        w.set_allow_sleeping(False)
+        scenes.build_world(w, s)
+        return w
+
+    a = make()
+    _continue(a, s, 10)
+    state = a.save_state()
+    ref = _continue(a, s, 10)
+
+    b = make()
+    b.load_state(state)
+    b.set_barrier_limit(1 << 20)
+    b.debug_hold_barriers(1)
+    b.step(s["dt"], s["vi"], s["pi"])
+    with pytest.raises(b2g.B2GError) as err:
+        b.synchronize()
+    assert err.value.code == b2g.ERR_TIMEOUT
+    b.debug_hold_barriers(0)
+    b.set_barrier_limit(0)
+    b.load_state(state)
+    got = _continue(b, s, 10)
+    for f in b2g.BODY_STATE.names:
+        assert np.array_equal(ref[0][f], got[0][f]), f
+    assert np.array_equal(ref[1], got[1])
