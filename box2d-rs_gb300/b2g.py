@@ -177,9 +177,12 @@ JOINT_DEF = np.dtype(
         ("length_a", "<f4"),
         ("length_b", "<f4"),
         ("ratio", "<f4"),
+        ("joint1", "<u4"),
+        ("joint2", "<u4"),
     ]
 )
 JOINT_DISTANCE = 3
+JOINT_GEAR = 6
 JOINT_WELD = 8
 JOINT_FRICTION = 9
 JOINT_MOTOR = 11
@@ -275,6 +278,17 @@ def pulley_joint(body_a, body_b, ground_a, ground_b, anchor_a, anchor_b, length_
     d["local_anchor_a"], d["local_anchor_b"] = anchor_a, anchor_b
     d["ground_anchor_a"], d["ground_anchor_b"] = ground_a, ground_b
     d["length_a"], d["length_b"], d["ratio"] = length_a, length_b, ratio
+    return d
+
+
+def gear_joint(joint1, joint2, body_a, body_b, ratio=1.0, collide_connected=False):
+    """B2gearJointDef: couples two revolute or prismatic joints (ids of joints created earlier) so that
+    coordinate1 + ratio * coordinate2 stays constant; body_a and body_b are the joints' second bodies."""
+    d = np.zeros(1, JOINT_DEF)
+    d["type"] = JOINT_GEAR
+    d["body_a"], d["body_b"] = body_a, body_b
+    d["collide_connected"] = int(bool(collide_connected))
+    d["joint1"], d["joint2"], d["ratio"] = joint1, joint2, ratio
     return d
 
 

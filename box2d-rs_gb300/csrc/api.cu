@@ -92,6 +92,16 @@ struct TapeHost {
     unsigned mismatches = 0;
 };
 
+/* What B2gearJoint::new (private/dynamics/joints/b2_gear_joint.rs:29-137) fixes when the joint is made:
+ * bodies C and D, the four local anchors, the prismatic sides' axes, the revolute sides' reference
+ * angles, the sides' types and the constant coordinate_a + ratio * coordinate_b. */
+struct GearFrame {
+    int body_c = 0, body_d = 0;
+    bool prismatic_a = false, prismatic_b = false;
+    V2 anchor_a{0, 0}, anchor_b{0, 0}, anchor_c{0, 0}, anchor_d{0, 0}, axis_c{0, 0}, axis_d{0, 0};
+    float ref_a = 0.0f, ref_b = 0.0f, constant = 0.0f;
+};
+
 struct World {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -104,6 +114,7 @@ struct World {
     bool kinematic_or_bullet = false;  /* a kinematic or bullet body exists */
     /* joints: definitions, host copies of their impulses, the colouring, body -> joints */
     std::vector<b2g_joint_def> joints;
+    std::vector<GearFrame> gear;       /* per joint: a gear joint's frame, fixed at creation */
     std::vector<float4> h_jimp, h_jimp2;
     std::vector<int> h_jorder, h_jcoff, h_jnt_off, h_jnt;
     bool joints_dirty = false;          /* joints changed since the device copy */
@@ -239,6 +250,9 @@ int fail(World* w, int code, const std::string& msg) { return fail(w, code, msg.
             return B2G_ERR_CUDA;                                               \
         }                                                                      \
     } while (0)
+
+/* Host-to-device copies of a world go on its stream (cudaMemcpyAsync): a plain cudaMemcpy from pageable
+ * memory may return before its transfer lands and is not ordered with the world's non-blocking stream. */
 
 template <class T>
 int dalloc(World* w, T** p, size_t n) {
@@ -692,8 +706,10 @@ int upload(World* w) {
     return B2G_OK;
 }
 
-/* device -> host mirrors for bodies and fixtures (before host-side edits after stepping) */
+/* device -> host mirrors for bodies and fixtures (before host-side edits after stepping). With host edits
+ * pending (host_dirty) the mirrors are already current: every device-side operation uploads them first. */
 int download_state(World* w) {
+    if (w->host_dirty) return B2G_OK;
     DevWorld& d = w->d;
     const int nb = w->uploaded_bodies;
     const int nf = w->uploaded_fixtures;
@@ -726,6 +742,26 @@ int download_joint_impulses(World* w) {
     return B2G_OK;
 }
 
+/* (Re)allocates the joint table for cap joints (its contents start at zero). */
+int alloc_joint_arrays(World* w, int cap) {
+    DevWorld& d = w->d;
+    dfree(w, &d.j_body); dfree(w, &d.j_body2); dfree(w, &d.j_anchor); dfree(w, &d.j_lim); dfree(w, &d.j_par);
+    dfree(w, &d.j_imp); dfree(w, &d.j_imp2); dfree(w, &d.j_rr); dfree(w, &d.j_k); dfree(w, &d.j_m); dfree(w, &d.j_s);
+    dfree(w, &d.j_x); dfree(w, &d.j_order); dfree(w, &d.j_coff); dfree(w, &d.b_jnt);
+    int rc = B2G_OK;
+    if ((rc = dalloc(w, &d.j_body, cap)) || (rc = dalloc(w, &d.j_body2, cap)) || (rc = dalloc(w, &d.j_anchor, cap)) ||
+        (rc = dalloc(w, &d.j_lim, cap)) || (rc = dalloc(w, &d.j_par, cap)) || (rc = dalloc(w, &d.j_imp, cap)) ||
+        (rc = dalloc(w, &d.j_imp2, cap)) || (rc = dalloc(w, &d.j_rr, cap)) || (rc = dalloc(w, &d.j_k, cap)) ||
+        (rc = dalloc(w, &d.j_m, cap)) || (rc = dalloc(w, &d.j_s, cap)) || (rc = dalloc(w, &d.j_x, cap)) ||
+        (rc = dalloc(w, &d.j_order, cap)) || (rc = dalloc(w, &d.j_coff, kMaxJointColours + 1)) ||
+        (rc = dalloc(w, &d.b_jnt, 2 * (size_t)cap)))
+        return rc;
+    w->joint_cap = cap;
+    drop_graphs(w);
+    ++w->alloc_generation;
+    return B2G_OK;
+}
+
 /* Uploads the joints: definitions, impulses, the colouring (greedy, in creation order: a joint takes
  * the first colour no earlier joint on one of its dynamic bodies has, so joints of a colour share no
  * body the solver writes) and body -> joints. */
@@ -735,20 +771,8 @@ int upload_joints(World* w) {
     const int nb = (int)w->h_flags.size();
     cudaStream_t s = w->stream;
     if (nj > w->joint_cap) {
-        dfree(w, &d.j_body); dfree(w, &d.j_anchor); dfree(w, &d.j_lim); dfree(w, &d.j_par); dfree(w, &d.j_imp);
-        dfree(w, &d.j_imp2); dfree(w, &d.j_rr); dfree(w, &d.j_k); dfree(w, &d.j_m); dfree(w, &d.j_s); dfree(w, &d.j_x);
-        dfree(w, &d.j_order); dfree(w, &d.j_coff); dfree(w, &d.b_jnt);
-        int rc = B2G_OK;
-        const int cap = nj;
-        if ((rc = dalloc(w, &d.j_body, cap)) || (rc = dalloc(w, &d.j_anchor, cap)) || (rc = dalloc(w, &d.j_lim, cap)) ||
-            (rc = dalloc(w, &d.j_par, cap)) || (rc = dalloc(w, &d.j_imp, cap)) || (rc = dalloc(w, &d.j_imp2, cap)) ||
-            (rc = dalloc(w, &d.j_rr, cap)) || (rc = dalloc(w, &d.j_k, cap)) || (rc = dalloc(w, &d.j_m, cap)) ||
-            (rc = dalloc(w, &d.j_s, cap)) || (rc = dalloc(w, &d.j_x, cap)) || (rc = dalloc(w, &d.j_order, cap)) ||
-            (rc = dalloc(w, &d.j_coff, kMaxJointColours + 1)) || (rc = dalloc(w, &d.b_jnt, 2 * (size_t)cap)))
-            return rc;
-        w->joint_cap = cap;
-        drop_graphs(w);
-        ++w->alloc_generation;
+        const int rc = alloc_joint_arrays(w, nj);
+        if (rc != B2G_OK) return rc;
     }
     std::vector<int> colour(nj, 0);
     std::vector<uint64_t> used(nb, 0);
@@ -757,15 +781,23 @@ int upload_joints(World* w) {
     for (int j = 0; j < nj; ++j) {
         if (w->h_jdead[j]) continue;  /* a destroyed joint is in no colour */
         ++nlive;
-        const uint32_t a = w->joints[j].body_a, b = w->joints[j].body_b;
-        const bool da = (w->h_flags[a] & BF_TYPE_MASK) == BODY_DYNAMIC, db = (w->h_flags[b] & BF_TYPE_MASK) == BODY_DYNAMIC;
-        const uint64_t busy = (da ? used[a] : 0ull) | (db ? used[b] : 0ull);
+        /* the bodies the joint writes: A and B, and a gear joint's C and D */
+        uint32_t jb[4] = {w->joints[j].body_a, w->joints[j].body_b, 0u, 0u};
+        int nbj = 2;
+        if (w->joints[j].type == B2G_JOINT_GEAR) {
+            jb[2] = (uint32_t)w->gear[j].body_c;
+            jb[3] = (uint32_t)w->gear[j].body_d;
+            nbj = 4;
+        }
+        uint64_t busy = 0;
+        for (int k = 0; k < nbj; ++k)
+            if ((w->h_flags[jb[k]] & BF_TYPE_MASK) == BODY_DYNAMIC) busy |= used[jb[k]];
         int c = 0;
         while (c < kMaxJointColours && (busy >> c) & 1ull) ++c;
         if (c == kMaxJointColours) return fail(w, B2G_ERR_CAPACITY, "a body has more joints than the joint colouring holds (64)");
         colour[j] = c;
-        if (da) used[a] |= 1ull << c;
-        if (db) used[b] |= 1ull << c;
+        for (int k = 0; k < nbj; ++k)
+            if ((w->h_flags[jb[k]] & BF_TYPE_MASK) == BODY_DYNAMIC) used[jb[k]] |= 1ull << c;
         ncol = std::max(ncol, c + 1);
     }
     w->h_jcoff.assign(kMaxJointColours + 1, 0);
@@ -797,14 +829,29 @@ int upload_joints(World* w) {
 #define U(dst, src, n) CUDA_OK(w, cudaMemcpyAsync((dst), (src), (size_t)(n) * sizeof(*(dst)), cudaMemcpyHostToDevice, s))
     U(d.b_jnt_off, w->h_jnt_off.data(), nb + 1);
     if (nj > 0) {
-        std::vector<int2> jb(nj);
-        std::vector<float4> an(nj), lim(nj), par(nj);
+        std::vector<int2> jb(nj), jb2(nj);
+        std::vector<float4> an(nj), lim(nj), par(nj), jx(nj);
+        std::vector<float2> js(nj);
         for (int j = 0; j < nj; ++j) {
             const b2g_joint_def& jd = w->joints[j];
             /* a destroyed joint joins no islands: its body pair is (a, a) */
             jb[j] = w->h_jdead[j] ? make_int2((int)jd.body_a, (int)jd.body_a) : make_int2((int)jd.body_a, (int)jd.body_b);
+            jb2[j] = jb[j];
+            jx[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            js[j] = make_float2(0.0f, 0.0f);
             an[j] = make_float4(jd.local_anchor_a.x, jd.local_anchor_a.y, jd.local_anchor_b.x, jd.local_anchor_b.y);
             uint32_t fl = ((uint32_t)jd.type << JF_TYPE_SHIFT) | (jd.collide_connected ? JF_COLLIDE : 0u);
+            if (jd.type == B2G_JOINT_GEAR) {
+                const GearFrame& g = w->gear[j];
+                jb2[j] = make_int2(g.body_c, g.body_d);
+                an[j] = make_float4(g.anchor_a.x, g.anchor_a.y, g.anchor_b.x, g.anchor_b.y);
+                lim[j] = make_float4(g.anchor_c.x, g.anchor_c.y, g.anchor_d.x, g.anchor_d.y);
+                jx[j] = make_float4(g.axis_c.x, g.axis_c.y, g.axis_d.x, g.axis_d.y);
+                js[j] = make_float2(g.ref_a, g.ref_b);
+                fl |= (g.prismatic_a ? JF_GEAR_A_PRISMATIC : 0u) | (g.prismatic_b ? JF_GEAR_B_PRISMATIC : 0u);
+                par[j] = make_float4(jd.ratio, __uint_as_float_host(fl), g.constant, 0.0f);
+                continue;
+            }
             if (jd.type == B2G_JOINT_PULLEY) {
                 /* the constant length_a + ratio * length_b (b2_pulley_joint.rs:33) is formed on the device */
                 lim[j] = make_float4(jd.ground_anchor_a.x, jd.ground_anchor_a.y, jd.ground_anchor_b.x, jd.ground_anchor_b.y);
@@ -848,6 +895,9 @@ int upload_joints(World* w) {
             }
         }
         U(d.j_body, jb.data(), nj);
+        U(d.j_body2, jb2.data(), nj);
+        U(d.j_x, jx.data(), nj);
+        U(d.j_s, js.data(), nj);
         U(d.j_anchor, an.data(), nj);
         U(d.j_lim, lim.data(), nj);
         U(d.j_par, par.data(), nj);
@@ -911,16 +961,17 @@ int prepare(World* w) {
         if (rc != B2G_OK) return rc;
         if (n_contacts > 0) {
             Contacts& c = w->d.c;
-            cudaMemcpy(c.key, key.data(), n_contacts * sizeof(uint64_t), cudaMemcpyHostToDevice);
-            cudaMemcpy(c.fix, fix.data(), n_contacts * sizeof(int2), cudaMemcpyHostToDevice);
-            cudaMemcpy(c.body, body.data(), n_contacts * sizeof(int2), cudaMemcpyHostToDevice);
-            cudaMemcpy(c.flags, flags.data(), n_contacts * sizeof(uint32_t), cudaMemcpyHostToDevice);
-            cudaMemcpy(c.mat, mat.data(), n_contacts * sizeof(float4), cudaMemcpyHostToDevice);
-            cudaMemcpy(c.mgeo, mgeo.data(), n_contacts * sizeof(float4), cudaMemcpyHostToDevice);
-            cudaMemcpy(c.mpts, mpts.data(), n_contacts * sizeof(float4), cudaMemcpyHostToDevice);
-            cudaMemcpy(c.mimp, mimp.data(), n_contacts * sizeof(float4), cudaMemcpyHostToDevice);
-            CUDA_OK(w, cudaMemcpy(c.mids, mids.data(), n_contacts * sizeof(uint4), cudaMemcpyHostToDevice));
-            CUDA_OK(w, cudaMemcpy(w->d.cnt + CNT_CONTACTS, &n_contacts, sizeof(int), cudaMemcpyHostToDevice));
+            cudaMemcpyAsync(c.key, key.data(), n_contacts * sizeof(uint64_t), cudaMemcpyHostToDevice, w->stream);
+            cudaMemcpyAsync(c.fix, fix.data(), n_contacts * sizeof(int2), cudaMemcpyHostToDevice, w->stream);
+            cudaMemcpyAsync(c.body, body.data(), n_contacts * sizeof(int2), cudaMemcpyHostToDevice, w->stream);
+            cudaMemcpyAsync(c.flags, flags.data(), n_contacts * sizeof(uint32_t), cudaMemcpyHostToDevice, w->stream);
+            cudaMemcpyAsync(c.mat, mat.data(), n_contacts * sizeof(float4), cudaMemcpyHostToDevice, w->stream);
+            cudaMemcpyAsync(c.mgeo, mgeo.data(), n_contacts * sizeof(float4), cudaMemcpyHostToDevice, w->stream);
+            cudaMemcpyAsync(c.mpts, mpts.data(), n_contacts * sizeof(float4), cudaMemcpyHostToDevice, w->stream);
+            cudaMemcpyAsync(c.mimp, mimp.data(), n_contacts * sizeof(float4), cudaMemcpyHostToDevice, w->stream);
+            CUDA_OK(w, cudaMemcpyAsync(c.mids, mids.data(), n_contacts * sizeof(uint4), cudaMemcpyHostToDevice, w->stream));
+            CUDA_OK(w, cudaMemcpyAsync(w->d.cnt + CNT_CONTACTS, &n_contacts, sizeof(int), cudaMemcpyHostToDevice, w->stream));
+            CUDA_OK(w, cudaStreamSynchronize(w->stream));
         }
         w->d.key_bits = old_key_bits;
     } else if (!w->allocated) {
@@ -939,7 +990,7 @@ int prepare(World* w) {
                 CUDA_OK(w, cudaMemcpy(key.data(), w->d.c.key, n_contacts * sizeof(uint64_t), cudaMemcpyDeviceToHost));
                 const uint64_t mask = (1ull << w->d.key_bits) - 1;
                 for (unsigned long long& k : key) k = ((k >> w->d.key_bits) << kb) | (k & mask);
-                CUDA_OK(w, cudaMemcpy(w->d.c.key, key.data(), n_contacts * sizeof(uint64_t), cudaMemcpyHostToDevice));
+                CUDA_OK(w, cudaMemcpyAsync(w->d.c.key, key.data(), n_contacts * sizeof(uint64_t), cudaMemcpyHostToDevice, w->stream));
             }
         }
         w->d.key_bits = kb;
@@ -1028,11 +1079,11 @@ int check_status(World* w) {
 int status_error(World* w, int status) {
     if (status == 0) return B2G_OK;
     const int zero = 0;
-    cudaMemcpy(w->d.cnt + CNT_STATUS, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(w->d.cnt + CNT_STATUS, &zero, sizeof(int), cudaMemcpyHostToDevice, w->stream);
     if (status & ST_BARRIER_TIMEOUT) {
         /* the barrier counters may be left mid-count: reset them */
         const int z2[2] = {0, 0};
-        cudaMemcpy(w->d.cnt + CNT_BARRIER, z2, sizeof(z2), cudaMemcpyHostToDevice);
+        cudaMemcpyAsync(w->d.cnt + CNT_BARRIER, z2, sizeof(z2), cudaMemcpyHostToDevice, w->stream);
         return fail(w, B2G_ERR_TIMEOUT, "a grid barrier wait timed out; the step's results are void");
     }
     if (status & (ST_CONTACT_OVERFLOW | ST_PAIR_OVERFLOW | ST_STACK_OVERFLOW | ST_COLOUR_OVERFLOW)) {
@@ -1119,7 +1170,7 @@ int hook_before_collide(World* w, HostContacts& old) {
         }
     }
     if (changed && old.n > 0)
-        CUDA_OK(w, cudaMemcpy(w->d.c.flags, old.flags.data(), old.n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        CUDA_OK(w, cudaMemcpyAsync(w->d.c.flags, old.flags.data(), old.n * sizeof(uint32_t), cudaMemcpyHostToDevice, w->stream));
     return B2G_OK;
 }
 
@@ -1151,8 +1202,8 @@ int hook_pre_solve(World* w, const HostContacts& old) {
         }
     }
     if (changed) {
-        CUDA_OK(w, cudaMemcpy(w->d.c.flags, now.flags.data(), now.n * sizeof(uint32_t), cudaMemcpyHostToDevice));
-        CUDA_OK(w, cudaMemcpy(w->d.c.mat, now.mat.data(), now.n * sizeof(float4), cudaMemcpyHostToDevice));
+        CUDA_OK(w, cudaMemcpyAsync(w->d.c.flags, now.flags.data(), now.n * sizeof(uint32_t), cudaMemcpyHostToDevice, w->stream));
+        CUDA_OK(w, cudaMemcpyAsync(w->d.c.mat, now.mat.data(), now.n * sizeof(float4), cudaMemcpyHostToDevice, w->stream));
     }
     return B2G_OK;
 }
@@ -1183,11 +1234,11 @@ int hook_new_pairs(World* w) {
     std::vector<uint32_t> idx(std::max(m, 1));
     for (int i = 0; i < m; ++i) idx[i] = (uint32_t)i;
     if (m > 0) {
-        CUDA_OK(w, cudaMemcpy(w->d.n_key, key.data(), m * sizeof(unsigned long long), cudaMemcpyHostToDevice));
-        CUDA_OK(w, cudaMemcpy(w->d.n_fix, fix.data(), m * sizeof(int2), cudaMemcpyHostToDevice));
-        CUDA_OK(w, cudaMemcpy(w->d.n_idx, idx.data(), m * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        CUDA_OK(w, cudaMemcpyAsync(w->d.n_key, key.data(), m * sizeof(unsigned long long), cudaMemcpyHostToDevice, w->stream));
+        CUDA_OK(w, cudaMemcpyAsync(w->d.n_fix, fix.data(), m * sizeof(int2), cudaMemcpyHostToDevice, w->stream));
+        CUDA_OK(w, cudaMemcpyAsync(w->d.n_idx, idx.data(), m * sizeof(uint32_t), cudaMemcpyHostToDevice, w->stream));
     }
-    CUDA_OK(w, cudaMemcpy(w->d.cnt + CNT_NEW, &m, sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_OK(w, cudaMemcpyAsync(w->d.cnt + CNT_NEW, &m, sizeof(int), cudaMemcpyHostToDevice, w->stream));
     return B2G_OK;
 }
 
@@ -1630,6 +1681,49 @@ int b2g_create_fixtures(void* p, const b2g_fixture_def* defs, int32_t n, uint32_
     return B2G_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+/* one side of B2gearJoint::new (b2_gear_joint.rs:62-82 / :91-111): the joint's local anchors, axis,
+ * reference angle and the side's coordinate on the bodies' current transforms */
+void gear_side(World* w, const b2g_joint_def& jd, V2& anchor_first, V2& anchor_second, V2& axis, float& ref,
+               bool& prismatic, float& coordinate) {
+    const int first = (int)jd.body_a, second = (int)jd.body_b;
+    anchor_first = mk(jd.local_anchor_a.x, jd.local_anchor_a.y);
+    anchor_second = mk(jd.local_anchor_b.x, jd.local_anchor_b.y);
+    ref = jd.reference_angle;
+    prismatic = jd.type == B2G_JOINT_PRISMATIC;
+    const Xf xf_second = host_xf(w, second), xf_first = host_xf(w, first);
+    if (!prismatic) {
+        axis = mk(0.0f, 0.0f);
+        coordinate = w->h_pos[second].z - w->h_pos[first].z - ref;
+        return;
+    }
+    /* the prismatic joint's unit axis (B2prismaticJoint::new, b2_prismatic_joint.rs:54-60) */
+    axis = mk(jd.local_axis_a.x, jd.local_axis_a.y);
+    normalize(axis);
+    const V2 p_second = mul_t(xf_first.q, add(mul(xf_second.q, anchor_second), sub(xf_second.p, xf_first.p)));
+    coordinate = dot(sub(p_second, anchor_first), axis);
+}
+
+GearFrame gear_frame(World* w, const b2g_joint_def& d) {
+    GearFrame g;
+    const b2g_joint_def& j1 = w->joints[d.joint1];
+    const b2g_joint_def& j2 = w->joints[d.joint2];
+    float coordinate_a = 0.0f, coordinate_b = 0.0f;
+    g.body_c = (int)j1.body_a;
+    g.body_d = (int)j2.body_a;
+    gear_side(w, j1, g.anchor_c, g.anchor_a, g.axis_c, g.ref_a, g.prismatic_a, coordinate_a);
+    gear_side(w, j2, g.anchor_d, g.anchor_b, g.axis_d, g.ref_b, g.prismatic_b, coordinate_b);
+    g.constant = coordinate_a + d.ratio * coordinate_b;
+    return g;
+}
+
+}  // namespace
+
+extern "C" {
+
 int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* ids) {
     World* w = W(p);
     if (!w || (!defs && n > 0) || n < 0) return B2G_ERR_INVALID_ARG;
@@ -1637,11 +1731,29 @@ int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* i
         const b2g_joint_def& d = defs[i];
         if (d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE && d.type != B2G_JOINT_WELD &&
             d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR && d.type != B2G_JOINT_MOUSE &&
-            d.type != B2G_JOINT_PRISMATIC && d.type != B2G_JOINT_WHEEL && d.type != B2G_JOINT_PULLEY)
-            return fail(w, B2G_ERR_UNSUPPORTED, "the gear joint is not on the GPU path");
+            d.type != B2G_JOINT_PRISMATIC && d.type != B2G_JOINT_WHEEL && d.type != B2G_JOINT_PULLEY &&
+            d.type != B2G_JOINT_GEAR)
+            return fail(w, B2G_ERR_UNSUPPORTED, "unknown joint type");
         if (d.body_a >= w->h_flags.size() || d.body_b >= w->h_flags.size() || d.body_a == d.body_b)
             return fail(w, B2G_ERR_INVALID_ARG, "joint body ids out of range or equal");
         if (w->h_bdead[d.body_a] || w->h_bdead[d.body_b]) return fail(w, B2G_ERR_INVALID_ARG, "a joint body was destroyed");
+        if (d.type == B2G_JOINT_GEAR) {
+            /* B2gearJoint::new asserts (b2_gear_joint.rs:29-60, 83-87): two revolute or prismatic joints made
+             * earlier; the gear's bodies are their second bodies, which must be dynamic */
+            const size_t made = w->joints.size() + (size_t)i;
+            if (d.joint1 >= made || d.joint2 >= made || (d.joint1 < w->joints.size() && w->h_jdead[d.joint1]) ||
+                (d.joint2 < w->joints.size() && w->h_jdead[d.joint2]))
+                return fail(w, B2G_ERR_INVALID_ARG, "a gear joint's joints must exist before it");
+            const b2g_joint_def& j1 = d.joint1 < w->joints.size() ? w->joints[d.joint1] : defs[d.joint1 - w->joints.size()];
+            const b2g_joint_def& j2 = d.joint2 < w->joints.size() ? w->joints[d.joint2] : defs[d.joint2 - w->joints.size()];
+            if ((j1.type != B2G_JOINT_REVOLUTE && j1.type != B2G_JOINT_PRISMATIC) ||
+                (j2.type != B2G_JOINT_REVOLUTE && j2.type != B2G_JOINT_PRISMATIC))
+                return fail(w, B2G_ERR_INVALID_ARG, "a gear joint couples revolute or prismatic joints");
+            if (d.body_a != j1.body_b || d.body_b != j2.body_b)
+                return fail(w, B2G_ERR_INVALID_ARG, "a gear joint's body_a / body_b must be its joints' body_b");
+            if ((w->h_flags[j1.body_b] & BF_TYPE_MASK) != BODY_DYNAMIC || (w->h_flags[j2.body_b] & BF_TYPE_MASK) != BODY_DYNAMIC)
+                return fail(w, B2G_ERR_INVALID_ARG, "a gear joint's joints must have a dynamic body_b");
+        }
         /* B2pulleyJointDef::initialize asserts ratio > B2_EPSILON (src/joints/b2_pulley_joint.rs:81) and
          * the joint's constructor ratio != 0 (private/dynamics/joints/b2_pulley_joint.rs:30) */
         if (d.type == B2G_JOINT_PULLEY && !(d.ratio > FLT_EPSILON))
@@ -1652,13 +1764,16 @@ int b2g_create_joints(void* p, const b2g_joint_def* defs, int32_t n, uint32_t* i
         int rc = download_joint_impulses(w);
         if (rc != B2G_OK) return rc;
         for (int i = 0; i < n && rc == B2G_OK; ++i)
-            if (defs[i].type == B2G_JOINT_MOUSE) rc = download_state(w);  /* body B's transform */
+            if (defs[i].type == B2G_JOINT_MOUSE || defs[i].type == B2G_JOINT_GEAR)
+                rc = download_state(w);  /* the bodies' transforms */
         if (rc != B2G_OK) return rc;
     }
     for (int i = 0; i < n; ++i) {
         if (ids) ids[i] = (uint32_t)w->joints.size();
         w->joints.push_back(defs[i]);
         w->h_jdead.push_back(0);
+        w->gear.emplace_back();
+        if (defs[i].type == B2G_JOINT_GEAR) w->gear.back() = gear_frame(w, defs[i]);
         if (defs[i].type == B2G_JOINT_MOUSE) {
             /* b2_mouse_joint_new (src/joints/b2_mouse_joint.rs:140-160): the target in body B's frame */
             const V2 la = mul_t(host_xf(w, (int)defs[i].body_b), mk(defs[i].target.x, defs[i].target.y));
@@ -1722,7 +1837,7 @@ int begin_host_edit(World* w, const std::vector<uint8_t>* fix_mark, const std::v
             w->pending_events.resize(k + (size_t)(n_events1 - n_events0));
             CUDA_OK(w, cudaMemcpy(w->pending_events.data() + k, w->d.events + n_events0,
                                   (size_t)(n_events1 - n_events0) * sizeof(int4), cudaMemcpyDeviceToHost));
-            CUDA_OK(w, cudaMemcpy(w->d.cnt + CNT_EVENTS, &n_events0, sizeof(int), cudaMemcpyHostToDevice));
+            CUDA_OK(w, cudaMemcpyAsync(w->d.cnt + CNT_EVENTS, &n_events0, sizeof(int), cudaMemcpyHostToDevice, w->stream));
         }
         int status = 0;
         CUDA_OK(w, cudaMemcpy(&status, w->d.cnt + CNT_STATUS, sizeof(int), cudaMemcpyDeviceToHost));
@@ -2460,6 +2575,7 @@ std::vector<unsigned char> host_state(const World* w) {
     put(&nj, sizeof(nj));
     put(w->joints.data(), (size_t)nj * sizeof(b2g_joint_def));
     put(w->h_jdead.data(), (size_t)nj);
+    put(w->gear.data(), (size_t)nj * sizeof(GearFrame));
     put(&nfree, sizeof(nfree));
     put(w->free_refids.data(), (size_t)nfree * sizeof(uint32_t));
     put(&w->next_node, sizeof(w->next_node));
@@ -2486,7 +2602,8 @@ int load_host_state(World* w, const unsigned char* src, const unsigned char* end
     if (!get(&nf, sizeof(nf)) || nf != (int32_t)w->h_fbody.size()) return fail(w, B2G_ERR_INVALID_ARG, "state fixture count");
     if (!get(w->h_fdead.data(), (size_t)nf)) return fail(w, B2G_ERR_INVALID_ARG, "truncated state");
     if (!get(&nj, sizeof(nj)) || nj != (int32_t)w->joints.size()) return fail(w, B2G_ERR_INVALID_ARG, "state joint count");
-    if (!get(w->joints.data(), (size_t)nj * sizeof(b2g_joint_def)) || !get(w->h_jdead.data(), (size_t)nj))
+    if (!get(w->joints.data(), (size_t)nj * sizeof(b2g_joint_def)) || !get(w->h_jdead.data(), (size_t)nj) ||
+        !get(w->gear.data(), (size_t)nj * sizeof(GearFrame)))
         return fail(w, B2G_ERR_INVALID_ARG, "truncated state");
     if (!get(&nfree, sizeof(nfree)) || nfree < 0) return fail(w, B2G_ERR_INVALID_ARG, "truncated state");
     w->free_refids.resize((size_t)nfree);
@@ -2621,9 +2738,10 @@ int b2g_state_load(void* p, const void* in, uint64_t bytes) {
     src += (size_t)h.n_alloc * sizeof(uint64_t);
     for (size_t i = 0; i < w->allocations.size(); ++i) {
         if ((size_t)(end - src) < w->alloc_bytes[i]) return fail(w, B2G_ERR_INVALID_ARG, "truncated state");
-        CUDA_OK(w, cudaMemcpy(w->allocations[i], src, w->alloc_bytes[i], cudaMemcpyHostToDevice));
+        CUDA_OK(w, cudaMemcpyAsync(w->allocations[i], src, w->alloc_bytes[i], cudaMemcpyHostToDevice, w->stream));
         src += w->alloc_bytes[i];
     }
+    CUDA_OK(w, cudaStreamSynchronize(w->stream));
     /* the contact table is the buffer that was current when saved */
     if ((w->swaps & 1) != h.swaps_parity) swap_contacts(w);
     w->d.key_bits = h.key_bits;

@@ -56,6 +56,8 @@ enum : uint32_t {
     JF_MOTOR = 1u << 1,
     JF_COLLIDE = 1u << 2,  /* collide_connected */
     JF_TYPE_SHIFT = 8,     /* the joint type (B2G_JOINT_*) sits in bits 8-15 */
+    JF_GEAR_A_PRISMATIC = 1u << 16,  /* a gear joint's first joint is prismatic (else revolute) */
+    JF_GEAR_B_PRISMATIC = 1u << 17,  /* its second joint is prismatic */
 };
 
 /* device status bits (sticky until read by the host) */
@@ -266,6 +268,7 @@ struct DevWorld {
      * joints sorted by colour (j_order, j_coff: n_jcolours + 1 offsets) and body -> joints */
     int n_joints, n_jcolours;
     int2* j_body;
+    int2* j_body2;               /* a gear joint's bodies C and D (the first bodies of its two joints) */
     float4 *j_anchor, *j_lim, *j_par, *j_imp, *j_imp2, *j_rr, *j_k, *j_m, *j_x;
     float2* j_s;
     int *j_order, *j_coff;

@@ -1,5 +1,8 @@
 /*
- * b2g_joint.cuh — the revolute and distance joints on the device. The revolute joint (B2revoluteJoint,
+ * b2g_joint.cuh — the joints on the device: revolute, prismatic, wheel, pulley, distance, weld,
+ * friction, motor, mouse and gear, each a restatement of its reference file's
+ * init_velocity_constraints / solve_velocity_constraints / solve_position_constraints in the same
+ * sequence of IEEE f32 operations (built without fused multiply-add). The revolute joint (B2revoluteJoint,
  * private/dynamics/joints/b2_revolute_joint.rs:21-287): init_velocity_constraints (anchors,
  * effective masses, warm start), solve_velocity_constraints (motor, lower and upper limits, the
  * point constraint) and solve_position_constraints (angular limit, then the point), each the
@@ -1307,6 +1310,179 @@ __device__ bool pulley_solve_position(const DevWorld& w, int j) {
     return linear_error < kLinearSlop;
 }
 
+/* ---- gear joint (B2gearJoint, private/dynamics/joints/b2_gear_joint.rs) ----
+ * Couples two revolute or prismatic joints: A and B are the second bodies of joint 1 and joint 2, C and
+ * D their first bodies (grounds, usually). j_body = (A, B), j_body2 = (C, D), j_anchor = (local anchor
+ * A, local anchor B), j_lim = (local anchor C, local anchor D), j_x = (local axis C, local axis D; zero
+ * for a revolute side), j_s = (reference angle A, reference angle B), j_par = (ratio, flags, constant,
+ * -) with JF_GEAR_A_PRISMATIC / JF_GEAR_B_PRISMATIC; j_imp.x = impulse. The step's temporaries: j_rr =
+ * (jv_ac, jv_bd), j_k = (jw_a, jw_b, jw_c, jw_d), j_m.x = effective mass. */
+
+struct GearJacobian {
+    V2 jv_ac, jv_bd;
+    float jw_a, jw_b, jw_c, jw_d, mass;
+};
+
+/* the Jacobian rows and the (not yet inverted) mass sum of :209-241 and :326-359, from the bodies'
+ * rotations; mA..mD are the bodies' (m, 1/m, I, 1/I) */
+__device__ __forceinline__ GearJacobian gear_jacobian(const DevWorld& w, int j, const Rot& qA, const Rot& qB,
+                                                      const Rot& qC, const Rot& qD, const float4& mA,
+                                                      const float4& mB, const float4& mC, const float4& mD) {
+    const int2 ab = w.j_body[j], cd = w.j_body2[j];
+    const float4 an = w.j_anchor[j], an2 = w.j_lim[j], ax = w.j_x[j], par = w.j_par[j];
+    const uint32_t fl = __float_as_uint(par.y);
+    const float ratio = par.x;
+    GearJacobian g;
+    g.mass = 0.0f;
+    if (!(fl & JF_GEAR_A_PRISMATIC)) {
+        g.jv_ac = mk(0.0f, 0.0f);
+        g.jw_a = 1.0f;
+        g.jw_c = 1.0f;
+        g.mass += mA.w + mC.w;
+    } else {
+        const float2 lcA = w.b_lc[ab.x], lcC = w.b_lc[cd.x];
+        const V2 u = mul(qC, mk(ax.x, ax.y));
+        const V2 rC = mul(qC, sub(mk(an2.x, an2.y), mk(lcC.x, lcC.y)));
+        const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+        g.jv_ac = u;
+        g.jw_c = cross(rC, u);
+        g.jw_a = cross(rA, u);
+        g.mass += mC.y + mA.y + mC.w * g.jw_c * g.jw_c + mA.w * g.jw_a * g.jw_a;
+    }
+    if (!(fl & JF_GEAR_B_PRISMATIC)) {
+        g.jv_bd = mk(0.0f, 0.0f);
+        g.jw_b = ratio;
+        g.jw_d = ratio;
+        g.mass += ratio * ratio * (mB.w + mD.w);
+    } else {
+        const float2 lcB = w.b_lc[ab.y], lcD = w.b_lc[cd.y];
+        const V2 u = mul(qD, mk(ax.z, ax.w));
+        const V2 rD = mul(qD, sub(mk(an2.z, an2.w), mk(lcD.x, lcD.y)));
+        const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+        g.jv_bd = scale(ratio, u);
+        g.jw_d = ratio * cross(rD, u);
+        g.jw_b = ratio * cross(rB, u);
+        g.mass += ratio * ratio * (mD.y + mB.y) + mD.w * g.jw_d * g.jw_d + mB.w * g.jw_b * g.jw_b;
+    }
+    return g;
+}
+
+/* the four bodies' velocities changed by the gear impulse (:264-273, :300-307): all four are read, then
+ * written back in the order A, B, C, D, so a body that is both A and D keeps D's result, as in the
+ * reference */
+__device__ __forceinline__ void gear_apply(const DevWorld& w, int j, const GearJacobian& g, float impulse,
+                                           const float4& mA, const float4& mB, const float4& mC, const float4& mD) {
+    const int2 ab = w.j_body[j], cd = w.j_body2[j];
+    const float4 va = w.b_vel[ab.x], vb = w.b_vel[ab.y], vc = w.b_vel[cd.x], vd = w.b_vel[cd.y];
+    V2 vA = mk(va.x, va.y), vB = mk(vb.x, vb.y), vC = mk(vc.x, vc.y), vD = mk(vd.x, vd.y);
+    float wA = va.z, wB = vb.z, wC = vc.z, wD = vd.z;
+    vA = add(vA, scale(mA.y * impulse, g.jv_ac));
+    wA += mA.w * impulse * g.jw_a;
+    vB = add(vB, scale(mB.y * impulse, g.jv_bd));
+    wB += mB.w * impulse * g.jw_b;
+    vC = sub(vC, scale(mC.y * impulse, g.jv_ac));
+    wC -= mC.w * impulse * g.jw_c;
+    vD = sub(vD, scale(mD.y * impulse, g.jv_bd));
+    wD -= mD.w * impulse * g.jw_d;
+    if (joint_body_dynamic(w, ab.x)) w.b_vel[ab.x] = make_float4(vA.x, vA.y, wA, va.w);
+    if (joint_body_dynamic(w, ab.y)) w.b_vel[ab.y] = make_float4(vB.x, vB.y, wB, vb.w);
+    if (joint_body_dynamic(w, cd.x)) w.b_vel[cd.x] = make_float4(vC.x, vC.y, wC, vc.w);
+    if (joint_body_dynamic(w, cd.y)) w.b_vel[cd.y] = make_float4(vD.x, vD.y, wD, vd.w);
+}
+
+/* init_velocity_constraints, :190-289 */
+__device__ void gear_init_velocity(const DevWorld& w, const StepParams& sp, int j) {
+    const int2 ab = w.j_body[j], cd = w.j_body2[j];
+    const float4 mA = w.b_mass[ab.x], mB = w.b_mass[ab.y], mC = w.b_mass[cd.x], mD = w.b_mass[cd.y];
+    const Rot qA = rot(w.b_pos[ab.x].z), qB = rot(w.b_pos[ab.y].z), qC = rot(w.b_pos[cd.x].z),
+              qD = rot(w.b_pos[cd.y].z);
+    GearJacobian g = gear_jacobian(w, j, qA, qB, qC, qD, mA, mB, mC, mD);
+    g.mass = g.mass > 0.0f ? fdiv(1.0f, g.mass) : 0.0f;
+    w.j_rr[j] = make_float4(g.jv_ac.x, g.jv_ac.y, g.jv_bd.x, g.jv_bd.y);
+    w.j_k[j] = make_float4(g.jw_a, g.jw_b, g.jw_c, g.jw_d);
+    w.j_m[j] = make_float4(g.mass, 0.0f, 0.0f, 0.0f);
+    float4 imp = w.j_imp[j];
+    if (sp.warm) {
+        gear_apply(w, j, g, imp.x, mA, mB, mC, mD);  /* the stored impulse, not scaled by dt_ratio (:264) */
+    } else {
+        imp.x = 0.0f;
+        w.j_imp[j] = imp;
+    }
+}
+
+/* solve_velocity_constraints, :291-319 */
+__device__ void gear_solve_velocity(const DevWorld& w, int j) {
+    const int2 ab = w.j_body[j], cd = w.j_body2[j];
+    const float4 mA = w.b_mass[ab.x], mB = w.b_mass[ab.y], mC = w.b_mass[cd.x], mD = w.b_mass[cd.y];
+    const float4 rr = w.j_rr[j], kk = w.j_k[j];
+    GearJacobian g;
+    g.jv_ac = mk(rr.x, rr.y);
+    g.jv_bd = mk(rr.z, rr.w);
+    g.jw_a = kk.x;
+    g.jw_b = kk.y;
+    g.jw_c = kk.z;
+    g.jw_d = kk.w;
+    g.mass = w.j_m[j].x;
+    const float4 va = w.b_vel[ab.x], vb = w.b_vel[ab.y], vc = w.b_vel[cd.x], vd = w.b_vel[cd.y];
+    float cdot = dot(g.jv_ac, sub(mk(va.x, va.y), mk(vc.x, vc.y))) + dot(g.jv_bd, sub(mk(vb.x, vb.y), mk(vd.x, vd.y)));
+    cdot += (g.jw_a * va.z - g.jw_c * vc.z) + (g.jw_b * vb.z - g.jw_d * vd.z);
+    const float impulse = -g.mass * cdot;
+    float4 imp = w.j_imp[j];
+    imp.x += impulse;
+    w.j_imp[j] = imp;
+    gear_apply(w, j, g, impulse, mA, mB, mC, mD);
+}
+
+/* solve_position_constraints, :321-393 (the linear error is never measured: the joint always reports
+ * itself solved) */
+__device__ bool gear_solve_position(const DevWorld& w, int j) {
+    const int2 ab = w.j_body[j], cd = w.j_body2[j];
+    const float4 mA = w.b_mass[ab.x], mB = w.b_mass[ab.y], mC = w.b_mass[cd.x], mD = w.b_mass[cd.y];
+    const float4 pa = w.b_pos[ab.x], pb = w.b_pos[ab.y], pc = w.b_pos[cd.x], pd = w.b_pos[cd.y];
+    V2 cA = mk(pa.x, pa.y), cB = mk(pb.x, pb.y), cC = mk(pc.x, pc.y), cD = mk(pd.x, pd.y);
+    float aA = pa.z, aB = pb.z, aC = pc.z, aD = pd.z;
+    const Rot qA = rot(aA), qB = rot(aB), qC = rot(aC), qD = rot(aD);
+    const GearJacobian g = gear_jacobian(w, j, qA, qB, qC, qD, mA, mB, mC, mD);
+    const float4 an = w.j_anchor[j], an2 = w.j_lim[j], ax = w.j_x[j], par = w.j_par[j];
+    const float2 ref = w.j_s[j];
+    const uint32_t fl = __float_as_uint(par.y);
+    float coordinate_a, coordinate_b;
+    if (!(fl & JF_GEAR_A_PRISMATIC)) {
+        coordinate_a = aA - aC - ref.x;
+    } else {
+        const float2 lcA = w.b_lc[ab.x], lcC = w.b_lc[cd.x];
+        const V2 rA = mul(qA, sub(mk(an.x, an.y), mk(lcA.x, lcA.y)));
+        const V2 p_c = sub(mk(an2.x, an2.y), mk(lcC.x, lcC.y));
+        const V2 p_a = mul_t(qC, add(rA, sub(cA, cC)));
+        coordinate_a = dot(sub(p_a, p_c), mk(ax.x, ax.y));
+    }
+    if (!(fl & JF_GEAR_B_PRISMATIC)) {
+        coordinate_b = aB - aD - ref.y;
+    } else {
+        const float2 lcB = w.b_lc[ab.y], lcD = w.b_lc[cd.y];
+        const V2 rB = mul(qB, sub(mk(an.z, an.w), mk(lcB.x, lcB.y)));
+        const V2 p_d = sub(mk(an2.z, an2.w), mk(lcD.x, lcD.y));
+        const V2 p_b = mul_t(qD, add(rB, sub(cB, cD)));
+        coordinate_b = dot(sub(p_b, p_d), mk(ax.z, ax.w));
+    }
+    const float C = (coordinate_a + par.x * coordinate_b) - par.z;
+    float impulse = 0.0f;
+    if (g.mass > 0.0f) impulse = fdiv(-C, g.mass);
+    cA = add(cA, scale(mA.y * impulse, g.jv_ac));
+    aA += mA.w * impulse * g.jw_a;
+    cB = add(cB, scale(mB.y * impulse, g.jv_bd));
+    aB += mB.w * impulse * g.jw_b;
+    cC = sub(cC, scale(mC.y * impulse, g.jv_ac));
+    aC -= mC.w * impulse * g.jw_c;
+    cD = sub(cD, scale(mD.y * impulse, g.jv_bd));
+    aD -= mD.w * impulse * g.jw_d;
+    if (joint_body_dynamic(w, ab.x)) w.b_pos[ab.x] = make_float4(cA.x, cA.y, aA, pa.w);
+    if (joint_body_dynamic(w, ab.y)) w.b_pos[ab.y] = make_float4(cB.x, cB.y, aB, pb.w);
+    if (joint_body_dynamic(w, cd.x)) w.b_pos[cd.x] = make_float4(cC.x, cC.y, aC, pc.w);
+    if (joint_body_dynamic(w, cd.y)) w.b_pos[cd.y] = make_float4(cD.x, cD.y, aD, pd.w);
+    return true;
+}
+
 __device__ __forceinline__ uint32_t joint_type(const DevWorld& w, int j) {
     return (__float_as_uint(w.j_par[j].y) >> JF_TYPE_SHIFT) & 0xffu;
 }
@@ -1508,6 +1684,7 @@ __device__ __forceinline__ void joint_init_velocity(const DevWorld& w, const Ste
     else if (t == B2G_JOINT_PRISMATIC) prismatic_init_velocity(w, sp, j);
     else if (t == B2G_JOINT_WHEEL) wheel_init_velocity(w, sp, j);
     else if (t == B2G_JOINT_PULLEY) pulley_init_velocity(w, sp, j);
+    else if (t == B2G_JOINT_GEAR) gear_init_velocity(w, sp, j);
     else revolute_init_velocity(w, sp, j);
 }
 __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const StepParams& sp, int j) {
@@ -1520,6 +1697,7 @@ __device__ __forceinline__ void joint_solve_velocity(const DevWorld& w, const St
     else if (t == B2G_JOINT_PRISMATIC) prismatic_solve_velocity(w, sp, j);
     else if (t == B2G_JOINT_WHEEL) wheel_solve_velocity(w, sp, j);
     else if (t == B2G_JOINT_PULLEY) pulley_solve_velocity(w, j);
+    else if (t == B2G_JOINT_GEAR) gear_solve_velocity(w, j);
     else revolute_solve_velocity(w, sp, j);
 }
 __device__ __forceinline__ bool joint_solve_position(const DevWorld& w, int j) {
@@ -1530,6 +1708,7 @@ __device__ __forceinline__ bool joint_solve_position(const DevWorld& w, int j) {
     if (t == B2G_JOINT_PRISMATIC) return prismatic_solve_position(w, j);
     if (t == B2G_JOINT_WHEEL) return wheel_solve_position(w, j);
     if (t == B2G_JOINT_PULLEY) return pulley_solve_position(w, j);
+    if (t == B2G_JOINT_GEAR) return gear_solve_position(w, j);
     return revolute_solve_position(w, j);
 }
 

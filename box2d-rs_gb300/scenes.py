@@ -492,6 +492,54 @@ def bridge(planks=30, seed=13, steps=240, drops=24):
     return _scene("bridge", bodies, np.concatenate(fixtures), steps, joints=np.concatenate(joints))
 
 
+def gears(steps=240, drops=12, seed=17):
+    """The box2d-rs testbed's gear joints (examples/testbed/tests/gear_joint.rs) with the gears' body_a /
+    body_b set to their joints' second bodies: a box hanging from a static disc with a disc hinged to
+    its lower end, geared to the box (the box is both A and D of that gear); a disc and a larger disc
+    hinged to the ground and geared 2:1, the larger one geared to a box sliding on a vertical prismatic
+    joint with limits. Boxes and circles dropped on top give them contacts to push through."""
+    rng = SplitMix64(seed)
+    bodies = b2g.body_defs(7 + drops)
+    bodies["allow_sleep"] = 0
+    fixtures = [b2g.edge_fixture(0, (50.0, 0.0), (-50.0, 0.0))]
+    # the first group: static disc 1, hanging box 2, disc 3
+    bodies[1]["position"] = (10.0, 9.0)
+    fixtures.append(b2g.circle_fixture(1, 1.0, density=5.0))
+    bodies[2]["type"], bodies[2]["position"] = b2g.DYNAMIC, (10.0, 8.0)
+    fixtures.append(b2g.box_fixture(2, 0.5, 5.0, density=5.0))
+    bodies[3]["type"], bodies[3]["position"] = b2g.DYNAMIC, (10.0, 6.0)
+    bodies[3]["angular_velocity"] = 1.5
+    fixtures.append(b2g.circle_fixture(3, 2.0, density=5.0))
+    # the second group: disc 4 and disc 5 hinged to the ground, box 6 on a vertical slider
+    bodies[4]["type"], bodies[4]["position"] = b2g.DYNAMIC, (-3.0, 12.0)
+    fixtures.append(b2g.circle_fixture(4, 1.0, density=5.0))
+    bodies[5]["type"], bodies[5]["position"] = b2g.DYNAMIC, (0.0, 12.0)
+    fixtures.append(b2g.circle_fixture(5, 2.0, density=5.0))
+    bodies[6]["type"], bodies[6]["position"] = b2g.DYNAMIC, (2.5, 12.0)
+    fixtures.append(b2g.box_fixture(6, 0.5, 5.0, density=5.0))
+    joints = [
+        b2g.revolute_joint(1, 2, (0.0, 0.0), (0.0, 1.0)),      # 0: static disc - box at (10, 9)
+        b2g.revolute_joint(2, 3, (0.0, -2.0), (0.0, 0.0)),     # 1: box - disc at (10, 6)
+        b2g.gear_joint(0, 1, 2, 3, ratio=2.0),                 # 2: body_a = 2, body_b = 3
+        b2g.revolute_joint(0, 4, (-3.0, 12.0), (0.0, 0.0)),    # 3: ground - disc 4
+        b2g.revolute_joint(0, 5, (0.0, 12.0), (0.0, 0.0)),     # 4: ground - disc 5
+        b2g.prismatic_joint(0, 6, (2.5, 12.0), (0.0, 0.0), (0.0, 1.0), limits=(-5.0, 5.0)),  # 5
+        b2g.gear_joint(3, 4, 4, 5, ratio=2.0),                 # 6
+        b2g.gear_joint(4, 5, 5, 6, ratio=-1.0 / 2.0),          # 7
+    ]
+    px = rng.uniform(drops, -6.0, 12.0)
+    py = rng.uniform(drops, 18.0, 30.0)
+    for k in range(drops):
+        b = 7 + k
+        bodies[b]["type"] = b2g.DYNAMIC
+        bodies[b]["position"] = (px[k], py[k])
+        if k % 2:
+            fixtures.append(b2g.circle_fixture(b, 0.5, density=1.0, friction=0.4))
+        else:
+            fixtures.append(b2g.box_fixture(b, 0.5, 0.4, density=1.0, friction=0.4))
+    return _scene("gears", bodies, np.concatenate(fixtures), steps, joints=np.concatenate(joints))
+
+
 def build_world(world, scene):
     """Create a scene's bodies, fixtures and joints in a B2world or OracleWorld."""
     world.create_bodies(scene["bodies"])

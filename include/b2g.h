@@ -141,6 +141,7 @@ typedef struct b2g_fixture_def {
 #define B2G_JOINT_MOUSE 5
 #define B2G_JOINT_WHEEL 7
 #define B2G_JOINT_MOTOR 11
+#define B2G_JOINT_GEAR 6
 typedef struct b2g_joint_def {
     int32_t type;              /* B2G_JOINT_* */
     uint32_t body_a, body_b;
@@ -160,6 +161,9 @@ typedef struct b2g_joint_def {
     float lower_translation, upper_translation, max_motor_force;
     b2g_vec2 ground_anchor_a, ground_anchor_b;
     float length_a, length_b, ratio;
+    /* gear joint (B2gearJointDef, src/joints/b2_gear_joint.rs): the revolute or prismatic joints it
+     * couples (ids of joints created earlier); body_a and body_b must be their second bodies; ratio */
+    uint32_t joint1, joint2;
 } b2g_joint_def;
 
 /* Body state read back after a step (B2body getters, src/b2_body.rs:650-680). */

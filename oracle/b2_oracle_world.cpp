@@ -129,6 +129,14 @@ struct Joint {
     Vec2 ground_a{0, 0}, ground_b{0, 0}, u_a{0, 0}, u_b{0, 0};
     float pulley_constant = 0, ratio = 1, pulley_impulse = 0, pulley_mass = 0;
     float weld_mass[9] = {0};  /* ex, ey, ez columns */
+    /* B2gearJoint (private/dynamics/joints/b2_gear_joint.rs): bodies C and D, the four local anchors, the
+     * prismatic sides' axes and the sides' reference angles fixed at creation; the step's Jacobian */
+    int body_c = -1, body_d = -1, index_c = 0, index_d = 0;
+    bool gear_prismatic_a = false, gear_prismatic_b = false;
+    Vec2 gear_anchor_a{0, 0}, gear_anchor_b{0, 0}, gear_anchor_c{0, 0}, gear_anchor_d{0, 0};
+    Vec2 gear_axis_c{0, 0}, gear_axis_d{0, 0}, jv_ac{0, 0}, jv_bd{0, 0}, lc_c{0, 0}, lc_d{0, 0};
+    float gear_ref_a = 0, gear_ref_b = 0, gear_constant = 0, gear_impulse = 0, gear_mass = 0;
+    float jw_a = 0, jw_b = 0, jw_c = 0, jw_d = 0, inv_mass_c = 0, inv_mass_d = 0, inv_ic = 0, inv_id = 0;
     bool collide_connected = false, island_flag = false, alive = true;
     Vec2 local_anchor_a{0, 0}, local_anchor_b{0, 0};
     float reference_angle = 0;
@@ -2156,7 +2164,154 @@ static bool pulley_solve_position(World& w, Joint& j) {
 }
 
 /* init_velocity_constraints (:21-116): anchors, effective masses, warm start */
+/* ---- gear joint, private/dynamics/joints/b2_gear_joint.rs ---- */
+
+/* the Jacobian rows and the (not yet inverted) mass of :209-241 and :326-359 */
+static float gear_jacobian(Joint& j, const Rot& qA, const Rot& qB, const Rot& qC, const Rot& qD, Vec2& jv_ac,
+                           Vec2& jv_bd, float& jw_a, float& jw_b, float& jw_c, float& jw_d) {
+    float mass = 0.0f;
+    if (!j.gear_prismatic_a) {
+        jv_ac = v2(0, 0);
+        jw_a = 1.0f;
+        jw_c = 1.0f;
+        mass += j.inv_ia + j.inv_ic;
+    } else {
+        const Vec2 u = mul(qC, j.gear_axis_c);
+        const Vec2 rC = mul(qC, j.gear_anchor_c - j.lc_c);
+        const Vec2 rA = mul(qA, j.gear_anchor_a - j.lc_a);
+        jv_ac = u;
+        jw_c = cross(rC, u);
+        jw_a = cross(rA, u);
+        mass += j.inv_mass_c + j.inv_mass_a + j.inv_ic * jw_c * jw_c + j.inv_ia * jw_a * jw_a;
+    }
+    if (!j.gear_prismatic_b) {
+        jv_bd = v2(0, 0);
+        jw_b = j.ratio;
+        jw_d = j.ratio;
+        mass += j.ratio * j.ratio * (j.inv_ib + j.inv_id);
+    } else {
+        const Vec2 u = mul(qD, j.gear_axis_d);
+        const Vec2 rD = mul(qD, j.gear_anchor_d - j.lc_d);
+        const Vec2 rB = mul(qB, j.gear_anchor_b - j.lc_b);
+        jv_bd = j.ratio * u;
+        jw_d = j.ratio * cross(rD, u);
+        jw_b = j.ratio * cross(rB, u);
+        mass += j.ratio * j.ratio * (j.inv_mass_d + j.inv_mass_b) + j.inv_id * jw_d * jw_d + j.inv_ib * jw_b * jw_b;
+    }
+    return mass;
+}
+
+/* the four island velocities changed by impulse (:264-273, :300-307): read all, write A, B, C, D */
+static void gear_apply_velocity(World& w, const Joint& j, float impulse) {
+    Vec2 vA = w.vel[j.index_a].v, vB = w.vel[j.index_b].v, vC = w.vel[j.index_c].v, vD = w.vel[j.index_d].v;
+    float wA = w.vel[j.index_a].w, wB = w.vel[j.index_b].w, wC = w.vel[j.index_c].w, wD = w.vel[j.index_d].w;
+    vA += (j.inv_mass_a * impulse) * j.jv_ac;
+    wA += j.inv_ia * impulse * j.jw_a;
+    vB += (j.inv_mass_b * impulse) * j.jv_bd;
+    wB += j.inv_ib * impulse * j.jw_b;
+    vC -= (j.inv_mass_c * impulse) * j.jv_ac;
+    wC -= j.inv_ic * impulse * j.jw_c;
+    vD -= (j.inv_mass_d * impulse) * j.jv_bd;
+    wD -= j.inv_id * impulse * j.jw_d;
+    w.vel[j.index_a].v = vA;
+    w.vel[j.index_a].w = wA;
+    w.vel[j.index_b].v = vB;
+    w.vel[j.index_b].w = wB;
+    w.vel[j.index_c].v = vC;
+    w.vel[j.index_c].w = wC;
+    w.vel[j.index_d].v = vD;
+    w.vel[j.index_d].w = wD;
+}
+
+/* init_velocity_constraints, :190-289 */
+static void gear_init_velocity(World& w, Joint& j, const Step& step) {
+    const Body* bs[4] = {&w.bodies[j.body_a], &w.bodies[j.body_b], &w.bodies[j.body_c], &w.bodies[j.body_d]};
+    j.index_a = bs[0]->island_index;
+    j.index_b = bs[1]->island_index;
+    j.index_c = bs[2]->island_index;
+    j.index_d = bs[3]->island_index;
+    j.lc_a = bs[0]->sweep.local_center;
+    j.lc_b = bs[1]->sweep.local_center;
+    j.lc_c = bs[2]->sweep.local_center;
+    j.lc_d = bs[3]->sweep.local_center;
+    j.inv_mass_a = bs[0]->inv_mass;
+    j.inv_mass_b = bs[1]->inv_mass;
+    j.inv_mass_c = bs[2]->inv_mass;
+    j.inv_mass_d = bs[3]->inv_mass;
+    j.inv_ia = bs[0]->inv_I;
+    j.inv_ib = bs[1]->inv_I;
+    j.inv_ic = bs[2]->inv_I;
+    j.inv_id = bs[3]->inv_I;
+    const Rot qA = rot(w.pos[j.index_a].a), qB = rot(w.pos[j.index_b].a), qC = rot(w.pos[j.index_c].a),
+              qD = rot(w.pos[j.index_d].a);
+    j.gear_mass = gear_jacobian(j, qA, qB, qC, qD, j.jv_ac, j.jv_bd, j.jw_a, j.jw_b, j.jw_c, j.jw_d);
+    j.gear_mass = j.gear_mass > 0.0f ? 1.0f / j.gear_mass : 0.0f;
+    if (step.warm) gear_apply_velocity(w, j, j.gear_impulse);
+    else j.gear_impulse = 0.0f;
+}
+
+/* solve_velocity_constraints, :291-319 */
+static void gear_solve_velocity(World& w, Joint& j) {
+    const Velocity A = w.vel[j.index_a], B = w.vel[j.index_b], C = w.vel[j.index_c], D = w.vel[j.index_d];
+    float cdot = dot(j.jv_ac, A.v - C.v) + dot(j.jv_bd, B.v - D.v);
+    cdot += (j.jw_a * A.w - j.jw_c * C.w) + (j.jw_b * B.w - j.jw_d * D.w);
+    const float impulse = -j.gear_mass * cdot;
+    j.gear_impulse += impulse;
+    gear_apply_velocity(w, j, impulse);
+}
+
+/* solve_position_constraints, :321-393 */
+static bool gear_solve_position(World& w, Joint& j) {
+    Vec2 cA = w.pos[j.index_a].c, cB = w.pos[j.index_b].c, cC = w.pos[j.index_c].c, cD = w.pos[j.index_d].c;
+    float aA = w.pos[j.index_a].a, aB = w.pos[j.index_b].a, aC = w.pos[j.index_c].a, aD = w.pos[j.index_d].a;
+    const Rot qA = rot(aA), qB = rot(aB), qC = rot(aC), qD = rot(aD);
+    Vec2 jv_ac, jv_bd;
+    float jw_a, jw_b, jw_c, jw_d;
+    const float mass = gear_jacobian(j, qA, qB, qC, qD, jv_ac, jv_bd, jw_a, jw_b, jw_c, jw_d);
+    float coordinate_a, coordinate_b;
+    if (!j.gear_prismatic_a) {
+        coordinate_a = aA - aC - j.gear_ref_a;
+    } else {
+        const Vec2 rA = mul(qA, j.gear_anchor_a - j.lc_a);
+        const Vec2 p_c = j.gear_anchor_c - j.lc_c;
+        const Vec2 p_a = mul_t(qC, rA + (cA - cC));
+        coordinate_a = dot(p_a - p_c, j.gear_axis_c);
+    }
+    if (!j.gear_prismatic_b) {
+        coordinate_b = aB - aD - j.gear_ref_b;
+    } else {
+        const Vec2 rB = mul(qB, j.gear_anchor_b - j.lc_b);
+        const Vec2 p_d = j.gear_anchor_d - j.lc_d;
+        const Vec2 p_b = mul_t(qD, rB + (cB - cD));
+        coordinate_b = dot(p_b - p_d, j.gear_axis_d);
+    }
+    const float C = (coordinate_a + j.ratio * coordinate_b) - j.gear_constant;
+    float impulse = 0.0f;
+    if (mass > 0.0f) impulse = -C / mass;
+    cA += j.inv_mass_a * impulse * jv_ac;
+    aA += j.inv_ia * impulse * jw_a;
+    cB += j.inv_mass_b * impulse * jv_bd;
+    aB += j.inv_ib * impulse * jw_b;
+    cC -= j.inv_mass_c * impulse * jv_ac;
+    aC -= j.inv_ic * impulse * jw_c;
+    cD -= j.inv_mass_d * impulse * jv_bd;
+    aD -= j.inv_id * impulse * jw_d;
+    w.pos[j.index_a].c = cA;
+    w.pos[j.index_a].a = aA;
+    w.pos[j.index_b].c = cB;
+    w.pos[j.index_b].a = aB;
+    w.pos[j.index_c].c = cC;
+    w.pos[j.index_c].a = aC;
+    w.pos[j.index_d].c = cD;
+    w.pos[j.index_d].a = aD;
+    return true;  /* the linear error is never measured (:392-393) */
+}
+
 static void joint_init_velocity(World& w, Joint& j, const Step& step) {
+    if (j.type == B2G_JOINT_GEAR) {
+        gear_init_velocity(w, j, step);
+        return;
+    }
     if (j.type == B2G_JOINT_MOTOR) {
         motor_init_velocity(w, j, step);
         return;
@@ -2252,6 +2407,10 @@ static void joint_init_velocity(World& w, Joint& j, const Step& step) {
 
 /* solve_velocity_constraints (:118-208): motor, lower and upper limits, point */
 static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
+    if (j.type == B2G_JOINT_GEAR) {
+        gear_solve_velocity(w, j);
+        return;
+    }
     if (j.type == B2G_JOINT_MOTOR) {
         motor_solve_velocity(w, j, step);
         return;
@@ -2340,6 +2499,7 @@ static void joint_solve_velocity(World& w, Joint& j, const Step& step) {
 
 /* solve_position_constraints (:210-287): angular limit, then the point */
 static bool joint_solve_position(World& w, Joint& j) {
+    if (j.type == B2G_JOINT_GEAR) return gear_solve_position(w, j);
     if (j.type == B2G_JOINT_DISTANCE) return distance_solve_position(w, j);
     if (j.type == B2G_JOINT_WELD) return weld_solve_position(w, j);
     /* b2_friction_joint.rs, b2_motor_joint.rs and b2_mouse_joint.rs: no position correction */
@@ -3250,7 +3410,9 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
         const b2g_joint_def& d = defs[i];
         if ((d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_DISTANCE && d.type != B2G_JOINT_WELD &&
              d.type != B2G_JOINT_FRICTION && d.type != B2G_JOINT_MOTOR && d.type != B2G_JOINT_MOUSE &&
-             d.type != B2G_JOINT_PRISMATIC && d.type != B2G_JOINT_WHEEL && d.type != B2G_JOINT_PULLEY) ||
+             d.type != B2G_JOINT_PRISMATIC && d.type != B2G_JOINT_WHEEL && d.type != B2G_JOINT_PULLEY &&
+             d.type != B2G_JOINT_GEAR) ||
+            (d.type == B2G_JOINT_GEAR && (d.joint1 >= w.joints.size() || d.joint2 >= w.joints.size())) ||
             d.body_a >= w.bodies.size() ||
             d.body_b >= w.bodies.size())
             return -1;
@@ -3292,6 +3454,40 @@ int ora_create_joints(void* p, const b2g_joint_def* defs, int n, uint32_t* ids) 
         j.local_anchor_b = v2(d.local_anchor_b.x, d.local_anchor_b.y);
         /* b2_mouse_joint_new (src/joints/b2_mouse_joint.rs:140-160): the target in body B's frame */
         if (j.type == B2G_JOINT_MOUSE) j.local_anchor_b = mul_t(w.bodies[j.body_b].xf, j.target);
+        if (j.type == B2G_JOINT_GEAR) {
+            /* B2gearJoint::new (private/dynamics/joints/b2_gear_joint.rs:29-137): each side's anchors, axis,
+             * reference angle and coordinate from its joint and the bodies' current transforms */
+            float coordinate[2];
+            for (int side = 0; side < 2; ++side) {
+                const Joint& J = w.joints[side == 0 ? d.joint1 : d.joint2];
+                const Body& F = w.bodies[J.body_a];
+                const Body& S = w.bodies[J.body_b];
+                const bool prismatic = J.type == B2G_JOINT_PRISMATIC;
+                const Vec2 axis = prismatic ? J.local_xaxis_a : v2(0, 0);
+                if (prismatic) {
+                    const Vec2 p_second = mul_t(F.xf.q, mul(S.xf.q, J.local_anchor_b) + (S.xf.p - F.xf.p));
+                    coordinate[side] = dot(p_second - J.local_anchor_a, axis);
+                } else {
+                    coordinate[side] = S.sweep.a - F.sweep.a - J.reference_angle;
+                }
+                if (side == 0) {
+                    j.body_c = J.body_a;
+                    j.gear_anchor_c = J.local_anchor_a;
+                    j.gear_anchor_a = J.local_anchor_b;
+                    j.gear_axis_c = axis;
+                    j.gear_ref_a = J.reference_angle;
+                    j.gear_prismatic_a = prismatic;
+                } else {
+                    j.body_d = J.body_a;
+                    j.gear_anchor_d = J.local_anchor_a;
+                    j.gear_anchor_b = J.local_anchor_b;
+                    j.gear_axis_d = axis;
+                    j.gear_ref_b = J.reference_angle;
+                    j.gear_prismatic_b = prismatic;
+                }
+            }
+            j.gear_constant = coordinate[0] + j.ratio * coordinate[1];
+        }
         j.reference_angle = d.reference_angle;
         j.enable_limit = d.enable_limit != 0;
         j.lower_angle = d.lower_angle;
@@ -3322,6 +3518,11 @@ int ora_get_joint_impulses(void* p, uint32_t first, uint32_t count, float* out) 
     if ((size_t)first + count > w.joints.size()) return -1;
     for (uint32_t i = 0; i < count; ++i) {
         const Joint& j = w.joints[first + i];
+        if (j.type == B2G_JOINT_GEAR) {
+            out[5 * i + 0] = j.gear_impulse;
+            for (int k = 1; k < 5; ++k) out[5 * i + k] = 0.0f;
+            continue;
+        }
         if (j.type == B2G_JOINT_PULLEY) {
             out[5 * i + 0] = j.pulley_impulse;
             for (int k = 1; k < 5; ++k) out[5 * i + k] = 0.0f;

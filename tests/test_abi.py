@@ -42,10 +42,11 @@ def test_struct_layouts(built, tmp_path):
     code = """#include <stdio.h>
 #include <stddef.h>
 #include "b2g.h"
-int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(b2g_world_def), sizeof(b2g_body_def),
+int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(b2g_world_def), sizeof(b2g_body_def),
  sizeof(b2g_fixture_def), sizeof(b2g_body_state), sizeof(b2g_contact_info), sizeof(b2g_contact_event),
  sizeof(b2g_profile), sizeof(b2g_counts), sizeof(b2g_tape_slot), sizeof(b2g_tape_step), sizeof(b2g_tape_info), sizeof(b2g_ray_hit), sizeof(b2g_launch_config),
- sizeof(b2g_sweep), sizeof(b2g_toi_output), sizeof(b2g_joint_def));
+ sizeof(b2g_sweep), sizeof(b2g_toi_output), sizeof(b2g_joint_def), sizeof(b2g_contact_impulse), sizeof(b2g_step_stats),
+ sizeof(b2g_contact_edit), offsetof(b2g_joint_def, joint2));
  return 0;}"""
     try:
         with open(src, "w") as f:
@@ -61,7 +62,8 @@ int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %
                      ctypes.sizeof(b2g.Profile), ctypes.sizeof(b2g.Counts), b2g.TAPE_SLOT.itemsize,
                      b2g.TAPE_STEP.itemsize, ctypes.sizeof(b2g.TapeInfo), b2g.RAY_HIT.itemsize,
                      ctypes.sizeof(b2g.LaunchConfig), b2g.SWEEP.itemsize, b2g.TOI_OUTPUT.itemsize,
-                     b2g.JOINT_DEF.itemsize]
+                     b2g.JOINT_DEF.itemsize, b2g.CONTACT_IMPULSE.itemsize, ctypes.sizeof(b2g.StepStats),
+                     ctypes.sizeof(b2g.ContactEdit), b2g.JOINT_DEF.fields["joint2"][1]]
 
 
 def test_invalid_arguments_are_rejected_without_a_device(built):

@@ -738,3 +738,21 @@ def test_pulley_joints_lockstep(built):
     st = gpu.get_body_states()
     assert np.all(np.isfinite(st["position"]))
     assert float(st["position"][2, 1]) < 5.0  # the heavier side went down
+
+
+def test_gear_joints_lockstep(built):
+    """Gear joints (B2gearJoint): a disc geared to the box it hangs from (the box is both bodies A and D
+    of that gear), two discs geared 2:1 on ground hinges, and the larger disc geared to a box on a
+    limited vertical slider (a revolute-prismatic gear); bodies and joint impulses bit-exact every step,
+    and the gear constraints hold: a4 + 2 a5 and a5 - 0.5 (y6 - 12) stay at their initial values."""
+    s = scenes.gears(steps=240)
+    recs, gpu, _ = parity.lockstep(s, 240)
+    for r in recs:
+        _assert_step(r)
+        assert r["joint_impulses_equal"], r
+    st = gpu.get_body_states()
+    assert abs(st["angle"][4] + 2.0 * st["angle"][5]) < 1e-3
+    assert abs(st["angle"][5] - 0.5 * (st["position"][6, 1] - 12.0)) < 1e-3
+    assert abs(st["angle"][4]) > 1.0, "the geared train should have turned"
+    with pytest.raises(b2g.B2GError):  # a gear whose body_a is not its first joint's second body
+        gpu.create_joints(b2g.gear_joint(0, 1, 1, 3))
