@@ -469,12 +469,14 @@ def run_pile(torch, flush, device, steps=20, warmup=3, cpu=True, n_boxes=250_000
     """High-contact pile: 250k boxes (half-extents 0.05-0.2 m) dropped into a 100 x 400 m walled container,
     1000 steps. The last `steps` steps of the 1000 are timed (device time, L2 flushed between steps),
     when the pile holds its most contact points. CPU: the oracle (libm sin/cos, 1 thread) stepped from
-    the GPU's state at the start of the window. Contact and pair capacities are given explicitly."""
+    the GPU's state at the start of the window. The world starts with 16M contacts and 4M new pairs of
+    capacity and grows them as needed (b2g_set_auto_grow)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     scene = scenes.pile(n_boxes=n_boxes, steps=scene_steps)
     dt, vi, pi = scene["dt"], scene["vi"], scene["pi"]
     w = b2g.B2world(gravity=scene["gravity"], device=device, contact_capacity=16_000_000, pair_capacity=4_000_000)
     w.set_allow_sleeping(False)
+    w.set_auto_grow(True)  # the falling column's stretched fat AABBs overlap many boxes below them
     scenes.build_world(w, scene)
     skip = scene_steps - steps - warmup
     for _ in range(skip):
@@ -511,7 +513,9 @@ def run_pile(torch, flush, device, steps=20, warmup=3, cpu=True, n_boxes=250_000
            "phase_ms_per_step": {k: v / steps for k, v in fine.items()},
            "solver_roofline": {"achieved": solver_ach, "peak": peak, "unit": "GB/s",
                                "frac": solver_ach / peak if solver_ach else None},
-           "capacities": {"contacts": 16_000_000, "pairs": 4_000_000}}
+           "capacities": {"initial_contacts": 16_000_000, "initial_pairs": 4_000_000,
+                          "contacts": st["contact_capacity"], "pairs": st["pair_capacity"],
+                          "grows": st["capacity_grows"]}}
     if cpu:
         import oracle
 

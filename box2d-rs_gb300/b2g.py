@@ -454,7 +454,8 @@ def pre_solve_callback(fn):
 
 class StepStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in ("bp_node_visits", "bp_leaf_checks", "new_pairs", "contacts", "constraints",
-                                               "interior_slots", "parts", "colours")]
+                                               "interior_slots", "parts", "colours", "contact_capacity",
+                                               "pair_capacity", "capacity_grows", "reserved")]
 
 
 class Counts(ctypes.Structure):
@@ -655,6 +656,7 @@ def load_library(path=LIB_PATH):
         "b2g_set_record_pairs": [vp, i32],
         "b2g_set_graph_capture": [vp, i32],
         "b2g_set_barrier_limit": [vp, ctypes.c_int64],
+        "b2g_set_auto_grow": [vp, i32],
         "b2g_debug_hold_barriers": [vp, i32],
         "b2g_get_phase_times": [vp, vp, i32],
         "b2g_get_step_stats": [vp, ctypes.POINTER(StepStats)],
@@ -890,6 +892,10 @@ class B2world:
 
     def set_graph_capture(self, flag):
         self._check(self._lib.b2g_set_graph_capture(self._h, int(flag)))
+
+    def set_auto_grow(self, flag):
+        """Contact and pair capacities grow on overflow, the pass repeated exactly (b2g_set_auto_grow)."""
+        self._check(self._lib.b2g_set_auto_grow(self._h, int(flag)))
 
     def set_barrier_limit(self, cycles):
         """Grid-barrier wait limit of the world's persistent kernels in clock cycles (0: default)."""

@@ -157,6 +157,9 @@ struct World {
     bool device_authoritative = false;
     std::vector<void*> allocations;
     std::vector<size_t> alloc_bytes;  /* byte size of each entry of allocations */
+    std::vector<void*> alloc_field;   /* the DevWorld member each entry was allocated into (its address) */
+    bool auto_grow = false;           /* b2g_set_auto_grow: contact / pair capacity grows on overflow */
+    int capacity_grows = 0;
     int user_contact_cap = 0, user_pair_cap = 0;
     Timer timer;
     b2g_profile profile{};
@@ -264,8 +267,16 @@ int dalloc(World* w, T** p, size_t n) {
     }
     w->allocations.push_back((void*)*p);
     w->alloc_bytes.push_back(n * sizeof(T));
+    w->alloc_field.push_back((void*)p);
     cudaMemsetAsync(*p, 0, n * sizeof(T), w->stream);
     return B2G_OK;
+}
+
+/* forgets entry k of the allocation list (the caller frees the memory) */
+void drop_allocation(World* w, size_t k) {
+    w->alloc_bytes.erase(w->alloc_bytes.begin() + k);
+    w->alloc_field.erase(w->alloc_field.begin() + k);
+    w->allocations.erase(w->allocations.begin() + k);
 }
 
 void drop_graphs(World* w);
@@ -275,10 +286,7 @@ template <class T>
 void dfree(World* w, T** p) {
     if (!*p) return;
     auto it = std::find(w->allocations.begin(), w->allocations.end(), (void*)*p);
-    if (it != w->allocations.end()) {
-        w->alloc_bytes.erase(w->alloc_bytes.begin() + (it - w->allocations.begin()));
-        w->allocations.erase(it);
-    }
+    if (it != w->allocations.end()) drop_allocation(w, (size_t)(it - w->allocations.begin()));
     cudaFree(*p);
     *p = nullptr;
 }
@@ -288,6 +296,7 @@ void free_all(World* w) {
     for (void* p : w->allocations) cudaFree(p);
     w->allocations.clear();
     w->alloc_bytes.clear();
+    w->alloc_field.clear();
     w->joint_cap = 0;
     w->d.j_body = nullptr;  /* the joint arrays went with the rest */
     w->allocated = false;
@@ -588,10 +597,13 @@ int write_barrier_settings(World* w) {
     return B2G_OK;
 }
 
-int allocate(World* w, int nb, int nf) {
+/* keep_body_cap / keep_fix_cap (when > 0): the body and fixture capacities to keep, so that a
+ * reallocation that only grows the contact and pair capacities keeps every per-body and per-fixture
+ * array's layout */
+int allocate(World* w, int nb, int nf, int keep_body_cap = 0, int keep_fix_cap = 0) {
     DevWorld& d = w->d;
-    const int body_cap = nb + nb / 4 + 1024;
-    const int fix_cap = nf + nf / 4 + 1024;
+    const int body_cap = keep_body_cap > 0 ? keep_body_cap : nb + nb / 4 + 1024;
+    const int fix_cap = keep_fix_cap > 0 ? keep_fix_cap : nf + nf / 4 + 1024;
     /* a capacity given in b2g_world_def is used as is; 0 picks one proportional to the fixtures */
     const int contact_cap = w->user_contact_cap > 0 ? w->user_contact_cap : 6 * fix_cap + 4096;
     const int pair_cap = w->user_pair_cap > 0 ? w->user_pair_cap : 4 * fix_cap + 4096;
@@ -760,6 +772,63 @@ int alloc_joint_arrays(World* w, int cap) {
     drop_graphs(w);
     ++w->alloc_generation;
     return B2G_OK;
+}
+
+/* Grows the contact and pair capacities in place: every buffer is reallocated with the same body and
+ * fixture capacities and the old contents copied to the front of its successor, matched by the
+ * DevWorld member that holds it (the contact tables trade members at every swap), so the contact
+ * table, the colouring and partition state and every other persistent array carry over unchanged. */
+int grow_capacities(World* w, int contact_cap, int pair_cap) {
+    CUDA_OK(w, cudaStreamSynchronize(w->stream));
+    const std::vector<void*> old_ptr = w->allocations, old_field = w->alloc_field;
+    const std::vector<size_t> old_bytes = w->alloc_bytes;
+    /* the buffer each member holds now and its size */
+    std::vector<void*> held(old_field.size());
+    std::vector<size_t> held_bytes(old_field.size(), 0);
+    for (size_t i = 0; i < old_field.size(); ++i) {
+        held[i] = *(void**)old_field[i];
+        const auto it = std::find(old_ptr.begin(), old_ptr.end(), held[i]);
+        if (it != old_ptr.end()) held_bytes[i] = old_bytes[(size_t)(it - old_ptr.begin())];
+    }
+    const int joint_cap = w->joint_cap;
+    drop_graphs(w);
+    w->allocations.clear();
+    w->alloc_bytes.clear();
+    w->alloc_field.clear();
+    DevWorld& d = w->d;
+    /* the old joint buffers are still referenced by d: forget them so the reallocation frees nothing */
+    d.j_body = d.j_body2 = nullptr;
+    d.j_anchor = d.j_lim = d.j_par = d.j_imp = d.j_imp2 = d.j_rr = d.j_k = d.j_m = d.j_x = nullptr;
+    d.j_s = nullptr;
+    d.j_order = d.j_coff = d.b_jnt = nullptr;
+    w->joint_cap = 0;
+    w->allocated = false;
+    w->user_contact_cap = contact_cap;
+    w->user_pair_cap = pair_cap;
+    int rc = allocate(w, d.n_bodies, d.n_fixtures, d.body_cap, d.fix_cap);
+    if (rc == B2G_OK && joint_cap > 0) rc = alloc_joint_arrays(w, joint_cap);
+    if (rc == B2G_OK) {
+        /* keep the relation between the swap parity and the table buffers that a saved state records:
+         * with an odd number of swaps the current table is the one allocated second */
+        if (w->swaps & 1) std::swap(d.c, d.c_alt);
+        /* on the world's stream, after the new buffers' zero fill and before any later launch */
+        for (size_t i = 0; i < w->allocations.size() && rc == B2G_OK; ++i) {
+            size_t k = old_field.size();  /* the member that holds this buffer now */
+            for (size_t f = 0; f < old_field.size() && k == old_field.size(); ++f)
+                if (*(void**)old_field[f] == w->allocations[i]) k = f;
+            if (k == old_field.size() || !held[k] || held_bytes[k] == 0) continue;
+            const cudaError_t e = cudaMemcpyAsync(w->allocations[i], held[k], std::min(held_bytes[k], w->alloc_bytes[i]),
+                                                  cudaMemcpyDeviceToDevice, w->stream);
+            if (e != cudaSuccess) rc = fail(w, B2G_ERR_CUDA, cudaGetErrorString(e));
+        }
+        const cudaError_t e = cudaStreamSynchronize(w->stream);
+        if (rc == B2G_OK && e != cudaSuccess) rc = fail(w, B2G_ERR_CUDA, cudaGetErrorString(e));
+    }
+    for (void* p : old_ptr) cudaFree(p);
+    if (rc != B2G_OK) return rc;
+    ++w->capacity_grows;
+    ++w->alloc_generation;
+    return write_barrier_settings(w);
 }
 
 /* Uploads the joints: definitions, impulses, the colouring (greedy, in creation order: a joint takes
@@ -959,6 +1028,8 @@ int prepare(World* w) {
         free_all(w);
         int rc = allocate(w, nb, nf);
         if (rc != B2G_OK) return rc;
+        /* keep the swap parity's relation to the table buffers (a saved state records it) */
+        if (w->swaps & 1) std::swap(w->d.c, w->d.c_alt);
         if (n_contacts > 0) {
             Contacts& c = w->d.c;
             cudaMemcpyAsync(c.key, key.data(), n_contacts * sizeof(uint64_t), cudaMemcpyHostToDevice, w->stream);
@@ -1310,10 +1381,7 @@ int ensure_minsep_buffers(World* w, int pi) {
     if (pi <= w->minsep_buffers) return B2G_OK;
     CUDA_OK(w, cudaStreamSynchronize(w->stream));
     auto it = std::find(w->allocations.begin(), w->allocations.end(), (void*)w->d.isl_minsep);
-    if (it != w->allocations.end()) {
-        w->alloc_bytes.erase(w->alloc_bytes.begin() + (it - w->allocations.begin()));
-        w->allocations.erase(it);
-    }
+    if (it != w->allocations.end()) drop_allocation(w, (size_t)(it - w->allocations.begin()));
     cudaFree(w->d.isl_minsep);
     w->minsep_buffers = pi;
     int rc = dalloc(w, &w->d.isl_minsep, (size_t)pi * w->d.body_cap);
@@ -1321,6 +1389,37 @@ int ensure_minsep_buffers(World* w, int pi) {
     drop_graphs(w);
     ++w->alloc_generation;
     return B2G_OK;
+}
+
+/* With auto-grow on: after a broadphase pass whose new pairs or merged contacts overflowed (the world's
+ * stream drained), the table it started from is made current again, the capacities grow (doubled, as
+ * often as needed) and the pass runs again with every proxy queried. The pass is the last thing that
+ * touched the contact table, and querying every proxy instead of the moved ones finds the same new
+ * contacts (a pair of unmoved overlapping proxies already has its contact or was rejected by add_pair's
+ * rules, which reject it again), so the world continues exactly as one that had the capacity from the
+ * start. Other device errors are reported as usual. */
+int recover_overflow(World* w, const StepParams& sp) {
+    const int growable = ST_CONTACT_OVERFLOW | ST_PAIR_OVERFLOW | ST_RECORD_OVERFLOW;
+    for (int attempt = 0; attempt < 16; ++attempt) {
+        CUDA_OK(w, cudaStreamSynchronize(w->stream));
+        int cnt[CNT_SIZE];
+        CUDA_OK(w, cudaMemcpy(cnt, w->d.cnt, sizeof(cnt), cudaMemcpyDeviceToHost));
+        const int status = cnt[CNT_STATUS];
+        if (!(status & growable) || (status & ~growable)) return status_error(w, status);
+        const int zero = 0, from = cnt[CNT_MERGE_FROM];
+        CUDA_OK(w, cudaMemcpyAsync(w->d.cnt + CNT_STATUS, &zero, sizeof(int), cudaMemcpyHostToDevice, w->stream));
+        swap_contacts(w);
+        CUDA_OK(w, cudaMemcpyAsync(w->d.cnt + CNT_CONTACTS, &from, sizeof(int), cudaMemcpyHostToDevice, w->stream));
+        const int cc = (status & ST_CONTACT_OVERFLOW) ? 2 * w->d.contact_cap : w->d.contact_cap;
+        const int pc = (status & (ST_PAIR_OVERFLOW | ST_RECORD_OVERFLOW)) ? 2 * w->d.pair_cap : w->d.pair_cap;
+        int rc = grow_capacities(w, cc, pc);
+        if (rc != B2G_OK) return rc;
+        launch_touch_all_proxies(w->d, w->stream);
+        launch_broadphase(w->d, sp, w->stream, w->num_sms);
+        swap_contacts(w);
+        CUDA_OK(w, cudaGetLastError());
+    }
+    return fail(w, B2G_ERR_CAPACITY, "capacities still overflow after repeated growth");
 }
 
 /* B2world::step, src/private/dynamics/b2_world.rs:903-959 */
@@ -1347,6 +1446,15 @@ int step(World* w, float dt, int vi, int pi) {
     if (!t.valid) {
         for (auto& e : t.e) cudaEventCreate(&e);
         t.valid = true;
+    }
+    const bool grow = w->auto_grow && !(w->tape && w->tape->recording) && !w->filter_fn;
+    if (grow && w->new_contacts) {
+        /* the initial pass of new fixtures on its own, checked before the step collides its contacts */
+        launch_broadphase(w->d, sp, s, w->num_sms);
+        swap_contacts(w);
+        w->new_contacts = false;
+        rc = recover_overflow(w, sp);
+        if (rc != B2G_OK) return rc;
     }
     /* Steady state (no fixtures added since the last step, dt > 0, warm-start ratio already
      * set): the step's launch sequence depends only on the parameters, the allocation and the
@@ -1416,6 +1524,7 @@ int step(World* w, float dt, int vi, int pi) {
     }
     CUDA_OK(w, cudaGetLastError());
     ++w->steps;
+    if (grow && dt > 0.0f) return recover_overflow(w, sp);
     return B2G_OK;
 }
 
@@ -2341,6 +2450,8 @@ int b2g_set_continuous_physics(void* p, int32_t flag) {
     World* w = W(p);
     if (flag && (w->filter_fn || w->pre_solve_fn))
         return fail(w, B2G_ERR_UNSUPPORTED, "host contact filters and pre_solve callbacks cannot run inside the continuous pass");
+    if (flag && w->auto_grow)
+        return fail(w, B2G_ERR_UNSUPPORTED, "automatic capacity growth does not cover the continuous pass");
     w->continuous = flag != 0;
     return B2G_OK;
 }
@@ -2376,6 +2487,15 @@ int b2g_set_contact_events(void* p, int32_t flag) {
 int b2g_set_record_pairs(void* p, int32_t flag) {
     if (!p) return B2G_ERR_INVALID_ARG;
     W(p)->record_pairs = flag != 0;
+    return B2G_OK;
+}
+
+int b2g_set_auto_grow(void* p, int32_t flag) {
+    World* w = W(p);
+    if (!w) return B2G_ERR_INVALID_ARG;
+    if (flag && w->continuous)
+        return fail(w, B2G_ERR_UNSUPPORTED, "automatic capacity growth does not cover the continuous pass; turn continuous physics off");
+    w->auto_grow = flag != 0;
     return B2G_OK;
 }
 
@@ -2500,6 +2620,9 @@ int b2g_get_step_stats(void* p, b2g_step_stats* out) {
     out->interior_slots = cnt[CNT_INTERIOR];
     out->parts = cnt[CNT_PARTS];
     out->colours = cnt[CNT_COLOURS];
+    out->contact_capacity = w->d.contact_cap;
+    out->pair_capacity = w->d.pair_cap;
+    out->capacity_grows = w->capacity_grows;
     return B2G_OK;
 }
 

@@ -102,6 +102,7 @@ enum {
     CNT_TOI_ITERS = 28,   /* iterations of the last continuous pass */
     CNT_TOI_PASSES = 29,  /* continuous passes run (their body marks are stamped with it) */
     CNT_TOI_ROLLBACKS = 30, /* passes restarted in sequential order after a conflict */
+    CNT_MERGE_FROM = 31,  /* contacts in the table the last merge started from */
     CNT_CASCADE = 40,     /* 3 ints: contacts collided per round of the wake cascade (rotating) */
     CNT_CASCADE_ROUNDS = 43, /* rounds of the last wake cascade */
     CNT_BARRIER_LIMIT = 44, /* grid-barrier wait limit in units of 1024 clock cycles (0: 2e9 cycles) */
@@ -339,6 +340,9 @@ void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s, boo
  * for filtering); body_pairs: contacts between these bodies are flagged for filtering */
 void launch_edit_contacts(const DevWorld& w, const uint8_t* fix_mark, const int2* body_pairs, int n_pairs,
                           bool record_events, cudaStream_t s);
+/* marks every proxy moved, so the next broadphase queries them all (a repeated pass after a capacity
+ * grew finds the same new contacts as the pass it replaces) */
+void launch_touch_all_proxies(const DevWorld& w, cudaStream_t s);
 /* flags the contacts of bodies a joint keeps apart (after joints were created) */
 void launch_flag_joint_contacts(const DevWorld& w, cudaStream_t s, int num_sms);
 void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cudaStream_t s);

@@ -517,6 +517,7 @@ __global__ void k_merge_new(DevWorld w, const uint32_t* rank) {
 __global__ void k_merge_finish(DevWorld w) {
     B2G_RETURN_IF_ABORTED(w);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
+        w.cnt[CNT_MERGE_FROM] = w.cnt[CNT_CONTACTS];
         int total = w.cnt[CNT_ALIVE] + w.cnt[CNT_NEW];
         if (total > w.contact_cap) {
             total = w.contact_cap;
@@ -526,7 +527,17 @@ __global__ void k_merge_finish(DevWorld w) {
     }
 }
 
+__global__ void k_touch_all(DevWorld w) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < w.n_fixtures; f += gridDim.x * blockDim.x)
+        w.f_moved[f] = w.f_refid[f] != 0xffffffffu ? 1 : 0;
+}
+
 }  // namespace
+
+void launch_touch_all_proxies(const DevWorld& w, cudaStream_t s) {
+    k_touch_all<<<grid_for(w.n_fixtures, kBlock, w.num_sms * 8), kBlock, 0, s>>>(w);
+    B2G_LAUNCHED(1);
+}
 
 /* Runs update_pairs + add_pair and merges: the caller swaps w.c and w.c_alt afterwards. */
 void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms,

@@ -329,10 +329,12 @@ int b2g_get_counts(void* world, b2g_counts* out);         /* get_body_count / ge
 /* Work counts of the last step, for traffic models of its kernels (not in the reference, whose
  * B2Profile holds times only): hierarchy nodes the broadphase traversal fetched and leaves it
  * checked, new contacts it found, the contact table's size, constraint slots solved (of them
- * part-locally), the parts and colours of the colouring. */
+ * part-locally), the parts and colours of the colouring; the contact and pair capacities and how
+ * often they grew (b2g_set_auto_grow). */
 typedef struct b2g_step_stats {
     int32_t bp_node_visits, bp_leaf_checks, new_pairs, contacts;
     int32_t constraints, interior_slots, parts, colours;
+    int32_t contact_capacity, pair_capacity, capacity_grows, reserved;
 } b2g_step_stats;
 int b2g_get_step_stats(void* world, b2g_step_stats* out);
 /* Exact checkpoint and resume (not in the reference's API, which serialises a world through serde,
@@ -442,6 +444,13 @@ int b2g_set_graph_capture(void* world, int32_t flag);
  * status check returns B2G_ERR_TIMEOUT and clears it, and the world can be restored with
  * b2g_state_load. The reference has no device waits (it panics or loops on the host). */
 int b2g_set_barrier_limit(void* world, int64_t cycles);
+/* Automatic growth of the contact and pair capacities (off by default; not with continuous physics or
+ * a host contact filter). When a step's broadphase finds more new pairs, or merges more contacts, than
+ * the capacities hold, b2g_step drains the world's stream, doubles the capacity (keeping every device
+ * buffer's contents) and repeats that pass with every proxy queried, which yields the same contacts;
+ * the world then continues bit for bit as one created with the larger capacities. The reference grows
+ * its containers on the host as needed; here each step with it on waits for the device once. */
+int b2g_set_auto_grow(void* world, int32_t flag);
 /* Test hook for the timeout path: every grid barrier of the world's kernels also waits for
  * `extra` arrivals that never come, so each wait runs out its limit (0 turns it off). */
 int b2g_debug_hold_barriers(void* world, int32_t extra);

@@ -305,6 +305,7 @@ def lockstep_window(scene, steps, skip=0, worlds=None, check_pairs=True, part_so
                       contact_capacity=scene.get("contact_capacity", 0), pair_capacity=scene.get("pair_capacity", 0))
     gpu.set_allow_sleeping(False)
     gpu.set_record_pairs(check_pairs)
+    gpu.set_auto_grow(bool(scene.get("auto_grow", False)))
     if part_solve is not None:
         gpu.set_part_solve(part_solve)
     scenes.build_world(gpu, scene)

@@ -289,3 +289,38 @@ def test_barrier_timeout_reports_and_world_recovers(built):
     for f in b2g.BODY_STATE.names:
         assert np.array_equal(ref[0][f], got[0][f]), f
     assert np.array_equal(ref[1], got[1])
+
+
+def test_auto_grow_continues_bit_for_bit(built):
+    """Contact and pair capacities far too small for the scene, with automatic growth on: every
+    overflow doubles the capacity and repeats the step's broadphase pass, and the world stays bit for
+    bit equal to one created with ample capacity (bodies and the whole contact table, every step); a
+    checkpoint taken after the growth loads into a world created with the grown capacities."""
+    s = scenes.mixed(n_circles=1500, n_polygons=1500, size=40.0, seed=13)
+
+    def make(**kw):
+        w = b2g.B2world(gravity=s["gravity"], **kw)
+        w.set_allow_sleeping(False)
+        scenes.build_world(w, s)
+        return w
+
+    small = make(contact_capacity=1500, pair_capacity=300)
+    small.set_auto_grow(True)
+    big = make()
+    for k in range(60):
+        small.step(s["dt"], s["vi"], s["pi"])
+        big.step(s["dt"], s["vi"], s["pi"])
+        a, b = small.get_body_states(), big.get_body_states()
+        for f in b2g.BODY_STATE.names:
+            assert np.array_equal(a[f], b[f]), (k, f)
+        ca, cb = small.get_contacts(), big.get_contacts()
+        assert np.array_equal(ca, cb), k
+    st = small.get_step_stats()
+    assert st["capacity_grows"] >= 2 and st["contact_capacity"] > 1500, st
+    # without growth the same small world reports the overflow
+    fixed = make(contact_capacity=1500, pair_capacity=300)
+    with pytest.raises(b2g.B2GError) as e:
+        for _ in range(10):
+            fixed.step(s["dt"], s["vi"], s["pi"])
+        fixed.synchronize()
+    assert e.value.code == b2g.ERR_CAPACITY

@@ -6,8 +6,10 @@ restatement of box2d-rs's step) solved in the GPU's constraint order:
   mixed 100k    50k circles + 50k 3-8-gons in a 1000 x 1000 m walled box: steps 1-20 from the start,
                 and steps 301-320 after the GPU has run 300 steps alone and the oracle has imported
                 its state (bodies, fat AABBs, the contact table with manifolds and impulses);
-  pile 250k     250k boxes dropped into a 100 x 400 m walled container: steps 981-984 of the
-                1000-step scene, from the GPU's state at step 980 (about a million contact points);
+  pile 250k     250k boxes dropped into a 100 x 400 m walled container: steps 981-983 of the
+                1000-step scene, from the GPU's state at step 980 (about 2.4 million contact points;
+                the falling column's stretched fat AABBs push the table past 16M entries on the way,
+                and the world grows its capacities as it steps);
   batch 4096    4096 worlds of 16-2048 bodies (log-uniform, 1.7M bodies): the GPU steps the whole
                 batch; 64 worlds of every log2 size bucket (7 buckets) are restated one oracle world
                 each, for steps 1-10 and for steps 151-160 from the GPU's state at step 150.
@@ -60,7 +62,8 @@ def test_pile_250k_settled_window(built, oracle_lib):
     assert scene["n_dynamic"] == 250_000
     scene["contact_capacity"] = 16_000_000
     scene["pair_capacity"] = 4_000_000
-    recs = parity.lockstep_window(scene, 4, skip=980)
+    scene["auto_grow"] = True
+    recs = parity.lockstep_window(scene, 3, skip=980)
     _check(recs)
     assert recs[-1]["constraints"] > 200_000, recs[-1]
 
