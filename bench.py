@@ -119,9 +119,11 @@ def bytes_model(st, scene_stats, vi, pi):
                    320 B, velocity iteration 208 B, position iteration 128 B, store 16 B
     k_collide      per contact: 116 B state + 2 shape records (polygon 16 B/vertex + 12, circle 12, edge 36)
     bp_sort        per proxy: bounds 24 B + keys 28 B + 4 radix passes x 24 B (key + payload read and
-                   written)
+                   written); nothing when the pass keeps the hierarchy (hierarchy_age > 0)
     bp_hierarchy   per proxy: build 36 B, leaves 36 B, refit 68 B, four-way records 144 B; per contact:
-                   row index 12 B
+                   row index 12 B. A pass that keeps the hierarchy: per proxy its moved flag 1 B, per moved
+                   proxy 140 B (leaf index and fat AABB read; the leaf, its parent's binary record and two
+                   four-way records located and written), per contact the row index 12 B
     bp_traverse    per fetched node 80 B (four child boxes + children), per checked leaf 32 B (its
                    payload, proxy ids, moved flags, contact row and key), per proxy 5 B (payload and
                    moved flag), per new pair 20 B
@@ -130,11 +132,12 @@ def bytes_model(st, scene_stats, vi, pi):
     nf, nb = scene_stats["n_fixtures"], scene_stats["n_dynamic"]
     nc, ncons = st["contacts"], st["constraints"]
     shape = scene_stats["shape_bytes_mean"]
+    rebuilt = st.get("hierarchy_age", 0) == 0
     return {
         "solver": nb * (72 + 48 + 40) + ncons * (320 + 208 * vi + 128 * pi + 16) + nf * (76 + shape),
         "collide": nc * (116 + 2 * shape),
-        "bp_sort": nf * (24 + 28 + SORT_PASSES * 24),
-        "bp_hierarchy": nf * (36 + 36 + 68 + 144) + nc * 12,
+        "bp_sort": nf * (24 + 28 + SORT_PASSES * 24) if rebuilt else 0,
+        "bp_hierarchy": (nf * (36 + 36 + 68 + 144) if rebuilt else nf + st.get("bp_moved_proxies", 0) * 140) + nc * 12,
         "bp_traverse": st["bp_node_visits"] * 80 + st["bp_leaf_checks"] * 32 + nf * 5 + st["new_pairs"] * 20,
         "merge": nc * 2 * 108,
     }
@@ -690,7 +693,8 @@ def main():
     total_ms = 0.0
     fine_ms = dict.fromkeys(b2g.B2world.PHASES + b2g.B2world.TREE_PHASES, 0.0)
     bytes_total = {}
-    work = {"bp_node_visits": 0, "bp_leaf_checks": 0, "new_pairs": 0, "contacts": 0, "constraints": 0}
+    work = {"bp_node_visits": 0, "bp_leaf_checks": 0, "bp_moved_proxies": 0, "new_pairs": 0, "contacts": 0,
+            "constraints": 0, "hierarchy_rebuilds": 0}
     snap_at = set(int(x) for x in np.linspace(0, args.steps - 1, 4)) if rank == 0 and not args.no_cpu_baseline else set()
     snaps = []
     for k in range(args.steps):
@@ -702,6 +706,7 @@ def main():
         for ph, v in w.get_phase_times(tree_split=True).items():
             fine_ms[ph] += v
         st = w.get_step_stats()  # this step's work counts (outside the timed events)
+        st["hierarchy_rebuilds"] = int(st["hierarchy_age"] == 0)
         for key in work:
             work[key] += st[key]
         for ph, v in bytes_model(st, stats, vi, pi).items():

@@ -455,7 +455,7 @@ def pre_solve_callback(fn):
 class StepStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in ("bp_node_visits", "bp_leaf_checks", "new_pairs", "contacts", "constraints",
                                                "interior_slots", "parts", "colours", "contact_capacity",
-                                               "pair_capacity", "capacity_grows", "reserved")]
+                                               "pair_capacity", "capacity_grows", "hierarchy_age", "bp_moved_proxies")]
 
 
 class Counts(ctypes.Structure):
@@ -657,6 +657,7 @@ def load_library(path=LIB_PATH):
         "b2g_set_graph_capture": [vp, i32],
         "b2g_set_barrier_limit": [vp, ctypes.c_int64],
         "b2g_set_auto_grow": [vp, i32],
+        "b2g_set_hierarchy_max_age": [vp, i32],
         "b2g_debug_hold_barriers": [vp, i32],
         "b2g_get_phase_times": [vp, vp, i32],
         "b2g_get_step_stats": [vp, ctypes.POINTER(StepStats)],
@@ -896,6 +897,10 @@ class B2world:
     def set_auto_grow(self, flag):
         """Contact and pair capacities grow on overflow, the pass repeated exactly (b2g_set_auto_grow)."""
         self._check(self._lib.b2g_set_auto_grow(self._h, int(flag)))
+
+    def set_hierarchy_max_age(self, passes):
+        """Passes the broadphase keeps its hierarchy before a rebuild (0: rebuild every pass)."""
+        self._check(self._lib.b2g_set_hierarchy_max_age(self._h, int(passes)))
 
     def set_barrier_limit(self, cycles):
         """Grid-barrier wait limit of the world's persistent kernels in clock cycles (0: default)."""

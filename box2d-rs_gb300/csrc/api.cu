@@ -174,6 +174,7 @@ struct World {
     int minsep_buffers = 2;  /* position-iteration separation buffers held in d.isl_minsep */
     int barrier_limit_units = 0;  /* grid-barrier wait limit / 1024 cycles (0: the kernels' default) */
     int barrier_hold = 0;         /* test hook: arrivals every grid barrier waits for in vain */
+    int hierarchy_max_age = 16;   /* b2g_set_hierarchy_max_age */
     TapeHost* tape = nullptr;
     LaunchCfg cfg;
     bool cfg_set = false;    /* chosen by the user or the autotuner: no bucket lookup */
@@ -593,6 +594,8 @@ int write_barrier_settings(World* w) {
     if (!w->allocated) return B2G_OK;
     const int v[2] = {w->barrier_limit_units, w->barrier_hold};
     CUDA_OK(w, cudaMemcpyAsync(w->d.cnt + CNT_BARRIER_LIMIT, v, sizeof(v), cudaMemcpyHostToDevice, w->stream));
+    const int age = w->hierarchy_max_age;
+    CUDA_OK(w, cudaMemcpyAsync(w->d.cnt + CNT_BP_MAX_AGE, &age, sizeof(age), cudaMemcpyHostToDevice, w->stream));
     CUDA_OK(w, cudaStreamSynchronize(w->stream));
     return B2G_OK;
 }
@@ -709,6 +712,9 @@ int upload(World* w) {
     U(d.b_fix_off, w->h_fix_off);
     if (nf > 0) U(d.b_fix, w->h_fix);
 #undef U
+    /* proxies may have changed (created, destroyed, moved or re-filtered on the host): the next
+     * broadphase pass rebuilds its hierarchy */
+    CUDA_OK(w, cudaMemsetAsync(d.cnt + CNT_BP_FORCE, 1, sizeof(int), s));
     CUDA_OK(w, cudaStreamSynchronize(s));
     w->uploaded_bodies = nb;
     w->uploaded_fixtures = nf;
@@ -1359,8 +1365,12 @@ void issue_step(World* w, const StepParams& sp, float dt, bool capturing = false
         });
         swap_contacts(w);
         mark(t.e[8]);
-        /* B2world::solve_toi (private/dynamics/b2_world.rs:946-950) */
-        if (w->continuous) launch_continuous(w->d, sp, s, w->num_sms);
+        /* B2world::solve_toi (private/dynamics/b2_world.rs:946-950); the pass moves hierarchy leaves
+         * in place without the four-way records, so the next broadphase pass rebuilds */
+        if (w->continuous) {
+            launch_continuous(w->d, sp, s, w->num_sms);
+            cudaMemsetAsync(w->d.cnt + CNT_BP_FORCE, 1, sizeof(int), s);
+        }
         mark(t.e[5]);
         w->inv_dt0 = sp.inv_dt;
     } else {
@@ -1415,7 +1425,7 @@ int recover_overflow(World* w, const StepParams& sp) {
         int rc = grow_capacities(w, cc, pc);
         if (rc != B2G_OK) return rc;
         launch_touch_all_proxies(w->d, w->stream);
-        launch_broadphase(w->d, sp, w->stream, w->num_sms);
+        launch_broadphase(w->d, sp, w->stream, w->num_sms, nullptr, BP_REPEAT);
         swap_contacts(w);
         CUDA_OK(w, cudaGetLastError());
     }
@@ -2527,6 +2537,13 @@ int b2g_set_barrier_limit(void* p, int64_t cycles) {
     return write_barrier_settings(w);
 }
 
+int b2g_set_hierarchy_max_age(void* p, int32_t passes) {
+    World* w = W(p);
+    if (!w || passes < 0) return B2G_ERR_INVALID_ARG;
+    w->hierarchy_max_age = passes;
+    return write_barrier_settings(w);
+}
+
 int b2g_debug_hold_barriers(void* p, int32_t extra) {
     World* w = W(p);
     if (!w || extra < 0) return B2G_ERR_INVALID_ARG;
@@ -2623,6 +2640,8 @@ int b2g_get_step_stats(void* p, b2g_step_stats* out) {
     out->contact_capacity = w->d.contact_cap;
     out->pair_capacity = w->d.pair_cap;
     out->capacity_grows = w->capacity_grows;
+    out->hierarchy_age = cnt[CNT_BP_AGE];
+    out->bp_moved_proxies = cnt[CNT_BP_LAST_MOVED];
     return B2G_OK;
 }
 
@@ -2884,7 +2903,7 @@ int b2g_state_load(void* p, const void* in, uint64_t bytes) {
     w->device_authoritative = true;
     rc = load_host_state(w, src, end);
     if (rc != B2G_OK) return rc;
-    /* the barrier settings are the world's, not the saved state's */
+    /* the barrier and hierarchy settings are the world's, not the saved state's */
     return write_barrier_settings(w);
 }
 

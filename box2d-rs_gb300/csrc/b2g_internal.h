@@ -120,13 +120,24 @@ enum {
     CNT_TOI_SNAP_EV = 38, /* CNT_EVENTS and CNT_TOI_EVENTS when the pass's snapshot was taken */
     CNT_TOI_SNAP_TE = 39,
     CNT_TOI_LAST = 40,
-    CNT_SIZE = 48
+    /* the broadphase hierarchy: rebuilt, or kept with its moved leaves updated in place */
+    CNT_BP_REBUILD = 48,  /* this pass rebuilds the hierarchy (1) or updates it in place (0) */
+    CNT_BP_AGE = 49,      /* passes since the last rebuild */
+    CNT_BP_MOVED = 50,    /* proxies the solver moved since the last pass (the fixture sync counts them) */
+    CNT_BP_DRIFT = 51,    /* proxies moved since the last rebuild */
+    CNT_BP_FORCE = 52,    /* nonzero: the host changed proxies, the next pass rebuilds */
+    CNT_BP_NF = 53,       /* proxies at the last rebuild */
+    CNT_BP_SORT_N = 54,   /* keys the pass sorts: the proxies on a rebuild, 0 otherwise */
+    CNT_BP_LAST_MOVED = 55, /* proxies the solver moved before the last pass */
+    CNT_BP_MAX_AGE = 56,  /* passes a kept hierarchy may reach before a rebuild (0: rebuild every pass) */
+    CNT_SIZE = 64
 };
 
 constexpr int kMaxColours = 256;   /* first-fit colours 0..63, then one per colouring round */
 constexpr int kFirstFitColours = 64;
 constexpr int kColourTail = 256;   /* uncoloured constraints one block finishes colouring (one per thread) */
 constexpr int kMaxParts = 1024;    /* body parts of the part-local solve (at most one per solver block) */
+constexpr int kKeyMortonBits = 30; /* broadphase keys: key world << 30 | Morton code (15 bits per axis) */
 constexpr int kMaxPosIters = 64;
 constexpr int kNoWake = 0x7f7f7f7f;  /* b_wake's "not woken" (a byte-wise memset value) */
 /* continuous pass lists (k_continuous.cu): partner contacts of one event, events of one
@@ -359,8 +370,11 @@ bool use_parts(const DevWorld& w, int num_sms, bool allowed);
 /* mark (optional) is called with 0 after the keys and their sort, 1 after the hierarchy (build,
  * refit, four-way records, contact rows), 2 after the traversal (before the contact merge), so the
  * caller can record profiling events there */
+/* mode: BP_AUTO (the pass decides whether to rebuild the hierarchy), BP_REBUILD, or BP_REPEAT (the
+ * same pass again, after a capacity overflow: the previous decision holds) */
+enum { BP_AUTO = 0, BP_REBUILD = 1, BP_REPEAT = 2 };
 void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms,
-                       const std::function<void(int)>& mark = nullptr);
+                       const std::function<void(int)>& mark = nullptr, int mode = BP_AUTO);
 void launch_set_transform(const DevWorld& w, int body, float px, float py, float angle, cudaStream_t s);
 void launch_clear_forces(const DevWorld& w, cudaStream_t s);
 void launch_collide_pairs(const ShapeRec* a, const float4* xa, const ShapeRec* b, const float4* xb, const int* kind,

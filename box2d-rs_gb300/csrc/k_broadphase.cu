@@ -6,7 +6,10 @@
  * b2_contact_manager_add_pair (src/private/dynamics/b2_contact_manager.rs:178-302).
  *
  * The reference inserts moved proxies into an incremental AVL-balanced tree and queries
- * it once per moved proxy. Here the tree is rebuilt every pass as a linear BVH:
+ * it once per moved proxy. Here the tree is a linear BVH, rebuilt when a pass decides so
+ * (k_bp_decide: proxies changed on the host, many proxies moved, or the hierarchy is a few
+ * passes old) and otherwise kept, with each moved proxy's leaf set to its new fat AABB and its
+ * ancestors' boxes grown to cover it (k_bp_update). A rebuild:
  *   1. centre bounds of all fat AABBs (atomic min/max on order-preserving ints),
  *   2. 64-bit keys world << 30 | Morton(15-bit x, 15-bit y), radix-sorted with the
  *      fixture index as payload (worlds occupy disjoint key ranges; a static proxy far
@@ -20,6 +23,8 @@
  *   5. one thread per moved proxy walks its world's two subtrees with a short stack and
  *      applies the reference's rule: skip itself; skip a moved partner whose proxy id is
  *      larger (that partner reports the pair); emit (min id, max id).
+ * Which pass rebuilds changes only how many nodes a query visits: boxes of internal nodes only
+ * have to contain their leaves, and leaves hold the exact fat AABBs.
  * The emitted set equals the reference's: every pair of overlapping fat AABBs with at
  * least one moved proxy, each once (b2_test_overlap is closed, so touching boxes pair).
  * add_pair's rejections run inline (same body, no dynamic body, default filter, edge-edge),
@@ -37,7 +42,7 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr int kStack = 64;
-constexpr int kMortonBits = 30;      /* 15 bits of cell per axis */
+constexpr int kMortonBits = kKeyMortonBits;  /* 15 bits of cell per axis */
 constexpr float kCellMax = 32767.0f;
 
 __device__ __forceinline__ int f2ord(float f) {
@@ -55,6 +60,34 @@ __device__ __forceinline__ uint32_t spread16(uint32_t x) {
     return x;
 }
 
+/* Rebuild the hierarchy when the host changed proxies (created, destroyed, edited, or the continuous
+ * pass moved leaves), when more than a quarter of the proxies moved since the last pass or more than
+ * half since the last rebuild (grown boxes make queries visit more nodes), or when the hierarchy is
+ * CNT_BP_MAX_AGE passes old (b2g_set_hierarchy_max_age). The decision depends only on the world's own
+ * state, so a world and its checkpointed copy decide alike. A repeated pass (the same pass run again
+ * after its capacities grew) keeps the decision. */
+__global__ void k_bp_decide(DevWorld w, int mode) {
+    B2G_RETURN_IF_ABORTED(w);
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    int* c = w.cnt;
+    const int n = w.n_fixtures;
+    if (mode == BP_REPEAT) return;
+    const int moved = c[CNT_BP_MOVED];
+    const long long drift = (long long)c[CNT_BP_DRIFT] + moved;
+    const bool rebuild = mode == BP_REBUILD || c[CNT_BP_FORCE] != 0 || c[CNT_BP_NF] != n || c[CNT_BP_AGE] >= c[CNT_BP_MAX_AGE] ||
+                         4LL * moved > n || 2LL * drift > n;
+    c[CNT_BP_REBUILD] = rebuild ? 1 : 0;
+    c[CNT_BP_SORT_N] = rebuild ? n : 0;
+    c[CNT_BP_AGE] = rebuild ? 0 : c[CNT_BP_AGE] + 1;
+    c[CNT_BP_DRIFT] = rebuild ? 0 : (int)drift;
+    c[CNT_BP_NF] = n;
+    c[CNT_BP_FORCE] = 0;
+    c[CNT_BP_LAST_MOVED] = moved;
+    c[CNT_BP_MOVED] = 0;
+}
+
+__device__ __forceinline__ bool bp_rebuilding(const DevWorld& w) { return w.cnt[CNT_BP_REBUILD] != 0; }
+
 __global__ void k_bp_init(DevWorld w) {
     B2G_RETURN_IF_ABORTED(w);
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -69,6 +102,7 @@ __global__ void k_bp_init(DevWorld w) {
         w.cnt[CNT_BP_VISITS] = 0;
         w.cnt[CNT_BP_CANDIDATES] = 0;
     }
+    if (!bp_rebuilding(w)) return;
     for (int i = t; i < 2 * w.num_worlds; i += gridDim.x * blockDim.x) {
         w.bp_world_first[i] = -1;
         w.bp_world_root[i] = INT_MIN;
@@ -77,6 +111,7 @@ __global__ void k_bp_init(DevWorld w) {
 
 __global__ void k_bp_bounds(DevWorld w) {
     B2G_RETURN_IF_ABORTED(w);
+    if (!bp_rebuilding(w)) return;
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x)
         w.b_rank[b] = INT_MAX;
     int mnx = INT_MAX, mny = INT_MAX, mxx = INT_MIN, mxy = INT_MIN, dyn = 0;
@@ -110,6 +145,7 @@ __global__ void k_bp_bounds(DevWorld w) {
 
 __global__ void k_bp_keys(DevWorld w) {
     B2G_RETURN_IF_ABORTED(w);
+    if (!bp_rebuilding(w)) return;
     float lx = 0.0f, ly = 0.0f, sx = 0.0f, sy = 0.0f;
     if (w.cnt[CNT_BOUNDS + 0] != INT_MAX) {
         lx = ord2f(w.cnt[CNT_BOUNDS + 0]);
@@ -150,6 +186,7 @@ __device__ __forceinline__ int delta(const unsigned long long* k, int n, int i, 
 /* Karras, "Maximizing parallelism in the construction of BVHs, octrees, and k-d trees" (HPG 2012) */
 __global__ void k_bp_build(DevWorld w) {
     B2G_RETURN_IF_ABORTED(w);
+    if (!bp_rebuilding(w)) return;
     const int n = w.n_fixtures;
     const unsigned long long* k = w.bp_key;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
@@ -188,12 +225,13 @@ __global__ void k_bp_build(DevWorld w) {
 
 __global__ void k_bp_leaves(DevWorld w) {
     B2G_RETURN_IF_ABORTED(w);
+    if (!bp_rebuilding(w)) return;
     const int n = w.n_fixtures;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const uint32_t f = w.bp_val[p];
         w.bp_leaf[p] = w.f_fat[f];
+        w.f_leaf[f] = p;
         atomicMin(&w.b_rank[w.f_body[f]], p);  /* the body's Morton rank: its first proxy's position */
-        w.rank_x[p] = 0ull;                      /* the colouring weighs ranks by constraints */
         const uint32_t wd = (uint32_t)(w.bp_key[p] >> kMortonBits);
         const bool first = p == 0 || (uint32_t)(w.bp_key[p - 1] >> kMortonBits) != wd;
         const bool last = p == n - 1 || (uint32_t)(w.bp_key[p + 1] >> kMortonBits) != wd;
@@ -208,6 +246,7 @@ __device__ __forceinline__ float4 box_union(float4 a, float4 b) {
 
 __global__ void k_bp_refit(DevWorld w) {
     B2G_RETURN_IF_ABORTED(w);
+    if (!bp_rebuilding(w)) return;
     const int n = w.n_fixtures;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         if (n < 2) break;
@@ -237,6 +276,7 @@ __device__ __forceinline__ bool box_overlap(float4 a, float4 b) { return overlap
  * levels at a time; the pairs found do not depend on the hierarchy's shape. */
 __global__ void k_bp_quad(DevWorld w) {
     B2G_RETURN_IF_ABORTED(w);
+    if (!bp_rebuilding(w)) return;
     const int n = w.n_fixtures;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
         const int2 ch = w.bp_node_child[i];
@@ -261,6 +301,89 @@ __global__ void k_bp_quad(DevWorld w) {
         for (; m < 4; ++m) qb[m] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         w.bp_quad_child[i] = make_int4(ids[0], ids[1], ids[2], ids[3]);
         for (int j = 0; j < 4; ++j) w.bp_quad_box[4 * (size_t)i + j] = qb[j];
+    }
+}
+
+/* componentwise growth of a stored box; returns whether this call changed it */
+__device__ __forceinline__ bool grow_lo(float* p, float v) {
+    int old = __float_as_int(*(volatile float*)p);
+    bool changed = false;
+    while (v < __int_as_float(old)) {
+        const int prev = atomicCAS((int*)p, old, __float_as_int(v));
+        if (prev == old) {
+            changed = true;
+            break;
+        }
+        old = prev;
+    }
+    return changed;
+}
+__device__ __forceinline__ bool grow_hi(float* p, float v) {
+    int old = __float_as_int(*(volatile float*)p);
+    bool changed = false;
+    while (v > __int_as_float(old)) {
+        const int prev = atomicCAS((int*)p, old, __float_as_int(v));
+        if (prev == old) {
+            changed = true;
+            break;
+        }
+        old = prev;
+    }
+    return changed;
+}
+__device__ __forceinline__ bool grow_box(float4* slot, float4 b) {
+    const bool x0 = grow_lo(&slot->x, b.x);
+    const bool y0 = grow_lo(&slot->y, b.y);
+    const bool x1 = grow_hi(&slot->z, b.z);
+    const bool y1 = grow_hi(&slot->w, b.w);
+    return x0 || y0 || x1 || y1;
+}
+/* the place of child id in node's four-way record (-1 if absent) */
+__device__ __forceinline__ int quad_place(const DevWorld& w, int node, int id) {
+    const int4 q = w.bp_quad_child[node];
+    return q.x == id ? 0 : q.y == id ? 1 : q.z == id ? 2 : q.w == id ? 3 : -1;
+}
+
+/* A pass that keeps the hierarchy: every moved proxy's leaf takes its new fat AABB exactly (the leaf
+ * box, its parent's record of it and the four-way records of its parent and grandparent), and each
+ * ancestor's record grows to cover it (the binary record in its parent and the four-way record in its
+ * grandparent). A walk stops at the first ancestor whose record already covered the box: whoever grew
+ * that record past it carries the growth further up, so when the kernel ends every ancestor covers
+ * every leaf below it. */
+__global__ void k_bp_update(DevWorld w) {
+    B2G_RETURN_IF_ABORTED(w);
+    if (bp_rebuilding(w)) return;
+    const int n = w.n_fixtures;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
+        if (!w.f_moved[f]) continue;
+        const int l = w.f_leaf[f];
+        if (l < 0 || l >= n) continue;
+        const float4 box = w.f_fat[f];
+        w.bp_leaf[l] = box;
+        if (n < 2) continue;
+        const int n1 = w.bp_parent[n - 1 + l];
+        const int2 c1 = w.bp_node_child[n1];
+        if (c1.x == ~l) w.bp_node_b0[n1] = box; else w.bp_node_b1[n1] = box;
+        int k = quad_place(w, n1, ~l);
+        if (k >= 0) w.bp_quad_box[4 * (size_t)n1 + k] = box;
+        if (n1 != 0) {
+            const int n2 = w.bp_parent[n1];
+            k = quad_place(w, n2, ~l);
+            if (k >= 0) w.bp_quad_box[4 * (size_t)n2 + k] = box;
+        }
+        int x = n1;
+        for (int guard = 0; guard < 128 && x != 0; ++guard) {
+            const int px = w.bp_parent[x];
+            const int2 pc = w.bp_node_child[px];
+            const bool changed = grow_box(pc.x == x ? &w.bp_node_b0[px] : &w.bp_node_b1[px], box);
+            if (px != 0) {
+                const int gp = w.bp_parent[px];
+                k = quad_place(w, gp, x);
+                if (k >= 0) grow_box(&w.bp_quad_box[4 * (size_t)gp + k], box);
+            }
+            if (!changed) break;
+            x = px;
+        }
     }
 }
 
@@ -464,9 +587,14 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
     }
 }
 
+/* the moved flags are consumed; the colouring's rank weights start from zero (they are indexed by
+ * Morton rank, of which there are as many as proxies) */
 __global__ void k_bp_clear_moved(DevWorld w) {
     B2G_RETURN_IF_ABORTED(w);
-    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < w.n_fixtures; f += gridDim.x * blockDim.x) w.f_moved[f] = 0;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < w.n_fixtures; f += gridDim.x * blockDim.x) {
+        w.f_moved[f] = 0;
+        w.rank_x[f] = 0ull;
+    }
 }
 
 __global__ void k_bp_clamp_new(DevWorld w) {
@@ -541,15 +669,16 @@ void launch_touch_all_proxies(const DevWorld& w, cudaStream_t s) {
 
 /* Runs update_pairs + add_pair and merges: the caller swaps w.c and w.c_alt afterwards. */
 void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, int num_sms,
-                       const std::function<void(int)>& mark) {
+                       const std::function<void(int)>& mark, int mode) {
     const int n = w.n_fixtures;
     const int gf = grid_for(n, kBlock, num_sms * 8);
+    k_bp_decide<<<1, 32, 0, s>>>(w, mode); B2G_LAUNCHED(1);
     k_bp_init<<<grid_for(2 * w.num_worlds, kBlock, 64), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
     if (n > 0) {
         k_bp_bounds<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_keys<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
-        radix_sort_pairs_coop(w.bp_key, w.bp_val, w.bp_key_alt, w.bp_val_alt, nullptr, n, kMortonBits + w.morton_world_bits,
-                              w.sort_hist, w.cnt, s, num_sms);
+        radix_sort_pairs_coop(w.bp_key, w.bp_val, w.bp_key_alt, w.bp_val_alt, &w.cnt[CNT_BP_SORT_N], n,
+                              kMortonBits + w.morton_world_bits, w.sort_hist, w.cnt, s, num_sms);
         if (mark) mark(0);
         if (n > 1) {
             k_bp_build<<<grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
@@ -559,6 +688,7 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
         if (n > 1) {
             k_bp_quad<<<grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         }
+        k_bp_update<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_rows<<<grid_for(w.contact_cap, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         if (mark) mark(1);
         const int tb = w.cfg_traverse_block;

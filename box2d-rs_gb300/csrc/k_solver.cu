@@ -383,11 +383,26 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
             block_scan_excl64(every, &all);
         }
         const unsigned long long wtot = all >> 32;
+        /* A batch of worlds cuts only at world boundaries: a world's bodies all take the part of the
+         * weight prefix at the world's first rank (ranks are grouped by world), so no constraint
+         * joins two parts, there are no boundary colours, and the parts never wait for each other.
+         * That needs the prefix at any rank: the chunks' prefixes are made global first. */
+        const bool aligned = w.num_worlds > 1;
+        if (aligned) {
+            for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) w.rank_x[r] += before;
+            if (!grid_barrier(w)) return;
+        }
+        const unsigned long long base_x = aligned ? 0ull : before;
         for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-            const unsigned long long x = before + w.rank_x[r];
-            const unsigned long long x1 = before + (r + 1 < r1 ? w.rank_x[r + 1] : carry);
+            const unsigned long long x = base_x + w.rank_x[r];
+            const unsigned long long x1 = r + 1 < r1 ? base_x + w.rank_x[r + 1] : before + carry;
             if ((uint32_t)x1 == (uint32_t)x || wtot == 0ull) continue;  /* no constraint at this rank */
-            const int part = min(P - 1, (int)(((x >> 32) * (unsigned long long)P) / wtot));
+            unsigned long long px = x;
+            if (aligned) {
+                const int first = w.bp_world_first[(uint32_t)(w.bp_key[r] >> kKeyMortonBits)];
+                if (first >= 0 && first <= r) px = w.rank_x[first];
+            }
+            const int part = min(P - 1, (int)(((px >> 32) * (unsigned long long)P) / wtot));
             const int c = (int)(uint32_t)x;
             if (c >= nf) continue;  /* cannot happen: at most one constraint body per rank */
             const int b = w.f_body[w.bp_val[r]];
@@ -402,7 +417,12 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
             const int part = w.b_part[w.cache_body[c]];
             if (c == 0 || w.b_part[w.cache_body[c - 1]] != part) {
                 w.part_cbeg[part] = c;
-                if (part > 0) w.part_rbeg[part] = w.b_rank[w.cache_body[c]];
+                int rb = w.b_rank[w.cache_body[c]];
+                if (w.num_worlds > 1) {  /* whole worlds: the range starts at the world's first rank */
+                    const int first = w.bp_world_first[(uint32_t)(w.bp_key[rb] >> kKeyMortonBits)];
+                    if (first >= 0 && first <= rb) rb = first;
+                }
+                if (part > 0) w.part_rbeg[part] = rb;
             }
             if (c == ncache - 1 || w.b_part[w.cache_body[c + 1]] != part) w.part_cend[part] = c + 1;
         }
@@ -1159,21 +1179,28 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
         uint32_t* cur = w.isl_minsep + (size_t)it * w.body_cap;
         if (parts) {
             /* the interior colours, then a barrier: islands span parts, and the next iteration's
-             * early exit reads this iteration's buffer */
+             * early exit reads this iteration's buffer. Without boundary constraints (a batch cut at
+             * world boundaries) no island spans two parts: each part's islands are written by its
+             * own block alone, so the iterations need no grid barrier until the positions go back. */
             if (it > 0) {
                 part_done_flags(w, pc, nbnd, it, tol);
                 __syncthreads();
             }
             part_pos_sweeps(w, pc, it, cur, tol);
-            part_store(pc, w.b_pos);
-            if (!grid_barrier(w)) return;
-            for (int c = 0; c < ncol; ++c) {
-                bnd_pos_sweep(w, pc, c, it, cur, tol);
+            if (ncol > 0) {
+                part_store(pc, w.b_pos);
                 if (!grid_barrier(w)) return;
-            }
-            if (it < sp.pi - 1) {
-                part_load(pc, w.b_pos);
-                __syncthreads();
+                for (int c = 0; c < ncol; ++c) {
+                    bnd_pos_sweep(w, pc, c, it, cur, tol);
+                    if (!grid_barrier(w)) return;
+                }
+                if (it < sp.pi - 1) {
+                    part_load(pc, w.b_pos);
+                    __syncthreads();
+                }
+            } else if (it == sp.pi - 1) {
+                part_store(pc, w.b_pos);
+                if (!grid_barrier(w)) return;
             }
             continue;
         }
@@ -1250,7 +1277,9 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
         }
     }
     if (!grid_barrier(w)) return;
-    /* phase 6b: synchronize fixtures (private/dynamics/b2_body.rs:455-475) */
+    /* phase 6b: synchronize fixtures (private/dynamics/b2_body.rs:455-475); the proxies moved are
+     * counted for the broadphase's rebuild decision */
+    unsigned moved = 0;
     for (int f = gtid; f < w.n_fixtures; f += gsize) {
         const int b = w.f_body[f];
         const uint32_t bf = w.b_flags[b];
@@ -1267,8 +1296,10 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
             xf1.q = rot(p0.z);
             xf1.p = sub(mk(p0.x, p0.y), mul(xf1.q, mk(lc.x, lc.y)));
         }
-        sync_fixture(w, f, xf1, xf2);
+        if (sync_fixture(w, f, xf1, xf2)) ++moved;
     }
+    moved = __reduce_add_sync(0xffffffffu, moved);
+    if ((threadIdx.x & 31) == 0 && moved) atomicAdd(&w.cnt[CNT_BP_MOVED], (int)moved);
 }
 
 __global__ void k_sleep_init(DevWorld w) {
@@ -1337,16 +1368,18 @@ int part_count(const DevWorld& w, int num_sms) {
     return std::max(1, std::min(std::min(num_sms, kMaxParts), w.n_fixtures / 256));
 }
 
-/* The part-local solve pays off while a part's bodies and constraints fit its block's shared
- * memory; a large batch of worlds (thousands of proxies per SM) keeps the grid-wide colour sweeps,
- * which spread each colour over every thread of the GPU. */
+/* In one world the part-local solve pays off while a part's bodies and constraints fit its block's
+ * shared memory; a larger world (thousands of proxies per SM) keeps the grid-wide colour sweeps,
+ * which spread each colour over every thread of the GPU. A batch of worlds is cut at world
+ * boundaries (no boundary colours, no grid barrier inside the sweeps), so it takes parts at any
+ * size: what its cache does not hold a part's block reads in global memory. */
 constexpr int kPartMaxProxiesPerSm = 2048;
 
 bool use_parts(const DevWorld& w, int num_sms, bool allowed) {
     /* joints are solved grid-wide before each contact sweep, so a world with joints runs the
      * grid-wide colour schedule */
     return allowed && w.n_joints == 0 && w.n_fixtures > 0 &&
-           (long long)w.n_fixtures <= (long long)num_sms * kPartMaxProxiesPerSm;
+           (w.num_worlds > 1 || (long long)w.n_fixtures <= (long long)num_sms * kPartMaxProxiesPerSm);
 }
 
 void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms, bool parts) {

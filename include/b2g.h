@@ -330,11 +330,14 @@ int b2g_get_counts(void* world, b2g_counts* out);         /* get_body_count / ge
  * B2Profile holds times only): hierarchy nodes the broadphase traversal fetched and leaves it
  * checked, new contacts it found, the contact table's size, constraint slots solved (of them
  * part-locally), the parts and colours of the colouring; the contact and pair capacities and how
- * often they grew (b2g_set_auto_grow). */
+ * often they grew (b2g_set_auto_grow); the broadphase hierarchy's age (0: the last pass rebuilt it; else
+ * the passes since, which kept it and updated the moved proxies' leaves in place) and the proxies the
+ * step's solver moved (the traversal's queries). */
 typedef struct b2g_step_stats {
     int32_t bp_node_visits, bp_leaf_checks, new_pairs, contacts;
     int32_t constraints, interior_slots, parts, colours;
-    int32_t contact_capacity, pair_capacity, capacity_grows, reserved;
+    int32_t contact_capacity, pair_capacity, capacity_grows, hierarchy_age;
+    int32_t bp_moved_proxies;
 } b2g_step_stats;
 int b2g_get_step_stats(void* world, b2g_step_stats* out);
 /* Exact checkpoint and resume (not in the reference's API, which serialises a world through serde,
@@ -451,6 +454,13 @@ int b2g_set_barrier_limit(void* world, int64_t cycles);
  * the world then continues bit for bit as one created with the larger capacities. The reference grows
  * its containers on the host as needed; here each step with it on waits for the device once. */
 int b2g_set_auto_grow(void* world, int32_t flag);
+/* The broadphase keeps its hierarchy between passes and updates only the moved proxies' leaves (their
+ * ancestors' boxes grow to cover them); it rebuilds when proxies were created, destroyed or edited on
+ * the host, when many proxies moved, or when the hierarchy is `passes` passes old (default 16; 0
+ * rebuilds every pass). The pairs found never depend on it (the reference's dynamic tree is likewise
+ * updated per moved proxy, b2_dynamic_tree.rs:109-168); with the part-local solve the solve order
+ * follows the hierarchy's Morton order, so the result bits do (b2g_get_solver_order exports it). */
+int b2g_set_hierarchy_max_age(void* world, int32_t passes);
 /* Test hook for the timeout path: every grid barrier of the world's kernels also waits for
  * `extra` arrivals that never come, so each wait runs out its limit (0 turns it off). */
 int b2g_debug_hold_barriers(void* world, int32_t extra);
