@@ -225,22 +225,25 @@ def timed_steps(world, scene, steps, flush, torch):
 
 
 def tune_blocks_per_sm(torch, flush, t, dt, vi, pi, turns=3, steps=3):
-    """After b2g_autotune (which times back-to-back steps): choose the persistent kernels' blocks
-    per SM on the scratch world `t` the way this bench times a step (device time, L2 flushed before
-    it); the two settings take turns. Returns the launch configuration to use."""
+    """After b2g_autotune (which times back-to-back steps): choose the persistent kernels' shape
+    (blocks per SM, and the solver's threads per block at one block per SM) on the scratch world `t`
+    the way this bench times a step (device time, L2 flushed before it); the settings take turns.
+    Returns the launch configuration to use."""
     base = t.get_launch_config()
-    total = {1: 0.0, 2: 0.0}
+    shapes = [(1, 256), (1, 512), (2, 256)]
+    total = dict.fromkeys(shapes, 0.0)
     for _ in range(turns):
-        for c in (1, 2):
-            t.set_launch_config(c, base["collide_block"], base["traverse_block"])
+        for c, sb in shapes:
+            t.set_launch_config(c, base["collide_block"], base["traverse_block"], sb)
             for _ in range(2):  # the step graph's captures for both contact-buffer parities
                 t.step(dt, vi, pi)
             for _ in range(steps):
                 flush.fill_(1.0)
                 torch.cuda.synchronize()
                 t.step(dt, vi, pi)
-                total[c] += t.get_profile()["step"]  # device time (CUDA events), as timed_steps
-    return dict(base, coop_blocks_per_sm=min(total, key=total.get))
+                total[(c, sb)] += t.get_profile()["step"]  # device time (CUDA events), as timed_steps
+    c, sb = min(total, key=total.get)
+    return dict(base, coop_blocks_per_sm=c, solver_block=sb)
 
 
 def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_bucket=6, rank=0, world_size=1,
@@ -694,7 +697,7 @@ def main():
     fine_ms = dict.fromkeys(b2g.B2world.PHASES + b2g.B2world.TREE_PHASES, 0.0)
     bytes_total = {}
     work = {"bp_node_visits": 0, "bp_leaf_checks": 0, "bp_moved_proxies": 0, "new_pairs": 0, "contacts": 0,
-            "constraints": 0, "hierarchy_rebuilds": 0}
+            "constraints": 0, "interior_slots": 0, "colours": 0, "hierarchy_rebuilds": 0}
     snap_at = set(int(x) for x in np.linspace(0, args.steps - 1, 4)) if rank == 0 and not args.no_cpu_baseline else set()
     snaps = []
     for k in range(args.steps):

@@ -66,7 +66,7 @@ struct GraphSlot {
 /* launch configuration: the user's (b2g_set_launch_config), else the autotuner's choice for the
  * world's size bucket if one was made in this process, else the defaults */
 struct LaunchCfg {
-    int coop_per_sm = 1, collide_block = 128, traverse_block = 256;
+    int coop_per_sm = 1, collide_block = 128, traverse_block = 256, solver_block = 256;
 };
 
 std::mutex g_tune_mutex;
@@ -209,6 +209,7 @@ void apply_launch_config(World* w) {
     w->d.cfg_coop_per_sm = w->cfg.coop_per_sm;
     w->d.cfg_collide_block = w->cfg.collide_block;
     w->d.cfg_traverse_block = w->cfg.traverse_block;
+    w->d.cfg_solver_block = w->cfg.coop_per_sm == 1 ? w->cfg.solver_block : 256;
 }
 
 
@@ -3430,6 +3431,7 @@ int b2g_get_launch_config(void* p, b2g_launch_config* out) {
     out->collide_block = w->cfg.collide_block;
     out->traverse_block = w->cfg.traverse_block;
     out->tuning_steps = w->tuning_steps;
+    out->solver_block = w->cfg.solver_block;
     return B2G_OK;
 }
 
@@ -3437,12 +3439,15 @@ int b2g_set_launch_config(void* p, const b2g_launch_config* c) {
     World* w = W(p);
     if (!w || !c) return B2G_ERR_INVALID_ARG;
     auto pow2 = [](int v, int lo, int hi) { return v >= lo && v <= hi && (v & (v - 1)) == 0; };
+    const int sb = c->solver_block == 0 ? 256 : c->solver_block;
     if (c->coop_blocks_per_sm < 1 || c->coop_blocks_per_sm > 2 || !pow2(c->collide_block, 32, 256) ||
-        !pow2(c->traverse_block, 32, 256))
-        return fail(w, B2G_ERR_INVALID_ARG, "coop_blocks_per_sm in {1, 2}; block sizes powers of two in [32, 256]");
+        !pow2(c->traverse_block, 32, 256) || (sb != 256 && sb != 512))
+        return fail(w, B2G_ERR_INVALID_ARG,
+                    "coop_blocks_per_sm in {1, 2}; block sizes powers of two in [32, 256]; solver_block 256 or 512");
     w->cfg.coop_per_sm = c->coop_blocks_per_sm;
     w->cfg.collide_block = c->collide_block;
     w->cfg.traverse_block = c->traverse_block;
+    w->cfg.solver_block = sb;
     w->cfg_set = true;
     apply_launch_config(w);
     drop_graphs(w);
@@ -3487,7 +3492,7 @@ int b2g_autotune(void* p, float dt, int32_t vi, int32_t pi, int32_t steps_per_ca
     if (w->h_flags.empty()) return fail(w, B2G_ERR_INVALID_ARG, "the world has no bodies");
     LaunchCfg best = w->cfg;
     w->cfg_set = true;
-    const int coop[] = {1, 2}, collide[] = {64, 128, 256}, traverse[] = {64, 128, 256};
+    const int coop[] = {1, 2}, collide[] = {64, 128, 256}, traverse[] = {64, 128, 256}, solver[] = {256, 512};
     /* the part-local solve caches a part in its block's shared memory: one block per SM */
     const int ncoop = use_parts(w->d, w->num_sms, w->part_solve) ? 1 : 2;
     /* the world keeps evolving while candidates are timed, so the candidates take turns over
@@ -3495,18 +3500,22 @@ int b2g_autotune(void* p, float dt, int32_t vi, int32_t pi, int32_t steps_per_ca
     const int rounds = std::max(1, std::min(steps_per_candidate / 2, 4));
     const int per_round = std::max(1, steps_per_candidate / rounds);
     int tuned = 0;
-    for (int knob = 0; knob < 3; ++knob) {
-        const int* cand = knob == 0 ? coop : knob == 1 ? collide : traverse;
-        const int nc = knob == 0 ? ncoop : 3;
+    auto field = [](LaunchCfg& c, int knob) -> int& {
+        return knob == 0 ? c.coop_per_sm : knob == 1 ? c.collide_block : knob == 2 ? c.traverse_block : c.solver_block;
+    };
+    for (int knob = 0; knob < 4; ++knob) {
+        const int* cand = knob == 0 ? coop : knob == 1 ? collide : knob == 2 ? traverse : solver;
+        /* 512 solver threads only with one block per SM (the registers of two would not fit) */
+        const int nc = knob == 0 ? ncoop : knob == 3 ? (best.coop_per_sm == 1 ? 2 : 1) : 3;
         if (nc == 1) {
-            (knob == 0 ? best.coop_per_sm : knob == 1 ? best.collide_block : best.traverse_block) = cand[0];
+            field(best, knob) = cand[0];
             continue;
         }
         double total[3] = {0.0, 0.0, 0.0};
         for (int r = 0; r < rounds; ++r) {
             for (int i = 0; i < nc; ++i) {
                 LaunchCfg c = best;
-                (knob == 0 ? c.coop_per_sm : knob == 1 ? c.collide_block : c.traverse_block) = cand[i];
+                field(c, knob) = cand[i];
                 w->cfg = c;
                 apply_launch_config(w);
                 drop_graphs(w);
@@ -3522,7 +3531,7 @@ int b2g_autotune(void* p, float dt, int32_t vi, int32_t pi, int32_t steps_per_ca
         int best_i = 0;
         for (int i = 1; i < nc; ++i)
             if (total[i] < total[best_i]) best_i = i;
-        (knob == 0 ? best.coop_per_sm : knob == 1 ? best.collide_block : best.traverse_block) = cand[best_i];
+        field(best, knob) = cand[best_i];
     }
     w->cfg = best;
     w->tuning_steps = tuned;

@@ -185,6 +185,7 @@ struct DevWorld {
     int cfg_coop_per_sm;      /* blocks per SM of the cooperative colouring and solver kernels */
     int cfg_collide_block;    /* threads per block of the narrowphase */
     int cfg_traverse_block;   /* threads per block of the broadphase traversal */
+    int cfg_solver_block;     /* threads per block of the persistent solver (256, or 512 at one block per SM) */
     int n_bodies, n_fixtures, num_worlds;
     int num_sms;              /* multiprocessors of the world's device (grid caps of the launchers) */
     int key_bits;      /* bits of the contact key (2 x refid bits) */

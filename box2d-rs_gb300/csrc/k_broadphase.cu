@@ -411,16 +411,32 @@ __global__ void k_bp_rows(DevWorld w) {
 
 /* A live contact with this key exists: a short scan of the key's row instead of a binary search
  * over the whole table (the check the reference makes by walking body B's contact list,
- * private/dynamics/b2_contact_manager.rs:199-224). */
+ * private/dynamics/b2_contact_manager.rs:199-224). A long row (a ground touching a whole layer of
+ * a pile) continues with a galloping search, so no check scans more than a few keys. */
+constexpr int kRowScan = 8;
+
 __device__ __forceinline__ bool contact_exists(const DevWorld& w, uint32_t lo, unsigned long long key, int n_contacts) {
     const int start = w.c_row[lo];
     if (start < 0 || start >= n_contacts || (w.c.key[start] >> w.key_bits) != lo) return false;
-    for (int i = start; i < n_contacts; ++i) {
+    const int scan_end = min(n_contacts, start + kRowScan);
+    for (int i = start; i < scan_end; ++i) {
         const unsigned long long k = w.c.key[i];
         if (k >= key) return k == key && !(w.c.flags[i] & CF_DEAD);
         if ((k >> w.key_bits) != lo) return false;
     }
-    return false;
+    /* keys [start, scan_end) are below `key`: gallop to a bound, then binary search */
+    int lo_i = scan_end, step = kRowScan, hi_i = scan_end;
+    while (hi_i < n_contacts && w.c.key[hi_i] < key) {
+        lo_i = hi_i + 1;
+        hi_i += step;
+        step <<= 1;
+    }
+    hi_i = min(hi_i, n_contacts);
+    while (lo_i < hi_i) {
+        const int mid = (lo_i + hi_i) >> 1;
+        if (w.c.key[mid] < key) lo_i = mid + 1; else hi_i = mid;
+    }
+    return lo_i < n_contacts && w.c.key[lo_i] == key && !(w.c.flags[lo_i] & CF_DEAD);
 }
 
 __device__ void handle_pair(const DevWorld& w, const StepParams& sp, int f, int g, uint32_t rf, int n_contacts) {

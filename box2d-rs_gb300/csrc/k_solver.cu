@@ -43,8 +43,35 @@ static_assert(kBlock == kMaxColours, "the colouring scans one histogram row of k
 __device__ __forceinline__ bool is_dynamic(uint32_t flags) { return (flags & BF_TYPE_MASK) == BODY_DYNAMIC; }
 __device__ __forceinline__ bool is_static(uint32_t flags) { return (flags & BF_TYPE_MASK) == BODY_STATIC; }
 
+/* Atomics on per-island words, aggregated over the lanes of a warp that execute them together: a
+ * pile that is one large island would otherwise send every constraint's update to the same word,
+ * and same-address atomics are serialised. Each lane calls once; the lanes with the same island
+ * combine their values and one of them updates the word (a zero value updates nothing). */
+__device__ __forceinline__ void agg_atomic_max(unsigned* words, int key, unsigned v) {
+    const unsigned peers = __match_any_sync(__activemask(), key);
+    const unsigned m = __reduce_max_sync(peers, v);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 && m != 0u) atomicMax(&words[key], m);
+}
+__device__ __forceinline__ void agg_atomic_or(unsigned* words, int key, unsigned v) {
+    const unsigned peers = __match_any_sync(__activemask(), key);
+    const unsigned m = __reduce_or_sync(peers, v);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 && m != 0u) atomicOr(&words[key], m);
+}
+__device__ __forceinline__ void agg_atomic_min(unsigned* words, int key, unsigned v) {
+    const unsigned peers = __match_any_sync(__activemask(), key);
+    const unsigned m = __reduce_min_sync(peers, v);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicMin(&words[key], m);
+}
+/* a counter incremented by every lane that executes this */
+__device__ __forceinline__ void agg_increment(int* counter) {
+    const unsigned act = __activemask();
+    if ((int)(threadIdx.x & 31) == __ffs(act) - 1) atomicAdd(counter, __popc(act));
+}
 
 /* ---------------- islands ---------------- */
+/* Other SMs relink roots during the union pass, and a link cached in this SM's L1 may still show
+ * a root that is no longer one: a find can stop early, at an ancestor. uf_union therefore goes on
+ * from the parent a failed link returns (read in L2), so every retry climbs at least one link. */
 __device__ __forceinline__ int uf_find(int* parent, int x) {
     int p = parent[x];
     while (p != x) {
@@ -56,13 +83,16 @@ __device__ __forceinline__ int uf_find(int* parent, int x) {
     return x;
 }
 
+/* link the larger root under the smaller; a failed link continues from the parent it found */
 __device__ __forceinline__ void uf_union(int* parent, int a, int b) {
-    for (int guard = 0; guard < 1 << 20; ++guard) {
-        a = uf_find(parent, a);
-        b = uf_find(parent, b);
-        if (a == b) return;
+    a = uf_find(parent, a);
+    b = uf_find(parent, b);
+    for (int guard = 0; guard < 1 << 20 && a != b; ++guard) {
         const int hi = a > b ? a : b, lo = a > b ? b : a;
-        if (atomicCAS(&parent[hi], hi, lo) == hi) return;
+        const int old = atomicCAS(&parent[hi], hi, lo);
+        if (old == hi) return;
+        a = uf_find(parent, old);
+        b = uf_find(parent, lo);
     }
 }
 
@@ -102,7 +132,7 @@ __global__ void k_island_compress(DevWorld w) {
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x) {
         const int r = uf_find(w.b_island, b);
         const uint32_t f = w.b_flags[b];
-        if ((f & BF_AWAKE) && (f & BF_ENABLED) && !is_static(f)) atomicOr(&w.isl_minsep[w.body_cap + r], 1u);
+        agg_atomic_or(w.isl_minsep + w.body_cap, r, ((f & BF_AWAKE) && (f & BF_ENABLED) && !is_static(f)) ? 1u : 0u);
     }
 }
 
@@ -557,7 +587,7 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
                 }
                 w.cons_colour[k] = colour;
             } else {
-                atomicAdd(&w.cnt[CNT_UNCOLOURED + (round & 1)], 1);
+                agg_increment(&w.cnt[CNT_UNCOLOURED + (round & 1)]);
             }
         }
         ++round;
@@ -849,7 +879,7 @@ __device__ void bnd_pos_sweep(const DevWorld& w, const PartCtx& pc, int c, int i
         const float ms = solve_position_math(sl, pa, pb);
         if (sl.idx.w & 1) w.b_pos[sl.idx.x] = pa;
         if (sl.idx.w & 2) w.b_pos[sl.idx.y] = pb;
-        if (ms < 0.0f) atomicMax(&cur[sl.island], __float_as_uint(-ms));
+        agg_atomic_max(cur, sl.island, ms < 0.0f ? __float_as_uint(-ms) : 0u);
     }
 }
 
@@ -931,7 +961,7 @@ __device__ void part_pos_sweeps(const DevWorld& w, const PartCtx& pc, int it, ui
             const float ms = solve_position_math(sl, pa, pb);
             if (sl.idx.w & 1) st_body(pc.state, w.b_pos, sl.idx.x, pa);
             if (sl.idx.w & 2) st_body(pc.state, w.b_pos, sl.idx.y, pb);
-            if (ms < 0.0f) atomicMax(&cur[sl.island], __float_as_uint(-ms));
+            agg_atomic_max(cur, sl.island, ms < 0.0f ? __float_as_uint(-ms) : 0u);
         }
         __syncthreads();
     }
@@ -951,7 +981,10 @@ __device__ __forceinline__ void part_load(const PartCtx& pc, const float4* glob)
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
+/* k_solve runs 256 or 512 threads per block (cfg_solver_block); nothing in it depends on which */
+constexpr int kSolveMaxBlock = 512;
+
+__global__ void __launch_bounds__(kSolveMaxBlock) k_solve(DevWorld w, StepParams sp) {
     B2G_RETURN_IF_ABORTED(w);
     grid_barrier_start();
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1213,7 +1246,7 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
                     done = __uint_as_float(w.isl_minsep[(size_t)j * w.body_cap + isl]) <= tol;
                 if (done) continue;
                 const float ms = solve_position_slot(w, k);
-                if (ms < 0.0f) atomicMax(&cur[isl], __float_as_uint(-ms));
+                agg_atomic_max(cur, isl, ms < 0.0f ? __float_as_uint(-ms) : 0u);
             }
             if (!grid_barrier(w)) return;
         }
@@ -1255,7 +1288,7 @@ __global__ void __launch_bounds__(kBlock) k_solve(DevWorld w, StepParams sp) {
                     st = v.w;
                 }
                 w.b_vel[b] = v;
-                atomicMin((unsigned*)&w.isl_sleep[w.b_island[b]], __float_as_uint(st));
+                agg_atomic_min((unsigned*)w.isl_sleep, w.b_island[b], __float_as_uint(st));
             }
         }
         if (sp.auto_clear) w.b_force[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -1422,7 +1455,8 @@ int launch_solver(const DevWorld& w, const StepParams& sp, cudaStream_t s, int n
     void* args[] = {&wc, &spc};
     B2G_LAUNCHED(1);
     cudaMemsetAsync(w.cnt + CNT_BARRIER, 0, sizeof(int), s);
-    return (int)cudaLaunchCooperativeKernel((const void*)k_solve, dim3(blocks), dim3(kBlock), args, smem, s);
+    const int threads = w.cfg_coop_per_sm == 1 && w.cfg_solver_block == kSolveMaxBlock ? kSolveMaxBlock : kBlock;
+    return (int)cudaLaunchCooperativeKernel((const void*)k_solve, dim3(blocks), dim3(threads), args, smem, s);
 }
 
 void launch_set_transform(const DevWorld& w, int body, float px, float py, float angle, cudaStream_t s) {

@@ -587,6 +587,8 @@ typedef struct b2g_launch_config {
     int32_t collide_block;        /* narrowphase threads per block: 32..256, power of two */
     int32_t traverse_block;       /* broadphase traversal threads per block: 32..256, power of two */
     int32_t tuning_steps;         /* out: steps the world's last b2g_autotune ran (ignored on set) */
+    int32_t solver_block;         /* solver threads per block: 256, or 512 with one block per SM (more
+                                     loads in flight on large worlds and batches); 0 on set: 256 */
 } b2g_launch_config;
 int b2g_get_launch_config(void* world, b2g_launch_config* out);
 int b2g_set_launch_config(void* world, const b2g_launch_config* config);

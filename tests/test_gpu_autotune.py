@@ -18,8 +18,8 @@ def _world(scene):
     return w
 
 
-@pytest.mark.parametrize("cfg", [dict(coop_blocks_per_sm=2, collide_block=64, traverse_block=64),
-                                 dict(coop_blocks_per_sm=1, collide_block=256, traverse_block=32)])
+@pytest.mark.parametrize("cfg", [dict(coop_blocks_per_sm=2, collide_block=64, traverse_block=64, solver_block=256),
+                                 dict(coop_blocks_per_sm=1, collide_block=256, traverse_block=32, solver_block=512)])
 def test_configurations_give_identical_results(built, cfg):
     s = scenes.mixed(n_circles=300, n_polygons=300, size=25.0, seed=21)
     a, b = _world(s), _world(s)
@@ -42,6 +42,7 @@ def test_autotune_steps_are_ordinary_steps(built):
     cfg = b.autotune(s["dt"], s["vi"], s["pi"], per)
     assert cfg["coop_blocks_per_sm"] in (1, 2)
     assert cfg["collide_block"] in (64, 128, 256) and cfg["traverse_block"] in (64, 128, 256)
+    assert cfg["solver_block"] in (256, 512)
     n = b.tuning_steps()
     assert n >= 2 * 3 * 3  # at least the two block-size knobs, every candidate stepped 2 + 1 times
     for _ in range(n):
@@ -64,4 +65,6 @@ def test_invalid_configuration_is_rejected(built):
         w.set_launch_config(coop_blocks_per_sm=3)
     with pytest.raises(b2g.B2GError):
         w.set_launch_config(collide_block=100)
+    with pytest.raises(b2g.B2GError):
+        w.set_launch_config(solver_block=384)
     w.close()
