@@ -654,7 +654,7 @@ int allocate(World* w, int nb, int nf, int keep_body_cap = 0, int keep_fix_cap =
     A(d.part_cbeg, kMaxParts); A(d.part_cend, kMaxParts); A(d.part_rbeg, kMaxParts);
     A(d.vc_idx, contact_cap); A(d.vc_inv, contact_cap); A(d.vc_nf, contact_cap); A(d.vc_r0, contact_cap);
     A(d.vc_r1, contact_cap); A(d.vc_m0, contact_cap); A(d.vc_m1, contact_cap); A(d.vc_imp, contact_cap);
-    A(d.vc_k, contact_cap); A(d.vc_island, contact_cap);
+    A(d.vc_k, contact_cap); A(d.vc_island, contact_cap); A(d.vc_code, contact_cap);
     A(d.pc_lp, contact_cap); A(d.pc_geo, contact_cap); A(d.pc_lc, contact_cap); A(d.pc_inv, contact_cap);
     A(d.pc_meta, contact_cap);
     A(d.bp_key, fix_cap); A(d.bp_val, fix_cap); A(d.bp_key_alt, fix_cap); A(d.bp_val_alt, fix_cap);

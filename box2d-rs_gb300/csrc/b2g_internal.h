@@ -256,6 +256,9 @@ struct DevWorld {
     int* part_rbeg;              /* kMaxParts: each part's first Morton rank when the partition was
                                     made (ascending); places bodies outside it by their rank */
     int4* vc_idx;                /* ia, ib, point count, flags (bit0 A dynamic, bit1 B dynamic) */
+    int2* vc_code;               /* part-local solve: the slot's bodies as its block addresses them
+                                    (cache entry, or -(body + 1) in global memory), for slots read
+                                    from global memory */
     float4 *vc_inv, *vc_nf, *vc_r0, *vc_r1, *vc_m0, *vc_m1, *vc_imp, *vc_k;
     float4 *pc_lp, *pc_geo, *pc_lc, *pc_inv, *pc_meta;
     int* vc_island;
@@ -398,6 +401,8 @@ void radix_sort_pairs(unsigned long long* key_a, uint32_t* val_a, unsigned long 
 void radix_sort_pairs_coop(unsigned long long* key_a, uint32_t* val_a, unsigned long long* key_b, uint32_t* val_b,
                            const int* d_n, int max_n, int bits, uint32_t* hist, int* cnt, cudaStream_t s, int num_sms);
 size_t radix_sort_hist_size(int max_n);
+/* sets a kernel's dynamic shared-memory limit on the current device (once per kernel and device) */
+void ensure_dynamic_smem(const void* fn, int bytes);
 size_t scan_tmp_size(int max_n);
 
 /* Host-side count of the kernels this library has launched (bench.py reports it per step). */

@@ -134,7 +134,25 @@ __global__ void k_bp_bounds(DevWorld w) {
         mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
     }
     for (int o = 16; o > 0; o >>= 1) dyn = max(dyn, __shfl_xor_sync(0xffffffffu, dyn, o));
+    /* then over the block's warps, so the five counters take one atomic per block */
+    __shared__ int s_red[5][kBlock / 32];
+    const int wid = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
+        s_red[0][wid] = mnx;
+        s_red[1][wid] = mny;
+        s_red[2][wid] = mxx;
+        s_red[3][wid] = mxy;
+        s_red[4][wid] = dyn;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < (int)(blockDim.x >> 5); ++i) {
+            mnx = min(mnx, s_red[0][i]);
+            mny = min(mny, s_red[1][i]);
+            mxx = max(mxx, s_red[2][i]);
+            mxy = max(mxy, s_red[3][i]);
+            dyn = max(dyn, s_red[4][i]);
+        }
         atomicMax(&w.cnt[CNT_DYN_EXTENT], dyn);
         atomicMin(&w.cnt[CNT_BOUNDS + 0], mnx);
         atomicMin(&w.cnt[CNT_BOUNDS + 1], mny);

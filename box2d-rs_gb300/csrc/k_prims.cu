@@ -37,6 +37,20 @@ int current_sm_count() {
     return counts[dev];
 }
 
+/* cudaFuncAttributeMaxDynamicSharedMemorySize of a kernel on the current device, set once per
+ * (kernel, device) */
+void ensure_dynamic_smem(const void* fn, int bytes) {
+    static std::mutex m;
+    static std::vector<std::pair<const void*, int>> done;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    std::lock_guard<std::mutex> lock(m);
+    for (const auto& e : done)
+        if (e.first == fn && e.second == dev) return;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess)
+        done.emplace_back(fn, dev);
+}
+
 namespace {
 constexpr int kScanBlock = 256;
 constexpr int kScanItems = 4;
@@ -269,6 +283,53 @@ __device__ void tile_histogram(const unsigned long long* __restrict__ keys, int 
     __syncthreads();
 }
 
+/* At most kSmallSort pairs are sorted by one block in shared memory (k_sort_small, a bitonic network
+ * over (key, value)): the multi-block radix sort of a few thousand keys costs two grid barriers per
+ * 8-bit pass. Ordering by (key, value) with values that are the input positions (fixture indices,
+ * emission slots) is the stable order the radix sort gives, so both produce the same result. */
+constexpr int kSmallSort = 16384;
+constexpr int kSmallSortBlock = 1024;
+constexpr int kSmallSortSmem = kSmallSort * (int)(sizeof(unsigned long long) + sizeof(uint32_t));
+
+__global__ void __launch_bounds__(kSmallSortBlock) k_sort_small(unsigned long long* keys, uint32_t* vals, const int* d_n,
+                                                                int max_n, int* cnt) {
+    if (world_aborted(cnt)) return;
+    const int n = load_n(d_n, max_n);
+    if (n <= 1 || n > kSmallSort) return;
+    extern __shared__ __align__(16) unsigned char s_small[];
+    unsigned long long* sk = reinterpret_cast<unsigned long long*>(s_small);
+    uint32_t* sv = reinterpret_cast<uint32_t*>(sk + kSmallSort);
+    int m = 1;
+    while (m < n) m <<= 1;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        sk[i] = i < n ? keys[i] : ~0ull;
+        sv[i] = i < n ? vals[i] : 0xffffffffu;
+    }
+    __syncthreads();
+    for (int k = 2; k <= m; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                const int p = i ^ j;
+                if (p <= i) continue;
+                const unsigned long long a = sk[i], b = sk[p];
+                const uint32_t va = sv[i], vb = sv[p];
+                const bool greater = a > b || (a == b && va > vb);
+                if (greater == ((i & k) == 0)) {
+                    sk[i] = b;
+                    sk[p] = a;
+                    sv[i] = vb;
+                    sv[p] = va;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        keys[i] = sk[i];
+        vals[i] = sv[i];
+    }
+}
+
 __global__ void __launch_bounds__(kSortBlock) k_radix_coop(unsigned long long* ka, uint32_t* va, unsigned long long* kb,
                                                            uint32_t* vb, const int* d_n, int max_n, int bits,
                                                            uint32_t* hist, int* cnt) {
@@ -281,6 +342,7 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_coop(unsigned long long* k
     const int n = load_n(d_n, max_n);
     const int passes = (bits + 7) / 8;
     if (n <= 0 || passes <= 0) return;
+    if (n <= kSmallSort && max_n > kSortTile) return;  /* k_sort_small sorted it */
     if (n <= kSortTile) {
         /* one tile: block 0 sorts alone, synchronising with __syncthreads only */
         if (blockIdx.x != 0) return;
@@ -379,6 +441,11 @@ void radix_sort_pairs_coop(unsigned long long* key_a, uint32_t* val_a, unsigned 
     }
     /* one block per SM keeps the grid barrier short; per_sm only guards co-residency */
     const int blocks = num_sms;
+    if (max_n > kSortTile) {
+        ensure_dynamic_smem((const void*)k_sort_small, kSmallSortSmem);
+        k_sort_small<<<1, kSmallSortBlock, kSmallSortSmem, s>>>(key_a, val_a, d_n, max_n, cnt);
+        B2G_LAUNCHED(1);
+    }
     void* args[] = {&key_a, &val_a, &key_b, &val_b, (void*)&d_n, &max_n, &bits, &hist, &cnt};
     cudaMemsetAsync(cnt + CNT_BARRIER, 0, sizeof(int), s);
     cudaLaunchCooperativeKernel((const void*)k_radix_coop, dim3(blocks), dim3(kSortBlock), args, 0, s);

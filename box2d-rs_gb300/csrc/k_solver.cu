@@ -922,26 +922,67 @@ __device__ __forceinline__ PosSlot part_pos_slot(const DevWorld& w, const PartCt
     return sl;
 }
 
-/* the part's interior colours (warm start or one velocity iteration) */
+/* a slot outside the block's cache, with the body codes its block wrote at the step's start (a load
+ * beside the slot's own instead of a lookup after it) */
+__device__ __forceinline__ VelSlot coded_vel_slot(const DevWorld& w, int k) {
+    VelSlot sl = vel_slot(w, k);
+    const int2 code = w.vc_code[k];
+    sl.idx.x = code.x;
+    sl.idx.y = code.y;
+    return sl;
+}
+__device__ __forceinline__ PosSlot coded_pos_slot(const DevWorld& w, int k) {
+    PosSlot sl = pos_slot(w, k);
+    const int2 code = w.vc_code[k];
+    sl.idx.x = code.x;
+    sl.idx.y = code.y;
+    return sl;
+}
+
+/* one velocity constraint of a part (warm start or a velocity iteration) on bodies va, vb */
+__device__ __forceinline__ void part_vel_solve(const VelSlot& sl, bool warm, float4& va, float4& vb, float4& imp) {
+    imp = sl.imp;
+    if (warm) warm_math(sl, va, vb);
+    else solve_velocity_math(sl, imp, va, vb);
+}
+
+/* the part's interior colours (warm start or one velocity iteration). Slots in shared memory come
+ * first; the rest are read from global memory two per thread at a time: both slots' loads, then
+ * both pairs of bodies, are in flight together (constraints of one colour share no body, so the
+ * two are independent and their order is immaterial). */
 __device__ void part_vel_sweeps(const DevWorld& w, const PartCtx& pc, bool warm) {
     VelSlot* vs = (VelSlot*)pc.slots;
     for (int c = 0; c < pc.ncol; ++c) {
         const int beg = pc.off[c], end = pc.off[c + 1];
-        for (int k = beg + threadIdx.x; k < end; k += blockDim.x) {
+        const int kc = max(beg, min(end, pc.ibeg + pc.cap_vel));  /* [beg, kc) cached */
+        for (int k = beg + threadIdx.x; k < kc; k += blockDim.x) {
             const int j = k - pc.ibeg;
-            const bool cached = j < pc.cap_vel;
-            const VelSlot sl = cached ? vs[j] : part_vel_slot(w, pc, k);
+            const VelSlot sl = vs[j];
             float4 va = ld_body(pc.state, w.b_vel, sl.idx.x), vb = ld_body(pc.state, w.b_vel, sl.idx.y);
-            if (warm) {
-                warm_math(sl, va, vb);
-            } else {
-                float4 imp = sl.imp;
-                solve_velocity_math(sl, imp, va, vb);
-                if (cached) vs[j].imp = imp;
-                else w.vc_imp[k] = imp;
-            }
+            float4 imp;
+            part_vel_solve(sl, warm, va, vb, imp);
+            if (!warm) vs[j].imp = imp;
             if (sl.idx.w & 1) st_body(pc.state, w.b_vel, sl.idx.x, va);
             if (sl.idx.w & 2) st_body(pc.state, w.b_vel, sl.idx.y, vb);
+        }
+        for (int k0 = kc + threadIdx.x; k0 < end; k0 += 2 * blockDim.x) {
+            const int k1 = k0 + (int)blockDim.x;
+            const bool two = k1 < end;
+            const VelSlot s0 = coded_vel_slot(w, k0);
+            const VelSlot s1 = coded_vel_slot(w, two ? k1 : k0);
+            float4 va0 = ld_body(pc.state, w.b_vel, s0.idx.x), vb0 = ld_body(pc.state, w.b_vel, s0.idx.y);
+            float4 va1 = ld_body(pc.state, w.b_vel, s1.idx.x), vb1 = ld_body(pc.state, w.b_vel, s1.idx.y);
+            float4 imp0, imp1;
+            part_vel_solve(s0, warm, va0, vb0, imp0);
+            if (!warm) w.vc_imp[k0] = imp0;
+            if (s0.idx.w & 1) st_body(pc.state, w.b_vel, s0.idx.x, va0);
+            if (s0.idx.w & 2) st_body(pc.state, w.b_vel, s0.idx.y, vb0);
+            if (two) {
+                part_vel_solve(s1, warm, va1, vb1, imp1);
+                if (!warm) w.vc_imp[k1] = imp1;
+                if (s1.idx.w & 1) st_body(pc.state, w.b_vel, s1.idx.x, va1);
+                if (s1.idx.w & 2) st_body(pc.state, w.b_vel, s1.idx.y, vb1);
+            }
         }
         __syncthreads();
     }
@@ -952,16 +993,39 @@ __device__ void part_pos_sweeps(const DevWorld& w, const PartCtx& pc, int it, ui
     const PosSlot* ps = (const PosSlot*)pc.slots;
     for (int c = 0; c < pc.ncol; ++c) {
         const int beg = pc.off[c], end = pc.off[c + 1];
-        for (int k = beg + threadIdx.x; k < end; k += blockDim.x) {
-            const int j = k - pc.ibeg;
-            const bool cached = j < pc.cap_pos;
-            const PosSlot sl = cached ? ps[j] : part_pos_slot(w, pc, k);
-            if (cached ? sl.pad[0] != 0 : island_done(w, sl.island, it, tol)) continue;
+        const int kc = max(beg, min(end, pc.ibeg + pc.cap_pos));  /* [beg, kc) cached */
+        for (int k = beg + threadIdx.x; k < kc; k += blockDim.x) {
+            const PosSlot sl = ps[k - pc.ibeg];
+            if (sl.pad[0] != 0) continue;
             float4 pa = ld_body(pc.state, w.b_pos, sl.idx.x), pb = ld_body(pc.state, w.b_pos, sl.idx.y);
             const float ms = solve_position_math(sl, pa, pb);
             if (sl.idx.w & 1) st_body(pc.state, w.b_pos, sl.idx.x, pa);
             if (sl.idx.w & 2) st_body(pc.state, w.b_pos, sl.idx.y, pb);
             agg_atomic_max(cur, sl.island, ms < 0.0f ? __float_as_uint(-ms) : 0u);
+        }
+        /* slots in global memory two per thread at a time, as in part_vel_sweeps */
+        for (int k0 = kc + threadIdx.x; k0 < end; k0 += 2 * blockDim.x) {
+            const int k1 = k0 + (int)blockDim.x;
+            const bool two = k1 < end;
+            const PosSlot s0 = coded_pos_slot(w, k0);
+            const PosSlot s1 = coded_pos_slot(w, two ? k1 : k0);
+            const bool run0 = !island_done(w, s0.island, it, tol);
+            const bool run1 = two && !island_done(w, s1.island, it, tol);
+            float4 pa0 = ld_body(pc.state, w.b_pos, s0.idx.x), pb0 = ld_body(pc.state, w.b_pos, s0.idx.y);
+            float4 pa1 = ld_body(pc.state, w.b_pos, s1.idx.x), pb1 = ld_body(pc.state, w.b_pos, s1.idx.y);
+            float ms0 = 0.0f, ms1 = 0.0f;
+            if (run0) {
+                ms0 = solve_position_math(s0, pa0, pb0);
+                if (s0.idx.w & 1) st_body(pc.state, w.b_pos, s0.idx.x, pa0);
+                if (s0.idx.w & 2) st_body(pc.state, w.b_pos, s0.idx.y, pb0);
+            }
+            if (run1) {
+                ms1 = solve_position_math(s1, pa1, pb1);
+                if (s1.idx.w & 1) st_body(pc.state, w.b_pos, s1.idx.x, pa1);
+                if (s1.idx.w & 2) st_body(pc.state, w.b_pos, s1.idx.y, pb1);
+            }
+            agg_atomic_max(cur, s0.island, ms0 < 0.0f ? __float_as_uint(-ms0) : 0u);
+            agg_atomic_max(cur, s1.island, ms1 < 0.0f ? __float_as_uint(-ms1) : 0u);
         }
         __syncthreads();
     }
@@ -1077,6 +1141,13 @@ __global__ void __launch_bounds__(kSolveMaxBlock) k_solve(DevWorld w, StepParams
         __syncthreads();
         VelSlot* vs = (VelSlot*)pc.slots;
         for (int j = threadIdx.x; j < pc.cap_vel; j += blockDim.x) vs[j] = part_vel_slot(w, pc, pc.ibeg + j);
+        /* the body codes of the slots read from global memory (the position sweeps' too: a PosSlot is
+         * smaller, so no fewer of them are cached) */
+        for (int j = pc.cap_vel + threadIdx.x; j < nint; j += blockDim.x) {
+            const int4 idx = w.vc_idx[pc.ibeg + j];
+            w.vc_code[pc.ibeg + j] = make_int2(body_code(w, pc, idx.x, (idx.w & 1) != 0),
+                                               body_code(w, pc, idx.y, (idx.w & 2) != 0));
+        }
         for (int c = 0; c < ncol; ++c) {
             int lo, hi;
             bnd_range(pc, c, &lo, &hi);
