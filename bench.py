@@ -225,12 +225,12 @@ def timed_steps(world, scene, steps, flush, torch):
 
 
 def tune_blocks_per_sm(torch, flush, t, dt, vi, pi, turns=3, steps=3):
-    """After b2g_autotune (which times back-to-back steps): choose the persistent kernels' shape
-    (blocks per SM, and the solver's threads per block at one block per SM) on the scratch world `t`
-    the way this bench times a step (device time, L2 flushed before it); the settings take turns.
+    """After b2g_autotune (which times back-to-back steps): choose the solver's threads per block (one
+    block per SM: the part-local solve gives each block an SM's shared memory) on the scratch world
+    `t` the way this bench times a step (device time, L2 flushed before it); the settings take turns.
     Returns the launch configuration to use."""
     base = t.get_launch_config()
-    shapes = [(1, 256), (1, 512), (2, 256)]
+    shapes = [(1, 256), (1, 512)]
     total = dict.fromkeys(shapes, 0.0)
     for _ in range(turns):
         for c, sb in shapes:
@@ -697,7 +697,8 @@ def main():
     fine_ms = dict.fromkeys(b2g.B2world.PHASES + b2g.B2world.TREE_PHASES, 0.0)
     bytes_total = {}
     work = {"bp_node_visits": 0, "bp_leaf_checks": 0, "bp_moved_proxies": 0, "new_pairs": 0, "contacts": 0,
-            "constraints": 0, "interior_slots": 0, "colours": 0, "hierarchy_rebuilds": 0}
+            "constraints": 0, "interior_slots": 0, "colours": 0, "hierarchy_rebuilds": 0,
+            "bp_warp_max_visits": 0, "bp_warp_max_checks": 0}
     snap_at = set(int(x) for x in np.linspace(0, args.steps - 1, 4)) if rank == 0 and not args.no_cpu_baseline else set()
     snaps = []
     for k in range(args.steps):

@@ -455,7 +455,8 @@ def pre_solve_callback(fn):
 class StepStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in ("bp_node_visits", "bp_leaf_checks", "new_pairs", "contacts", "constraints",
                                                "interior_slots", "parts", "colours", "contact_capacity",
-                                               "pair_capacity", "capacity_grows", "hierarchy_age", "bp_moved_proxies")]
+                                               "pair_capacity", "capacity_grows", "hierarchy_age", "bp_moved_proxies",
+                                               "bp_warp_max_visits", "bp_warp_max_checks")]
 
 
 class Counts(ctypes.Structure):

@@ -2643,6 +2643,8 @@ int b2g_get_step_stats(void* p, b2g_step_stats* out) {
     out->capacity_grows = w->capacity_grows;
     out->hierarchy_age = cnt[CNT_BP_AGE];
     out->bp_moved_proxies = cnt[CNT_BP_LAST_MOVED];
+    out->bp_warp_max_visits = cnt[CNT_BP_WARP_VISITS];
+    out->bp_warp_max_checks = cnt[CNT_BP_WARP_CHECKS];
     return B2G_OK;
 }
 

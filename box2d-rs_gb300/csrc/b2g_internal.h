@@ -130,6 +130,8 @@ enum {
     CNT_BP_SORT_N = 54,   /* keys the pass sorts: the proxies on a rebuild, 0 otherwise */
     CNT_BP_LAST_MOVED = 55, /* proxies the solver moved before the last pass */
     CNT_BP_MAX_AGE = 56,  /* passes a kept hierarchy may reach before a rebuild (0: rebuild every pass) */
+    CNT_BP_WARP_VISITS = 57, /* the most node fetches one warp of the last traversal made */
+    CNT_BP_WARP_CHECKS = 58, /* the most leaf checks one warp of the last traversal made */
     CNT_SIZE = 64
 };
 
@@ -137,7 +139,7 @@ constexpr int kMaxColours = 256;   /* first-fit colours 0..63, then one per colo
 constexpr int kFirstFitColours = 64;
 constexpr int kColourTail = 256;   /* uncoloured constraints one block finishes colouring (one per thread) */
 constexpr int kMaxParts = 1024;    /* body parts of the part-local solve (at most one per solver block) */
-constexpr int kKeyMortonBits = 30; /* broadphase keys: key world << 30 | Morton code (15 bits per axis) */
+constexpr int kKeyMortonBits = 22; /* broadphase keys: key world << 22 | Morton code (11 bits per axis) */
 constexpr int kMaxPosIters = 64;
 constexpr int kNoWake = 0x7f7f7f7f;  /* b_wake's "not woken" (a byte-wise memset value) */
 /* continuous pass lists (k_continuous.cu): partner contacts of one event, events of one
@@ -396,13 +398,14 @@ void scan_exclusive_u32(const uint32_t* in, uint32_t* out, const int* d_n, int m
 /* stable LSD radix sort of (key, value) pairs by key bits [0, bits); n from device; result in *_a. */
 void radix_sort_pairs(unsigned long long* key_a, uint32_t* val_a, unsigned long long* key_b, uint32_t* val_b,
                       const int* d_n, int max_n, int bits, uint32_t* hist, cudaStream_t s);
-/* the same sort as one cooperative launch (3 grid barriers per 8-bit pass; inputs of at most
- * 2048 items are sorted by a single block); uses cnt's barrier words */
+/* the same sort as one cooperative launch (2 grid barriers per 8-bit pass; inputs of at most
+ * 2048 items are sorted by a single block, inputs of at most 8192 by a rank count in three small
+ * kernels); uses cnt's barrier words. zero_or_max: the count is known to be 0 or max_n (no
+ * rank-count launches when max_n is large). */
 void radix_sort_pairs_coop(unsigned long long* key_a, uint32_t* val_a, unsigned long long* key_b, uint32_t* val_b,
-                           const int* d_n, int max_n, int bits, uint32_t* hist, int* cnt, cudaStream_t s, int num_sms);
+                           const int* d_n, int max_n, int bits, uint32_t* hist, int* cnt, cudaStream_t s, int num_sms,
+                           bool zero_or_max = false);
 size_t radix_sort_hist_size(int max_n);
-/* sets a kernel's dynamic shared-memory limit on the current device (once per kernel and device) */
-void ensure_dynamic_smem(const void* fn, int bytes);
 size_t scan_tmp_size(int max_n);
 
 /* Host-side count of the kernels this library has launched (bench.py reports it per step). */

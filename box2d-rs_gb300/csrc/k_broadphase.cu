@@ -11,11 +11,12 @@
  * passes old) and otherwise kept, with each moved proxy's leaf set to its new fat AABB and its
  * ancestors' boxes grown to cover it (k_bp_update). A rebuild:
  *   1. centre bounds of all fat AABBs (atomic min/max on order-preserving ints),
- *   2. 64-bit keys world << 30 | Morton(15-bit x, 15-bit y), radix-sorted with the
+ *   2. 64-bit keys world << 22 | Morton(11-bit x, 11-bit y), radix-sorted with the
  *      fixture index as payload (worlds occupy disjoint key ranges; a static proxy far
  *      larger than every dynamic one takes key world  world + num_worlds, so grounds and
  *      walls form a small hierarchy of their own instead of inflating every ancestor box;
- *      a single world then sorts 31 key bits, four 8-bit passes),
+ *      a single world then sorts 23 key bits, three 8-bit passes; 2048 cells per axis keep a
+ *      cell near one body in the densest scenes),
  *   3. Karras (2012) hierarchy over the sorted keys (ties broken by position) — every
  *      internal node stores both children's boxes, and after the refit a four-way record of
  *      its grandchildren, so a traversal step is one 80-byte fetch and four overlap tests,
@@ -42,8 +43,8 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr int kStack = 64;
-constexpr int kMortonBits = kKeyMortonBits;  /* 15 bits of cell per axis */
-constexpr float kCellMax = 32767.0f;
+constexpr int kMortonBits = kKeyMortonBits;  /* 11 bits of cell per axis */
+constexpr float kCellMax = 2047.0f;
 
 __device__ __forceinline__ int f2ord(float f) {
     int i = __float_as_int(f);
@@ -101,6 +102,8 @@ __global__ void k_bp_init(DevWorld w) {
         w.cnt[CNT_DYN_EXTENT] = 0;
         w.cnt[CNT_BP_VISITS] = 0;
         w.cnt[CNT_BP_CANDIDATES] = 0;
+        w.cnt[CNT_BP_WARP_VISITS] = 0;
+        w.cnt[CNT_BP_WARP_CHECKS] = 0;
     }
     if (!bp_rebuilding(w)) return;
     for (int i = t; i < 2 * w.num_worlds; i += gridDim.x * blockDim.x) {
@@ -262,6 +265,15 @@ __device__ __forceinline__ float4 box_union(float4 a, float4 b) {
     return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fmaxf(a.z, b.z), fmaxf(a.w, b.w));
 }
 
+/* arrival count with release (this thread's box store before it) and acquire (the sibling's after it) */
+__device__ __forceinline__ unsigned arrive_acq_rel(unsigned* p) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+
+/* Bottom-up: each leaf's thread stores its box in its parent's record and arrives; the second of
+ * the two children to arrive reads its sibling's box (in L2) and carries the union up. */
 __global__ void k_bp_refit(DevWorld w) {
     B2G_RETURN_IF_ABORTED(w);
     if (!bp_rebuilding(w)) return;
@@ -273,13 +285,11 @@ __global__ void k_bp_refit(DevWorld w) {
         int node = w.bp_parent[n - 1 + p];
         for (int guard = 0; guard < 128; ++guard) {
             const int2 ch = w.bp_node_child[node];
-            if (ch.x == child) w.bp_node_b0[node] = box; else w.bp_node_b1[node] = box;
-            __threadfence();
-            if (atomicAdd(&w.bp_flag[node], 1u) == 0u) break;  /* the sibling finishes this node */
-            __threadfence();
-            const float4 b0 = __ldcg(&w.bp_node_b0[node]);
-            const float4 b1 = __ldcg(&w.bp_node_b1[node]);
-            box = box_union(b0, b1);
+            const bool left = ch.x == child;
+            (left ? w.bp_node_b0 : w.bp_node_b1)[node] = box;
+            if (arrive_acq_rel(&w.bp_flag[node]) == 0u) break;  /* the sibling finishes this node */
+            const float4 sib = __ldcg(&(left ? w.bp_node_b1 : w.bp_node_b0)[node]);
+            box = left ? box_union(box, sib) : box_union(sib, box);
             if (node == 0) break;
             child = node;
             node = w.bp_parent[node];
@@ -618,6 +628,8 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
     if (lane == 0 && (visits | candidates)) {
         atomicAdd((unsigned*)&w.cnt[CNT_BP_VISITS], visits);
         atomicAdd((unsigned*)&w.cnt[CNT_BP_CANDIDATES], candidates);
+        atomicMax((unsigned*)&w.cnt[CNT_BP_WARP_VISITS], visits);
+        atomicMax((unsigned*)&w.cnt[CNT_BP_WARP_CHECKS], candidates);
     }
 }
 
@@ -712,7 +724,7 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
         k_bp_bounds<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_keys<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         radix_sort_pairs_coop(w.bp_key, w.bp_val, w.bp_key_alt, w.bp_val_alt, &w.cnt[CNT_BP_SORT_N], n,
-                              kMortonBits + w.morton_world_bits, w.sort_hist, w.cnt, s, num_sms);
+                              kMortonBits + w.morton_world_bits, w.sort_hist, w.cnt, s, num_sms, true);
         if (mark) mark(0);
         if (n > 1) {
             k_bp_build<<<grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);

@@ -12,6 +12,7 @@
  *      __match_any_sync groups equal digits, and per-warp counts are prefixed across
  *      the 8 warps in shared memory, so every item's rank preserves input order.
  */
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -35,20 +36,6 @@ int current_sm_count() {
         counts[dev] = n;
     }
     return counts[dev];
-}
-
-/* cudaFuncAttributeMaxDynamicSharedMemorySize of a kernel on the current device, set once per
- * (kernel, device) */
-void ensure_dynamic_smem(const void* fn, int bytes) {
-    static std::mutex m;
-    static std::vector<std::pair<const void*, int>> done;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return;
-    std::lock_guard<std::mutex> lock(m);
-    for (const auto& e : done)
-        if (e.first == fn && e.second == dev) return;
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess)
-        done.emplace_back(fn, dev);
 }
 
 namespace {
@@ -283,50 +270,70 @@ __device__ void tile_histogram(const unsigned long long* __restrict__ keys, int 
     __syncthreads();
 }
 
-/* At most kSmallSort pairs are sorted by one block in shared memory (k_sort_small, a bitonic network
- * over (key, value)): the multi-block radix sort of a few thousand keys costs two grid barriers per
- * 8-bit pass. Ordering by (key, value) with values that are the input positions (fixture indices,
- * emission slots) is the stable order the radix sort gives, so both produce the same result. */
-constexpr int kSmallSort = 16384;
-constexpr int kSmallSortBlock = 1024;
-constexpr int kSmallSortSmem = kSmallSort * (int)(sizeof(unsigned long long) + sizeof(uint32_t));
+/* Between one tile and kRankSort pairs, the sort is a rank count instead of the multi-block radix
+ * sort (whose two grid barriers per 8-bit pass dominate a few thousand keys): a block takes one
+ * tile x of keys and a slice of the tiles y; each thread counts, for its key of tile x, the keys of
+ * those tiles that precede it in (key, input position) order and adds the count to the key's rank
+ * (one atomic per key and slice); the keys then go to their ranks. The order is the radix sort's
+ * (stable: equal keys keep their input order). A fixed grid of kRankBlocks is mapped onto the
+ * tiles and slices of the actual count. */
+constexpr int kRankSort = 8192;  /* the count is quadratic: beyond this the radix sort is faster */
+constexpr int kRankTile = 256;
+constexpr int kRankBlocks = 1024;
 
-__global__ void __launch_bounds__(kSmallSortBlock) k_sort_small(unsigned long long* keys, uint32_t* vals, const int* d_n,
-                                                                int max_n, int* cnt) {
+__global__ void __launch_bounds__(kRankTile) k_rank_count(const unsigned long long* __restrict__ keys, const int* d_n,
+                                                          int max_n, uint32_t* rank, int* cnt) {
     if (world_aborted(cnt)) return;
     const int n = load_n(d_n, max_n);
-    if (n <= 1 || n > kSmallSort) return;
-    extern __shared__ __align__(16) unsigned char s_small[];
-    unsigned long long* sk = reinterpret_cast<unsigned long long*>(s_small);
-    uint32_t* sv = reinterpret_cast<uint32_t*>(sk + kSmallSort);
-    int m = 1;
-    while (m < n) m <<= 1;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        sk[i] = i < n ? keys[i] : ~0ull;
-        sv[i] = i < n ? vals[i] : 0xffffffffu;
-    }
-    __syncthreads();
-    for (int k = 2; k <= m; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < m; i += blockDim.x) {
-                const int p = i ^ j;
-                if (p <= i) continue;
-                const unsigned long long a = sk[i], b = sk[p];
-                const uint32_t va = sv[i], vb = sv[p];
-                const bool greater = a > b || (a == b && va > vb);
-                if (greater == ((i & k) == 0)) {
-                    sk[i] = b;
-                    sk[p] = a;
-                    sv[i] = vb;
-                    sv[p] = va;
-                }
-            }
-            __syncthreads();
+    if (n <= kSortTile || n > kRankSort) return;
+    __shared__ unsigned long long s_k[kRankTile];
+    const int tiles = (n + kRankTile - 1) / kRankTile;
+    const int slices = max(1, min(tiles, (int)gridDim.x / tiles));
+    if ((int)blockIdx.x >= tiles * slices) return;
+    const int tx = blockIdx.x % tiles, sl = blockIdx.x / tiles;
+    const int per = (tiles + slices - 1) / slices;
+    const int y0 = sl * per, y1 = min(tiles, y0 + per);
+    const int j = tx * kRankTile + threadIdx.x;
+    const unsigned long long kj = j < n ? keys[j] : 0ull;
+    uint32_t r = 0;
+    for (int ty = y0; ty < y1; ++ty) {
+        const int i0 = ty * kRankTile;
+        const int m = min(kRankTile, n - i0);
+        __syncthreads();  /* the previous tile's keys are no longer read */
+        if (threadIdx.x < m) s_k[threadIdx.x] = keys[i0 + threadIdx.x];
+        __syncthreads();
+        for (int i = 0; i < m; ++i) {
+            const unsigned long long ki = s_k[i];
+            r += (ki < kj || (ki == kj && i0 + i < j)) ? 1u : 0u;
         }
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        keys[i] = sk[i];
-        vals[i] = sv[i];
+    if (j < n && r) atomicAdd(&rank[j], r);
+}
+
+__global__ void k_rank_scatter(const unsigned long long* __restrict__ kin, const uint32_t* __restrict__ vin,
+                               unsigned long long* __restrict__ kout, uint32_t* __restrict__ vout, const int* d_n,
+                               int max_n, const uint32_t* rank, int* cnt) {
+    if (world_aborted(cnt)) return;
+    const int n = load_n(d_n, max_n);
+    if (n <= kSortTile || n > kRankSort) return;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t r = rank[j];
+        if (r < (uint32_t)n) {
+            kout[r] = kin[j];
+            vout[r] = vin[j];
+        }
+    }
+}
+
+__global__ void k_rank_copy(const unsigned long long* __restrict__ kin, const uint32_t* __restrict__ vin,
+                            unsigned long long* __restrict__ kout, uint32_t* __restrict__ vout, const int* d_n, int max_n,
+                            int* cnt) {
+    if (world_aborted(cnt)) return;
+    const int n = load_n(d_n, max_n);
+    if (n <= kSortTile || n > kRankSort) return;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        kout[j] = kin[j];
+        vout[j] = vin[j];
     }
 }
 
@@ -342,7 +349,7 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_coop(unsigned long long* k
     const int n = load_n(d_n, max_n);
     const int passes = (bits + 7) / 8;
     if (n <= 0 || passes <= 0) return;
-    if (n <= kSmallSort && max_n > kSortTile) return;  /* k_sort_small sorted it */
+    if (n > kSortTile && n <= kRankSort && max_n > kSortTile) return;  /* the rank count sorted it */
     if (n <= kSortTile) {
         /* one tile: block 0 sorts alone, synchronising with __syncthreads only */
         if (blockIdx.x != 0) return;
@@ -432,7 +439,8 @@ void scan_exclusive_u32(const uint32_t* in, uint32_t* out, const int* d_n, int m
 }
 
 void radix_sort_pairs_coop(unsigned long long* key_a, uint32_t* val_a, unsigned long long* key_b, uint32_t* val_b,
-                           const int* d_n, int max_n, int bits, uint32_t* hist, int* cnt, cudaStream_t s, int num_sms) {
+                           const int* d_n, int max_n, int bits, uint32_t* hist, int* cnt, cudaStream_t s, int num_sms,
+                           bool zero_or_max) {
     static int per_sm = 0;
     if (!per_sm) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_radix_coop, kSortBlock, 0);
@@ -441,10 +449,15 @@ void radix_sort_pairs_coop(unsigned long long* key_a, uint32_t* val_a, unsigned 
     }
     /* one block per SM keeps the grid barrier short; per_sm only guards co-residency */
     const int blocks = num_sms;
-    if (max_n > kSortTile) {
-        ensure_dynamic_smem((const void*)k_sort_small, kSmallSortSmem);
-        k_sort_small<<<1, kSmallSortBlock, kSmallSortSmem, s>>>(key_a, val_a, d_n, max_n, cnt);
-        B2G_LAUNCHED(1);
+    if (max_n > kSortTile && (!zero_or_max || max_n <= kRankSort)) {
+        /* the rank count for inputs between one tile and kRankSort keys (each kernel checks n) */
+        const int m = std::min(max_n, kRankSort);
+        const int tiles = (m + kRankTile - 1) / kRankTile;
+        cudaMemsetAsync(hist, 0, (size_t)m * sizeof(uint32_t), s);
+        k_rank_count<<<kRankBlocks, kRankTile, 0, s>>>(key_a, d_n, max_n, hist, cnt);
+        k_rank_scatter<<<tiles, kRankTile, 0, s>>>(key_a, val_a, key_b, val_b, d_n, max_n, hist, cnt);
+        k_rank_copy<<<tiles, kRankTile, 0, s>>>(key_b, val_b, key_a, val_a, d_n, max_n, cnt);
+        B2G_LAUNCHED(3);
     }
     void* args[] = {&key_a, &val_a, &key_b, &val_b, (void*)&d_n, &max_n, &bits, &hist, &cnt};
     cudaMemsetAsync(cnt + CNT_BARRIER, 0, sizeof(int), s);
@@ -454,7 +467,8 @@ void radix_sort_pairs_coop(unsigned long long* key_a, uint32_t* val_a, unsigned 
 
 size_t radix_sort_hist_size(int max_n) {
     const int tiles = (max_n + kSortTile - 1) / kSortTile;
-    return (size_t)tiles * 256 * 2 + scan_tmp_size(tiles * 256) + 16;
+    /* the rank count uses the first kRankSort entries */
+    return std::max((size_t)tiles * 256 * 2 + scan_tmp_size(tiles * 256) + 16, (size_t)kRankSort);
 }
 
 void radix_sort_pairs(unsigned long long* key_a, uint32_t* val_a, unsigned long long* key_b, uint32_t* val_b,

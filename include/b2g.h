@@ -331,13 +331,14 @@ int b2g_get_counts(void* world, b2g_counts* out);         /* get_body_count / ge
  * checked, new contacts it found, the contact table's size, constraint slots solved (of them
  * part-locally), the parts and colours of the colouring; the contact and pair capacities and how
  * often they grew (b2g_set_auto_grow); the broadphase hierarchy's age (0: the last pass rebuilt it; else
- * the passes since, which kept it and updated the moved proxies' leaves in place) and the proxies the
- * step's solver moved (the traversal's queries). */
+ * the passes since, which kept it and updated the moved proxies' leaves in place), the proxies the
+ * step's solver moved (the traversal's queries), and the most node fetches and leaf checks one warp
+ * of the traversal made (its load balance). */
 typedef struct b2g_step_stats {
     int32_t bp_node_visits, bp_leaf_checks, new_pairs, contacts;
     int32_t constraints, interior_slots, parts, colours;
     int32_t contact_capacity, pair_capacity, capacity_grows, hierarchy_age;
-    int32_t bp_moved_proxies;
+    int32_t bp_moved_proxies, bp_warp_max_visits, bp_warp_max_checks;
 } b2g_step_stats;
 int b2g_get_step_stats(void* world, b2g_step_stats* out);
 /* Exact checkpoint and resume (not in the reference's API, which serialises a world through serde,
