@@ -105,7 +105,7 @@ struct GearFrame {
 struct World {
     int device = 0;
     cudaStream_t stream = nullptr;
-    int num_sms = 152;
+    int num_sms = 0;  /* the device's multiprocessors, queried when the world is made */
     b2g_vec2 gravity{0.0f, -10.0f};
     int num_worlds = 1;
     bool warm = true, continuous = false, allow_sleep = true, auto_clear = true;
@@ -643,7 +643,7 @@ int allocate(World* w, int nb, int nf, int keep_body_cap = 0, int keep_fix_cap =
         A(c->mat, contact_cap); A(c->mgeo, contact_cap); A(c->mpts, contact_cap); A(c->mimp, contact_cap);
         A(c->mids, contact_cap);
     }
-    A(d.c_rank, contact_cap); A(d.c_row, 2 * (size_t)fix_cap + 2);
+    A(d.c_rank, contact_cap); A(d.c_row, 2 * (size_t)fix_cap + 2); A(d.c_row_end, 2 * (size_t)fix_cap + 2);
     A(d.n_key, pair_cap); A(d.n_fix, pair_cap); A(d.n_idx, pair_cap); A(d.n_key_alt, pair_cap); A(d.n_idx_alt, pair_cap);
     A(d.cons_contact, contact_cap); A(d.cons_colour, contact_cap); A(d.cons_island, contact_cap);
     A(d.s_contact, contact_cap); A(d.s_cons, contact_cap); A(d.s_fix, contact_cap);

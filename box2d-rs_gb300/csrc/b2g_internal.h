@@ -225,6 +225,7 @@ struct DevWorld {
     /* contacts: current table and the merge target */
     Contacts c, c_alt;
     int* c_rank;                 /* exclusive scan of alive flags during a merge */
+    int* c_row_end;              /* per proxy id: one past the last contact of that row (same validity) */
     int* c_row;                  /* per proxy id: first contact of the sorted table whose key starts with
                                     it (valid only when that contact's key does: see k_bp_rows) */
     /* new contacts from the broadphase */

@@ -72,6 +72,18 @@ __global__ void k_bp_decide(DevWorld w, int mode) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     int* c = w.cnt;
     const int n = w.n_fixtures;
+    /* the pass's counters */
+    c[CNT_BOUNDS + 0] = INT_MAX;
+    c[CNT_BOUNDS + 1] = INT_MAX;
+    c[CNT_BOUNDS + 2] = INT_MIN;
+    c[CNT_BOUNDS + 3] = INT_MIN;
+    c[CNT_NEW] = 0;
+    c[CNT_PAIRS] = 0;
+    c[CNT_DYN_EXTENT] = 0;
+    c[CNT_BP_VISITS] = 0;
+    c[CNT_BP_CANDIDATES] = 0;
+    c[CNT_BP_WARP_VISITS] = 0;
+    c[CNT_BP_WARP_CHECKS] = 0;
     if (mode == BP_REPEAT) return;
     const int moved = c[CNT_BP_MOVED];
     const long long drift = (long long)c[CNT_BP_DRIFT] + moved;
@@ -89,34 +101,16 @@ __global__ void k_bp_decide(DevWorld w, int mode) {
 
 __device__ __forceinline__ bool bp_rebuilding(const DevWorld& w) { return w.cnt[CNT_BP_REBUILD] != 0; }
 
-__global__ void k_bp_init(DevWorld w) {
-    B2G_RETURN_IF_ABORTED(w);
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t == 0) {
-        w.cnt[CNT_BOUNDS + 0] = INT_MAX;
-        w.cnt[CNT_BOUNDS + 1] = INT_MAX;
-        w.cnt[CNT_BOUNDS + 2] = INT_MIN;
-        w.cnt[CNT_BOUNDS + 3] = INT_MIN;
-        w.cnt[CNT_NEW] = 0;
-        w.cnt[CNT_PAIRS] = 0;
-        w.cnt[CNT_DYN_EXTENT] = 0;
-        w.cnt[CNT_BP_VISITS] = 0;
-        w.cnt[CNT_BP_CANDIDATES] = 0;
-        w.cnt[CNT_BP_WARP_VISITS] = 0;
-        w.cnt[CNT_BP_WARP_CHECKS] = 0;
-    }
-    if (!bp_rebuilding(w)) return;
-    for (int i = t; i < 2 * w.num_worlds; i += gridDim.x * blockDim.x) {
-        w.bp_world_first[i] = -1;
-        w.bp_world_root[i] = INT_MIN;
-    }
-}
 
 __global__ void k_bp_bounds(DevWorld w) {
     B2G_RETURN_IF_ABORTED(w);
     if (!bp_rebuilding(w)) return;
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x)
         w.b_rank[b] = INT_MAX;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * w.num_worlds; i += gridDim.x * blockDim.x) {
+        w.bp_world_first[i] = -1;
+        w.bp_world_root[i] = INT_MIN;
+    }
     int mnx = INT_MAX, mny = INT_MAX, mxx = INT_MIN, mxy = INT_MIN, dyn = 0;
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < w.n_fixtures; f += gridDim.x * blockDim.x) {
         const float4 a = w.f_fat[f];
@@ -242,12 +236,7 @@ __global__ void k_bp_build(DevWorld w) {
             if (first && last) w.bp_world_root[wl] = i;
         }
     }
-}
-
-__global__ void k_bp_leaves(DevWorld w) {
-    B2G_RETURN_IF_ABORTED(w);
-    if (!bp_rebuilding(w)) return;
-    const int n = w.n_fixtures;
+    /* the leaves: each proxy's box in sorted order, its place, its body's Morton rank */
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const uint32_t f = w.bp_val[p];
         w.bp_leaf[p] = w.f_fat[f];
@@ -260,6 +249,7 @@ __global__ void k_bp_leaves(DevWorld w) {
         if (first && last) w.bp_world_root[wd] = ~p;  /* a world with a single proxy */
     }
 }
+
 
 __device__ __forceinline__ float4 box_union(float4 a, float4 b) {
     return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fmaxf(a.z, b.z), fmaxf(a.w, b.w));
@@ -372,14 +362,24 @@ __device__ __forceinline__ int quad_place(const DevWorld& w, int node, int id) {
     return q.x == id ? 0 : q.y == id ? 1 : q.z == id ? 2 : q.w == id ? 3 : -1;
 }
 
-/* A pass that keeps the hierarchy: every moved proxy's leaf takes its new fat AABB exactly (the leaf
- * box, its parent's record of it and the four-way records of its parent and grandparent), and each
- * ancestor's record grows to cover it (the binary record in its parent and the four-way record in its
- * grandparent). A walk stops at the first ancestor whose record already covered the box: whoever grew
+/* The contact rows (every pass), then, in a pass that keeps the hierarchy: every moved proxy's leaf
+ * takes its new fat AABB exactly (the leaf box, its parent's record of it and the four-way records of
+ * its parent and grandparent), and each ancestor's record grows to cover it (the binary record in its
+ * parent and the four-way record in its grandparent). A walk stops at the first ancestor whose record already covered the box: whoever grew
  * that record past it carries the growth further up, so when the kernel ends every ancestor covers
  * every leaf below it. */
 __global__ void k_bp_update(DevWorld w) {
     B2G_RETURN_IF_ABORTED(w);
+    /* every pass: the row index of the key-sorted contact table, c_row[r] = the first contact whose
+     * key's high part is proxy id r. Entries of ids with no contact keep stale values; a reader
+     * accepts c_row[r] only if that contact's key starts with r, which a stale entry cannot satisfy
+     * (ids with contacts are rewritten every pass and the table is sorted). */
+    const int nc = w.cnt[CNT_CONTACTS];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+        const unsigned long long r = w.c.key[i] >> w.key_bits;
+        if (i == 0 || (w.c.key[i - 1] >> w.key_bits) != r) w.c_row[r] = i;
+        if (i == nc - 1 || (w.c.key[i + 1] >> w.key_bits) != r) w.c_row_end[r] = i + 1;
+    }
     if (bp_rebuilding(w)) return;
     const int n = w.n_fixtures;
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
@@ -424,65 +424,64 @@ __device__ __forceinline__ int lower_bound_u64(const unsigned long long* a, int 
     return lo;
 }
 
-/* Row index of the key-sorted contact table: c_row[r] = first contact whose key's high part is
- * proxy id r. Entries of ids with no contact keep stale values; a reader accepts c_row[r] only if
- * that contact's key starts with r, which a stale entry cannot satisfy (ids with contacts are
- * rewritten every pass and the table is sorted). */
-__global__ void k_bp_rows(DevWorld w) {
-    B2G_RETURN_IF_ABORTED(w);
-    const int n = w.cnt[CNT_CONTACTS];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const unsigned long long r = w.c.key[i] >> w.key_bits;
-        if (i == 0 || (w.c.key[i - 1] >> w.key_bits) != r) w.c_row[r] = i;
-    }
-}
-
-/* A live contact with this key exists: a short scan of the key's row instead of a binary search
- * over the whole table (the check the reference makes by walking body B's contact list,
- * private/dynamics/b2_contact_manager.rs:199-224). A long row (a ground touching a whole layer of
- * a pile) continues with a galloping search, so no check scans more than a few keys. */
+/* A live contact with this key exists: a search of the key's row of the sorted table instead of the
+ * whole table (the check the reference makes by walking body B's contact list,
+ * private/dynamics/b2_contact_manager.rs:199-224): a short row is scanned, a long one (a ground
+ * touching a whole layer of a pile) is searched by bisection. The row's bounds (c_row, c_row_end)
+ * and its first key come from the caller, which loads them for several pairs at a time. */
 constexpr int kRowScan = 8;
 
-__device__ __forceinline__ bool contact_exists(const DevWorld& w, uint32_t lo, unsigned long long key, int n_contacts) {
-    const int start = w.c_row[lo];
-    if (start < 0 || start >= n_contacts || (w.c.key[start] >> w.key_bits) != lo) return false;
-    const int scan_end = min(n_contacts, start + kRowScan);
-    for (int i = start; i < scan_end; ++i) {
-        const unsigned long long k = w.c.key[i];
-        if (k >= key) return k == key && !(w.c.flags[i] & CF_DEAD);
-        if ((k >> w.key_bits) != lo) return false;
+__device__ __forceinline__ bool contact_exists_from(const DevWorld& w, uint32_t lo, unsigned long long key, int start,
+                                                    int end, unsigned long long first, int n_contacts) {
+    if (start < 0 || start >= n_contacts || (first >> w.key_bits) != lo) return false;
+    if (first >= key) return first == key && !(w.c.flags[start] & CF_DEAD);
+    end = min(end, n_contacts);
+    int i = start + 1;
+    if (end - i <= kRowScan) {
+        for (; i < end; ++i) {
+            const unsigned long long k = w.c.key[i];
+            if (k >= key) return k == key && !(w.c.flags[i] & CF_DEAD);
+        }
+        return false;
     }
-    /* keys [start, scan_end) are below `key`: gallop to a bound, then binary search */
-    int lo_i = scan_end, step = kRowScan, hi_i = scan_end;
-    while (hi_i < n_contacts && w.c.key[hi_i] < key) {
-        lo_i = hi_i + 1;
-        hi_i += step;
-        step <<= 1;
+    int hi = end;
+    while (i < hi) {
+        const int mid = (i + hi) >> 1;
+        if (w.c.key[mid] < key) i = mid + 1; else hi = mid;
     }
-    hi_i = min(hi_i, n_contacts);
-    while (lo_i < hi_i) {
-        const int mid = (lo_i + hi_i) >> 1;
-        if (w.c.key[mid] < key) lo_i = mid + 1; else hi_i = mid;
-    }
-    return lo_i < n_contacts && w.c.key[lo_i] == key && !(w.c.flags[lo_i] & CF_DEAD);
+    return i < end && w.c.key[i] == key && !(w.c.flags[i] & CF_DEAD);
 }
 
-__device__ void handle_pair(const DevWorld& w, const StepParams& sp, int f, int g, uint32_t rf, int n_contacts) {
-    const uint32_t rg = w.f_refid[g];
+/* A slot of a list whose length is *counter, for every lane that executes this together: one atomic
+ * per group of lanes (every accepted pair taking a slot with its own atomic on the one counter word
+ * serialised them; a pile's traversal accepts tens of thousands per pass) */
+__device__ __forceinline__ int agg_slot(int* counter) {
+    const unsigned act = __activemask();
+    const int lane = (int)(threadIdx.x & 31);
+    const int leader = __ffs(act) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(act));
+    base = __shfl_sync(act, base, leader);
+    return base + __popc(act & ((1u << lane) - 1u));
+}
+
+/* add_pair for the pair (f, g) of proxy ids rf, rg with key `key` (lo = the smaller id), whose row
+ * in the contact table starts at `start` with key `first` (both read beforehand) */
+__device__ void handle_pair(const DevWorld& w, const StepParams& sp, int f, int g, uint32_t rf, uint32_t rg,
+                            unsigned long long key, uint32_t lo, int start, int end, unsigned long long first,
+                            int n_contacts) {
     if (sp.record_pairs) {
-        const int slot = atomicAdd(&w.cnt[CNT_PAIRS], 1);
+        const int slot = agg_slot(&w.cnt[CNT_PAIRS]);
         if (slot < w.pair_cap) w.pairs[slot] = make_uint2((uint32_t)min(f, g), (uint32_t)max(f, g));
         else atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_RECORD_OVERFLOW);
     }
     /* most overlapping pairs already have a contact: test that first (the order of the tests
      * does not change which pairs are added) */
-    const uint32_t lo = rf < rg ? rf : rg, hi = rf < rg ? rg : rf;
-    const unsigned long long key = ((unsigned long long)lo << w.key_bits) | hi;
-    if (contact_exists(w, lo, key, n_contacts)) return;
+    if (contact_exists_from(w, lo, key, start, end, first, n_contacts)) return;
     /* add_pair: fixture A is the one with the smaller proxy id */
     int fa, fb;
     if (!pair_accept(w, rf < rg ? f : g, rf < rg ? g : f, fa, fb, !sp.custom_filter)) return;
-    const int slot = atomicAdd(&w.cnt[CNT_NEW], 1);
+    const int slot = agg_slot(&w.cnt[CNT_NEW]);
     if (slot < w.pair_cap) {
         w.n_key[slot] = key;
         w.n_fix[slot] = make_int2(fa, fb);
@@ -490,6 +489,57 @@ __device__ void handle_pair(const DevWorld& w, const StepParams& sp, int f, int 
     } else {
         atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_PAIR_OVERFLOW);
     }
+}
+
+/* The partner checks of up to kCheckBatch queued leaves of one lane (entries i0, i0 + 32, ...): the
+ * reference's rules (skip itself; skip a moved partner with the larger proxy id, which reports the
+ * pair) and add_pair. Each check is a chain of dependent loads (partner, its proxy id and moved
+ * flag, the contact row's bounds, its first key), so the batch issues each link of all its chains together.
+ * Returns the entries checked. */
+constexpr int kCheckBatch = 4;
+
+__device__ __forceinline__ unsigned check_batch(const DevWorld& w, const StepParams& sp, const uint2* queue, int i0, int nq,
+                                                int n_contacts) {
+    int ff[kCheckBatch], g[kCheckBatch];
+    bool ok[kCheckBatch];
+    unsigned n = 0;
+#pragma unroll
+    for (int k = 0; k < kCheckBatch; ++k) {
+        const int i = i0 + 32 * k;
+        ok[k] = i < nq;
+        const uint2 e = ok[k] ? queue[i] : make_uint2(0u, 0u);
+        ff[k] = (int)e.x;
+        g[k] = ok[k] ? (int)w.bp_val[e.y] : 0;
+        n += ok[k] ? 1u : 0u;
+    }
+    uint32_t rf[kCheckBatch], rg[kCheckBatch];
+#pragma unroll
+    for (int k = 0; k < kCheckBatch; ++k) {
+        rf[k] = ok[k] ? w.f_refid[ff[k]] : 0u;
+        rg[k] = ok[k] ? w.f_refid[g[k]] : 0u;
+        const bool moved = ok[k] && w.f_moved[g[k]] != 0;
+        ok[k] = ok[k] && g[k] != ff[k] && !(moved && rg[k] > rf[k]);
+    }
+    uint32_t lo[kCheckBatch];
+    int start[kCheckBatch], end[kCheckBatch];
+#pragma unroll
+    for (int k = 0; k < kCheckBatch; ++k) {
+        lo[k] = rf[k] < rg[k] ? rf[k] : rg[k];
+        start[k] = ok[k] ? w.c_row[lo[k]] : -1;
+        end[k] = ok[k] ? w.c_row_end[lo[k]] : -1;
+    }
+    unsigned long long first[kCheckBatch];
+#pragma unroll
+    for (int k = 0; k < kCheckBatch; ++k)
+        first[k] = ok[k] && start[k] >= 0 && start[k] < n_contacts ? w.c.key[start[k]] : ~0ull;
+#pragma unroll
+    for (int k = 0; k < kCheckBatch; ++k) {
+        if (!ok[k]) continue;
+        const uint32_t hi = rf[k] < rg[k] ? rg[k] : rf[k];
+        const unsigned long long key = ((unsigned long long)lo[k] << w.key_bits) | hi;
+        handle_pair(w, sp, ff[k], g[k], rf[k], rg[k], key, lo[k], start[k], end[k], first[k], n_contacts);
+    }
+    return n;
 }
 
 /* One lane per moved proxy starts a walk of the hierarchies, and a warp walks in step:
@@ -546,6 +596,8 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
         int nq = 0;
         /* queue the leaves found so far: a warp prefix sum gives each lane its place */
         auto enqueue = [&]() {
+            const unsigned finders = __ballot_sync(full, nfound > 0);
+            if (finders == 0u) return;  /* most steps of a walk find no leaf */
             int incl = nfound;
             for (int o = 1; o < 32; o <<= 1) {
                 const int y = __shfl_up_sync(full, incl, o);
@@ -608,15 +660,8 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
             const bool more = __any_sync(full, top > bot);
             if (nq >= 32 || (!more && nq > 0)) {
                 __syncwarp();
-                for (int i = lane; i < nq; i += 32) {
-                    ++candidates;
-                    const uint2 e = queue[i];
-                    const int ff = (int)e.x, g = (int)w.bp_val[e.y];
-                    if (g == ff) continue;
-                    const uint32_t rf = w.f_refid[ff];
-                    if (w.f_moved[g] && w.f_refid[g] > rf) continue;
-                    handle_pair(w, sp, ff, g, rf, n_contacts);
-                }
+                for (int i0 = lane; i0 < nq; i0 += 32 * kCheckBatch)
+                    candidates += check_batch(w, sp, queue, i0, nq, n_contacts);
                 __syncwarp();
                 nq = 0;
             }
@@ -643,10 +688,6 @@ __global__ void k_bp_clear_moved(DevWorld w) {
     }
 }
 
-__global__ void k_bp_clamp_new(DevWorld w) {
-    B2G_RETURN_IF_ABORTED(w);
-    if (blockIdx.x == 0 && threadIdx.x == 0 && w.cnt[CNT_NEW] > w.pair_cap) w.cnt[CNT_NEW] = w.pair_cap;
-}
 
 /* ---- merge of surviving contacts and new contacts (both key-sorted) ---- */
 __global__ void k_merge_flags(DevWorld w, uint32_t* flag) {
@@ -659,7 +700,7 @@ __global__ void k_merge_flags(DevWorld w, uint32_t* flag) {
 __global__ void k_merge_old(DevWorld w, const uint32_t* flag, const uint32_t* rank) {
     B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
-    const int nn = w.cnt[CNT_NEW];
+    const int nn = min(w.cnt[CNT_NEW], w.pair_cap);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (!flag[i]) continue;
         const int pos = (int)rank[i] + lower_bound_u64(w.n_key, nn, w.c.key[i]);
@@ -672,7 +713,7 @@ __global__ void k_merge_old(DevWorld w, const uint32_t* flag, const uint32_t* ra
 __global__ void k_merge_new(DevWorld w, const uint32_t* rank) {
     B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
-    const int nn = w.cnt[CNT_NEW];
+    const int nn = min(w.cnt[CNT_NEW], w.pair_cap);
     const int alive = w.cnt[CNT_ALIVE];
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nn; j += gridDim.x * blockDim.x) {
         const unsigned long long key = w.n_key[j];
@@ -692,7 +733,7 @@ __global__ void k_merge_finish(DevWorld w) {
     B2G_RETURN_IF_ABORTED(w);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         w.cnt[CNT_MERGE_FROM] = w.cnt[CNT_CONTACTS];
-        int total = w.cnt[CNT_ALIVE] + w.cnt[CNT_NEW];
+        int total = w.cnt[CNT_ALIVE] + min(w.cnt[CNT_NEW], w.pair_cap);
         if (total > w.contact_cap) {
             total = w.contact_cap;
             atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_CONTACT_OVERFLOW);
@@ -719,29 +760,23 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
     const int n = w.n_fixtures;
     const int gf = grid_for(n, kBlock, num_sms * 8);
     k_bp_decide<<<1, 32, 0, s>>>(w, mode); B2G_LAUNCHED(1);
-    k_bp_init<<<grid_for(2 * w.num_worlds, kBlock, 64), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
     if (n > 0) {
         k_bp_bounds<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_keys<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         radix_sort_pairs_coop(w.bp_key, w.bp_val, w.bp_key_alt, w.bp_val_alt, &w.cnt[CNT_BP_SORT_N], n,
                               kMortonBits + w.morton_world_bits, w.sort_hist, w.cnt, s, num_sms, true);
         if (mark) mark(0);
-        if (n > 1) {
-            k_bp_build<<<grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
-        }
-        k_bp_leaves<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        k_bp_build<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         k_bp_refit<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         if (n > 1) {
             k_bp_quad<<<grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         }
-        k_bp_update<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
-        k_bp_rows<<<grid_for(w.contact_cap, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        k_bp_update<<<grid_for(std::max(n, w.contact_cap), kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
         if (mark) mark(1);
         const int tb = w.cfg_traverse_block;
         k_bp_traverse<<<grid_for(n, tb, num_sms * 2048 / tb), tb, 0, s>>>(w, sp); B2G_LAUNCHED(1);
         k_bp_clear_moved<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
     }
-    k_bp_clamp_new<<<1, 32, 0, s>>>(w); B2G_LAUNCHED(1);
     if (mark) mark(2);
     /* sort new keys; payload = emission slot */
     radix_sort_pairs_coop(w.n_key, w.n_idx, w.n_key_alt, w.n_idx_alt, &w.cnt[CNT_NEW], w.pair_cap, 2 * w.key_bits,

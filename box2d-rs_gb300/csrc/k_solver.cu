@@ -96,93 +96,8 @@ __device__ __forceinline__ void uf_union(int* parent, int a, int b) {
     }
 }
 
-__global__ void k_island_init(DevWorld w) {
-    B2G_RETURN_IF_ABORTED(w);
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x) {
-        w.b_island[b] = b;
-        w.isl_minsep[w.body_cap + b] = 0u;  /* "island has an awake member" */
-        w.b_flags[b] &= ~BF_ISLAND;
-    }
-}
-
 __device__ __forceinline__ bool contact_is_constraint(uint32_t cf) {
     return (cf & (CF_TOUCHING | CF_ENABLED | CF_DEAD | CF_SENSOR)) == (CF_TOUCHING | CF_ENABLED);
-}
-
-__global__ void k_island_union(DevWorld w) {
-    B2G_RETURN_IF_ABORTED(w);
-    const int n = w.cnt[CNT_CONTACTS];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (!contact_is_constraint(w.c.flags[i])) continue;
-        const int2 bd = w.c.body[i];
-        if (is_static(w.b_flags[bd.x]) || is_static(w.b_flags[bd.y])) continue;
-        uf_union(w.b_island, bd.x, bd.y);
-    }
-    /* joints join islands too, unless a body is disabled (private/dynamics/b2_world.rs:466-489) */
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.n_joints; j += gridDim.x * blockDim.x) {
-        const int2 bd = w.j_body[j];
-        const uint32_t fa = w.b_flags[bd.x], fb = w.b_flags[bd.y];
-        if (is_static(fa) || is_static(fb) || !(fa & BF_ENABLED) || !(fb & BF_ENABLED)) continue;
-        uf_union(w.b_island, bd.x, bd.y);
-    }
-}
-
-__global__ void k_island_compress(DevWorld w) {
-    B2G_RETURN_IF_ABORTED(w);
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x) {
-        const int r = uf_find(w.b_island, b);
-        const uint32_t f = w.b_flags[b];
-        agg_atomic_or(w.isl_minsep + w.body_cap, r, ((f & BF_AWAKE) && (f & BF_ENABLED) && !is_static(f)) ? 1u : 0u);
-    }
-}
-
-__global__ void k_island_mark(DevWorld w) {
-    B2G_RETURN_IF_ABORTED(w);
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x) {
-        int r = w.b_island[b];
-        r = w.b_island[r];  /* compress left every body at most one hop from its root */
-        while (w.b_island[r] != r) r = w.b_island[r];
-        w.b_island[b] = r;
-        const uint32_t f = w.b_flags[b];
-        if (!is_static(f) && (f & BF_ENABLED) && w.isl_minsep[w.body_cap + r]) w.b_flags[b] = f | BF_AWAKE | BF_ISLAND;
-    }
-}
-
-/* flag[i] = 1 if contact i is a constraint of a solved island */
-__global__ void k_cons_flags(DevWorld w, uint32_t* flag) {
-    B2G_RETURN_IF_ABORTED(w);
-    const int n = w.cnt[CNT_CONTACTS];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t sel = 0;
-        if (contact_is_constraint(w.c.flags[i])) {
-            const int2 bd = w.c.body[i];
-            const uint32_t fa = w.b_flags[bd.x], fb = w.b_flags[bd.y];
-            sel = ((fa & BF_ISLAND) || (fb & BF_ISLAND)) ? 1u : 0u;
-        }
-        flag[i] = sel;
-    }
-}
-
-__global__ void k_cons_scatter(DevWorld w, const uint32_t* flag, const uint32_t* pos) {
-    B2G_RETURN_IF_ABORTED(w);
-    const int n = w.cnt[CNT_CONTACTS];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (!flag[i]) continue;
-        const int k = (int)pos[i];
-        if (k >= w.cons_cap) {
-            atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_CONTACT_OVERFLOW);
-            continue;
-        }
-        const int2 bd = w.c.body[i];
-        const int b = is_static(w.b_flags[bd.x]) ? bd.y : bd.x;
-        w.cons_contact[k] = i;
-        w.cons_island[k] = w.b_island[b];
-    }
-}
-
-__global__ void k_cons_clamp(DevWorld w) {
-    B2G_RETURN_IF_ABORTED(w);
-    if (threadIdx.x == 0 && blockIdx.x == 0 && w.cnt[CNT_CONS] > w.cons_cap) w.cnt[CNT_CONS] = w.cons_cap;
 }
 
 /* ---------------- colouring (cooperative) ---------------- */
@@ -1045,6 +960,99 @@ __device__ __forceinline__ void part_load(const PartCtx& pc, const float4* glob)
     }
 }
 
+/* Islands and the constraint list in one cooperative launch, its passes separated by grid barriers:
+ * reset, union over the constraints and joints (B2world::solve's DFS, private/dynamics/
+ * b2_world.rs:375-491, as connected components), each body's root and its island's awake flag,
+ * the solved bodies' flags, then the constraint list in contact order (each block counts its chunk
+ * of the table, the chunks' counts give each block its offset, and a block scan places the block's
+ * constraints). */
+__global__ void __launch_bounds__(kBlock) k_islands(DevWorld w, int allow_sleep) {
+    B2G_RETURN_IF_ABORTED(w);
+    grid_barrier_start();
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gsize = gridDim.x * blockDim.x;
+    const int nb = w.n_bodies;
+    for (int b = gtid; b < nb; b += gsize) {
+        w.b_island[b] = b;
+        w.isl_minsep[w.body_cap + b] = 0u;  /* "island has an awake member" */
+        w.b_flags[b] &= ~BF_ISLAND;
+        if (allow_sleep) w.isl_sleep[b] = kMaxFloat;
+    }
+    if (!grid_barrier(w)) return;
+    const int n = w.cnt[CNT_CONTACTS];
+    for (int i = gtid; i < n; i += gsize) {
+        if (!contact_is_constraint(w.c.flags[i])) continue;
+        const int2 bd = w.c.body[i];
+        if (is_static(w.b_flags[bd.x]) || is_static(w.b_flags[bd.y])) continue;
+        uf_union(w.b_island, bd.x, bd.y);
+    }
+    for (int j = gtid; j < w.n_joints; j += gsize) {
+        const int2 bd = w.j_body[j];
+        const uint32_t fa = w.b_flags[bd.x], fb = w.b_flags[bd.y];
+        if (is_static(fa) || is_static(fb) || !(fa & BF_ENABLED) || !(fb & BF_ENABLED)) continue;
+        uf_union(w.b_island, bd.x, bd.y);
+    }
+    if (!grid_barrier(w)) return;
+    for (int b = gtid; b < nb; b += gsize) {
+        const int r = uf_find(w.b_island, b);
+        const uint32_t f = w.b_flags[b];
+        agg_atomic_or(w.isl_minsep + w.body_cap, r, ((f & BF_AWAKE) && (f & BF_ENABLED) && !is_static(f)) ? 1u : 0u);
+    }
+    if (!grid_barrier(w)) return;
+    for (int b = gtid; b < nb; b += gsize) {
+        int r = w.b_island[b];
+        r = w.b_island[r];
+        while (w.b_island[r] != r) r = w.b_island[r];
+        w.b_island[b] = r;
+        const uint32_t f = w.b_flags[b];
+        if (!is_static(f) && (f & BF_ENABLED) && w.isl_minsep[w.body_cap + r]) w.b_flags[b] = f | BF_AWAKE | BF_ISLAND;
+    }
+    if (!grid_barrier(w)) return;
+    /* the constraint list: this block's chunk of the contact table */
+    const int chunk = (n + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int c0 = min(n, (int)blockIdx.x * chunk), c1 = min(n, c0 + chunk);
+    auto selected = [&](int i) {
+        if (!contact_is_constraint(w.c.flags[i])) return 0;
+        const int2 bd = w.c.body[i];
+        return ((w.b_flags[bd.x] & BF_ISLAND) || (w.b_flags[bd.y] & BF_ISLAND)) ? 1 : 0;
+    };
+    int mine = 0;
+    for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) mine += selected(i);
+    int block_total;
+    block_scan_excl(mine, &block_total);
+    if (threadIdx.x == 0) w.blk_tot[blockIdx.x] = (unsigned long long)block_total;
+    if (!grid_barrier(w)) return;
+    int before_part = 0, all_part = 0;
+    for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
+        const int t = (int)w.blk_tot[q];
+        if (q < (int)blockIdx.x) before_part += t;
+        all_part += t;
+    }
+    int before, all;
+    block_scan_excl(before_part, &before);
+    block_scan_excl(all_part, &all);
+    int carry = 0;
+    for (int base = c0; base < c1; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const int sel = i < c1 ? selected(i) : 0;
+        int tot;
+        const int ex = block_scan_excl(sel, &tot);
+        if (sel) {
+            const int k = before + carry + ex;
+            if (k < w.cons_cap) {
+                const int2 bd = w.c.body[i];
+                const int b = is_static(w.b_flags[bd.x]) ? bd.y : bd.x;
+                w.cons_contact[k] = i;
+                w.cons_island[k] = w.b_island[b];
+            } else {
+                atomicOr((unsigned*)&w.cnt[CNT_STATUS], ST_CONTACT_OVERFLOW);
+            }
+        }
+        carry += tot;
+    }
+    if (gtid == 0) w.cnt[CNT_CONS] = min(all, w.cons_cap);
+}
+
 /* k_solve runs 256 or 512 threads per block (cfg_solver_block); nothing in it depends on which */
 constexpr int kSolveMaxBlock = 512;
 
@@ -1406,12 +1414,6 @@ __global__ void __launch_bounds__(kSolveMaxBlock) k_solve(DevWorld w, StepParams
     if ((threadIdx.x & 31) == 0 && moved) atomicAdd(&w.cnt[CNT_BP_MOVED], (int)moved);
 }
 
-__global__ void k_sleep_init(DevWorld w) {
-    B2G_RETURN_IF_ABORTED(w);
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x)
-        w.isl_sleep[b] = kMaxFloat;
-}
-
 __global__ void k_set_transform(DevWorld w, int body, float px, float py, float angle) {
     /* B2body::set_transform, private/dynamics/b2_body.rs:418-447 */
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1449,20 +1451,15 @@ int coop_blocks(const void* fn, int num_sms) {
 }  // namespace
 
 void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cudaStream_t s) {
-    const int gb = grid_for(w.n_bodies, kBlock, w.num_sms * 8);
-    const int gc = grid_for(w.contact_cap, kBlock, w.num_sms * 8);
-    k_island_init<<<gb, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
-    k_island_union<<<gc, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
-    k_island_compress<<<gb, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
-    k_island_mark<<<gb, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
-    uint32_t* flag = w.scan_tmp;                        /* contact_cap */
-    uint32_t* pos = w.scan_tmp + w.contact_cap;          /* contact_cap */
-    uint32_t* tmp = w.scan_tmp + 2 * (size_t)w.contact_cap;
-    k_cons_flags<<<gc, kBlock, 0, s>>>(w, flag); B2G_LAUNCHED(1);
-    scan_exclusive_u32(flag, pos, &w.cnt[CNT_CONTACTS], w.contact_cap, tmp, &w.cnt[CNT_CONS], s);
-    k_cons_scatter<<<gc, kBlock, 0, s>>>(w, flag, pos); B2G_LAUNCHED(1);
-    k_cons_clamp<<<1, 32, 0, s>>>(w); B2G_LAUNCHED(1);
-    if (sp.allow_sleep) k_sleep_init<<<gb, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+    if (w.n_bodies > 0) {
+        DevWorld wc = w;
+        int allow_sleep = sp.allow_sleep;
+        void* args[] = {&wc, &allow_sleep};
+        cudaMemsetAsync(w.cnt + CNT_BARRIER, 0, sizeof(int), s);
+        cudaLaunchCooperativeKernel((const void*)k_islands, dim3(coop_blocks((const void*)k_islands, w.num_sms)),
+                                    dim3(kBlock), args, 0, s);
+        B2G_LAUNCHED(1);
+    }
 }
 
 /* Parts of the part-local solve: about one per 256 proxies, at most one per SM, whatever the

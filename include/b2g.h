@@ -217,9 +217,10 @@ int64_t b2g_get_launch_count(void);
  *                B2body::create_fixture (src/b2_body.rs:233) ---- */
 int b2g_create_bodies(void* world, const b2g_body_def* defs, int32_t n, uint32_t* out_ids);
 int b2g_create_fixtures(void* world, const b2g_fixture_def* defs, int32_t n, uint32_t* out_ids);
-/* B2world::create_joint (private/dynamics/b2_world.rs:156-276): revolute and distance joints. A joint that
- * does not let its bodies collide flags their contacts for the next collide, which destroys them.
- * A world with joints runs the grid-wide colour schedule (no part-local solve) and cannot be taped. */
+/* B2world::create_joint (private/dynamics/b2_world.rs:156-276): every joint type of b2g_joint_def (the ten
+ * of B2JointType). A joint that does not let its bodies collide flags their contacts for the next
+ * collide, which destroys them. A world with joints runs the grid-wide colour schedule (no
+ * part-local solve) and cannot be taped. */
 int b2g_create_joints(void* world, const b2g_joint_def* defs, int32_t n, uint32_t* out_ids);
 
 /* ---- destruction and filtering ----
