@@ -225,25 +225,31 @@ def timed_steps(world, scene, steps, flush, torch):
 
 
 def tune_blocks_per_sm(torch, flush, t, dt, vi, pi, turns=3, steps=3):
-    """After b2g_autotune (which times back-to-back steps): choose the solver's threads per block (one
-    block per SM: the part-local solve gives each block an SM's shared memory) on the scratch world
-    `t` the way this bench times a step (device time, L2 flushed before it); the settings take turns.
-    Returns the launch configuration to use."""
-    base = t.get_launch_config()
-    shapes = [(1, 256), (1, 512)]
-    total = dict.fromkeys(shapes, 0.0)
+    """After b2g_autotune (which times back-to-back steps with warm caches): choose among its pick, the
+    default configuration and both with 512 solver threads per block, on the scratch world `t`, the
+    way this bench times a step (device time, L2 flushed before it); the candidates take turns.
+    Returns the launch configuration to use (one block per SM: the part-local solve gives each block
+    an SM's shared memory)."""
+    tuned = t.get_launch_config()
+    default = {"coop_blocks_per_sm": 1, "collide_block": 128, "traverse_block": 256, "solver_block": 256}
+    cands = []
+    for base in (dict(tuned, coop_blocks_per_sm=1), default):
+        for sb in (256, 512):
+            c = dict(base, solver_block=sb)
+            if c not in cands:
+                cands.append(c)
+    total = [0.0] * len(cands)
     for _ in range(turns):
-        for c, sb in shapes:
-            t.set_launch_config(c, base["collide_block"], base["traverse_block"], sb)
+        for i, c in enumerate(cands):
+            t.set_launch_config(**c)
             for _ in range(2):  # the step graph's captures for both contact-buffer parities
                 t.step(dt, vi, pi)
             for _ in range(steps):
                 flush.fill_(1.0)
                 torch.cuda.synchronize()
                 t.step(dt, vi, pi)
-                total[(c, sb)] += t.get_profile()["step"]  # device time (CUDA events), as timed_steps
-    c, sb = min(total, key=total.get)
-    return dict(base, coop_blocks_per_sm=c, solver_block=sb)
+                total[i] += t.get_profile()["step"]  # device time (CUDA events), as timed_steps
+    return cands[min(range(len(cands)), key=lambda i: total[i])]
 
 
 def run_batched(torch, flush, device, num_worlds=4096, steps=300, warmup=3, per_bucket=6, rank=0, world_size=1,
