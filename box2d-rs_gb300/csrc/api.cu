@@ -627,7 +627,6 @@ int allocate(World* w, int nb, int nf, int keep_body_cap = 0, int keep_fix_cap =
     A(d.b_xf, body_cap); A(d.b_pos, body_cap); A(d.b_pos0, body_cap); A(d.b_vel, body_cap);
     A(d.b_force, body_cap); A(d.b_mass, body_cap); A(d.b_damp, body_cap); A(d.b_lc, body_cap);
     A(d.b_flags, body_cap); A(d.b_world, body_cap); A(d.b_island, body_cap); A(d.b_rank, body_cap);
-    A(d.b_deg, 2 * (size_t)body_cap);
     A(d.b_part, body_cap); A(d.b_cidx, body_cap);
     A(d.b_cmin, 4 * (size_t)body_cap); A(d.b_cmask, 2 * (size_t)body_cap);
     /* one per-island separation buffer per position iteration (at least 2: the island pass

@@ -201,8 +201,6 @@ struct DevWorld {
     int* b_rank;                 /* smallest sorted position of the body's proxies in the last
                                     broadphase (Morton order), INT_MAX if none */
     int* b_part;                 /* part-local solve: the body's part (valid for constraint bodies) */
-    int* b_deg;                  /* colouring: constraints of each class at the body (2 x body_cap,
-                                    interior then boundary; zero between colourings) */
     int* b_cidx;                 /* part-local solve: the body's place among constraint bodies in
                                     rank order (valid for constraint bodies) */
     unsigned long long* b_cmin;  /* colouring: minimum priority of uncoloured constraints,

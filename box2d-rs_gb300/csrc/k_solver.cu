@@ -110,15 +110,6 @@ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
     return x;
 }
 
-/* Jones-Plassmann priority of constraint k (smaller key first): the constraints whose bodies carry
- * the most constraints of the same class go first (they have the fewest colours to choose from),
- * then a hash; the index makes every key unique. */
-__device__ __forceinline__ unsigned long long jp_key(const DevWorld& w, int k, int2 bd, size_t cm) {
-    const int deg = w.b_deg[cm + bd.x] + w.b_deg[cm + bd.y];
-    const uint32_t prio = ((uint32_t)(255 - min(deg, 255)) << 24) | (hash32((uint32_t)k) & 0xffffffu);
-    return ((unsigned long long)prio << 32) | (uint32_t)k;
-}
-
 /* Block-wide exclusive scan of one int per thread (blockDim.x == kBlock); *total gets the sum. */
 __device__ __forceinline__ int block_scan_excl(int v, int* total) {
     __shared__ int s_warp[kBlock / 32];
@@ -207,7 +198,7 @@ __device__ int colour_tail(const DevWorld& w, int round) {
                 stale[cm + bd.y] = kNone;
             }
             if (w.cons_colour[k] >= 0) continue;
-            const unsigned long long key = jp_key(w, k, bd, cm);
+            const unsigned long long key = ((unsigned long long)hash32((uint32_t)k) << 32) | (uint32_t)k;
             if (is_dynamic(w.b_flags[bd.x])) atomicMin(&offer[cm + bd.x], key);
             if (is_dynamic(w.b_flags[bd.y])) atomicMin(&offer[cm + bd.y], key);
         }
@@ -218,7 +209,7 @@ __device__ int colour_tail(const DevWorld& w, int round) {
             if (w.cons_colour[k] >= 0) continue;
             const int2 bd = w.c.body[w.cons_contact[k]];
             const size_t cm = w.cons_part[k] < 0 ? bc : 0;
-            const unsigned long long key = jp_key(w, k, bd, cm);
+            const unsigned long long key = ((unsigned long long)hash32((uint32_t)k) << 32) | (uint32_t)k;
             const bool da = is_dynamic(w.b_flags[bd.x]), db = is_dynamic(w.b_flags[bd.y]);
             const bool winA = !da || offer[cm + bd.x] == key;
             const bool winB = !db || offer[cm + bd.y] == key;
@@ -419,12 +410,6 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
         }
         w.cons_part[k] = part;
         const uint32_t cls = part < 0 ? 1u : 0u;
-        {   /* the class's constraint count at each dynamic body (jp_key's degree) */
-            const int2 bd = w.c.body[ci];
-            const size_t cm = cls ? bc : 0;
-            if (is_dynamic(w.b_flags[bd.x])) atomicAdd(&w.b_deg[cm + bd.x], 1);
-            if (is_dynamic(w.b_flags[bd.y])) atomicAdd(&w.b_deg[cm + bd.y], 1);
-        }
         const uint32_t kept = w.c.mids[ci].w;
         w.cons_colour[k] = (keep && (kept >> 7) == stamp && ((kept >> 6) & 1u) == cls) ? (int)(kept & 63u) : -1;
     }
@@ -484,7 +469,7 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
                 stale[cm + bd.y] = kNone;
             }
             if (w.cons_colour[k] >= 0) continue;
-            const unsigned long long key = jp_key(w, k, bd, cm);
+            const unsigned long long key = ((unsigned long long)hash32((uint32_t)k) << 32) | (uint32_t)k;
             if (is_dynamic(w.b_flags[bd.x])) atomicMin(&offer[cm + bd.x], key);
             if (is_dynamic(w.b_flags[bd.y])) atomicMin(&offer[cm + bd.y], key);
         }
@@ -495,7 +480,7 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
             if (w.cons_colour[k] >= 0) continue;
             const int2 bd = w.c.body[w.cons_contact[k]];
             const size_t cm = w.cons_part[k] < 0 ? bc : 0;
-            const unsigned long long key = jp_key(w, k, bd, cm);
+            const unsigned long long key = ((unsigned long long)hash32((uint32_t)k) << 32) | (uint32_t)k;
             const bool da = is_dynamic(w.b_flags[bd.x]), db = is_dynamic(w.b_flags[bd.y]);
             const bool winA = !da || offer[cm + bd.x] == key;
             const bool winB = !db || offer[cm + bd.y] == key;
@@ -524,15 +509,10 @@ __global__ void __launch_bounds__(kBlock) k_colour(DevWorld w, int nparts) {
         if (!grid_barrier(w)) return;
     }
     if (gtid == 0 && w.cnt[CNT_TAIL] == 0) w.cnt[CNT_ROUNDS] = round;
-    /* histogram rows: part p's interior colours are row p, the boundary colours row P; the degree
-     * counts go back to zero for the next colouring */
+    /* histogram rows: part p's interior colours are row p, the boundary colours row P */
     for (int k = gtid; k < n; k += gsize) {
         const int part = w.cons_part[k];
         atomicAdd(&w.col_hist[(part < 0 ? P : part) * kMaxColours + w.cons_colour[k]], 1);
-        const int2 bd = w.c.body[w.cons_contact[k]];
-        const size_t cm = part < 0 ? bc : 0;
-        w.b_deg[cm + bd.x] = 0;
-        w.b_deg[cm + bd.y] = 0;
     }
     if (!grid_barrier(w)) return;
     for (int r = blockIdx.x; r <= P; r += gridDim.x) {
