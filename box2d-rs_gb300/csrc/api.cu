@@ -650,7 +650,7 @@ int allocate(World* w, int nb, int nf, int keep_body_cap = 0, int keep_fix_cap =
     A(d.cons_part, contact_cap); A(d.col_tail, kColourTail);
     A(d.col_off, kMaxColours + 1); A(d.col_hist, (size_t)(kMaxParts + 1) * kMaxColours);
     A(d.part_off, (size_t)kMaxParts * (kMaxColours + 1)); A(d.part_ncol, kMaxParts); A(d.part_tot, kMaxParts + 1);
-    A(d.rank_x, fix_cap); A(d.blk_tot, kMaxParts); A(d.cache_body, fix_cap);
+    A(d.rank_x, fix_cap); A(d.blk_tot, std::max(kMaxParts, 8 * w->num_sms)); A(d.cache_body, fix_cap);
     A(d.part_cbeg, kMaxParts); A(d.part_cend, kMaxParts); A(d.part_rbeg, kMaxParts);
     A(d.vc_idx, contact_cap); A(d.vc_inv, contact_cap); A(d.vc_nf, contact_cap); A(d.vc_r0, contact_cap);
     A(d.vc_r1, contact_cap); A(d.vc_m0, contact_cap); A(d.vc_m1, contact_cap); A(d.vc_imp, contact_cap);

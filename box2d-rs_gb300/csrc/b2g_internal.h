@@ -252,7 +252,8 @@ struct DevWorld {
     int* part_tot;               /* kMaxParts + 1: slots of each histogram row */
     unsigned long long* rank_x;  /* per Morton rank: constraint endpoints << 32 | has-any, then
                                     its exclusive prefix within the scanning block's chunk */
-    unsigned long long* blk_tot; /* kMaxParts: chunk totals of that scan */
+    unsigned long long* blk_tot; /* per block of a cooperative launch (at least kMaxParts and 8 per SM): chunk
+                                    totals of that scan and of k_islands' constraint count */
     int* cache_body;             /* constraint bodies in rank order */
     int* part_cbeg;              /* kMaxParts: each part's first entry of cache_body */
     int* part_cend;              /* kMaxParts: one past its last */
@@ -348,6 +349,31 @@ __device__ __forceinline__ bool world_aborted(const int* cnt) {
     do {                          \
         if (world_aborted((w).cnt)) return; \
     } while (0)
+
+/* Programmatic dependent launch: a kernel launched with launch_pdl may be scheduled while the
+ * kernel before it on the stream drains (its launch no longer waits behind that kernel's last
+ * block). pdl_entry() waits until that kernel has completed and its writes are visible (at once for
+ * a kernel launched without the attribute) and lets the next kernel be scheduled in turn; every
+ * kernel launched with launch_pdl calls it before it reads memory. */
+__device__ __forceinline__ void pdl_entry() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
 
 /* kernel-file launchers */
 /* may_sleep: some body may be asleep (sleeping allowed, or a body made asleep): contacts then see

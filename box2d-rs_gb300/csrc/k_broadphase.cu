@@ -68,6 +68,7 @@ __device__ __forceinline__ uint32_t spread16(uint32_t x) {
  * state, so a world and its checkpointed copy decide alike. A repeated pass (the same pass run again
  * after its capacities grew) keeps the decision. */
 __global__ void k_bp_decide(DevWorld w, int mode) {
+    pdl_entry();
     B2G_RETURN_IF_ABORTED(w);
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     int* c = w.cnt;
@@ -103,6 +104,7 @@ __device__ __forceinline__ bool bp_rebuilding(const DevWorld& w) { return w.cnt[
 
 
 __global__ void k_bp_bounds(DevWorld w) {
+    pdl_entry();
     B2G_RETURN_IF_ABORTED(w);
     if (!bp_rebuilding(w)) return;
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.n_bodies; b += gridDim.x * blockDim.x)
@@ -159,6 +161,7 @@ __global__ void k_bp_bounds(DevWorld w) {
 }
 
 __global__ void k_bp_keys(DevWorld w) {
+    pdl_entry();
     B2G_RETURN_IF_ABORTED(w);
     if (!bp_rebuilding(w)) return;
     float lx = 0.0f, ly = 0.0f, sx = 0.0f, sy = 0.0f;
@@ -200,6 +203,7 @@ __device__ __forceinline__ int delta(const unsigned long long* k, int n, int i, 
 
 /* Karras, "Maximizing parallelism in the construction of BVHs, octrees, and k-d trees" (HPG 2012) */
 __global__ void k_bp_build(DevWorld w) {
+    pdl_entry();
     B2G_RETURN_IF_ABORTED(w);
     if (!bp_rebuilding(w)) return;
     const int n = w.n_fixtures;
@@ -265,6 +269,7 @@ __device__ __forceinline__ unsigned arrive_acq_rel(unsigned* p) {
 /* Bottom-up: each leaf's thread stores its box in its parent's record and arrives; the second of
  * the two children to arrive reads its sibling's box (in L2) and carries the union up. */
 __global__ void k_bp_refit(DevWorld w) {
+    pdl_entry();
     B2G_RETURN_IF_ABORTED(w);
     if (!bp_rebuilding(w)) return;
     const int n = w.n_fixtures;
@@ -293,6 +298,7 @@ __device__ __forceinline__ bool box_overlap(float4 a, float4 b) { return overlap
  * stands for itself). A traversal then tests four boxes per dependent fetch and descends two
  * levels at a time; the pairs found do not depend on the hierarchy's shape. */
 __global__ void k_bp_quad(DevWorld w) {
+    pdl_entry();
     B2G_RETURN_IF_ABORTED(w);
     if (!bp_rebuilding(w)) return;
     const int n = w.n_fixtures;
@@ -369,6 +375,7 @@ __device__ __forceinline__ int quad_place(const DevWorld& w, int node, int id) {
  * that record past it carries the growth further up, so when the kernel ends every ancestor covers
  * every leaf below it. */
 __global__ void k_bp_update(DevWorld w) {
+    pdl_entry();
     B2G_RETURN_IF_ABORTED(w);
     /* every pass: the row index of the key-sorted contact table, c_row[r] = the first contact whose
      * key's high part is proxy id r. Entries of ids with no contact keep stale values; a reader
@@ -553,6 +560,7 @@ constexpr int kLeafQueue = 224;  /* 31 left over + 32 lanes x 4 leaves in one ro
                                     2 single-proxy roots per lane */
 
 __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams sp) {
+    pdl_entry();
     B2G_RETURN_IF_ABORTED(w);
     __shared__ uint2 s_queue[kBlock / 32][kLeafQueue];
     __shared__ int s_give_node[kBlock / 32][32];
@@ -681,6 +689,7 @@ __global__ void __launch_bounds__(kBlock) k_bp_traverse(DevWorld w, StepParams s
 /* the moved flags are consumed; the colouring's rank weights start from zero (they are indexed by
  * Morton rank, of which there are as many as proxies) */
 __global__ void k_bp_clear_moved(DevWorld w) {
+    pdl_entry();
     B2G_RETURN_IF_ABORTED(w);
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < w.n_fixtures; f += gridDim.x * blockDim.x) {
         w.f_moved[f] = 0;
@@ -691,6 +700,7 @@ __global__ void k_bp_clear_moved(DevWorld w) {
 
 /* ---- merge of surviving contacts and new contacts (both key-sorted) ---- */
 __global__ void k_merge_flags(DevWorld w, uint32_t* flag) {
+    pdl_entry();
     B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -698,6 +708,7 @@ __global__ void k_merge_flags(DevWorld w, uint32_t* flag) {
 }
 
 __global__ void k_merge_old(DevWorld w, const uint32_t* flag, const uint32_t* rank) {
+    pdl_entry();
     B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
     const int nn = min(w.cnt[CNT_NEW], w.pair_cap);
@@ -711,6 +722,7 @@ __global__ void k_merge_old(DevWorld w, const uint32_t* flag, const uint32_t* ra
 
 /* b2_contact_create + B2contact::new (private/dynamics/b2_contact.rs:11-60): mixing laws of src/b2_contact.rs:29-46 */
 __global__ void k_merge_new(DevWorld w, const uint32_t* rank) {
+    pdl_entry();
     B2G_RETURN_IF_ABORTED(w);
     const int n = w.cnt[CNT_CONTACTS];
     const int nn = min(w.cnt[CNT_NEW], w.pair_cap);
@@ -730,6 +742,7 @@ __global__ void k_merge_new(DevWorld w, const uint32_t* rank) {
 }
 
 __global__ void k_merge_finish(DevWorld w) {
+    pdl_entry();
     B2G_RETURN_IF_ABORTED(w);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         w.cnt[CNT_MERGE_FROM] = w.cnt[CNT_CONTACTS];
@@ -759,23 +772,24 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
                        const std::function<void(int)>& mark, int mode) {
     const int n = w.n_fixtures;
     const int gf = grid_for(n, kBlock, num_sms * 8);
-    k_bp_decide<<<1, 32, 0, s>>>(w, mode); B2G_LAUNCHED(1);
+    launch_pdl(k_bp_decide, 1, 32, 0, s, w, mode); B2G_LAUNCHED(1);
     if (n > 0) {
-        k_bp_bounds<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
-        k_bp_keys<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        launch_pdl(k_bp_bounds, gf, kBlock, 0, s, w); B2G_LAUNCHED(1);
+        launch_pdl(k_bp_keys, gf, kBlock, 0, s, w); B2G_LAUNCHED(1);
         radix_sort_pairs_coop(w.bp_key, w.bp_val, w.bp_key_alt, w.bp_val_alt, &w.cnt[CNT_BP_SORT_N], n,
                               kMortonBits + w.morton_world_bits, w.sort_hist, w.cnt, s, num_sms, true);
         if (mark) mark(0);
-        k_bp_build<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
-        k_bp_refit<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        launch_pdl(k_bp_build, gf, kBlock, 0, s, w); B2G_LAUNCHED(1);
+        launch_pdl(k_bp_refit, gf, kBlock, 0, s, w); B2G_LAUNCHED(1);
         if (n > 1) {
-            k_bp_quad<<<grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+            launch_pdl(k_bp_quad, grid_for(n - 1, kBlock, num_sms * 8), kBlock, 0, s, w); B2G_LAUNCHED(1);
         }
-        k_bp_update<<<grid_for(std::max(n, w.contact_cap), kBlock, num_sms * 8), kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        launch_pdl(k_bp_update, grid_for(std::max(n, w.contact_cap), kBlock, num_sms * 8), kBlock, 0, s, w);
+        B2G_LAUNCHED(1);
         if (mark) mark(1);
         const int tb = w.cfg_traverse_block;
-        k_bp_traverse<<<grid_for(n, tb, num_sms * 2048 / tb), tb, 0, s>>>(w, sp); B2G_LAUNCHED(1);
-        k_bp_clear_moved<<<gf, kBlock, 0, s>>>(w); B2G_LAUNCHED(1);
+        launch_pdl(k_bp_traverse, grid_for(n, tb, num_sms * 2048 / tb), tb, 0, s, w, sp); B2G_LAUNCHED(1);
+        launch_pdl(k_bp_clear_moved, gf, kBlock, 0, s, w); B2G_LAUNCHED(1);
     }
     if (mark) mark(2);
     /* sort new keys; payload = emission slot */
@@ -785,11 +799,12 @@ void launch_broadphase(const DevWorld& w, const StepParams& sp, cudaStream_t s, 
     uint32_t* rank = w.scan_tmp + w.contact_cap;
     uint32_t* tmp = w.scan_tmp + 2 * (size_t)w.contact_cap;
     const int gc = grid_for(w.contact_cap, kBlock, num_sms * 8);
-    k_merge_flags<<<gc, kBlock, 0, s>>>(w, flag); B2G_LAUNCHED(1);
+    launch_pdl(k_merge_flags, gc, kBlock, 0, s, w, flag); B2G_LAUNCHED(1);
     scan_exclusive_u32(flag, rank, &w.cnt[CNT_CONTACTS], w.contact_cap, tmp, &w.cnt[CNT_ALIVE], s);
-    k_merge_old<<<gc, kBlock, 0, s>>>(w, flag, rank); B2G_LAUNCHED(1);
-    k_merge_new<<<grid_for(w.pair_cap, kBlock, num_sms * 8), kBlock, 0, s>>>(w, rank); B2G_LAUNCHED(1);
-    k_merge_finish<<<1, 32, 0, s>>>(w); B2G_LAUNCHED(1);
+    launch_pdl(k_merge_old, gc, kBlock, 0, s, w, (const uint32_t*)flag, (const uint32_t*)rank); B2G_LAUNCHED(1);
+    launch_pdl(k_merge_new, grid_for(w.pair_cap, kBlock, num_sms * 8), kBlock, 0, s, w, (const uint32_t*)rank);
+    B2G_LAUNCHED(1);
+    launch_pdl(k_merge_finish, 1, 32, 0, s, w); B2G_LAUNCHED(1);
 }
 
 }  // namespace b2g

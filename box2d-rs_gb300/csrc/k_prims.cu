@@ -82,6 +82,7 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
 
 __global__ void k_scan_tiles(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, const int* d_n, int max_n,
                              uint32_t* __restrict__ tile_sums) {
+    pdl_entry();
     const int n = load_n(d_n, max_n);
     const int base = blockIdx.x * kScanTile;
     if (base >= n) {
@@ -109,6 +110,7 @@ __global__ void k_scan_tiles(const uint32_t* __restrict__ in, uint32_t* __restri
 
 /* one block scans all tile sums (looping over chunks), writes the grand total */
 __global__ void k_scan_sums(uint32_t* tile_sums, int tiles, int* d_total) {
+    pdl_entry();
     __shared__ uint32_t carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
@@ -126,6 +128,7 @@ __global__ void k_scan_sums(uint32_t* tile_sums, int tiles, int* d_total) {
 }
 
 __global__ void k_scan_add(uint32_t* __restrict__ out, const int* d_n, int max_n, const uint32_t* __restrict__ tile_sums) {
+    pdl_entry();
     const int n = load_n(d_n, max_n);
     const int base = blockIdx.x * kScanTile;
     if (base >= n) return;
@@ -283,6 +286,7 @@ constexpr int kRankBlocks = 1024;
 
 __global__ void __launch_bounds__(kRankTile) k_rank_count(const unsigned long long* __restrict__ keys, const int* d_n,
                                                           int max_n, uint32_t* rank, int* cnt) {
+    pdl_entry();
     if (world_aborted(cnt)) return;
     const int n = load_n(d_n, max_n);
     if (n <= kSortTile || n > kRankSort) return;
@@ -313,6 +317,7 @@ __global__ void __launch_bounds__(kRankTile) k_rank_count(const unsigned long lo
 __global__ void k_rank_scatter(const unsigned long long* __restrict__ kin, const uint32_t* __restrict__ vin,
                                unsigned long long* __restrict__ kout, uint32_t* __restrict__ vout, const int* d_n,
                                int max_n, const uint32_t* rank, int* cnt) {
+    pdl_entry();
     if (world_aborted(cnt)) return;
     const int n = load_n(d_n, max_n);
     if (n <= kSortTile || n > kRankSort) return;
@@ -328,6 +333,7 @@ __global__ void k_rank_scatter(const unsigned long long* __restrict__ kin, const
 __global__ void k_rank_copy(const unsigned long long* __restrict__ kin, const uint32_t* __restrict__ vin,
                             unsigned long long* __restrict__ kout, uint32_t* __restrict__ vout, const int* d_n, int max_n,
                             int* cnt) {
+    pdl_entry();
     if (world_aborted(cnt)) return;
     const int n = load_n(d_n, max_n);
     if (n <= kSortTile || n > kRankSort) return;
@@ -433,9 +439,9 @@ void scan_exclusive_u32(const uint32_t* in, uint32_t* out, const int* d_n, int m
                         cudaStream_t s) {
     const int tiles = (max_n + kScanTile - 1) / kScanTile;
     if (tiles == 0) return;
-    k_scan_tiles<<<tiles, kScanBlock, 0, s>>>(in, out, d_n, max_n, tmp); B2G_LAUNCHED(1);
-    k_scan_sums<<<1, 1024, 0, s>>>(tmp, tiles, d_total); B2G_LAUNCHED(1);
-    k_scan_add<<<tiles, kScanBlock, 0, s>>>(out, d_n, max_n, tmp); B2G_LAUNCHED(1);
+    launch_pdl(k_scan_tiles, tiles, kScanBlock, 0, s, in, out, d_n, max_n, tmp); B2G_LAUNCHED(1);
+    launch_pdl(k_scan_sums, 1, 1024, 0, s, tmp, tiles, d_total); B2G_LAUNCHED(1);
+    launch_pdl(k_scan_add, tiles, kScanBlock, 0, s, out, d_n, max_n, (const uint32_t*)tmp); B2G_LAUNCHED(1);
 }
 
 void radix_sort_pairs_coop(unsigned long long* key_a, uint32_t* val_a, unsigned long long* key_b, uint32_t* val_b,
@@ -454,9 +460,11 @@ void radix_sort_pairs_coop(unsigned long long* key_a, uint32_t* val_a, unsigned 
         const int m = std::min(max_n, kRankSort);
         const int tiles = (m + kRankTile - 1) / kRankTile;
         cudaMemsetAsync(hist, 0, (size_t)m * sizeof(uint32_t), s);
-        k_rank_count<<<kRankBlocks, kRankTile, 0, s>>>(key_a, d_n, max_n, hist, cnt);
-        k_rank_scatter<<<tiles, kRankTile, 0, s>>>(key_a, val_a, key_b, val_b, d_n, max_n, hist, cnt);
-        k_rank_copy<<<tiles, kRankTile, 0, s>>>(key_b, val_b, key_a, val_a, d_n, max_n, cnt);
+        launch_pdl(k_rank_count, kRankBlocks, kRankTile, 0, s, (const unsigned long long*)key_a, d_n, max_n, hist, cnt);
+        launch_pdl(k_rank_scatter, tiles, kRankTile, 0, s, (const unsigned long long*)key_a, (const uint32_t*)val_a,
+                   key_b, val_b, d_n, max_n, (const uint32_t*)hist, cnt);
+        launch_pdl(k_rank_copy, tiles, kRankTile, 0, s, (const unsigned long long*)key_b, (const uint32_t*)val_b, key_a,
+                   val_a, d_n, max_n, cnt);
         B2G_LAUNCHED(3);
     }
     void* args[] = {&key_a, &val_a, &key_b, &val_b, (void*)&d_n, &max_n, &bits, &hist, &cnt};

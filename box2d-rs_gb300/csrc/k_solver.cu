@@ -1450,14 +1450,22 @@ int coop_blocks(const void* fn, int num_sms) {
 
 }  // namespace
 
+/* k_islands runs one block per SM for a world of up to 64k bodies and more blocks per SM for larger
+ * ones (up to what can be co-resident): its passes stride over all bodies and contacts, so a large
+ * batch wants more threads in flight, while a small world wants the shortest grid barriers. */
 void launch_islands_and_constraints(const DevWorld& w, const StepParams& sp, cudaStream_t s) {
     if (w.n_bodies > 0) {
+        static int resident = 0;
+        if (!resident) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, (const void*)k_islands, kBlock, 0);
+            resident = std::max(1, std::min(resident, 8));
+        }
+        const int per_sm = std::max(1, std::min(resident, w.n_bodies / 65536));
         DevWorld wc = w;
         int allow_sleep = sp.allow_sleep;
         void* args[] = {&wc, &allow_sleep};
         cudaMemsetAsync(w.cnt + CNT_BARRIER, 0, sizeof(int), s);
-        cudaLaunchCooperativeKernel((const void*)k_islands, dim3(coop_blocks((const void*)k_islands, w.num_sms)),
-                                    dim3(kBlock), args, 0, s);
+        cudaLaunchCooperativeKernel((const void*)k_islands, dim3(w.num_sms * per_sm), dim3(kBlock), args, 0, s);
         B2G_LAUNCHED(1);
     }
 }
@@ -1484,7 +1492,15 @@ bool use_parts(const DevWorld& w, int num_sms, bool allowed) {
 }
 
 void launch_colouring(const DevWorld& w, cudaStream_t s, int num_sms, bool parts) {
-    const int blocks = coop_blocks((const void*)k_colour, num_sms) * w.cfg_coop_per_sm;
+    /* more blocks per SM for large worlds (as k_islands): the colouring's passes stride over every
+     * constraint and body */
+    static int resident = 0;
+    if (!resident) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, (const void*)k_colour, kBlock, 0);
+        resident = std::max(1, std::min(resident, 8));
+    }
+    const int per_sm = std::max(w.cfg_coop_per_sm, std::min(resident, w.n_bodies / 65536));
+    const int blocks = coop_blocks((const void*)k_colour, num_sms) * per_sm;
     DevWorld wc = w;
     int nparts = use_parts(w, num_sms, parts) ? part_count(w, num_sms) : 0;
     void* args[] = {&wc, &nparts};
