@@ -117,7 +117,7 @@ def bytes_model(st, scene_stats, vi, pi):
     k_solve        per dynamic body: integrate velocities 72 B, integrate positions 48 B, write-back 40 B;
                    per proxy: fixture sync 76 B + shape bytes; per constraint slot: init + warm start
                    320 B, velocity iteration 208 B, position iteration 128 B, store 16 B
-    k_collide      per contact: 116 B state + 2 shape records (polygon 16 B/vertex + 12, circle 12, edge 36)
+    k_collide      per contact: 116 B state + 2 shapes (polygon 16 B/vertex + 12, circle 12, edge 36)
     bp_sort        per proxy: bounds 24 B + keys 28 B + 4 radix passes x 24 B (key + payload read and
                    written); nothing when the pass keeps the hierarchy (hierarchy_age > 0)
     bp_hierarchy   per proxy: build 36 B, leaves 36 B, refit 68 B, four-way records 144 B; per contact:
@@ -231,7 +231,8 @@ def tune_blocks_per_sm(torch, flush, t, dt, vi, pi, turns=3, steps=3):
     Returns the launch configuration to use (one block per SM: the part-local solve gives each block
     an SM's shared memory)."""
     tuned = t.get_launch_config()
-    default = {"coop_blocks_per_sm": 1, "collide_block": 128, "traverse_block": 256, "solver_block": 256}
+    default = {"coop_blocks_per_sm": 1, "collide_block": 128, "traverse_block": 256, "solver_block": 256,
+               "collide_group": 0}
     cands = []
     for base in (dict(tuned, coop_blocks_per_sm=1), default):
         for sb in (256, 512):

@@ -391,7 +391,8 @@ assert TAPE_SLOT.itemsize == 144 and TAPE_STEP.itemsize == 48
 
 class LaunchConfig(ctypes.Structure):
     _fields_ = [("coop_blocks_per_sm", ctypes.c_int32), ("collide_block", ctypes.c_int32),
-                ("traverse_block", ctypes.c_int32), ("tuning_steps", ctypes.c_int32), ("solver_block", ctypes.c_int32)]
+                ("traverse_block", ctypes.c_int32), ("tuning_steps", ctypes.c_int32), ("solver_block", ctypes.c_int32),
+                ("collide_group", ctypes.c_int32)]
 
     def as_dict(self):
         return {n: int(getattr(self, n)) for n, _ in self._fields_ if n != "tuning_steps"}
@@ -1052,8 +1053,9 @@ class B2world:
         self._check(self._lib.b2g_get_launch_config(self._h, ctypes.byref(c)))
         return c.as_dict()
 
-    def set_launch_config(self, coop_blocks_per_sm=1, collide_block=128, traverse_block=256, solver_block=256):
-        c = LaunchConfig(coop_blocks_per_sm, collide_block, traverse_block, 0, solver_block)
+    def set_launch_config(self, coop_blocks_per_sm=1, collide_block=128, traverse_block=256, solver_block=256,
+                          collide_group=0):
+        c = LaunchConfig(coop_blocks_per_sm, collide_block, traverse_block, 0, solver_block, collide_group)
         self._check(self._lib.b2g_set_launch_config(self._h, ctypes.byref(c)))
 
     def autotune(self, dt, velocity_iterations, position_iterations, steps_per_candidate=4):

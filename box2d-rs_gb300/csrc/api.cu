@@ -66,7 +66,7 @@ struct GraphSlot {
 /* launch configuration: the user's (b2g_set_launch_config), else the autotuner's choice for the
  * world's size bucket if one was made in this process, else the defaults */
 struct LaunchCfg {
-    int coop_per_sm = 1, collide_block = 128, traverse_block = 256, solver_block = 256;
+    int coop_per_sm = 1, collide_block = 128, traverse_block = 256, solver_block = 256, collide_group = kCollideGroup;
 };
 
 std::mutex g_tune_mutex;
@@ -210,6 +210,7 @@ void apply_launch_config(World* w) {
     w->d.cfg_collide_block = w->cfg.collide_block;
     w->d.cfg_traverse_block = w->cfg.traverse_block;
     w->d.cfg_solver_block = w->cfg.coop_per_sm == 1 ? w->cfg.solver_block : 256;
+    w->d.cfg_collide_group = w->cfg.collide_group;
 }
 
 
@@ -635,8 +636,9 @@ int allocate(World* w, int nb, int nf, int keep_body_cap = 0, int keep_fix_cap =
     A(d.isl_minsep, (size_t)w->minsep_buffers * body_cap); A(d.isl_done, body_cap); A(d.isl_sleep, body_cap);
     A(d.b_wake, body_cap); A(d.b_dwake, body_cap); A(d.c_done, contact_cap);
     cudaMemsetAsync(d.b_wake, 0x7f, (size_t)body_cap * sizeof(int), w->stream);  /* kNoWake */
-    A(d.f_shape, fix_cap); A(d.f_body, fix_cap); A(d.f_mat, fix_cap); A(d.f_filter, fix_cap);
-    A(d.f_group, fix_cap); A(d.f_refid, fix_cap); A(d.f_fat, fix_cap); A(d.f_moved, fix_cap);
+    A(d.f_shape, fix_cap); A(d.f_vn, (size_t)kMaxPolygonVertices * fix_cap); A(d.f_hdr, fix_cap);
+    A(d.f_body, fix_cap); A(d.f_mat, fix_cap); A(d.f_filter, fix_cap); A(d.f_group, fix_cap);
+    A(d.f_refid, fix_cap); A(d.f_fat, fix_cap); A(d.f_moved, fix_cap);
     Contacts* cs[2] = {&d.c, &d.c_alt};
     for (Contacts* c : cs) {
         A(c->key, contact_cap); A(c->fix, contact_cap); A(c->body, contact_cap); A(c->flags, contact_cap);
@@ -700,6 +702,7 @@ int upload(World* w) {
     if (nf > 0) {
         U(d.f_shape, w->h_shape); U(d.f_body, w->h_fbody); U(d.f_mat, w->h_fmat); U(d.f_filter, w->h_filter);
         U(d.f_group, w->h_group); U(d.f_refid, w->h_refid); U(d.f_fat, w->h_fat); U(d.f_moved, w->h_moved);
+        launch_shape_rows(d, nf, s);  /* the narrowphase's structure-of-arrays copy of f_shape */
     }
     /* body -> fixtures (the continuous pass synchronises an island body's proxies) */
     w->h_fix_off.assign((size_t)nb + 1, 0);
@@ -3434,6 +3437,7 @@ int b2g_get_launch_config(void* p, b2g_launch_config* out) {
     out->traverse_block = w->cfg.traverse_block;
     out->tuning_steps = w->tuning_steps;
     out->solver_block = w->cfg.solver_block;
+    out->collide_group = w->cfg.collide_group;
     return B2G_OK;
 }
 
@@ -3443,13 +3447,15 @@ int b2g_set_launch_config(void* p, const b2g_launch_config* c) {
     auto pow2 = [](int v, int lo, int hi) { return v >= lo && v <= hi && (v & (v - 1)) == 0; };
     const int sb = c->solver_block == 0 ? 256 : c->solver_block;
     if (c->coop_blocks_per_sm < 1 || c->coop_blocks_per_sm > 2 || !pow2(c->collide_block, 32, 256) ||
-        !pow2(c->traverse_block, 32, 256) || (sb != 256 && sb != 512))
+        !pow2(c->traverse_block, 32, 256) || (sb != 256 && sb != 512) || c->collide_group < 0 || c->collide_group > 32)
         return fail(w, B2G_ERR_INVALID_ARG,
-                    "coop_blocks_per_sm in {1, 2}; block sizes powers of two in [32, 256]; solver_block 256 or 512");
+                    "coop_blocks_per_sm in {1, 2}; block sizes powers of two in [32, 256]; solver_block 256 or 512; "
+                    "collide_group in [0, 32]");
     w->cfg.coop_per_sm = c->coop_blocks_per_sm;
     w->cfg.collide_block = c->collide_block;
     w->cfg.traverse_block = c->traverse_block;
     w->cfg.solver_block = sb;
+    w->cfg.collide_group = c->collide_group;
     w->cfg_set = true;
     apply_launch_config(w);
     drop_graphs(w);
@@ -3480,7 +3486,8 @@ int timed_steps(World* w, float dt, int vi, int pi, int steps, double* ms) {
 extern "C" {
 
 /* Coordinate search over the launch configuration on the world's own next steps: for each knob in
- * turn (persistent-kernel blocks per SM, narrowphase block, traversal block) the candidates take
+ * turn (persistent-kernel blocks per SM, narrowphase block, traversal block, solver block, the
+ * narrowphase's polygon pairs per warp batch taken eight lanes to a pair) the candidates take
  * turns over up to four rounds, each turn two untimed steps (the step graph's captures for both
  * contact-buffer parities) and its share of `steps_per_candidate` timed steps; the fastest in
  * total is kept. With the part-local solve the
@@ -3494,7 +3501,8 @@ int b2g_autotune(void* p, float dt, int32_t vi, int32_t pi, int32_t steps_per_ca
     if (w->h_flags.empty()) return fail(w, B2G_ERR_INVALID_ARG, "the world has no bodies");
     LaunchCfg best = w->cfg;
     w->cfg_set = true;
-    const int coop[] = {1, 2}, collide[] = {64, 128, 256}, traverse[] = {64, 128, 256}, solver[] = {256, 512};
+    const int coop[] = {1, 2}, collide[] = {64, 128, 256}, traverse[] = {64, 128, 256}, solver[] = {256, 512},
+              group[] = {0, 8, 32};
     /* the part-local solve caches a part in its block's shared memory: one block per SM */
     const int ncoop = use_parts(w->d, w->num_sms, w->part_solve) ? 1 : 2;
     /* the world keeps evolving while candidates are timed, so the candidates take turns over
@@ -3503,10 +3511,11 @@ int b2g_autotune(void* p, float dt, int32_t vi, int32_t pi, int32_t steps_per_ca
     const int per_round = std::max(1, steps_per_candidate / rounds);
     int tuned = 0;
     auto field = [](LaunchCfg& c, int knob) -> int& {
-        return knob == 0 ? c.coop_per_sm : knob == 1 ? c.collide_block : knob == 2 ? c.traverse_block : c.solver_block;
+        return knob == 0 ? c.coop_per_sm : knob == 1 ? c.collide_block : knob == 2 ? c.traverse_block
+               : knob == 3 ? c.solver_block : c.collide_group;
     };
-    for (int knob = 0; knob < 4; ++knob) {
-        const int* cand = knob == 0 ? coop : knob == 1 ? collide : knob == 2 ? traverse : solver;
+    for (int knob = 0; knob < 5; ++knob) {
+        const int* cand = knob == 0 ? coop : knob == 1 ? collide : knob == 2 ? traverse : knob == 3 ? solver : group;
         /* 512 solver threads only with one block per SM (the registers of two would not fit) */
         const int nc = knob == 0 ? ncoop : knob == 3 ? (best.coop_per_sm == 1 ? 2 : 1) : 3;
         if (nc == 1) {

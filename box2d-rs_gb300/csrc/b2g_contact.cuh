@@ -45,58 +45,61 @@ __device__ __forceinline__ Xf load_xf(const DevWorld& w, int b) {
     return r;
 }
 
-/* B2contact::update of contact i (flags: its current flags; fx, bd: its fixtures and bodies; ids:
- * its manifold ids word): re-enable it, evaluate the manifold on the bodies' transforms, carry
- * impulses from old points with the same feature id, update the touching flag, wake both bodies
- * when it changes (at once, or noted at table place wake_at >= 0: wake_body_at), and record
- * begin/end events. Returns whether the contact touches. */
-__device__ __forceinline__ bool contact_update(const DevWorld& w, bool record_events, int i, uint32_t flags, int2 fx,
-                                               int2 bd, uint4 ids, int wake_at = -1) {
+/* fixture f's rows of the structure-of-arrays shape tables */
+__device__ __forceinline__ ShapeRows shape_rows(const DevWorld& w, int f) {
+    const float4 h = w.f_hdr[f];
+    ShapeRows r;
+    r.vn = w.f_vn + (size_t)f * kMaxPolygonVertices;
+    r.centroid = mk(h.x, h.y);
+    r.radius = h.z;
+    r.meta = __float_as_int(h.w);
+    return r;
+}
+
+/* the manifold a routine starts from: no points, zero geometry and ids */
+__device__ __forceinline__ void manifold_init(Manifold& m) {
+    m.type = MANIFOLD_CIRCLES;
+    m.count = 0;
+    m.ln = mk(0.0f, 0.0f);
+    m.lp = mk(0.0f, 0.0f);
+    m.p[0] = m.p[1] = mk(0.0f, 0.0f);
+    m.id[0] = m.id[1] = 0u;
+}
+
+/* The part of B2contact::update (private/dynamics/b2_contact.rs:103-218) after the manifold m of
+ * contact i has been evaluated (flags: its current flags; fx, bd: its fixtures and bodies; ids: its
+ * manifold ids word): re-enable it, carry impulses from old points with the same feature id, update
+ * the touching flag, wake both bodies when it changes (at once, or noted at table place wake_at >= 0:
+ * wake_body_at) and record begin/end events. set_flags are or-ed into the stored flags. Returns
+ * whether the contact touches. */
+__device__ __forceinline__ bool contact_finish(const DevWorld& w, bool record_events, int i, uint32_t flags, int2 fx,
+                                               int2 bd, uint4 ids, const Manifold& m, int wake_at, uint32_t set_flags) {
     const bool was_touching = (flags & CF_TOUCHING) != 0;
     const int old_count = (int)((ids.z >> 8) & 0xffu);
-    flags |= CF_ENABLED;
-    bool touching = false;
-    if (flags & CF_SENSOR) {
-        /* sensor overlap tests (GJK) are outside the GPU path: sensors never touch */
-        w.c.mids[i] = make_uint4(ids.x, ids.y, ids.z & 0xffu, ids.w);
-    } else {
-        const int kind = (int)((flags >> CF_KIND_SHIFT) & 7u);
-        const Xf xfA = load_xf(w, bd.x);
-        const Xf xfB = load_xf(w, bd.y);
-        const ShapeRec sa = w.f_shape[fx.x];
-        const ShapeRec sb = w.f_shape[fx.y];
-        Manifold m;
-        m.type = MANIFOLD_CIRCLES;
-        m.count = 0;
-        m.ln = mk(0.0f, 0.0f);
-        m.lp = mk(0.0f, 0.0f);
-        m.p[0] = m.p[1] = mk(0.0f, 0.0f);
-        m.id[0] = m.id[1] = 0u;
-        evaluate(kind, m, sa, xfA, sb, xfB);
-        const float4 oldimp = w.c.mimp[i];
-        float ni[2] = {0.0f, 0.0f}, ti[2] = {0.0f, 0.0f};
-        for (int p = 0; p < m.count; ++p) {
-            if (old_count > 0 && ids.x == m.id[p]) {
-                ni[p] = oldimp.x;
-                ti[p] = oldimp.y;
-            } else if (old_count > 1 && ids.y == m.id[p]) {
-                ni[p] = oldimp.z;
-                ti[p] = oldimp.w;
-            }
+    flags |= CF_ENABLED | set_flags;
+    const float4 oldimp = w.c.mimp[i];
+    float ni[2] = {0.0f, 0.0f}, ti[2] = {0.0f, 0.0f};
+    for (int p = 0; p < m.count; ++p) {
+        if (old_count > 0 && ids.x == m.id[p]) {
+            ni[p] = oldimp.x;
+            ti[p] = oldimp.y;
+        } else if (old_count > 1 && ids.y == m.id[p]) {
+            ni[p] = oldimp.z;
+            ti[p] = oldimp.w;
         }
-        touching = m.count > 0;
-        w.c.mgeo[i] = make_float4(m.ln.x, m.ln.y, m.lp.x, m.lp.y);
-        w.c.mpts[i] = make_float4(m.p[0].x, m.p[0].y, m.p[1].x, m.p[1].y);
-        w.c.mimp[i] = make_float4(ni[0], ti[0], ni[1], ti[1]);
-        w.c.mids[i] = make_uint4(m.id[0], m.id[1], (uint32_t)m.type | ((uint32_t)m.count << 8), ids.w);
-        if (touching != was_touching) {
-            if (wake_at < 0) {
-                wake_body(w, bd.x);
-                wake_body(w, bd.y);
-            } else {
-                wake_body_at(w, bd.x, wake_at);
-                wake_body_at(w, bd.y, wake_at);
-            }
+    }
+    const bool touching = m.count > 0;
+    w.c.mgeo[i] = make_float4(m.ln.x, m.ln.y, m.lp.x, m.lp.y);
+    w.c.mpts[i] = make_float4(m.p[0].x, m.p[0].y, m.p[1].x, m.p[1].y);
+    w.c.mimp[i] = make_float4(ni[0], ti[0], ni[1], ti[1]);
+    w.c.mids[i] = make_uint4(m.id[0], m.id[1], (uint32_t)m.type | ((uint32_t)m.count << 8), ids.w);
+    if (touching != was_touching) {
+        if (wake_at < 0) {
+            wake_body(w, bd.x);
+            wake_body(w, bd.y);
+        } else {
+            wake_body_at(w, bd.x, wake_at);
+            wake_body_at(w, bd.y, wake_at);
         }
     }
     w.c.flags[i] = touching ? (flags | CF_TOUCHING) : (flags & ~CF_TOUCHING);
@@ -105,6 +108,26 @@ __device__ __forceinline__ bool contact_update(const DevWorld& w, bool record_ev
         if (was_touching && !touching) push_event(w, 1, fx.x, fx.y);
     }
     return touching;
+}
+
+/* B2contact::update of contact i, one thread: the manifold evaluated by the routine of the
+ * contact's kind on the bodies' transforms, then contact_finish. A sensor keeps no points (sensor
+ * overlap tests, GJK, are outside the GPU path: sensors never touch). Returns whether the contact
+ * touches. */
+__device__ __forceinline__ bool contact_update(const DevWorld& w, bool record_events, int i, uint32_t flags, int2 fx,
+                                               int2 bd, uint4 ids, int wake_at = -1, uint32_t set_flags = 0u) {
+    if (flags & CF_SENSOR) {
+        const bool was_touching = (flags & CF_TOUCHING) != 0;
+        w.c.mids[i] = make_uint4(ids.x, ids.y, ids.z & 0xffu, ids.w);
+        w.c.flags[i] = (flags | CF_ENABLED | set_flags) & ~CF_TOUCHING;
+        if (record_events && was_touching) push_event(w, 1, fx.x, fx.y);
+        return false;
+    }
+    const int kind = (int)((flags >> CF_KIND_SHIFT) & 7u);
+    Manifold m;
+    manifold_init(m);
+    evaluate(kind, m, shape_rows(w, fx.x), load_xf(w, bd.x), shape_rows(w, fx.y), load_xf(w, bd.y));
+    return contact_finish(w, record_events, i, flags, fx, bd, ids, m, wake_at, set_flags);
 }
 
 /* register table of b2_contact_registers.rs:67-103: +1 keep order, -1 swap, 0 no contact */

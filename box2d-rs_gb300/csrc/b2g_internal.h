@@ -7,7 +7,9 @@
  *   bodies    b_xf(p.x,p.y,sin,cos) b_pos(c.x,c.y,a,-) b_pos0(c0.x,c0.y,a0,-)
  *             b_vel(v.x,v.y,w,sleep_time) b_force(f.x,f.y,torque,-) b_mass(m,1/m,I,1/I)
  *             b_damp(lin,ang,gravity_scale,-) b_lc(local centre) b_flags b_world b_island
- *   fixtures  f_shape (144-byte ShapeRec) f_body f_mat(friction,restitution,threshold,density)
+ *   fixtures  f_shape (144-byte ShapeRec) and its structure-of-arrays copy for the narrowphase:
+ *             f_vn (8 rows per fixture: vertex k and the normal of edge k) and f_hdr (centroid.x,
+ *             centroid.y, radius, meta bits); f_body f_mat(friction,restitution,threshold,density)
  *             f_filter(category|mask<<16, group|sensor<<16) f_refid (the reference's proxy id)
  *             f_fat (fat AABB lo.x,lo.y,hi.x,hi.y) f_moved
  *   contacts  sorted by key = refid_min << 32 | refid_max (double-buffered, merged each step)
@@ -139,6 +141,9 @@ constexpr int kMaxColours = 256;   /* first-fit colours 0..63, then one per colo
 constexpr int kFirstFitColours = 64;
 constexpr int kColourTail = 256;   /* uncoloured constraints one block finishes colouring (one per thread) */
 constexpr int kMaxParts = 1024;    /* body parts of the part-local solve (at most one per solver block) */
+/* default of cfg_collide_group: one lane per pair (measured on GB300 at least as fast as the 8-lane
+ * segments on the mixed 100k scene, the 4096-world batch and the 250k-box pile) */
+constexpr int kCollideGroup = 0;
 constexpr int kKeyMortonBits = 22; /* broadphase keys: key world << 22 | Morton code (11 bits per axis) */
 constexpr int kMaxPosIters = 64;
 constexpr int kNoWake = 0x7f7f7f7f;  /* b_wake's "not woken" (a byte-wise memset value) */
@@ -188,6 +193,8 @@ struct DevWorld {
     int cfg_collide_block;    /* threads per block of the narrowphase */
     int cfg_traverse_block;   /* threads per block of the broadphase traversal */
     int cfg_solver_block;     /* threads per block of the persistent solver (256, or 512 at one block per SM) */
+    int cfg_collide_group;    /* narrowphase: a warp batch with at most this many polygon pairs evaluates
+                                 them eight lanes to a pair (collide_polygons_group); more, a lane each */
     int n_bodies, n_fixtures, num_worlds;
     int num_sms;              /* multiprocessors of the world's device (grid caps of the launchers) */
     int key_bits;      /* bits of the contact key (2 x refid bits) */
@@ -215,6 +222,8 @@ struct DevWorld {
     float* isl_sleep;            /* per island root: min sleep time (as ordered uint bits) */
     /* fixtures */
     ShapeRec* f_shape;
+    float4* f_vn;                /* kMaxPolygonVertices rows per fixture (f * 8 + k): v.x, v.y, n.x, n.y */
+    float4* f_hdr;               /* centroid.x, centroid.y, radius, meta word (bits) */
     int* f_body;
     float4* f_mat;
     uint32_t* f_filter;          /* category | mask << 16 */
@@ -379,6 +388,7 @@ inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
 /* may_sleep: some body may be asleep (sleeping allowed, or a body made asleep): contacts then see
  * the bodies woken by contacts before them in the table's key order, as in the reference's list */
 void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s, bool may_sleep, int num_sms);
+void launch_shape_rows(const DevWorld& w, int n_fixtures, cudaStream_t s);
 /* contact edits of destroy / refilter calls between steps (k_edit_contacts in k_collide.cu): fix_mark
  * per fixture, bit 0 destroyed (its contacts are destroyed), bit 1 refiltered (its contacts are flagged
  * for filtering); body_pairs: contacts between these bodies are flagged for filtering */

@@ -4,7 +4,8 @@
  * Reference: b2_contact_manager_collide, src/private/dynamics/b2_contact_manager.rs:83-171,
  * and b2_contact_update, src/private/dynamics/b2_contact.rs:103-218.
  *
- * One thread per contact of the (key-sorted) contact table:
+ * Each warp takes batches of 32 consecutive contacts of the (key-sorted) contact table, one lane per
+ * contact for the bookkeeping:
  *   - skip when neither body is awake and non-static. The reference's loop sees, at each contact
  *     of its list, the bodies woken by the updates before it; where bodies may sleep, a wake is
  *     noted with the waking contact's table place, a contact counts a body woken at an earlier
@@ -17,8 +18,12 @@
  *   - otherwise evaluate the manifold with the routine of the contact's kind, carry
  *     normal/tangent impulses from old points with the same feature id, update the
  *     touching flag, wake both bodies when it changes, and emit begin/end events.
- * Algorithmic bytes per evaluated contact: ~116 B of contact/manifold state + two
- * 144-byte shape records + two body transforms.
+ * The manifolds of a batch are evaluated per kind: polygon pairs four at a time, eight lanes to a
+ * pair (collide_polygons_group: lane k holds row k of both polygons), the other kinds one lane per
+ * pair. Shapes are read from the structure-of-arrays rows (f_vn, f_hdr): a polygon's rows are one
+ * coalesced 16·V-byte read across its pair's lanes.
+ * Algorithmic bytes per evaluated contact: ~116 B of contact/manifold state + the two shapes' rows
+ * (16 B header + 16 B per vertex row) + two body transforms.
  */
 #include "b2g_contact.cuh"
 #include "b2g_sync.cuh"
@@ -36,10 +41,21 @@ __device__ __forceinline__ bool active_for(const DevWorld& w, int b, uint32_t f,
     return deferred && ((volatile int*)w.b_wake)[b] < i;
 }
 
-/* b2_contact_manager_collide for contact i; false if it was skipped as inactive */
-__device__ __forceinline__ bool collide_contact(const DevWorld& w, const StepParams& sp, int i, bool deferred) {
+enum { HEAD_SKIPPED = 0, HEAD_DONE = 1, HEAD_EVALUATE = 2 };
+
+/* a contact whose manifold is to be evaluated: its flags, fixtures, bodies and manifold ids */
+struct Head {
+    uint32_t flags;
+    int2 fx, bd;
+    uint4 ids;
+};
+
+/* b2_contact_manager_collide for contact i up to the manifold's evaluation: HEAD_SKIPPED if it was
+ * skipped as inactive, HEAD_DONE if nothing is left to do (dead, destroyed now, or a sensor, whose
+ * update needs no shapes), HEAD_EVALUATE with h filled if its manifold is to be evaluated */
+__device__ __forceinline__ int collide_head(const DevWorld& w, const StepParams& sp, int i, bool deferred, Head& h) {
     uint32_t flags = w.c.flags[i];
-    if (flags & CF_DEAD) return true;
+    if (flags & CF_DEAD) return HEAD_DONE;
     const int2 fx = w.c.fix[i];
     const int2 bd = w.c.body[i];
     const uint32_t fa_flags = w.b_flags[bd.x];
@@ -54,7 +70,7 @@ __device__ __forceinline__ bool collide_contact(const DevWorld& w, const StepPar
     }
     if (!destroy && !active_for(w, bd.x, fa_flags, i, deferred) && !active_for(w, bd.y, fb_flags, i, deferred)) {
         if (sp.pre_solve && (flags & CF_UPDATED)) w.c.flags[i] = flags & ~CF_UPDATED;
-        return false;
+        return HEAD_SKIPPED;
     }
     const float4 A = w.f_fat[fx.x];
     const float4 B = w.f_fat[fx.y];
@@ -74,44 +90,122 @@ __device__ __forceinline__ bool collide_contact(const DevWorld& w, const StepPar
             }
         }
         w.c.flags[i] = (flags | CF_DEAD) & ~CF_TOUCHING;
-        return true;
+        return HEAD_DONE;
     }
-    contact_update(w, sp.record_events != 0, i, flags, fx, bd, ids, deferred ? i : -1);
-    if (sp.pre_solve) w.c.flags[i] |= CF_UPDATED;
-    return true;
+    if (flags & CF_SENSOR) {
+        contact_update(w, sp.record_events != 0, i, flags, fx, bd, ids, deferred ? i : -1,
+                       sp.pre_solve ? CF_UPDATED : 0u);
+        return HEAD_DONE;
+    }
+    h.flags = flags;
+    h.fx = fx;
+    h.bd = bd;
+    h.ids = ids;
+    return HEAD_EVALUATE;
+}
+
+/* The manifolds of one batch: every lane of the warp calls this together; a lane whose state is
+ * HEAD_EVALUATE has contact i (described by h) evaluated and finished. When the batch holds at most
+ * cfg_collide_group polygon pairs, they go four at a time through collide_polygons_group, each
+ * finished by its segment's first lane (a batch of mixed kinds: the few polygon pairs no longer
+ * hold the warp through a scalar polygon scan); otherwise every lane evaluates its own pair (a
+ * batch of polygon pairs only keeps all 32 lanes busy that way). */
+__device__ __forceinline__ void collide_batch(const DevWorld& w, const StepParams& sp, int i, int state, const Head& h,
+                                              bool deferred) {
+    const int lane = threadIdx.x & 31;
+    const bool rec = sp.record_events != 0;
+    const uint32_t set_flags = sp.pre_solve ? CF_UPDATED : 0u;
+    const int kind = state == HEAD_EVALUATE ? (int)((h.flags >> CF_KIND_SHIFT) & 7u) : -1;
+    const unsigned polygons = __ballot_sync(kFullWarp, kind == KIND_POLYGONS);
+    const bool segments = __popc(polygons) <= w.cfg_collide_group;
+    if (kind >= 0 && (kind != KIND_POLYGONS || !segments)) {
+        Manifold m;
+        manifold_init(m);
+        evaluate(kind, m, shape_rows(w, h.fx.x), load_xf(w, h.bd.x), shape_rows(w, h.fx.y), load_xf(w, h.bd.y));
+        contact_finish(w, rec, i, h.flags, h.fx, h.bd, h.ids, m, deferred ? i : -1, set_flags);
+    }
+    unsigned todo = segments ? polygons : 0u;
+    const int seg = lane >> 3, row = lane & 7;
+    while (todo) {
+        const int src = seg_source(todo, seg);
+        todo = seg_rest(todo);
+        const int from = src >= 0 ? src : lane;
+        const int ci = __shfl_sync(kFullWarp, i, from);
+        const int2 fx = make_int2(__shfl_sync(kFullWarp, h.fx.x, from), __shfl_sync(kFullWarp, h.fx.y, from));
+        const int2 bd = make_int2(__shfl_sync(kFullWarp, h.bd.x, from), __shfl_sync(kFullWarp, h.bd.y, from));
+        float4 la = make_float4(0.0f, 0.0f, 0.0f, 0.0f), lb = la, ha = la, hb = la;
+        Xf xa, xb;
+        xa.p = xb.p = mk(0.0f, 0.0f);
+        xa.q.s = xb.q.s = 0.0f;
+        xa.q.c = xb.q.c = 1.0f;
+        if (src >= 0) {
+            ha = w.f_hdr[fx.x];
+            hb = w.f_hdr[fx.y];
+            la = w.f_vn[(size_t)fx.x * kMaxPolygonVertices + row];
+            lb = w.f_vn[(size_t)fx.y * kMaxPolygonVertices + row];
+            xa = load_xf(w, bd.x);
+            xb = load_xf(w, bd.y);
+        }
+        Manifold m;
+        manifold_init(m);
+        collide_polygons_group(m, row, la, (__float_as_int(ha.w) >> 8) & 0xff, ha.z, xa, lb,
+                               (__float_as_int(hb.w) >> 8) & 0xff, hb.z, xb);
+        const uint32_t cflags = __shfl_sync(kFullWarp, h.flags, from);
+        const uint4 ids = make_uint4(__shfl_sync(kFullWarp, h.ids.x, from), __shfl_sync(kFullWarp, h.ids.y, from),
+                                     __shfl_sync(kFullWarp, h.ids.z, from), __shfl_sync(kFullWarp, h.ids.w, from));
+        if (src >= 0 && row == 0) contact_finish(w, rec, ci, cflags, fx, bd, ids, m, deferred ? ci : -1, set_flags);
+    }
+}
+
+/* all lanes of the warp leave together when the world has been aborted */
+__device__ __forceinline__ bool warp_aborted(const DevWorld& w) {
+    return __any_sync(kFullWarp, world_aborted(w.cnt));
 }
 
 }  // namespace
 
-__global__ void __launch_bounds__(256) k_collide(DevWorld w, StepParams sp, int deferred) {
-    B2G_RETURN_IF_ABORTED(w);
+__global__ void __launch_bounds__(256, 4) k_collide(DevWorld w, StepParams sp, int deferred) {
+    if (warp_aborted(w)) return;
     const int n = w.cnt[CNT_CONTACTS];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const bool done = collide_contact(w, sp, i, deferred != 0);
-        if (deferred) w.c_done[i] = done ? 1 : 0;
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x - lane; base < n; base += stride) {
+        const int i = base + lane;
+        Head h;
+        const int state = i < n ? collide_head(w, sp, i, deferred != 0, h) : HEAD_SKIPPED;
+        if (deferred && i < n) w.c_done[i] = state != HEAD_SKIPPED ? 1 : 0;
+        collide_batch(w, sp, i, state, h, deferred != 0);
     }
 }
 
 /* The contacts skipped as inactive whose body a contact earlier in the table woke: collided in
  * rounds until a round finds none (a chain of wakes along the table's order). */
 __global__ void __launch_bounds__(256) k_collide_cascade(DevWorld w, StepParams sp) {
-    B2G_RETURN_IF_ABORTED(w);
+    if (warp_aborted(w)) return;
     grid_barrier_start();
     const int n = w.cnt[CNT_CONTACTS];
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
     volatile int* vcnt = w.cnt;
     int round = 0;
     for (; round < n + 1; ++round) {
         if (gtid == 0) vcnt[CNT_CASCADE + (round + 1) % 3] = 0;
         int mine = 0;
-        for (int i = gtid; i < n; i += gridDim.x * blockDim.x) {
-            if (w.c_done[i]) continue;
-            const int2 bd = w.c.body[i];
-            const uint32_t fa = w.b_flags[bd.x], fb = w.b_flags[bd.y];
-            if (!active_for(w, bd.x, fa, i, true) && !active_for(w, bd.y, fb, i, true)) continue;
-            collide_contact(w, sp, i, true);
-            w.c_done[i] = 1;
-            ++mine;
+        for (int base = gtid - lane; base < n; base += gridDim.x * blockDim.x) {
+            const int i = base + lane;
+            bool want = i < n && !w.c_done[i];
+            if (want) {
+                const int2 bd = w.c.body[i];
+                const uint32_t fa = w.b_flags[bd.x], fb = w.b_flags[bd.y];
+                want = active_for(w, bd.x, fa, i, true) || active_for(w, bd.y, fb, i, true);
+            }
+            Head h;
+            const int state = want ? collide_head(w, sp, i, true, h) : HEAD_SKIPPED;
+            collide_batch(w, sp, i, state, h, true);
+            if (want) {
+                w.c_done[i] = 1;
+                ++mine;
+            }
         }
         if (mine) atomicAdd(&w.cnt[CNT_CASCADE + round % 3], mine);
         if (!grid_barrier(w)) return;
@@ -199,6 +293,26 @@ void launch_flag_joint_contacts(const DevWorld& w, cudaStream_t s, int num_sms) 
     B2G_LAUNCHED(1);
 }
 
+/* The narrowphase's structure-of-arrays copy of fixtures [0, n)'s shape records: row k of fixture f
+ * (f_vn[f * 8 + k]) = (v[k], n[k]) for the rows its shape uses (a polygon's vertex count, a circle's
+ * centre, an edge's four vertices), zeros past them; f_hdr[f] = (centroid, radius, meta bits). */
+__global__ void k_shape_rows(DevWorld w, int n) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n * kMaxPolygonVertices; t += gridDim.x * blockDim.x) {
+        const int f = t / kMaxPolygonVertices, k = t % kMaxPolygonVertices;
+        const ShapeRec& s = w.f_shape[f];
+        const int type = shape_type(s);
+        const int rows = type == SHAPE_POLYGON ? shape_count(s) : type == SHAPE_EDGE ? 4 : 1;
+        w.f_vn[t] = k < rows ? make_float4(s.v[k].x, s.v[k].y, s.n[k].x, s.n[k].y) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (k == 0) w.f_hdr[f] = make_float4(s.centroid.x, s.centroid.y, s.radius, __int_as_float(s.meta));
+    }
+}
+
+void launch_shape_rows(const DevWorld& w, int n_fixtures, cudaStream_t s) {
+    if (n_fixtures <= 0) return;
+    k_shape_rows<<<grid_for(n_fixtures * kMaxPolygonVertices, 256, w.num_sms * 8), 256, 0, s>>>(w, n_fixtures);
+    B2G_LAUNCHED(1);
+}
+
 void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s, bool may_sleep, int num_sms) {
     const int block = w.cfg_collide_block;
     k_collide<<<grid_for(w.contact_cap, block, w.num_sms * 2048 / block), block, 0, s>>>(w, sp, may_sleep ? 1 : 0);
@@ -215,30 +329,80 @@ void launch_collide(const DevWorld& w, const StepParams& sp, cudaStream_t s, boo
 }
 
 /* Stand-alone manifolds of independent shape pairs (the public b2_collide_* functions,
- * src/b2_collision.rs:259-315). xf = (x, y, sin, cos) per shape. */
+ * src/b2_collision.rs:259-315). xf = (x, y, sin, cos) per shape. Batches of 32 pairs per warp as in
+ * k_collide: a batch with at most kPairsCollideGroup polygon pairs takes them four at a time through
+ * collide_polygons_group, the rest (and a batch with more) one lane each. Shape pairs of mixed kinds
+ * use both forms, so the routine's known answers pin the segment form a world's launch configuration
+ * can choose as well as the one-lane form. */
+constexpr int kPairsCollideGroup = 8;
+
 __global__ void k_collide_pairs(const ShapeRec* a, const float4* xa, const ShapeRec* b, const float4* xb,
                                 const int* kind, int n, float4* geo, float4* pts, uint4* ids) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        Xf A, B;
-        const float4 x0 = xa[i], x1 = xb[i];
-        A.p = mk(x0.x, x0.y);
-        A.q.s = x0.z;
-        A.q.c = x0.w;
-        B.p = mk(x1.x, x1.y);
-        B.q.s = x1.z;
-        B.q.c = x1.w;
-        Manifold m;
-        m.type = MANIFOLD_CIRCLES;
-        m.count = 0;
-        m.ln = m.lp = mk(0.0f, 0.0f);
-        m.p[0] = m.p[1] = mk(0.0f, 0.0f);
-        m.id[0] = m.id[1] = 0u;
-        const ShapeRec sa = a[i];
-        const ShapeRec sb = b[i];
-        evaluate(kind[i], m, sa, A, sb, B);
+    const int lane = threadIdx.x & 31;
+    const int seg = lane >> 3, row = lane & 7;
+    auto load = [](const float4* x, int i) {
+        const float4 v = x[i];
+        Xf t;
+        t.p = mk(v.x, v.y);
+        t.q.s = v.z;
+        t.q.c = v.w;
+        return t;
+    };
+    auto store = [&](int i, const Manifold& m) {
         geo[i] = make_float4(m.ln.x, m.ln.y, m.lp.x, m.lp.y);
         pts[i] = make_float4(m.p[0].x, m.p[0].y, m.p[1].x, m.p[1].y);
         ids[i] = make_uint4(m.id[0], m.id[1], (uint32_t)m.type | ((uint32_t)m.count << 8), 0u);
+    };
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x - lane; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + lane;
+        const int k = i < n ? kind[i] : -1;
+        const unsigned polygons = __ballot_sync(kFullWarp, i < n && k == KIND_POLYGONS);
+        const bool segments = __popc(polygons) <= kPairsCollideGroup;
+        if (i < n && (k != KIND_POLYGONS || !segments)) {
+            Manifold m;
+            m.type = MANIFOLD_CIRCLES;
+            m.count = 0;
+            m.ln = m.lp = mk(0.0f, 0.0f);
+            m.p[0] = m.p[1] = mk(0.0f, 0.0f);
+            m.id[0] = m.id[1] = 0u;
+            const ShapeRec sa = a[i];
+            const ShapeRec sb = b[i];
+            evaluate(k, m, sa, load(xa, i), sb, load(xb, i));
+            store(i, m);
+        }
+        unsigned todo = segments ? polygons : 0u;
+        while (todo) {
+            const int src = seg_source(todo, seg);
+            todo = seg_rest(todo);
+            const int ci = __shfl_sync(kFullWarp, i, src >= 0 ? src : lane);
+            float4 la = make_float4(0.0f, 0.0f, 0.0f, 0.0f), lb = la;
+            int na = 0, nb = 0;
+            float ra = 0.0f, rb = 0.0f;
+            Xf A, B;
+            A.p = B.p = mk(0.0f, 0.0f);
+            A.q.s = B.q.s = 0.0f;
+            A.q.c = B.q.c = 1.0f;
+            if (src >= 0) {
+                const ShapeRec& sa = a[ci];
+                const ShapeRec& sb = b[ci];
+                la = make_float4(sa.v[row].x, sa.v[row].y, sa.n[row].x, sa.n[row].y);
+                lb = make_float4(sb.v[row].x, sb.v[row].y, sb.n[row].x, sb.n[row].y);
+                na = shape_count(sa);
+                nb = shape_count(sb);
+                ra = sa.radius;
+                rb = sb.radius;
+                A = load(xa, ci);
+                B = load(xb, ci);
+            }
+            Manifold m;
+            m.type = MANIFOLD_CIRCLES;
+            m.count = 0;
+            m.ln = m.lp = mk(0.0f, 0.0f);
+            m.p[0] = m.p[1] = mk(0.0f, 0.0f);
+            m.id[0] = m.id[1] = 0u;
+            collide_polygons_group(m, row, la, na, ra, A, lb, nb, rb, B);
+            if (src >= 0 && row == 0) store(ci, m);
+        }
     }
 }
 

@@ -591,11 +591,15 @@ typedef struct b2g_launch_config {
     int32_t tuning_steps;         /* out: steps the world's last b2g_autotune ran (ignored on set) */
     int32_t solver_block;         /* solver threads per block: 256, or 512 with one block per SM (more
                                      loads in flight on large worlds and batches); 0 on set: 256 */
+    int32_t collide_group;        /* narrowphase pairs per warp: a warp's batch of 32 contacts with at
+                                     most this many polygon pairs evaluates each of them on 8 lanes (4
+                                     pairs at a time); more, one lane per pair. 0..32, default 0 */
 } b2g_launch_config;
 int b2g_get_launch_config(void* world, b2g_launch_config* out);
 int b2g_set_launch_config(void* world, const b2g_launch_config* config);
 /* Time the world's next steps under candidate configurations (one knob at a time: blocks per SM,
- * narrowphase block, traversal block; each candidate 1 untimed + steps_per_candidate timed steps),
+ * narrowphase block, traversal block, solver block, narrowphase pairs per warp (collide_group 0, 8 or
+ * 32); each candidate 2 untimed steps and its share of steps_per_candidate timed steps),
  * keep the fastest for this world and for later worlds of the same size bucket (log2 bodies per
  * world, single or batch) created in this process. The tuning steps are ordinary steps of the
  * world with the given dt and iterations. */

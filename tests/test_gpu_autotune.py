@@ -18,8 +18,10 @@ def _world(scene):
     return w
 
 
-@pytest.mark.parametrize("cfg", [dict(coop_blocks_per_sm=2, collide_block=64, traverse_block=64, solver_block=256),
-                                 dict(coop_blocks_per_sm=1, collide_block=256, traverse_block=32, solver_block=512)])
+@pytest.mark.parametrize("cfg", [dict(coop_blocks_per_sm=2, collide_block=64, traverse_block=64, solver_block=256,
+                                      collide_group=8),
+                                 dict(coop_blocks_per_sm=1, collide_block=256, traverse_block=32, solver_block=512,
+                                      collide_group=32)])
 def test_configurations_give_identical_results(built, cfg):
     s = scenes.mixed(n_circles=300, n_polygons=300, size=25.0, seed=21)
     a, b = _world(s), _world(s)
@@ -43,6 +45,7 @@ def test_autotune_steps_are_ordinary_steps(built):
     assert cfg["coop_blocks_per_sm"] in (1, 2)
     assert cfg["collide_block"] in (64, 128, 256) and cfg["traverse_block"] in (64, 128, 256)
     assert cfg["solver_block"] in (256, 512)
+    assert cfg["collide_group"] in (0, 8, 32)
     n = b.tuning_steps()
     assert n >= 2 * 3 * 3  # at least the two block-size knobs, every candidate stepped 2 + 1 times
     for _ in range(n):
@@ -67,4 +70,6 @@ def test_invalid_configuration_is_rejected(built):
         w.set_launch_config(collide_block=100)
     with pytest.raises(b2g.B2GError):
         w.set_launch_config(solver_block=384)
+    with pytest.raises(b2g.B2GError):
+        w.set_launch_config(collide_group=33)
     w.close()
