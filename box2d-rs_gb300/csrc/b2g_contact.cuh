@@ -45,9 +45,8 @@ __device__ __forceinline__ Xf load_xf(const DevWorld& w, int b) {
     return r;
 }
 
-/* fixture f's rows of the structure-of-arrays shape tables */
-__device__ __forceinline__ ShapeRows shape_rows(const DevWorld& w, int f) {
-    const float4 h = w.f_hdr[f];
+/* fixture f's rows of the structure-of-arrays shape tables (h: its header, f_hdr[f]) */
+__device__ __forceinline__ ShapeRows shape_rows(const DevWorld& w, int f, float4 h) {
     ShapeRows r;
     r.vn = w.f_vn + (size_t)f * kMaxPolygonVertices;
     r.centroid = mk(h.x, h.y);
@@ -55,6 +54,7 @@ __device__ __forceinline__ ShapeRows shape_rows(const DevWorld& w, int f) {
     r.meta = __float_as_int(h.w);
     return r;
 }
+__device__ __forceinline__ ShapeRows shape_rows(const DevWorld& w, int f) { return shape_rows(w, f, w.f_hdr[f]); }
 
 /* the manifold a routine starts from: no points, zero geometry and ids */
 __device__ __forceinline__ void manifold_init(Manifold& m) {
@@ -67,17 +67,18 @@ __device__ __forceinline__ void manifold_init(Manifold& m) {
 }
 
 /* The part of B2contact::update (private/dynamics/b2_contact.rs:103-218) after the manifold m of
- * contact i has been evaluated (flags: its current flags; fx, bd: its fixtures and bodies; ids: its
- * manifold ids word): re-enable it, carry impulses from old points with the same feature id, update
- * the touching flag, wake both bodies when it changes (at once, or noted at table place wake_at >= 0:
- * wake_body_at) and record begin/end events. set_flags are or-ed into the stored flags. Returns
- * whether the contact touches. */
+ * contact i has been evaluated (flags: its current flags; fx, bd: its fixtures and bodies; ids,
+ * oldimp: its manifold ids word and impulses): re-enable it, carry impulses from old points with the
+ * same feature id, update the touching flag, wake both bodies when it changes (at once, or noted at
+ * table place wake_at >= 0: wake_body_at) and record begin/end events. set_flags are or-ed into the
+ * stored flags. The ids and impulses are stored only where they changed (a contact that stays apart
+ * keeps both). Returns whether the contact touches. */
 __device__ __forceinline__ bool contact_finish(const DevWorld& w, bool record_events, int i, uint32_t flags, int2 fx,
-                                               int2 bd, uint4 ids, const Manifold& m, int wake_at, uint32_t set_flags) {
+                                               int2 bd, uint4 ids, float4 oldimp, const Manifold& m, int wake_at,
+                                               uint32_t set_flags) {
     const bool was_touching = (flags & CF_TOUCHING) != 0;
     const int old_count = (int)((ids.z >> 8) & 0xffu);
     flags |= CF_ENABLED | set_flags;
-    const float4 oldimp = w.c.mimp[i];
     float ni[2] = {0.0f, 0.0f}, ti[2] = {0.0f, 0.0f};
     for (int p = 0; p < m.count; ++p) {
         if (old_count > 0 && ids.x == m.id[p]) {
@@ -91,8 +92,12 @@ __device__ __forceinline__ bool contact_finish(const DevWorld& w, bool record_ev
     const bool touching = m.count > 0;
     w.c.mgeo[i] = make_float4(m.ln.x, m.ln.y, m.lp.x, m.lp.y);
     w.c.mpts[i] = make_float4(m.p[0].x, m.p[0].y, m.p[1].x, m.p[1].y);
-    w.c.mimp[i] = make_float4(ni[0], ti[0], ni[1], ti[1]);
-    w.c.mids[i] = make_uint4(m.id[0], m.id[1], (uint32_t)m.type | ((uint32_t)m.count << 8), ids.w);
+    const float4 imp = make_float4(ni[0], ti[0], ni[1], ti[1]);
+    if (__float_as_uint(imp.x) != __float_as_uint(oldimp.x) || __float_as_uint(imp.y) != __float_as_uint(oldimp.y) ||
+        __float_as_uint(imp.z) != __float_as_uint(oldimp.z) || __float_as_uint(imp.w) != __float_as_uint(oldimp.w))
+        w.c.mimp[i] = imp;
+    const uint4 nids = make_uint4(m.id[0], m.id[1], (uint32_t)m.type | ((uint32_t)m.count << 8), ids.w);
+    if (nids.x != ids.x || nids.y != ids.y || nids.z != ids.z) w.c.mids[i] = nids;
     if (touching != was_touching) {
         if (wake_at < 0) {
             wake_body(w, bd.x);
@@ -127,7 +132,7 @@ __device__ __forceinline__ bool contact_update(const DevWorld& w, bool record_ev
     Manifold m;
     manifold_init(m);
     evaluate(kind, m, shape_rows(w, fx.x), load_xf(w, bd.x), shape_rows(w, fx.y), load_xf(w, bd.y));
-    return contact_finish(w, record_events, i, flags, fx, bd, ids, m, wake_at, set_flags);
+    return contact_finish(w, record_events, i, flags, fx, bd, ids, w.c.mimp[i], m, wake_at, set_flags);
 }
 
 /* register table of b2_contact_registers.rs:67-103: +1 keep order, -1 swap, 0 no contact */

@@ -54,12 +54,17 @@ struct Head {
  * skipped as inactive, HEAD_DONE if nothing is left to do (dead, destroyed now, or a sensor, whose
  * update needs no shapes), HEAD_EVALUATE with h filled if its manifold is to be evaluated */
 __device__ __forceinline__ int collide_head(const DevWorld& w, const StepParams& sp, int i, bool deferred, Head& h) {
+    /* the contact's own fields go out together, then its bodies' flags and its fixtures' fat AABBs
+     * together: two rounds of loads before any decision */
     uint32_t flags = w.c.flags[i];
-    if (flags & CF_DEAD) return HEAD_DONE;
     const int2 fx = w.c.fix[i];
     const int2 bd = w.c.body[i];
+    const uint4 ids = w.c.mids[i];
+    if (flags & CF_DEAD) return HEAD_DONE;
     const uint32_t fa_flags = w.b_flags[bd.x];
     const uint32_t fb_flags = w.b_flags[bd.y];
+    const float4 A = w.f_fat[fx.x];
+    const float4 B = w.f_fat[fx.y];
     bool destroy = false;
     if (flags & CF_FILTER) {
         /* flagged for filtering (a joint made or destroyed, new filter data): should these bodies and
@@ -72,10 +77,7 @@ __device__ __forceinline__ int collide_head(const DevWorld& w, const StepParams&
         if (sp.pre_solve && (flags & CF_UPDATED)) w.c.flags[i] = flags & ~CF_UPDATED;
         return HEAD_SKIPPED;
     }
-    const float4 A = w.f_fat[fx.x];
-    const float4 B = w.f_fat[fx.y];
     const bool was_touching = (flags & CF_TOUCHING) != 0;
-    const uint4 ids = w.c.mids[i];
     const int old_count = (int)((ids.z >> 8) & 0xffu);
     if (destroy || !overlap4(A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w)) {
         /* destroyed after the pass (the reference collects them and destroys them after its loop) */
@@ -122,7 +124,7 @@ __device__ __forceinline__ void collide_batch(const DevWorld& w, const StepParam
         Manifold m;
         manifold_init(m);
         evaluate(kind, m, shape_rows(w, h.fx.x), load_xf(w, h.bd.x), shape_rows(w, h.fx.y), load_xf(w, h.bd.y));
-        contact_finish(w, rec, i, h.flags, h.fx, h.bd, h.ids, m, deferred ? i : -1, set_flags);
+        contact_finish(w, rec, i, h.flags, h.fx, h.bd, h.ids, w.c.mimp[i], m, deferred ? i : -1, set_flags);
     }
     unsigned todo = segments ? polygons : 0u;
     const int seg = lane >> 3, row = lane & 7;
@@ -153,7 +155,8 @@ __device__ __forceinline__ void collide_batch(const DevWorld& w, const StepParam
         const uint32_t cflags = __shfl_sync(kFullWarp, h.flags, from);
         const uint4 ids = make_uint4(__shfl_sync(kFullWarp, h.ids.x, from), __shfl_sync(kFullWarp, h.ids.y, from),
                                      __shfl_sync(kFullWarp, h.ids.z, from), __shfl_sync(kFullWarp, h.ids.w, from));
-        if (src >= 0 && row == 0) contact_finish(w, rec, ci, cflags, fx, bd, ids, m, deferred ? ci : -1, set_flags);
+        if (src >= 0 && row == 0)
+            contact_finish(w, rec, ci, cflags, fx, bd, ids, w.c.mimp[ci], m, deferred ? ci : -1, set_flags);
     }
 }
 
