@@ -18,10 +18,11 @@
  *   - otherwise evaluate the manifold with the routine of the contact's kind, carry
  *     normal/tangent impulses from old points with the same feature id, update the
  *     touching flag, wake both bodies when it changes, and emit begin/end events.
- * The manifolds of a batch are evaluated per kind: polygon pairs four at a time, eight lanes to a
- * pair (collide_polygons_group: lane k holds row k of both polygons), the other kinds one lane per
- * pair. Shapes are read from the structure-of-arrays rows (f_vn, f_hdr): a polygon's rows are one
- * coalesced 16·V-byte read across its pair's lanes.
+ * Then the batch's manifolds: one lane per pair, or, for a batch with at most cfg_collide_group
+ * polygon pairs, those pairs four at a time, eight lanes to a pair (collide_polygons_group: lane k
+ * holds row k of both polygons; the default, 0, keeps one lane per pair, which measured at least as
+ * fast on GB300). Shapes are read from the structure-of-arrays rows (f_vn, f_hdr): a polygon's used
+ * rows are one contiguous 16·V-byte read.
  * Algorithmic bytes per evaluated contact: ~116 B of contact/manifold state + the two shapes' rows
  * (16 B header + 16 B per vertex row) + two body transforms.
  */
@@ -109,9 +110,7 @@ __device__ __forceinline__ int collide_head(const DevWorld& w, const StepParams&
 /* The manifolds of one batch: every lane of the warp calls this together; a lane whose state is
  * HEAD_EVALUATE has contact i (described by h) evaluated and finished. When the batch holds at most
  * cfg_collide_group polygon pairs, they go four at a time through collide_polygons_group, each
- * finished by its segment's first lane (a batch of mixed kinds: the few polygon pairs no longer
- * hold the warp through a scalar polygon scan); otherwise every lane evaluates its own pair (a
- * batch of polygon pairs only keeps all 32 lanes busy that way). */
+ * finished by its segment's first lane; otherwise every lane evaluates its own pair. */
 __device__ __forceinline__ void collide_batch(const DevWorld& w, const StepParams& sp, int i, int state, const Head& h,
                                               bool deferred) {
     const int lane = threadIdx.x & 31;
@@ -300,19 +299,21 @@ void launch_flag_joint_contacts(const DevWorld& w, cudaStream_t s, int num_sms) 
  * (f_vn[f * 8 + k]) = (v[k], n[k]) for the rows its shape uses (a polygon's vertex count, a circle's
  * centre, an edge's four vertices), zeros past them; f_hdr[f] = (centroid, radius, meta bits). */
 __global__ void k_shape_rows(DevWorld w, int n) {
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n * kMaxPolygonVertices; t += gridDim.x * blockDim.x) {
-        const int f = t / kMaxPolygonVertices, k = t % kMaxPolygonVertices;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
         const ShapeRec& s = w.f_shape[f];
         const int type = shape_type(s);
         const int rows = type == SHAPE_POLYGON ? shape_count(s) : type == SHAPE_EDGE ? 4 : 1;
-        w.f_vn[t] = k < rows ? make_float4(s.v[k].x, s.v[k].y, s.n[k].x, s.n[k].y) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (k == 0) w.f_hdr[f] = make_float4(s.centroid.x, s.centroid.y, s.radius, __int_as_float(s.meta));
+        float4* vn = w.f_vn + (size_t)f * kMaxPolygonVertices;
+#pragma unroll
+        for (int k = 0; k < kMaxPolygonVertices; ++k)
+            vn[k] = k < rows ? make_float4(s.v[k].x, s.v[k].y, s.n[k].x, s.n[k].y) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        w.f_hdr[f] = make_float4(s.centroid.x, s.centroid.y, s.radius, __int_as_float(s.meta));
     }
 }
 
 void launch_shape_rows(const DevWorld& w, int n_fixtures, cudaStream_t s) {
     if (n_fixtures <= 0) return;
-    k_shape_rows<<<grid_for(n_fixtures * kMaxPolygonVertices, 256, w.num_sms * 8), 256, 0, s>>>(w, n_fixtures);
+    k_shape_rows<<<grid_for(n_fixtures, 256, w.num_sms * 8), 256, 0, s>>>(w, n_fixtures);
     B2G_LAUNCHED(1);
 }
 
