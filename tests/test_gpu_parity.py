@@ -334,24 +334,61 @@ def test_sleeping_pyramid_lockstep(built):
     assert recs[-1]["awake"] == 0
 
 
-def test_sleeping_pile_woken_lockstep(built):
-    """A pile of 40 boxes falls asleep, then a heavy box dropped from 145 m lands on it: the
-    sleeping pile's contacts become active as the wake spreads, in the reference's order within
-    each collide pass (its list order, here the key order on both sides)."""
+def _woken_pile():
+    """40 boxes that fall asleep in a pile, and a heavy box dropped from 145 m onto them."""
     s = scenes.pile(n_boxes=40, width=4.0, height=4.0, seed=11, spacing=0.45)
     nb = len(s["bodies"])
     drop = b2g.body_defs(1)
     drop["type"] = b2g.DYNAMIC
     drop["position"] = (0.3, 145.0)
     fx = b2g.box_fixture(nb, 0.6, 0.6, density=20.0, friction=0.6)
-    s = _sleepy(dict(s, bodies=np.concatenate([s["bodies"], drop]), fixtures=np.concatenate([s["fixtures"], fx]),
-                     n_dynamic=s["n_dynamic"] + 1))
-    recs, gpu, _ = parity.lockstep(s, 440)
+    return _sleepy(dict(s, bodies=np.concatenate([s["bodies"], drop]), fixtures=np.concatenate([s["fixtures"], fx]),
+                        n_dynamic=s["n_dynamic"] + 1))
+
+
+def test_sleeping_pile_woken_lockstep(built):
+    """A pile of 40 boxes falls asleep, then a heavy box dropped from 145 m lands on it: the
+    sleeping pile's contacts become active as the wake spreads, in the reference's order within
+    each collide pass (its list order, here the key order on both sides)."""
+    recs, gpu, _ = parity.lockstep(_woken_pile(), 440)
     for r in recs:
         _assert_step(r)
     awake = [r["awake"] for r in recs]
     assert min(awake[230:320]) <= 1      # the pile slept before the box arrived
     assert max(awake[340:]) > 30         # and woke up
+
+
+def _collide_group(group):
+    """a lockstep before_step hook that sets the GPU world's narrowphase pairs per warp batch"""
+    def hook(k, gpu, ora):
+        if k == 0:
+            gpu.set_launch_config(collide_group=group)
+    return hook
+
+
+@pytest.mark.parametrize("group", [8, 32])
+def test_segment_narrowphase_lockstep(built, group):
+    """Polygon pairs evaluated eight lanes to a pair (collide_polygons_group) in every warp batch
+    holding at most `group` of them: a settling box pile (nearly every contact a polygon pair) and a
+    dense mixed pile, bit-exact with the oracle every step."""
+    for s, steps in ((scenes.pile(n_boxes=2000, width=12.0, height=40.0, seed=3, spacing=0.6), 100),
+                     (scenes.mixed(n_circles=1500, n_polygons=1500, size=40.0, seed=13), 40)):
+        recs, gpu, _ = parity.lockstep(s, steps, before_step=_collide_group(group))
+        assert gpu.get_launch_config()["collide_group"] == group
+        for r in recs:
+            _assert_step(r)
+        assert max(r["constraints"] for r in recs) > 200
+
+
+def test_segment_narrowphase_wake_cascade_lockstep(built):
+    """The wake cascade of a sleeping world (contacts collided in rounds as a wake spreads along the
+    table) with every polygon pair evaluated eight lanes to a pair."""
+    recs, gpu, _ = parity.lockstep(_woken_pile(), 440, before_step=_collide_group(32))
+    for r in recs:
+        _assert_step(r)
+    awake = [r["awake"] for r in recs]
+    assert min(awake[230:320]) <= 1
+    assert max(awake[340:]) > 30
 
 
 def test_revolute_bridge_lockstep(built):
